@@ -1,0 +1,219 @@
+// Oracle: a CPU restatement of LehrFEM++'s assembly-and-solve path.
+//
+// TEST INFRASTRUCTURE ONLY.  This code is the checker for the GPU library in
+// lehrfempp_gb300/: only tests/, __graft_entry__.smoke() and bench.py's
+// cpu_baseline / --impl reference legs may load it.  The product never links,
+// imports or calls anything under oracle/.
+//
+// Every function restates one piece of the reference (file:line relative to
+// the LehrFEM++ source tree).  The structure follows the reference closely
+// (std::map edge numbering, per-cell provider Eval with a per-quadrature-point
+// loop, triplet push_back in cell order) because the oracle's job is to
+// reproduce the reference's numbering and arithmetic, not to be fast.
+//
+// Pinning: the oracle is checked against every golden vector the reference's
+// own tests hold for this path (tests/test_oracle_golden.py): the 10x10 and
+// 36x36 assembled matrices of lib/lf/assemble/test/assembly_tests.cc, the
+// fix-dof exact solution of lib/lf/assemble/test/coomatrix_tests.cc, the
+// reaction-diffusion bilinear-form values of
+// lib/lf/uscalfe/test/lagr_fe_tests.cc:807-883, volume row sums and quadrature
+// exactness.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <functional>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace lfo {
+
+using idx_t = int64_t;
+
+struct Error : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// ---------------------------------------------------------------- quadrature
+// lib/lf/quad/quad_rule.h:58-195: points (2 x n, column k = point k), weights.
+struct QuadRule {
+  int degree = 0;
+  std::vector<double> x, y, w;
+  int n() const { return static_cast<int>(w.size()); }
+};
+// lib/lf/quad/gauss_quadrature.cc:16-69 (points on [0,1], weights sum to 1).
+void GaussLegendre(int n, std::vector<double>& pts, std::vector<double>& wts);
+// lib/lf/quad/make_quad_rule.cc:21-157 for kTria (hard-coded tables deg<=8)
+// and kQuad (tensor Gauss-Legendre, n = deg/2+1).
+QuadRule MakeQuadRule(bool is_quad, int degree);
+
+// ------------------------------------------------------ reference elements
+// Lagrangian reference shape functions of lib/lf/uscalfe/lagr_fe.h:57-1484.
+// phi[i], dphi[i][0..1] at one reference point.
+int NumShapeFunctions(bool is_quad, int degree);
+void EvalShape(bool is_quad, int degree, double xh, double yh, double* phi,
+               double (*dphi)[2]);
+// Evaluation nodes (x,y per local shape function) used by NodalProjection.
+void EvaluationNodes(bool is_quad, int degree, std::vector<double>& xy);
+
+// ---------------------------------------------------------------- geometry
+// lib/lf/geometry/tria_o1.cc:50-74 and quad_o1.cc:67-156.
+struct CellGeom {
+  bool is_quad;
+  double v[4][2];
+  // JacobianInverseGramian (= (J^T)^{-1} for 2D), |det J| and Global().
+  void JinvT(double xh, double yh, double out[2][2]) const;
+  double IntegrationElement(double xh, double yh) const;
+  void Global(double xh, double yh, double out[2]) const;
+};
+// tria_o1.cc:10-48 / quad_o1.cc:12-58 (tol 1e-8); returns false if degenerate.
+bool NonDegenerate(const CellGeom& g, double tol = 1.0e-8);
+
+// -------------------------------------------------------------------- mesh
+// The numbering of lib/lf/mesh/hybrid2d/mesh.cc:178-810.
+struct Mesh {
+  idx_t num_nodes = 0;
+  std::vector<double> xy;                       // 2 per node
+  idx_t num_cells = 0;
+  std::vector<std::array<idx_t, 4>> cell_nodes;  // -1 padded (tria)
+  idx_t num_edges = 0;
+  std::vector<std::array<idx_t, 2>> edge_nodes;  // by global edge index
+  std::vector<std::array<idx_t, 4>> cell_edges;  // global edge indices
+  std::vector<std::array<int8_t, 4>> cell_ori;   // +1 / -1
+  std::vector<int32_t> edge_num_cells;           // CountNumSuperEntities
+  bool IsQuad(idx_t c) const { return cell_nodes[c][3] >= 0; }
+  int NumVerts(idx_t c) const { return IsQuad(c) ? 4 : 3; }
+  CellGeom Geom(idx_t c) const;
+};
+// hybrid2d::Mesh ctor: preset edges keep their registration index, edges
+// created by cells are numbered afterwards in std::map (min,max) order; an
+// edge's direction is that of its first creator.
+Mesh BuildMesh(idx_t num_nodes, const double* xy, idx_t num_cells,
+               const int64_t* cell_nodes /*4 per cell, -1 pad*/,
+               idx_t num_preset, const int64_t* preset_edges /*2 per edge*/);
+
+// Structured builders: lib/lf/mesh/utils/tp_triag_mesh_builder.cc:18-178 and
+// tp_quad_mesh_builder.cc:18-94.  Return the factory input arrays.
+struct FactoryInput {
+  std::vector<double> xy;
+  std::vector<int64_t> cells;   // 4 per cell
+  std::vector<int64_t> edges;   // 2 per preset edge
+};
+FactoryInput TPTriagInput(idx_t nx, idx_t ny, double x0, double y0, double x1,
+                          double y1);
+FactoryInput TPQuadInput(idx_t nx, idx_t ny, double x0, double y0, double x1,
+                         double y1);
+// lib/lf/mesh/test_utils/test_meshes.cc:14 selector 0 (scale 1).
+FactoryInput TestMesh0Input(double scale = 1.0);
+
+// lib/lf/mesh/utils/special_entity_sets.cc:64-90 (all codims).
+void FlagEntitiesOnBoundary(const Mesh& m, std::vector<uint8_t>& node_flags,
+                            std::vector<uint8_t>& edge_flags);
+
+// ------------------------------------------------------------- dof handler
+// lib/lf/assemble/dofhandler.cc:86-338 (UniformFEDofHandler).
+struct DofHandler {
+  const Mesh* mesh = nullptr;
+  int np = 0, ns = 0, nt = 0, nq = 0;  // interior dofs per point/seg/tria/quad
+  int n_node = 0, n_edge = 0, n_tria = 0, n_quad = 0, n_cell = 0;
+  idx_t num_dofs = 0;
+  std::vector<idx_t> node_dofs, edge_dofs, cell_dofs;
+  std::vector<std::pair<int, idx_t>> dof_entity;  // (codim, entity index)
+  int NumLocalDofs(idx_t c) const { return mesh->IsQuad(c) ? n_quad : n_tria; }
+  const idx_t* GlobalDofIndices(idx_t c) const { return &cell_dofs[c * n_cell]; }
+};
+DofHandler MakeDofHandler(const Mesh& m, int np, int ns, int nt, int nq,
+                          bool check_edge_orientation = true);
+// uniform_scalar_fe_space.h:241-342 for FeSpaceLagrangeO{1,2,3}.
+DofHandler MakeLagrangeDofHandler(const Mesh& m, int degree);
+
+// ---------------------------------------------------------- mesh functions
+// A scalar MeshFunction (mesh_function_traits.h:149-155) evaluated on a cell
+// at reference points.  Kinds: constant (mesh_function_constant.h:25-45),
+// per-cell array, O1 nodal interpolant (fe/mesh_function_fe.h:44-115),
+// analytic x->f(x) (mesh_function_global.h:54-94).
+struct MeshFunction {
+  enum Kind { kZero = 0, kConstant = 1, kPerCell = 2, kNodalO1 = 3, kAnalytic = 4 };
+  int kind = kZero;
+  double value = 0.0;
+  std::vector<double> data;
+  std::function<double(double, double)> fn;
+  // Optional 2x2 tensor-valued coefficient (only used by the reference's
+  // tensor-coefficient test): returns row-major a00,a01,a10,a11.
+  std::function<void(double, double, double*)> tensor_fn;
+  bool IsTensor() const { return static_cast<bool>(tensor_fn); }
+  void Eval(const Mesh& m, idx_t cell, const QuadRule& qr,
+            std::vector<double>& out) const;
+  void EvalTensor(const Mesh& m, idx_t cell, const QuadRule& qr,
+                  std::vector<std::array<double, 4>>& out) const;
+};
+
+// Built-in analytic families (shared meaning with the library's lfg_coeff).
+std::function<double(double, double)> AnalyticFunction(int func_id,
+                                                       const double* p);
+
+// ---------------------------------------------------------------- assembly
+struct Triplet {
+  int32_t row, col;
+  double value;
+};
+// lib/lf/assemble/coomatrix.h:51-225.
+struct COOMatrix {
+  idx_t rows = 0, cols = 0;
+  std::vector<Triplet> triplets;
+  void AddToEntry(idx_t i, idx_t j, double v) {
+    triplets.push_back({static_cast<int32_t>(i), static_cast<int32_t>(j), v});
+  }
+};
+
+// ReactionDiffusionElementMatrixProvider (uscalfe/loc_comp_ellbvp.h:85-339).
+struct RDProvider {
+  const Mesh* mesh;
+  int degree;
+  MeshFunction alpha, gamma;
+  QuadRule qr_tria, qr_quad;
+  bool have_tria = false, have_quad = false;
+  // per-rule precomputed shape function tables (precomputed_scalar_...h:72-78)
+  std::vector<double> phi_t, dphi_t, phi_q, dphi_q;
+  void Init();
+  void Eval(idx_t cell, std::vector<double>& mat /* n*n row major */) const;
+};
+// ScalarLoadElementVectorProvider (loc_comp_ellbvp.h:562-746).
+struct LoadProvider {
+  const Mesh* mesh;
+  int degree;
+  MeshFunction f;
+  QuadRule qr_tria, qr_quad;
+  std::vector<double> phi_t, phi_q;
+  void Init();
+  void Eval(idx_t cell, std::vector<double>& vec) const;
+};
+
+// AssembleMatrixLocally / AssembleVectorLocally (assemble/assembler.h:114-365).
+void AssembleMatrixLocally(const DofHandler& dh,
+                           const std::function<void(idx_t, std::vector<double>&)>& eval,
+                           COOMatrix& A);
+void AssembleVectorLocally(const DofHandler& dh,
+                           const std::function<void(idx_t, std::vector<double>&)>& eval,
+                           std::vector<double>& b);
+
+// FixFlaggedSolutionComponents (assemble/fix_dof.h:86-138).
+void FixFlaggedSolutionComponents(const uint8_t* flags, const double* values,
+                                  COOMatrix& A, std::vector<double>& b);
+// FixFlaggedSolutionCompAlt (fix_dof.h:183-219).
+void FixFlaggedSolutionCompAlt(const uint8_t* flags, const double* values,
+                               COOMatrix& A, std::vector<double>& b);
+
+// COOMatrix::makeSparse (coomatrix.h:172-180) = Eigen setFromTriplets: per
+// (row,col) the duplicates are summed in triplet order.  Output is CSR.
+void MakeSparseCSR(const COOMatrix& A, std::vector<int64_t>& rowptr,
+                   std::vector<int32_t>& colind, std::vector<double>& val);
+
+// fe/fe_tools.h:198-259 NodalProjection for Lagrangian spaces.
+void NodalProjection(const DofHandler& dh, int degree,
+                     const std::function<double(double, double)>& u,
+                     std::vector<double>& out);
+
+}  // namespace lfo

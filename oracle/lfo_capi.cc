@@ -1,0 +1,352 @@
+// Oracle (test infrastructure only): flat C entry points so that the Python
+// test-suite can drive the restatement through ctypes.  Every call returns 0
+// on success; on failure it returns -1 and copies the message into err.
+#include <cstring>
+#include <memory>
+
+#include "lfo.h"
+
+using namespace lfo;
+
+namespace {
+struct Space {
+  const Mesh* mesh;
+  int degree;  // 0 for a generic layout
+  DofHandler dh;
+};
+struct Input {
+  FactoryInput in;
+};
+struct CSR {
+  std::vector<int64_t> rowptr;
+  std::vector<int32_t> col;
+  std::vector<double> val;
+};
+
+void SetErr(char* err, int n, const char* msg) {
+  if (err && n > 0) {
+    std::strncpy(err, msg, n - 1);
+    err[n - 1] = 0;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+typedef struct {
+  int32_t kind;
+  int32_t func;
+  double value;
+  const double* data;
+  double p[16];
+} lfo_coeff;
+
+static MeshFunction ToMF(const lfo_coeff* c, size_t n_data) {
+  MeshFunction mf;
+  if (!c) return mf;
+  mf.kind = c->kind;
+  mf.value = c->value;
+  if (c->kind == MeshFunction::kPerCell || c->kind == MeshFunction::kNodalO1)
+    mf.data.assign(c->data, c->data + n_data);
+  if (c->kind == MeshFunction::kAnalytic) mf.fn = AnalyticFunction(c->func, c->p);
+  return mf;
+}
+
+#define LFO_TRY try {
+#define LFO_CATCH                      \
+  }                                    \
+  catch (const std::exception& e) {    \
+    SetErr(err, errlen, e.what());     \
+    return -1;                         \
+  }                                    \
+  return 0;
+
+int lfo_input_create(int kind, int64_t nx, int64_t ny, double x0, double y0, double x1,
+                     double y1, void** out, int64_t* sizes, char* err, int errlen) {
+  LFO_TRY
+  auto* h = new Input;
+  if (kind == 0) h->in = TPTriagInput(nx, ny, x0, y0, x1, y1);
+  else if (kind == 1) h->in = TPQuadInput(nx, ny, x0, y0, x1, y1);
+  else h->in = TestMesh0Input(x0 == 0.0 ? 1.0 : x0);
+  sizes[0] = static_cast<int64_t>(h->in.xy.size() / 2);
+  sizes[1] = static_cast<int64_t>(h->in.cells.size() / 4);
+  sizes[2] = static_cast<int64_t>(h->in.edges.size() / 2);
+  *out = h;
+  LFO_CATCH
+}
+
+void lfo_input_copy(void* h, double* xy, int64_t* cells, int64_t* edges) {
+  auto* in = static_cast<Input*>(h);
+  std::memcpy(xy, in->in.xy.data(), in->in.xy.size() * sizeof(double));
+  std::memcpy(cells, in->in.cells.data(), in->in.cells.size() * sizeof(int64_t));
+  if (!in->in.edges.empty())
+    std::memcpy(edges, in->in.edges.data(), in->in.edges.size() * sizeof(int64_t));
+}
+void lfo_input_destroy(void* h) { delete static_cast<Input*>(h); }
+
+int lfo_mesh_create(int64_t nv, const double* xy, int64_t nc, const int64_t* cells,
+                    int64_t npre, const int64_t* pre, void** out, char* err, int errlen) {
+  LFO_TRY
+  auto m = std::make_unique<Mesh>(BuildMesh(nv, xy, nc, cells, npre, pre));
+  // MeshFactory(check_completeness = true): every node on an edge, every edge
+  // on a cell (hybrid2d/mesh.cc:566-600)
+  std::vector<uint8_t> used(m->num_nodes, 0);
+  for (idx_t e = 0; e < m->num_edges; ++e) {
+    if (m->edge_num_cells[e] == 0)
+      throw Error("Mesh is incomplete: Edge with global index " + std::to_string(e) +
+                  " does not belong to a cell.");
+    used[m->edge_nodes[e][0]] = used[m->edge_nodes[e][1]] = 1;
+  }
+  for (idx_t v = 0; v < m->num_nodes; ++v)
+    if (!used[v])
+      throw Error("Mesh is incomplete: Node with global index " + std::to_string(v) +
+                  " is not part of any edge.");
+  *out = m.release();
+  LFO_CATCH
+}
+void lfo_mesh_destroy(void* m) { delete static_cast<Mesh*>(m); }
+void lfo_mesh_sizes(void* mp, int64_t* s) {
+  auto* m = static_cast<Mesh*>(mp);
+  s[0] = m->num_nodes;
+  s[1] = m->num_edges;
+  s[2] = m->num_cells;
+}
+void lfo_mesh_topology(void* mp, int64_t* edge_nodes, int64_t* cell_edges, int8_t* cell_ori,
+                       int32_t* edge_ncells) {
+  auto* m = static_cast<Mesh*>(mp);
+  for (idx_t e = 0; e < m->num_edges; ++e) {
+    edge_nodes[2 * e] = m->edge_nodes[e][0];
+    edge_nodes[2 * e + 1] = m->edge_nodes[e][1];
+    edge_ncells[e] = m->edge_num_cells[e];
+  }
+  for (idx_t c = 0; c < m->num_cells; ++c)
+    for (int k = 0; k < 4; ++k) {
+      cell_edges[4 * c + k] = m->cell_edges[c][k];
+      cell_ori[4 * c + k] = m->cell_ori[c][k];
+    }
+}
+void lfo_boundary_flags(void* mp, uint8_t* nf, uint8_t* ef) {
+  std::vector<uint8_t> a, b;
+  FlagEntitiesOnBoundary(*static_cast<Mesh*>(mp), a, b);
+  std::memcpy(nf, a.data(), a.size());
+  std::memcpy(ef, b.data(), b.size());
+}
+int lfo_mesh_degenerate_cells(void* mp, int64_t* count) {
+  auto* m = static_cast<Mesh*>(mp);
+  int64_t n = 0;
+  for (idx_t c = 0; c < m->num_cells; ++c)
+    if (!NonDegenerate(m->Geom(c))) ++n;
+  *count = n;
+  return 0;
+}
+
+int lfo_space_create(void* mp, int degree, int np, int ns, int nt, int nq, void** out,
+                     char* err, int errlen) {
+  LFO_TRY
+  auto* m = static_cast<Mesh*>(mp);
+  auto s = std::make_unique<Space>();
+  s->mesh = m;
+  s->degree = degree;
+  s->dh = degree > 0 ? MakeLagrangeDofHandler(*m, degree) : MakeDofHandler(*m, np, ns, nt, nq);
+  *out = s.release();
+  LFO_CATCH
+}
+void lfo_space_destroy(void* s) { delete static_cast<Space*>(s); }
+void lfo_space_info(void* sp, int64_t* info) {
+  auto* s = static_cast<Space*>(sp);
+  info[0] = s->dh.num_dofs;
+  info[1] = s->dh.n_cell;
+  info[2] = s->dh.n_tria;
+  info[3] = s->dh.n_quad;
+}
+void lfo_space_cell_dofs(void* sp, int64_t* out) {
+  auto* s = static_cast<Space*>(sp);
+  std::memcpy(out, s->dh.cell_dofs.data(), s->dh.cell_dofs.size() * sizeof(int64_t));
+}
+void lfo_space_dof_entity(void* sp, int32_t* codim, int64_t* idx) {
+  auto* s = static_cast<Space*>(sp);
+  for (size_t k = 0; k < s->dh.dof_entity.size(); ++k) {
+    codim[k] = s->dh.dof_entity[k].first;
+    idx[k] = s->dh.dof_entity[k].second;
+  }
+}
+
+int lfo_quad_rule(int is_quad, int degree, double* x, double* y, double* w, int* n,
+                  char* err, int errlen) {
+  LFO_TRY
+  QuadRule qr = MakeQuadRule(is_quad != 0, degree);
+  *n = qr.n();
+  if (x) {
+    std::memcpy(x, qr.x.data(), qr.n() * sizeof(double));
+    std::memcpy(y, qr.y.data(), qr.n() * sizeof(double));
+    std::memcpy(w, qr.w.data(), qr.n() * sizeof(double));
+  }
+  LFO_CATCH
+}
+
+int lfo_assemble_rd(void* sp, const lfo_coeff* alpha, const lfo_coeff* gamma, int qdeg_tria,
+                    int qdeg_quad, int64_t first_cell, int64_t last_cell, void** out, char* err,
+                    int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  RDProvider p;
+  p.mesh = &m;
+  p.degree = s->degree;
+  const size_t nd = alpha && alpha->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells;
+  const size_t nd2 = gamma && gamma->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells;
+  p.alpha = ToMF(alpha, nd);
+  p.gamma = ToMF(gamma, nd2);
+  const int dt = qdeg_tria > 0 ? qdeg_tria : 2 * s->degree;
+  const int dq = qdeg_quad > 0 ? qdeg_quad : 2 * s->degree;
+  if (qdeg_tria >= 0) { p.qr_tria = MakeQuadRule(false, dt); p.have_tria = true; }
+  if (qdeg_quad >= 0) { p.qr_quad = MakeQuadRule(true, dq); p.have_quad = true; }
+  p.Init();
+  auto A = std::make_unique<COOMatrix>();
+  A->rows = A->cols = s->dh.num_dofs;
+  if (last_cell < 0) last_cell = m.num_cells;
+  std::vector<double> em;
+  for (idx_t c = first_cell; c < last_cell; ++c) {
+    const int n = s->dh.NumLocalDofs(c);
+    const idx_t* dofs = s->dh.GlobalDofIndices(c);
+    p.Eval(c, em);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) A->AddToEntry(dofs[i], dofs[j], em[i * n + j]);
+  }
+  *out = A.release();
+  LFO_CATCH
+}
+
+int lfo_assemble_load(void* sp, const lfo_coeff* f, int qdeg_tria, int qdeg_quad, double* b,
+                      char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  LoadProvider p;
+  p.mesh = &m;
+  p.degree = s->degree;
+  p.f = ToMF(f, f && f->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  p.qr_tria = MakeQuadRule(false, qdeg_tria > 0 ? qdeg_tria : 2 * s->degree);
+  p.qr_quad = MakeQuadRule(true, qdeg_quad > 0 ? qdeg_quad : 2 * s->degree);
+  p.Init();
+  std::vector<double> bv(b, b + s->dh.num_dofs);
+  AssembleVectorLocally(s->dh, [&](idx_t c, std::vector<double>& v) { p.Eval(c, v); }, bv);
+  std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
+int lfo_assemble_tabulated(void* sp, const double* elem, int ld, double* vec_elem, double* b,
+                           void** out, char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  auto A = std::make_unique<COOMatrix>();
+  A->rows = A->cols = s->dh.num_dofs;
+  AssembleMatrixLocally(
+      s->dh,
+      [&](idx_t c, std::vector<double>& em) {
+        em.assign(elem + c * ld * ld, elem + (c + 1) * ld * ld);
+      },
+      *A);
+  if (vec_elem && b) {
+    std::vector<double> bv(b, b + s->dh.num_dofs);
+    AssembleVectorLocally(
+        s->dh,
+        [&](idx_t c, std::vector<double>& ev) { ev.assign(vec_elem + c * ld, vec_elem + (c + 1) * ld); },
+        bv);
+    std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  }
+  *out = A.release();
+  LFO_CATCH
+}
+
+void* lfo_coo_create(int64_t rows, int64_t cols, int64_t n, const int32_t* r, const int32_t* c,
+                     const double* v) {
+  auto* A = new COOMatrix;
+  A->rows = rows;
+  A->cols = cols;
+  for (int64_t k = 0; k < n; ++k) A->AddToEntry(r[k], c[k], v[k]);
+  return A;
+}
+void lfo_coo_destroy(void* a) { delete static_cast<COOMatrix*>(a); }
+int64_t lfo_coo_size(void* a) { return static_cast<int64_t>(static_cast<COOMatrix*>(a)->triplets.size()); }
+void lfo_coo_copy(void* a, int32_t* r, int32_t* c, double* v) {
+  auto* A = static_cast<COOMatrix*>(a);
+  for (size_t k = 0; k < A->triplets.size(); ++k) {
+    r[k] = A->triplets[k].row;
+    c[k] = A->triplets[k].col;
+    v[k] = A->triplets[k].value;
+  }
+}
+
+int lfo_fix_flagged(void* a, const uint8_t* flags, const double* vals, double* b, int alt,
+                    char* err, int errlen) {
+  LFO_TRY
+  auto* A = static_cast<COOMatrix*>(a);
+  std::vector<double> bv(b, b + A->rows);
+  if (alt) FixFlaggedSolutionCompAlt(flags, vals, *A, bv);
+  else FixFlaggedSolutionComponents(flags, vals, *A, bv);
+  std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
+void* lfo_csr_create(void* a, int64_t* sizes) {
+  auto* A = static_cast<COOMatrix*>(a);
+  auto* C = new CSR;
+  MakeSparseCSR(*A, C->rowptr, C->col, C->val);
+  sizes[0] = A->rows;
+  sizes[1] = static_cast<int64_t>(C->col.size());
+  return C;
+}
+void lfo_csr_copy(void* h, int64_t* rowptr, int32_t* col, double* val) {
+  auto* C = static_cast<CSR*>(h);
+  std::memcpy(rowptr, C->rowptr.data(), C->rowptr.size() * sizeof(int64_t));
+  std::memcpy(col, C->col.data(), C->col.size() * sizeof(int32_t));
+  std::memcpy(val, C->val.data(), C->val.size() * sizeof(double));
+}
+void lfo_csr_destroy(void* h) { delete static_cast<CSR*>(h); }
+
+int lfo_nodal_projection(void* sp, int func, const double* p, double* out, char* err,
+                         int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  std::vector<double> v;
+  NodalProjection(s->dh, s->degree, AnalyticFunction(func, p), v);
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
+  LFO_CATCH
+}
+
+// Restatement of lf_fe_linear.ReactionDiffusion (uscalfe/test/lagr_fe_tests.cc:
+// 807-832): O1 on test mesh 0 with the tensor coefficient [[1, x], [y, xy]],
+// gamma = xy, a = 1+x+2y, b = 3x, degree-4 rules; returns a^T A b.
+int lfo_kat_tensor_rd(double* value, char* err, int errlen) {
+  LFO_TRY
+  FactoryInput in = TestMesh0Input(1.0);
+  Mesh m = BuildMesh(10, in.xy.data(), 9, in.cells.data(), 0, nullptr);
+  DofHandler dh = MakeLagrangeDofHandler(m, 1);
+  RDProvider p;
+  p.mesh = &m;
+  p.degree = 1;
+  p.alpha.kind = MeshFunction::kAnalytic;
+  p.alpha.tensor_fn = [](double x, double y, double* a) {
+    a[0] = 1; a[1] = x; a[2] = y; a[3] = x * y;
+  };
+  p.gamma.kind = MeshFunction::kAnalytic;
+  p.gamma.fn = [](double x, double y) { return x * y; };
+  p.qr_tria = MakeQuadRule(false, 4);
+  p.qr_quad = MakeQuadRule(true, 4);
+  p.have_tria = p.have_quad = true;
+  p.Init();
+  COOMatrix A;
+  A.rows = A.cols = dh.num_dofs;
+  AssembleMatrixLocally(dh, [&](idx_t c, std::vector<double>& em) { p.Eval(c, em); }, A);
+  std::vector<double> a, b;
+  NodalProjection(dh, 1, [](double x, double y) { return 1 + x + 2 * y; }, a);
+  NodalProjection(dh, 1, [](double x, double) { return 3 * x; }, b);
+  double s = 0;
+  for (const Triplet& t : A.triplets) s += a[t.row] * t.value * b[t.col];
+  *value = s;
+  LFO_CATCH
+}
+
+}  // extern "C"

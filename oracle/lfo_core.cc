@@ -1,0 +1,803 @@
+// Oracle (test infrastructure only): CPU restatement of the LehrFEM++ path.
+// See lfo.h for scope and the rule that only tests / smoke / bench baselines
+// may use it.  File:line citations are relative to the LehrFEM++ source tree.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "lfo.h"
+
+namespace lfo {
+
+#include "tria_rules.inc"
+
+// =========================================================== quadrature ====
+
+// lib/lf/quad/gauss_quadrature.cc:16-69.  The reference runs Newton's method in
+// a 57-bit binary float; long double (64-bit mantissa on x86-64, 113-bit on
+// aarch64) gives the same roots after rounding to double up to 1 ulp.
+void GaussLegendre(int n, std::vector<double>& pts, std::vector<double>& wts) {
+  if (n <= 0) throw Error("GaussLegendre: num_points must be positive");
+  pts.assign(n, 0.0);
+  wts.assign(n, 0.0);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  const int m = (n + 1) / 2;
+  for (int i = 0; i < m; ++i) {
+    long double z = std::cos(pi * (i + 0.75L) / (n + 0.5L));
+    long double z1, pp;
+    int guard = 0;
+    do {
+      long double p1 = 1.0L, p2 = 0.0L, p3;
+      for (int j = 0; j < n; ++j) {
+        p3 = p2;
+        p2 = p1;
+        p1 = ((2.0L * j + 1.0L) * z * p2 - j * p3) / (j + 1.0L);
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0L);
+      z1 = z;
+      z = z1 - p1 / pp;
+    } while (std::fabs(z - z1) > 1e-17L && ++guard < 100);
+    pts[i] = static_cast<double>(0.5L * (1.0L - z));
+    pts[n - 1 - i] = static_cast<double>(0.5L * (1.0L + z));
+    wts[i] = static_cast<double>(1.0L / ((1.0L - z * z) * pp * pp));
+    wts[n - 1 - i] = wts[i];
+  }
+}
+
+// lib/lf/quad/make_quad_rule.cc:21-157.
+QuadRule MakeQuadRule(bool is_quad, int degree) {
+  QuadRule qr;
+  if (is_quad) {
+    const int n = degree / 2 + 1;
+    std::vector<double> p, w;
+    GaussLegendre(n, p, w);
+    // points row0 = kron(x, ones(n)) (x slow), row1 = repeat(x) (y fast);
+    // weights = kron(w, w)  (make_quad_rule.cc:28-37)
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        qr.x.push_back(p[a]);
+        qr.y.push_back(p[b]);
+        qr.w.push_back(w[a] * w[b]);
+      }
+    qr.degree = 2 * n - 1;
+    return qr;
+  }
+  int d = degree;
+  if (d == 3) d = 4;  // make_quad_rule.cc:44-46
+  if (d < 1 || d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0)
+    throw Error("MakeQuadRule: triangle rule of degree " + std::to_string(degree) +
+                " is not tabulated in the oracle");
+  const int np = kTriaRuleIndex[d][0], off = kTriaRuleIndex[d][1];
+  for (int k = 0; k < np; ++k) {
+    qr.x.push_back(kTriaRuleRows[off + k][0]);
+    qr.y.push_back(kTriaRuleRows[off + k][1]);
+    qr.w.push_back(kTriaRuleRows[off + k][2]);
+  }
+  qr.degree = d;
+  return qr;
+}
+
+// ================================================== reference elements ====
+namespace {
+// FeLagrangeO2Segment (lagr_fe.h:563-700)
+inline void SegO2(double x, double b[3], double db[3]) {
+  b[0] = 2.0 * (1.0 - x) * (0.5 - x);
+  b[1] = 2.0 * x * (x - 0.5);
+  b[2] = 4.0 * (1.0 - x) * x;
+  db[0] = 4.0 * x - 3.0;
+  db[1] = 4.0 * x - 1.0;
+  db[2] = 4.0 - 8.0 * x;
+}
+// FeLagrangeO3Segment (lagr_fe.h:1155-1277)
+inline void SegO3(double x, double b[4], double db[4]) {
+  b[0] = 4.5 * (1.0 - x) * (1.0 / 3.0 - x) * (2.0 / 3.0 - x);
+  b[1] = 4.5 * x * (x - 1.0 / 3.0) * (x - 2.0 / 3.0);
+  b[2] = 13.5 * x * (1 - x) * (2.0 / 3.0 - x);
+  b[3] = 13.5 * x * (1 - x) * (x - 1.0 / 3.0);
+  db[0] = -13.5 * x * x + 18.0 * x - 5.5;
+  db[1] = 13.5 * x * x - 9.0 * x + 1.0;
+  db[2] = 40.5 * x * x - 45 * x + 9;
+  db[3] = -40.5 * x * x + 36 * x - 4.5;
+}
+// ksegment_to_quad_mapping_ of FeLagrangeO2Quad (lagr_fe.h:914-925) and
+// FeLagrangeO3Quad (lagr_fe.h:1462-1480).
+const int kO2QuadMap[9][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0},
+                              {1, 2}, {2, 1}, {0, 2}, {2, 2}};
+const int kO3QuadMap[16][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0}, {3, 0},
+                               {1, 2}, {1, 3}, {3, 1}, {2, 1}, {0, 3}, {0, 2},
+                               {2, 2}, {3, 2}, {3, 3}, {2, 3}};
+}  // namespace
+
+int NumShapeFunctions(bool is_quad, int degree) {
+  static const int t[4] = {0, 3, 6, 10}, q[4] = {0, 4, 9, 16};
+  if (degree < 1 || degree > 3) throw Error("degree must be 1..3");
+  return is_quad ? q[degree] : t[degree];
+}
+
+void EvalShape(bool is_quad, int degree, double x0, double x1, double* phi,
+               double (*dphi)[2]) {
+  if (!is_quad && degree == 1) {  // FeLagrangeO1Tria lagr_fe.h:57-160
+    phi[0] = 1.0 - x0 - x1;
+    phi[1] = x0;
+    phi[2] = x1;
+    dphi[0][0] = -1; dphi[0][1] = -1;
+    dphi[1][0] = 1;  dphi[1][1] = 0;
+    dphi[2][0] = 0;  dphi[2][1] = 1;
+  } else if (is_quad && degree == 1) {  // FeLagrangeO1Quad lagr_fe.h:165-280
+    phi[0] = (1 - x0) * (1 - x1);
+    phi[1] = x0 * (1 - x1);
+    phi[2] = x0 * x1;
+    phi[3] = (1 - x0) * x1;
+    dphi[0][0] = x1 - 1.0;  dphi[0][1] = x0 - 1.0;
+    dphi[1][0] = 1.0 - x1;  dphi[1][1] = -x0;
+    dphi[2][0] = x1;        dphi[2][1] = x0;
+    dphi[3][0] = -x1;       dphi[3][1] = 1.0 - x0;
+  } else if (!is_quad && degree == 2) {  // FeLagrangeO2Tria lagr_fe.h:400-560
+    phi[0] = 2.0 * (1 - x0 - x1) * (0.5 - x0 - x1);
+    phi[1] = 2.0 * x0 * (x0 - 0.5);
+    phi[2] = 2.0 * x1 * (x1 - 0.5);
+    phi[3] = 4.0 * (1 - x0 - x1) * x0;
+    phi[4] = 4.0 * x0 * x1;
+    phi[5] = 4.0 * (1 - x0 - x1) * x1;
+    dphi[0][0] = -3.0 + 4.0 * x0 + 4.0 * x1;  dphi[0][1] = -3.0 + 4.0 * x0 + 4.0 * x1;
+    dphi[1][0] = 4.0 * x0 - 1.0;              dphi[1][1] = 0.0;
+    dphi[2][0] = 0.0;                         dphi[2][1] = 4.0 * x1 - 1.0;
+    dphi[3][0] = 4 - 0 - 8.0 * x0 - 4.0 * x1; dphi[3][1] = -4 * x0;
+    dphi[4][0] = 4.0 * x1;                    dphi[4][1] = 4.0 * x0;
+    dphi[5][0] = -4.0 * x1;                   dphi[5][1] = 4.0 - 8.0 * x1 - 4.0 * x0;
+  } else if (is_quad && degree == 2) {  // FeLagrangeO2Quad lagr_fe.h:713-925
+    double bx[3], dbx[3], by[3], dby[3];
+    SegO2(x0, bx, dbx);
+    SegO2(x1, by, dby);
+    for (int i = 0; i < 9; ++i) {
+      const int a = kO2QuadMap[i][0], b = kO2QuadMap[i][1];
+      phi[i] = bx[a] * by[b];
+      dphi[i][0] = dbx[a] * by[b];
+      dphi[i][1] = dby[b] * bx[a];
+    }
+  } else if (!is_quad && degree == 3) {  // FeLagrangeO3Tria lagr_fe.h:945-1150
+    const double l0 = 1 - x0 - x1, l1 = x0, l2 = x1;
+    const double t = 1 / 3.0, tt = 2 / 3.0;
+    phi[0] = 4.5 * l0 * (l0 - t) * (l0 - tt);
+    phi[1] = 4.5 * l1 * (l1 - t) * (l1 - tt);
+    phi[2] = 4.5 * l2 * (l2 - t) * (l2 - tt);
+    phi[3] = 13.5 * l0 * l1 * (l0 - t);
+    phi[4] = 13.5 * l0 * l1 * (l1 - t);
+    phi[5] = 13.5 * l1 * l2 * (l1 - t);
+    phi[6] = 13.5 * l1 * l2 * (l2 - t);
+    phi[7] = 13.5 * l2 * l0 * (l2 - t);
+    phi[8] = 13.5 * l2 * l0 * (l0 - t);
+    phi[9] = 27.0 * l0 * l1 * l2;
+    const double g0 = -4.5 * ((l0 - t) * (l0 - tt) + l0 * (l0 - tt) + l0 * (l0 - t));
+    dphi[0][0] = g0;
+    dphi[0][1] = g0;
+    dphi[1][0] = 4.5 * ((l1 - t) * (l1 - tt) + l1 * (l1 - tt) + l1 * (l1 - t));
+    dphi[1][1] = 0.0;
+    dphi[2][0] = 0.0;
+    dphi[2][1] = 4.5 * ((l2 - t) * (l2 - tt) + l2 * (l2 - tt) + l2 * (l2 - t));
+    dphi[3][0] = 13.5 * (-l1 * (l0 - t) + l0 * (l0 - t) - l0 * l1);
+    dphi[3][1] = -13.5 * (l1 * (l0 - t) + l0 * l1);
+    dphi[4][0] = 13.5 * (-l1 * (l1 - t) + l0 * (l1 - t) + l0 * l1);
+    dphi[4][1] = -13.5 * l1 * (l1 - t);
+    dphi[5][0] = 13.5 * (l2 * (l1 - t) + l1 * l2);
+    dphi[5][1] = 13.5 * (l1 * (l1 - t));
+    dphi[6][0] = 13.5 * (l2 * (l2 - t));
+    dphi[6][1] = 13.5 * (l1 * (l2 - t) + l1 * l2);
+    dphi[7][0] = -13.5 * l2 * (l2 - t);
+    dphi[7][1] = 13.5 * (l0 * (l2 - t) - l2 * (l2 - t) + l0 * l2);
+    dphi[8][0] = -13.5 * (l2 * (l0 - t) + l2 * l0);
+    dphi[8][1] = 13.5 * (l0 * (l0 - t) - l2 * (l0 - t) - l2 * l0);
+    dphi[9][0] = 27.0 * (-l1 * l2 + l0 * l2);
+    dphi[9][1] = 27.0 * (-l1 * l2 + l0 * l1);
+  } else if (is_quad && degree == 3) {  // FeLagrangeO3Quad lagr_fe.h:1279-1480
+    double bx[4], dbx[4], by[4], dby[4];
+    SegO3(x0, bx, dbx);
+    SegO3(x1, by, dby);
+    for (int i = 0; i < 16; ++i) {
+      const int a = kO3QuadMap[i][0], b = kO3QuadMap[i][1];
+      phi[i] = bx[a] * by[b];
+      dphi[i][0] = dbx[a] * by[b];
+      dphi[i][1] = dby[b] * bx[a];
+    }
+  } else {
+    throw Error("EvalShape: unsupported degree");
+  }
+}
+
+void EvaluationNodes(bool is_quad, int degree, std::vector<double>& xy) {
+  const double t = 1.0 / 3.0;
+  xy.clear();
+  auto add = [&](double a, double b) { xy.push_back(a); xy.push_back(b); };
+  if (!is_quad) {
+    add(0, 0); add(1, 0); add(0, 1);
+    if (degree == 2) { add(0.5, 0); add(0.5, 0.5); add(0, 0.5); }
+    if (degree == 3) {
+      // edges << 1,2,2,1,0,0 / 0,0,1,2,2,1 scaled by 1/3 (lagr_fe.h:1124-1136)
+      const double ex[6] = {1, 2, 2, 1, 0, 0}, ey[6] = {0, 0, 1, 2, 2, 1};
+      for (int k = 0; k < 6; ++k) add(ex[k] * t, ey[k] * t);
+      add(1.0 / 3.0, 1.0 / 3.0);
+    }
+  } else {
+    add(0, 0); add(1, 0); add(1, 1); add(0, 1);
+    if (degree == 2) {
+      add(0.5, 0); add(1, 0.5); add(0.5, 1); add(0, 0.5); add(0.5, 0.5);
+    }
+    if (degree == 3) {
+      const double mx[8] = {1, 2, 3, 3, 2, 1, 0, 0}, my[8] = {0, 0, 1, 2, 3, 3, 2, 1};
+      for (int k = 0; k < 8; ++k) add(mx[k] * t, my[k] * t);
+      const double ix[4] = {1, 2, 2, 1}, iy[4] = {1, 1, 2, 2};
+      for (int k = 0; k < 4; ++k) add(ix[k] * t, iy[k] * t);
+    }
+  }
+}
+
+// ============================================================ geometry ====
+namespace {
+// Eigen 2x2 inverse of M = J^T (Eigen/src/LU/InverseImpl.h, size-2 path):
+// invdet = 1/det; inv = [m11, -m01; -m10, m00] * invdet.
+inline void InverseTranspose(const double J[2][2], double out[2][2]) {
+  const double m00 = J[0][0], m01 = J[1][0], m10 = J[0][1], m11 = J[1][1];
+  const double det = m00 * m11 - m10 * m01;
+  const double invdet = 1.0 / det;
+  out[0][0] = m11 * invdet;
+  out[1][0] = -m10 * invdet;
+  out[0][1] = -m01 * invdet;
+  out[1][1] = m00 * invdet;
+}
+inline void Jacobian(const CellGeom& g, double xh, double yh, double J[2][2]) {
+  if (!g.is_quad) {  // tria_o1.cc:56
+    for (int d = 0; d < 2; ++d) {
+      J[d][0] = g.v[1][d] - g.v[0][d];
+      J[d][1] = g.v[2][d] - g.v[0][d];
+    }
+  } else {  // quad_o1.cc:93-99
+    for (int d = 0; d < 2; ++d) {
+      J[d][0] = (g.v[1][d] - g.v[0][d]) * (1 - yh) + (g.v[2][d] - g.v[3][d]) * yh;
+      J[d][1] = (g.v[3][d] - g.v[0][d]) * (1 - xh) + (g.v[2][d] - g.v[1][d]) * xh;
+    }
+  }
+}
+}  // namespace
+
+void CellGeom::JinvT(double xh, double yh, double out[2][2]) const {
+  double J[2][2];
+  Jacobian(*this, xh, yh, J);
+  InverseTranspose(J, out);
+}
+double CellGeom::IntegrationElement(double xh, double yh) const {
+  double J[2][2];
+  Jacobian(*this, xh, yh, J);
+  return std::abs(J[0][0] * J[1][1] - J[1][0] * J[0][1]);
+}
+void CellGeom::Global(double xh, double yh, double out[2]) const {
+  for (int d = 0; d < 2; ++d) {
+    if (!is_quad) {  // tria_o1.cc:68-72
+      out[d] = v[0][d] * (1 - xh - yh) + v[1][d] * xh + v[2][d] * yh;
+    } else {  // quad_o1.cc:73-87
+      out[d] = v[0][d] * ((1 - xh) * (1 - yh)) + v[1][d] * (xh * (1 - yh)) +
+               v[2][d] * (xh * yh) + v[3][d] * ((1 - xh) * yh);
+    }
+  }
+}
+
+bool NonDegenerate(const CellGeom& g, double tol) {
+  const int nv = g.is_quad ? 4 : 3;
+  double lensq[4], circum = 0;
+  for (int k = 0; k < nv; ++k) {
+    const double* a = g.v[k];
+    const double* b = g.v[(k + 1) % nv];
+    lensq[k] = (b[0] - a[0]) * (b[0] - a[0]) + (b[1] - a[1]) * (b[1] - a[1]);
+    circum += lensq[k];
+  }
+  for (int k = 0; k < nv; ++k)
+    if (!(lensq[k] > tol * circum)) return false;
+  const double ar1 = (g.v[1][0] - g.v[0][0]) * (g.v[2][1] - g.v[0][1]) -
+                     (g.v[1][1] - g.v[0][1]) * (g.v[2][0] - g.v[0][0]);
+  double area = std::fabs(ar1);
+  if (g.is_quad) {
+    const double ar2 = (g.v[3][0] - g.v[0][0]) * (g.v[2][1] - g.v[0][1]) -
+                       (g.v[3][1] - g.v[0][1]) * (g.v[2][0] - g.v[0][0]);
+    area += std::fabs(ar2);
+  }
+  return area > tol * circum;
+}
+
+// ================================================================ mesh ====
+
+CellGeom Mesh::Geom(idx_t c) const {
+  CellGeom g;
+  g.is_quad = IsQuad(c);
+  for (int k = 0; k < 4; ++k) {
+    const idx_t v = cell_nodes[c][k];
+    g.v[k][0] = v >= 0 ? xy[2 * v] : 0.0;
+    g.v[k][1] = v >= 0 ? xy[2 * v + 1] : 0.0;
+  }
+  return g;
+}
+
+namespace {
+// EndpointIndexPair of hybrid2d/mesh.cc:130-165: compares by (min,max) and
+// remembers the endpoint order of whoever created it.
+struct EdgeKey {
+  idx_t lo, hi;
+  bool operator<(const EdgeKey& o) const { return lo == o.lo ? hi < o.hi : lo < o.lo; }
+};
+struct EdgeData {
+  idx_t p0, p1;
+  idx_t global_index;
+  std::vector<std::pair<idx_t, int>> adj;  // (cell, local edge)
+};
+}  // namespace
+
+Mesh BuildMesh(idx_t num_nodes, const double* xy, idx_t num_cells,
+               const int64_t* cn, idx_t num_preset, const int64_t* pe) {
+  Mesh m;
+  m.num_nodes = num_nodes;
+  m.xy.assign(xy, xy + 2 * num_nodes);
+  m.num_cells = num_cells;
+  m.cell_nodes.resize(num_cells);
+  std::map<EdgeKey, EdgeData> edge_map;
+  // predefined edges (mesh.cc:237-274)
+  idx_t edge_index = 0;
+  for (idx_t e = 0; e < num_preset; ++e) {
+    const idx_t a = pe[2 * e], b = pe[2 * e + 1];
+    if (a < 0 || b < 0 || a >= num_nodes || b >= num_nodes || a == b)
+      throw Error("illegal preset edge " + std::to_string(e));
+    EdgeKey k{std::min(a, b), std::max(a, b)};
+    auto ins = edge_map.insert({k, EdgeData{a, b, edge_index, {}}});
+    if (!ins.second) throw Error("duplicate preset edge " + std::to_string(e));
+    ++edge_index;
+  }
+  // cells (mesh.cc:305-437)
+  for (idx_t c = 0; c < num_cells; ++c) {
+    for (int k = 0; k < 4; ++k) m.cell_nodes[c][k] = cn[4 * c + k];
+    const int nv = m.cell_nodes[c][3] < 0 ? 3 : 4;
+    for (int k = 0; k < nv; ++k)
+      if (m.cell_nodes[c][k] < 0 || m.cell_nodes[c][k] >= num_nodes)
+        throw Error("cell " + std::to_string(c) + ": invalid node index");
+    for (int j = 0; j < nv; ++j) {
+      // local edge j = (v_j, v_{j+1 mod nv}) (base/ref_el.h:126-129)
+      const idx_t a = m.cell_nodes[c][j], b = m.cell_nodes[c][(j + 1) % nv];
+      if (a == b) throw Error("cell " + std::to_string(c) + ": loop edge");
+      EdgeKey k{std::min(a, b), std::max(a, b)};
+      auto it = edge_map.find(k);
+      if (it == edge_map.end()) {
+        edge_map.insert({k, EdgeData{a, b, -1, {{c, j}}}});
+      } else {
+        it->second.adj.push_back({c, j});
+      }
+    }
+  }
+  // number the remaining edges in map order (mesh.cc:523-563)
+  m.num_edges = static_cast<idx_t>(edge_map.size());
+  m.edge_nodes.assign(m.num_edges, {-1, -1});
+  m.edge_num_cells.assign(m.num_edges, 0);
+  m.cell_edges.assign(num_cells, {-1, -1, -1, -1});
+  m.cell_ori.assign(num_cells, {0, 0, 0, 0});
+  for (auto& kv : edge_map) {
+    EdgeData& ed = kv.second;
+    if (ed.global_index == -1) ed.global_index = edge_index++;
+    m.edge_nodes[ed.global_index] = {ed.p0, ed.p1};
+    m.edge_num_cells[ed.global_index] = static_cast<int32_t>(ed.adj.size());
+    for (auto& a : ed.adj) m.cell_edges[a.first][a.second] = ed.global_index;
+  }
+  // relative orientations (hybrid2d/triangle.cc:71-77, quad.cc:76)
+  for (idx_t c = 0; c < num_cells; ++c) {
+    const int nv = m.NumVerts(c);
+    for (int j = 0; j < nv; ++j)
+      m.cell_ori[c][j] = (m.edge_nodes[m.cell_edges[c][j]][0] == m.cell_nodes[c][j]) ? 1 : -1;
+  }
+  return m;
+}
+
+FactoryInput TPTriagInput(idx_t nx, idx_t ny, double x0, double y0, double x1,
+                          double y1) {
+  FactoryInput in;
+  const double hx = (x1 - x0) / nx, hy = (y1 - y0) / ny;
+  auto vid = [&](idx_t i, idx_t j) { return i + j * (nx + 1); };  // VertexIndex
+  for (idx_t j = 0; j <= ny; ++j)
+    for (idx_t i = 0; i <= nx; ++i) {
+      in.xy.push_back(x0 + static_cast<double>(static_cast<uint64_t>(i)) * hx);
+      in.xy.push_back(y0 + static_cast<double>(static_cast<uint64_t>(j)) * hy);
+    }
+  auto edge = [&](idx_t a, idx_t b) { in.edges.push_back(a); in.edges.push_back(b); };
+  for (idx_t i = 0; i < nx; ++i)
+    for (idx_t j = 0; j <= ny; ++j) edge(vid(i, j), vid(i + 1, j));
+  for (idx_t i = 0; i <= nx; ++i)
+    for (idx_t j = 0; j < ny; ++j) edge(vid(i, j), vid(i, j + 1));
+  for (idx_t i = 0; i < nx; ++i)
+    for (idx_t j = 0; j < ny; ++j) edge(vid(i, j), vid(i + 1, j + 1));
+  for (idx_t i = 0; i < nx; ++i)
+    for (idx_t j = 0; j < ny; ++j) {
+      const int64_t up[4] = {vid(i, j), vid(i + 1, j + 1), vid(i, j + 1), -1};
+      const int64_t lo[4] = {vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), -1};
+      in.cells.insert(in.cells.end(), up, up + 4);
+      in.cells.insert(in.cells.end(), lo, lo + 4);
+    }
+  return in;
+}
+
+FactoryInput TPQuadInput(idx_t nx, idx_t ny, double x0, double y0, double x1,
+                         double y1) {
+  FactoryInput in;
+  const double hx = (x1 - x0) / nx, hy = (y1 - y0) / ny;
+  auto vid = [&](idx_t i, idx_t j) { return i + j * (nx + 1); };
+  for (idx_t j = 0; j <= ny; ++j)
+    for (idx_t i = 0; i <= nx; ++i) {
+      in.xy.push_back(x0 + static_cast<double>(static_cast<uint64_t>(i)) * hx);
+      in.xy.push_back(y0 + static_cast<double>(static_cast<uint64_t>(j)) * hy);
+    }
+  for (idx_t i = 0; i < nx; ++i)
+    for (idx_t j = 0; j < ny; ++j) {
+      const int64_t q[4] = {vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)};
+      in.cells.insert(in.cells.end(), q, q + 4);
+    }
+  return in;
+}
+
+FactoryInput TestMesh0Input(double s) {
+  FactoryInput in;
+  const double pts[10][2] = {{1.5, 2}, {1, 1}, {2, 1}, {0, 0}, {1.5, 0},
+                             {3, 0},   {3, 2}, {3, 3}, {0, 3}, {0, 1}};
+  for (auto& p : pts) { in.xy.push_back(p[0] * s); in.xy.push_back(p[1] * s); }
+  const int64_t cells[9][4] = {{0, 8, 9, -1}, {3, 4, 1, -1}, {4, 2, 1, -1},
+                               {4, 5, 2, -1}, {5, 6, 2, -1}, {3, 1, 0, 9},
+                               {2, 6, 7, 0},  {0, 7, 8, -1}, {0, 1, 2, -1}};
+  for (auto& c : cells) in.cells.insert(in.cells.end(), c, c + 4);
+  return in;
+}
+
+void FlagEntitiesOnBoundary(const Mesh& m, std::vector<uint8_t>& nf,
+                            std::vector<uint8_t>& ef) {
+  nf.assign(m.num_nodes, 0);
+  ef.assign(m.num_edges, 0);
+  for (idx_t e = 0; e < m.num_edges; ++e)
+    if (m.edge_num_cells[e] == 1) {
+      ef[e] = 1;
+      nf[m.edge_nodes[e][0]] = 1;
+      nf[m.edge_nodes[e][1]] = 1;
+    }
+}
+
+// ========================================================= dof handler ====
+
+DofHandler MakeDofHandler(const Mesh& m, int np, int ns, int nt, int nq,
+                          bool check_edge_orientation) {
+  DofHandler d;
+  d.mesh = &m;
+  d.np = np; d.ns = ns; d.nt = nt; d.nq = nq;
+  // InitTotalNumDofs (dofhandler.cc:131-139)
+  d.n_node = np;
+  d.n_edge = 2 * np + ns;
+  d.n_tria = 3 * np + 3 * ns + nt;
+  d.n_quad = 4 * np + 4 * ns + nq;
+  d.n_cell = std::max(d.n_tria, d.n_quad);
+  idx_t dof = 0;
+  // Step I: nodes
+  d.node_dofs.assign(m.num_nodes * np, -1);
+  for (idx_t v = 0; v < m.num_nodes; ++v)
+    for (int j = 0; j < np; ++j) {
+      d.node_dofs[v * np + j] = dof++;
+      d.dof_entity.push_back({2, v});
+    }
+  // Step II: edges (endpoint dofs copied in edge direction, then interior)
+  d.edge_dofs.assign(m.num_edges * d.n_edge, -1);
+  for (idx_t e = 0; e < m.num_edges; ++e) {
+    idx_t off = e * d.n_edge;
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < np; ++j) d.edge_dofs[off++] = d.node_dofs[m.edge_nodes[e][k] * np + j];
+    for (int j = 0; j < ns; ++j) {
+      d.edge_dofs[off++] = dof++;
+      d.dof_entity.push_back({1, e});
+    }
+  }
+  // Step III: cells
+  const int ext_edge = d.n_edge - ns;
+  d.cell_dofs.assign(m.num_cells * d.n_cell, -1);
+  for (idx_t c = 0; c < m.num_cells; ++c) {
+    idx_t off = c * d.n_cell;
+    const int nv = m.NumVerts(c);
+    for (int k = 0; k < nv; ++k)
+      for (int j = 0; j < np; ++j) d.cell_dofs[off++] = d.node_dofs[m.cell_nodes[c][k] * np + j];
+    for (int k = 0; k < nv; ++k) {
+      const idx_t e = m.cell_edges[c][k];
+      const idx_t base = e * d.n_edge + ext_edge;
+      if (!check_edge_orientation || m.cell_ori[c][k] > 0) {
+        for (int j = 0; j < ns; ++j) d.cell_dofs[off++] = d.edge_dofs[base + j];
+      } else {
+        for (int j = ns - 1; j >= 0; --j) d.cell_dofs[off++] = d.edge_dofs[base + j];
+      }
+    }
+    const int nint = nv == 3 ? nt : nq;
+    for (int j = 0; j < nint; ++j) {
+      d.cell_dofs[off++] = dof++;
+      d.dof_entity.push_back({0, c});
+    }
+  }
+  d.num_dofs = dof;
+  return d;
+}
+
+DofHandler MakeLagrangeDofHandler(const Mesh& m, int degree) {
+  // {pt:1, seg:p-1, tria:(p-1)(p-2)/2, quad:(p-1)^2} (lagr_fe.h NumRefShapeFunctions)
+  const int p = degree;
+  return MakeDofHandler(m, 1, p - 1, (p - 1) * (p - 2) / 2, (p - 1) * (p - 1));
+}
+
+// ====================================================== mesh functions ====
+
+std::function<double(double, double)> AnalyticFunction(int func_id, const double* p) {
+  std::vector<double> q(p, p + 16);
+  const double pi = 3.14159265358979323846;
+  switch (func_id) {
+    case 1:  // polynomial sum_{i,j<=3} p[4i+j] x^i y^j
+      return [q](double x, double y) {
+        double xi[4] = {1, x, x * x, x * x * x}, yj[4] = {1, y, y * y, y * y * y};
+        double s = 0;
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) s += q[4 * i + j] * (xi[i] * yj[j]);
+        return s;
+      };
+    case 2:  // p0 + p1 sin(p2 pi x) sin(p3 pi y)
+      return [q, pi](double x, double y) {
+        return q[0] + q[1] * (std::sin(q[2] * pi * x) * std::sin(q[3] * pi * y));
+      };
+    case 3:  // p0 + p1 sin(p2 pi x) cos(p3 pi y)
+      return [q, pi](double x, double y) {
+        return q[0] + q[1] * (std::sin(q[2] * pi * x) * std::cos(q[3] * pi * y));
+      };
+    default:
+      throw Error("unknown analytic function id " + std::to_string(func_id));
+  }
+}
+
+void MeshFunction::Eval(const Mesh& m, idx_t cell, const QuadRule& qr,
+                        std::vector<double>& out) const {
+  out.assign(qr.n(), 0.0);
+  switch (kind) {
+    case kZero: return;
+    case kConstant:
+      for (auto& o : out) o = value;
+      return;
+    case kPerCell:
+      for (auto& o : out) o = data[cell];
+      return;
+    case kNodalO1: {
+      // MeshFunctionFE over an O1 space: value = local dofs . shape values
+      const bool q = m.IsQuad(cell);
+      const int nv = m.NumVerts(cell);
+      double phi[16], dphi[16][2];
+      for (int k = 0; k < qr.n(); ++k) {
+        EvalShape(q, 1, qr.x[k], qr.y[k], phi, dphi);
+        double s = 0;
+        for (int j = 0; j < nv; ++j) s += data[m.cell_nodes[cell][j]] * phi[j];
+        out[k] = s;
+      }
+      return;
+    }
+    case kAnalytic: {
+      const CellGeom g = m.Geom(cell);
+      for (int k = 0; k < qr.n(); ++k) {
+        double X[2];
+        g.Global(qr.x[k], qr.y[k], X);
+        out[k] = fn(X[0], X[1]);
+      }
+      return;
+    }
+  }
+  throw Error("bad mesh function kind");
+}
+
+void MeshFunction::EvalTensor(const Mesh& m, idx_t cell, const QuadRule& qr,
+                              std::vector<std::array<double, 4>>& out) const {
+  out.assign(qr.n(), {0, 0, 0, 0});
+  const CellGeom g = m.Geom(cell);
+  for (int k = 0; k < qr.n(); ++k) {
+    double X[2];
+    g.Global(qr.x[k], qr.y[k], X);
+    tensor_fn(X[0], X[1], out[k].data());
+  }
+}
+
+// ============================================================ providers ====
+namespace {
+void Tabulate(bool is_quad, int degree, const QuadRule& qr, std::vector<double>& phi,
+              std::vector<double>& dphi) {
+  const int n = NumShapeFunctions(is_quad, degree);
+  phi.assign(static_cast<size_t>(n) * qr.n(), 0.0);
+  dphi.assign(static_cast<size_t>(n) * qr.n() * 2, 0.0);
+  double p[16], dp[16][2];
+  for (int k = 0; k < qr.n(); ++k) {
+    EvalShape(is_quad, degree, qr.x[k], qr.y[k], p, dp);
+    for (int i = 0; i < n; ++i) {
+      phi[k * n + i] = p[i];
+      dphi[(k * n + i) * 2 + 0] = dp[i][0];
+      dphi[(k * n + i) * 2 + 1] = dp[i][1];
+    }
+  }
+}
+}  // namespace
+
+void RDProvider::Init() {
+  if (have_tria) Tabulate(false, degree, qr_tria, phi_t, dphi_t);
+  if (have_quad) Tabulate(true, degree, qr_quad, phi_q, dphi_q);
+}
+
+// ReactionDiffusionElementMatrixProvider::Eval (loc_comp_ellbvp.h:266-339).
+void RDProvider::Eval(idx_t cell, std::vector<double>& mat) const {
+  const bool q = mesh->IsQuad(cell);
+  if ((q && !have_quad) || (!q && !have_tria))
+    throw Error("No local shape function information or no quadrature rule for "
+                "reference element type");  // loc_comp_ellbvp.h:278-287
+  const QuadRule& qr = q ? qr_quad : qr_tria;
+  const std::vector<double>& phi = q ? phi_q : phi_t;
+  const std::vector<double>& dphi = q ? dphi_q : dphi_t;
+  const int n = NumShapeFunctions(q, degree);
+  const CellGeom g = mesh->Geom(cell);
+  if (!NonDegenerate(g)) throw Error("degenerate cell " + std::to_string(cell));
+  std::vector<double> av, gv;
+  std::vector<std::array<double, 4>> at;
+  if (alpha.IsTensor()) alpha.EvalTensor(*mesh, cell, qr, at);
+  else alpha.Eval(*mesh, cell, qr, av);
+  gamma.Eval(*mesh, cell, qr, gv);
+  mat.assign(static_cast<size_t>(n) * n, 0.0);
+  std::vector<double> G(2 * n), AG(2 * n);
+  for (int k = 0; k < qr.n(); ++k) {
+    const double w = qr.w[k] * g.IntegrationElement(qr.x[k], qr.y[k]);
+    double JT[2][2];
+    g.JinvT(qr.x[k], qr.y[k], JT);
+    // trf_grad = JinvT * grad^T (2 x n)
+    for (int i = 0; i < n; ++i) {
+      const double gx = dphi[(k * n + i) * 2], gy = dphi[(k * n + i) * 2 + 1];
+      G[i] = JT[0][0] * gx + JT[0][1] * gy;
+      G[n + i] = JT[1][0] * gx + JT[1][1] * gy;
+    }
+    if (alpha.IsTensor()) {
+      const auto& A = at[k];
+      for (int i = 0; i < n; ++i) {
+        AG[i] = A[0] * G[i] + A[1] * G[n + i];
+        AG[n + i] = A[2] * G[i] + A[3] * G[n + i];
+      }
+    } else {
+      for (int i = 0; i < 2 * n; ++i) AG[i] = av[k] * G[i];
+    }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        const double gg = G[i] * AG[j] + G[n + i] * AG[n + j];
+        const double mm = (gv[k] * phi[k * n + i]) * phi[k * n + j];
+        mat[i * n + j] += w * (gg + mm);
+      }
+  }
+}
+
+void LoadProvider::Init() {
+  std::vector<double> d;
+  Tabulate(false, degree, qr_tria, phi_t, d);
+  Tabulate(true, degree, qr_quad, phi_q, d);
+}
+
+// ScalarLoadElementVectorProvider::Eval (loc_comp_ellbvp.h:691-746).
+void LoadProvider::Eval(idx_t cell, std::vector<double>& vec) const {
+  const bool q = mesh->IsQuad(cell);
+  const QuadRule& qr = q ? qr_quad : qr_tria;
+  const std::vector<double>& phi = q ? phi_q : phi_t;
+  const int n = NumShapeFunctions(q, degree);
+  const CellGeom g = mesh->Geom(cell);
+  std::vector<double> fv;
+  f.Eval(*mesh, cell, qr, fv);
+  vec.assign(n, 0.0);
+  for (int k = 0; k < qr.n(); ++k) {
+    const double s = qr.w[k] * g.IntegrationElement(qr.x[k], qr.y[k]) * fv[k];
+    for (int i = 0; i < n; ++i) vec[i] += s * phi[k * n + i];
+  }
+}
+
+// ============================================================ assembly ====
+
+void AssembleMatrixLocally(const DofHandler& dh,
+                           const std::function<void(idx_t, std::vector<double>&)>& eval,
+                           COOMatrix& A) {
+  std::vector<double> em;
+  for (idx_t c = 0; c < dh.mesh->num_cells; ++c) {
+    const int n = dh.NumLocalDofs(c);
+    const idx_t* dofs = dh.GlobalDofIndices(c);
+    eval(c, em);
+    const int ld = static_cast<int>(std::lround(std::sqrt(static_cast<double>(em.size()))));
+    if (ld < n) throw Error("element matrix too small");
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) A.AddToEntry(dofs[i], dofs[j], em[i * ld + j]);
+  }
+}
+
+void AssembleVectorLocally(const DofHandler& dh,
+                           const std::function<void(idx_t, std::vector<double>&)>& eval,
+                           std::vector<double>& b) {
+  std::vector<double> ev;
+  for (idx_t c = 0; c < dh.mesh->num_cells; ++c) {
+    const int n = dh.NumLocalDofs(c);
+    const idx_t* dofs = dh.GlobalDofIndices(c);
+    eval(c, ev);
+    for (int i = 0; i < n; ++i) b[dofs[i]] += ev[i];
+  }
+}
+
+void FixFlaggedSolutionComponents(const uint8_t* flags, const double* values,
+                                  COOMatrix& A, std::vector<double>& b) {
+  const idx_t N = A.cols;
+  {
+    std::vector<double> tmp(N);
+    for (idx_t k = 0; k < N; ++k) tmp[k] = flags[k] ? values[k] : 0.0;
+    // MatVecMult(-1.0, tmp, b) (coomatrix.h:248-260)
+    for (const Triplet& t : A.triplets) b[t.row] += t.value * (-1.0 * tmp[t.col]);
+  }
+  for (idx_t k = 0; k < N; ++k)
+    if (flags[k]) b[k] = values[k];
+  // setZero(pred): order-preserving std::remove_if (coomatrix.h:108-115)
+  auto last = std::remove_if(A.triplets.begin(), A.triplets.end(), [&](const Triplet& t) {
+    return flags[t.row] || flags[t.col];
+  });
+  A.triplets.erase(last, A.triplets.end());
+  for (idx_t k = 0; k < N; ++k)
+    if (flags[k]) A.AddToEntry(k, k, 1.0);
+}
+
+void FixFlaggedSolutionCompAlt(const uint8_t* flags, const double* values,
+                               COOMatrix& A, std::vector<double>& b) {
+  const idx_t N = A.cols;
+  for (idx_t k = 0; k < N; ++k)
+    if (flags[k]) b[k] = values[k];
+  auto last = std::remove_if(A.triplets.begin(), A.triplets.end(),
+                             [&](const Triplet& t) { return flags[t.row] != 0; });
+  A.triplets.erase(last, A.triplets.end());
+  for (idx_t k = 0; k < N; ++k)
+    if (flags[k]) A.AddToEntry(k, k, 1.0);
+}
+
+void MakeSparseCSR(const COOMatrix& A, std::vector<int64_t>& rowptr,
+                   std::vector<int32_t>& colind, std::vector<double>& val) {
+  const size_t nt = A.triplets.size();
+  std::vector<size_t> perm(nt);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
+    const Triplet &x = A.triplets[a], &y = A.triplets[b];
+    return x.row != y.row ? x.row < y.row : x.col < y.col;
+  });
+  rowptr.assign(A.rows + 1, 0);
+  colind.clear();
+  val.clear();
+  for (size_t k = 0; k < nt; ++k) {
+    const Triplet& t = A.triplets[perm[k]];
+    if (!colind.empty() && k > 0) {
+      const Triplet& p = A.triplets[perm[k - 1]];
+      if (p.row == t.row && p.col == t.col) {
+        val.back() = val.back() + t.value;  // collapseDuplicates: acc + next
+        continue;
+      }
+    }
+    colind.push_back(t.col);
+    val.push_back(t.value);
+    rowptr[t.row + 1]++;
+  }
+  for (idx_t r = 0; r < A.rows; ++r) rowptr[r + 1] += rowptr[r];
+}
+
+void NodalProjection(const DofHandler& dh, int degree,
+                     const std::function<double(double, double)>& u,
+                     std::vector<double>& out) {
+  out.assign(dh.num_dofs, 0.0);
+  std::vector<double> nodes;
+  for (idx_t c = 0; c < dh.mesh->num_cells; ++c) {
+    const bool q = dh.mesh->IsQuad(c);
+    EvaluationNodes(q, degree, nodes);
+    const CellGeom g = dh.mesh->Geom(c);
+    const int n = dh.NumLocalDofs(c);
+    const idx_t* dofs = dh.GlobalDofIndices(c);
+    for (int j = 0; j < n; ++j) {
+      double X[2];
+      g.Global(nodes[2 * j], nodes[2 * j + 1], X);
+      out[dofs[j]] = u(X[0], X[1]);
+    }
+  }
+}
+
+}  // namespace lfo

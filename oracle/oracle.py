@@ -1,0 +1,322 @@
+"""ctypes front end of the oracle (test infrastructure only).
+
+The oracle is a CPU restatement of LehrFEM++'s assembly path (see lfo.h).  Only
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs may import this
+module; the library in lehrfempp_gb300/ never does.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+_lock = threading.Lock()
+
+ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC = 0, 1, 2, 3, 4
+FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (g++, a few seconds)."""
+    srcs = [os.path.join(_HERE, f) for f in ("lfo_core.cc", "lfo_capi.cc", "lfo.h", "tria_rules.inc")]
+    if not force and os.path.exists(_LIB_PATH):
+        if os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
+            return _LIB_PATH
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class lfo_coeff(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("func", C.c_int32), ("value", C.c_double),
+                ("data", C.POINTER(C.c_double)), ("p", C.c_double * 16)]
+
+
+def coeff(kind=ZERO, value=0.0, data=None, func=0, params=()):
+    c = lfo_coeff()
+    c.kind = kind
+    c.value = value
+    c.func = func
+    keep = None
+    if data is not None:
+        keep = np.ascontiguousarray(data, dtype=np.float64)
+        c.data = keep.ctypes.data_as(C.POINTER(C.c_double))
+    for i, v in enumerate(params):
+        c.p[i] = v
+    c._keep = keep  # keep the array alive with the struct
+    return c
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(_LIB_PATH)
+            vp, i64, i32, dp = C.c_void_p, C.c_int64, C.c_int32, C.c_double
+            P = C.POINTER
+            L.lfo_input_create.argtypes = [C.c_int, i64, i64, dp, dp, dp, dp, P(vp), P(i64), C.c_char_p, C.c_int]
+            L.lfo_input_copy.argtypes = [vp, P(dp), P(i64), P(i64)]
+            L.lfo_input_destroy.argtypes = [vp]
+            L.lfo_mesh_create.argtypes = [i64, P(dp), i64, P(i64), i64, P(i64), P(vp), C.c_char_p, C.c_int]
+            L.lfo_mesh_destroy.argtypes = [vp]
+            L.lfo_mesh_sizes.argtypes = [vp, P(i64)]
+            L.lfo_mesh_topology.argtypes = [vp, P(i64), P(i64), P(C.c_int8), P(i32)]
+            L.lfo_boundary_flags.argtypes = [vp, P(C.c_uint8), P(C.c_uint8)]
+            L.lfo_mesh_degenerate_cells.argtypes = [vp, P(i64)]
+            L.lfo_space_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(vp), C.c_char_p, C.c_int]
+            L.lfo_space_destroy.argtypes = [vp]
+            L.lfo_space_info.argtypes = [vp, P(i64)]
+            L.lfo_space_cell_dofs.argtypes = [vp, P(i64)]
+            L.lfo_space_dof_entity.argtypes = [vp, P(i32), P(i64)]
+            L.lfo_quad_rule.argtypes = [C.c_int, C.c_int, P(dp), P(dp), P(dp), P(C.c_int), C.c_char_p, C.c_int]
+            L.lfo_assemble_rd.argtypes = [vp, P(lfo_coeff), P(lfo_coeff), C.c_int, C.c_int, i64, i64, P(vp), C.c_char_p, C.c_int]
+            L.lfo_assemble_load.argtypes = [vp, P(lfo_coeff), C.c_int, C.c_int, P(dp), C.c_char_p, C.c_int]
+            L.lfo_assemble_tabulated.argtypes = [vp, P(dp), C.c_int, P(dp), P(dp), P(vp), C.c_char_p, C.c_int]
+            L.lfo_coo_create.argtypes = [i64, i64, i64, P(i32), P(i32), P(dp)]
+            L.lfo_coo_create.restype = vp
+            L.lfo_coo_destroy.argtypes = [vp]
+            L.lfo_coo_size.argtypes = [vp]
+            L.lfo_coo_size.restype = i64
+            L.lfo_coo_copy.argtypes = [vp, P(i32), P(i32), P(dp)]
+            L.lfo_fix_flagged.argtypes = [vp, P(C.c_uint8), P(dp), P(dp), C.c_int, C.c_char_p, C.c_int]
+            L.lfo_csr_create.argtypes = [vp, P(i64)]
+            L.lfo_csr_create.restype = vp
+            L.lfo_csr_copy.argtypes = [vp, P(i64), P(i32), P(dp)]
+            L.lfo_csr_destroy.argtypes = [vp]
+            L.lfo_nodal_projection.argtypes = [vp, C.c_int, P(dp), P(dp), C.c_char_p, C.c_int]
+            L.lfo_kat_tensor_rd.argtypes = [P(dp), C.c_char_p, C.c_int]
+            _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def _check(rc, err):
+    if rc != 0:
+        raise RuntimeError("oracle: " + err.value.decode(errors="replace"))
+
+
+def _err():
+    return C.create_string_buffer(512)
+
+
+def factory_input(kind, nx=0, ny=0, x0=0.0, y0=0.0, x1=1.0, y1=1.0):
+    """Factory arrays (xy, cells[4], preset edges[2]) of a reference builder.
+
+    kind: "tptriag" (TPTriagMeshBuilder), "tpquad" (TPQuadMeshBuilder) or
+    "test0" (GenerateHybrid2DTestMesh(0), x0 = scale)."""
+    L = lib()
+    k = {"tptriag": 0, "tpquad": 1, "test0": 2}[kind]
+    h = C.c_void_p()
+    sizes = np.zeros(3, np.int64)
+    err = _err()
+    _check(L.lfo_input_create(k, nx, ny, x0, y0, x1, y1, C.byref(h), _p(sizes, C.c_int64), err, 512), err)
+    xy = np.zeros((sizes[0], 2))
+    cells = np.zeros((sizes[1], 4), np.int64)
+    edges = np.zeros((max(sizes[2], 1), 2), np.int64)
+    L.lfo_input_copy(h, _p(xy, C.c_double), _p(cells, C.c_int64), _p(edges, C.c_int64))
+    L.lfo_input_destroy(h)
+    return xy, cells, edges[: sizes[2]]
+
+
+class Mesh:
+    """hybrid2d::Mesh numbering restated (mesh.cc:178-810)."""
+
+    def __init__(self, xy, cells, preset_edges=None):
+        L = lib()
+        self.xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+        self.cells = np.ascontiguousarray(cells, np.int64).reshape(-1, 4)
+        pe = np.zeros((0, 2), np.int64) if preset_edges is None else np.ascontiguousarray(preset_edges, np.int64).reshape(-1, 2)
+        self._pe = pe
+        self.h = C.c_void_p()
+        err = _err()
+        _check(L.lfo_mesh_create(len(self.xy), _p(self.xy, C.c_double), len(self.cells), _p(self.cells, C.c_int64),
+                                 len(pe), _p(pe, C.c_int64) if len(pe) else None, C.byref(self.h), err, 512), err)
+        s = np.zeros(3, np.int64)
+        L.lfo_mesh_sizes(self.h, _p(s, C.c_int64))
+        self.num_nodes, self.num_edges, self.num_cells = (int(v) for v in s)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.lfo_mesh_destroy(self.h)
+            self.h = None
+
+    def topology(self):
+        en = np.zeros((self.num_edges, 2), np.int64)
+        ce = np.zeros((self.num_cells, 4), np.int64)
+        co = np.zeros((self.num_cells, 4), np.int8)
+        nc = np.zeros(self.num_edges, np.int32)
+        lib().lfo_mesh_topology(self.h, _p(en, C.c_int64), _p(ce, C.c_int64), _p(co, C.c_int8), _p(nc, C.c_int32))
+        return en, ce, co, nc
+
+    def boundary_flags(self):
+        nf = np.zeros(self.num_nodes, np.uint8)
+        ef = np.zeros(self.num_edges, np.uint8)
+        lib().lfo_boundary_flags(self.h, _p(nf, C.c_uint8), _p(ef, C.c_uint8))
+        return nf, ef
+
+    def num_degenerate(self):
+        n = C.c_int64()
+        lib().lfo_mesh_degenerate_cells(self.h, C.byref(n))
+        return n.value
+
+
+class Space:
+    """UniformFEDofHandler (dofhandler.cc:86-338); degree>0 = FeSpaceLagrangeO<degree>."""
+
+    def __init__(self, mesh, degree=0, layout=(0, 0, 0, 0)):
+        self.mesh = mesh
+        self.degree = degree
+        self.h = C.c_void_p()
+        err = _err()
+        _check(lib().lfo_space_create(mesh.h, degree, *layout, C.byref(self.h), err, 512), err)
+        info = np.zeros(4, np.int64)
+        lib().lfo_space_info(self.h, _p(info, C.c_int64))
+        self.num_dofs, self.n_cell, self.n_tria, self.n_quad = (int(v) for v in info)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.lfo_space_destroy(self.h)
+            self.h = None
+
+    def cell_dofs(self):
+        out = np.zeros((self.mesh.num_cells, self.n_cell), np.int64)
+        lib().lfo_space_cell_dofs(self.h, _p(out, C.c_int64))
+        return out
+
+    def dof_entities(self):
+        cod = np.zeros(self.num_dofs, np.int32)
+        idx = np.zeros(self.num_dofs, np.int64)
+        lib().lfo_space_dof_entity(self.h, _p(cod, C.c_int32), _p(idx, C.c_int64))
+        return cod, idx
+
+    def boundary_dof_flags(self):
+        """Selector of the reference drivers: dof flagged iff its entity is on the boundary."""
+        nf, ef = self.mesh.boundary_flags()
+        cod, idx = self.dof_entities()
+        fl = np.zeros(self.num_dofs, np.uint8)
+        fl[cod == 2] = nf[idx[cod == 2]]
+        fl[cod == 1] = ef[idx[cod == 1]]
+        return fl
+
+
+class COO:
+    def __init__(self, h, rows, cols):
+        self.h = h
+        self.rows = rows
+        self.cols = cols
+
+    @classmethod
+    def from_arrays(cls, rows, cols, r, c, v):
+        r = np.ascontiguousarray(r, np.int32)
+        c = np.ascontiguousarray(c, np.int32)
+        v = np.ascontiguousarray(v, np.float64)
+        h = lib().lfo_coo_create(rows, cols, len(v), _p(r, C.c_int32), _p(c, C.c_int32), _p(v, C.c_double))
+        return cls(C.c_void_p(h), rows, cols)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.lfo_coo_destroy(self.h)
+            self.h = None
+
+    def __len__(self):
+        return int(lib().lfo_coo_size(self.h))
+
+    def arrays(self):
+        n = len(self)
+        r = np.zeros(n, np.int32)
+        c = np.zeros(n, np.int32)
+        v = np.zeros(n, np.float64)
+        if n:
+            lib().lfo_coo_copy(self.h, _p(r, C.c_int32), _p(c, C.c_int32), _p(v, C.c_double))
+        return r, c, v
+
+    def fix_flagged(self, flags, values, b, alt=False):
+        flags = np.ascontiguousarray(flags, np.uint8)
+        values = np.ascontiguousarray(values, np.float64)
+        assert b.dtype == np.float64 and b.flags.c_contiguous
+        err = _err()
+        _check(lib().lfo_fix_flagged(self.h, _p(flags, C.c_uint8), _p(values, C.c_double), _p(b, C.c_double),
+                                     int(alt), err, 512), err)
+
+    def to_csr(self):
+        sizes = np.zeros(2, np.int64)
+        h = lib().lfo_csr_create(self.h, _p(sizes, C.c_int64))
+        rowptr = np.zeros(sizes[0] + 1, np.int64)
+        col = np.zeros(sizes[1], np.int32)
+        val = np.zeros(sizes[1], np.float64)
+        lib().lfo_csr_copy(h, _p(rowptr, C.c_int64), _p(col, C.c_int32), _p(val, C.c_double))
+        lib().lfo_csr_destroy(h)
+        return rowptr, col, val
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        rowptr, col, val = self.to_csr()
+        return sp.csr_matrix((val, col, rowptr), shape=(self.rows, self.cols))
+
+
+def assemble_rd(space, alpha, gamma, qdeg_tria=0, qdeg_quad=0, cells=(0, -1)):
+    """AssembleMatrixLocally with ReactionDiffusionElementMatrixProvider.
+
+    qdeg = 0 selects the default 2p rule; -1 leaves the cell type without a rule."""
+    h = C.c_void_p()
+    err = _err()
+    _check(lib().lfo_assemble_rd(space.h, C.byref(alpha), C.byref(gamma), qdeg_tria, qdeg_quad, cells[0], cells[1],
+                                 C.byref(h), err, 512), err)
+    return COO(h, space.num_dofs, space.num_dofs)
+
+
+def assemble_load(space, f, qdeg_tria=0, qdeg_quad=0, b=None):
+    b = np.zeros(space.num_dofs) if b is None else np.ascontiguousarray(b, np.float64).copy()
+    err = _err()
+    _check(lib().lfo_assemble_load(space.h, C.byref(f), qdeg_tria, qdeg_quad, _p(b, C.c_double), err, 512), err)
+    return b
+
+
+def assemble_tabulated(space, elem, vec_elem=None):
+    """AssembleMatrixLocally/AssembleVectorLocally with a provider that returns
+    the given element matrices elem[cell] (ld x ld, row major)."""
+    elem = np.ascontiguousarray(elem, np.float64)
+    ld = elem.shape[1]
+    h = C.c_void_p()
+    err = _err()
+    b = None
+    if vec_elem is not None:
+        vec_elem = np.ascontiguousarray(vec_elem, np.float64)
+        b = np.zeros(space.num_dofs)
+    _check(lib().lfo_assemble_tabulated(space.h, _p(elem, C.c_double), ld,
+                                        _p(vec_elem, C.c_double) if vec_elem is not None else None,
+                                        _p(b, C.c_double) if b is not None else None, C.byref(h), err, 512), err)
+    return COO(h, space.num_dofs, space.num_dofs), b
+
+
+def nodal_projection(space, func, params):
+    out = np.zeros(space.num_dofs)
+    p = np.zeros(16)
+    p[: len(params)] = params
+    err = _err()
+    _check(lib().lfo_nodal_projection(space.h, func, _p(p, C.c_double), _p(out, C.c_double), err, 512), err)
+    return out
+
+
+def quad_rule(is_quad, degree):
+    n = C.c_int()
+    err = _err()
+    _check(lib().lfo_quad_rule(int(is_quad), degree, None, None, None, C.byref(n), err, 512), err)
+    x, y, w = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+    _check(lib().lfo_quad_rule(int(is_quad), degree, _p(x, C.c_double), _p(y, C.c_double), _p(w, C.c_double),
+                               C.byref(n), err, 512), err)
+    return x, y, w
+
+
+def kat_tensor_rd():
+    v = C.c_double()
+    err = _err()
+    _check(lib().lfo_kat_tensor_rd(C.byref(v), err, 512), err)
+    return v.value

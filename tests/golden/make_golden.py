@@ -1,0 +1,77 @@
+"""Extract the reference's own golden values for this path into a JSON fixture.
+
+Reads (as text) the LehrFEM++ test sources and writes reference_goldens.json
+next to this script.  The fixture is committed; the GPU machine never needs the
+reference checkout.  Sources:
+
+  lib/lf/assemble/test/assembly_tests.cc   10x10 ref_mat (mat_assembly_test) and
+                                           36x36 ref_mat (edge_dof_static)
+  lib/lf/assemble/test/coomatrix_tests.cc  fix_dof exact solution
+  lib/lf/uscalfe/test/lagr_fe_tests.cc     reaction-diffusion bilinear forms
+
+usage: python tests/golden/make_golden.py /root/reference
+"""
+import json
+import os
+import re
+import sys
+
+
+def _matrix_after(text, marker, n):
+    i = text.index(marker)
+    j = text.index("<<", i)
+    k = text.index(";", j)
+    body = text[j + 2:k]
+    vals = [float(v) for v in re.findall(r"-?\d+(?:\.\d+)?", body)]
+    assert len(vals) == n * n, (marker, len(vals))
+    return [vals[r * n:(r + 1) * n] for r in range(n)]
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    at = open(os.path.join(ref, "lib/lf/assemble/test/assembly_tests.cc")).read()
+    ct = open(os.path.join(ref, "lib/lf/assemble/test/coomatrix_tests.cc")).read()
+    lt = open(os.path.join(ref, "lib/lf/uscalfe/test/lagr_fe_tests.cc")).read()
+
+    ref10 = _matrix_after(at, "Eigen::MatrixXd ref_mat(10, 10);", 10)
+    ref36 = _matrix_after(at, "Eigen::MatrixXd ref_mat(36, 36);", 36)
+    m = re.search(r"exact << (1, 1, -1[^;]+);", ct)
+    exact = [float(v) for v in m.group(1).split(",")]
+
+    def near(pattern):
+        mm = re.search(pattern, lt)
+        return mm.group(1)
+
+    kat = {
+        "O1_tensor_deg4": {"value_expr": near(r"EXPECT_NEAR\(product, (7911\. / 8\.)"), "value": 7911.0 / 8.0},
+        "O2_deg6": {"value_expr": near(r"EXPECT_NEAR\(product, (81\.)"), "value": 81.0},
+        "O3_deg8": {"value_expr": near(r"EXPECT_NEAR\(product, (1996731 / 280\.)"), "value": 1996731.0 / 280.0},
+        "tolerance": 1.0e-2,
+    }
+    out = {
+        "source": "LehrFEM++ test sources (read as text by tests/golden/make_golden.py)",
+        "mat_assembly_test_ref10": {
+            "file": "lib/lf/assemble/test/assembly_tests.cc:256-262",
+            "layout": "{Point:1}; compare dense(i,j) == ref[ent(i)][ent(j)], ent = node index of dof",
+            "matrix": ref10,
+        },
+        "edge_dof_static_ref36": {
+            "file": "lib/lf/assemble/test/assembly_tests.cc:394-455",
+            "layout": "{Segment:2}; compare dense(i,j) == ref[i][j]",
+            "matrix": ref36,
+        },
+        "fix_dof_exact": {
+            "file": "lib/lf/assemble/test/coomatrix_tests.cc:118-120",
+            "N": 10, "fixed": [[2, -1.0], [4, -2.0], [8, -3.0]], "tolerance": 1.0e-12,
+            "solution": exact,
+        },
+        "reaction_diffusion_kat": dict(kat, file="lib/lf/uscalfe/test/lagr_fe_tests.cc:807-883"),
+    }
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()
