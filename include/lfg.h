@@ -1,0 +1,299 @@
+/*
+ * lfg.h -- C-ABI of the GB300-native LehrFEM++ assembly-and-solve path.
+ *
+ * This is the drop-in boundary.  LehrFEM++ has no FFI of its own: its API for
+ * this path is a set of C++20 templates and concepts.  Each entry point below
+ * replaces one of them and is bound by the header-only C++ facade in
+ * include/lf/ (same class and function names as the reference) or, from
+ * Python, by lehrfempp_gb300/_capi.py (ctypes).  Citations are file:line in the
+ * LehrFEM++ source tree.
+ *
+ * Conventions
+ *   - Every function returns an lfg_status; LFG_OK == 0.  Nothing aborts; the
+ *     message of the last failure on a context is lfg_ctx_last_error().
+ *   - Arrays named *_dev are device pointers (allocated with lfg_malloc or by
+ *     any CUDA allocator on the context's device); arrays named *_host are host
+ *     pointers (pageable or pinned).  Sizes are element counts.
+ *   - All work of a context is ordered on the context's CUDA stream
+ *     (lfg_ctx_stream).  Calls on one context are not re-entrant; distinct
+ *     contexts are independent (reference: single-threaded library).
+ *   - Index types: DOF / node / edge / cell indices are int32 on the device;
+ *     a triplet is {int32 row, int32 col, double value} = 16 bytes, the memory
+ *     layout of Eigen::Triplet<double> (assemble/coomatrix.h:55).
+ */
+#ifndef LFG_H_
+#define LFG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  LFG_OK = 0,
+  LFG_INVALID_ARG = 1,      /* bad handle, size or index (LF_ASSERT_MSG in the reference)   */
+  LFG_DEGENERATE_CELL = 2,  /* geometry/tria_o1.cc:10-48, quad_o1.cc:12-58 (LF_VERIFY_MSG)   */
+  LFG_CAPACITY = 3,         /* output buffer too small; nothing was written                   */
+  LFG_UNSUPPORTED = 4,      /* coefficient kind / degree outside the supported set           */
+  LFG_NOT_CONVERGED = 5,    /* iterative solve hit its iteration cap                           */
+  LFG_CUDA_ERROR = 6,       /* a CUDA runtime call failed                                      */
+  LFG_MISSING_RULE = 7,     /* no quadrature rule for a cell type (loc_comp_ellbvp.h:278-287)  */
+  LFG_INCOMPLETE_MESH = 8,  /* hybrid2d/mesh.cc:566-600 check_completeness                     */
+  LFG_OUT_OF_MEMORY = 9
+} lfg_status;
+
+typedef struct lfg_ctx lfg_ctx;
+typedef struct lfg_mesh lfg_mesh;
+typedef struct lfg_space lfg_space;
+typedef struct lfg_coo lfg_coo;
+typedef struct lfg_csr lfg_csr;
+
+/* Eigen::Triplet<double> (StorageIndex int) layout. */
+typedef struct {
+  int32_t row;
+  int32_t col;
+  double value;
+} lfg_triplet;
+
+/* ------------------------------------------------------------------ context */
+lfg_status lfg_ctx_create(int device, lfg_ctx** out);
+lfg_status lfg_ctx_destroy(lfg_ctx* ctx);
+const char* lfg_ctx_last_error(const lfg_ctx* ctx);
+void* lfg_ctx_stream(lfg_ctx* ctx); /* the cudaStream_t all work is ordered on */
+lfg_status lfg_ctx_synchronize(lfg_ctx* ctx);
+/* Kernel launches issued by the library on this context since creation. */
+lfg_status lfg_ctx_launch_count(const lfg_ctx* ctx, int64_t* launches);
+
+/* Device memory and copies on the context's stream (no torch needed). */
+lfg_status lfg_malloc(lfg_ctx* ctx, size_t bytes, void** dev);
+lfg_status lfg_free(lfg_ctx* ctx, void* dev);
+lfg_status lfg_host_alloc(lfg_ctx* ctx, size_t bytes, void** pinned_host);
+lfg_status lfg_host_free(lfg_ctx* ctx, void* pinned_host);
+lfg_status lfg_memcpy_h2d(lfg_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes);
+lfg_status lfg_memcpy_d2h(lfg_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes);
+lfg_status lfg_memcpy_d2d(lfg_ctx* ctx, void* dst_dev, const void* src_dev, size_t bytes);
+lfg_status lfg_memset(lfg_ctx* ctx, void* dev, int value, size_t bytes);
+
+/* CUDA-event timing on the context stream, and an L2 flush (writes a buffer
+ * larger than L2) for cold-cache measurements. */
+lfg_status lfg_timer_begin(lfg_ctx* ctx);
+lfg_status lfg_timer_end(lfg_ctx* ctx, float* elapsed_ms);
+lfg_status lfg_l2_flush(lfg_ctx* ctx);
+/* Per-kernel timing (no reference counterpart; replaces lf::base::Timer,
+ * base/timer.h:64-278, for device work): while enabled, every element-kernel
+ * launch is bracketed by CUDA events on the context stream and accumulated
+ * under its kernel family name ("rd_tria_uniform", "rd_general_quad", ...). */
+lfg_status lfg_profile_enable(lfg_ctx* ctx, int enable);
+lfg_status lfg_profile_read(lfg_ctx* ctx, const char* family, double* total_ms, int64_t* launches);
+lfg_status lfg_profile_reset(lfg_ctx* ctx);
+/* Measured FP64 FMA throughput of this device (independent FMA chains on all
+ * SMs), the denominator of the FP64 roofline fraction. */
+lfg_status lfg_measure_fp64_peak(lfg_ctx* ctx, double* tflops);
+
+/* --------------------------------------------------------------------- mesh
+ * Replaces lf::mesh::hybrid2d::MeshFactory::AddPoint/AddEntity/Build
+ * (mesh/hybrid2d/mesh_factory.cc:18-125, mesh.cc:178-810).
+ *   node_xy_host        2 doubles per node, in AddPoint order
+ *   cell_nodes_host     4 int32 per cell in AddEntity order; -1 in slot 3 = triangle
+ *   preset_edges_host   2 int32 per edge registered before the cells (may be NULL)
+ * Numbering (bit-exact with the reference): nodes and cells keep their order;
+ * preset edges keep their registration index, edges created by cells follow
+ * in lexicographic (min, max) node order; an edge points the way its first
+ * creator lists it; relative orientation of local edge j (v_j -> v_{j+1}) is
+ * positive iff the edge starts at v_j.  Degenerate cells (tol 1e-8) and
+ * incomplete meshes are rejected. */
+lfg_status lfg_mesh_create(lfg_ctx* ctx, int64_t num_nodes, const double* node_xy_host,
+                           int64_t num_cells, const int32_t* cell_nodes_host,
+                           int64_t num_preset_edges, const int32_t* preset_edges_host,
+                           lfg_mesh** out);
+/* lf::mesh::utils::TPTriagMeshBuilder::Build (mesh/utils/tp_triag_mesh_builder.cc:18-178)
+ * and TPQuadMeshBuilder::Build (tp_quad_mesh_builder.cc:18-94), generated on the device. */
+lfg_status lfg_mesh_create_tp_triag(lfg_ctx* ctx, int64_t nx, int64_t ny, double x0, double y0,
+                                    double x1, double y1, lfg_mesh** out);
+lfg_status lfg_mesh_create_tp_quad(lfg_ctx* ctx, int64_t nx, int64_t ny, double x0, double y0,
+                                   double x1, double y1, lfg_mesh** out);
+lfg_status lfg_mesh_destroy(lfg_mesh* mesh);
+/* Mesh::NumEntities (mesh/mesh_interface.h:92-208); also counts by cell type. */
+lfg_status lfg_mesh_sizes(const lfg_mesh* mesh, int64_t* num_nodes, int64_t* num_edges,
+                          int64_t* num_cells, int64_t* num_trias, int64_t* num_quads);
+/* Topology for inspection: edge endpoints (2/edge, in edge direction), cell
+ * edges (4/cell, -1 pad), relative orientations (4/cell, +1/-1, 0 pad),
+ * number of cells adjacent to each edge (CountNumSuperEntities). */
+lfg_status lfg_mesh_download_topology(lfg_mesh* mesh, int32_t* edge_nodes_host,
+                                      int32_t* cell_edges_host, int8_t* cell_ori_host,
+                                      int32_t* edge_num_cells_host);
+/* Device arrays of the mesh: node_xy (2*N doubles), cell_nodes (4*C int32). */
+lfg_status lfg_mesh_device_arrays(lfg_mesh* mesh, const double** node_xy_dev,
+                                  const int32_t** cell_nodes_dev);
+/* Replace the node coordinates (same topology), from host or device memory. */
+lfg_status lfg_mesh_set_coords(lfg_mesh* mesh, const double* node_xy, int from_device);
+/* flagEntitiesOnBoundary (mesh/utils/special_entity_sets.cc:64-90): 1 byte per
+ * node / edge, device output. */
+lfg_status lfg_mesh_boundary_flags(lfg_mesh* mesh, uint8_t* node_flags_dev,
+                                   uint8_t* edge_flags_dev);
+
+/* ------------------------------------------------------------ FE space/dofs
+ * UniformFEDofHandler (assemble/dofhandler.h:260-503, dofhandler.cc:86-338)
+ * with num interior dofs per point / segment / tria / quad, check_edge_orientation
+ * = true.  lfg_space_create_lagrange = FeSpaceLagrangeO{1,2,3}
+ * (uscalfe/fe_space_lagrange_o1.h:45-51 etc.; layout uniform_scalar_fe_space.h:241-342). */
+lfg_status lfg_space_create(lfg_mesh* mesh, int np, int ns, int nt, int nq, lfg_space** out);
+lfg_status lfg_space_create_lagrange(lfg_mesh* mesh, int degree, lfg_space** out);
+lfg_status lfg_space_destroy(lfg_space* space);
+/* NumDofs, NumLocalDofs per tria / quad, row stride of the cell dof table,
+ * and the number of triplets one AssembleMatrixLocally call emits. */
+lfg_status lfg_space_info(const lfg_space* space, int64_t* num_dofs, int32_t* n_tria,
+                          int32_t* n_quad, int32_t* n_cell_stride, int64_t* num_triplets);
+/* GlobalDofIndices of every cell (num_cells x n_cell_stride, -1 pad), host out. */
+lfg_status lfg_space_download_cell_dofs(lfg_space* space, int32_t* cell_dofs_host);
+/* Entity(dof) for every dof: codim (2 node, 1 edge, 0 cell) and index, host out. */
+lfg_status lfg_space_download_dof_entities(lfg_space* space, int8_t* codim_host,
+                                           int32_t* index_host);
+/* Selector of the reference drivers: dof flagged iff its entity lies on the
+ * boundary (flagEntitiesOnBoundary + DofHandler::Entity), device output. */
+lfg_status lfg_space_boundary_dof_flags(lfg_space* space, uint8_t* flags_dev);
+
+/* ------------------------------------------------------------- coefficients
+ * A scalar MeshFunction (mesh/utils/mesh_function_traits.h:149-155) from a
+ * closed set that runs on the device:
+ *   LFG_COEFF_ZERO / CONSTANT        MeshFunctionConstant (mesh_function_constant.h:25-45)
+ *   LFG_COEFF_PER_CELL               one value per cell, data_dev[num_cells]
+ *   LFG_COEFF_NODAL_O1               MeshFunctionFE of an O1 dof vector,
+ *                                    data_dev[num_nodes] (fe/mesh_function_fe.h:44-115)
+ *   LFG_COEFF_ANALYTIC               MeshFunctionGlobal of a built-in function
+ *                                    (mesh_function_global.h:54-94) chosen by func:
+ *     LFG_FN_POLY    sum_{i,j<=3} p[4i+j] x^i y^j
+ *     LFG_FN_SINSIN  p0 + p1 sin(p2 pi x) sin(p3 pi y)
+ *     LFG_FN_SINCOS  p0 + p1 sin(p2 pi x) cos(p3 pi y)
+ * Arbitrary host lambdas cannot run on the GPU: anything else is LFG_UNSUPPORTED. */
+enum {
+  LFG_COEFF_ZERO = 0,
+  LFG_COEFF_CONSTANT = 1,
+  LFG_COEFF_PER_CELL = 2,
+  LFG_COEFF_NODAL_O1 = 3,
+  LFG_COEFF_ANALYTIC = 4
+};
+enum { LFG_FN_POLY = 1, LFG_FN_SINSIN = 2, LFG_FN_SINCOS = 3 };
+
+typedef struct {
+  int32_t kind;
+  int32_t func;
+  double value;
+  const double* data_dev;
+  double p[16];
+} lfg_coeff;
+
+/* ReactionDiffusionElementMatrixProvider (uscalfe/loc_comp_ellbvp.h:85-339):
+ * A_K = sum_k w_k |det J| [ (J^-T grad b_i)^T alpha (J^-T grad b_j) + gamma b_i b_j ].
+ * qr_degree_* = 0 selects the default degree 2p (loc_comp_ellbvp.h:227-228);
+ * a positive value selects make_QuadRule(type, degree) (the qr_collection
+ * constructor, :237-263); -1 leaves that cell type without a rule, and cells
+ * of that type then fail with LFG_MISSING_RULE. */
+typedef struct {
+  lfg_coeff alpha;
+  lfg_coeff gamma;
+  int32_t qr_degree_tria;
+  int32_t qr_degree_quad;
+} lfg_rd_provider;
+
+/* ScalarLoadElementVectorProvider (loc_comp_ellbvp.h:562-746). */
+typedef struct {
+  lfg_coeff f;
+  int32_t qr_degree_tria;
+  int32_t qr_degree_quad;
+} lfg_load_provider;
+
+/* ---------------------------------------------------------------- COO matrix
+ * lf::assemble::COOMatrix<double> (assemble/coomatrix.h:51-225) on the device. */
+lfg_status lfg_coo_create(lfg_ctx* ctx, int64_t rows, int64_t cols, int64_t capacity,
+                          lfg_coo** out);
+/* Wrap caller-owned device memory of `capacity` triplets holding `size` entries. */
+lfg_status lfg_coo_wrap(lfg_ctx* ctx, int64_t rows, int64_t cols, lfg_triplet* triplets_dev,
+                        int64_t capacity, int64_t size, lfg_coo** out);
+lfg_status lfg_coo_destroy(lfg_coo* coo);
+lfg_status lfg_coo_size(const lfg_coo* coo, int64_t* size);
+lfg_status lfg_coo_triplets(lfg_coo* coo, lfg_triplet** triplets_dev);
+/* COOMatrix::setZero() (coomatrix.h:95-98): drop all triplets. */
+lfg_status lfg_coo_set_zero(lfg_coo* coo);
+/* Copy the first `count` triplets to host memory (count <= size). */
+lfg_status lfg_coo_download(lfg_coo* coo, lfg_triplet* host, int64_t count);
+/* Append host triplets (AddToEntry for each). */
+lfg_status lfg_coo_append_host(lfg_coo* coo, const lfg_triplet* host, int64_t count);
+
+/* ------------------------------------------------------------------ assembly
+ * AssembleMatrixLocally(0, dofh, dofh, provider, A) (assemble/assembler.h:114-186):
+ * appends sum_K n_K^2 triplets to A, cells in index order, (i,j) row-major within
+ * a cell, row = GlobalDofIndices(K)[i], col = GlobalDofIndices(K)[j]. */
+lfg_status lfg_assemble_matrix_rd(lfg_space* space, const lfg_rd_provider* provider,
+                                  lfg_coo* coo);
+/* AssembleVectorLocally(0, dofh, provider, b) (assembler.h:298-327):
+ * b_dev[dof] += element vector entries, cells in index order (deterministic). */
+lfg_status lfg_assemble_vector_load(lfg_space* space, const lfg_load_provider* provider,
+                                    double* b_dev);
+/* Assembly with caller-tabulated element matrices / vectors: elem_dev holds
+ * num_cells blocks of ld x ld (row major; the first n_K x n_K entries are used),
+ * vec_dev num_cells blocks of ld.  This is the EntityMatrixProvider /
+ * EntityVectorProvider concept (assemble/assemble_concepts.h:95-99, 210-214)
+ * for providers whose Eval was computed elsewhere. */
+lfg_status lfg_assemble_matrix_tabulated(lfg_space* space, const double* elem_dev, int32_t ld,
+                                         lfg_coo* coo);
+lfg_status lfg_assemble_vector_tabulated(lfg_space* space, const double* vec_dev, int32_t ld,
+                                         double* b_dev);
+
+/* -------------------------------------------------------- Dirichlet fixing
+ * FixFlaggedSolutionComponents (assemble/fix_dof.h:86-138) with a tabulated
+ * selector: flags_dev[k] != 0 <=> dof k fixed to values_dev[k].
+ * b -= A xhat; b[k] = value[k] on fixed k; triplets with a fixed row or column
+ * are removed keeping the order of the others; (k,k,1.0) appended for fixed k
+ * in ascending order.  LFG_CAPACITY (nothing modified) if the appended
+ * diagonal does not fit. */
+lfg_status lfg_fix_flagged_solution_components(lfg_coo* coo, const uint8_t* flags_dev,
+                                               const double* values_dev, double* b_dev);
+/* FixFlaggedSolutionCompAlt (fix_dof.h:183-219): only fixed rows are removed. */
+lfg_status lfg_fix_flagged_solution_comp_alt(lfg_coo* coo, const uint8_t* flags_dev,
+                                             const double* values_dev, double* b_dev);
+
+/* ------------------------------------------------------------- CSR + solve
+ * COOMatrix::makeSparse (coomatrix.h:172-180) -> Eigen::setFromTriplets: the
+ * duplicates of each (row, col) are summed in triplet order.  Stored as CSR
+ * (int64 row pointers, int32 columns, double values). */
+lfg_status lfg_csr_from_coo(lfg_coo* coo, lfg_csr** out);
+lfg_status lfg_csr_destroy(lfg_csr* csr);
+lfg_status lfg_csr_info(const lfg_csr* csr, int64_t* rows, int64_t* cols, int64_t* nnz);
+lfg_status lfg_csr_download(lfg_csr* csr, int64_t* rowptr_host, int32_t* col_host,
+                            double* val_host);
+/* y = A x (FP64). */
+lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
+
+/* Solve A x = b for the (symmetric positive definite, after fixing) Galerkin
+ * matrix.  The reference solves with Eigen::SparseLU in its drivers
+ * (examples/ellbvp_linfe/homDir_linfe_demo.cc:168-174); on the GPU the solve is
+ * a Jacobi-preconditioned CG:
+ *   LFG_SOLVE_FP64   FP64 PCG to ||b - A x|| <= rtol ||b||
+ *   LFG_SOLVE_MIXED  FP32 PCG inner iterations (FP32 matrix copy and vectors)
+ *                    inside FP64 iterative refinement: r = b - A x in FP64,
+ *                    x += d in FP64, to the same FP64 residual criterion.
+ * x_dev holds the initial guess on entry. */
+enum { LFG_SOLVE_FP64 = 0, LFG_SOLVE_MIXED = 1 };
+typedef struct {
+  int32_t precision;
+  int32_t max_iterations;        /* total inner PCG iterations allowed           */
+  double rtol;                   /* relative residual target (FP64)              */
+  double inner_rtol;             /* mixed: relative reduction per inner solve    */
+  int32_t check_every;           /* convergence checks every N iterations        */
+} lfg_solve_opts;
+typedef struct {
+  int32_t iterations;            /* PCG iterations (all inner iterations)        */
+  int32_t refinements;           /* outer FP64 refinement steps (mixed)          */
+  double rel_residual;           /* final ||b - A x|| / ||b|| in FP64            */
+  int32_t converged;
+} lfg_solve_stats;
+lfg_status lfg_solve_pcg(lfg_csr* csr, const double* b_dev, double* x_dev,
+                         const lfg_solve_opts* opts, lfg_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LFG_H_ */

@@ -1,0 +1,486 @@
+"""GB300-native LehrFEM++ assembly-and-solve path (Python binding of the C-ABI).
+
+The compute path is the CUDA library lehrfempp_gb300/_build/liblfg.so built
+from csrc/ for sm_103a; this module only marshals arguments through ctypes.
+There is no CPU fallback: without the library or a GPU every call raises.
+
+Names follow the reference (lf::mesh / lf::assemble / lf::uscalfe):
+  Mesh              hybrid2d::MeshFactory + Build, TPTriag/TPQuadMeshBuilder
+  Space             UniformFEDofHandler / FeSpaceLagrangeO{1,2,3}
+  COOMatrix         assemble::COOMatrix<double> on the device
+  assemble_matrix_rd   AssembleMatrixLocally + ReactionDiffusionElementMatrixProvider
+  assemble_vector_load AssembleVectorLocally + ScalarLoadElementVectorProvider
+  COOMatrix.fix_flagged_solution_components   FixFlaggedSolutionComponents
+  COOMatrix.make_sparse                        COOMatrix::makeSparse (CSR)
+  CSRMatrix.solve_pcg                          Jacobi-PCG, FP64 or mixed precision
+"""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import _capi
+from ._capi import (lfg_coeff, lfg_load_provider, lfg_rd_provider, lfg_solve_opts, lfg_solve_stats,
+                    lfg_triplet)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "liblfg.so")
+_lib = None
+_lock = threading.Lock()
+
+# status codes (include/lfg.h)
+OK, INVALID_ARG, DEGENERATE_CELL, CAPACITY, UNSUPPORTED, NOT_CONVERGED, CUDA_ERROR, MISSING_RULE, \
+    INCOMPLETE_MESH, OUT_OF_MEMORY = range(10)
+STATUS_NAMES = ["OK", "INVALID_ARG", "DEGENERATE_CELL", "CAPACITY", "UNSUPPORTED", "NOT_CONVERGED",
+                "CUDA_ERROR", "MISSING_RULE", "INCOMPLETE_MESH", "OUT_OF_MEMORY"]
+
+# coefficient kinds and analytic families
+ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC = 0, 1, 2, 3, 4
+FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
+SOLVE_FP64, SOLVE_MIXED = 0, 1
+
+TRIPLET_DTYPE = np.dtype([("row", np.int32), ("col", np.int32), ("value", np.float64)])
+
+
+class LfgError(RuntimeError):
+    def __init__(self, code, msg):
+        self.code = code
+        super().__init__("%s: %s" % (STATUS_NAMES[code] if 0 <= code < len(STATUS_NAMES) else code, msg))
+
+
+def build(force=False, verbose=False):
+    from . import builder
+    return builder.build(force=force, verbose=verbose)
+
+
+def load(build_if_missing=True):
+    """Load liblfg.so (building it with nvcc first if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                if not build_if_missing:
+                    raise RuntimeError("GPU library %s is missing: run lehrfempp_gb300.build()" % LIB_PATH)
+                build()
+            _lib = _capi.declare(C.CDLL(LIB_PATH))
+    return _lib
+
+
+def lib():
+    return load()
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Context:
+    """lfg_ctx: one device, one CUDA stream."""
+
+    def __init__(self, device=0):
+        L = lib()
+        self.h = C.c_void_p()
+        rc = L.lfg_ctx_create(device, C.byref(self.h))
+        if rc != OK:
+            raise LfgError(rc, "could not create a CUDA context on device %d (is a GPU visible?)" % device)
+        self._children = []
+
+    def check(self, rc):
+        if rc != OK:
+            msg = lib().lfg_ctx_last_error(self.h)
+            raise LfgError(rc, msg.decode(errors="replace") if msg else "")
+
+    def close(self):
+        if self.h:
+            lib().lfg_ctx_synchronize(self.h)
+            lib().lfg_ctx_destroy(self.h)
+            self.h = None
+
+    def synchronize(self):
+        self.check(lib().lfg_ctx_synchronize(self.h))
+
+    def launches(self):
+        n = C.c_int64()
+        self.check(lib().lfg_ctx_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    # memory
+    def empty(self, shape, dtype):
+        return DeviceArray(self, shape, dtype)
+
+    def to_device(self, a):
+        a = np.ascontiguousarray(a)
+        d = DeviceArray(self, a.shape, a.dtype)
+        d.upload(a)
+        return d
+
+    def zeros(self, shape, dtype=np.float64):
+        d = DeviceArray(self, shape, dtype)
+        d.fill_zero()
+        return d
+
+    # timing on the context stream
+    def timer_begin(self):
+        self.check(lib().lfg_timer_begin(self.h))
+
+    def timer_end(self):
+        ms = C.c_float()
+        self.check(lib().lfg_timer_end(self.h, C.byref(ms)))
+        return ms.value
+
+    def l2_flush(self):
+        self.check(lib().lfg_l2_flush(self.h))
+
+    def pinned(self, shape, dtype):
+        return PinnedArray(self, shape, dtype)
+
+    # per-kernel-family event timing
+    def profile(self, enable=True):
+        self.check(lib().lfg_profile_enable(self.h, int(enable)))
+
+    def profile_read(self, family):
+        ms, n = C.c_double(), C.c_int64()
+        self.check(lib().lfg_profile_read(self.h, family.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def profile_reset(self):
+        self.check(lib().lfg_profile_reset(self.h))
+
+    def fp64_peak_tflops(self):
+        t = C.c_double()
+        self.check(lib().lfg_measure_fp64_peak(self.h, C.byref(t)))
+        return t.value
+
+
+class DeviceArray:
+    """A device allocation made through lfg_malloc (stream ordered)."""
+
+    def __init__(self, ctx, shape, dtype):
+        self.ctx = ctx
+        self.shape = tuple(np.atleast_1d(shape)) if not isinstance(shape, tuple) else shape
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self.ptr = C.c_void_p()
+        ctx.check(lib().lfg_malloc(ctx.h, self.nbytes, C.byref(self.ptr)))
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ctx.h:
+                lib().lfg_free(self.ctx.h, self.ptr)
+        except Exception:
+            pass
+        self.ptr = None
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.nbytes == self.nbytes, (a.nbytes, self.nbytes)
+        self.ctx.check(lib().lfg_memcpy_h2d(self.ctx.h, self.ptr, a.ctypes.data, self.nbytes))
+        self.ctx.synchronize()  # the host buffer may be temporary
+
+    def upload_async(self, host):
+        """Copy from a PinnedArray without synchronizing."""
+        self.ctx.check(lib().lfg_memcpy_h2d(self.ctx.h, self.ptr, host.ptr, self.nbytes))
+
+    def download(self):
+        out = np.empty(self.shape, self.dtype)
+        self.ctx.check(lib().lfg_memcpy_d2h(self.ctx.h, out.ctypes.data, self.ptr, self.nbytes))
+        return out
+
+    def download_into(self, host):
+        self.ctx.check(lib().lfg_memcpy_d2h(self.ctx.h, host.ptr, self.ptr, self.nbytes))
+
+    def fill_zero(self):
+        self.ctx.check(lib().lfg_memset(self.ctx.h, self.ptr, 0, self.nbytes))
+
+    def copy_from(self, other):
+        self.ctx.check(lib().lfg_memcpy_d2d(self.ctx.h, self.ptr, other.ptr, self.nbytes))
+
+
+class PinnedArray:
+    """Page-locked host memory (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, ctx, shape, dtype):
+        self.ctx = ctx
+        self.dtype = np.dtype(dtype)
+        self.shape = shape if isinstance(shape, tuple) else (int(shape),)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self.ptr = C.c_void_p()
+        ctx.check(lib().lfg_host_alloc(ctx.h, max(self.nbytes, 1), C.byref(self.ptr)))
+        buf = (C.c_char * max(self.nbytes, 1)).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(self.shape))).reshape(self.shape)
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ctx.h:
+                lib().lfg_host_free(self.ctx.h, self.ptr)
+        except Exception:
+            pass
+        self.ptr = None
+
+
+def coeff(kind=ZERO, value=0.0, data=None, func=0, params=()):
+    """lfg_coeff: data is a DeviceArray (per cell / per node) or None."""
+    c = lfg_coeff()
+    c.kind = kind
+    c.value = value
+    c.func = func
+    c.data_dev = data.ptr.value if data is not None else None
+    for i, v in enumerate(params):
+        c.p[i] = v
+    return c
+
+
+class Mesh:
+    """A 2D hybrid mesh on the device (hybrid2d::Mesh numbering)."""
+
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self.h = h
+        nv, ne, nc, nt, nq = (C.c_int64() for _ in range(5))
+        ctx.check(lib().lfg_mesh_sizes(h, C.byref(nv), C.byref(ne), C.byref(nc), C.byref(nt), C.byref(nq)))
+        self.num_nodes, self.num_edges, self.num_cells = nv.value, ne.value, nc.value
+        self.num_trias, self.num_quads = nt.value, nq.value
+
+    @classmethod
+    def from_factory(cls, ctx, xy, cells, preset_edges=None):
+        """MeshFactory::AddPoint / AddEntity / Build from arrays (cells: 4 per cell, -1 pad)."""
+        xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 2)
+        cells = np.ascontiguousarray(cells, np.int32).reshape(-1, 4)
+        pe = None if preset_edges is None or len(preset_edges) == 0 else \
+            np.ascontiguousarray(preset_edges, np.int32).reshape(-1, 2)
+        h = C.c_void_p()
+        ctx.check(lib().lfg_mesh_create(ctx.h, len(xy), _p(xy, C.c_double), len(cells), _p(cells, C.c_int32),
+                                        0 if pe is None else len(pe), None if pe is None else _p(pe, C.c_int32),
+                                        C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def tp_triag(cls, ctx, nx, ny, x0=0.0, y0=0.0, x1=1.0, y1=1.0):
+        h = C.c_void_p()
+        ctx.check(lib().lfg_mesh_create_tp_triag(ctx.h, nx, ny, x0, y0, x1, y1, C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def tp_quad(cls, ctx, nx, ny, x0=0.0, y0=0.0, x1=1.0, y1=1.0):
+        h = C.c_void_p()
+        ctx.check(lib().lfg_mesh_create_tp_quad(ctx.h, nx, ny, x0, y0, x1, y1, C.byref(h)))
+        return cls(ctx, h)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_mesh_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def topology(self):
+        en = np.zeros((self.num_edges, 2), np.int32)
+        ce = np.zeros((self.num_cells, 4), np.int32)
+        co = np.zeros((self.num_cells, 4), np.int8)
+        nc = np.zeros(self.num_edges, np.int32)
+        self.ctx.check(lib().lfg_mesh_download_topology(self.h, _p(en, C.c_int32), _p(ce, C.c_int32),
+                                                        _p(co, C.c_int8), _p(nc, C.c_int32)))
+        return en, ce, co, nc
+
+    def boundary_flags(self):
+        nf = self.ctx.empty(self.num_nodes, np.uint8)
+        ef = self.ctx.empty(max(self.num_edges, 1), np.uint8)
+        self.ctx.check(lib().lfg_mesh_boundary_flags(self.h, nf.ptr, ef.ptr))
+        return nf.download(), ef.download()[: self.num_edges]
+
+    def set_coords(self, xy):
+        if isinstance(xy, DeviceArray):
+            self.ctx.check(lib().lfg_mesh_set_coords(self.h, xy.ptr, 1))
+        else:
+            xy = np.ascontiguousarray(xy, np.float64)
+            self.ctx.check(lib().lfg_mesh_set_coords(self.h, xy.ctypes.data_as(C.c_void_p), 0))
+            self.ctx.synchronize()
+
+    def device_arrays(self):
+        xy, cells = C.c_void_p(), C.c_void_p()
+        self.ctx.check(lib().lfg_mesh_device_arrays(self.h, C.byref(xy), C.byref(cells)))
+        return xy, cells
+
+
+class Space:
+    """UniformFEDofHandler; Space.lagrange(mesh, p) = FeSpaceLagrangeO<p>."""
+
+    def __init__(self, mesh, h, degree):
+        self.mesh = mesh
+        self.ctx = mesh.ctx
+        self.h = h
+        self.degree = degree
+        nd, nt, nq, ncs, ntr = C.c_int64(), C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
+        self.ctx.check(lib().lfg_space_info(h, C.byref(nd), C.byref(nt), C.byref(nq), C.byref(ncs), C.byref(ntr)))
+        self.num_dofs, self.n_tria, self.n_quad, self.n_cell = nd.value, nt.value, nq.value, ncs.value
+        self.num_triplets = ntr.value
+
+    @classmethod
+    def lagrange(cls, mesh, degree):
+        h = C.c_void_p()
+        mesh.ctx.check(lib().lfg_space_create_lagrange(mesh.h, degree, C.byref(h)))
+        return cls(mesh, h, degree)
+
+    @classmethod
+    def layout(cls, mesh, np_, ns, nt, nq):
+        h = C.c_void_p()
+        mesh.ctx.check(lib().lfg_space_create(mesh.h, np_, ns, nt, nq, C.byref(h)))
+        return cls(mesh, h, 0)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_space_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def cell_dofs(self):
+        out = np.zeros((self.mesh.num_cells, self.n_cell), np.int32)
+        self.ctx.check(lib().lfg_space_download_cell_dofs(self.h, _p(out, C.c_int32)))
+        return out
+
+    def dof_entities(self):
+        cod = np.zeros(self.num_dofs, np.int8)
+        idx = np.zeros(self.num_dofs, np.int32)
+        self.ctx.check(lib().lfg_space_download_dof_entities(self.h, _p(cod, C.c_int8), _p(idx, C.c_int32)))
+        return cod, idx
+
+    def boundary_dof_flags(self):
+        f = self.ctx.empty(self.num_dofs, np.uint8)
+        self.ctx.check(lib().lfg_space_boundary_dof_flags(self.h, f.ptr))
+        return f
+
+
+class COOMatrix:
+    """assemble::COOMatrix<double> held in device memory."""
+
+    def __init__(self, ctx, rows, cols, capacity):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        ctx.check(lib().lfg_coo_create(ctx.h, rows, cols, capacity, C.byref(self.h)))
+        self.rows, self.cols, self.capacity = rows, cols, capacity
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_coo_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def __len__(self):
+        n = C.c_int64()
+        self.ctx.check(lib().lfg_coo_size(self.h, C.byref(n)))
+        return n.value
+
+    def set_zero(self):
+        self.ctx.check(lib().lfg_coo_set_zero(self.h))
+
+    def triplets(self):
+        n = len(self)
+        out = np.zeros(n, TRIPLET_DTYPE)
+        if n:
+            self.ctx.check(lib().lfg_coo_download(self.h, out.ctypes.data, n))
+        return out
+
+    def download_into(self, pinned, count=None):
+        n = len(self) if count is None else count
+        self.ctx.check(lib().lfg_coo_download(self.h, pinned.ptr, n))
+
+    def append(self, rows, cols, vals):
+        t = np.zeros(len(vals), TRIPLET_DTYPE)
+        t["row"], t["col"], t["value"] = rows, cols, vals
+        self.ctx.check(lib().lfg_coo_append_host(self.h, t.ctypes.data, len(t)))
+        self.ctx.synchronize()
+
+    def fix_flagged_solution_components(self, flags, values, b):
+        self.ctx.check(lib().lfg_fix_flagged_solution_components(self.h, flags.ptr, values.ptr, b.ptr))
+
+    def fix_flagged_solution_comp_alt(self, flags, values, b):
+        self.ctx.check(lib().lfg_fix_flagged_solution_comp_alt(self.h, flags.ptr, values.ptr, b.ptr))
+
+    def make_sparse(self):
+        h = C.c_void_p()
+        self.ctx.check(lib().lfg_csr_from_coo(self.h, C.byref(h)))
+        return CSRMatrix(self.ctx, h)
+
+
+class CSRMatrix:
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self.h = h
+        r, c, n = C.c_int64(), C.c_int64(), C.c_int64()
+        ctx.check(lib().lfg_csr_info(h, C.byref(r), C.byref(c), C.byref(n)))
+        self.rows, self.cols, self.nnz = r.value, c.value, n.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_csr_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def download(self):
+        rp = np.zeros(self.rows + 1, np.int64)
+        col = np.zeros(self.nnz, np.int32)
+        val = np.zeros(self.nnz, np.float64)
+        self.ctx.check(lib().lfg_csr_download(self.h, _p(rp, C.c_int64), _p(col, C.c_int32), _p(val, C.c_double)))
+        return rp, col, val
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        rp, col, val = self.download()
+        return sp.csr_matrix((val, col, rp), shape=(self.rows, self.cols))
+
+    def spmv(self, x, y):
+        self.ctx.check(lib().lfg_csr_spmv(self.h, x.ptr, y.ptr))
+
+    def solve_pcg(self, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=1e-4,
+                  check_every=32, raise_on_failure=True):
+        o = lfg_solve_opts()
+        o.precision, o.rtol, o.max_iterations, o.inner_rtol, o.check_every = (precision, rtol, max_iterations,
+                                                                             inner_rtol, check_every)
+        st = lfg_solve_stats()
+        rc = lib().lfg_solve_pcg(self.h, b.ptr, x.ptr, C.byref(o), C.byref(st))
+        if rc != OK and (raise_on_failure or rc != NOT_CONVERGED):
+            self.ctx.check(rc)
+        return {"iterations": st.iterations, "refinements": st.refinements, "rel_residual": st.rel_residual,
+                "converged": bool(st.converged)}
+
+
+def rd_provider(alpha, gamma, qr_degree_tria=0, qr_degree_quad=0):
+    p = lfg_rd_provider()
+    p.alpha, p.gamma = alpha, gamma
+    p.qr_degree_tria, p.qr_degree_quad = qr_degree_tria, qr_degree_quad
+    return p
+
+
+def load_provider(f, qr_degree_tria=0, qr_degree_quad=0):
+    p = lfg_load_provider()
+    p.f = f
+    p.qr_degree_tria, p.qr_degree_quad = qr_degree_tria, qr_degree_quad
+    return p
+
+
+def assemble_matrix_rd(space, provider, coo):
+    space.ctx.check(lib().lfg_assemble_matrix_rd(space.h, C.byref(provider), coo.h))
+
+
+def assemble_vector_load(space, provider, b):
+    space.ctx.check(lib().lfg_assemble_vector_load(space.h, C.byref(provider), b.ptr))
+
+
+def assemble_matrix_tabulated(space, elem_dev, ld, coo):
+    space.ctx.check(lib().lfg_assemble_matrix_tabulated(space.h, elem_dev.ptr, ld, coo.h))
+
+
+def assemble_vector_tabulated(space, vec_dev, ld, b):
+    space.ctx.check(lib().lfg_assemble_vector_tabulated(space.h, vec_dev.ptr, ld, b.ptr))

@@ -1,0 +1,111 @@
+"""ctypes declarations of the C-ABI in include/lfg.h.
+
+This is the Python-side binding a caller uses in place of the reference's C++
+templates (the C++ facade in include/lf/ is the other binding).  Every
+function listed in include/lfg.h is declared here; tests check both lists
+against the exported symbols of the shared library.
+"""
+import ctypes as C
+
+c_status = C.c_int
+vp = C.c_void_p
+i8, i32, i64 = C.c_int8, C.c_int32, C.c_int64
+u8 = C.c_uint8
+dbl = C.c_double
+sz = C.c_size_t
+P = C.POINTER
+
+
+class lfg_triplet(C.Structure):
+    _fields_ = [("row", i32), ("col", i32), ("value", dbl)]
+
+
+class lfg_coeff(C.Structure):
+    _fields_ = [("kind", i32), ("func", i32), ("value", dbl), ("data_dev", vp), ("p", dbl * 16)]
+
+
+class lfg_rd_provider(C.Structure):
+    _fields_ = [("alpha", lfg_coeff), ("gamma", lfg_coeff), ("qr_degree_tria", i32), ("qr_degree_quad", i32)]
+
+
+class lfg_load_provider(C.Structure):
+    _fields_ = [("f", lfg_coeff), ("qr_degree_tria", i32), ("qr_degree_quad", i32)]
+
+
+class lfg_solve_opts(C.Structure):
+    _fields_ = [("precision", i32), ("max_iterations", i32), ("rtol", dbl), ("inner_rtol", dbl),
+                ("check_every", i32)]
+
+
+class lfg_solve_stats(C.Structure):
+    _fields_ = [("iterations", i32), ("refinements", i32), ("rel_residual", dbl), ("converged", i32)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "lfg_ctx_create": (c_status, [C.c_int, P(vp)]),
+    "lfg_ctx_destroy": (c_status, [vp]),
+    "lfg_ctx_last_error": (C.c_char_p, [vp]),
+    "lfg_ctx_stream": (vp, [vp]),
+    "lfg_ctx_synchronize": (c_status, [vp]),
+    "lfg_ctx_launch_count": (c_status, [vp, P(i64)]),
+    "lfg_malloc": (c_status, [vp, sz, P(vp)]),
+    "lfg_free": (c_status, [vp, vp]),
+    "lfg_host_alloc": (c_status, [vp, sz, P(vp)]),
+    "lfg_host_free": (c_status, [vp, vp]),
+    "lfg_memcpy_h2d": (c_status, [vp, vp, vp, sz]),
+    "lfg_memcpy_d2h": (c_status, [vp, vp, vp, sz]),
+    "lfg_memcpy_d2d": (c_status, [vp, vp, vp, sz]),
+    "lfg_memset": (c_status, [vp, vp, C.c_int, sz]),
+    "lfg_timer_begin": (c_status, [vp]),
+    "lfg_timer_end": (c_status, [vp, P(C.c_float)]),
+    "lfg_l2_flush": (c_status, [vp]),
+    "lfg_profile_enable": (c_status, [vp, C.c_int]),
+    "lfg_profile_read": (c_status, [vp, C.c_char_p, P(dbl), P(i64)]),
+    "lfg_profile_reset": (c_status, [vp]),
+    "lfg_measure_fp64_peak": (c_status, [vp, P(dbl)]),
+    "lfg_mesh_create": (c_status, [vp, i64, P(dbl), i64, P(i32), i64, P(i32), P(vp)]),
+    "lfg_mesh_create_tp_triag": (c_status, [vp, i64, i64, dbl, dbl, dbl, dbl, P(vp)]),
+    "lfg_mesh_create_tp_quad": (c_status, [vp, i64, i64, dbl, dbl, dbl, dbl, P(vp)]),
+    "lfg_mesh_destroy": (c_status, [vp]),
+    "lfg_mesh_sizes": (c_status, [vp, P(i64), P(i64), P(i64), P(i64), P(i64)]),
+    "lfg_mesh_download_topology": (c_status, [vp, P(i32), P(i32), P(i8), P(i32)]),
+    "lfg_mesh_device_arrays": (c_status, [vp, P(vp), P(vp)]),
+    "lfg_mesh_set_coords": (c_status, [vp, vp, C.c_int]),
+    "lfg_mesh_boundary_flags": (c_status, [vp, vp, vp]),
+    "lfg_space_create": (c_status, [vp, C.c_int, C.c_int, C.c_int, C.c_int, P(vp)]),
+    "lfg_space_create_lagrange": (c_status, [vp, C.c_int, P(vp)]),
+    "lfg_space_destroy": (c_status, [vp]),
+    "lfg_space_info": (c_status, [vp, P(i64), P(i32), P(i32), P(i32), P(i64)]),
+    "lfg_space_download_cell_dofs": (c_status, [vp, P(i32)]),
+    "lfg_space_download_dof_entities": (c_status, [vp, P(i8), P(i32)]),
+    "lfg_space_boundary_dof_flags": (c_status, [vp, vp]),
+    "lfg_coo_create": (c_status, [vp, i64, i64, i64, P(vp)]),
+    "lfg_coo_wrap": (c_status, [vp, i64, i64, vp, i64, i64, P(vp)]),
+    "lfg_coo_destroy": (c_status, [vp]),
+    "lfg_coo_size": (c_status, [vp, P(i64)]),
+    "lfg_coo_triplets": (c_status, [vp, P(vp)]),
+    "lfg_coo_set_zero": (c_status, [vp]),
+    "lfg_coo_download": (c_status, [vp, vp, i64]),
+    "lfg_coo_append_host": (c_status, [vp, vp, i64]),
+    "lfg_assemble_matrix_rd": (c_status, [vp, P(lfg_rd_provider), vp]),
+    "lfg_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
+    "lfg_assemble_matrix_tabulated": (c_status, [vp, vp, i32, vp]),
+    "lfg_assemble_vector_tabulated": (c_status, [vp, vp, i32, vp]),
+    "lfg_fix_flagged_solution_components": (c_status, [vp, vp, vp, vp]),
+    "lfg_fix_flagged_solution_comp_alt": (c_status, [vp, vp, vp, vp]),
+    "lfg_csr_from_coo": (c_status, [vp, P(vp)]),
+    "lfg_csr_destroy": (c_status, [vp]),
+    "lfg_csr_info": (c_status, [vp, P(i64), P(i64), P(i64)]),
+    "lfg_csr_download": (c_status, [vp, P(i64), P(i32), P(dbl)]),
+    "lfg_csr_spmv": (c_status, [vp, vp, vp]),
+    "lfg_solve_pcg": (c_status, [vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats)]),
+}
+
+
+def declare(lib):
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib

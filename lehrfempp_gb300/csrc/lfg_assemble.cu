@@ -1,0 +1,699 @@
+// Element kernels: AssembleMatrixLocally with ReactionDiffusionElementMatrixProvider
+// and AssembleVectorLocally with ScalarLoadElementVectorProvider
+// (assemble/assembler.h:114-365, uscalfe/loc_comp_ellbvp.h:266-339, 691-746).
+//
+// Output contract (bit-exact indices and order): the triplets of cell K start
+// at coo_base + sum_{K' < K} n_{K'}^2 and run over (i, j) row-major with
+// row = dofs_K[i], col = dofs_K[j].  Values are the element matrix entries in
+// FP64.  The reference's per-quadrature-point sum
+//     A_K = sum_k w_k |det J_k| [ G_k^T alpha_k G_k + gamma_k phi_k phi_k^T ],
+//     G_k = J_k^{-T} grad(phi_hat)(q_k)
+// is evaluated as
+//     A_K(i,j) = sum_k [ c00_k T0 + c01_k T1 + c11_k T2 + m_k T3 ](k; i, j)
+// with c = w |det J| alpha J^{-1} J^{-T} (3 numbers per point), m = w |det J| gamma
+// and the cell-independent tables T(k; i,j) = {g_i0 g_j0, g_i0 g_j1 + g_i1 g_j0,
+// g_i1 g_j1, phi_i phi_j} of reference gradients g.  Only the upper triangle
+// i <= j is computed (the element matrix is symmetric) and mirrored.
+// For affine triangles with cell-constant alpha/gamma the point sum is folded
+// into R(i,j) = sum_k w_k T(k; i,j) once per rule, so a cell costs 3-4 FMAs
+// per entry.  Both are exact reformulations; they differ from the reference
+// only by rounding (checked to 1e-12 of max|A_K| in the parity tests).
+//
+// The device does FP64 arithmetic; cells are processed one per thread from
+// per-type cell lists (triangles and quadrilaterals run as separate launches
+// so a warp never diverges on the cell type).
+#include <map>
+
+#include "lfg_api.h"
+#include "lfg_internal.h"
+
+namespace lfg {
+void EnsureIncidence(lfg_space* sp);
+
+namespace {
+
+constexpr int kMaxQ = 25;
+
+struct CoeffDev {
+  int kind;
+  int func;
+  double value;
+  const double* data;
+  double p[16];
+};
+
+Tab TabLayout(int n, int nq) {
+  Tab t;
+  t.n = n; t.nq = nq; t.E = n * (n + 1) / 2;
+  t.off_w = 0;
+  t.off_qx = nq;
+  t.off_qy = 2 * nq;
+  t.off_phi = 3 * nq;
+  t.off_T = t.off_phi + nq * n;
+  t.off_R = t.off_T + nq * t.E * 4;
+  t.off_L = t.off_R + t.E * 4;
+  t.off_o1 = t.off_L + n;
+  t.total = t.off_o1 + nq * 4;
+  return t;
+}
+
+struct AsmArgs {
+  const int32_t* bucket;
+  int64_t count;
+  const int4* cells;
+  const double2* xy;
+  const int32_t* cell_dofs;
+  int n_cell;
+  const int64_t* tri_offset;  // per cell (triplet matrices) or loc_offset (vectors)
+  lfg_triplet* out;
+  double* vout;
+  const double* tab;
+  Tab L;
+  CoeffDev alpha, gamma;
+};
+
+// ------------------------------------------------------------- device helpers
+
+__device__ __forceinline__ void StoreTriplet(lfg_triplet* p, int r, int c, double v) {
+  const long long bits = __double_as_longlong(v);
+  int4 w = make_int4(r, c, static_cast<int>(bits & 0xffffffffll), static_cast<int>(bits >> 32));
+  *reinterpret_cast<int4*>(p) = w;
+}
+
+__device__ double EvalAnalytic(const CoeffDev& f, double x, double y) {
+  const double pi = 3.141592653589793;
+  switch (f.func) {
+    case LFG_FN_POLY: {
+      // Horner in y inside Horner in x: sum_i x^i sum_j p[4i+j] y^j
+      double s = 0.0;
+      for (int i = 3; i >= 0; --i) {
+        const double* q = f.p + 4 * i;
+        const double py = ((q[3] * y + q[2]) * y + q[1]) * y + q[0];
+        s = s * x + py;
+      }
+      return s;
+    }
+    case LFG_FN_SINSIN:
+      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * sin(f.p[3] * pi * y));
+    case LFG_FN_SINCOS:
+      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * cos(f.p[3] * pi * y));
+  }
+  return 0.0;
+}
+
+// Value of a coefficient at reference point k of cell c.
+template <bool QUAD>
+__device__ double EvalCoeff(const CoeffDev& f, int c, const int4& cn, const double2 (&v)[4], int k,
+                            const double* sw, const double* sqx, const double* sqy,
+                            const double* so1) {
+  switch (f.kind) {
+    case LFG_COEFF_ZERO: return 0.0;
+    case LFG_COEFF_CONSTANT: return f.value;
+    case LFG_COEFF_PER_CELL: return f.data[c];
+    case LFG_COEFF_NODAL_O1: {
+      double s = f.data[cn.x] * so1[k * 4 + 0];
+      s += f.data[cn.y] * so1[k * 4 + 1];
+      s += f.data[cn.z] * so1[k * 4 + 2];
+      if (QUAD) s += f.data[cn.w] * so1[k * 4 + 3];
+      return s;
+    }
+    case LFG_COEFF_ANALYTIC: {
+      const double xh = sqx[k], yh = sqy[k];
+      double X, Y;
+      if (!QUAD) {
+        const double l0 = 1.0 - xh - yh;
+        X = v[0].x * l0 + v[1].x * xh + v[2].x * yh;
+        Y = v[0].y * l0 + v[1].y * xh + v[2].y * yh;
+      } else {
+        const double b0 = (1 - xh) * (1 - yh), b1 = xh * (1 - yh), b2 = xh * yh, b3 = (1 - xh) * yh;
+        X = v[0].x * b0 + v[1].x * b1 + v[2].x * b2 + v[3].x * b3;
+        Y = v[0].y * b0 + v[1].y * b1 + v[2].y * b2 + v[3].y * b3;
+      }
+      return EvalAnalytic(f, X, Y);
+    }
+  }
+  return 0.0;
+}
+
+__device__ __forceinline__ double CellConst(const CoeffDev& f, int c) {
+  return f.kind == LFG_COEFF_CONSTANT ? f.value : f.kind == LFG_COEFF_PER_CELL ? f.data[c] : 0.0;
+}
+
+template <bool QUAD>
+__device__ __forceinline__ void LoadVerts(const AsmArgs& a, int c, int4& cn, double2 (&v)[4]) {
+  cn = a.cells[c];
+  v[0] = a.xy[cn.x];
+  v[1] = a.xy[cn.y];
+  v[2] = a.xy[cn.z];
+  v[3] = QUAD ? a.xy[cn.w] : make_double2(0.0, 0.0);
+}
+
+// |det J| * J^{-1} J^{-T} of an affine triangle: adj(J) adj(J)^T / |det J|.
+__device__ __forceinline__ void TriaMetric(const double2 (&v)[4], double& m00, double& m01,
+                                           double& m11, double& adet) {
+  const double j00 = v[1].x - v[0].x, j01 = v[2].x - v[0].x;
+  const double j10 = v[1].y - v[0].y, j11 = v[2].y - v[0].y;
+  const double det = j00 * j11 - j10 * j01;
+  adet = fabs(det);
+  const double inv = 1.0 / adet;
+  m00 = (j11 * j11 + j01 * j01) * inv;
+  m01 = -(j11 * j10 + j01 * j00) * inv;
+  m11 = (j10 * j10 + j00 * j00) * inv;
+}
+
+// Same at reference point (xh, yh) of a bilinear quadrilateral (quad_o1.cc:93-99).
+__device__ __forceinline__ void QuadMetric(const double2 (&v)[4], double xh, double yh, double& m00,
+                                           double& m01, double& m11, double& adet) {
+  const double j00 = (v[1].x - v[0].x) * (1 - yh) + (v[2].x - v[3].x) * yh;
+  const double j10 = (v[1].y - v[0].y) * (1 - yh) + (v[2].y - v[3].y) * yh;
+  const double j01 = (v[3].x - v[0].x) * (1 - xh) + (v[2].x - v[1].x) * xh;
+  const double j11 = (v[3].y - v[0].y) * (1 - xh) + (v[2].y - v[1].y) * xh;
+  const double det = j00 * j11 - j10 * j01;
+  adet = fabs(det);
+  const double inv = 1.0 / adet;
+  m00 = (j11 * j11 + j01 * j01) * inv;
+  m01 = -(j11 * j10 + j01 * j00) * inv;
+  m11 = (j10 * j10 + j00 * j00) * inv;
+}
+
+__device__ __forceinline__ void LoadTable(const double* __restrict__ g, double* s, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
+  __syncthreads();
+}
+
+// -------------------------------------------------- general (per point) path
+// One thread per cell.  Accumulators are kept in registers in chunks of at
+// most 64 upper-triangle entries; every chunk re-runs the point loop.
+template <int DEG, bool QUAD, bool VARY, bool MASS>
+__global__ void __launch_bounds__(128) RDGeneralKernel(AsmArgs a) {
+  constexpr int N = QUAD ? (DEG + 1) * (DEG + 1) : (DEG + 1) * (DEG + 2) / 2;
+  constexpr int E = N * (N + 1) / 2;
+  constexpr int CH = E < 64 ? E : 64;
+  extern __shared__ double sm[];
+  LoadTable(a.tab, sm, a.L.total);
+  const double* sw = sm + a.L.off_w;
+  const double* sqx = sm + a.L.off_qx;
+  const double* sqy = sm + a.L.off_qy;
+  const double* sT = sm + a.L.off_T;
+  const double* so1 = sm + a.L.off_o1;
+  const int nq = a.L.nq;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < a.count;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = a.bucket[t];
+    int4 cn;
+    double2 v[4];
+    LoadVerts<QUAD>(a, c, cn, v);
+    double tm00 = 0, tm01 = 0, tm11 = 0, tdet = 0;
+    if (!QUAD) TriaMetric(v, tm00, tm01, tm11, tdet);
+    double al = 0, ga = 0;
+    if (!VARY) {
+      al = CellConst(a.alpha, c);
+      ga = CellConst(a.gamma, c);
+    }
+    int dofs[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+    lfg_triplet* base = a.out + a.tri_offset[c];
+#pragma unroll
+    for (int e0 = 0; e0 < E; e0 += CH) {
+      double acc[CH];
+#pragma unroll
+      for (int e = 0; e < CH; ++e) acc[e] = 0.0;
+      for (int k = 0; k < nq; ++k) {
+        double m00, m01, m11, adet;
+        if (QUAD) QuadMetric(v, sqx[k], sqy[k], m00, m01, m11, adet);
+        else { m00 = tm00; m01 = tm01; m11 = tm11; adet = tdet; }
+        double alk = al, gak = ga;
+        if (VARY) {
+          alk = EvalCoeff<QUAD>(a.alpha, c, cn, v, k, sw, sqx, sqy, so1);
+          if (MASS) gak = EvalCoeff<QUAD>(a.gamma, c, cn, v, k, sw, sqx, sqy, so1);
+        }
+        const double s = sw[k] * alk;
+        const double c00 = s * m00, c01 = s * m01, c11 = s * m11;
+        const double mk = sw[k] * adet * gak;
+        const double* Tk = sT + k * E * 4;
+#pragma unroll
+        for (int e = 0; e < CH; ++e) {
+          if (e0 + e < E) {
+            const double* T = Tk + (e0 + e) * 4;
+            double r = acc[e];
+            r = fma(c00, T[0], r);
+            r = fma(c01, T[1], r);
+            r = fma(c11, T[2], r);
+            if (MASS) r = fma(mk, T[3], r);
+            acc[e] = r;
+          }
+        }
+      }
+      // scatter the chunk's entries to (i, j) and (j, i)
+      int e = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+#pragma unroll
+        for (int j = i; j < N; ++j, ++e) {
+          if (e >= e0 && e < e0 + CH) {
+            const double val = acc[e - e0];
+            StoreTriplet(base + i * N + j, dofs[i], dofs[j], val);
+            if (j != i) StoreTriplet(base + j * N + i, dofs[j], dofs[i], val);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------- affine triangles, cell-constant coeffs
+// A_K = alpha |det J| sum_ab M_ab R_ab + gamma |det J| R_mass, staged in shared
+// memory so that the triplets leave the SM as coalesced 16-byte stores.
+template <int DEG, bool MASS>
+__global__ void __launch_bounds__(DEG == 3 ? 64 : 128) RDTriaUniformKernel(AsmArgs a) {
+  constexpr int N = (DEG + 1) * (DEG + 2) / 2;
+  constexpr int E = N * (N + 1) / 2;
+  constexpr int TILE = DEG == 3 ? 64 : 128;
+  constexpr int NN = N * N;
+  constexpr int STRIDE = NN + 1;  // pad one triplet per cell: conflict-free staging
+  extern __shared__ double sm[];
+  double* sR = sm;
+  lfg_triplet* stage = reinterpret_cast<lfg_triplet*>(sm + ((E * 4 + 1) & ~1));
+  for (int i = threadIdx.x; i < E * 4; i += blockDim.x) sR[i] = a.tab[a.L.off_R + i];
+  __syncthreads();
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
+       t0 += static_cast<int64_t>(gridDim.x) * TILE) {
+    const int64_t t = t0 + threadIdx.x;
+    const int ncell_tile = static_cast<int>(a.count - t0 < TILE ? a.count - t0 : TILE);
+    if (threadIdx.x < ncell_tile) {
+      const int c = a.bucket[t];
+      int4 cn;
+      double2 v[4];
+      LoadVerts<false>(a, c, cn, v);
+      double m00, m01, m11, adet;
+      TriaMetric(v, m00, m01, m11, adet);
+      const double al = CellConst(a.alpha, c);
+      const double a00 = al * m00, a01 = al * m01, a11 = al * m11;
+      const double mm = MASS ? CellConst(a.gamma, c) * adet : 0.0;
+      int dofs[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      lfg_triplet* st = stage + threadIdx.x * STRIDE;
+      int e = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+#pragma unroll
+        for (int j = i; j < N; ++j, ++e) {
+          const double* R = sR + e * 4;
+          double r = a00 * R[0];
+          r = fma(a01, R[1], r);
+          r = fma(a11, R[2], r);
+          if (MASS) r = fma(mm, R[3], r);
+          StoreTriplet(st + i * N + j, dofs[i], dofs[j], r);
+          if (j != i) StoreTriplet(st + j * N + i, dofs[j], dofs[i], r);
+        }
+      }
+    }
+    __syncthreads();
+    // copy-out: each cell block is contiguous in the output
+    const int c_first = a.bucket[t0];
+    const bool contiguous = (a.bucket[t0 + ncell_tile - 1] - c_first) == ncell_tile - 1;
+    if (contiguous) {
+      lfg_triplet* dst = a.out + a.tri_offset[c_first];
+      const int total = ncell_tile * NN;
+      for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int cl = q / NN, w = q - cl * NN;
+        *reinterpret_cast<int4*>(dst + q) = *reinterpret_cast<const int4*>(stage + cl * STRIDE + w);
+      }
+    } else {
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int cl = warp; cl < ncell_tile; cl += blockDim.x >> 5) {
+        lfg_triplet* dst = a.out + a.tri_offset[a.bucket[t0 + cl]];
+        for (int w = lane; w < NN; w += 32)
+          *reinterpret_cast<int4*>(dst + w) = *reinterpret_cast<const int4*>(stage + cl * STRIDE + w);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------------- load vector
+template <int DEG, bool QUAD, bool VARY>
+__global__ void __launch_bounds__(128) LoadVectorKernel(AsmArgs a) {
+  constexpr int N = QUAD ? (DEG + 1) * (DEG + 1) : (DEG + 1) * (DEG + 2) / 2;
+  extern __shared__ double sm[];
+  LoadTable(a.tab, sm, a.L.total);
+  const double* sw = sm + a.L.off_w;
+  const double* sqx = sm + a.L.off_qx;
+  const double* sqy = sm + a.L.off_qy;
+  const double* sphi = sm + a.L.off_phi;
+  const double* sL = sm + a.L.off_L;
+  const double* so1 = sm + a.L.off_o1;
+  const int nq = a.L.nq;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < a.count;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = a.bucket[t];
+    int4 cn;
+    double2 v[4];
+    LoadVerts<QUAD>(a, c, cn, v);
+    double vec[N];
+    if (!QUAD && !VARY) {
+      double m00, m01, m11, adet;
+      TriaMetric(v, m00, m01, m11, adet);
+      const double s = CellConst(a.alpha, c) * adet;
+#pragma unroll
+      for (int i = 0; i < N; ++i) vec[i] = s * sL[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < N; ++i) vec[i] = 0.0;
+      double tdet = 0;
+      if (!QUAD) {
+        double m00, m01, m11;
+        TriaMetric(v, m00, m01, m11, tdet);
+      }
+      for (int k = 0; k < nq; ++k) {
+        double adet = tdet;
+        if (QUAD) {
+          double m00, m01, m11;
+          QuadMetric(v, sqx[k], sqy[k], m00, m01, m11, adet);
+        }
+        const double f = VARY ? EvalCoeff<QUAD>(a.alpha, c, cn, v, k, sw, sqx, sqy, so1)
+                              : CellConst(a.alpha, c);
+        const double s = sw[k] * adet * f;
+#pragma unroll
+        for (int i = 0; i < N; ++i) vec[i] = fma(s, sphi[k * N + i], vec[i]);
+      }
+    }
+    double* dst = a.vout + a.tri_offset[c];
+#pragma unroll
+    for (int i = 0; i < N; ++i) dst[i] = vec[i];
+  }
+}
+
+// b[d] += contributions in ascending cell order (AssembleVectorLocally order).
+__global__ void GatherVectorKernel(int64_t ndofs, const int64_t* __restrict__ ptr,
+                                   const uint64_t* __restrict__ slot, const double* __restrict__ ev,
+                                   double* __restrict__ b) {
+  for (int64_t d = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; d < ndofs;
+       d += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double s = b[d];
+    for (int64_t q = ptr[d]; q < ptr[d + 1]; ++q) s += ev[slot[q]];
+    b[d] = s;
+  }
+}
+
+// Tabulated providers.
+__global__ void TabulatedMatrixKernel(int64_t nc, const int4* __restrict__ cells,
+                                      const int32_t* __restrict__ cell_dofs, int n_cell, int n_tria,
+                                      int n_quad, const double* __restrict__ elem, int ld,
+                                      const int64_t* __restrict__ tri_offset, lfg_triplet* out) {
+  for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; c < nc;
+       c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int n = cells[c].w < 0 ? n_tria : n_quad;
+    const int32_t* d = cell_dofs + c * n_cell;
+    const double* em = elem + c * ld * ld;
+    lfg_triplet* o = out + tri_offset[c];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) StoreTriplet(o + i * n + j, d[i], d[j], em[i * ld + j]);
+  }
+}
+
+__global__ void TabulatedVectorKernel(int64_t nc, const int64_t* __restrict__ loc_offset,
+                                      const double* __restrict__ vec, int ld, double* ev) {
+  for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; c < nc;
+       c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t b = loc_offset[c], n = loc_offset[c + 1] - b;
+    for (int i = 0; i < n; ++i) ev[b + i] = vec[c * ld + i];
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+void BuildTable(bool quad, int degree, int rule_degree, std::vector<double>& h, Tab& L) {
+  Rule r;
+  if (!MakeRule(quad, rule_degree, r))
+    Fail(LFG_UNSUPPORTED, "no quadrature rule of degree " + std::to_string(rule_degree) +
+                              (quad ? " for quadrilaterals" : " for triangles"));
+  if (r.n > kMaxQ) Fail(LFG_UNSUPPORTED, "quadrature rule has too many points");
+  const int n = NumShape(quad, degree);
+  L = TabLayout(n, r.n);
+  h.assign(L.total, 0.0);
+  double phi[16], dphi[16][2], p1[16], d1[16][2];
+  for (int k = 0; k < r.n; ++k) {
+    h[L.off_w + k] = r.w[k];
+    h[L.off_qx + k] = r.x[k];
+    h[L.off_qy + k] = r.y[k];
+    Shape(quad, degree, r.x[k], r.y[k], phi, dphi);
+    Shape(quad, 1, r.x[k], r.y[k], p1, d1);
+    for (int i = 0; i < n; ++i) h[L.off_phi + k * n + i] = phi[i];
+    for (int i = 0; i < (quad ? 4 : 3); ++i) h[L.off_o1 + k * 4 + i] = p1[i];
+    int e = 0;
+    for (int i = 0; i < n; ++i)
+      for (int j = i; j < n; ++j, ++e) {
+        double* T = &h[L.off_T + (k * L.E + e) * 4];
+        T[0] = dphi[i][0] * dphi[j][0];
+        T[1] = dphi[i][0] * dphi[j][1] + dphi[i][1] * dphi[j][0];
+        T[2] = dphi[i][1] * dphi[j][1];
+        T[3] = phi[i] * phi[j];
+      }
+  }
+  // folded tables in long double: R = sum_k w_k T_k, L = sum_k w_k phi_k
+  for (int e = 0; e < L.E; ++e)
+    for (int q = 0; q < 4; ++q) {
+      long double s = 0.0L;
+      for (int k = 0; k < r.n; ++k)
+        s += static_cast<long double>(r.w[k]) * h[L.off_T + (k * L.E + e) * 4 + q];
+      h[L.off_R + e * 4 + q] = static_cast<double>(s);
+    }
+  for (int i = 0; i < n; ++i) {
+    long double s = 0.0L;
+    for (int k = 0; k < r.n; ++k) s += static_cast<long double>(r.w[k]) * h[L.off_phi + k * n + i];
+    h[L.off_L + i] = static_cast<double>(s);
+  }
+}
+
+const double* GetTable(lfg_space* sp, bool quad, int degree, int rule_degree, Tab& L) {
+  lfg_ctx* ctx = sp->mesh->ctx;
+  const int key = (quad ? 1 << 20 : 0) | (degree << 10) | rule_degree;
+  auto it = ctx->tables.find(key);
+  if (it != ctx->tables.end()) {
+    L = it->second.layout;
+    return it->second.buf.as<double>();
+  }
+  std::vector<double> h;
+  BuildTable(quad, degree, rule_degree, h, L);
+  TableEntry& ent = ctx->tables[key];
+  ent.layout = L;
+  ent.buf.alloc(h.size() * sizeof(double), ctx->stream);
+  LFG_CUDA(cudaMemcpyAsync(ent.buf.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ent.buf.as<double>();
+}
+
+CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
+  CoeffDev d;
+  d.kind = c.kind;
+  d.func = c.func;
+  d.value = c.value;
+  d.data = c.data_dev;
+  for (int i = 0; i < 16; ++i) d.p[i] = c.p[i];
+  if (c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_ANALYTIC)
+    Fail(LFG_UNSUPPORTED, std::string(what) + ": unsupported coefficient kind");
+  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1) && !c.data_dev)
+    Fail(LFG_INVALID_ARG, std::string(what) + ": coefficient data pointer is null");
+  if (c.kind == LFG_COEFF_ANALYTIC && (c.func < LFG_FN_POLY || c.func > LFG_FN_SINCOS))
+    Fail(LFG_UNSUPPORTED, std::string(what) + ": unknown analytic function");
+  return d;
+}
+
+bool Uniform(const lfg_coeff& c) {
+  return c.kind == LFG_COEFF_ZERO || c.kind == LFG_COEFF_CONSTANT || c.kind == LFG_COEFF_PER_CELL;
+}
+
+template <class K>
+void Launch(K kernel, lfg_ctx* ctx, int64_t count, size_t smem, const AsmArgs& a, int block = 128) {
+  if (count <= 0) return;
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  int per_sm = 0;
+  LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem));
+  if (per_sm < 1) per_sm = 1;
+  int64_t blocks = (count + block - 1) / block;
+  blocks = std::min<int64_t>(blocks, static_cast<int64_t>(ctx->num_sms) * per_sm);
+  kernel<<<static_cast<unsigned>(blocks), block, smem, ctx->stream>>>(a);
+  LFG_LAUNCHED(ctx);
+}
+
+template <int DEG, bool QUAD>
+void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, bool uniform, bool mass) {
+  const size_t smem_gen = a.L.total * sizeof(double);
+  if (!QUAD && uniform) {
+    constexpr int N = (DEG + 1) * (DEG + 2) / 2;
+    constexpr int E = N * (N + 1) / 2;
+    constexpr int TILE = DEG == 3 ? 64 : 128;
+    const size_t smem = ((E * 4 + 1) & ~1) * sizeof(double) + TILE * (N * N + 1) * sizeof(lfg_triplet);
+    ProfScope prof(ctx, "rd_tria_uniform");
+    if (mass) Launch(RDTriaUniformKernel<DEG, true>, ctx, a.count, smem, a, TILE);
+    else Launch(RDTriaUniformKernel<DEG, false>, ctx, a.count, smem, a, TILE);
+    return;
+  }
+  ProfScope prof(ctx, QUAD ? "rd_general_quad" : "rd_general_tria");
+  if (uniform) {
+    if (mass) Launch(RDGeneralKernel<DEG, QUAD, false, true>, ctx, a.count, smem_gen, a);
+    else Launch(RDGeneralKernel<DEG, QUAD, false, false>, ctx, a.count, smem_gen, a);
+  } else {
+    if (mass) Launch(RDGeneralKernel<DEG, QUAD, true, true>, ctx, a.count, smem_gen, a);
+    else Launch(RDGeneralKernel<DEG, QUAD, true, false>, ctx, a.count, smem_gen, a);
+  }
+}
+
+template <bool QUAD>
+void DispatchRD(lfg_ctx* ctx, int degree, const AsmArgs& a, bool uniform, bool mass) {
+  switch (degree) {
+    case 1: LaunchRD<1, QUAD>(ctx, a, uniform, mass); break;
+    case 2: LaunchRD<2, QUAD>(ctx, a, uniform, mass); break;
+    case 3: LaunchRD<3, QUAD>(ctx, a, uniform, mass); break;
+  }
+}
+
+template <bool QUAD>
+void DispatchLoad(lfg_ctx* ctx, int degree, const AsmArgs& a, bool vary) {
+  const size_t smem = a.L.total * sizeof(double);
+  ProfScope prof(ctx, QUAD ? "load_quad" : "load_tria");
+  switch (degree) {
+    case 1: vary ? Launch(LoadVectorKernel<1, QUAD, true>, ctx, a.count, smem, a)
+                 : Launch(LoadVectorKernel<1, QUAD, false>, ctx, a.count, smem, a); break;
+    case 2: vary ? Launch(LoadVectorKernel<2, QUAD, true>, ctx, a.count, smem, a)
+                 : Launch(LoadVectorKernel<2, QUAD, false>, ctx, a.count, smem, a); break;
+    case 3: vary ? Launch(LoadVectorKernel<3, QUAD, true>, ctx, a.count, smem, a)
+                 : Launch(LoadVectorKernel<3, QUAD, false>, ctx, a.count, smem, a); break;
+  }
+}
+
+int RuleDegree(int requested, int degree) { return requested == 0 ? 2 * degree : requested; }
+
+AsmArgs BaseArgs(lfg_space* sp) {
+  AsmArgs a{};
+  a.cells = sp->mesh->cell_nodes.as<int4>();
+  a.xy = sp->mesh->xy.as<double2>();
+  a.cell_dofs = sp->cell_dofs.as<int32_t>();
+  a.n_cell = sp->n_cell;
+  return a;
+}
+
+}  // namespace
+
+// Element vectors of the load provider into sp->scratch_vec (exposed for the
+// vector assembly and the gradient path).
+void LoadElementVectors(lfg_space* sp, const lfg_load_provider* pr, double* ev) {
+  lfg_ctx* ctx = sp->mesh->ctx;
+  lfg_mesh* m = sp->mesh;
+  const int deg = sp->degree;
+  AsmArgs a = BaseArgs(sp);
+  a.tri_offset = sp->loc_offset.as<int64_t>();
+  a.vout = ev;
+  a.alpha = ToDev(pr->f, m, "load f");
+  const bool vary = !Uniform(pr->f);
+  if (m->ntria) {
+    if (pr->qr_degree_tria < 0) Fail(LFG_MISSING_RULE, "no quadrature rule for triangles");
+    a.tab = GetTable(sp, false, deg, RuleDegree(pr->qr_degree_tria, deg), a.L);
+    a.bucket = m->tria_list.as<int32_t>();
+    a.count = m->ntria;
+    DispatchLoad<false>(ctx, deg, a, vary);
+  }
+  if (m->nquad) {
+    if (pr->qr_degree_quad < 0) Fail(LFG_MISSING_RULE, "no quadrature rule for quadrilaterals");
+    a.tab = GetTable(sp, true, deg, RuleDegree(pr->qr_degree_quad, deg), a.L);
+    a.bucket = m->quad_list.as<int32_t>();
+    a.count = m->nquad;
+    DispatchLoad<true>(ctx, deg, a, vary);
+  }
+}
+
+}  // namespace lfg
+
+using namespace lfg;
+
+extern "C" {
+
+lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!pr || !coo) Fail(LFG_INVALID_ARG, "lfg_assemble_matrix_rd: null argument");
+  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "reaction-diffusion provider needs a Lagrangian space");
+  if (coo->rows < sp->num_dofs || coo->cols < sp->num_dofs)
+    Fail(LFG_INVALID_ARG, "COO matrix smaller than the number of dofs");
+  lfg_mesh* m = sp->mesh;
+  if (m->ntria && pr->qr_degree_tria < 0)
+    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type TRIA");
+  if (m->nquad && pr->qr_degree_quad < 0)
+    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type QUAD");
+  if (coo->size + sp->num_triplets > coo->capacity)
+    Fail(LFG_CAPACITY, "COO capacity " + std::to_string(coo->capacity) + " < " +
+                           std::to_string(coo->size + sp->num_triplets));
+  AsmArgs a = BaseArgs(sp);
+  a.tri_offset = sp->tri_offset.as<int64_t>();
+  a.out = coo->d + coo->size;
+  a.alpha = ToDev(pr->alpha, m, "alpha");
+  a.gamma = ToDev(pr->gamma, m, "gamma");
+  const bool uniform = Uniform(pr->alpha) && Uniform(pr->gamma);
+  const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
+  const int deg = sp->degree;
+  if (m->ntria) {
+    a.tab = GetTable(sp, false, deg, RuleDegree(pr->qr_degree_tria, deg), a.L);
+    a.bucket = m->tria_list.as<int32_t>();
+    a.count = m->ntria;
+    DispatchRD<false>(sp->mesh->ctx, deg, a, uniform, mass);
+  }
+  if (m->nquad) {
+    a.tab = GetTable(sp, true, deg, RuleDegree(pr->qr_degree_quad, deg), a.L);
+    a.bucket = m->quad_list.as<int32_t>();
+    a.count = m->nquad;
+    DispatchRD<true>(sp->mesh->ctx, deg, a, uniform, mass);
+  }
+  coo->size += sp->num_triplets;
+  LFG_API_END
+}
+
+lfg_status lfg_assemble_vector_load(lfg_space* sp, const lfg_load_provider* pr, double* b) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!pr || !b) Fail(LFG_INVALID_ARG, "lfg_assemble_vector_load: null argument");
+  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "load provider needs a Lagrangian space");
+  lfg_ctx* ctx = sp->mesh->ctx;
+  EnsureIncidence(sp);
+  LoadElementVectors(sp, pr, sp->scratch_vec.as<double>());
+  GatherVectorKernel<<<GridFor(ctx, sp->num_dofs, 256), 256, 0, ctx->stream>>>(
+      sp->num_dofs, sp->inc_ptr.as<int64_t>(), sp->inc_slot.as<uint64_t>(), sp->scratch_vec.as<double>(), b);
+  LFG_LAUNCHED(ctx);
+  LFG_API_END
+}
+
+lfg_status lfg_assemble_matrix_tabulated(lfg_space* sp, const double* elem, int32_t ld, lfg_coo* coo) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!elem || !coo || ld < sp->n_cell) Fail(LFG_INVALID_ARG, "lfg_assemble_matrix_tabulated: bad argument");
+  if (coo->rows < sp->num_dofs || coo->cols < sp->num_dofs)
+    Fail(LFG_INVALID_ARG, "COO matrix smaller than the number of dofs");
+  if (coo->size + sp->num_triplets > coo->capacity) Fail(LFG_CAPACITY, "COO capacity too small");
+  lfg_ctx* ctx = sp->mesh->ctx;
+  TabulatedMatrixKernel<<<GridFor(ctx, sp->mesh->nc, 128), 128, 0, ctx->stream>>>(
+      sp->mesh->nc, sp->mesh->cell_nodes.as<int4>(), sp->cell_dofs.as<int32_t>(), sp->n_cell, sp->n_tria,
+      sp->n_quad, elem, ld, sp->tri_offset.as<int64_t>(), coo->d + coo->size);
+  LFG_LAUNCHED(ctx);
+  coo->size += sp->num_triplets;
+  LFG_API_END
+}
+
+lfg_status lfg_assemble_vector_tabulated(lfg_space* sp, const double* vec, int32_t ld, double* b) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!vec || !b || ld < sp->n_cell) Fail(LFG_INVALID_ARG, "lfg_assemble_vector_tabulated: bad argument");
+  lfg_ctx* ctx = sp->mesh->ctx;
+  EnsureIncidence(sp);
+  TabulatedVectorKernel<<<GridFor(ctx, sp->mesh->nc, 128), 128, 0, ctx->stream>>>(
+      sp->mesh->nc, sp->loc_offset.as<int64_t>(), vec, ld, sp->scratch_vec.as<double>());
+  LFG_LAUNCHED(ctx);
+  GatherVectorKernel<<<GridFor(ctx, sp->num_dofs, 256), 256, 0, ctx->stream>>>(
+      sp->num_dofs, sp->inc_ptr.as<int64_t>(), sp->inc_slot.as<uint64_t>(), sp->scratch_vec.as<double>(), b);
+  LFG_LAUNCHED(ctx);
+  LFG_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,178 @@
+// Internal declarations of the GB300 library behind include/lfg.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/lfg.h"
+
+namespace lfg {
+
+// Status with message: every entry point converts an exception of this type
+// into its return code and stores the message on the context.
+struct Failure {
+  lfg_status code;
+  std::string msg;
+};
+
+[[noreturn]] void Fail(lfg_status code, const std::string& msg);
+void CudaCheck(cudaError_t e, const char* what);
+#define LFG_CUDA(call) ::lfg::CudaCheck((call), #call)
+
+// Owning device buffer (stream-ordered allocation on the context stream).
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p; bytes = o.bytes; stream = o.stream;
+      o.p = nullptr; o.bytes = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void alloc(size_t n, cudaStream_t s);
+  void reset();
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace lfg
+
+namespace lfg {
+// Layout of one device table block (reference-element data for one cell type,
+// degree and quadrature rule); offsets are in doubles.
+struct Tab {
+  int n, nq, E;
+  int off_w, off_qx, off_qy, off_phi, off_T, off_R, off_L, off_o1, total;
+};
+struct TableEntry {
+  Tab layout;
+  DevBuf buf;
+};
+}  // namespace lfg
+
+struct lfg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  std::string last_error;
+  int64_t launches = 0;
+  int num_sms = 0;
+  lfg::DevBuf flush;   // L2 flush buffer
+  lfg::DevBuf status;  // device error word(s)
+  // pinned host mirror of small device results
+  void* pinned_small = nullptr;
+  // reference-element tables keyed by (cell type, degree, rule degree)
+  std::map<int, lfg::TableEntry> tables;
+  // per-kernel-family event timing (lfg_profile_*)
+  bool profiling = false;
+  struct ProfRec {
+    std::string family;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof_pending;
+  std::map<std::string, std::pair<double, int64_t>> prof_totals;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+namespace lfg {
+// Brackets the launches inside its lifetime with events on the context stream
+// when profiling is enabled.
+struct ProfScope {
+  lfg_ctx* ctx;
+  size_t idx = static_cast<size_t>(-1);
+  ProfScope(lfg_ctx* c, const char* family);
+  ~ProfScope();
+};
+}  // namespace lfg
+
+struct lfg_mesh {
+  lfg_ctx* ctx = nullptr;
+  int64_t nv = 0, ne = 0, nc = 0, ntria = 0, nquad = 0;
+  lfg::DevBuf xy;          // double2[nv]
+  lfg::DevBuf cell_nodes;  // int4[nc]  (w = -1 for a triangle)
+  lfg::DevBuf cell_edges;  // int4[nc]
+  lfg::DevBuf cell_ori;    // uint8[nc]: bit j set = local edge j negatively oriented
+  lfg::DevBuf edge_nodes;  // int2[ne]
+  lfg::DevBuf edge_ncell;  // int32[ne]
+  lfg::DevBuf tria_list;   // int32[ntria]: cell indices of triangles (ascending)
+  lfg::DevBuf quad_list;   // int32[nquad]
+};
+
+struct lfg_space {
+  lfg_mesh* mesh = nullptr;
+  int degree = 0;  // 0 = generic layout
+  int np = 0, ns = 0, nt = 0, nq = 0;
+  int n_tria = 0, n_quad = 0, n_cell = 0, n_edge = 0;
+  int64_t num_dofs = 0;
+  int64_t num_triplets = 0;   // sum_K n_K^2
+  int64_t num_local = 0;      // sum_K n_K
+  lfg::DevBuf cell_dofs;      // int32[nc * n_cell]
+  lfg::DevBuf tri_offset;     // int64[nc + 1]: prefix of n_K^2 (hybrid meshes)
+  lfg::DevBuf loc_offset;     // int64[nc + 1]: prefix of n_K
+  // dof -> (cell, local) incidence sorted by (dof, cell): deterministic
+  // AssembleVectorLocally as a per-dof ordered gather.
+  lfg::DevBuf inc_ptr;        // int64[num_dofs + 1]
+  lfg::DevBuf inc_slot;       // int64[sum_K n_K]: loc_offset[cell] + local
+  lfg::DevBuf scratch_vec;    // double[sum_K n_K] element vectors
+};
+
+struct lfg_coo {
+  lfg_ctx* ctx = nullptr;
+  int64_t rows = 0, cols = 0, capacity = 0, size = 0;
+  lfg_triplet* d = nullptr;
+  lfg::DevBuf owned;
+};
+
+struct lfg_csr {
+  lfg_ctx* ctx = nullptr;
+  int64_t rows = 0, cols = 0, nnz = 0;
+  lfg::DevBuf rowptr;  // int64[rows + 1]
+  lfg::DevBuf col;     // int32[nnz]
+  lfg::DevBuf val;     // double[nnz]
+  lfg::DevBuf val32;   // float[nnz] (mixed-precision solve, built lazily)
+  lfg::DevBuf rowptr32;  // int32[rows + 1] when nnz < 2^31 (SpMV)
+  lfg::DevBuf dinv;    // double[rows] Jacobi
+  lfg::DevBuf dinv32;  // float[rows]
+};
+
+namespace lfg {
+
+// Grid-size helper: multiples of the SM count for grid-stride kernels.
+int GridFor(lfg_ctx* ctx, int64_t n, int block, int per_thread = 1);
+void CountLaunch(lfg_ctx* ctx, int n = 1);
+
+// ---- device primitives (lfg_primitives.cu) ----
+// Exclusive scan of int64 values (in-place allowed).  Returns the total.
+int64_t ExclusiveScanI64(lfg_ctx* ctx, const int64_t* in, int64_t* out, int64_t n);
+// Stable LSD radix sort of (uint64 key, uint32 value) pairs on the low `bits`
+// bits of the key.  keys/vals are overwritten with the sorted sequence.
+void RadixSortPairs(lfg_ctx* ctx, uint64_t* keys, uint32_t* vals, int64_t n, int bits);
+// Same with 64-bit payloads.
+void RadixSortPairs64(lfg_ctx* ctx, uint64_t* keys, uint64_t* vals, int64_t n, int bits);
+// Read a device int32 error word written by kernels (0 = ok); resets it.
+int32_t ReadAndClearStatus(lfg_ctx* ctx, int32_t* detail = nullptr);
+int32_t* StatusWord(lfg_ctx* ctx);
+// Copy a small device value to the host synchronously (stream ordered).
+void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
+
+// ---- quadrature / reference elements (lfg_tables.cc) ----
+struct Rule {
+  int n = 0;
+  std::vector<double> x, y, w;
+};
+bool MakeRule(bool is_quad, int degree, Rule& out);  // false if not tabulated
+int NumShape(bool is_quad, int degree);
+void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]);
+
+}  // namespace lfg

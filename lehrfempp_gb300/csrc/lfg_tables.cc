@@ -1,0 +1,172 @@
+// Host-side reference-element data: quadrature rules and Lagrangian shape
+// functions, tabulated once per (cell type, degree, rule) and shipped to the
+// device.  Only these tables reach the GPU (lf::quad and the reference finite
+// elements are set-up work in the reference too:
+// uscalfe/precomputed_scalar_reference_finite_element.h:43-184).
+#include <cmath>
+
+#include "lfg_internal.h"
+
+namespace lfg {
+namespace {
+#include "tria_rules.inc"
+
+// Gauss-Legendre on [0,1] by Newton iteration on the Legendre recurrence
+// (the algorithm of quad/gauss_quadrature.cc:16-69), in long double.
+void GaussLegendre01(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    long double z = std::cos(pi * (i + 0.75L) / (n + 0.5L)), zprev, dp;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1.0L, p1 = 0.0L;
+      for (int j = 0; j < n; ++j) {
+        const long double pm = p1;
+        p1 = p0;
+        p0 = ((2.0L * j + 1.0L) * z * p1 - j * pm) / (j + 1.0L);
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0L);
+      zprev = z;
+      z = zprev - p0 / dp;
+      if (std::fabs(z - zprev) <= 1e-17L) break;
+    }
+    x[i] = static_cast<double>(0.5L * (1.0L - z));
+    x[n - 1 - i] = static_cast<double>(0.5L * (1.0L + z));
+    w[i] = w[n - 1 - i] = static_cast<double>(1.0L / ((1.0L - z * z) * dp * dp));
+  }
+}
+
+// 1D Lagrange basis of degree p on the nodes used by the reference's segment
+// elements: O1 {0,1}; O2 {0,1,1/2}; O3 {0,1,1/3,2/3} (lagr_fe.h:284,563,1155).
+void Seg(int p, double t, double* b, double* db) {
+  if (p == 1) {
+    b[0] = 1.0 - t; b[1] = t;
+    db[0] = -1.0;   db[1] = 1.0;
+  } else if (p == 2) {
+    b[0] = 2.0 * (1.0 - t) * (0.5 - t);
+    b[1] = 2.0 * t * (t - 0.5);
+    b[2] = 4.0 * (1.0 - t) * t;
+    db[0] = 4.0 * t - 3.0;
+    db[1] = 4.0 * t - 1.0;
+    db[2] = 4.0 - 8.0 * t;
+  } else {
+    const double a = 1.0 / 3.0, c = 2.0 / 3.0;
+    b[0] = 4.5 * (1.0 - t) * (a - t) * (c - t);
+    b[1] = 4.5 * t * (t - a) * (t - c);
+    b[2] = 13.5 * t * (1.0 - t) * (c - t);
+    b[3] = 13.5 * t * (1.0 - t) * (t - a);
+    db[0] = -13.5 * t * t + 18.0 * t - 5.5;
+    db[1] = 13.5 * t * t - 9.0 * t + 1.0;
+    db[2] = 40.5 * t * t - 45.0 * t + 9.0;
+    db[3] = -40.5 * t * t + 36.0 * t - 4.5;
+  }
+}
+
+// Local numbering of the tensor-product quad elements: vertices, then per
+// edge its interior nodes in edge direction, then interior nodes
+// (lagr_fe.h:914-925, 1462-1480).  Entry = (1D index in x, 1D index in y).
+const int kQuadO1[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+const int kQuadO2[9][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0}, {1, 2}, {2, 1}, {0, 2}, {2, 2}};
+const int kQuadO3[16][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0}, {3, 0}, {1, 2}, {1, 3},
+                            {3, 1}, {2, 1}, {0, 3}, {0, 2}, {2, 2}, {3, 2}, {3, 3}, {2, 3}};
+
+}  // namespace
+
+bool MakeRule(bool is_quad, int degree, Rule& r) {
+  r = Rule();
+  if (degree < 1) return false;
+  if (is_quad) {
+    const int m = degree / 2 + 1;  // make_quad_rule.cc:28
+    std::vector<double> x, w;
+    GaussLegendre01(m, x, w);
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b) {
+        r.x.push_back(x[a]);
+        r.y.push_back(x[b]);
+        r.w.push_back(w[a] * w[b]);
+      }
+  } else {
+    const int d = degree == 3 ? 4 : degree;
+    if (d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0) return false;
+    for (int k = 0; k < kTriaRuleIndex[d][0]; ++k) {
+      const double* row = kTriaRuleRows[kTriaRuleIndex[d][1] + k];
+      r.x.push_back(row[0]);
+      r.y.push_back(row[1]);
+      r.w.push_back(row[2]);
+    }
+  }
+  r.n = static_cast<int>(r.w.size());
+  return true;
+}
+
+int NumShape(bool is_quad, int degree) {
+  return is_quad ? (degree + 1) * (degree + 1) : (degree + 1) * (degree + 2) / 2;
+}
+
+void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]) {
+  if (is_quad) {
+    double bx[4], dbx[4], by[4], dby[4];
+    Seg(degree, x, bx, dbx);
+    Seg(degree, y, by, dby);
+    const int(*map)[2] = degree == 1 ? kQuadO1 : degree == 2 ? kQuadO2 : kQuadO3;
+    for (int i = 0; i < NumShape(true, degree); ++i) {
+      const int a = map[i][0], b = map[i][1];
+      phi[i] = bx[a] * by[b];
+      dphi[i][0] = dbx[a] * by[b];
+      dphi[i][1] = bx[a] * dby[b];
+    }
+    return;
+  }
+  // Triangles in barycentric coordinates l0 = 1-x-y, l1 = x, l2 = y with
+  // d l0 = (-1,-1), d l1 = (1,0), d l2 = (0,1).
+  const double l[3] = {1.0 - x - y, x, y};
+  const double dl[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+  if (degree == 1) {
+    for (int i = 0; i < 3; ++i) {
+      phi[i] = l[i];
+      dphi[i][0] = dl[i][0];
+      dphi[i][1] = dl[i][1];
+    }
+    return;
+  }
+  if (degree == 2) {
+    // vertices: l(2l-1); edge midpoints of (0,1), (1,2), (2,0): 4 la lb
+    for (int i = 0; i < 3; ++i) {
+      phi[i] = l[i] * (2.0 * l[i] - 1.0);
+      for (int d = 0; d < 2; ++d) dphi[i][d] = (4.0 * l[i] - 1.0) * dl[i][d];
+    }
+    const int e[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    for (int k = 0; k < 3; ++k) {
+      const int a = e[k][0], b = e[k][1];
+      phi[3 + k] = 4.0 * l[a] * l[b];
+      for (int d = 0; d < 2; ++d) dphi[3 + k][d] = 4.0 * (dl[a][d] * l[b] + l[a] * dl[b][d]);
+    }
+    return;
+  }
+  // degree 3: vertices 9/2 l(l-1/3)(l-2/3); edge (a,b) nodes at 1/3 and 2/3
+  // from a: 27/2 la lb (la-1/3) then 27/2 la lb (lb-1/3); bubble 27 l0 l1 l2.
+  const double t = 1.0 / 3.0, tt = 2.0 / 3.0;
+  for (int i = 0; i < 3; ++i) {
+    phi[i] = 4.5 * l[i] * (l[i] - t) * (l[i] - tt);
+    const double dv = 4.5 * ((l[i] - t) * (l[i] - tt) + l[i] * (l[i] - tt) + l[i] * (l[i] - t));
+    for (int d = 0; d < 2; ++d) dphi[i][d] = dv * dl[i][d];
+  }
+  const int e[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  for (int k = 0; k < 3; ++k) {
+    const int a = e[k][0], b = e[k][1];
+    phi[3 + 2 * k] = 13.5 * l[a] * l[b] * (l[a] - t);
+    phi[4 + 2 * k] = 13.5 * l[a] * l[b] * (l[b] - t);
+    for (int d = 0; d < 2; ++d) {
+      dphi[3 + 2 * k][d] = 13.5 * (dl[a][d] * l[b] * (l[a] - t) + l[a] * dl[b][d] * (l[a] - t) +
+                                   l[a] * l[b] * dl[a][d]);
+      dphi[4 + 2 * k][d] = 13.5 * (dl[a][d] * l[b] * (l[b] - t) + l[a] * dl[b][d] * (l[b] - t) +
+                                   l[a] * l[b] * dl[b][d]);
+    }
+  }
+  phi[9] = 27.0 * l[0] * l[1] * l[2];
+  for (int d = 0; d < 2; ++d)
+    dphi[9][d] = 27.0 * (dl[0][d] * l[1] * l[2] + l[0] * dl[1][d] * l[2] + l[0] * l[1] * dl[2][d]);
+}
+
+}  // namespace lfg

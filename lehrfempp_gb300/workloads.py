@@ -1,0 +1,150 @@
+"""Seeded synthetic inputs for the five measured configurations.
+
+Each builder returns a plain description (numpy arrays + coefficient specs)
+that both the GPU library and the oracle consume, so the two sides see the
+same mesh, numbering input and coefficients.  Sizes are parameters: tests use
+small instances of the same generators, the benchmark the full ones.
+
+Coefficient spec: ("zero",) | ("const", v) | ("cell", array) | ("nodal", array)
+                  | ("poly", p16) | ("sinsin", p0, p1, p2, p3) | ("sincos", ...)
+"""
+import numpy as np
+
+
+def poly(**terms):
+    """16 coefficients p[4i+j] of sum c_ij x^i y^j; keys c, x1, y2, x1y1, ..."""
+    p = np.zeros(16)
+    for k, val in terms.items():
+        if k == "c":
+            p[0] += val
+            continue
+        i = int(k[1]) if k.startswith("x") else 0
+        j = int(k[k.index("y") + 1]) if "y" in k else 0
+        p[4 * i + j] += val
+    return p
+
+
+def tp_triag_spec(n):
+    return {"kind": "tptriag", "nx": n, "ny": n}
+
+
+def config1(n=64):
+    """Plain method: 64x64 TPTriag, O1, alpha = 1+x^2+y^2, gamma = 1,
+    f = sin(pi x) sin(pi y), degree-4 rules, homogeneous Dirichlet."""
+    return {
+        "name": "c1_tptriag%d_o1" % n, "mesh": tp_triag_spec(n), "degree": 1,
+        "alpha": ("poly", poly(c=1.0, x2=1.0, y2=1.0)), "gamma": ("const", 1.0),
+        "f": ("sinsin", 0.0, 1.0, 1.0, 1.0), "qr_tria": 4, "qr_quad": 4, "dirichlet": 0.0,
+    }
+
+
+def hybrid_mesh(n, seed=2, p_quad=0.5, jitter=0.2):
+    """n x n squares on [0,1]^2; each square is a quadrilateral or split into
+    the two triangles of the TPTriag pattern with probability 1/2; interior
+    nodes jittered by U(-jitter h, jitter h) per coordinate.  Cells are listed
+    square by square (j outer, i inner); only cells are given to the factory,
+    so edges are numbered in (min, max) node order."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / n
+    i = np.arange(n + 1)
+    X, Y = np.meshgrid(i * h, i * h)  # [j, i]
+    xy = np.stack([X.ravel(), Y.ravel()], axis=1)
+    inner = np.zeros((n + 1, n + 1), bool)
+    inner[1:-1, 1:-1] = True
+    inner = inner.ravel()
+    d = rng.uniform(-jitter * h, jitter * h, size=(inner.sum(), 2))
+    xy[inner] += d
+    is_quad = rng.random(n * n) < p_quad
+    jj, ii = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    ii, jj = ii.ravel(), jj.ravel()
+    v00 = ii + jj * (n + 1)
+    v10 = v00 + 1
+    v01 = v00 + (n + 1)
+    v11 = v01 + 1
+    quad = np.stack([v00, v10, v11, v01], 1)
+    tri_up = np.stack([v00, v11, v01, np.full_like(v00, -1)], 1)
+    tri_lo = np.stack([v00, v10, v11, np.full_like(v00, -1)], 1)
+    # square s contributes [quad] or [up triangle, low triangle]
+    count = np.where(is_quad, 1, 2)
+    starts = np.concatenate([[0], np.cumsum(count)[:-1]])
+    out = np.empty((int(count.sum()), 4), np.int64)
+    out[starts] = np.where(is_quad[:, None], quad, tri_up)
+    out[starts[~is_quad] + 1] = tri_lo[~is_quad]
+    return xy, out
+
+
+def config2(n=2048, seed=2):
+    """Large hybrid mesh, precision form: O2, alpha per-cell LogNormal(0, 1),
+    gamma = 0, f = 1, default rules (degree 4), homogeneous Dirichlet."""
+    xy, cells = hybrid_mesh(n, seed=seed)
+    rng = np.random.default_rng(seed + 1000)
+    alpha = np.exp(rng.standard_normal(len(cells)))
+    return {
+        "name": "c2_hybrid%d_o2" % n, "mesh": {"kind": "factory", "xy": xy, "cells": cells, "edges": None},
+        "degree": 2, "alpha": ("cell", alpha), "gamma": ("zero",), "f": ("const", 1.0),
+        "qr_tria": 0, "qr_quad": 0, "dirichlet": 0.0,
+    }
+
+
+def config3(n=1024, seed=3):
+    """High order: TPTriag n x n, O3, degree-6 rules, alpha = 1 + 0.5 sin(4 pi x)
+    cos(4 pi y), gamma = 1, f = O1 interpolant of i.i.d. N(0,1) nodal values."""
+    rng = np.random.default_rng(seed)
+    fn = rng.standard_normal((n + 1) * (n + 1))
+    return {
+        "name": "c3_tptriag%d_o3" % n, "mesh": tp_triag_spec(n), "degree": 3,
+        "alpha": ("sincos", 1.0, 0.5, 4.0, 4.0), "gamma": ("const", 1.0), "f": ("nodal", fn),
+        "qr_tria": 6, "qr_quad": 6, "dirichlet": 0.0,
+    }
+
+
+def config5(n=1024, seed=5):
+    """Differentiation form: TPTriag n x n, O1, alpha = exp(theta) per cell,
+    theta ~ N(0, 0.5^2), gamma = 0, f = 1, Dirichlet 0."""
+    rng = np.random.default_rng(seed)
+    theta = 0.5 * rng.standard_normal(2 * n * n)
+    return {
+        "name": "c5_tptriag%d_o1" % n, "mesh": tp_triag_spec(n), "degree": 1,
+        "alpha": ("cell", np.exp(theta)), "gamma": ("zero",), "f": ("const", 1.0),
+        "qr_tria": 0, "qr_quad": 0, "dirichlet": 0.0, "theta": theta,
+    }
+
+
+def batch_sizes(count=512, lo=24, hi=320, seed=4):
+    """Config 4: mesh sizes n ~ round(exp(U(ln lo, ln hi))) and degrees 1|2."""
+    rng = np.random.default_rng(seed)
+    ns = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(int)
+    degs = np.where(rng.random(count) < 0.5, 1, 2)
+    return ns, degs
+
+
+# ------------------------------------------------------------- GPU helpers
+
+def build_mesh(ctx, spec):
+    import lehrfempp_gb300 as L
+    if spec["kind"] == "tptriag":
+        return L.Mesh.tp_triag(ctx, spec["nx"], spec["ny"])
+    if spec["kind"] == "tpquad":
+        return L.Mesh.tp_quad(ctx, spec["nx"], spec["ny"])
+    return L.Mesh.from_factory(ctx, spec["xy"], spec["cells"], spec.get("edges"))
+
+
+def to_coeff(ctx, spec, keep):
+    """lfg_coeff for a spec; device arrays are appended to `keep`."""
+    import lehrfempp_gb300 as L
+    k = spec[0]
+    if k == "zero":
+        return L.coeff(L.ZERO)
+    if k == "const":
+        return L.coeff(L.CONSTANT, spec[1])
+    if k in ("cell", "nodal"):
+        d = ctx.to_device(np.asarray(spec[1], np.float64))
+        keep.append(d)
+        return L.coeff(L.PER_CELL if k == "cell" else L.NODAL_O1, data=d)
+    if k == "poly":
+        return L.coeff(L.ANALYTIC, func=L.FN_POLY, params=list(spec[1]))
+    if k == "sinsin":
+        return L.coeff(L.ANALYTIC, func=L.FN_SINSIN, params=list(spec[1:]))
+    if k == "sincos":
+        return L.coeff(L.ANALYTIC, func=L.FN_SINCOS, params=list(spec[1:]))
+    raise ValueError(spec)

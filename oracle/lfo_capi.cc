@@ -2,7 +2,9 @@
 // test-suite can drive the restatement through ctypes.  Every call returns 0
 // on success; on failure it returns -1 and copies the message into err.
 #include <cstring>
+#include <chrono>
 #include <memory>
+#include <thread>
 
 #include "lfo.h"
 
@@ -215,6 +217,64 @@ int lfo_assemble_rd(void* sp, const lfo_coeff* alpha, const lfo_coeff* gamma, in
       for (int j = 0; j < n; ++j) A->AddToEntry(dofs[i], dofs[j], em[i * n + j]);
   }
   *out = A.release();
+  LFO_CATCH
+}
+
+// The same cell loop split into contiguous cell ranges over `nthreads`
+// std::threads, each writing its cells' triplets at their final positions, so
+// the result equals the serial COO.  Used to time the CPU path with all host
+// cores; returns wall seconds of the assembly (provider set-up excluded).
+int lfo_assemble_rd_parallel(void* sp, const lfo_coeff* alpha, const lfo_coeff* gamma,
+                             int qdeg_tria, int qdeg_quad, int64_t first_cell, int64_t last_cell,
+                             int nthreads, double* seconds, int64_t* ntriplets, char* err,
+                             int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  RDProvider p;
+  p.mesh = &m;
+  p.degree = s->degree;
+  p.alpha = ToMF(alpha, alpha && alpha->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  p.gamma = ToMF(gamma, gamma && gamma->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  p.qr_tria = MakeQuadRule(false, qdeg_tria > 0 ? qdeg_tria : 2 * s->degree);
+  p.qr_quad = MakeQuadRule(true, qdeg_quad > 0 ? qdeg_quad : 2 * s->degree);
+  p.have_tria = p.have_quad = true;
+  p.Init();
+  if (last_cell < 0) last_cell = m.num_cells;
+  std::vector<int64_t> off(last_cell - first_cell + 1, 0);
+  for (idx_t c = first_cell; c < last_cell; ++c) {
+    const int n = s->dh.NumLocalDofs(c);
+    off[c - first_cell + 1] = off[c - first_cell] + n * n;
+  }
+  std::vector<Triplet> out(off.back());
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> pool;
+  std::vector<std::string> errors(nthreads);
+  const idx_t total = last_cell - first_cell;
+  for (int t = 0; t < nthreads; ++t) {
+    pool.emplace_back([&, t]() {
+      try {
+        std::vector<double> em;
+        const idx_t lo = first_cell + total * t / nthreads, hi = first_cell + total * (t + 1) / nthreads;
+        for (idx_t c = lo; c < hi; ++c) {
+          const int n = s->dh.NumLocalDofs(c);
+          const idx_t* dofs = s->dh.GlobalDofIndices(c);
+          p.Eval(c, em);
+          Triplet* o = &out[off[c - first_cell]];
+          for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+              o[i * n + j] = {static_cast<int32_t>(dofs[i]), static_cast<int32_t>(dofs[j]), em[i * n + j]};
+        }
+      } catch (const std::exception& e) {
+        errors[t] = e.what();
+      }
+    });
+  }
+  for (auto& th : pool) th.join();
+  for (auto& e : errors)
+    if (!e.empty()) throw Error(e);
+  *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  *ntriplets = static_cast<int64_t>(out.size());
   LFO_CATCH
 }
 

@@ -320,3 +320,20 @@ def kat_tensor_rd():
     err = _err()
     _check(lib().lfo_kat_tensor_rd(C.byref(v), err, 512), err)
     return v.value
+
+
+def assemble_rd_parallel(space, alpha, gamma, qdeg_tria=0, qdeg_quad=0, cells=(0, -1), threads=1):
+    """Threaded cell-range assembly (same triplets as assemble_rd); returns
+    (wall seconds, number of triplets)."""
+    L = lib()
+    if not hasattr(L, "_par_declared"):
+        L.lfo_assemble_rd_parallel.argtypes = [C.c_void_p, C.POINTER(lfo_coeff), C.POINTER(lfo_coeff), C.c_int,
+                                               C.c_int, C.c_int64, C.c_int64, C.c_int, C.POINTER(C.c_double),
+                                               C.POINTER(C.c_int64), C.c_char_p, C.c_int]
+        L._par_declared = True
+    sec = C.c_double()
+    n = C.c_int64()
+    err = _err()
+    _check(L.lfo_assemble_rd_parallel(space.h, C.byref(alpha), C.byref(gamma), qdeg_tria, qdeg_quad, cells[0],
+                                      cells[1], threads, C.byref(sec), C.byref(n), err, 512), err)
+    return sec.value, n.value

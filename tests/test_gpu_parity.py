@@ -1,0 +1,346 @@
+"""Parity of the sm_103a path with the oracle, through the C-ABI (GPU only).
+
+Indices and triplet order must be bit-exact; values within 1e-12 of the
+element matrix scale (max |A_K|); solutions within 1e-8 relative of the FP64
+direct solve.
+"""
+import numpy as np
+import pytest
+
+from helpers import cell_index_matrices, dense, edge_dof_assembler_matrices
+from parity import VALUE_RTOL, O, L, W, Run, block_sizes, compare_triplets, oracle_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _topology_equal(gm, om):
+    en, ce, co, nc = gm.topology()
+    oen, oce, oco, onc = om.topology()
+    assert (gm.num_nodes, gm.num_edges, gm.num_cells) == (om.num_nodes, om.num_edges, om.num_cells)
+    assert np.array_equal(en, oen)
+    assert np.array_equal(ce, oce)
+    assert np.array_equal(co, oco)
+    assert np.array_equal(nc, onc)
+
+
+@pytest.mark.parametrize("spec", [
+    {"kind": "tptriag", "nx": 5, "ny": 3},
+    {"kind": "tpquad", "nx": 4, "ny": 6},
+    "test0", "hybrid",
+])
+def test_mesh_numbering(ctx, spec):
+    if spec == "test0":
+        xy, cells, _ = O.factory_input("test0", x0=1.0)
+        spec = {"kind": "factory", "xy": xy, "cells": cells, "edges": None}
+    elif spec == "hybrid":
+        xy, cells = W.hybrid_mesh(12, seed=7)
+        spec = {"kind": "factory", "xy": xy, "cells": cells, "edges": None}
+    gm = W.build_mesh(ctx, spec)
+    om = oracle_mesh(spec)
+    _topology_equal(gm, om)
+    nf, ef = gm.boundary_flags()
+    onf, oef = om.boundary_flags()
+    assert np.array_equal(nf, onf) and np.array_equal(ef, oef)
+
+
+def test_factory_with_preset_edges(ctx):
+    """Preset edges keep their registration index; the rest follow in (min,max) order."""
+    xy, cells, pe = O.factory_input("tptriag", 4, 3)
+    sel = pe[::3]  # register a third of the edges, in reversed direction
+    sel = sel[:, ::-1].copy()
+    om = O.Mesh(xy, cells, sel)
+    gm = L.Mesh.from_factory(ctx, xy, cells, sel)
+    _topology_equal(gm, om)
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3])
+@pytest.mark.parametrize("which", ["tptriag", "tpquad", "hybrid"])
+def test_dof_numbering(ctx, degree, which):
+    if which == "hybrid":
+        xy, cells = W.hybrid_mesh(9, seed=11)
+        spec = {"kind": "factory", "xy": xy, "cells": cells, "edges": None}
+    else:
+        spec = {"kind": which, "nx": 4, "ny": 3}
+    gs = L.Space.lagrange(W.build_mesh(ctx, spec), degree)
+    os_ = O.Space(oracle_mesh(spec), degree)
+    assert gs.num_dofs == os_.num_dofs
+    assert np.array_equal(gs.cell_dofs(), os_.cell_dofs())
+    cod, idx = gs.dof_entities()
+    ocod, oidx = os_.dof_entities()
+    assert np.array_equal(cod, ocod) and np.array_equal(idx, oidx)
+    assert np.array_equal(gs.boundary_dof_flags().download(), os_.boundary_dof_flags())
+
+
+def test_golden_ref10(ctx, goldens):
+    """The 10x10 golden of lf_assembly.mat_assembly_test through the GPU path."""
+    ref = np.array(goldens["mat_assembly_test_ref10"]["matrix"])
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    m = L.Mesh.from_factory(ctx, xy, cells)
+    s = L.Space.layout(m, 1, 0, 0, 0)
+    e, v = cell_index_matrices(m.num_cells)
+    coo = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, s.num_triplets)
+    L.assemble_matrix_tabulated(s, ctx.to_device(e), 4, coo)
+    t = coo.triplets()
+    cod, ent = s.dof_entities()
+    assert np.array_equal(dense(10, 10, t["row"], t["col"], t["value"]), ref[np.ix_(ent, ent)])
+    b = ctx.zeros(s.num_dofs)
+    L.assemble_vector_tabulated(s, ctx.to_device(v), 4, b)
+    assert np.array_equal(b.download(), np.diag(ref)[ent])
+    # makeSparse on the device gives the same matrix
+    assert np.array_equal(coo.make_sparse().to_scipy().toarray(), ref[np.ix_(ent, ent)])
+
+
+def test_golden_ref36(ctx, goldens):
+    """The 36x36 golden of lf_assembly.edge_dof_static (two dofs per edge)."""
+    ref = np.array(goldens["edge_dof_static_ref36"]["matrix"])
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    m = L.Mesh.from_factory(ctx, xy, cells)
+    s = L.Space.layout(m, 0, 2, 0, 0)
+    coo = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, s.num_triplets)
+    L.assemble_matrix_tabulated(s, ctx.to_device(edge_dof_assembler_matrices(m.num_cells)), 8, coo)
+    t = coo.triplets()
+    assert np.array_equal(dense(36, 36, t["row"], t["col"], t["value"]), ref)
+
+
+WORKLOADS = {
+    "c1": lambda: W.config1(64),
+    "c2": lambda: W.config2(24),
+    "c3": lambda: W.config3(12),
+    "c5": lambda: W.config5(16),
+}
+
+
+@pytest.mark.parametrize("name", sorted(WORKLOADS))
+def test_matrix_parity(ctx, name):
+    r = Run(ctx, WORKLOADS[name]())
+    coo = r.gpu_matrix()
+    ro, co, vo = r.oracle_matrix().arrays()
+    compare_triplets(coo.triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
+
+
+@pytest.mark.parametrize("name", sorted(WORKLOADS))
+def test_vector_parity(ctx, name):
+    r = Run(ctx, WORKLOADS[name]())
+    b = r.gpu_vector().download()
+    bo = r.oracle_vector()
+    scale = np.abs(bo).max()
+    assert np.abs(b - bo).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("degree,quad", [(1, True), (2, False), (3, True), (3, False), (2, True)])
+@pytest.mark.parametrize("coef", ["uniform", "varying"])
+def test_matrix_parity_all_elements(ctx, degree, quad, coef):
+    spec = {"kind": "tpquad" if quad else "tptriag", "nx": 5, "ny": 4}
+    if coef == "uniform":
+        alpha, gamma = ("const", 1.7), ("const", 0.3)
+    else:
+        alpha, gamma = ("poly", W.poly(c=1.0, x1y1=2.0, y2=1.0)), ("sincos", 1.0, 0.25, 2.0, 1.0)
+    wl = {"mesh": spec, "degree": degree, "alpha": alpha, "gamma": gamma, "f": ("poly", W.poly(c=1.0, x1=1.0)),
+          "qr_tria": 0, "qr_quad": 0}
+    r = Run(ctx, wl)
+    ro, co, vo = r.oracle_matrix().arrays()
+    compare_triplets(r.gpu_matrix().triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
+    b = r.gpu_vector().download()
+    bo = r.oracle_vector()
+    assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
+
+
+def test_append_semantics(ctx):
+    """AssembleMatrixLocally appends to the triplets already in the matrix."""
+    r = Run(ctx, W.config1(8))
+    coo = L.COOMatrix(ctx, r.space.num_dofs, r.space.num_dofs, 2 * r.space.num_triplets)
+    p = L.rd_provider(W.to_coeff(ctx, r.wl["alpha"], r.keep), W.to_coeff(ctx, r.wl["gamma"], r.keep), 4, 4)
+    L.assemble_matrix_rd(r.space, p, coo)
+    L.assemble_matrix_rd(r.space, p, coo)
+    t = coo.triplets()
+    n = r.space.num_triplets
+    assert len(t) == 2 * n and np.array_equal(t[:n], t[n:])
+
+
+def test_fix_and_csr_parity(ctx):
+    r = Run(ctx, W.config2(16))
+    coo = r.gpu_matrix()
+    b = r.gpu_vector()
+    flags = r.space.boundary_dof_flags()
+    vals_h = np.linspace(-1, 1, r.space.num_dofs)  # non-homogeneous to exercise b -= A xhat
+    vals = ctx.to_device(vals_h)
+    coo.fix_flagged_solution_components(flags, vals, b)
+    A = r.oracle_matrix()
+    bo = r.oracle_vector()
+    oflags = r.ospace.boundary_dof_flags()
+    assert np.array_equal(flags.download(), oflags)
+    A.fix_flagged(oflags, vals_h, bo)
+    ro, co, vo = A.arrays()
+    t = coo.triplets()
+    assert np.array_equal(t["row"], ro) and np.array_equal(t["col"], co)
+    assert np.abs(t["value"] - vo).max() <= VALUE_RTOL * np.abs(vo).max()
+    bg = b.download()
+    assert np.abs(bg - bo).max() <= 1e-12 * np.abs(bo).max()
+    # makeSparse
+    csr = coo.make_sparse()
+    rp, col, val = csr.download()
+    orp, ocol, oval = A.to_csr()
+    assert np.array_equal(rp, orp) and np.array_equal(col, ocol)
+    assert np.abs(val - oval).max() <= VALUE_RTOL * np.abs(oval).max()
+
+
+def test_fix_alt_parity(ctx):
+    r = Run(ctx, W.config1(6))
+    coo = r.gpu_matrix()
+    b = r.gpu_vector()
+    flags = r.space.boundary_dof_flags()
+    vals_h = np.full(r.space.num_dofs, 0.5)
+    coo.fix_flagged_solution_comp_alt(flags, ctx.to_device(vals_h), b)
+    A = r.oracle_matrix()
+    bo = r.oracle_vector()
+    A.fix_flagged(r.ospace.boundary_dof_flags(), vals_h, bo, alt=True)
+    ro, co, vo = A.arrays()
+    t = coo.triplets()
+    assert np.array_equal(t["row"], ro) and np.array_equal(t["col"], co)
+    assert np.abs(b.download() - bo).max() <= 1e-12 * np.abs(bo).max()
+
+
+def test_fix_dof_exact_solution_gpu(ctx, goldens):
+    """fix_dof_flags (coomatrix_tests.cc:181-239) through the device COO, fix, CSR and PCG."""
+    g = goldens["fix_dof_exact"]
+    N = 10
+    r, c, v = [], [], []
+    for k in range(N):
+        if k > 0:
+            r.append(k); c.append(k - 1); v.append(-1.0)
+        if k < N - 1:
+            r.append(k); c.append(k + 1); v.append(-1.0)
+        r.append(k); c.append(k); v.append(2.0)
+    coo = L.COOMatrix(ctx, N, N, 64)
+    coo.append(r, c, v)
+    b = ctx.to_device(np.arange(1, N + 1, dtype=np.float64))
+    flags = np.zeros(N, np.uint8)
+    vals = np.ones(N)
+    for k, val in g["fixed"]:
+        flags[k] = 1
+        vals[k] = val
+    coo.fix_flagged_solution_components(ctx.to_device(flags), ctx.to_device(vals), b)
+    x = ctx.zeros(N)
+    st = coo.make_sparse().solve_pcg(b, x, rtol=1e-14)
+    assert st["converged"]
+    assert np.linalg.norm(x.download() - np.array(g["solution"])) < g["tolerance"]
+
+
+@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
+def test_solve_parity(ctx, name, precision):
+    """GPU PCG vs an FP64 sparse direct solve of the oracle's system (the
+    reference solves with Eigen SparseLU; SuperLU is the same algorithm)."""
+    import scipy.sparse.linalg as spla
+    r = Run(ctx, WORKLOADS[name]())
+    coo = r.gpu_matrix()
+    b = r.gpu_vector()
+    flags = r.space.boundary_dof_flags()
+    coo.fix_flagged_solution_components(flags, ctx.zeros(r.space.num_dofs), b)
+    x = ctx.zeros(r.space.num_dofs)
+    st = coo.make_sparse().solve_pcg(b, x, precision=precision, rtol=1e-12)
+    assert st["converged"], st
+    A = r.oracle_matrix()
+    bo = r.oracle_vector()
+    A.fix_flagged(r.ospace.boundary_dof_flags(), np.zeros(r.space.num_dofs), bo)
+    xo = spla.splu(A.to_scipy().tocsc()).solve(bo)
+    err = np.linalg.norm(x.download() - xo) / np.linalg.norm(xo)
+    assert err <= 1e-8, err
+
+
+@pytest.mark.parametrize("degree,alpha,gamma,a,b,qdeg,key", [
+    (2, W.poly(x1=1), W.poly(x1y1=1), W.poly(x2=1, y2=1), W.poly(x2=1, y2=-1), 6, "O2_deg6"),
+    (3, W.poly(y1=1), W.poly(x1y1=1), W.poly(x3=1, y3=1), W.poly(x1y2=1), 8, "O3_deg8"),
+])
+def test_kat_reaction_diffusion_gpu(ctx, goldens, degree, alpha, gamma, a, b, qdeg, key):
+    """lf_fe_quadratic/cubic.ReactionDiffusion with the matrix assembled on the GPU."""
+    k = goldens["reaction_diffusion_kat"]
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    m = L.Mesh.from_factory(ctx, xy, cells)
+    s = L.Space.lagrange(m, degree)
+    coo = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, s.num_triplets)
+    L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.ANALYTIC, func=L.FN_POLY, params=list(alpha)),
+                                          L.coeff(L.ANALYTIC, func=L.FN_POLY, params=list(gamma)), qdeg, qdeg), coo)
+    os_ = O.Space(O.Mesh(xy, cells), degree)
+    av = O.nodal_projection(os_, O.FN_POLY, a)
+    bv = O.nodal_projection(os_, O.FN_POLY, b)
+    val = av @ (coo.make_sparse().to_scipy() @ bv)
+    assert abs(val - k[key]["value"]) < k["tolerance"]
+
+
+def test_full_size_config3_properties(ctx):
+    """Config 3 at full size (1024x1024 O3, 209.7M triplets): exact symmetry of
+    every element block, total mass = |Omega| (stiffness rows sum to zero), and
+    sampled cell ranges against the oracle."""
+    wl = W.config3(1024)
+    mesh = W.build_mesh(ctx, wl["mesh"])
+    space = L.Space.lagrange(mesh, 3)
+    assert space.num_dofs == 9443329 and space.num_triplets == 2097152 * 100
+    keep = []
+    coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, space.num_triplets)
+    L.assemble_matrix_rd(space, L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep),
+                                              6, 6), coo)
+    t = coo.triplets()
+    v = t["value"].reshape(-1, 10, 10)
+    assert np.array_equal(v, v.transpose(0, 2, 1))
+    # per cell: sum_ij A_K(i,j) = gamma |K| (stiffness rows sum to zero)
+    cell_sum = v.sum(axis=(1, 2))
+    scale = np.abs(v).max(axis=(1, 2))
+    assert (np.abs(cell_sum - 0.5 / 1024 ** 2) <= 1e-12 * 100 * scale).all()
+    assert np.array_equal(t["row"].reshape(-1, 10, 10), t["col"].reshape(-1, 10, 10).transpose(0, 2, 1))
+    om = oracle_mesh(wl["mesh"])
+    os_ = O.Space(om, 3)
+    from parity import oracle_coeff
+    for lo, hi in [(0, 512), (1048576, 1049088), (2097152 - 512, 2097152)]:
+        A = O.assemble_rd(os_, oracle_coeff(wl["alpha"]), oracle_coeff(wl["gamma"]), 6, 6, (lo, hi))
+        ro, co, vo = A.arrays()
+        compare_triplets(t[lo * 100:hi * 100], ro, co, vo, np.full(hi - lo, 100))
+
+
+def test_errors(ctx):
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    m = L.Mesh.from_factory(ctx, xy, cells)
+    s = L.Space.lagrange(m, 1)
+    coo = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, s.num_triplets)
+    # missing quadrature rule for quads (loc_comp_ellbvp.h:278-287)
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO), 2, -1), coo)
+    assert e.value.code == L.MISSING_RULE and len(coo) == 0
+    # capacity
+    small = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, 10)
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO)), small)
+    assert e.value.code == L.CAPACITY and len(small) == 0
+    # unsupported coefficient kind
+    bad = L.coeff(L.CONSTANT, 1.0)
+    bad.kind = 9
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd(s, L.rd_provider(bad, L.coeff(L.ZERO)), coo)
+    assert e.value.code == L.UNSUPPORTED
+    # degenerate cell (collapsed triangle)
+    xy2 = np.array([[0, 0], [1, 0], [2, 0], [0, 1]], float)
+    with pytest.raises(L.LfgError) as e:
+        L.Mesh.from_factory(ctx, xy2, np.array([[0, 1, 2, -1], [0, 2, 3, -1]]))
+    assert e.value.code == L.DEGENERATE_CELL
+    # incomplete mesh (node 3 unused)
+    with pytest.raises(L.LfgError) as e:
+        L.Mesh.from_factory(ctx, np.array([[0, 0], [1, 0], [0, 1], [4, 4]], float), np.array([[0, 1, 2, -1]]))
+    assert e.value.code == L.INCOMPLETE_MESH
+    # bad node index
+    with pytest.raises(L.LfgError) as e:
+        L.Mesh.from_factory(ctx, np.array([[0, 0], [1, 0], [0, 1]], float), np.array([[0, 1, 7, -1]]))
+    assert e.value.code == L.INVALID_ARG
+    # the context is still usable afterwards
+    L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO)), coo)
+    assert len(coo) == s.num_triplets
+
+
+def test_not_converged_status(ctx):
+    r = Run(ctx, W.config1(16))
+    coo = r.gpu_matrix()
+    b = r.gpu_vector()
+    coo.fix_flagged_solution_components(r.space.boundary_dof_flags(), ctx.zeros(r.space.num_dofs), b)
+    x = ctx.zeros(r.space.num_dofs)
+    with pytest.raises(L.LfgError) as e:
+        coo.make_sparse().solve_pcg(b, x, rtol=1e-14, max_iterations=2, check_every=2)
+    assert e.value.code == L.NOT_CONVERGED
