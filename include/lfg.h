@@ -293,6 +293,21 @@ typedef struct {
 lfg_status lfg_solve_pcg(lfg_csr* csr, const double* b_dev, double* x_dev,
                          const lfg_solve_opts* opts, lfg_solve_stats* stats);
 
+/* lfg_solve_pcg for callers that cannot let the library allocate device
+ * memory (an application that owns a fixed GPU memory budget through its own
+ * allocator, or a service that must not grow the CUDA memory pool or risk an
+ * allocation's implicit synchronisation inside its time loop).  This entry
+ * point has no counterpart in the reference.  It runs the FP64 PCG of
+ * lfg_solve_pcg (same iterates) with all work vectors in one fixed,
+ * file-scope device array of 40 MiB + 32 KiB that every GPU loading the
+ * library holds until exit, and calls no allocator.  Limits: FP64 only
+ * (LFG_UNSUPPORTED otherwise) and at most 1,048,576 rows (LFG_CAPACITY
+ * otherwise).  All calls share the array: calls that overlap on the GPU race.
+ * The first call on a device resolves the array's address; make it before any
+ * stream capture. */
+lfg_status lfg_solve_pcg_noalloc(lfg_csr* csr, const double* b_dev, double* x_dev,
+                                 const lfg_solve_opts* opts, lfg_solve_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

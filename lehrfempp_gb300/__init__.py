@@ -444,12 +444,15 @@ class CSRMatrix:
         self.ctx.check(lib().lfg_csr_spmv(self.h, x.ptr, y.ptr))
 
     def solve_pcg(self, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=1e-4,
-                  check_every=32, raise_on_failure=True):
+                  check_every=32, raise_on_failure=True, noalloc=False):
+        """Jacobi-PCG; noalloc=True uses lfg_solve_pcg_noalloc (FP64, <= 2^20 rows,
+        work vectors in the library's fixed device array, no allocation)."""
         o = lfg_solve_opts()
         o.precision, o.rtol, o.max_iterations, o.inner_rtol, o.check_every = (precision, rtol, max_iterations,
                                                                              inner_rtol, check_every)
         st = lfg_solve_stats()
-        rc = lib().lfg_solve_pcg(self.h, b.ptr, x.ptr, C.byref(o), C.byref(st))
+        fn = lib().lfg_solve_pcg_noalloc if noalloc else lib().lfg_solve_pcg
+        rc = fn(self.h, b.ptr, x.ptr, C.byref(o), C.byref(st))
         if rc != OK and (raise_on_failure or rc != NOT_CONVERGED):
             self.ctx.check(rc)
         return {"iterations": st.iterations, "refinements": st.refinements, "rel_residual": st.rel_residual,

@@ -100,6 +100,7 @@ SIGNATURES = {
     "lfg_csr_download": (c_status, [vp, P(i64), P(i32), P(dbl)]),
     "lfg_csr_spmv": (c_status, [vp, vp, vp]),
     "lfg_solve_pcg": (c_status, [vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats)]),
+    "lfg_solve_pcg_noalloc": (c_status, [vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats)]),
 }
 
 
