@@ -260,7 +260,7 @@ def run_ours(args):
     for _ in range(max(3, args.steps // 4)):
         step()
     fam = {}
-    for f in ("rd_tria_uniform", "rd_general_tria", "rd_general_quad"):
+    for f in ("rd_tria_df", "rd_quad_df", "rd_general_tria", "rd_general_quad"):
         t, n = ctx.profile_read(f)
         if n:
             fam[f] = (t / n, n)
@@ -334,6 +334,7 @@ def run_ours(args):
                          "fp64": {"achieved_tflops": fp64_ach, "peak_tflops_measured": fp64_peak,
                                   "frac": fp64_ach / fp64_peak}},
             "kernels_ms": {k: v[0] for k, v in fam.items()},
+            "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
             "e2e": e2e, "cpu_baseline": cpu, "solve": solve,

@@ -25,6 +25,7 @@
 #include <map>
 
 #include "lfg_api.h"
+#include "lfg_elem.h"
 #include "lfg_internal.h"
 
 namespace lfg {
@@ -70,6 +71,7 @@ struct AsmArgs {
   const double* tab;
   Tab L;
   CoeffDev alpha, gamma;
+  unsigned long long* fallback;  // cells that took the FP64 route (diagnostics)
 };
 
 // ------------------------------------------------------------- device helpers
@@ -262,73 +264,156 @@ __global__ void __launch_bounds__(128) RDGeneralKernel(AsmArgs a) {
   }
 }
 
-// ------------------------------------- affine triangles, cell-constant coeffs
-// A_K = alpha |det J| sum_ab M_ab R_ab + gamma |det J| R_mass, staged in shared
-// memory so that the triplets leave the SM as coalesced 16-byte stores.
+// ------------------------------------ cell-constant coefficients, df32 path
+// Triangles and quadrilaterals with constant / per-cell alpha and gamma.  One
+// thread per cell computes the upper triangle of A_K in df32 (lfg_elem.h):
+// FP64 only for the coordinate differences, everything else on the FP32
+// pipes (GB300 issues ~60 FP32 FMAs per FP64 operation).  Cells whose inputs
+// leave the df32-safe range take the FP64 formula instead.  The values and
+// dof indices of a 128-cell tile are staged in shared memory and written out
+// as fully coalesced 16-byte triplets (every 32-byte sector is written whole).
+
+// Upper-triangle index of (i, j), i <= j, in "for i: for j >= i" order.
+template <int N>
+__device__ __forceinline__ int UpperIndex(int i, int j) {
+  const int a = i < j ? i : j, b = i < j ? j : i;
+  return a * N - (a * (a - 1)) / 2 + (b - a);
+}
+
+// Writes the staged tile: triplet w of cell cl goes to out + off[cl] + w.
+template <int N>
+__device__ __forceinline__ void WriteTile(lfg_triplet* out, int ncell, const double* svals,
+                                          const int* sdofs, const int64_t* soff) {
+  constexpr int NN = N * N, E = N * (N + 1) / 2;
+  for (int q = threadIdx.x; q < ncell * NN; q += blockDim.x) {
+    const int cl = q / NN, w = q - cl * NN;
+    const int i = w / N, j = w - i * N;
+    StoreTriplet(out + soff[cl] + w, sdofs[cl * N + i], sdofs[cl * N + j], svals[cl * E + UpperIndex<N>(i, j)]);
+  }
+}
+
+struct DfArgs {
+  const float* tab;  // df32 table block (pairs)
+  DfLayout L;
+};
+
 template <int DEG, bool MASS>
-__global__ void __launch_bounds__(DEG == 3 ? 64 : 128) RDTriaUniformKernel(AsmArgs a) {
+__global__ void __launch_bounds__(128) RDTriaDfKernel(AsmArgs a, DfArgs d) {
+  using elem::f2;
   constexpr int N = (DEG + 1) * (DEG + 2) / 2;
   constexpr int E = N * (N + 1) / 2;
-  constexpr int TILE = DEG == 3 ? 64 : 128;
-  constexpr int NN = N * N;
-  constexpr int STRIDE = NN + 1;  // pad one triplet per cell: conflict-free staging
-  extern __shared__ double sm[];
-  double* sR = sm;
-  lfg_triplet* stage = reinterpret_cast<lfg_triplet*>(sm + ((E * 4 + 1) & ~1));
-  for (int i = threadIdx.x; i < E * 4; i += blockDim.x) sR[i] = a.tab[a.L.off_R + i];
+  constexpr int TILE = 128;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  f2* sR = reinterpret_cast<f2*>(smraw);
+  double* svals = reinterpret_cast<double*>(smraw + ((E * 4 * sizeof(f2) + 15) & ~15));
+  int64_t* soff = reinterpret_cast<int64_t*>(svals + TILE * E);
+  int* sdofs = reinterpret_cast<int*>(soff + TILE);
+  const f2* gR = reinterpret_cast<const f2*>(d.tab) + d.L.off_R;
+  for (int i = threadIdx.x; i < E * 4; i += blockDim.x) sR[i] = gR[i];
   __syncthreads();
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
        t0 += static_cast<int64_t>(gridDim.x) * TILE) {
-    const int64_t t = t0 + threadIdx.x;
-    const int ncell_tile = static_cast<int>(a.count - t0 < TILE ? a.count - t0 : TILE);
-    if (threadIdx.x < ncell_tile) {
-      const int c = a.bucket[t];
+    const int ncell = static_cast<int>(a.count - t0 < TILE ? a.count - t0 : TILE);
+    if (threadIdx.x < ncell) {
+      const int c = a.bucket[t0 + threadIdx.x];
       int4 cn;
       double2 v[4];
       LoadVerts<false>(a, c, cn, v);
-      double m00, m01, m11, adet;
-      TriaMetric(v, m00, m01, m11, adet);
+      const double jac[4] = {v[1].x - v[0].x, v[2].x - v[0].x, v[1].y - v[0].y, v[2].y - v[0].y};
       const double al = CellConst(a.alpha, c);
-      const double a00 = al * m00, a01 = al * m01, a11 = al * m11;
-      const double mm = MASS ? CellConst(a.gamma, c) * adet : 0.0;
-      int dofs[N];
-#pragma unroll
-      for (int i = 0; i < N; ++i) dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
-      lfg_triplet* st = stage + threadIdx.x * STRIDE;
-      int e = 0;
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-#pragma unroll
-        for (int j = i; j < N; ++j, ++e) {
-          const double* R = sR + e * 4;
-          double r = a00 * R[0];
-          r = fma(a01, R[1], r);
-          r = fma(a11, R[2], r);
-          if (MASS) r = fma(mm, R[3], r);
-          StoreTriplet(st + i * N + j, dofs[i], dofs[j], r);
-          if (j != i) StoreTriplet(st + j * N + i, dofs[j], dofs[i], r);
-        }
+      const double ga = MASS ? CellConst(a.gamma, c) : 0.0;
+      double* vals = svals + threadIdx.x * E;
+      if (elem::DfSafe(jac[0]) && elem::DfSafe(jac[1]) && elem::DfSafe(jac[2]) && elem::DfSafe(jac[3]) &&
+          elem::DfSafe(al) && elem::DfSafe(ga)) {
+        elem::TriaUniformDF<E, MASS>(jac, al, ga, sR, vals);
+      } else {
+        elem::TriaUniformF64<E, MASS>(jac, al, ga, a.tab + a.L.off_R, vals);
+        atomicAdd(a.fallback, 1ull);
       }
+#pragma unroll
+      for (int i = 0; i < N; ++i) sdofs[threadIdx.x * N + i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      soff[threadIdx.x] = a.tri_offset[c];
     }
     __syncthreads();
-    // copy-out: each cell block is contiguous in the output
-    const int c_first = a.bucket[t0];
-    const bool contiguous = (a.bucket[t0 + ncell_tile - 1] - c_first) == ncell_tile - 1;
-    if (contiguous) {
-      lfg_triplet* dst = a.out + a.tri_offset[c_first];
-      const int total = ncell_tile * NN;
-      for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int cl = q / NN, w = q - cl * NN;
-        *reinterpret_cast<int4*>(dst + q) = *reinterpret_cast<const int4*>(stage + cl * STRIDE + w);
-      }
-    } else {
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int cl = warp; cl < ncell_tile; cl += blockDim.x >> 5) {
-        lfg_triplet* dst = a.out + a.tri_offset[a.bucket[t0 + cl]];
-        for (int w = lane; w < NN; w += 32)
-          *reinterpret_cast<int4*>(dst + w) = *reinterpret_cast<const int4*>(stage + cl * STRIDE + w);
-      }
+    WriteTile<N>(a.out, ncell, svals, sdofs, soff);
+    __syncthreads();
+  }
+}
+
+// FP64 per-point formula of a quadrilateral with cell-constant coefficients
+// (cells outside the df32 range), accumulating into vals[E].
+template <int N, bool MASS>
+__device__ void QuadUniformF64(const double2 (&v)[4], double al, double ga, const double* tab, const Tab& L,
+                               double* vals) {
+  constexpr int E = N * (N + 1) / 2;
+  for (int e = 0; e < E; ++e) vals[e] = 0.0;
+  for (int k = 0; k < L.nq; ++k) {
+    double m00, m01, m11, adet;
+    QuadMetric(v, tab[L.off_qx + k], tab[L.off_qy + k], m00, m01, m11, adet);
+    const double s = tab[L.off_w + k] * al;
+    const double mk = tab[L.off_w + k] * adet * ga;
+    const double* Tk = tab + L.off_T + k * E * 4;
+    for (int e = 0; e < E; ++e) {
+      double r = vals[e];
+      r = fma(s * m00, Tk[e * 4 + 0], r);
+      r = fma(s * m01, Tk[e * 4 + 1], r);
+      r = fma(s * m11, Tk[e * 4 + 2], r);
+      if (MASS) r = fma(mk, Tk[e * 4 + 3], r);
+      vals[e] = r;
     }
+  }
+}
+
+template <int DEG, int M, bool MASS>
+__global__ void __launch_bounds__(128) RDQuadDfKernel(AsmArgs a, DfArgs d) {
+  using elem::f2;
+  constexpr int N = (DEG + 1) * (DEG + 1);
+  constexpr int E = N * (N + 1) / 2;
+  constexpr int NQ = M * M;
+  constexpr int TILE = E > 64 ? 64 : 128;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  f2* sT = reinterpret_cast<f2*>(smraw);  // [NQ][E][4], then W[NQ], t[M]
+  f2* sW = sT + NQ * E * 4;
+  f2* st = sW + NQ;
+  double* svals = reinterpret_cast<double*>(smraw + (((NQ * E * 4 + NQ + M) * sizeof(f2) + 15) & ~15));
+  int64_t* soff = reinterpret_cast<int64_t*>(svals + TILE * E);
+  int* sdofs = reinterpret_cast<int*>(soff + TILE);
+  const f2* g = reinterpret_cast<const f2*>(d.tab);
+  for (int i = threadIdx.x; i < NQ * E * 4; i += blockDim.x) sT[i] = g[d.L.off_T + i];
+  for (int i = threadIdx.x; i < NQ; i += blockDim.x) sW[i] = g[d.L.off_W + i];
+  for (int i = threadIdx.x; i < M; i += blockDim.x) st[i] = g[d.L.off_t + i];
+  __syncthreads();
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
+       t0 += static_cast<int64_t>(gridDim.x) * TILE) {
+    const int ncell = static_cast<int>(a.count - t0 < TILE ? a.count - t0 : TILE);
+    if (threadIdx.x < ncell) {
+      const int c = a.bucket[t0 + threadIdx.x];
+      int4 cn;
+      double2 v[4];
+      LoadVerts<true>(a, c, cn, v);
+      // J col0 = a + d yh, col1 = c + d xh (quad_o1.cc:93-99)
+      const double acd[6] = {v[1].x - v[0].x, v[1].y - v[0].y, v[3].x - v[0].x, v[3].y - v[0].y,
+                             (v[0].x - v[1].x) + (v[2].x - v[3].x), (v[0].y - v[1].y) + (v[2].y - v[3].y)};
+      const double al = CellConst(a.alpha, c);
+      const double ga = MASS ? CellConst(a.gamma, c) : 0.0;
+      double* vals = svals + threadIdx.x * E;
+      bool safe = elem::DfSafe(al) && elem::DfSafe(ga);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) safe = safe && elem::DfSafe(acd[k]);
+      if (safe) {
+        f2 cpt[NQ][4];
+        elem::QuadPointCoeffsDF<M, MASS>(acd, al, ga, st, sW, cpt);
+        elem::QuadContractDF<E, NQ, MASS>(cpt, sT, vals);
+      } else {
+        QuadUniformF64<N, MASS>(v, al, ga, a.tab, a.L, vals);
+        atomicAdd(a.fallback, 1ull);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) sdofs[threadIdx.x * N + i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      soff[threadIdx.x] = a.tri_offset[c];
+    }
+    __syncthreads();
+    WriteTile<N>(a.out, ncell, svals, sdofs, soff);
     __syncthreads();
   }
 }
@@ -487,6 +572,28 @@ const double* GetTable(lfg_space* sp, bool quad, int degree, int rule_degree, Ta
   return ent.buf.as<double>();
 }
 
+// df32 tables (binary32 pairs) of the cell-constant-coefficient kernels.
+DfArgs GetDfTable(lfg_space* sp, bool quad, int degree, int rule_degree) {
+  lfg_ctx* ctx = sp->mesh->ctx;
+  const int key = (quad ? 1 << 20 : 0) | (degree << 10) | rule_degree;
+  auto it = ctx->dftables.find(key);
+  if (it == ctx->dftables.end()) {
+    std::vector<float> h;
+    DfLayout L;
+    if (!BuildDfTables(quad, degree, rule_degree, h, L)) Fail(LFG_UNSUPPORTED, "no quadrature rule");
+    DfTableEntry& ent = ctx->dftables[key];
+    ent.layout = L;
+    ent.buf.alloc(h.size() * sizeof(float), ctx->stream);
+    LFG_CUDA(cudaMemcpyAsync(ent.buf.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+    it = ctx->dftables.find(key);
+  }
+  DfArgs d;
+  d.tab = it->second.buf.as<float>();
+  d.L = it->second.layout;
+  return d;
+}
+
 CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
   CoeffDev d;
   d.kind = c.kind;
@@ -507,8 +614,8 @@ bool Uniform(const lfg_coeff& c) {
   return c.kind == LFG_COEFF_ZERO || c.kind == LFG_COEFF_CONSTANT || c.kind == LFG_COEFF_PER_CELL;
 }
 
-template <class K>
-void Launch(K kernel, lfg_ctx* ctx, int64_t count, size_t smem, const AsmArgs& a, int block = 128) {
+template <class K, class... Args>
+void Launch(K kernel, lfg_ctx* ctx, int64_t count, size_t smem, int block, const Args&... args) {
   if (count <= 0) return;
   LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
@@ -516,39 +623,56 @@ void Launch(K kernel, lfg_ctx* ctx, int64_t count, size_t smem, const AsmArgs& a
   if (per_sm < 1) per_sm = 1;
   int64_t blocks = (count + block - 1) / block;
   blocks = std::min<int64_t>(blocks, static_cast<int64_t>(ctx->num_sms) * per_sm);
-  kernel<<<static_cast<unsigned>(blocks), block, smem, ctx->stream>>>(a);
+  kernel<<<static_cast<unsigned>(blocks), block, smem, ctx->stream>>>(args...);
   LFG_LAUNCHED(ctx);
 }
 
+template <int DEG, int M, bool MASS>
+void LaunchQuadDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  constexpr int N = (DEG + 1) * (DEG + 1), E = N * (N + 1) / 2, NQ = M * M, TILE = E > 64 ? 64 : 128;
+  const size_t smem = (((NQ * E * 4 + NQ + M) * 8 + 15) & ~size_t(15)) + TILE * (E * 8 + 8 + N * 4);
+  Launch(RDQuadDfKernel<DEG, M, MASS>, ctx, a.count, smem, 128, a, d);
+}
+
 template <int DEG, bool QUAD>
-void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, bool uniform, bool mass) {
+void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, bool mass) {
   const size_t smem_gen = a.L.total * sizeof(double);
-  if (!QUAD && uniform) {
-    constexpr int N = (DEG + 1) * (DEG + 2) / 2;
-    constexpr int E = N * (N + 1) / 2;
-    constexpr int TILE = DEG == 3 ? 64 : 128;
-    const size_t smem = ((E * 4 + 1) & ~1) * sizeof(double) + TILE * (N * N + 1) * sizeof(lfg_triplet);
-    ProfScope prof(ctx, "rd_tria_uniform");
-    if (mass) Launch(RDTriaUniformKernel<DEG, true>, ctx, a.count, smem, a, TILE);
-    else Launch(RDTriaUniformKernel<DEG, false>, ctx, a.count, smem, a, TILE);
+  if (uniform && d.tab && !QUAD) {
+    constexpr int N = (DEG + 1) * (DEG + 2) / 2, E = N * (N + 1) / 2;
+    const size_t smem = ((E * 4 * 8 + 15) & ~size_t(15)) + 128 * (E * 8 + 8 + N * 4);
+    ProfScope prof(ctx, "rd_tria_df");
+    if (mass) Launch(RDTriaDfKernel<DEG, true>, ctx, a.count, smem, 128, a, d);
+    else Launch(RDTriaDfKernel<DEG, false>, ctx, a.count, smem, 128, a, d);
+    return;
+  }
+  if (uniform && d.tab && QUAD && d.L.m >= 2 && d.L.m <= 4) {
+    ProfScope prof(ctx, "rd_quad_df");
+    switch (d.L.m * 2 + (mass ? 1 : 0)) {
+      case 4: LaunchQuadDf<DEG, 2, false>(ctx, a, d); break;
+      case 5: LaunchQuadDf<DEG, 2, true>(ctx, a, d); break;
+      case 6: LaunchQuadDf<DEG, 3, false>(ctx, a, d); break;
+      case 7: LaunchQuadDf<DEG, 3, true>(ctx, a, d); break;
+      case 8: LaunchQuadDf<DEG, 4, false>(ctx, a, d); break;
+      case 9: LaunchQuadDf<DEG, 4, true>(ctx, a, d); break;
+    }
     return;
   }
   ProfScope prof(ctx, QUAD ? "rd_general_quad" : "rd_general_tria");
   if (uniform) {
-    if (mass) Launch(RDGeneralKernel<DEG, QUAD, false, true>, ctx, a.count, smem_gen, a);
-    else Launch(RDGeneralKernel<DEG, QUAD, false, false>, ctx, a.count, smem_gen, a);
+    if (mass) Launch(RDGeneralKernel<DEG, QUAD, false, true>, ctx, a.count, smem_gen, 128, a);
+    else Launch(RDGeneralKernel<DEG, QUAD, false, false>, ctx, a.count, smem_gen, 128, a);
   } else {
-    if (mass) Launch(RDGeneralKernel<DEG, QUAD, true, true>, ctx, a.count, smem_gen, a);
-    else Launch(RDGeneralKernel<DEG, QUAD, true, false>, ctx, a.count, smem_gen, a);
+    if (mass) Launch(RDGeneralKernel<DEG, QUAD, true, true>, ctx, a.count, smem_gen, 128, a);
+    else Launch(RDGeneralKernel<DEG, QUAD, true, false>, ctx, a.count, smem_gen, 128, a);
   }
 }
 
 template <bool QUAD>
-void DispatchRD(lfg_ctx* ctx, int degree, const AsmArgs& a, bool uniform, bool mass) {
+void DispatchRD(lfg_ctx* ctx, int degree, const AsmArgs& a, const DfArgs& d, bool uniform, bool mass) {
   switch (degree) {
-    case 1: LaunchRD<1, QUAD>(ctx, a, uniform, mass); break;
-    case 2: LaunchRD<2, QUAD>(ctx, a, uniform, mass); break;
-    case 3: LaunchRD<3, QUAD>(ctx, a, uniform, mass); break;
+    case 1: LaunchRD<1, QUAD>(ctx, a, d, uniform, mass); break;
+    case 2: LaunchRD<2, QUAD>(ctx, a, d, uniform, mass); break;
+    case 3: LaunchRD<3, QUAD>(ctx, a, d, uniform, mass); break;
   }
 }
 
@@ -557,12 +681,12 @@ void DispatchLoad(lfg_ctx* ctx, int degree, const AsmArgs& a, bool vary) {
   const size_t smem = a.L.total * sizeof(double);
   ProfScope prof(ctx, QUAD ? "load_quad" : "load_tria");
   switch (degree) {
-    case 1: vary ? Launch(LoadVectorKernel<1, QUAD, true>, ctx, a.count, smem, a)
-                 : Launch(LoadVectorKernel<1, QUAD, false>, ctx, a.count, smem, a); break;
-    case 2: vary ? Launch(LoadVectorKernel<2, QUAD, true>, ctx, a.count, smem, a)
-                 : Launch(LoadVectorKernel<2, QUAD, false>, ctx, a.count, smem, a); break;
-    case 3: vary ? Launch(LoadVectorKernel<3, QUAD, true>, ctx, a.count, smem, a)
-                 : Launch(LoadVectorKernel<3, QUAD, false>, ctx, a.count, smem, a); break;
+    case 1: vary ? Launch(LoadVectorKernel<1, QUAD, true>, ctx, a.count, smem, 128, a)
+                 : Launch(LoadVectorKernel<1, QUAD, false>, ctx, a.count, smem, 128, a); break;
+    case 2: vary ? Launch(LoadVectorKernel<2, QUAD, true>, ctx, a.count, smem, 128, a)
+                 : Launch(LoadVectorKernel<2, QUAD, false>, ctx, a.count, smem, 128, a); break;
+    case 3: vary ? Launch(LoadVectorKernel<3, QUAD, true>, ctx, a.count, smem, 128, a)
+                 : Launch(LoadVectorKernel<3, QUAD, false>, ctx, a.count, smem, 128, a); break;
   }
 }
 
@@ -570,6 +694,7 @@ int RuleDegree(int requested, int degree) { return requested == 0 ? 2 * degree :
 
 AsmArgs BaseArgs(lfg_space* sp) {
   AsmArgs a{};
+  a.fallback = reinterpret_cast<unsigned long long*>(StatusWord(sp->mesh->ctx) + 12);
   a.cells = sp->mesh->cell_nodes.as<int4>();
   a.xy = sp->mesh->xy.as<double2>();
   a.cell_dofs = sp->cell_dofs.as<int32_t>();
@@ -635,17 +760,20 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_
   const bool uniform = Uniform(pr->alpha) && Uniform(pr->gamma);
   const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
   const int deg = sp->degree;
+  DfArgs none{nullptr, DfLayout()};
   if (m->ntria) {
-    a.tab = GetTable(sp, false, deg, RuleDegree(pr->qr_degree_tria, deg), a.L);
+    const int rd = RuleDegree(pr->qr_degree_tria, deg);
+    a.tab = GetTable(sp, false, deg, rd, a.L);
     a.bucket = m->tria_list.as<int32_t>();
     a.count = m->ntria;
-    DispatchRD<false>(sp->mesh->ctx, deg, a, uniform, mass);
+    DispatchRD<false>(sp->mesh->ctx, deg, a, uniform ? GetDfTable(sp, false, deg, rd) : none, uniform, mass);
   }
   if (m->nquad) {
-    a.tab = GetTable(sp, true, deg, RuleDegree(pr->qr_degree_quad, deg), a.L);
+    const int rd = RuleDegree(pr->qr_degree_quad, deg);
+    a.tab = GetTable(sp, true, deg, rd, a.L);
     a.bucket = m->quad_list.as<int32_t>();
     a.count = m->nquad;
-    DispatchRD<true>(sp->mesh->ctx, deg, a, uniform, mass);
+    DispatchRD<true>(sp->mesh->ctx, deg, a, uniform ? GetDfTable(sp, true, deg, rd) : none, uniform, mass);
   }
   coo->size += sp->num_triplets;
   LFG_API_END

@@ -127,6 +127,13 @@ lfg_status lfg_profile_enable(lfg_ctx* ctx, int enable) {
 lfg_status lfg_profile_read(lfg_ctx* ctx, const char* family, double* total_ms, int64_t* launches) {
   LFG_API_BEGIN(ctx)
   if (!family) Fail(LFG_INVALID_ARG, "null family");
+  if (std::string(family) == "fp64_fallback_cells") {  // element-kernel cells computed in FP64
+    unsigned long long n = 0;
+    D2HSync(ctx, &n, StatusWord(ctx) + 12, sizeof(n));
+    if (total_ms) *total_ms = static_cast<double>(n);
+    if (launches) *launches = static_cast<int64_t>(n);
+    return LFG_OK;
+  }
   ResolveProfile(ctx);
   auto it = ctx->prof_totals.find(family);
   if (total_ms) *total_ms = it == ctx->prof_totals.end() ? 0.0 : it->second.first;
@@ -197,12 +204,16 @@ lfg_status lfg_ctx_create(int device, lfg_ctx** out) {
   }
 }
 
-lfg_status lfg_ctx_destroy(lfg_ctx* ctx) {
-  if (!ctx) return LFG_INVALID_ARG;
+}  // extern "C"
+
+namespace lfg {
+namespace {
+void FreeCtx(lfg_ctx* ctx) {
   cudaSetDevice(ctx->device);
   ctx->flush.reset();
   ctx->status.reset();
   ctx->tables.clear();
+  ctx->dftables.clear();
   cudaStreamSynchronize(ctx->stream);
   for (auto& r : ctx->prof_pending) {
     cudaEventDestroy(r.a);
@@ -214,6 +225,22 @@ lfg_status lfg_ctx_destroy(lfg_ctx* ctx) {
   cudaEventDestroy(ctx->t1);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+}  // namespace
+
+void RetainCtx(lfg_ctx* ctx) { ++ctx->refs; }
+
+void ReleaseCtx(lfg_ctx* ctx) {
+  if (--ctx->refs == 0 && ctx->destroyed) FreeCtx(ctx);
+}
+}  // namespace lfg
+
+extern "C" {
+
+lfg_status lfg_ctx_destroy(lfg_ctx* ctx) {
+  if (!ctx || ctx->destroyed) return LFG_INVALID_ARG;
+  ctx->destroyed = true;
+  if (ctx->refs == 0) lfg::FreeCtx(ctx);
   return LFG_OK;
 }
 

@@ -124,6 +124,7 @@ lfg_status lfg_coo_create(lfg_ctx* ctx, int64_t rows, int64_t cols, int64_t capa
   if (rows >= (int64_t(1) << 31) || cols >= (int64_t(1) << 31))
     Fail(LFG_INVALID_ARG, "COO dimensions exceed the int32 triplet index range");
   auto* c = new lfg_coo;
+  c->ref.Set(ctx);
   c->ctx = ctx;
   c->rows = rows;
   c->cols = cols;
@@ -145,6 +146,7 @@ lfg_status lfg_coo_wrap(lfg_ctx* ctx, int64_t rows, int64_t cols, lfg_triplet* d
   if (!out || !d || size < 0 || size > capacity) Fail(LFG_INVALID_ARG, "lfg_coo_wrap: bad argument");
   if (reinterpret_cast<uintptr_t>(d) % 16) Fail(LFG_INVALID_ARG, "triplet buffer must be 16-byte aligned");
   auto* c = new lfg_coo;
+  c->ref.Set(ctx);
   c->ctx = ctx;
   c->rows = rows;
   c->cols = cols;

@@ -452,6 +452,7 @@ lfg_status lfg_csr_from_coo(lfg_coo* coo, lfg_csr** out) {
   const int64_t n = coo->size;
   if (n >= (int64_t(1) << 32)) Fail(LFG_UNSUPPORTED, "more than 2^32 triplets");
   auto* A = new lfg_csr;
+  A->ref.Set(ctx);
   A->ctx = ctx;
   A->rows = coo->rows;
   A->cols = coo->cols;

@@ -1,0 +1,169 @@
+// Element matrices of ReactionDiffusionElementMatrixProvider for cells with
+// cell-constant alpha / gamma (uscalfe/loc_comp_ellbvp.h:266-339), in df32
+// arithmetic (lfg_df32.h).  Host + device code: the kernels in
+// lfg_assemble.cu and the CPU precision test use these functions.
+//
+// Upper-triangle entry e = (i, j), i <= j, in the order
+//   for i in 0..n-1: for j in i..n-1.
+// Tables (built by lfg_tables.cc, split into binary32 pairs):
+//   triangle  R[e][4]     = sum_k w_k {g_i0 g_j0, g_i0 g_j1 + g_i1 g_j0, g_i1 g_j1, phi_i phi_j}
+//   quad      T[k][e][4]  = the same terms at point k (no weight), and per point
+//             W[k] = w_k, 1D abscissae t[m] (points are x slow, y fast).
+// With c = w |det J| alpha J^-1 J^-T = w alpha adj(J) adj(J)^T / |det J| the
+// entries are  A(i,j) = sum_k c00 T0 + c01 T1 + c11 T2 + w |det J| gamma T3.
+#pragma once
+
+#include "lfg_df32.h"
+
+#if defined(__CUDACC__)
+#define DF_UNROLL _Pragma("unroll")
+#define DF_NOUNROLL _Pragma("unroll 1")
+#else
+#define DF_UNROLL
+#define DF_NOUNROLL
+#endif
+
+namespace lfg {
+namespace elem {
+
+using df::f2;
+
+// df32 is used when the cell's inputs keep every intermediate in binary32
+// range; other cells take the FP64 route.
+DF_HD bool DfSafe(double x) {
+  const double a = x < 0 ? -x : x;
+  return a == 0.0 || (a >= 9.094947017729282e-13 && a <= 1.099511627776e12);  // [2^-40, 2^40]
+}
+
+// ------------------------------------------------------------------ triangles
+
+// |det J| J^-1 J^-T (3 entries) and |det J| of the affine map with columns
+// (j00, j10) = v1 - v0 and (j01, j11) = v2 - v0 (geometry/tria_o1.cc:56-61).
+DF_HD void TriaMetricDF(f2 j00, f2 j01, f2 j10, f2 j11, f2& m00, f2& m01, f2& m11, f2& adet) {
+  using namespace df;
+  const f2 det = Sub(Mul(j00, j11), Mul(j10, j01));
+  adet = Abs(det);
+  const f2 r = Rcp(adet);
+  m00 = Mul(Add(Mul(j11, j11), Mul(j01, j01)), r);
+  m01 = Neg(Mul(Add(Mul(j11, j10), Mul(j01, j00)), r));
+  m11 = Mul(Add(Mul(j10, j10), Mul(j00, j00)), r);
+}
+
+// Upper triangle of the triangle element matrix, E = n(n+1)/2 values.
+template <int E, bool MASS>
+DF_HD void TriaUniformDF(const double (&jac)[4] /* j00, j01, j10, j11 */, double alpha, double gamma,
+                         const f2* R /* [E][4] */, double* out) {
+  using namespace df;
+  f2 m00, m01, m11, adet;
+  TriaMetricDF(FromDouble(jac[0]), FromDouble(jac[1]), FromDouble(jac[2]), FromDouble(jac[3]), m00, m01, m11, adet);
+  const f2 al = FromDouble(alpha);
+  const f2 a00 = Mul(al, m00), a01 = Mul(al, m01), a11 = Mul(al, m11);
+  f2 mm = {0.0f, 0.0f};
+  if (MASS) mm = Mul(FromDouble(gamma), adet);
+  DF_UNROLL
+  for (int e = 0; e < E; ++e) {
+    Acc acc;
+    acc.AddProd(a00, R[4 * e + 0]);
+    acc.AddProd(a01, R[4 * e + 1]);
+    acc.AddProd(a11, R[4 * e + 2]);
+    if (MASS) acc.AddProd(mm, R[4 * e + 3]);
+    out[e] = ToDouble(acc.Value());
+  }
+}
+
+// FP64 version of the same formula (cells outside the df32 range).
+template <int E, bool MASS>
+DF_HD void TriaUniformF64(const double (&jac)[4], double alpha, double gamma, const double* R, double* out) {
+  const double j00 = jac[0], j01 = jac[1], j10 = jac[2], j11 = jac[3];
+  const double det = j00 * j11 - j10 * j01;
+  const double adet = det < 0 ? -det : det;
+  const double inv = 1.0 / adet;
+  const double a00 = alpha * ((j11 * j11 + j01 * j01) * inv);
+  const double a01 = alpha * (-(j11 * j10 + j01 * j00) * inv);
+  const double a11 = alpha * ((j10 * j10 + j00 * j00) * inv);
+  const double mm = MASS ? gamma * adet : 0.0;
+  for (int e = 0; e < E; ++e) {
+    double r = a00 * R[4 * e];
+    r = fma(a01, R[4 * e + 1], r);
+    r = fma(a11, R[4 * e + 2], r);
+    if (MASS) r = fma(mm, R[4 * e + 3], r);
+    out[e] = r;
+  }
+}
+
+// -------------------------------------------------------------- quadrilaterals
+
+// Per-point coefficients c[k] = {c00, c01, c11, m} of a bilinear quadrilateral
+// on an M x M tensor rule.  a = v1 - v0, c = v3 - v0, d = v0 - v1 + v2 - v3
+// (FP64 differences, geometry/quad_o1.cc:93-99 rewritten: J col0 = a + d yh,
+// col1 = c + d xh), everything after the differences in df32.
+template <int M, bool MASS>
+DF_HD void QuadPointCoeffsDF(const double (&acd)[6] /* ax, ay, cx, cy, dx, dy */, double alpha, double gamma,
+                             const f2* t /* [M] abscissae */, const f2* W /* [M*M] weights */, f2 (*c)[4]) {
+  using namespace df;
+  const f2 ax = FromDouble(acd[0]), ay = FromDouble(acd[1]), cx = FromDouble(acd[2]), cy = FromDouble(acd[3]);
+  const f2 dx = FromDouble(acd[4]), dy = FromDouble(acd[5]);
+  const f2 al = FromDouble(alpha);
+  const f2 ga = MASS ? FromDouble(gamma) : f2{0.0f, 0.0f};
+  f2 j00[M], j10[M], j01[M], j11[M], m00[M], m11[M];
+  DF_UNROLL
+  for (int q = 0; q < M; ++q) {  // column 0 at yh = t[q], column 1 at xh = t[q]
+    j00[q] = MulAdd(dx, t[q], ax);
+    j10[q] = MulAdd(dy, t[q], ay);
+    j01[q] = MulAdd(dx, t[q], cx);
+    j11[q] = MulAdd(dy, t[q], cy);
+  }
+  DF_UNROLL
+  for (int q = 0; q < M; ++q) {
+    m00[q] = Add(Mul(j11[q], j11[q]), Mul(j01[q], j01[q]));  // depends on xh only
+    m11[q] = Add(Mul(j10[q], j10[q]), Mul(j00[q], j00[q]));  // depends on yh only
+  }
+  DF_UNROLL
+  for (int p = 0; p < M; ++p) {    // xh index
+    DF_UNROLL
+    for (int q = 0; q < M; ++q) {  // yh index
+      const int k = p * M + q;
+      const f2 det = Sub(Mul(j00[q], j11[p]), Mul(j10[q], j01[p]));
+      const f2 adet = Abs(det);
+      const f2 s = Mul(Mul(W[k], al), Rcp(adet));
+      const f2 m01 = Neg(Add(Mul(j11[p], j10[q]), Mul(j01[p], j00[q])));
+      c[k][0] = Mul(s, m00[p]);
+      c[k][1] = Mul(s, m01);
+      c[k][2] = Mul(s, m11[q]);
+      if (MASS) c[k][3] = Mul(Mul(W[k], adet), ga);
+    }
+  }
+}
+
+// Number of upper-triangle entries contracted together (a divisor of E): the
+// G accumulators give instruction-level parallelism while the loop over the
+// E/G groups stays a runtime loop, so the code fits the instruction cache.
+template <int E>
+constexpr int ContractGroup() {
+  return E % 5 == 0 ? 5 : (E % 4 == 0 ? 4 : (E % 3 == 0 ? 3 : 1));
+}
+
+// All upper-triangle entries: sum over points of c . T.
+template <int E, int NQ, bool MASS>
+DF_HD void QuadContractDF(const f2 (*c)[4], const f2* T /* [NQ][E][4] */, double* out) {
+  using namespace df;
+  constexpr int G = ContractGroup<E>();
+  DF_NOUNROLL
+  for (int e0 = 0; e0 < E; e0 += G) {
+    Acc acc[G];
+    DF_UNROLL
+    for (int k = 0; k < NQ; ++k) {
+      const f2* te = T + (static_cast<long>(k) * E + e0) * 4;
+      DF_UNROLL
+      for (int ab = 0; ab < (MASS ? 4 : 3); ++ab) {
+        DF_UNROLL
+        for (int g = 0; g < G; ++g) acc[g].AddProd(c[k][ab], te[g * 4 + ab]);
+      }
+    }
+    DF_UNROLL
+    for (int g = 0; g < G; ++g) out[e0 + g] = ToDouble(acc[g].Value());
+  }
+}
+
+}  // namespace elem
+}  // namespace lfg

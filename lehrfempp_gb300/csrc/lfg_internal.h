@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/lfg.h"
+#include "lfg_tables.h"
 
 namespace lfg {
 
@@ -59,9 +60,18 @@ struct TableEntry {
   Tab layout;
   DevBuf buf;
 };
+struct DfTableEntry {
+  DfLayout layout;
+  DevBuf buf;
+};
 }  // namespace lfg
 
 struct lfg_ctx {
+  // Meshes, COO and CSR matrices hold a reference; lfg_ctx_destroy only marks
+  // the context and the last release frees it, so a handle destroyed after its
+  // context is still safe.
+  int64_t refs = 0;
+  bool destroyed = false;
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -74,6 +84,7 @@ struct lfg_ctx {
   void* pinned_small = nullptr;
   // reference-element tables keyed by (cell type, degree, rule degree)
   std::map<int, lfg::TableEntry> tables;
+  std::map<int, lfg::DfTableEntry> dftables;
   // per-kernel-family event timing (lfg_profile_*)
   bool profiling = false;
   struct ProfRec {
@@ -86,6 +97,24 @@ struct lfg_ctx {
 };
 
 namespace lfg {
+void RetainCtx(lfg_ctx* ctx);
+void ReleaseCtx(lfg_ctx* ctx);
+// First member of every handle: declared first, destroyed last, so the
+// handle's device buffers are freed before the context reference is dropped.
+struct CtxRef {
+  lfg_ctx* c = nullptr;
+  CtxRef() = default;
+  CtxRef(const CtxRef&) = delete;
+  CtxRef& operator=(const CtxRef&) = delete;
+  void Set(lfg_ctx* x) {
+    c = x;
+    RetainCtx(x);
+  }
+  ~CtxRef() {
+    if (c) ReleaseCtx(c);
+  }
+};
+
 // Brackets the launches inside its lifetime with events on the context stream
 // when profiling is enabled.
 struct ProfScope {
@@ -97,6 +126,7 @@ struct ProfScope {
 }  // namespace lfg
 
 struct lfg_mesh {
+  lfg::CtxRef ref;
   lfg_ctx* ctx = nullptr;
   int64_t nv = 0, ne = 0, nc = 0, ntria = 0, nquad = 0;
   lfg::DevBuf xy;          // double2[nv]
@@ -110,6 +140,7 @@ struct lfg_mesh {
 };
 
 struct lfg_space {
+  lfg::CtxRef ref;
   lfg_mesh* mesh = nullptr;
   int degree = 0;  // 0 = generic layout
   int np = 0, ns = 0, nt = 0, nq = 0;
@@ -128,6 +159,7 @@ struct lfg_space {
 };
 
 struct lfg_coo {
+  lfg::CtxRef ref;
   lfg_ctx* ctx = nullptr;
   int64_t rows = 0, cols = 0, capacity = 0, size = 0;
   lfg_triplet* d = nullptr;
@@ -135,6 +167,7 @@ struct lfg_coo {
 };
 
 struct lfg_csr {
+  lfg::CtxRef ref;
   lfg_ctx* ctx = nullptr;
   int64_t rows = 0, cols = 0, nnz = 0;
   lfg::DevBuf rowptr;  // int64[rows + 1]
@@ -147,6 +180,11 @@ struct lfg_csr {
 };
 
 namespace lfg {
+
+// Context lifetime: children retain the context; the last release after
+// lfg_ctx_destroy frees it.
+void RetainCtx(lfg_ctx* ctx);
+void ReleaseCtx(lfg_ctx* ctx);
 
 // Grid-size helper: multiples of the SM count for grid-stride kernels.
 int GridFor(lfg_ctx* ctx, int64_t n, int block, int per_thread = 1);
@@ -165,14 +203,5 @@ int32_t ReadAndClearStatus(lfg_ctx* ctx, int32_t* detail = nullptr);
 int32_t* StatusWord(lfg_ctx* ctx);
 // Copy a small device value to the host synchronously (stream ordered).
 void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
-
-// ---- quadrature / reference elements (lfg_tables.cc) ----
-struct Rule {
-  int n = 0;
-  std::vector<double> x, y, w;
-};
-bool MakeRule(bool is_quad, int degree, Rule& out);  // false if not tabulated
-int NumShape(bool is_quad, int degree);
-void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]);
 
 }  // namespace lfg

@@ -389,6 +389,7 @@ lfg_mesh* NewMesh(lfg_ctx* ctx, int64_t nv, int64_t nc) {
   if (nv <= 0 || nc <= 0) Fail(LFG_INVALID_ARG, "mesh needs nodes and cells");
   if (nv >= (int64_t(1) << 31) || nc >= (int64_t(1) << 31)) Fail(LFG_INVALID_ARG, "mesh too large");
   auto* m = new lfg_mesh;
+  m->ref.Set(ctx);
   m->ctx = ctx;
   m->nv = nv;
   m->nc = nc;

@@ -136,6 +136,7 @@ lfg_status lfg_space_create(lfg_mesh* m, int np, int ns, int nt, int nq, lfg_spa
   auto* sp = new lfg_space;
   try {
     cudaStream_t s = m->ctx->stream;
+    sp->ref.Set(m->ctx);
     sp->mesh = m;
     sp->np = np; sp->ns = ns; sp->nt = nt; sp->nq = nq;
     // InitTotalNumDofs (dofhandler.cc:131-139)
@@ -189,7 +190,7 @@ lfg_status lfg_space_create_lagrange(lfg_mesh* m, int degree, lfg_space** out) {
 
 lfg_status lfg_space_destroy(lfg_space* sp) {
   if (!sp) return LFG_INVALID_ARG;
-  cudaSetDevice(sp->mesh->ctx->device);
+  cudaSetDevice(sp->ref.c->device);
   delete sp;
   return LFG_OK;
 }

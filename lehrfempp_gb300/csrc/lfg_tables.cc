@@ -5,11 +5,18 @@
 // uscalfe/precomputed_scalar_reference_finite_element.h:43-184).
 #include <cmath>
 
-#include "lfg_internal.h"
+#include "lfg_tables.h"
 
 namespace lfg {
 namespace {
 #include "tria_rules.inc"
+
+// binary32 pair of a long double value: hi rounded to nearest, lo the rest.
+void Split(long double v, float* dst) {
+  const float h = static_cast<float>(v);
+  dst[0] = h;
+  dst[1] = static_cast<float>(v - static_cast<long double>(h));
+}
 
 // Gauss-Legendre on [0,1] by Newton iteration on the Legendre recurrence
 // (the algorithm of quad/gauss_quadrature.cc:16-69), in long double.
@@ -167,6 +174,49 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
   phi[9] = 27.0 * l[0] * l[1] * l[2];
   for (int d = 0; d < 2; ++d)
     dphi[9][d] = 27.0 * (dl[0][d] * l[1] * l[2] + l[0] * dl[1][d] * l[2] + l[0] * l[1] * dl[2][d]);
+}
+
+bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& out, DfLayout& L) {
+  Rule r;
+  if (!MakeRule(quad, rule_degree, r)) return false;
+  L = DfLayout();
+  L.n = NumShape(quad, degree);
+  L.E = L.n * (L.n + 1) / 2;
+  L.nq = r.n;
+  L.m = quad ? rule_degree / 2 + 1 : 0;  // Gauss-Legendre points per direction (make_quad_rule.cc:28)
+  L.off_R = 0;
+  L.off_L = L.off_R + L.E * 4;
+  L.off_T = L.off_L + L.n;
+  L.off_W = L.off_T + (quad ? L.nq * L.E * 4 : 0);
+  L.off_t = L.off_W + L.nq;
+  L.total = L.off_t + L.m;
+  out.assign(2 * static_cast<size_t>(L.total), 0.0f);
+  std::vector<long double> R(L.E * 4, 0.0L), Ls(L.n, 0.0L);
+  double phi[16], dphi[16][2];
+  for (int k = 0; k < r.n; ++k) {
+    Shape(quad, degree, r.x[k], r.y[k], phi, dphi);
+    const long double w = r.w[k];
+    int e = 0;
+    for (int i = 0; i < L.n; ++i)
+      for (int j = i; j < L.n; ++j, ++e) {
+        const long double gi0 = dphi[i][0], gi1 = dphi[i][1], gj0 = dphi[j][0], gj1 = dphi[j][1];
+        const long double t[4] = {gi0 * gj0, gi0 * gj1 + gi1 * gj0, gi1 * gj1,
+                                  static_cast<long double>(phi[i]) * phi[j]};
+        for (int q = 0; q < 4; ++q) {
+          R[4 * e + q] += w * t[q];
+          if (quad) Split(t[q], &out[2 * (L.off_T + (k * L.E + e) * 4 + q)]);
+        }
+      }
+    for (int i = 0; i < L.n; ++i) Ls[i] += w * phi[i];
+    if (quad) Split(w, &out[2 * (L.off_W + k)]);
+  }
+  for (int q = 0; q < L.E * 4; ++q) Split(R[q], &out[2 * (L.off_R + q)]);
+  for (int i = 0; i < L.n; ++i) Split(Ls[i], &out[2 * (L.off_L + i)]);
+  if (quad) {
+    // 1D abscissae: the x coordinate of points (p, 0), p = 0..m-1
+    for (int p = 0; p < L.m; ++p) Split(r.x[p * L.m], &out[2 * (L.off_t + p)]);
+  }
+  return true;
 }
 
 }  // namespace lfg

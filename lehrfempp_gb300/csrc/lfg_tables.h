@@ -1,0 +1,32 @@
+// Reference-element data built on the host (no CUDA dependency): quadrature
+// rules, Lagrangian shape functions and the df32 (binary32-pair) tables of
+// the element kernels.
+#pragma once
+
+#include <vector>
+
+namespace lfg {
+
+struct Rule {
+  int n = 0;
+  std::vector<double> x, y, w;
+};
+// make_QuadRule (quad/make_quad_rule.cc:21-157): triangles from the
+// reference's tables (degree <= 8, 3 -> 4), quads tensor Gauss-Legendre with
+// degree/2+1 points per direction, x slow / y fast.  False if not available.
+bool MakeRule(bool is_quad, int degree, Rule& out);
+int NumShape(bool is_quad, int degree);
+void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]);
+
+// df32 tables (pairs of floats; offsets in pairs):
+//   R[E][4]    folded sums sum_k w_k {g_i0 g_j0, g_i0 g_j1 + g_i1 g_j0, g_i1 g_j1, phi_i phi_j}
+//   L[n]       folded load sums sum_k w_k phi_i
+//   T[nq][E][4] the same terms per point (no weight)      (quads)
+//   W[nq]      point weights,  t[m] 1D abscissae            (quads)
+struct DfLayout {
+  int n = 0, E = 0, nq = 0, m = 0;
+  int off_R = 0, off_L = 0, off_T = 0, off_W = 0, off_t = 0, total = 0;
+};
+bool BuildDfTables(bool is_quad, int degree, int rule_degree, std::vector<float>& out, DfLayout& L);
+
+}  // namespace lfg

@@ -145,6 +145,24 @@ def test_matrix_parity_all_elements(ctx, degree, quad, coef):
     assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
 
 
+@pytest.mark.parametrize("degree", [1, 2, 3])
+def test_fp64_route_for_out_of_range_cells(ctx, degree):
+    """Cells whose coefficients fall outside the df32 range (|alpha| > 2^40 or
+    < 2^-40) are computed by the FP64 formula inside the same kernels."""
+    xy, cells = W.hybrid_mesh(10, seed=3)
+    rng = np.random.default_rng(1)
+    alpha = np.exp(rng.standard_normal(len(cells)))
+    alpha[::3] *= 1e14
+    alpha[1::5] *= 1e-14
+    gamma = np.exp(rng.standard_normal(len(cells)))
+    gamma[::4] *= 1e15
+    wl = {"mesh": {"kind": "factory", "xy": xy, "cells": cells, "edges": None}, "degree": degree,
+          "alpha": ("cell", alpha), "gamma": ("cell", gamma), "f": ("const", 1.0), "qr_tria": 0, "qr_quad": 0}
+    r = Run(ctx, wl)
+    ro, co, vo = r.oracle_matrix().arrays()
+    compare_triplets(r.gpu_matrix().triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
+
+
 def test_append_semantics(ctx):
     """AssembleMatrixLocally appends to the triplets already in the matrix."""
     r = Run(ctx, W.config1(8))
@@ -333,6 +351,21 @@ def test_errors(ctx):
     # the context is still usable afterwards
     L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO)), coo)
     assert len(coo) == s.num_triplets
+
+
+def test_handles_outlive_context():
+    """Destroying the context before its meshes / matrices is safe: the
+    context is freed when the last handle is released."""
+    c = L.Context(0)
+    mesh = L.Mesh.tp_triag(c, 4, 4)
+    space = L.Space.lagrange(mesh, 2)
+    coo = L.COOMatrix(c, space.num_dofs, space.num_dofs, space.num_triplets)
+    L.assemble_matrix_rd(space, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO)), coo)
+    csr = coo.make_sparse()
+    c.close()
+    del csr, coo, space, mesh
+    import gc
+    gc.collect()
 
 
 def test_not_converged_status(ctx):
