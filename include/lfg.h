@@ -173,7 +173,8 @@ enum {
   LFG_COEFF_CONSTANT = 1,
   LFG_COEFF_PER_CELL = 2,
   LFG_COEFF_NODAL_O1 = 3,
-  LFG_COEFF_ANALYTIC = 4
+  LFG_COEFF_ANALYTIC = 4,
+  LFG_COEFF_PER_CELL_EXP = 5  /* exp(data_dev[cell]): a per-cell log-coefficient */
 };
 enum { LFG_FN_POLY = 1, LFG_FN_SINSIN = 2, LFG_FN_SINCOS = 3 };
 
@@ -307,6 +308,107 @@ lfg_status lfg_solve_pcg(lfg_csr* csr, const double* b_dev, double* x_dev,
  * stream capture. */
 lfg_status lfg_solve_pcg_noalloc(lfg_csr* csr, const double* b_dev, double* x_dev,
                                  const lfg_solve_opts* opts, lfg_solve_stats* stats);
+
+/* ------------------------------------------------------ differentiation
+ * No reference counterpart (the reference has no derivatives).  For
+ * J(theta) = 1/2 ||u - u_obs||^2 and A(theta) u = b after
+ * FixFlaggedSolutionComponents (free block A_ff, identity on flagged dofs,
+ * b_f -= A_fd g), the adjoint lambda solves A lambda = u - u_obs and
+ *   dJ/dtheta_c = - sum_{i free, j} lambda_i (dA_K/dtheta_c)_ij u_j ,
+ * the sum over the dofs of cell c; u_j at flagged dofs is the Dirichlet
+ * value g_j.  Only the diffusion part of A_K depends on theta:
+ *   alpha = exp(theta_c) (LFG_COEFF_PER_CELL_EXP): dA_K/dtheta_c = alpha_c S_K,
+ *   alpha = theta_c      (LFG_COEFF_PER_CELL):     dA_K/dtheta_c = S_K,
+ * with S_K the element stiffness matrix for alpha = 1 (with gamma = 0 and
+ * alpha = exp(theta) this is A_K itself).  Other alpha kinds: LFG_UNSUPPORTED.
+ * lfg_loss_l2_misfit: J (host, deterministic reduction) and dJ/du = u - u_obs
+ * (device; skipped when misfit_dev is NULL), FP64.
+ * lfg_grad_rd_cellwise: grad_dev[c] for every cell, lambda taken as zero at
+ * dofs with fixed_flags_dev[i] != 0 (NULL: no flagged dofs); FP64
+ * arithmetic and accumulation, one value per cell (no atomics). */
+lfg_status lfg_loss_l2_misfit(lfg_ctx* ctx, int64_t n, const double* u_dev, const double* u_obs_dev,
+                              double* loss_host, double* misfit_dev);
+lfg_status lfg_grad_rd_cellwise(lfg_space* space, const lfg_rd_provider* provider,
+                                const double* u_dev, const double* lambda_dev,
+                                const uint8_t* fixed_flags_dev, double* grad_dev);
+
+/* Forward/backward Function object of theta -> J (the autograd.Function
+ * contract: forward(theta) returns J and saves what backward needs;
+ * backward(dL/dJ) returns dL/dtheta = dL/dJ * dJ/dtheta).
+ *   forward : A(theta) = AssembleMatrixLocally(ReactionDiffusion(exp(theta), 0)),
+ *             b = AssembleVectorLocally(load), FixFlaggedSolutionComponents,
+ *             PCG solve A u = b, J = 1/2 ||u - u_obs||^2.
+ *   backward: adjoint PCG solve A lambda = (u - u_obs) on free dofs, then
+ *             lfg_grad_rd_cellwise scaled by dL/dJ.
+ * recompute = 0 keeps the Galerkin matrix, u and u - u_obs between the two
+ * calls; recompute = 1 keeps only a copy of theta (8 bytes per cell) and
+ * backward re-assembles and re-solves for u first (the memory-saving mode).
+ * The space must outlive the object.  Backward before any forward is
+ * LFG_INVALID_ARG; backward may run more than once after one forward. */
+typedef struct lfg_rd_adjoint lfg_rd_adjoint;
+typedef struct {
+  lfg_load_provider load;        /* right-hand side f and its rules */
+  int32_t qr_degree_tria;        /* rules of the stiffness matrix (0 = 2 * degree) */
+  int32_t qr_degree_quad;
+  const uint8_t* flags_dev;      /* Dirichlet dofs (NULL: boundary dofs of the space) */
+  const double* dirichlet_dev;   /* values at flagged dofs, length num_dofs (NULL: 0) */
+  lfg_solve_opts solve;          /* forward and adjoint PCG */
+  int32_t recompute;
+} lfg_rd_adjoint_opts;
+lfg_status lfg_rd_adjoint_create(lfg_space* space, const lfg_rd_adjoint_opts* opts,
+                                 const double* u_obs_dev, lfg_rd_adjoint** out);
+lfg_status lfg_rd_adjoint_destroy(lfg_rd_adjoint* f);
+/* theta_dev: num_cells log-coefficients.  u_out_dev (may be NULL) receives u. */
+lfg_status lfg_rd_adjoint_forward(lfg_rd_adjoint* f, const double* theta_dev, double* loss_host,
+                                  double* u_out_dev);
+lfg_status lfg_rd_adjoint_backward(lfg_rd_adjoint* f, double grad_loss, double* grad_theta_dev);
+/* Solver statistics of the last forward (u) and adjoint (lambda) solves;
+ * saved_bytes: device memory held between forward and backward. */
+lfg_status lfg_rd_adjoint_stats(const lfg_rd_adjoint* f, lfg_solve_stats* forward,
+                                lfg_solve_stats* adjoint, int64_t* saved_bytes);
+
+/* ---------------------------------------------------------- batched form
+ * Many independent problems (no reference counterpart: the reference loops
+ * over problems one at a time, each with AssembleMatrixLocally + SparseLU).
+ * A batch is a list of spaces (each on its own mesh) viewed as one
+ * block-diagonal system: mesh b's dofs occupy global rows
+ * [dof_offset[b], dof_offset[b+1]) and its triplets the range
+ * [triplet_offset[b], triplet_offset[b+1]) of a batch COO, in exactly the
+ * order AssembleMatrixLocally gives for that mesh alone, with row/col shifted
+ * by dof_offset[b].  Batch-wide coefficient arrays are indexed by batch cell
+ * (cell_offset[b] + local cell). */
+typedef struct lfg_batch lfg_batch;
+lfg_status lfg_batch_create(lfg_ctx* ctx, int32_t num_spaces, lfg_space* const* spaces,
+                            lfg_batch** out);
+lfg_status lfg_batch_destroy(lfg_batch* batch);
+lfg_status lfg_batch_info(const lfg_batch* batch, int32_t* num_spaces, int64_t* total_dofs,
+                          int64_t* total_cells, int64_t* total_triplets);
+/* Host copies of the offset arrays (num_spaces + 1 entries each, any may be NULL). */
+lfg_status lfg_batch_offsets(const lfg_batch* batch, int64_t* dof_offset, int64_t* cell_offset,
+                             int64_t* triplet_offset);
+/* All element matrices of all meshes in one persistent launch (cells with
+ * constant / per-cell alpha and gamma; triangles).  Appends total_triplets
+ * to coo (global indices).  The first call tunes the launch shape (threads
+ * per CTA, CTAs per SM) by timing the candidates on this batch; the choice is
+ * kept in the batch (lfg_batch_tuning). */
+lfg_status lfg_batch_assemble_matrix_rd(lfg_batch* batch, const lfg_rd_provider* provider,
+                                        lfg_coo* coo);
+lfg_status lfg_batch_tuning(const lfg_batch* batch, int32_t* threads_per_cta, int32_t* ctas_per_sm,
+                            double* best_ms);
+/* AssembleVectorLocally of every mesh into b_dev[total_dofs] (global rows). */
+lfg_status lfg_batch_assemble_vector_load(lfg_batch* batch, const lfg_load_provider* provider,
+                                          double* b_dev);
+/* Boundary-dof selector of every mesh, flags_dev[total_dofs]. */
+lfg_status lfg_batch_boundary_dof_flags(lfg_batch* batch, uint8_t* flags_dev);
+/* Batched PCG: one independent Jacobi-PCG per block of the block-diagonal
+ * CSR (each with its own step lengths and stopping test), all advanced
+ * together by the same kernels, replayed from a CUDA graph.  precision FP64 or
+ * MIXED (FP32 inner iterations, FP64 residual refinement).  per_block_stats
+ * (num_spaces entries, may be NULL) and the summary stats (iterations = the
+ * longest block, converged = all blocks). */
+lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const double* b_dev,
+                               double* x_dev, const lfg_solve_opts* opts, lfg_solve_stats* stats,
+                               lfg_solve_stats* per_block_stats);
 
 #ifdef __cplusplus
 }

@@ -21,7 +21,7 @@ import threading
 import numpy as np
 
 from . import _capi
-from ._capi import (lfg_coeff, lfg_load_provider, lfg_rd_provider, lfg_solve_opts, lfg_solve_stats,
+from ._capi import (lfg_rd_adjoint_opts, lfg_coeff, lfg_load_provider, lfg_rd_provider, lfg_solve_opts, lfg_solve_stats,
                     lfg_triplet)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -36,7 +36,7 @@ STATUS_NAMES = ["OK", "INVALID_ARG", "DEGENERATE_CELL", "CAPACITY", "UNSUPPORTED
                 "CUDA_ERROR", "MISSING_RULE", "INCOMPLETE_MESH", "OUT_OF_MEMORY"]
 
 # coefficient kinds and analytic families
-ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC = 0, 1, 2, 3, 4
+ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
 FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 
@@ -307,6 +307,16 @@ class Mesh:
         self.ctx.check(lib().lfg_mesh_device_arrays(self.h, C.byref(xy), C.byref(cells)))
         return xy, cells
 
+    def geometry(self):
+        """(xy[num_nodes, 2] float64, cells[num_cells, 4] int32; -1 pads triangles)."""
+        dxy, dcells = self.device_arrays()
+        xy = np.zeros((self.num_nodes, 2), np.float64)
+        cells = np.zeros((self.num_cells, 4), np.int32)
+        self.ctx.check(lib().lfg_memcpy_d2h(self.ctx.h, xy.ctypes.data_as(C.c_void_p), dxy, xy.nbytes))
+        self.ctx.check(lib().lfg_memcpy_d2h(self.ctx.h, cells.ctypes.data_as(C.c_void_p), dcells, cells.nbytes))
+        self.ctx.synchronize()
+        return xy, cells
+
 
 class Space:
     """UniformFEDofHandler; Space.lagrange(mesh, p) = FeSpaceLagrangeO<p>."""
@@ -459,6 +469,65 @@ class CSRMatrix:
                 "converged": bool(st.converged)}
 
 
+class Batch:
+    """Many independent spaces viewed as one block-diagonal system (lfg_batch)."""
+
+    def __init__(self, ctx, spaces):
+        self.ctx = ctx
+        self.spaces = list(spaces)  # keep the spaces (and meshes) alive
+        arr = (C.c_void_p * len(self.spaces))(*[s.h.value for s in self.spaces])
+        self.h = C.c_void_p()
+        ctx.check(lib().lfg_batch_create(ctx.h, len(self.spaces), arr, C.byref(self.h)))
+        n, d, c, t = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int64()
+        ctx.check(lib().lfg_batch_info(self.h, C.byref(n), C.byref(d), C.byref(c), C.byref(t)))
+        self.num_spaces, self.num_dofs, self.num_cells, self.num_triplets = n.value, d.value, c.value, t.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_batch_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def offsets(self):
+        n = self.num_spaces + 1
+        d, c, t = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n, np.int64)
+        self.ctx.check(lib().lfg_batch_offsets(self.h, _p(d, C.c_int64), _p(c, C.c_int64), _p(t, C.c_int64)))
+        return d, c, t
+
+    def assemble_matrix_rd(self, provider, coo):
+        self.ctx.check(lib().lfg_batch_assemble_matrix_rd(self.h, C.byref(provider), coo.h))
+
+    def tuning(self):
+        th, ct, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self.ctx.check(lib().lfg_batch_tuning(self.h, C.byref(th), C.byref(ct), C.byref(ms)))
+        return th.value, ct.value, ms.value
+
+    def assemble_vector_load(self, provider, b):
+        self.ctx.check(lib().lfg_batch_assemble_vector_load(self.h, C.byref(provider), b.ptr))
+
+    def boundary_dof_flags(self):
+        f = self.ctx.empty(self.num_dofs, np.uint8)
+        self.ctx.check(lib().lfg_batch_boundary_dof_flags(self.h, f.ptr))
+        return f
+
+    def solve_pcg(self, csr, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=1e-4,
+                  check_every=32, raise_on_failure=True):
+        o = lfg_solve_opts()
+        o.precision, o.rtol, o.max_iterations, o.inner_rtol, o.check_every = (precision, rtol, max_iterations,
+                                                                             inner_rtol, check_every)
+        st = lfg_solve_stats()
+        per = (lfg_solve_stats * self.num_spaces)()
+        rc = lib().lfg_batch_solve_pcg(self.h, csr.h, b.ptr, x.ptr, C.byref(o), C.byref(st), per)
+        if rc != OK and (raise_on_failure or rc != NOT_CONVERGED):
+            self.ctx.check(rc)
+        blocks = [{"iterations": p.iterations, "refinements": p.refinements, "rel_residual": p.rel_residual,
+                   "converged": bool(p.converged)} for p in per]
+        return {"iterations": st.iterations, "refinements": st.refinements, "rel_residual": st.rel_residual,
+                "converged": bool(st.converged), "blocks": blocks}
+
+
 def rd_provider(alpha, gamma, qr_degree_tria=0, qr_degree_quad=0):
     p = lfg_rd_provider()
     p.alpha, p.gamma = alpha, gamma
@@ -487,3 +556,62 @@ def assemble_matrix_tabulated(space, elem_dev, ld, coo):
 
 def assemble_vector_tabulated(space, vec_dev, ld, b):
     space.ctx.check(lib().lfg_assemble_vector_tabulated(space.h, vec_dev.ptr, ld, b.ptr))
+
+
+def loss_l2_misfit(ctx, u, u_obs, misfit=None):
+    """J = 1/2 ||u - u_obs||^2 (returned) and, if given, misfit = u - u_obs."""
+    out = C.c_double()
+    ctx.check(lib().lfg_loss_l2_misfit(ctx.h, u.size, u.ptr, u_obs.ptr, C.byref(out),
+                                       misfit.ptr if misfit is not None else None))
+    return out.value
+
+
+def grad_rd_cellwise(space, provider, u, lam, flags, grad):
+    """grad[c] = -lambda_K^T (dA_K/dtheta_c) u_K, lambda zero at flagged dofs."""
+    space.ctx.check(lib().lfg_grad_rd_cellwise(space.h, C.byref(provider), u.ptr, lam.ptr,
+                                               flags.ptr if flags is not None else None, grad.ptr))
+
+
+class RDAdjoint:
+    """theta -> J = 1/2 ||u(theta) - u_obs||^2 as a forward/backward Function
+    object (lfg_rd_adjoint_*): alpha = exp(theta) per cell, gamma = 0."""
+
+    def __init__(self, space, u_obs, load, qr_degree_tria=0, qr_degree_quad=0, flags=None, dirichlet=None,
+                 precision=SOLVE_FP64, rtol=1e-12, max_iterations=200000, inner_rtol=1e-4, check_every=32,
+                 recompute=False):
+        self.ctx = space.ctx
+        self.space = space  # must outlive the object
+        o = lfg_rd_adjoint_opts()
+        o.load = load
+        o.qr_degree_tria, o.qr_degree_quad = qr_degree_tria, qr_degree_quad
+        o.flags_dev = flags.ptr if flags is not None else None
+        o.dirichlet_dev = dirichlet.ptr if dirichlet is not None else None
+        o.solve.precision, o.solve.rtol, o.solve.max_iterations = precision, rtol, max_iterations
+        o.solve.inner_rtol, o.solve.check_every = inner_rtol, check_every
+        o.recompute = 1 if recompute else 0
+        self.h = C.c_void_p()
+        self.ctx.check(lib().lfg_rd_adjoint_create(space.h, C.byref(o), u_obs.ptr, C.byref(self.h)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_rd_adjoint_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def forward(self, theta, u_out=None):
+        loss = C.c_double()
+        self.ctx.check(lib().lfg_rd_adjoint_forward(self.h, theta.ptr, C.byref(loss),
+                                                    u_out.ptr if u_out is not None else None))
+        return loss.value
+
+    def backward(self, grad_theta, grad_loss=1.0):
+        self.ctx.check(lib().lfg_rd_adjoint_backward(self.h, float(grad_loss), grad_theta.ptr))
+
+    def stats(self):
+        f, a, n = lfg_solve_stats(), lfg_solve_stats(), C.c_int64()
+        self.ctx.check(lib().lfg_rd_adjoint_stats(self.h, C.byref(f), C.byref(a), C.byref(n)))
+        cv = lambda st: {"iterations": st.iterations, "refinements": st.refinements,
+                         "rel_residual": st.rel_residual, "converged": bool(st.converged)}
+        return {"forward": cv(f), "adjoint": cv(a), "saved_bytes": n.value}

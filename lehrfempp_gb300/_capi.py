@@ -41,6 +41,11 @@ class lfg_solve_stats(C.Structure):
     _fields_ = [("iterations", i32), ("refinements", i32), ("rel_residual", dbl), ("converged", i32)]
 
 
+class lfg_rd_adjoint_opts(C.Structure):
+    _fields_ = [("load", lfg_load_provider), ("qr_degree_tria", i32), ("qr_degree_quad", i32),
+                ("flags_dev", vp), ("dirichlet_dev", vp), ("solve", lfg_solve_opts), ("recompute", i32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "lfg_ctx_create": (c_status, [C.c_int, P(vp)]),
@@ -101,6 +106,22 @@ SIGNATURES = {
     "lfg_csr_spmv": (c_status, [vp, vp, vp]),
     "lfg_solve_pcg": (c_status, [vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats)]),
     "lfg_solve_pcg_noalloc": (c_status, [vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats)]),
+    "lfg_loss_l2_misfit": (c_status, [vp, i64, vp, vp, P(dbl), vp]),
+    "lfg_grad_rd_cellwise": (c_status, [vp, P(lfg_rd_provider), vp, vp, vp, vp]),
+    "lfg_rd_adjoint_create": (c_status, [vp, P(lfg_rd_adjoint_opts), vp, P(vp)]),
+    "lfg_rd_adjoint_destroy": (c_status, [vp]),
+    "lfg_rd_adjoint_forward": (c_status, [vp, vp, P(dbl), vp]),
+    "lfg_rd_adjoint_backward": (c_status, [vp, dbl, vp]),
+    "lfg_rd_adjoint_stats": (c_status, [vp, P(lfg_solve_stats), P(lfg_solve_stats), P(i64)]),
+    "lfg_batch_create": (c_status, [vp, i32, P(vp), P(vp)]),
+    "lfg_batch_destroy": (c_status, [vp]),
+    "lfg_batch_info": (c_status, [vp, P(i32), P(i64), P(i64), P(i64)]),
+    "lfg_batch_offsets": (c_status, [vp, P(i64), P(i64), P(i64)]),
+    "lfg_batch_assemble_matrix_rd": (c_status, [vp, P(lfg_rd_provider), vp]),
+    "lfg_batch_tuning": (c_status, [vp, P(i32), P(i32), P(dbl)]),
+    "lfg_batch_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
+    "lfg_batch_boundary_dof_flags": (c_status, [vp, vp]),
+    "lfg_batch_solve_pcg": (c_status, [vp, vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats), P(lfg_solve_stats)]),
 }
 
 

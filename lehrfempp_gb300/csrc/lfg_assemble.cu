@@ -54,7 +54,8 @@ Tab TabLayout(int n, int nq) {
   t.off_R = t.off_T + nq * t.E * 4;
   t.off_L = t.off_R + t.E * 4;
   t.off_o1 = t.off_L + n;
-  t.total = t.off_o1 + nq * 4;
+  t.off_G = t.off_o1 + nq * 4;  // reference gradients [nq][n][2]
+  t.total = t.off_G + nq * n * 2;
   return t;
 }
 
@@ -112,6 +113,7 @@ __device__ double EvalCoeff(const CoeffDev& f, int c, const int4& cn, const doub
     case LFG_COEFF_ZERO: return 0.0;
     case LFG_COEFF_CONSTANT: return f.value;
     case LFG_COEFF_PER_CELL: return f.data[c];
+    case LFG_COEFF_PER_CELL_EXP: return exp(f.data[c]);
     case LFG_COEFF_NODAL_O1: {
       double s = f.data[cn.x] * so1[k * 4 + 0];
       s += f.data[cn.y] * so1[k * 4 + 1];
@@ -138,7 +140,12 @@ __device__ double EvalCoeff(const CoeffDev& f, int c, const int4& cn, const doub
 }
 
 __device__ __forceinline__ double CellConst(const CoeffDev& f, int c) {
-  return f.kind == LFG_COEFF_CONSTANT ? f.value : f.kind == LFG_COEFF_PER_CELL ? f.data[c] : 0.0;
+  switch (f.kind) {
+    case LFG_COEFF_CONSTANT: return f.value;
+    case LFG_COEFF_PER_CELL: return f.data[c];
+    case LFG_COEFF_PER_CELL_EXP: return exp(f.data[c]);
+  }
+  return 0.0;
 }
 
 template <bool QUAD>
@@ -508,6 +515,107 @@ __global__ void TabulatedVectorKernel(int64_t nc, const int64_t* __restrict__ lo
   }
 }
 
+// ---------------------------------------------------------- differentiation
+// grad[c] = -scale_c * sum_k w_k (G_k lambda)^T (|det J_k| J_k^{-1} J_k^{-T}) (G_k u)
+// with G_k lambda = sum_i lambda_i grad(phi_hat_i)(q_k) (reference gradients)
+// and scale_c = exp(theta_c) or 1.  This is -lambda_K^T (dA_K/dtheta_c) u_K
+// without forming A_K: 4n + 6 FP64 operations per point instead of the
+// n^2-entry element matrix.  Flagged dofs contribute lambda_i = 0.
+template <int DEG, bool QUAD>
+__global__ void __launch_bounds__(128) GradRDKernel(AsmArgs a, const double* __restrict__ u,
+                                                    const double* __restrict__ lam,
+                                                    const uint8_t* __restrict__ flags, double gscale,
+                                                    double* __restrict__ grad) {
+  constexpr int N = QUAD ? (DEG + 1) * (DEG + 1) : (DEG + 1) * (DEG + 2) / 2;
+  extern __shared__ double sm[];
+  const int nq = a.L.nq;
+  double* sw = sm;
+  double* sqx = sw + nq;
+  double* sqy = sqx + nq;
+  double* sG = sqy + nq;
+  for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+    sw[i] = a.tab[a.L.off_w + i];
+    sqx[i] = a.tab[a.L.off_qx + i];
+    sqy[i] = a.tab[a.L.off_qy + i];
+  }
+  for (int i = threadIdx.x; i < nq * N * 2; i += blockDim.x) sG[i] = a.tab[a.L.off_G + i];
+  __syncthreads();
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < a.count;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = a.bucket[t];
+    int4 cn;
+    double2 v[4];
+    LoadVerts<QUAD>(a, c, cn, v);
+    double uk[N], lk[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const int d = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      uk[i] = u[d];
+      lk[i] = (flags && flags[d]) ? 0.0 : lam[d];
+    }
+    double m00 = 0, m01 = 0, m11 = 0, adet = 0;
+    if (!QUAD) TriaMetric(v, m00, m01, m11, adet);
+    double s = 0.0;
+    for (int k = 0; k < nq; ++k) {
+      if (QUAD) QuadMetric(v, sqx[k], sqy[k], m00, m01, m11, adet);
+      const double* g = sG + k * N * 2;
+      double gu0 = 0, gu1 = 0, gl0 = 0, gl1 = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        gu0 = fma(uk[i], g[2 * i], gu0);
+        gu1 = fma(uk[i], g[2 * i + 1], gu1);
+        gl0 = fma(lk[i], g[2 * i], gl0);
+        gl1 = fma(lk[i], g[2 * i + 1], gl1);
+      }
+      double q = m00 * gl0 * gu0;
+      q = fma(m01, fma(gl0, gu1, gl1 * gu0), q);
+      q = fma(m11 * gl1, gu1, q);
+      s = fma(sw[k], q, s);
+    }
+    const double scale = a.alpha.kind == LFG_COEFF_PER_CELL_EXP ? exp(a.alpha.data[c]) : 1.0;
+    grad[c] = -gscale * scale * s;
+  }
+}
+
+// Deterministic 1/2 sum (u - u_obs)^2: fixed chunks of kMisfitChunk entries,
+// each summed by one block in a fixed order, then one block over the chunks.
+constexpr int kMisfitChunk = 8192;
+
+__global__ void __launch_bounds__(256) MisfitKernel(int64_t n, const double* __restrict__ u,
+                                                    const double* __restrict__ uo, double* __restrict__ r,
+                                                    double* __restrict__ part) {
+  __shared__ double red[256];
+  const int64_t b0 = static_cast<int64_t>(blockIdx.x) * kMisfitChunk;
+  const int64_t b1 = b0 + kMisfitChunk < n ? b0 + kMisfitChunk : n;
+  double s = 0.0;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += 256) {
+    const double d = u[i] - uo[i];
+    if (r) r[i] = d;
+    s = fma(d, d, s);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(256) SumPartsKernel(int64_t m, const double* __restrict__ part,
+                                                      double scale, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = scale * red[0];
+}
+
 // ------------------------------------------------------------------ host side
 
 void BuildTable(bool quad, int degree, int rule_degree, std::vector<double>& h, Tab& L) {
@@ -527,6 +635,10 @@ void BuildTable(bool quad, int degree, int rule_degree, std::vector<double>& h, 
     Shape(quad, degree, r.x[k], r.y[k], phi, dphi);
     Shape(quad, 1, r.x[k], r.y[k], p1, d1);
     for (int i = 0; i < n; ++i) h[L.off_phi + k * n + i] = phi[i];
+    for (int i = 0; i < n; ++i) {
+      h[L.off_G + (k * n + i) * 2 + 0] = dphi[i][0];
+      h[L.off_G + (k * n + i) * 2 + 1] = dphi[i][1];
+    }
     for (int i = 0; i < (quad ? 4 : 3); ++i) h[L.off_o1 + k * 4 + i] = p1[i];
     int e = 0;
     for (int i = 0; i < n; ++i)
@@ -601,9 +713,10 @@ CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
   d.value = c.value;
   d.data = c.data_dev;
   for (int i = 0; i < 16; ++i) d.p[i] = c.p[i];
-  if (c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_ANALYTIC)
+  if (c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_PER_CELL_EXP)
     Fail(LFG_UNSUPPORTED, std::string(what) + ": unsupported coefficient kind");
-  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1) && !c.data_dev)
+  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1 || c.kind == LFG_COEFF_PER_CELL_EXP) &&
+      !c.data_dev)
     Fail(LFG_INVALID_ARG, std::string(what) + ": coefficient data pointer is null");
   if (c.kind == LFG_COEFF_ANALYTIC && (c.func < LFG_FN_POLY || c.func > LFG_FN_SINCOS))
     Fail(LFG_UNSUPPORTED, std::string(what) + ": unknown analytic function");
@@ -611,7 +724,8 @@ CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
 }
 
 bool Uniform(const lfg_coeff& c) {
-  return c.kind == LFG_COEFF_ZERO || c.kind == LFG_COEFF_CONSTANT || c.kind == LFG_COEFF_PER_CELL;
+  return c.kind == LFG_COEFF_ZERO || c.kind == LFG_COEFF_CONSTANT || c.kind == LFG_COEFF_PER_CELL ||
+         c.kind == LFG_COEFF_PER_CELL_EXP;
 }
 
 template <class K, class... Args>
@@ -731,6 +845,40 @@ void LoadElementVectors(lfg_space* sp, const lfg_load_provider* pr, double* ev) 
   }
 }
 
+// grad[c] = -gscale * lambda_K^T (dA_K/dtheta_c) u_K for every cell (the
+// differentiation entry point and the adjoint Function object share it).
+void GradRDCellwise(lfg_space* sp, const lfg_rd_provider* pr, const double* u, const double* lam,
+                    const uint8_t* flags, double gscale, double* grad) {
+  if (!pr || !u || !lam || !grad) Fail(LFG_INVALID_ARG, "lfg_grad_rd_cellwise: null argument");
+  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "gradient needs a Lagrangian space");
+  if (pr->alpha.kind != LFG_COEFF_PER_CELL && pr->alpha.kind != LFG_COEFF_PER_CELL_EXP)
+    Fail(LFG_UNSUPPORTED, "gradient: alpha must be a per-cell (or per-cell exp) coefficient");
+  lfg_mesh* m = sp->mesh;
+  lfg_ctx* ctx = m->ctx;
+  if (m->ntria && pr->qr_degree_tria < 0) Fail(LFG_MISSING_RULE, "no quadrature rule for triangles");
+  if (m->nquad && pr->qr_degree_quad < 0) Fail(LFG_MISSING_RULE, "no quadrature rule for quadrilaterals");
+  AsmArgs a = BaseArgs(sp);
+  a.alpha = ToDev(pr->alpha, m, "alpha");
+  const int deg = sp->degree;
+  ProfScope prof(ctx, "grad_rd");
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool quad = pass == 1;
+    a.count = quad ? m->nquad : m->ntria;
+    if (!a.count) continue;
+    a.tab = GetTable(sp, quad, deg, RuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, deg), a.L);
+    a.bucket = quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
+    const size_t smem = static_cast<size_t>(a.L.nq) * (3 + 2 * a.L.n) * sizeof(double);
+    switch (deg * 2 + (quad ? 1 : 0)) {
+      case 2: Launch(GradRDKernel<1, false>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+      case 3: Launch(GradRDKernel<1, true>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+      case 4: Launch(GradRDKernel<2, false>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+      case 5: Launch(GradRDKernel<2, true>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+      case 6: Launch(GradRDKernel<3, false>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+      case 7: Launch(GradRDKernel<3, true>, ctx, a.count, smem, 128, a, u, lam, flags, gscale, grad); break;
+    }
+  }
+}
+
 }  // namespace lfg
 
 using namespace lfg;
@@ -821,6 +969,36 @@ lfg_status lfg_assemble_vector_tabulated(lfg_space* sp, const double* vec, int32
   GatherVectorKernel<<<GridFor(ctx, sp->num_dofs, 256), 256, 0, ctx->stream>>>(
       sp->num_dofs, sp->inc_ptr.as<int64_t>(), sp->inc_slot.as<uint64_t>(), sp->scratch_vec.as<double>(), b);
   LFG_LAUNCHED(ctx);
+  LFG_API_END
+}
+
+lfg_status lfg_loss_l2_misfit(lfg_ctx* ctx, int64_t n, const double* u, const double* u_obs, double* loss,
+                              double* misfit) {
+  if (!ctx) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(ctx)
+  if (n < 0 || (n > 0 && (!u || !u_obs)) || !loss) Fail(LFG_INVALID_ARG, "lfg_loss_l2_misfit: bad argument");
+  const int64_t parts = n == 0 ? 1 : (n + kMisfitChunk - 1) / kMisfitChunk;
+  DevBuf part;
+  part.alloc((parts + 1) * sizeof(double), ctx->stream);
+  double* p = part.as<double>();
+  if (n == 0) {
+    LFG_CUDA(cudaMemsetAsync(p, 0, sizeof(double), ctx->stream));
+  } else {
+    ProfScope prof(ctx, "misfit");
+    MisfitKernel<<<static_cast<unsigned>(parts), 256, 0, ctx->stream>>>(n, u, u_obs, misfit, p);
+    LFG_LAUNCHED(ctx);
+  }
+  SumPartsKernel<<<1, 256, 0, ctx->stream>>>(parts, p, 0.5, p + parts);
+  LFG_LAUNCHED(ctx);
+  D2HSync(ctx, loss, p + parts, sizeof(double));
+  LFG_API_END
+}
+
+lfg_status lfg_grad_rd_cellwise(lfg_space* sp, const lfg_rd_provider* pr, const double* u, const double* lam,
+                                const uint8_t* flags, double* grad) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  GradRDCellwise(sp, pr, u, lam, flags, 1.0, grad);
   LFG_API_END
 }
 

@@ -1,0 +1,893 @@
+// Batched form: hundreds of independent meshes assembled in one persistent
+// launch and solved by one batched Jacobi-PCG replayed from a CUDA graph.
+//
+// The batch is viewed as one block-diagonal system.  Mesh b owns global rows
+// [dof_off[b], dof_off[b+1]) and the triplet range [trip_off[b], trip_off[b+1])
+// of the batch COO, filled in the order of AssembleMatrixLocally on mesh b
+// alone (assemble/assembler.h:114-186) with row/col shifted by dof_off[b].
+// The existing fix (lfg_fix_*) and COO->CSR (lfg_csr_from_coo) then act on
+// the whole batch at once; only assembly and the solve need batch awareness.
+//
+// Assembly: work items are tiles of T consecutive cells of one mesh (T =
+// threads per CTA); a persistent grid loops over the items, finds the item's
+// mesh by binary search in the tile prefix, and runs the df32 triangle body
+// for the mesh's degree (lfg_elem.h).  T and the CTAs per SM are chosen by
+// timing the candidates on the first call (the autotuner).
+//
+// Solve: rows are cut into chunks that never straddle two meshes; every PCG
+// kernel works chunk by chunk and every per-mesh scalar (step length,
+// direction update, residual) is a sum of that mesh's chunk partials in a
+// fixed order, so each block of the system follows exactly its own PCG.
+// Converged meshes are frozen (no more updates) while the others continue.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "lfg_api.h"
+#include "lfg_elem.h"
+#include "lfg_internal.h"
+
+namespace lfg {
+
+struct BatchMesh {
+  const double2* xy;
+  const int4* cells;
+  const int32_t* cell_dofs;
+  const int64_t* tri_offset;
+  int n_cell;
+  int degree;
+  int64_t ncells;
+  int64_t dof_off;
+  int64_t cell_off;
+  int64_t trip_off;
+};
+
+}  // namespace lfg
+
+struct lfg_batch {
+  lfg::CtxRef ref;
+  lfg_ctx* ctx = nullptr;
+  int nb = 0;
+  std::vector<lfg_space*> spaces;
+  std::vector<int64_t> dof_off, cell_off, trip_off;
+  lfg::DevBuf meshes;  // BatchMesh[nb]
+  int max_degree = 0;
+  // autotuning result
+  bool tuned = false;
+  int threads = 128, ctas_per_sm = 0;
+  double best_ms = 0.0;
+  // PCG chunks
+  lfg::DevBuf chunk_mesh, chunk_start, mesh_chunk_off;
+  int64_t nchunks = 0;
+  std::vector<int64_t> h_mesh_chunk_off;
+};
+
+namespace lfg {
+void EnsureIncidence(lfg_space* sp);
+namespace {
+
+using elem::f2;
+
+constexpr int kMaxBatchThreads = 256;
+
+struct BatchArgs {
+  const BatchMesh* meshes;
+  int nb;
+  const int64_t* tile_prefix;  // nb + 1
+  int64_t total_tiles;
+  lfg_triplet* out;
+  const double* alpha;  // per batch cell, or null (constant alpha_value)
+  double alpha_value;
+  const double* gamma;
+  double gamma_value;
+  const f2* tabs[4];    // df32 R tables per degree (index = degree)
+  const double* tabs64[4];  // FP64 R tables per degree
+  unsigned long long* fallback;
+};
+
+__device__ __forceinline__ void StoreTripletB(lfg_triplet* p, int r, int c, double v) {
+  const long long bits = __double_as_longlong(v);
+  *reinterpret_cast<int4*>(p) = make_int4(r, c, static_cast<int>(bits & 0xffffffffll), static_cast<int>(bits >> 32));
+}
+
+template <int N>
+__device__ __forceinline__ int UpperIdx(int i, int j) {
+  const int a = i < j ? i : j, b = i < j ? j : i;
+  return a * N - (a * (a - 1)) / 2 + (b - a);
+}
+
+template <int DEG, bool MASS>
+__device__ void BatchTile(const BatchArgs& A, const BatchMesh& m, int64_t first, int ncell, unsigned char* smem) {
+  constexpr int N = (DEG + 1) * (DEG + 2) / 2;
+  constexpr int E = N * (N + 1) / 2;
+  constexpr int NN = N * N;
+  const int T = blockDim.x;
+  double* svals = reinterpret_cast<double*>(smem);
+  int64_t* soff = reinterpret_cast<int64_t*>(svals + T * E);
+  int* sdofs = reinterpret_cast<int*>(soff + T);
+  if (threadIdx.x < ncell) {
+    const int64_t c = first + threadIdx.x;
+    const int4 cn = m.cells[c];
+    const double2 v0 = m.xy[cn.x], v1 = m.xy[cn.y], v2 = m.xy[cn.z];
+    const double jac[4] = {v1.x - v0.x, v2.x - v0.x, v1.y - v0.y, v2.y - v0.y};
+    const double al = A.alpha ? A.alpha[m.cell_off + c] : A.alpha_value;
+    const double ga = MASS ? (A.gamma ? A.gamma[m.cell_off + c] : A.gamma_value) : 0.0;
+    double* vals = svals + threadIdx.x * E;
+    if (elem::DfSafe(jac[0]) && elem::DfSafe(jac[1]) && elem::DfSafe(jac[2]) && elem::DfSafe(jac[3]) &&
+        elem::DfSafe(al) && elem::DfSafe(ga)) {
+      elem::TriaUniformDF<E, MASS>(jac, al, ga, A.tabs[DEG], vals);
+    } else {
+      elem::TriaUniformF64<E, MASS>(jac, al, ga, A.tabs64[DEG], vals);
+      atomicAdd(A.fallback, 1ull);
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      sdofs[threadIdx.x * N + i] = m.cell_dofs[c * m.n_cell + i] + static_cast<int>(m.dof_off);
+    soff[threadIdx.x] = m.trip_off + m.tri_offset[c];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < ncell * NN; q += T) {
+    const int cl = q / NN, w = q - cl * NN;
+    const int i = w / N, j = w - i * N;
+    StoreTripletB(A.out + soff[cl] + w, sdofs[cl * N + i], sdofs[cl * N + j], svals[cl * E + UpperIdx<N>(i, j)]);
+  }
+  __syncthreads();
+}
+
+template <bool MASS>
+__global__ void __launch_bounds__(kMaxBatchThreads) BatchAssembleKernel(BatchArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_mesh;
+  for (int64_t t = blockIdx.x; t < A.total_tiles; t += gridDim.x) {
+    if (threadIdx.x == 0) {  // mesh of this tile: last b with tile_prefix[b] <= t
+      int lo = 0, hi = A.nb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.tile_prefix[mid] <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      s_mesh = lo;
+    }
+    __syncthreads();
+    const BatchMesh m = A.meshes[s_mesh];
+    const int64_t first = (t - A.tile_prefix[s_mesh]) * blockDim.x;
+    const int64_t left = m.ncells - first;
+    const int ncell = static_cast<int>(left < blockDim.x ? left : blockDim.x);
+    __syncthreads();
+    switch (m.degree) {
+      case 1: BatchTile<1, MASS>(A, m, first, ncell, smem); break;
+      case 2: BatchTile<2, MASS>(A, m, first, ncell, smem); break;
+      case 3: BatchTile<3, MASS>(A, m, first, ncell, smem); break;
+    }
+  }
+}
+
+size_t StagePerCell(int degree) {
+  const int N = (degree + 1) * (degree + 2) / 2, E = N * (N + 1) / 2;
+  return E * 8 + 8 + N * 4;
+}
+
+// ------------------------------------------------------------ batched PCG
+constexpr int kChunk = 2048;
+constexpr int kPB = 256;  // threads per block of the PCG kernels
+constexpr int kLanes = 8;
+
+struct Chunks {
+  const int32_t* mesh;        // chunk -> mesh
+  const int64_t* start;       // chunk -> first row (nchunks + 1: start[nchunks] = total rows)
+  const int64_t* mesh_chunk;  // mesh -> first chunk (nb + 1)
+  int64_t nchunks;
+};
+
+__device__ double BlockReduce(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (blockDim.x >> 5); ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// sum of a mesh's chunk partials, in chunk order (thread 0), broadcast
+__device__ double MeshSum(const double* part, const Chunks& C, int b, double* sh) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int64_t c = C.mesh_chunk[b]; c < C.mesh_chunk[b + 1]; ++c) s += part[c];
+    *sh = s;
+  }
+  __syncthreads();
+  const double s = *sh;
+  __syncthreads();
+  return s;
+}
+
+template <class T>
+__device__ __forceinline__ T RowDotB(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                     const T* __restrict__ val, const T* __restrict__ x, int64_t r, int64_t end,
+                                     int sub) {
+  T s = T(0);
+  if (r < end)
+    for (int q = rp[r] + sub; q < rp[r + 1]; q += kLanes) s = fma(val[q], x[col[q]], s);
+#pragma unroll
+  for (int o = kLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLanes);
+  return s;
+}
+
+// q = A p on the chunk's rows, pq partial; frozen meshes skipped.
+template <class T>
+__global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, const int32_t* __restrict__ rp,
+                                                   const int32_t* __restrict__ col, const T* __restrict__ val,
+                                                   const T* __restrict__ p, T* __restrict__ q,
+                                                   const int32_t* __restrict__ frozen, double* __restrict__ pq) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    if (frozen[C.mesh[c]]) continue;  // uniform per block
+    const int64_t s = C.start[c], e = C.start[c + 1];
+    const int sub = threadIdx.x % kLanes, grp = threadIdx.x / kLanes;
+    T acc = T(0);
+    for (int64_t wb = s; wb < e; wb += kPB / kLanes) {
+      const int64_t r = wb + grp;
+      const T v = RowDotB<T>(rp, col, val, p, r, e, sub);
+      if (sub == 0 && r < e) {
+        q[r] = v;
+        acc = fma(p[r], v, acc);
+      }
+    }
+    const double tot = BlockReduce(static_cast<double>(acc), red);
+    if (threadIdx.x == 0) pq[c] = tot;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPB) BUpdateKernel(Chunks C, const double* __restrict__ pq,
+                                                     const double* __restrict__ rz_old, const T* __restrict__ dinv,
+                                                     const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
+                                                     T* __restrict__ r, T* __restrict__ z,
+                                                     const int32_t* __restrict__ frozen, double* __restrict__ rz_new,
+                                                     double* __restrict__ rr) {
+  __shared__ double red[32];
+  __shared__ double sh;
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) {
+      if (threadIdx.x == 0) rz_new[c] = rz_old[c];
+      continue;
+    }
+    const double pqs = MeshSum(pq, C, b, &sh);
+    const double rzs = MeshSum(rz_old, C, b, &sh);
+    const T alpha = static_cast<T>(pqs != 0.0 ? rzs / pqs : 0.0);
+    T arz = T(0), arr = T(0);
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      x[i] = fma(alpha, p[i], x[i]);
+      const T ri = fma(-alpha, q[i], r[i]);
+      r[i] = ri;
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      arz = fma(ri, zi, arz);
+      arr = fma(ri, ri, arr);
+    }
+    const double s1 = BlockReduce(static_cast<double>(arz), red);
+    const double s2 = BlockReduce(static_cast<double>(arr), red);
+    if (threadIdx.x == 0) {
+      rz_new[c] = s1;
+      rr[c] = s2;
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const double* __restrict__ rz_new,
+                                                        const double* __restrict__ rz_old, const T* __restrict__ z,
+                                                        T* __restrict__ p, const int32_t* __restrict__ frozen) {
+  __shared__ double sh;
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) continue;
+    const double rn = MeshSum(rz_new, C, b, &sh);
+    const double ro = MeshSum(rz_old, C, b, &sh);
+    const T beta = static_cast<T>(ro != 0.0 ? rn / ro : 0.0);
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPB) BStartKernel(Chunks C, const T* __restrict__ dinv, const T* __restrict__ r,
+                                                    T* __restrict__ z, T* __restrict__ p, double* __restrict__ rz,
+                                                    double* __restrict__ rr) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    T arz = T(0), arr = T(0);
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      const T ri = r[i];
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      p[i] = zi;
+      arz = fma(ri, zi, arz);
+      arr = fma(ri, ri, arr);
+    }
+    const double s1 = BlockReduce(static_cast<double>(arz), red);
+    const double s2 = BlockReduce(static_cast<double>(arr), red);
+    if (threadIdx.x == 0) {
+      rz[c] = s1;
+      rr[c] = s2;
+    }
+  }
+}
+
+// r = b - A x (FP64) and rr partials; optional x == null means x = 0.
+__global__ void __launch_bounds__(kPB) BResidualKernel(Chunks C, const int32_t* __restrict__ rp,
+                                                       const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                       const double* __restrict__ x, const double* __restrict__ b,
+                                                       double* __restrict__ r, double* __restrict__ rr) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int64_t s = C.start[c], e = C.start[c + 1];
+    const int sub = threadIdx.x % kLanes, grp = threadIdx.x / kLanes;
+    double acc = 0.0;
+    for (int64_t wb = s; wb < e; wb += kPB / kLanes) {
+      const int64_t i = wb + grp;
+      const double v = x ? RowDotB<double>(rp, col, val, x, i, e, sub) : 0.0;
+      if (sub == 0 && i < e) {
+        const double ri = b[i] - v;
+        r[i] = ri;
+        acc = fma(ri, ri, acc);
+      }
+    }
+    const double tot = BlockReduce(acc, red);
+    if (threadIdx.x == 0) rr[c] = tot;
+  }
+}
+
+// r32 = r64 * scale[mesh], d32 = 0 (mixed-precision inner start)
+__global__ void BScaleKernel(Chunks C, const double* __restrict__ r, const double* __restrict__ scale,
+                             float* __restrict__ r32, float* __restrict__ d32) {
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const double s = scale[C.mesh[c]];
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      r32[i] = static_cast<float>(r[i] * s);
+      d32[i] = 0.0f;
+    }
+  }
+}
+
+// x += d32 / scale[mesh] for meshes still being refined
+__global__ void BCorrectKernel(Chunks C, const float* __restrict__ d, const double* __restrict__ scale,
+                               const int32_t* __restrict__ done, double* __restrict__ x) {
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (done[b]) continue;
+    const double inv = 1.0 / scale[b];
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x)
+      x[i] += static_cast<double>(d[i]) * inv;
+  }
+}
+
+__global__ void BDiagKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                            const double* __restrict__ val, double* __restrict__ dinv, float* __restrict__ dinv32,
+                            int32_t* st) {
+  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double d = 0.0;
+    for (int64_t q = rp[r]; q < rp[r + 1]; ++q)
+      if (col[q] == r) d = val[q];
+    if (!(d > 0.0)) atomicCAS(st, 0, static_cast<int>(r) + 1);
+    dinv[r] = d > 0.0 ? 1.0 / d : 0.0;
+    dinv32[r] = static_cast<float>(dinv[r]);
+  }
+}
+
+__global__ void BToFloatKernel(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    b[i] = static_cast<float>(a[i]);
+}
+
+__global__ void BRowPtr32Kernel(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    b[i] = static_cast<int32_t>(a[i]);
+}
+
+// Per-mesh sums of chunk partials on the host (chunk order).
+void MeshSums(lfg_batch* B, const double* dev_part, std::vector<double>& out) {
+  std::vector<double> h(B->nchunks);
+  LFG_CUDA(cudaMemcpyAsync(h.data(), dev_part, B->nchunks * sizeof(double), cudaMemcpyDeviceToHost, B->ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(B->ctx->stream));
+  out.assign(B->nb, 0.0);
+  for (int b = 0; b < B->nb; ++b)
+    for (int64_t c = B->h_mesh_chunk_off[b]; c < B->h_mesh_chunk_off[b + 1]; ++c) out[b] += h[c];
+}
+
+template <class T>
+struct BState {
+  DevBuf r, z, p, q, pq, rz[2], rr;
+};
+
+template <class T>
+void BAlloc(lfg_ctx* ctx, int64_t n, int64_t nch, BState<T>& S) {
+  cudaStream_t s = ctx->stream;
+  S.r.alloc(n * sizeof(T), s);
+  S.z.alloc(n * sizeof(T), s);
+  S.p.alloc(n * sizeof(T), s);
+  S.q.alloc(n * sizeof(T), s);
+  S.pq.alloc(nch * sizeof(double), s);
+  S.rz[0].alloc(nch * sizeof(double), s);
+  S.rz[1].alloc(nch * sizeof(double), s);
+  S.rr.alloc(nch * sizeof(double), s);
+}
+
+// Batched PCG in precision T on S.r (filled): per-mesh targets target_rr[b]
+// (squared norms); meshes with done[b] start frozen.  Returns per-mesh
+// iterations in it_out and final recursive rr in rr_out.
+template <class T>
+void BRunPcg(lfg_batch* B, lfg_csr* A, const T* val, const T* dinv, T* x, BState<T>& S, const Chunks& C,
+             const std::vector<double>& target_rr, std::vector<int32_t>& frozen_h, DevBuf& frozen_d, int max_it,
+             int check_every, std::vector<int>& it_out, std::vector<double>& rr_out) {
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
+  const int32_t* rp = A->rowptr32.as<int32_t>();
+  const int32_t* col = A->col.as<int32_t>();
+  BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(), S.p.template as<T>(),
+                                      S.rz[0].template as<double>(), S.rr.template as<double>());
+  LFG_LAUNCHED(ctx);
+  std::vector<double> rr;
+  MeshSums(B, S.rr.template as<double>(), rr);
+  it_out.assign(B->nb, 0);
+  for (int b = 0; b < B->nb; ++b)
+    if (!(rr[b] > target_rr[b])) frozen_h[b] = 1;
+  LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  const int body = std::max(2, check_every + (check_every & 1));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < body; ++k) {
+    double* rz_old = S.rz[k & 1].template as<double>();
+    double* rz_new = S.rz[(k + 1) & 1].template as<double>();
+    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, rp, col, val, S.p.template as<T>(), S.q.template as<T>(),
+                                       frozen_d.as<int32_t>(), S.pq.template as<double>());
+    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, S.pq.template as<double>(), rz_old, dinv, S.p.template as<T>(),
+                                         S.q.template as<T>(), x, S.r.template as<T>(), S.z.template as<T>(),
+                                         frozen_d.as<int32_t>(), rz_new, S.rr.template as<double>());
+    BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, rz_new, rz_old, S.z.template as<T>(), S.p.template as<T>(),
+                                            frozen_d.as<int32_t>());
+  }
+  LFG_CUDA(cudaStreamEndCapture(s, &graph));
+  LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  int it = 0;
+  try {
+    while (it < max_it) {
+      int active = 0;
+      for (int b = 0; b < B->nb; ++b) active += !frozen_h[b];
+      if (!active) break;
+      LFG_CUDA(cudaGraphLaunch(exec, s));
+      CountLaunch(ctx, 3 * body);
+      it += body;
+      MeshSums(B, S.rr.template as<double>(), rr);
+      bool changed = false;
+      for (int b = 0; b < B->nb; ++b)
+        if (!frozen_h[b]) {
+          it_out[b] = it;
+          if (!(rr[b] > target_rr[b])) {
+            frozen_h[b] = 1;
+            changed = true;
+          }
+        }
+      if (changed)
+        LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+  } catch (...) {
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    throw;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  rr_out = rr;
+}
+
+}  // namespace
+}  // namespace lfg
+
+using namespace lfg;
+
+extern "C" {
+
+lfg_status lfg_batch_create(lfg_ctx* ctx, int32_t n, lfg_space* const* spaces, lfg_batch** out) {
+  LFG_API_BEGIN(ctx)
+  if (!out || n <= 0 || !spaces) Fail(LFG_INVALID_ARG, "lfg_batch_create: bad argument");
+  auto* B = new lfg_batch;
+  try {
+    B->ref.Set(ctx);
+    B->ctx = ctx;
+    B->nb = n;
+    B->spaces.assign(spaces, spaces + n);
+    B->dof_off.assign(n + 1, 0);
+    B->cell_off.assign(n + 1, 0);
+    B->trip_off.assign(n + 1, 0);
+    std::vector<BatchMesh> hm(n);
+    for (int b = 0; b < n; ++b) {
+      lfg_space* sp = spaces[b];
+      if (!sp || sp->mesh->ctx != ctx) Fail(LFG_INVALID_ARG, "space " + std::to_string(b) + " is null or on another context");
+      if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "batched assembly needs Lagrangian spaces");
+      if (sp->mesh->nquad) Fail(LFG_UNSUPPORTED, "batched assembly supports triangular meshes");
+      B->dof_off[b + 1] = B->dof_off[b] + sp->num_dofs;
+      B->cell_off[b + 1] = B->cell_off[b] + sp->mesh->nc;
+      B->trip_off[b + 1] = B->trip_off[b] + sp->num_triplets;
+      B->max_degree = std::max(B->max_degree, sp->degree);
+      BatchMesh& m = hm[b];
+      m.xy = sp->mesh->xy.as<double2>();
+      m.cells = sp->mesh->cell_nodes.as<int4>();
+      m.cell_dofs = sp->cell_dofs.as<int32_t>();
+      m.tri_offset = sp->tri_offset.as<int64_t>();
+      m.n_cell = sp->n_cell;
+      m.degree = sp->degree;
+      m.ncells = sp->mesh->nc;
+      m.dof_off = B->dof_off[b];
+      m.cell_off = B->cell_off[b];
+      m.trip_off = B->trip_off[b];
+    }
+    if (B->dof_off[n] >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "batch has more than 2^31 dofs");
+    B->meshes.alloc(n * sizeof(BatchMesh), ctx->stream);
+    LFG_CUDA(cudaMemcpyAsync(B->meshes.p, hm.data(), n * sizeof(BatchMesh), cudaMemcpyHostToDevice, ctx->stream));
+    // PCG chunks (never straddling two meshes)
+    std::vector<int32_t> cm;
+    std::vector<int64_t> cs, mc(n + 1, 0);
+    for (int b = 0; b < n; ++b) {
+      mc[b] = static_cast<int64_t>(cm.size());
+      for (int64_t r = B->dof_off[b]; r < B->dof_off[b + 1]; r += kChunk) {
+        cm.push_back(b);
+        cs.push_back(r);
+      }
+    }
+    mc[n] = static_cast<int64_t>(cm.size());
+    cs.push_back(B->dof_off[n]);
+    B->nchunks = static_cast<int64_t>(cm.size());
+    B->h_mesh_chunk_off = mc;
+    B->chunk_mesh.alloc(cm.size() * sizeof(int32_t), ctx->stream);
+    B->chunk_start.alloc(cs.size() * sizeof(int64_t), ctx->stream);
+    B->mesh_chunk_off.alloc(mc.size() * sizeof(int64_t), ctx->stream);
+    LFG_CUDA(cudaMemcpyAsync(B->chunk_mesh.p, cm.data(), cm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    LFG_CUDA(cudaMemcpyAsync(B->chunk_start.p, cs.data(), cs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    LFG_CUDA(cudaMemcpyAsync(B->mesh_chunk_off.p, mc.data(), mc.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    delete B;
+    throw;
+  }
+  *out = B;
+  LFG_API_END
+}
+
+lfg_status lfg_batch_destroy(lfg_batch* B) {
+  if (!B) return LFG_INVALID_ARG;
+  cudaSetDevice(B->ctx->device);
+  delete B;
+  return LFG_OK;
+}
+
+lfg_status lfg_batch_info(const lfg_batch* B, int32_t* n, int64_t* dofs, int64_t* cells, int64_t* trips) {
+  if (!B) return LFG_INVALID_ARG;
+  if (n) *n = B->nb;
+  if (dofs) *dofs = B->dof_off[B->nb];
+  if (cells) *cells = B->cell_off[B->nb];
+  if (trips) *trips = B->trip_off[B->nb];
+  return LFG_OK;
+}
+
+lfg_status lfg_batch_offsets(const lfg_batch* B, int64_t* dof, int64_t* cell, int64_t* trip) {
+  if (!B) return LFG_INVALID_ARG;
+  for (int b = 0; b <= B->nb; ++b) {
+    if (dof) dof[b] = B->dof_off[b];
+    if (cell) cell[b] = B->cell_off[b];
+    if (trip) trip[b] = B->trip_off[b];
+  }
+  return LFG_OK;
+}
+
+lfg_status lfg_batch_tuning(const lfg_batch* B, int32_t* threads, int32_t* ctas, double* ms) {
+  if (!B) return LFG_INVALID_ARG;
+  if (threads) *threads = B->tuned ? B->threads : 0;
+  if (ctas) *ctas = B->tuned ? B->ctas_per_sm : 0;
+  if (ms) *ms = B->best_ms;
+  return LFG_OK;
+}
+
+lfg_status lfg_batch_assemble_matrix_rd(lfg_batch* B, const lfg_rd_provider* pr, lfg_coo* coo) {
+  if (!B) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  if (!pr || !coo) Fail(LFG_INVALID_ARG, "lfg_batch_assemble_matrix_rd: null argument");
+  const int64_t total = B->trip_off[B->nb];
+  if (coo->rows < B->dof_off[B->nb] || coo->cols < B->dof_off[B->nb])
+    Fail(LFG_INVALID_ARG, "COO matrix smaller than the batch");
+  if (coo->size + total > coo->capacity) Fail(LFG_CAPACITY, "COO capacity too small for the batch");
+  auto cell_const = [&](const lfg_coeff& c, const double*& data, double& value, const char* what) {
+    data = nullptr;
+    value = 0.0;
+    if (c.kind == LFG_COEFF_CONSTANT) value = c.value;
+    else if (c.kind == LFG_COEFF_PER_CELL) {
+      if (!c.data_dev) Fail(LFG_INVALID_ARG, std::string(what) + ": null data");
+      data = c.data_dev;
+    } else if (c.kind != LFG_COEFF_ZERO) {
+      Fail(LFG_UNSUPPORTED, std::string(what) + ": batched assembly takes constant or per-cell coefficients");
+    }
+  };
+  BatchArgs A{};
+  cell_const(pr->alpha, A.alpha, A.alpha_value, "alpha");
+  cell_const(pr->gamma, A.gamma, A.gamma_value, "gamma");
+  const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
+  if (pr->qr_degree_tria < 0) Fail(LFG_MISSING_RULE, "no quadrature rule for triangles");
+  // tables per degree (rule: default 2p or the given degree)
+  std::vector<float> hdf;
+  std::vector<double> h64;
+  DevBuf tabs;
+  {
+    std::vector<std::pair<size_t, size_t>> offs(4, {0, 0});
+    std::vector<unsigned char> blob;
+    for (int deg = 1; deg <= 3; ++deg) {
+      const int rd = pr->qr_degree_tria > 0 ? pr->qr_degree_tria : 2 * deg;
+      DfLayout dl;
+      if (!BuildDfTables(false, deg, rd, hdf, dl)) Fail(LFG_UNSUPPORTED, "no quadrature rule of that degree");
+      // FP64 folded R from the df32 pair (hi + lo): exact to the pair's precision
+      h64.assign(dl.E * 4, 0.0);
+      for (int q = 0; q < dl.E * 4; ++q)
+        h64[q] = static_cast<double>(hdf[2 * (dl.off_R + q)]) + static_cast<double>(hdf[2 * (dl.off_R + q) + 1]);
+      const size_t o1 = blob.size();
+      const size_t bytes_df = dl.E * 4 * 2 * sizeof(float);
+      blob.resize(o1 + bytes_df);
+      std::memcpy(blob.data() + o1, hdf.data() + 2 * dl.off_R, bytes_df);
+      const size_t o2 = (blob.size() + 15) & ~size_t(15);
+      blob.resize(o2 + h64.size() * sizeof(double));
+      std::memcpy(blob.data() + o2, h64.data(), h64.size() * sizeof(double));
+      blob.resize((blob.size() + 15) & ~size_t(15));
+      offs[deg] = {o1, o2};
+    }
+    tabs.alloc(blob.size(), s);
+    LFG_CUDA(cudaMemcpyAsync(tabs.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+    for (int deg = 1; deg <= 3; ++deg) {
+      A.tabs[deg] = reinterpret_cast<const f2*>(tabs.as<unsigned char>() + offs[deg].first);
+      A.tabs64[deg] = reinterpret_cast<const double*>(tabs.as<unsigned char>() + offs[deg].second);
+    }
+  }
+  A.meshes = B->meshes.as<BatchMesh>();
+  A.nb = B->nb;
+  A.out = coo->d + coo->size;
+  A.fallback = reinterpret_cast<unsigned long long*>(StatusWord(ctx) + 12);
+  const size_t stage = StagePerCell(B->max_degree);
+  auto kernel = mass ? BatchAssembleKernel<true> : BatchAssembleKernel<false>;
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(kMaxBatchThreads * stage)));
+  DevBuf prefix;
+  prefix.alloc((B->nb + 1) * sizeof(int64_t), s);
+  auto launch = [&](int threads, int ctas) {
+    std::vector<int64_t> tp(B->nb + 1, 0);
+    for (int b = 0; b < B->nb; ++b)
+      tp[b + 1] = tp[b] + (B->spaces[b]->mesh->nc + threads - 1) / threads;
+    LFG_CUDA(cudaMemcpyAsync(prefix.p, tp.data(), tp.size() * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    A.tile_prefix = prefix.as<int64_t>();
+    A.total_tiles = tp[B->nb];
+    const size_t smem = threads * stage;
+    const int64_t grid = std::min<int64_t>(A.total_tiles, static_cast<int64_t>(ctx->num_sms) * ctas);
+    kernel<<<static_cast<unsigned>(std::max<int64_t>(grid, 1)), threads, smem, s>>>(A);
+    LFG_LAUNCHED(ctx);
+  };
+  if (!B->tuned) {
+    // autotuner: time every (threads per CTA, CTAs per SM) candidate once
+    double best = 1e30;
+    for (int threads : {64, 128, 256}) {
+      int occ = 0;
+      LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, threads * stage));
+      for (int ctas : {std::max(occ, 1), std::max(occ / 2, 1), std::max(2 * occ, 1)}) {
+        launch(threads, ctas);  // warm
+        LFG_CUDA(cudaEventRecord(ctx->t0, s));
+        launch(threads, ctas);
+        LFG_CUDA(cudaEventRecord(ctx->t1, s));
+        LFG_CUDA(cudaEventSynchronize(ctx->t1));
+        float ms = 0.f;
+        LFG_CUDA(cudaEventElapsedTime(&ms, ctx->t0, ctx->t1));
+        if (ms < best) {
+          best = ms;
+          B->threads = threads;
+          B->ctas_per_sm = ctas;
+        }
+      }
+    }
+    B->best_ms = best;
+    B->tuned = true;
+  }
+  {
+    ProfScope prof(ctx, "batch_assemble");
+    launch(B->threads, B->ctas_per_sm);
+  }
+  coo->size += total;
+  LFG_API_END
+}
+
+lfg_status lfg_batch_assemble_vector_load(lfg_batch* B, const lfg_load_provider* pr, double* bvec) {
+  if (!B) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  if (!pr || !bvec) Fail(LFG_INVALID_ARG, "lfg_batch_assemble_vector_load: null argument");
+  if (pr->f.kind == LFG_COEFF_NODAL_O1) Fail(LFG_UNSUPPORTED, "batched load: nodal coefficients are not supported");
+  for (int b = 0; b < B->nb; ++b) {
+    lfg_load_provider p = *pr;
+    if (p.f.kind == LFG_COEFF_PER_CELL) p.f.data_dev = pr->f.data_dev + B->cell_off[b];
+    const lfg_status st = lfg_assemble_vector_load(B->spaces[b], &p, bvec + B->dof_off[b]);
+    if (st != LFG_OK) Fail(st, B->ctx->last_error);
+  }
+  LFG_API_END
+}
+
+lfg_status lfg_batch_boundary_dof_flags(lfg_batch* B, uint8_t* flags) {
+  if (!B) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  if (!flags) Fail(LFG_INVALID_ARG, "null flags");
+  for (int b = 0; b < B->nb; ++b) {
+    const lfg_status st = lfg_space_boundary_dof_flags(B->spaces[b], flags + B->dof_off[b]);
+    if (st != LFG_OK) Fail(st, B->ctx->last_error);
+  }
+  LFG_API_END
+}
+
+lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, double* x,
+                               const lfg_solve_opts* opts, lfg_solve_stats* stats, lfg_solve_stats* per) {
+  if (!B || !A) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  if (!bvec || !x || !opts) Fail(LFG_INVALID_ARG, "lfg_batch_solve_pcg: null argument");
+  const int64_t n = B->dof_off[B->nb];
+  if (A->rows != n || A->cols != n) Fail(LFG_INVALID_ARG, "matrix size differs from the batch");
+  if (A->nnz >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "solver needs nnz < 2^31");
+  // solver-side CSR data (same fields lfg_solve_pcg uses)
+  if (!A->rowptr32.p) {
+    A->rowptr32.alloc((n + 1) * sizeof(int32_t), s);
+    BRowPtr32Kernel<<<GridFor(ctx, n + 1, 256), 256, 0, s>>>(n + 1, A->rowptr.as<int64_t>(), A->rowptr32.as<int32_t>());
+    LFG_LAUNCHED(ctx);
+  }
+  if (!A->dinv.p) {
+    A->dinv.alloc(n * sizeof(double), s);
+    A->dinv32.alloc(n * sizeof(float), s);
+    ReadAndClearStatus(ctx);
+    BDiagKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, A->rowptr.as<int64_t>(), A->col.as<int32_t>(),
+                                                     A->val.as<double>(), A->dinv.as<double>(), A->dinv32.as<float>(),
+                                                     StatusWord(ctx));
+    LFG_LAUNCHED(ctx);
+    if (int32_t code = ReadAndClearStatus(ctx)) {
+      A->dinv.reset();
+      Fail(LFG_INVALID_ARG, "Jacobi preconditioner: non-positive diagonal in row " + std::to_string(code - 1));
+    }
+  }
+  Chunks C{B->chunk_mesh.as<int32_t>(), B->chunk_start.as<int64_t>(), B->mesh_chunk_off.as<int64_t>(), B->nchunks};
+  const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
+  const int check = opts->check_every > 0 ? opts->check_every : 32;
+  const int max_it = opts->max_iterations > 0 ? opts->max_iterations : 100000;
+  const double rtol = opts->rtol > 0 ? opts->rtol : 1e-10;
+  BState<double> S;
+  BAlloc(ctx, n, C.nchunks, S);
+  DevBuf frozen;
+  frozen.alloc(B->nb * sizeof(int32_t), s);
+  std::vector<double> bb, rr;
+  BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), nullptr,
+                                      bvec, S.r.as<double>(), S.rr.as<double>());
+  LFG_LAUNCHED(ctx);
+  MeshSums(B, S.rr.as<double>(), bb);
+  BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x, bvec,
+                                      S.r.as<double>(), S.rr.as<double>());
+  LFG_LAUNCHED(ctx);
+  MeshSums(B, S.rr.as<double>(), rr);
+  std::vector<double> target(B->nb);
+  for (int b = 0; b < B->nb; ++b) target[b] = rtol * rtol * bb[b];
+  std::vector<int32_t> frozen_h(B->nb, 0);
+  std::vector<int> its(B->nb, 0), refinements(B->nb, 0);
+  if (opts->precision == LFG_SOLVE_FP64) {
+    std::vector<int> it1;
+    std::vector<double> rr1;
+    // restart on the true residual when the recursive one drifted (<= 4 times)
+    for (int round = 0; round < 5; ++round) {
+      std::vector<int32_t> fz(B->nb, 0);
+      int active = 0;
+      for (int b = 0; b < B->nb; ++b) {
+        fz[b] = !(rr[b] > target[b]);
+        active += !fz[b];
+      }
+      if (!active) break;
+      BRunPcg<double>(B, A, A->val.as<double>(), A->dinv.as<double>(), x, S, C, target, fz, frozen, max_it, check,
+                      it1, rr1);
+      for (int b = 0; b < B->nb; ++b) {
+        its[b] += it1[b];
+        refinements[b] += it1[b] > 0;
+      }
+      BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
+                                          bvec, S.r.as<double>(), S.rr.as<double>());
+      LFG_LAUNCHED(ctx);
+      MeshSums(B, S.rr.as<double>(), rr);
+    }
+  } else if (opts->precision == LFG_SOLVE_MIXED) {
+    // FP32 matrix copy and FP32 inner PCG state
+    if (!A->val32.p) {
+      A->val32.alloc(std::max<int64_t>(A->nnz, 1) * sizeof(float), s);
+      BToFloatKernel<<<GridFor(ctx, A->nnz, 256), 256, 0, s>>>(A->nnz, A->val.as<double>(), A->val32.as<float>());
+      LFG_LAUNCHED(ctx);
+    }
+    BState<float> S32;
+    BAlloc(ctx, n, C.nchunks, S32);
+    DevBuf d32, scale, done;
+    d32.alloc(n * sizeof(float), s);
+    scale.alloc(B->nb * sizeof(double), s);
+    done.alloc(B->nb * sizeof(int32_t), s);
+    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : 1e-4;
+    std::vector<double> sc(B->nb), tin(B->nb);
+    std::vector<int32_t> dn(B->nb), fz(B->nb);
+    std::vector<int> it1;
+    std::vector<double> rr1;
+    for (int outer = 0; outer < 200; ++outer) {
+      int active = 0;
+      for (int b = 0; b < B->nb; ++b) {
+        dn[b] = !(rr[b] > target[b]);
+        active += !dn[b];
+        const double rn = std::sqrt(rr[b]);
+        sc[b] = rn > 0 ? 1.0 / rn : 1.0;
+        const double need = std::max(inner, rn > 0 ? 0.5 * std::sqrt(target[b]) / rn : inner);
+        tin[b] = need * need;
+        fz[b] = dn[b];
+      }
+      if (!active) break;
+      LFG_CUDA(cudaMemcpyAsync(scale.p, sc.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
+      LFG_CUDA(cudaMemcpyAsync(done.p, dn.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
+      LFG_LAUNCHED(ctx);
+      BRunPcg<float>(B, A, A->val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), S32, C, tin, fz, frozen,
+                     max_it, check, it1, rr1);
+      BCorrectKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), done.as<int32_t>(), x);
+      LFG_LAUNCHED(ctx);
+      BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
+                                          bvec, S.r.as<double>(), S.rr.as<double>());
+      LFG_LAUNCHED(ctx);
+      std::vector<double> rr_new;
+      MeshSums(B, S.rr.as<double>(), rr_new);
+      bool progress = false;
+      for (int b = 0; b < B->nb; ++b)
+        if (!dn[b]) {
+          its[b] += std::max(it1[b], 1);
+          refinements[b] += 1;
+          progress = progress || rr_new[b] < rr[b];
+        }
+      rr = rr_new;
+      if (!progress) break;
+    }
+  } else {
+    Fail(LFG_INVALID_ARG, "unknown solve precision");
+  }
+  lfg_solve_stats tot{};
+  tot.converged = 1;
+  double worst = 0.0;
+  for (int b = 0; b < B->nb; ++b) {
+    lfg_solve_stats sb{};
+    sb.iterations = its[b];
+    sb.refinements = refinements[b];
+    sb.rel_residual = bb[b] > 0 ? std::sqrt(rr[b] / bb[b]) : 0.0;
+    sb.converged = bb[b] == 0 || sb.rel_residual <= rtol * 1.0000001;
+    if (per) per[b] = sb;
+    tot.iterations = std::max(tot.iterations, sb.iterations);
+    tot.refinements = std::max(tot.refinements, sb.refinements);
+    tot.converged = tot.converged && sb.converged;
+    worst = std::max(worst, sb.rel_residual);
+  }
+  tot.rel_residual = worst;
+  if (stats) *stats = tot;
+  if (!tot.converged) {
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "batched PCG: not all blocks converged (worst rel. residual %.3e)", worst);
+    Fail(LFG_NOT_CONVERGED, buf);
+  }
+  LFG_API_END
+}
+
+}  // extern "C"

@@ -54,7 +54,7 @@ namespace lfg {
 // degree and quadrature rule); offsets are in doubles.
 struct Tab {
   int n, nq, E;
-  int off_w, off_qx, off_qy, off_phi, off_T, off_R, off_L, off_o1, total;
+  int off_w, off_qx, off_qy, off_phi, off_T, off_R, off_L, off_o1, off_G, total;
 };
 struct TableEntry {
   Tab layout;

@@ -100,7 +100,9 @@ def config3(n=1024, seed=3):
 
 def config5(n=1024, seed=5):
     """Differentiation form: TPTriag n x n, O1, alpha = exp(theta) per cell,
-    theta ~ N(0, 0.5^2), gamma = 0, f = 1, Dirichlet 0."""
+    theta ~ N(0, 0.5^2), gamma = 0, f = 1, Dirichlet 0.  Observations are
+    u(theta_true(cell centroids)) + observation_noise (built by the caller,
+    which owns the solver)."""
     rng = np.random.default_rng(seed)
     theta = 0.5 * rng.standard_normal(2 * n * n)
     return {
@@ -110,12 +112,52 @@ def config5(n=1024, seed=5):
     }
 
 
+def cell_centroids(xy, cells):
+    """Vertex averages of triangles (cells[:, 3] < 0) and quadrilaterals."""
+    cells = np.asarray(cells)
+    quad = cells[:, 3] >= 0
+    c = np.where(cells < 0, cells[:, :1], cells)  # pad triangles with vertex 0
+    s = xy[c[:, 0]] + xy[c[:, 1]] + xy[c[:, 2]] + np.where(quad[:, None], xy[c[:, 3]], 0.0)
+    return s / np.where(quad, 4.0, 3.0)[:, None]
+
+
+def theta_true(centroids, seed=55, bumps=8):
+    """Smooth log-conductivity: sum of `bumps` Gaussian bumps with centres
+    U[0.15, 0.85]^2, widths U[0.05, 0.15] and amplitudes U[-1, 1]."""
+    rng = np.random.default_rng(seed)
+    ctr = rng.uniform(0.15, 0.85, (bumps, 2))
+    wid = rng.uniform(0.05, 0.15, bumps)
+    amp = rng.uniform(-1.0, 1.0, bumps)
+    t = np.zeros(len(centroids))
+    for k in range(bumps):
+        d2 = ((centroids - ctr[k]) ** 2).sum(axis=1)
+        t += amp[k] * np.exp(-d2 / (2.0 * wid[k] ** 2))
+    return t
+
+
+def observation_noise(ndofs, seed=56, sigma=1e-3):
+    return sigma * np.random.default_rng(seed).standard_normal(ndofs)
+
+
 def batch_sizes(count=512, lo=24, hi=320, seed=4):
     """Config 4: mesh sizes n ~ round(exp(U(ln lo, ln hi))) and degrees 1|2."""
     rng = np.random.default_rng(seed)
     ns = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(int)
     degs = np.where(rng.random(count) < 0.5, 1, 2)
     return ns, degs
+
+
+def config4(count=512, lo=24, hi=320, seed=4):
+    """Batching form: `count` TPTriag n x n unit-square meshes (n log-uniform in
+    [lo, hi]), O1 or O2 (50/50), alpha per cell LogNormal(0, 0.5^2), gamma = 1,
+    f = 1, homogeneous Dirichlet.  alpha is one array over the batch cells
+    (mesh after mesh)."""
+    ns, degs = batch_sizes(count, lo, hi, seed)
+    rng = np.random.default_rng(seed + 1000)
+    cells = 2 * ns.astype(np.int64) ** 2
+    alpha = np.exp(0.5 * rng.standard_normal(int(cells.sum())))
+    return {"name": "c4_batch%d" % count, "ns": ns, "degrees": degs, "alpha": alpha, "gamma": 1.0, "f": 1.0,
+            "cells": cells}
 
 
 # ------------------------------------------------------------- GPU helpers

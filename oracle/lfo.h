@@ -133,9 +133,10 @@ DofHandler MakeLagrangeDofHandler(const Mesh& m, int degree);
 // A scalar MeshFunction (mesh_function_traits.h:149-155) evaluated on a cell
 // at reference points.  Kinds: constant (mesh_function_constant.h:25-45),
 // per-cell array, O1 nodal interpolant (fe/mesh_function_fe.h:44-115),
-// analytic x->f(x) (mesh_function_global.h:54-94).
+// analytic x->f(x) (mesh_function_global.h:54-94), and exp of a per-cell
+// array (a log-coefficient; no reference counterpart).
 struct MeshFunction {
-  enum Kind { kZero = 0, kConstant = 1, kPerCell = 2, kNodalO1 = 3, kAnalytic = 4 };
+  enum Kind { kZero = 0, kConstant = 1, kPerCell = 2, kNodalO1 = 3, kAnalytic = 4, kPerCellExp = 5 };
   int kind = kZero;
   double value = 0.0;
   std::vector<double> data;

@@ -49,7 +49,8 @@ static MeshFunction ToMF(const lfo_coeff* c, size_t n_data) {
   if (!c) return mf;
   mf.kind = c->kind;
   mf.value = c->value;
-  if (c->kind == MeshFunction::kPerCell || c->kind == MeshFunction::kNodalO1)
+  if (c->kind == MeshFunction::kPerCell || c->kind == MeshFunction::kNodalO1 ||
+      c->kind == MeshFunction::kPerCellExp)
     mf.data.assign(c->data, c->data + n_data);
   if (c->kind == MeshFunction::kAnalytic) mf.fn = AnalyticFunction(c->func, c->p);
   return mf;

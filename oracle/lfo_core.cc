@@ -562,6 +562,9 @@ void MeshFunction::Eval(const Mesh& m, idx_t cell, const QuadRule& qr,
     case kPerCell:
       for (auto& o : out) o = data[cell];
       return;
+    case kPerCellExp:
+      for (auto& o : out) o = std::exp(data[cell]);
+      return;
     case kNodalO1: {
       // MeshFunctionFE over an O1 space: value = local dofs . shape values
       const bool q = m.IsQuad(cell);

@@ -16,7 +16,7 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 _lock = threading.Lock()
 
-ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC = 0, 1, 2, 3, 4
+ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
 FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
 
 
@@ -337,3 +337,46 @@ def assemble_rd_parallel(space, alpha, gamma, qdeg_tria=0, qdeg_quad=0, cells=(0
     _check(L.lfo_assemble_rd_parallel(space.h, C.byref(alpha), C.byref(gamma), qdeg_tria, qdeg_quad, cells[0],
                                       cells[1], threads, C.byref(sec), C.byref(n), err, 512), err)
     return sec.value, n.value
+
+
+# ------------------------------------------------------------ differentiation
+# CPU FP64 reference gradient of J(theta) = 1/2 ||u - u_obs||^2 with
+# alpha = exp(theta) per cell and gamma = 0 (no reference counterpart; built
+# from the restated ReactionDiffusionElementMatrixProvider, which gives A_K,
+# and two sparse LU solves of the fixed system).
+
+def element_blocks(space):
+    """Start offsets of the per-cell n_K^2 triplet blocks of assemble_rd."""
+    cells = space.mesh.cells
+    sizes = np.where(cells[:, 3] >= 0, space.n_quad ** 2, space.n_tria ** 2)
+    return np.concatenate([[0], np.cumsum(sizes)])
+
+
+def cellwise_bilinear(space, A, lam, u):
+    """Per cell sum_{ij} lam[dof_i] A_K(i,j) u[dof_j] over the cell-ordered
+    triplet blocks of an (unfixed) assemble_rd matrix."""
+    r, c, v = A.arrays()
+    offs = element_blocks(space)
+    return np.add.reduceat(lam[r] * v * u[c], offs[:-1])
+
+
+def adjoint_gradient(space, theta, f, u_obs, flags, g=None, qdeg_tria=0, qdeg_quad=0):
+    """J, u, lambda and dJ/dtheta in FP64: assemble, fix, SparseLU for u and
+    for the adjoint A lambda = (u - u_obs) on free dofs, then
+    dJ/dtheta_c = -sum_{i free, j} lambda_i A_K(i,j) u_j."""
+    import scipy.sparse.linalg as spla
+    nd = space.num_dofs
+    g = np.zeros(nd) if g is None else np.asarray(g, np.float64)
+    A = assemble_rd(space, coeff(PER_CELL_EXP, data=theta), coeff(ZERO), qdeg_tria, qdeg_quad)
+    Af = assemble_rd(space, coeff(PER_CELL_EXP, data=theta), coeff(ZERO), qdeg_tria, qdeg_quad)
+    b = assemble_load(space, f)
+    Af.fix_flagged(flags, g, b)
+    lu = spla.splu(Af.to_scipy().tocsc())
+    u = lu.solve(b)
+    r = u - u_obs
+    J = 0.5 * float(r @ r)
+    rhs = np.where(flags != 0, 0.0, r)
+    lam = lu.solve(rhs)
+    lam_m = np.where(flags != 0, 0.0, lam)
+    grad = -cellwise_bilinear(space, A, lam_m, u)
+    return J, u, lam, grad

@@ -1,0 +1,207 @@
+// Drives the C++ facade (lf_gb300.hpp) the way a LehrFEM++ driver drives
+// lf::assemble, and checks it against the oracle (the CPU restatement, linked
+// from its shared library): triplet indices and order bit-exact, values within
+// 1e-12 of each element matrix's largest entry, the load vector within 1e-12,
+// a converged PCG solve, and the adjoint Function object against central
+// differences of its own forward.  Exit status 0 = all checks passed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "lf_gb300.hpp"
+
+extern "C" {
+typedef struct {
+  int32_t kind, func;
+  double value;
+  const double* data;
+  double p[16];
+} lfo_coeff;
+int lfo_input_create(int kind, int64_t nx, int64_t ny, double x0, double y0, double x1, double y1, void** out,
+                     int64_t* sizes, char* err, int errlen);
+void lfo_input_copy(void* h, double* xy, int64_t* cells, int64_t* edges);
+void lfo_input_destroy(void* h);
+int lfo_mesh_create(int64_t nv, const double* xy, int64_t nc, const int64_t* cells, int64_t npre, const int64_t* pre,
+                    void** out, char* err, int errlen);
+void lfo_mesh_destroy(void* m);
+int lfo_space_create(void* mp, int degree, int np, int ns, int nt, int nq, void** out, char* err, int errlen);
+void lfo_space_destroy(void* s);
+int lfo_assemble_rd(void* sp, const lfo_coeff* alpha, const lfo_coeff* gamma, int qdeg_tria, int qdeg_quad,
+                    int64_t first_cell, int64_t last_cell, void** out, char* err, int errlen);
+int lfo_assemble_load(void* sp, const lfo_coeff* f, int qdeg_tria, int qdeg_quad, double* b, char* err, int errlen);
+int64_t lfo_coo_size(void* a);
+void lfo_coo_copy(void* a, int32_t* r, int32_t* c, double* v);
+void lfo_coo_destroy(void* a);
+}
+
+namespace g = lf::gb300;
+
+static int failures = 0;
+#define CHECK(cond, ...)                   \
+  do {                                     \
+    if (!(cond)) {                         \
+      std::printf("FAIL %s:%d: ", __FILE__, __LINE__); \
+      std::printf(__VA_ARGS__);            \
+      std::printf("\n");                   \
+      ++failures;                          \
+    }                                      \
+  } while (0)
+
+static void CheckAssembly(const g::Context& ctx, int nx, int ny, int degree) {
+  auto mesh = g::mesh::TPTriagMeshBuilder(ctx).setBottomLeftCorner(0, 0).setTopRightCorner(1, 1)
+                  .setNumXCells(nx).setNumYCells(ny).Build();
+  std::shared_ptr<g::uscalfe::FeSpaceLagrange> fes =
+      degree == 1 ? g::uscalfe::FeSpaceLagrangeO<1>(mesh)
+                  : degree == 2 ? g::uscalfe::FeSpaceLagrangeO<2>(mesh) : g::uscalfe::FeSpaceLagrangeO<3>(mesh);
+  const int64_t nd = fes->NumDofs();
+  // alpha = 1 + x^2 + y^2, gamma = 1, f = sin(pi x) sin(pi y)
+  std::vector<double> pa(16, 0.0);
+  pa[0] = 1.0; pa[8] = 1.0; pa[2] = 1.0;
+  g::uscalfe::ReactionDiffusionElementMatrixProvider rd(fes, g::uscalfe::MeshFunction::Analytic(LFG_FN_POLY, pa),
+                                                        g::uscalfe::MeshFunction::Constant(1.0), 4, 4);
+  g::uscalfe::ScalarLoadElementVectorProvider lp(fes, g::uscalfe::MeshFunction::Analytic(LFG_FN_SINSIN, {0, 1, 1, 1}),
+                                                 4, 4);
+  g::assemble::COOMatrix A(ctx, nd, nd, fes->NumTriplets() + nd);
+  g::assemble::AssembleMatrixLocally(0, *fes, *fes, rd, A);
+  g::DeviceVector<double> b(ctx, nd);
+  b.SetZero();
+  g::assemble::AssembleVectorLocally(0, *fes, lp, b);
+  const std::vector<lfg_triplet> t = A.Download();
+
+  // the oracle on the same mesh
+  char err[512];
+  void *in = nullptr, *om = nullptr, *os = nullptr, *oc = nullptr;
+  int64_t sz[3];
+  lfo_input_create(0, nx, ny, 0, 0, 1, 1, &in, sz, err, 512);
+  std::vector<double> xy(sz[0] * 2);
+  std::vector<int64_t> cells(sz[1] * 4), edges(sz[2] * 2 + 2);
+  lfo_input_copy(in, xy.data(), cells.data(), edges.data());
+  CHECK(lfo_mesh_create(sz[0], xy.data(), sz[1], cells.data(), sz[2], edges.data(), &om, err, 512) == 0, "%s", err);
+  CHECK(lfo_space_create(om, degree, 0, 0, 0, 0, &os, err, 512) == 0, "%s", err);
+  lfo_coeff alpha{}, gamma{}, f{};
+  alpha.kind = 4; alpha.func = LFG_FN_POLY;
+  for (int i = 0; i < 16; ++i) alpha.p[i] = pa[i];
+  gamma.kind = 1; gamma.value = 1.0;
+  f.kind = 4; f.func = LFG_FN_SINSIN; f.p[1] = 1; f.p[2] = 1; f.p[3] = 1;
+  CHECK(lfo_assemble_rd(os, &alpha, &gamma, 4, 4, 0, -1, &oc, err, 512) == 0, "%s", err);
+  const int64_t n = lfo_coo_size(oc);
+  std::vector<int32_t> r(n), c(n);
+  std::vector<double> v(n);
+  lfo_coo_copy(oc, r.data(), c.data(), v.data());
+  CHECK(static_cast<int64_t>(t.size()) == n, "triplet count %zu vs %lld", t.size(), static_cast<long long>(n));
+  const int nloc = (degree + 1) * (degree + 2) / 2, blk = nloc * nloc;
+  for (int64_t k0 = 0; k0 < n && static_cast<size_t>(k0) < t.size(); k0 += blk) {
+    double scale = 0.0;
+    for (int q = 0; q < blk; ++q) scale = std::fmax(scale, std::fabs(v[k0 + q]));
+    for (int q = 0; q < blk; ++q) {
+      const int64_t k = k0 + q;
+      CHECK(t[k].row == r[k] && t[k].col == c[k], "index mismatch at %lld", static_cast<long long>(k));
+      CHECK(std::fabs(t[k].value - v[k]) <= 1e-12 * scale, "value mismatch at %lld: %.17g vs %.17g",
+            static_cast<long long>(k), t[k].value, v[k]);
+    }
+  }
+  std::vector<double> bo(nd, 0.0);
+  CHECK(lfo_assemble_load(os, &f, 4, 4, bo.data(), err, 512) == 0, "%s", err);
+  const std::vector<double> bg = b.Download();
+  double bmax = 0.0, berr = 0.0;
+  for (int64_t i = 0; i < nd; ++i) {
+    bmax = std::fmax(bmax, std::fabs(bo[i]));
+    berr = std::fmax(berr, std::fabs(bg[i] - bo[i]));
+  }
+  CHECK(berr <= 1e-12 * bmax, "load vector error %.3g of %.3g", berr, bmax);
+  lfo_coo_destroy(oc);
+  lfo_space_destroy(os);
+  lfo_mesh_destroy(om);
+  lfo_input_destroy(in);
+
+  // Dirichlet 0 on the boundary, solve
+  g::DeviceVector<uint8_t> flags = fes->BoundaryDofFlags();
+  g::DeviceVector<double> zero(ctx, nd);
+  zero.SetZero();
+  g::assemble::FixFlaggedSolutionComponents(flags, zero, A, b);
+  g::solve::CSRMatrix S = A.makeSparse();
+  g::DeviceVector<double> x(ctx, nd);
+  x.SetZero();
+  g::solve::SolveOptions so;
+  so.rtol = 1e-12;
+  const lfg_solve_stats st = g::solve::SolvePCG(ctx, S, b, x, so);
+  CHECK(st.converged && st.rel_residual <= 1e-12, "PCG: converged %d residual %.3g", st.converged, st.rel_residual);
+  std::printf("assembly O%d %dx%d: %lld triplets, %lld dofs, PCG %d iterations\n", degree, nx, ny,
+              static_cast<long long>(n), static_cast<long long>(nd), st.iterations);
+
+  // capacity errors surface as lf::gb300::Error
+  g::assemble::COOMatrix small(ctx, nd, nd, 4);
+  bool threw = false;
+  try {
+    g::assemble::AssembleMatrixLocally(0, *fes, *fes, rd, small);
+  } catch (const g::Error& e) {
+    threw = e.code() == LFG_CAPACITY;
+  }
+  CHECK(threw, "capacity overflow did not throw LFG_CAPACITY");
+}
+
+static double Lcg(uint64_t& s) {
+  s = s * 6364136223846793005ull + 1442695040888963407ull;
+  return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
+}
+
+static void CheckAdjoint(const g::Context& ctx) {
+  auto mesh = g::mesh::TPTriagMeshBuilder(ctx).setNumXCells(8).setNumYCells(8).Build();
+  auto fes = g::uscalfe::FeSpaceLagrangeO<1>(mesh);
+  const int64_t nc = mesh->NumEntities(0), nd = fes->NumDofs();
+  uint64_t seed = 12345;
+  std::vector<double> th(nc), uo(nd);
+  for (auto& t : th) t = Lcg(seed) - 0.5;
+  for (auto& u : uo) u = 0.02 * Lcg(seed);
+  g::DeviceVector<double> theta(ctx, th), u_obs(ctx, uo), grad(ctx, nc);
+  g::adjoint::InverseConductivityFunction::Options o;
+  o.solve.rtol = 1e-14;
+  g::adjoint::InverseConductivityFunction F(fes, u_obs, o);
+  const double J = F.Forward(theta);
+  F.Backward(1.0, grad);
+  const std::vector<double> gr = grad.Download();
+  double gmax = 0.0;
+  for (double x : gr) gmax = std::fmax(gmax, std::fabs(x));
+  const double h = 1e-6;
+  double worst = 0.0;
+  for (int k = 0; k < 8; ++k) {
+    const int64_t cidx = (k * 37 + 5) % nc;
+    std::vector<double> tp = th, tm = th;
+    tp[cidx] += h;
+    tm[cidx] -= h;
+    g::DeviceVector<double> dp(ctx, tp), dm(ctx, tm);
+    const double fd = (F.Forward(dp) - F.Forward(dm)) / (2 * h);
+    worst = std::fmax(worst, std::fabs(fd - gr[cidx]));
+  }
+  CHECK(worst <= 1e-6 * gmax, "central differences: error %.3g of max |g| %.3g", worst, gmax);
+  // recompute mode: the same bits, only theta saved
+  o.recompute = true;
+  g::adjoint::InverseConductivityFunction R(fes, u_obs, o);
+  g::DeviceVector<double> grad2(ctx, nc);
+  const double J2 = R.Forward(theta);
+  CHECK(R.SavedBytes() == nc * 8, "recompute mode saved %lld bytes", static_cast<long long>(R.SavedBytes()));
+  R.Backward(1.0, grad2);
+  const std::vector<double> g2 = grad2.Download();
+  CHECK(J2 == J && std::memcmp(g2.data(), gr.data(), nc * sizeof(double)) == 0, "recompute mode differs");
+  std::printf("adjoint: J %.6g, max |dJ/dtheta| %.3g, FD error %.3g\n", J, gmax, worst);
+}
+
+int main() {
+  try {
+    g::Context ctx(0);
+    CheckAssembly(ctx, 12, 10, 1);
+    CheckAssembly(ctx, 9, 7, 2);
+    CheckAssembly(ctx, 6, 5, 3);
+    CheckAdjoint(ctx);
+  } catch (const g::Error& e) {
+    std::printf("FAIL: uncaught lf::gb300::Error %d: %s\n", static_cast<int>(e.code()), e.what());
+    return 1;
+  }
+  if (failures) {
+    std::printf("%d check(s) failed\n", failures);
+    return 1;
+  }
+  std::printf("facade_test OK\n");
+  return 0;
+}

@@ -56,3 +56,17 @@ def test_workload_generators():
     assert len(wl["alpha"][1]) == len(wl["mesh"]["cells"])
     ns, degs = W.batch_sizes()
     assert ns.min() >= 24 and ns.max() <= 320 and set(degs) == {1, 2}
+
+
+def test_cpp_facade_compiles_and_links(tmp_path):
+    """The C++ facade header compiles as C++17 and its driver links against
+    liblfg.so and the oracle library (no GPU call is made)."""
+    from parity import L, O
+    L.load()
+    O.lib()
+    lib_dir, orc_dir = os.path.dirname(L.LIB_PATH), os.path.dirname(O._LIB_PATH)
+    exe = str(tmp_path / "facade_test")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "facade_test.cc"), "-L", lib_dir, "-llfg", "-L", orc_dir,
+                    "-loracle", "-Wl,-rpath," + lib_dir + ":" + orc_dir, "-o", exe], check=True)
+    assert os.path.exists(exe)

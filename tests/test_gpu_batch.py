@@ -1,0 +1,85 @@
+"""Batched form (GPU): persistent multi-mesh assembly and batched PCG.
+
+Each mesh's segment of the batch COO must equal that mesh's own assembly
+(indices shifted by the mesh's dof offset, identical order and values), and
+each block of the batched solve must match a direct FP64 solve of the oracle's
+system for that mesh."""
+import numpy as np
+import pytest
+
+from parity import O, L, W, block_sizes, compare_triplets, oracle_coeff
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(ctx, ns, degs, seed=9):
+    rng = np.random.default_rng(seed)
+    meshes = [L.Mesh.tp_triag(ctx, int(n), int(n)) for n in ns]
+    spaces = [L.Space.lagrange(m, int(d)) for m, d in zip(meshes, degs)]
+    batch = L.Batch(ctx, spaces)
+    alpha = np.exp(0.5 * rng.standard_normal(batch.num_cells))
+    return meshes, spaces, batch, alpha
+
+
+def _assemble(ctx, batch, alpha_d, gamma=1.0):
+    coo = L.COOMatrix(ctx, batch.num_dofs, batch.num_dofs, batch.num_triplets + batch.num_dofs)
+    batch.assemble_matrix_rd(L.rd_provider(L.coeff(L.PER_CELL, data=alpha_d), L.coeff(L.CONSTANT, gamma)), coo)
+    return coo
+
+
+def test_batch_assembly_matches_single_meshes(ctx):
+    ns, degs = [3, 5, 7, 4, 6, 8, 2, 9], [1, 2, 1, 2, 2, 1, 3, 2]
+    meshes, spaces, batch, alpha = _batch(ctx, ns, degs)
+    alpha_d = ctx.to_device(alpha)
+    coo = _assemble(ctx, batch, alpha_d)
+    th, ct, ms = batch.tuning()
+    assert th in (64, 128, 256) and ct >= 1 and ms > 0
+    t = coo.triplets()
+    dof, cell, trip = batch.offsets()
+    assert len(t) == trip[-1]
+    for b, (sp, n, d) in enumerate(zip(spaces, ns, degs)):
+        seg = t[trip[b]:trip[b + 1]]
+        a_b = ctx.to_device(alpha[cell[b]:cell[b + 1]])
+        single = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets)
+        L.assemble_matrix_rd(sp, L.rd_provider(L.coeff(L.PER_CELL, data=a_b), L.coeff(L.CONSTANT, 1.0)), single)
+        st = single.triplets()
+        assert np.array_equal(seg["row"] - dof[b], st["row"]) and np.array_equal(seg["col"] - dof[b], st["col"])
+        assert np.array_equal(seg["value"], st["value"])
+        xy, cells, pe = O.factory_input("tptriag", n, n)
+        os_ = O.Space(O.Mesh(xy, cells, pe), d)
+        A = O.assemble_rd(os_, O.coeff(O.PER_CELL, data=alpha[cell[b]:cell[b + 1]]), O.coeff(O.CONSTANT, 1.0))
+        ro, co, vo = A.arrays()
+        seg2 = seg.copy()
+        seg2["row"] -= dof[b]
+        seg2["col"] -= dof[b]
+        compare_triplets(seg2, ro, co, vo, block_sizes(cells, os_.n_tria, os_.n_quad))
+
+
+@pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
+def test_batch_solve_matches_direct_solves(ctx, precision):
+    import scipy.sparse.linalg as spla
+    ns, degs = [6, 11, 4, 9, 14, 7], [1, 2, 2, 1, 2, 1]
+    meshes, spaces, batch, alpha = _batch(ctx, ns, degs, seed=3)
+    alpha_d = ctx.to_device(alpha)
+    coo = _assemble(ctx, batch, alpha_d)
+    b = ctx.zeros(batch.num_dofs)
+    batch.assemble_vector_load(L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+    coo.fix_flagged_solution_components(batch.boundary_dof_flags(), ctx.zeros(batch.num_dofs), b)
+    csr = coo.make_sparse()
+    x = ctx.zeros(batch.num_dofs)
+    st = batch.solve_pcg(csr, b, x, precision=precision, rtol=1e-12, check_every=8)
+    assert st["converged"] and all(blk["converged"] for blk in st["blocks"])
+    xs = x.download()
+    dof, cell, _ = batch.offsets()
+    for k, (n, d) in enumerate(zip(ns, degs)):
+        xy, cells, pe = O.factory_input("tptriag", n, n)
+        os_ = O.Space(O.Mesh(xy, cells, pe), d)
+        A = O.assemble_rd(os_, O.coeff(O.PER_CELL, data=alpha[cell[k]:cell[k + 1]]), O.coeff(O.CONSTANT, 1.0))
+        bo = O.assemble_load(os_, O.coeff(O.CONSTANT, 1.0))
+        A.fix_flagged(os_.boundary_dof_flags(), np.zeros(os_.num_dofs), bo)
+        xo = spla.splu(A.to_scipy().tocsc()).solve(bo)
+        err = np.linalg.norm(xs[dof[k]:dof[k + 1]] - xo) / np.linalg.norm(xo)
+        assert err <= 1e-8, (k, err)
+    # blocks of different size take different iteration counts
+    its = [blk["iterations"] for blk in st["blocks"]]
+    assert max(its) > min(its)
