@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--solve-size", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=512, help="config-4 meshes (0: skip the batch leg)")
+    ap.add_argument("--grad-size", type=int, default=1024, help="config-5 mesh size (0: skip the gradient leg)")
     return ap.parse_args()
 
 
@@ -114,20 +116,6 @@ def algorithmic_bytes(space, mesh, kind):
         n, nv, cells = space.n_quad, 4, mesh.num_quads
     per_cell = 16 * n * n + 4 * nv + 16 * nv + 8 + 4 * n
     return per_cell * cells, per_cell
-
-
-def fp64_flops(space, mesh, kind):
-    """FP64 operations the kernels issue per cell (counted from the source):
-    triangles (folded rule): metric ~14 + 3 FMA per upper-triangle entry;
-    quadrilaterals: per point ~22 (metric) + 3 FMA per upper-triangle entry."""
-    if kind == "tria":
-        n = space.n_tria
-        e = n * (n + 1) // 2
-        return (2 * (14 + 3 * e)) * mesh.num_trias
-    n = space.n_quad
-    e = n * (n + 1) // 2
-    nq = 9
-    return (2 * nq * (22 + 3 * e)) * mesh.num_quads
 
 
 def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
@@ -207,6 +195,171 @@ def solve_leg(L, W, ctx, n):
     return out
 
 
+def batch_leg(L, W, ctx, count):
+    """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
+    one persistent assembly launch + load + fix + COO->CSR + batched PCG to
+    relative residual 1e-10 per mesh.  DOFs/s of the batched mixed and FP64
+    solves, of the plain path (one mesh at a time: assemble, fix, CSR, FP64
+    PCG) on every 8th mesh, and the per-mesh error against a batched FP64
+    solve to 1e-13."""
+    wl = W.config4(count)
+    t0 = time.perf_counter()
+    meshes = [L.Mesh.tp_triag(ctx, int(n), int(n)) for n in wl["ns"]]
+    spaces = [L.Space.lagrange(m, int(d)) for m, d in zip(meshes, wl["degrees"])]
+    batch = L.Batch(ctx, spaces)
+    setup_s = time.perf_counter() - t0
+    nd = batch.num_dofs
+    alpha_d = ctx.to_device(wl["alpha"])
+    prov = L.rd_provider(L.coeff(L.PER_CELL, data=alpha_d), L.coeff(L.CONSTANT, wl["gamma"]))
+    lprov = L.load_provider(L.coeff(L.CONSTANT, wl["f"]))
+    flags = batch.boundary_dof_flags()
+    zeros = ctx.zeros(nd)
+    dof, _, _ = batch.offsets()
+
+    def run(precision, rtol):
+        coo = L.COOMatrix(ctx, nd, nd, batch.num_triplets + nd)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        l0 = ctx.launches()
+        batch.assemble_matrix_rd(prov, coo)
+        b = ctx.zeros(nd)
+        batch.assemble_vector_load(lprov, b)
+        coo.fix_flagged_solution_components(flags, zeros, b)
+        A = coo.make_sparse()
+        del coo
+        x = ctx.zeros(nd)
+        st = batch.solve_pcg(A, b, x, precision=precision, rtol=rtol, raise_on_failure=False)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        return x, st, dt, ctx.launches() - l0
+
+    run(L.SOLVE_MIXED, 1e-10)  # autotunes the assembly launch, warms allocations
+    out = {"workload": "%d TPTriag meshes n in [24, 320] log-uniform, O1/O2 50/50, alpha LogNormal(0, 0.5^2), "
+                       "gamma 1, f 1, Dirichlet 0" % count,
+           "meshes": count, "dofs": int(nd), "cells": int(batch.num_cells), "triplets": int(batch.num_triplets),
+           "setup_s": setup_s}
+    th, ct, ms = batch.tuning()
+    out["autotuner"] = {"threads_per_cta": th, "ctas_per_sm": ct, "assembly_ms": ms}
+    xs = {}
+    for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
+        x, st, dt, launches = run(prec, 1e-10)
+        xs[name] = x.download()
+        its = [blk["iterations"] for blk in st["blocks"]]
+        out[name] = {"dofs_per_s": nd / dt, "seconds": dt, "gpu_launches": launches, "max_iterations": max(its),
+                     "all_converged": bool(st["converged"])}
+    xr, st, _, _ = run(L.SOLVE_FP64, 1e-13)
+    r = xr.download()
+    for name in xs:
+        errs = [float(np.linalg.norm(xs[name][dof[k]:dof[k + 1]] - r[dof[k]:dof[k + 1]]) /
+                      np.linalg.norm(r[dof[k]:dof[k + 1]])) for k in range(count)]
+        out[name]["per_mesh_rel_err_vs_fp64_1e-13"] = {"max": max(errs), "median": statistics.median(errs)}
+    # the plain FP64 path, one mesh after another, on every 8th mesh
+    sample = list(range(0, count, 8))
+    sd = 0
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for k in sample:
+        sp = spaces[k]
+        c0, c1 = int(batch.offsets()[1][k]), int(batch.offsets()[1][k + 1])
+        a_k = ctx.to_device(wl["alpha"][c0:c1])
+        coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets + sp.num_dofs)
+        L.assemble_matrix_rd(sp, L.rd_provider(L.coeff(L.PER_CELL, data=a_k), L.coeff(L.CONSTANT, wl["gamma"])), coo)
+        b = ctx.zeros(sp.num_dofs)
+        L.assemble_vector_load(sp, lprov, b)
+        coo.fix_flagged_solution_components(sp.boundary_dof_flags(), ctx.zeros(sp.num_dofs), b)
+        A = coo.make_sparse()
+        x = ctx.zeros(sp.num_dofs)
+        A.solve_pcg(b, x, precision=L.SOLVE_FP64, rtol=1e-10, raise_on_failure=False)
+        sd += sp.num_dofs
+    ctx.synchronize()
+    dt = time.perf_counter() - t0
+    out["plain_fp64"] = {"dofs_per_s": sd / dt, "seconds": dt, "sample": "every 8th mesh (%d meshes, %d dofs)" %
+                                                                         (len(sample), sd)}
+    out["mixed_batched_vs_plain_fp64"] = out["mixed"]["dofs_per_s"] / out["plain_fp64"]["dofs_per_s"]
+    return out
+
+
+def gradient_leg(L, W, ctx, n, steps, cpu_check=True):
+    """Config 5: TPTriag n x n, O1, alpha = exp(theta), theta ~ N(0, 0.5^2).
+    One gradient evaluation = forward (assemble, fix, CSR, FP64 PCG to
+    relative residual 1e-9, J) + backward (adjoint FP64 PCG, cellwise
+    gradient kernel).  At this size the FP64 rounding floor of the relative
+    residual, eps ||A|| ||u|| / ||b||, is about 1e-10 (b scales with h^2).  Observations
+    come from theta_true (8 Gaussian bumps) + N(0, 1e-3^2) noise."""
+    wl = W.config5(n)
+    mesh = L.Mesh.tp_triag(ctx, n, n)
+    sp = L.Space.lagrange(mesh, 1)
+    xy, cells = mesh.geometry()
+    tt = ctx.to_device(W.theta_true(W.cell_centroids(xy, cells)))
+    lprov = L.load_provider(L.coeff(L.CONSTANT, 1.0))
+    u_true = ctx.zeros(sp.num_dofs)
+    L.RDAdjoint(sp, ctx.zeros(sp.num_dofs), lprov, rtol=1e-9).forward(tt, u_true)
+    u_obs = ctx.to_device(u_true.download() + W.observation_noise(sp.num_dofs))
+    theta = ctx.to_device(wl["theta"])
+    grad = ctx.zeros(mesh.num_cells)
+    out = {"workload": "TPTriag %dx%d O1 (%d cells, %d dofs), alpha = exp(theta), gamma 0, f 1, Dirichlet 0" %
+                       (n, n, mesh.num_cells, sp.num_dofs)}
+    for mode in ("store", "recompute"):
+        fn = L.RDAdjoint(sp, u_obs, lprov, rtol=1e-9, recompute=(mode == "recompute"))
+        fn.forward(theta)
+        fn.backward(grad)  # warm-up
+        ctx.synchronize()
+        ctx.profile(True)
+        ctx.profile_reset()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            J = fn.forward(theta)
+            saved = fn.stats()["saved_bytes"]
+            fn.backward(grad)
+        ctx.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        gt, gn = ctx.profile_read("grad_rd")
+        ctx.profile(False)
+        st = fn.stats()
+        out[mode] = {"grad_evals_per_s": 1.0 / dt, "seconds_per_eval": dt, "J": J,
+                     "saved_bytes_between_calls": saved, "forward_iterations": st["forward"]["iterations"],
+                     "adjoint_iterations": st["adjoint"]["iterations"],
+                     "grad_kernel_ms": gt / max(gn, 1)}
+        del fn
+    g = grad.download()
+    out["max_abs_grad"] = float(np.abs(g).max())
+    # the gradient kernel alone against its HBM roofline: per cell 16 (cell
+    # nodes) + 3 * 16 (coordinates) + 3 * 4 (dofs) + 3 * 8 (u) + 3 * 8 (lambda)
+    # + 3 (flags) + 8 (theta) + 8 (gradient) bytes
+    per_cell = 16 + 48 + 12 + 24 + 24 + 3 + 8 + 8
+    kms = out["store"]["grad_kernel_ms"]
+    out["grad_kernel"] = {"bytes_per_cell": per_cell, "achieved_gbs": per_cell * mesh.num_cells / (kms * 1e-3) / 1e9}
+    if cpu_check:
+        out["cpu_baseline"] = gradient_cpu_check(L, W, ctx, 128)
+    return out
+
+
+def gradient_cpu_check(L, W, ctx, n):
+    """The oracle's FP64 CPU gradient (element matrices + two SparseLU solves)
+    at n x n, timed on one host core, and the GPU gradient on the same inputs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    wl = W.config5(n)
+    xy_o, cells_o, pe = O.factory_input("tptriag", n, n)
+    osp = O.Space(O.Mesh(xy_o, cells_o, pe), 1)
+    flags = osp.boundary_dof_flags()
+    rng_obs = 0.01 * np.random.default_rng(77).standard_normal(osp.num_dofs)
+    t0 = time.perf_counter()
+    J, _, _, g_ref = O.adjoint_gradient(osp, wl["theta"], O.coeff(O.CONSTANT, 1.0), rng_obs, flags)
+    cpu_s = time.perf_counter() - t0
+    mesh = L.Mesh.tp_triag(ctx, n, n)
+    sp = L.Space.lagrange(mesh, 1)
+    fn = L.RDAdjoint(sp, ctx.to_device(rng_obs), L.load_provider(L.coeff(L.CONSTANT, 1.0)), rtol=1e-11)
+    Jg = fn.forward(ctx.to_device(wl["theta"]))
+    grad = ctx.zeros(mesh.num_cells)
+    fn.backward(grad)
+    g = grad.download()
+    return {"value": 1.0 / cpu_s, "unit": "gradient evaluations/s", "cores": 1, "kind": "port",
+            "sample": "oracle FP64 gradient (SparseLU) on TPTriag %dx%d O1, not the full-size workload" % (n, n),
+            "gpu_rel_err_vs_cpu_fp64": float(np.abs(g - g_ref).max() / np.abs(g_ref).max()),
+            "loss_rel_diff": abs(Jg - J) / J}
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import lehrfempp_gb300 as L
@@ -276,9 +429,6 @@ def run_ours(args):
         peaks_src = "fallback 6800 GB/s"
         hbm_peak = 6800.0
     achieved = alg_bytes / (fam[dom][0] * 1e-3) / 1e9
-    fp64_peak = ctx.fp64_peak_tflops()
-    fl = fp64_flops(space, mesh, kind)
-    fp64_ach = fl / (fam[dom][0] * 1e-3) / 1e12
     whole_bytes = sum(algorithmic_bytes(space, mesh, k)[0] for k in ("tria", "quad"))
 
     # load vector (AssembleVectorLocally) time, informational
@@ -307,9 +457,18 @@ def run_ours(args):
         e2e = {"value": world * ntrip / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(alpha_h.nbytes),
                "d2h_bytes_per_step": int(ntrip * 16), "ms_per_step": e2e_s * 1e3}
         del t_pin
-    solve = None
-    if args.solve_size > 0:
-        solve = solve_leg(L, W, ctx, args.solve_size)
+    del coo
+
+    def leg(fn, *a, **k):
+        try:
+            return fn(*a, **k)
+        except Exception as e:  # a failing side leg is reported, not fatal to the headline line
+            return {"error": "%s: %s" % (type(e).__name__, e)}
+
+    solve = leg(solve_leg, L, W, ctx, args.solve_size) if args.solve_size > 0 else None
+    batch = leg(batch_leg, L, W, ctx, args.batch_count) if args.batch_count > 0 else None
+    gradient = leg(gradient_leg, L, W, ctx, args.grad_size, steps=3,
+                   cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.grad_size > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -330,14 +489,12 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None, "kernel": dom,
                          "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_cell": per_cell,
-                         "avg_launch_ms": fam[dom][0], "peak_source": peaks_src,
-                         "fp64": {"achieved_tflops": fp64_ach, "peak_tflops_measured": fp64_peak,
-                                  "frac": fp64_ach / fp64_peak}},
+                         "avg_launch_ms": fam[dom][0], "peak_source": peaks_src},
             "kernels_ms": {k: v[0] for k, v in fam.items()},
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "solve": solve,
+            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "batch": batch, "gradient": gradient,
         }
         print(json.dumps(line))
     ctx.close()

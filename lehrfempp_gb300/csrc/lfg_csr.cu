@@ -8,12 +8,21 @@
 // order) and each run is summed left to right, which reproduces those sums
 // bit for bit.
 //
-// The solver keeps every scalar on the device: a PCG iteration is three
-// kernels (SpMV fused with <p, Ap>; x/r/z update fused with <r, z> and <r, r>;
-// p update), block partial sums are reduced by every consumer block in the
-// same fixed order (deterministic), and the iteration body is captured in a
-// CUDA graph replayed `check_every` iterations at a time.
+// The solver keeps every scalar on the device.  A PCG iteration is two
+// kernels: (1) the search-direction update p = z + beta p_old fused into the
+// SpMV q = A p over a SELL-32 copy of the matrix (one thread per row, the
+// row's entries loaded column-major across the warp, so every load of a
+// slice is coalesced and a thread's loads are independent), with <p, q>;
+// (2) x += alpha p, r -= alpha q, z = D^-1 r with <r, z> and <r, r>.  Each
+// kernel's block partials are summed by the last block to finish (counter +
+// fence), in block order, so the scalars alpha and beta are deterministic and
+// computed once; the next kernel reads them from device memory.  The neighbour
+// values p_c = z_c + beta p_old_c are recomputed inside the SpMV with the same
+// fma as the row owner, so p needs two buffers (read old, write new).  The
+// iteration body is captured in a CUDA graph replayed `check_every`
+// iterations at a time; the host reads one residual norm per replay.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <vector>
 
@@ -154,9 +163,19 @@ __global__ void ResidualKernel(int64_t rows, const int32_t* __restrict__ rp, con
 
 // ------------------------------------------------------------------- PCG
 constexpr int kPcgBlock = 256;
+constexpr int kSlice = 32;
 
-template <class T>
-__device__ double BlockSum(double v, double* red) {
+// Scalars of one PCG run, on the device.  rz[cur] is <r, z> of the current
+// residual; the update kernel writes rz[cur ^ 1].
+struct PcgScalars {
+  double rz[2];
+  double alpha, beta, rr, pq;
+  unsigned int counter;
+  unsigned int pad;
+};
+
+// Block sum of v (warp shuffles, then warps in order); result in thread 0.
+__device__ __forceinline__ double BlockSum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -167,107 +186,236 @@ __device__ double BlockSum(double v, double* red) {
   return s;
 }
 
-// Every block sums the same partial array in the same order.
-__device__ double SumPartials(const double* __restrict__ part, int n, double* red) {
-  double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+// Publishes this block's partials (already written by thread 0) and tells
+// whether this block finished last.  No block waits for another.
+__device__ __forceinline__ bool FinishedLast(unsigned int* counter) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < (blockDim.x >> 5); ++w) s += red[w];
-  __syncthreads();
-  return s;
+  return last;
 }
 
-// q = A p and partials of <p, q>.
+// Sum of part[j * stride + off], j < n, in a fixed order (per-thread strided
+// sums, then BlockSum); called by the last block only.
+__device__ double SumParts(const double* part, int n, int stride, int off, double* red) {
+  double v = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) v += __ldcg(part + static_cast<int64_t>(j) * stride + off);
+  return BlockSum(v, red);
+}
+
+// Per-thread dot-product accumulator: FP64 for FP64 vectors; for FP32
+// vectors a float sum of the thread's few terms, widened once (every FP32 ->
+// FP64 conversion and FP64 FMA runs on GB300's narrow FP64 pipe).
 template <class T>
-__global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, const int32_t* __restrict__ rp,
-                                                           const int32_t* __restrict__ col,
-                                                           const T* __restrict__ val, const T* __restrict__ p,
-                                                           T* __restrict__ q, double* __restrict__ part) {
+struct DotAcc {
+  double v = 0.0;
+  __device__ void add(T a, T b) { v = fma(a, b, v); }
+  __device__ double get() const { return v; }
+};
+template <>
+struct DotAcc<float> {
+  float v = 0.0f;
+  __device__ void add(float a, float b) { v = fmaf(a, b, v); }
+  __device__ double get() const { return static_cast<double>(v); }
+};
+
+// q = A p (SELL-32) and alpha = rz[cur] / <p, q>.  FUSED: p is formed on the
+// fly as p_new = z + beta p_old (neighbour values recomputed with the owner's
+// fma; p_new written by the owner) -- used for FP32, where the extra FMAs are
+// cheap.  Otherwise p_old is the finished direction and p_new is unused.
+template <class T, bool FUSED>
+__global__ void __launch_bounds__(kPcgBlock) PcgSpmvDirKernel(int64_t rows, int64_t nslices,
+                                                              const int64_t* __restrict__ sptr,
+                                                              const int32_t* __restrict__ scol,
+                                                              const T* __restrict__ sval, const T* __restrict__ z,
+                                                              const T* __restrict__ p_old, T* __restrict__ p_new,
+                                                              T* __restrict__ q, int cur, double* __restrict__ part,
+                                                              PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
-  T acc = T(0);
-  LFG_ROW_LOOP(i) {
-    const T s = RowDot<T, T>(rp, col, val, p, i, rows, sub);
-    if (sub == 0 && i < rows) {
-      q[i] = s;
-      acc = fma(p[i], s, acc);
+  __shared__ T sbeta;
+  if (threadIdx.x == 0) sbeta = FUSED ? static_cast<T>(sc->beta) : T(0);
+  __syncthreads();
+  const T beta = sbeta;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  DotAcc<T> acc;
+  for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+    const int64_t r = sl * kSlice + lane;
+    const int64_t b0 = sptr[sl];
+    const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
+    if (r < rows) {
+      const int32_t* cp = scol + b0 + lane;
+      const T* vp = sval + b0 + lane;
+      T sum = T(0);
+#pragma unroll 4
+      for (int k = 0; k < w; ++k) {
+        const int c = cp[k * kSlice];
+        const T pc = FUSED ? fma(beta, p_old[c], z[c]) : p_old[c];
+        sum = fma(vp[k * kSlice], pc, sum);
+      }
+      const T pi = FUSED ? fma(beta, p_old[r], z[r]) : p_old[r];
+      if (FUSED) p_new[r] = pi;
+      q[r] = sum;
+      acc.add(pi, sum);
     }
   }
-  const double tot = BlockSum<T>(static_cast<double>(acc), red);
+  const double tot = BlockSum(acc.get(), red);
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
+  if (FinishedLast(&sc->counter)) {
+    const double pq = SumParts(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      sc->pq = pq;
+      sc->alpha = pq != 0.0 ? sc->rz[cur] / pq : 0.0;
+      sc->counter = 0;
+    }
+  }
 }
 
-// alpha = rz / <p,q>; x += alpha p; r -= alpha q; z = D^-1 r; partials <r,z>, <r,r>.
+// x += alpha p; r -= alpha q; z = D^-1 r; rz[cur ^ 1] = <r, z>, rr = <r, r>,
+// beta = rz[cur ^ 1] / rz[cur].  Several elements per thread and trip, loads
+// first, so each thread keeps several independent loads in flight.
 template <class T>
-__global__ void __launch_bounds__(kPcgBlock) PcgUpdateKernel(int64_t rows, const double* __restrict__ pq_part,
-                                                             const double* __restrict__ rz_old_part, int nparts,
-                                                             const T* __restrict__ dinv, const T* __restrict__ p,
-                                                             const T* __restrict__ q, T* __restrict__ x,
-                                                             T* __restrict__ r, T* __restrict__ z,
-                                                             double* __restrict__ rz_part,
-                                                             double* __restrict__ rr_part) {
+__global__ void __launch_bounds__(kPcgBlock, 4) PcgUpdateKernel(int64_t rows, const T* __restrict__ dinv,
+                                                             const T* __restrict__ p, const T* __restrict__ q,
+                                                             T* __restrict__ x, T* __restrict__ r,
+                                                             T* __restrict__ z, int cur, double* __restrict__ part,
+                                                             PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
-  const double pq = SumPartials(pq_part, nparts, red);
-  const double rz = SumPartials(rz_old_part, nparts, red);
-  const T alpha = static_cast<T>(pq != 0.0 ? rz / pq : 0.0);
-  T arz = T(0), arr = T(0);
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    x[i] = fma(alpha, p[i], x[i]);
-    const T ri = fma(-alpha, q[i], r[i]);
-    r[i] = ri;
-    const T zi = dinv[i] * ri;
-    z[i] = zi;
-    arz = fma(ri, zi, arz);
-    arr = fma(ri, ri, arr);
+  __shared__ T salpha;
+  if (threadIdx.x == 0) salpha = static_cast<T>(sc->alpha);
+  __syncthreads();
+  const T alpha = salpha;
+  DotAcc<T> arz, arr;
+  constexpr int U = sizeof(T) == 8 ? 2 : 4;  // elements per thread and trip
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i0 < rows; i0 += U * stride) {
+    T pv[U], qv[U], xv[U], rv[U], dv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < rows) {
+        pv[u] = p[i]; qv[u] = q[i]; xv[u] = x[i]; rv[u] = r[i]; dv[u] = dinv[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < rows) {
+        x[i] = fma(alpha, pv[u], xv[u]);
+        const T ri = fma(-alpha, qv[u], rv[u]);
+        r[i] = ri;
+        const T zi = dv[u] * ri;
+        z[i] = zi;
+        arz.add(ri, zi);
+        arr.add(ri, ri);
+      }
+    }
   }
-  const double s1 = BlockSum<T>(static_cast<double>(arz), red);
-  const double s2 = BlockSum<T>(static_cast<double>(arr), red);
+  const double s1 = BlockSum(arz.get(), red);
+  const double s2 = BlockSum(arr.get(), red);
   if (threadIdx.x == 0) {
-    rz_part[blockIdx.x] = s1;
-    rr_part[blockIdx.x] = s2;
+    part[2 * blockIdx.x] = s1;
+    part[2 * blockIdx.x + 1] = s2;
+  }
+  if (FinishedLast(&sc->counter)) {
+    const double rz = SumParts(part, gridDim.x, 2, 0, red);
+    const double rr = SumParts(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      const double rz_old = sc->rz[cur];
+      sc->rz[cur ^ 1] = rz;
+      sc->beta = rz_old != 0.0 ? rz / rz_old : 0.0;
+      sc->rr = rr;
+      sc->counter = 0;
+    }
   }
 }
 
-// beta = rz_new / rz_old; p = z + beta p.
+// p = z + beta p (the FP64 path's separate direction update: one FP64 FMA
+// per row instead of one per matrix entry in the fused SpMV).
 template <class T>
-__global__ void __launch_bounds__(kPcgBlock) PcgDirectionKernel(int64_t rows, const double* __restrict__ rz_new_part,
-                                                                const double* __restrict__ rz_old_part, int nparts,
-                                                                const T* __restrict__ z, T* __restrict__ p) {
-  __shared__ double red[32];
-  const double rn = SumPartials(rz_new_part, nparts, red);
-  const double ro = SumPartials(rz_old_part, nparts, red);
-  const T beta = static_cast<T>(ro != 0.0 ? rn / ro : 0.0);
+__global__ void __launch_bounds__(kPcgBlock) PcgDirectionKernel(int64_t rows, const T* __restrict__ z,
+                                                                T* __restrict__ p, const PcgScalars* __restrict__ sc) {
+  __shared__ T sbeta;
+  if (threadIdx.x == 0) sbeta = static_cast<T>(sc->beta);
+  __syncthreads();
+  const T beta = sbeta;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     p[i] = fma(beta, p[i], z[i]);
 }
 
-// z = D^-1 r, p = z, partials <r,z>, <r,r> (PCG start).
+// z = D^-1 r, p_old = z (so the first direction update, with beta = 0, gives
+// p = z), rz[0] = <r, z>, rr = <r, r>.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgStartKernel(int64_t rows, const T* __restrict__ dinv,
                                                             const T* __restrict__ r, T* __restrict__ z,
-                                                            T* __restrict__ p, double* __restrict__ rz_part,
-                                                            double* __restrict__ rr_part) {
+                                                            T* __restrict__ p, double* __restrict__ part,
+                                                            PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
-  T arz = T(0), arr = T(0);
+  double arz = 0.0, arr = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const T ri = r[i];
     const T zi = dinv[i] * ri;
     z[i] = zi;
     p[i] = zi;
-    arz = fma(ri, zi, arz);
-    arr = fma(ri, ri, arr);
-  }
-  const double s1 = BlockSum<T>(static_cast<double>(arz), red);
-  const double s2 = BlockSum<T>(static_cast<double>(arr), red);
+    arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
+    arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
+  }  // (once per run: FP64 accumulation regardless of T)
+  const double s1 = BlockSum(arz, red);
+  const double s2 = BlockSum(arr, red);
   if (threadIdx.x == 0) {
-    rz_part[blockIdx.x] = s1;
-    rr_part[blockIdx.x] = s2;
+    part[2 * blockIdx.x] = s1;
+    part[2 * blockIdx.x + 1] = s2;
+  }
+  if (FinishedLast(&sc->counter)) {
+    const double rz = SumParts(part, gridDim.x, 2, 0, red);
+    const double rr = SumParts(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      sc->rz[0] = rz;
+      sc->rz[1] = 0.0;
+      sc->beta = 0.0;
+      sc->alpha = 0.0;
+      sc->rr = rr;
+      sc->counter = 0;
+    }
+  }
+}
+
+// SELL-32 construction: width of each slice (longest row, times 32)...
+__global__ void SellWidthKernel(int64_t rows, int64_t nslices, const int64_t* __restrict__ rp,
+                                int64_t* __restrict__ width) {
+  for (int64_t sl = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; sl < nslices;
+       sl += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t w = 0;
+    for (int l = 0; l < kSlice; ++l) {
+      const int64_t r = sl * kSlice + l;
+      if (r < rows) w = max(w, rp[r + 1] - rp[r]);
+    }
+    width[sl] = w * kSlice;
+  }
+}
+
+// ... and the entries, column-major per slice; padding entries point at the
+// row itself with value 0.
+__global__ void SellFillKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                               const double* __restrict__ val, const int64_t* __restrict__ sptr,
+                               int32_t* __restrict__ scol, double* __restrict__ sval) {
+  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t sl = r / kSlice, lane = r % kSlice;
+    const int64_t b0 = sptr[sl] + lane;
+    const int w = static_cast<int>((sptr[sl + 1] - sptr[sl]) / kSlice);
+    const int64_t a = rp[r], len = rp[r + 1] - a;
+    for (int k = 0; k < w; ++k) {
+      const bool in = k < len;
+      scol[b0 + static_cast<int64_t>(k) * kSlice] = in ? col[a + k] : static_cast<int32_t>(r);
+      sval[b0 + static_cast<int64_t>(k) * kSlice] = in ? val[a + k] : 0.0;
+    }
   }
 }
 
@@ -343,60 +491,115 @@ void PrepareSolve(lfg_csr* A) {
     A->dinv.reset();
     Fail(LFG_INVALID_ARG, "Jacobi preconditioner: non-positive diagonal in row " + std::to_string(code - 1));
   }
+  // SELL-32 copy
+  A->nslices = (A->rows + kSlice - 1) / kSlice;
+  A->sell_ptr.alloc((A->nslices + 1) * sizeof(int64_t), s);
+  SellWidthKernel<<<GridFor(ctx, A->nslices, 256), 256, 0, s>>>(A->rows, A->nslices, A->rowptr.as<int64_t>(),
+                                                               A->sell_ptr.as<int64_t>());
+  LFG_LAUNCHED(ctx);
+  A->sell_nnz = ExclusiveScanI64(ctx, A->sell_ptr.as<int64_t>(), A->sell_ptr.as<int64_t>(), A->nslices);
+  LFG_CUDA(cudaMemcpyAsync(A->sell_ptr.as<int64_t>() + A->nslices, &A->sell_nnz, sizeof(int64_t),
+                           cudaMemcpyHostToDevice, s));
+  if (A->sell_nnz >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "solver needs padded nnz < 2^31");
+  A->sell_col.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(int32_t), s);
+  A->sell_val.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(double), s);
+  SellFillKernel<<<GridFor(ctx, A->rows, 256), 256, 0, s>>>(A->rows, A->rowptr.as<int64_t>(), A->col.as<int32_t>(),
+                                                            A->val.as<double>(), A->sell_ptr.as<int64_t>(),
+                                                            A->sell_col.as<int32_t>(), A->sell_val.as<double>());
+  LFG_LAUNCHED(ctx);
+  LFG_CUDA(cudaStreamSynchronize(s));  // the host copy of sell_nnz above is a stack value
 }
 
 void EnsureFloatValues(lfg_csr* A) {
-  if (A->val32.p) return;
   lfg_ctx* ctx = A->ctx;
-  A->val32.alloc(std::max<int64_t>(A->nnz, 1) * sizeof(float), ctx->stream);
-  ToFloatKernel<<<GridFor(ctx, A->nnz, 256), 256, 0, ctx->stream>>>(A->nnz, A->val.as<double>(), A->val32.as<float>());
-  LFG_LAUNCHED(ctx);
+  if (!A->val32.p) {
+    A->val32.alloc(std::max<int64_t>(A->nnz, 1) * sizeof(float), ctx->stream);
+    ToFloatKernel<<<GridFor(ctx, A->nnz, 256), 256, 0, ctx->stream>>>(A->nnz, A->val.as<double>(),
+                                                                       A->val32.as<float>());
+    LFG_LAUNCHED(ctx);
+  }
+  if (!A->sell_val32.p) {
+    A->sell_val32.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(float), ctx->stream);
+    ToFloatKernel<<<GridFor(ctx, A->sell_nnz, 256), 256, 0, ctx->stream>>>(A->sell_nnz, A->sell_val.as<double>(),
+                                                                            A->sell_val32.as<float>());
+    LFG_LAUNCHED(ctx);
+  }
 }
 
-// PCG on A x = b in precision T (x holds the initial guess; the FP64 path
-// starts from r = b - A x, the FP32 inner path from r = b with x = 0).
+// Work vectors of one PCG run in precision T.  r is filled by the caller;
+// res holds the block partials of the FP64 residual kernel.
 template <class T>
 struct PcgState {
-  DevBuf r, z, p, q;
-  DevBuf pq, rz[2], rr;
+  DevBuf r, z, p[2], q;
+  DevBuf part, res, scal;
   int nb = 0;
 };
 
 template <class T>
-int RunPcg(lfg_csr* A, const T* val, const T* dinv, T* x, T* r_init_owner, int64_t n, double target_rr,
-           int max_it, int check_every, PcgState<T>& S, double& rr_out) {
-  // r is S.r (already filled); returns iterations done
+void AllocState(lfg_ctx* ctx, int64_t n, PcgState<T>& S) {
+  cudaStream_t s = ctx->stream;
+  S.nb = std::max(1, std::min<int>(ctx->num_sms * 8, static_cast<int>((n + kPcgBlock - 1) / kPcgBlock)));
+  S.r.alloc(n * sizeof(T), s);
+  S.z.alloc(n * sizeof(T), s);
+  S.p[0].alloc(n * sizeof(T), s);
+  S.p[1].alloc(n * sizeof(T), s);
+  S.q.alloc(n * sizeof(T), s);
+  S.part.alloc(2 * static_cast<size_t>(ctx->num_sms) * 8 * sizeof(double), s);  // >= 2 * any grid used
+  S.res.alloc(S.nb * sizeof(double), s);
+  S.scal.alloc(sizeof(PcgScalars), s);
+  LFG_CUDA(cudaMemsetAsync(S.scal.p, 0, sizeof(PcgScalars), s));
+}
+
+double ReadRR(lfg_ctx* ctx, const DevBuf& scal) {
+  double rr = 0.0;
+  D2HSync(ctx, &rr, reinterpret_cast<const char*>(scal.p) + offsetof(PcgScalars, rr), sizeof(double));
+  return rr;
+}
+
+// PCG on A x = b in precision T from the residual already in S.r (x holds
+// the matching iterate).  Returns the iterations done; rr_out = <r, r> of the
+// recursively updated residual.
+template <class T>
+int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double target_rr, int max_it,
+           int check_every, PcgState<T>& S, double& rr_out) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   const int nb = S.nb;
-  const int32_t* rp = A->rowptr32.as<int32_t>();
-  const int32_t* col = A->col.as<int32_t>();
-  const int spmv_blocks = nb;
-  std::vector<double> tmp;
+  const int spmv_blocks = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (A->nslices + 7) / 8)));
+  constexpr int U = sizeof(T) == 8 ? 2 : 4;
+  const int update_blocks = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 4, (n + U * kPcgBlock - 1) / (U * kPcgBlock))));
+  PcgScalars* sc = S.scal.template as<PcgScalars>();
+  double* part = S.part.template as<double>();
   PcgStartKernel<T><<<nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
-                                             S.p.template as<T>(), S.rz[0].template as<double>(),
-                                             S.rr.template as<double>());
+                                             S.p[0].template as<T>(), part, sc);
   LFG_LAUNCHED(ctx);
-  double rr = HostSum(ctx, S.rr.template as<double>(), nb, tmp);
+  double rr = ReadRR(ctx, S.scal);
   int it = 0;
-  if (rr <= target_rr) {
+  if (!(rr > target_rr)) {
     rr_out = rr;
     return 0;
   }
-  // capture `check_every` iterations (an even count: the two <r,z> buffers alternate)
+  // `body` iterations per graph (even: the p buffers and rz slots alternate)
   const int body = std::max(2, check_every + (check_every & 1));
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  constexpr bool kFused = sizeof(T) == 4;
   for (int k = 0; k < body; ++k) {
-    double* rz_old = S.rz[k & 1].template as<double>();
-    double* rz_new = S.rz[(k + 1) & 1].template as<double>();
-    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(n, rp, col, val, S.p.template as<T>(), S.q.template as<T>(),
-                                                       S.pq.template as<double>());
-    PcgUpdateKernel<T><<<nb, kPcgBlock, 0, s>>>(n, S.pq.template as<double>(), rz_old, nb, dinv, S.p.template as<T>(),
-                                                S.q.template as<T>(), x, S.r.template as<T>(), S.z.template as<T>(),
-                                                rz_new, S.rr.template as<double>());
-    PcgDirectionKernel<T><<<nb, kPcgBlock, 0, s>>>(n, rz_new, rz_old, nb, S.z.template as<T>(), S.p.template as<T>());
+    const int cur = k & 1;
+    T* p_old = S.p[kFused ? cur : 0].template as<T>();
+    T* p_new = S.p[kFused ? (cur ^ 1) : 0].template as<T>();
+    if (!kFused) {
+      PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p_old, sc);
+    }
+    PcgSpmvDirKernel<T, kFused><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
+                                                                  A->sell_col.as<int32_t>(), sval,
+                                                                  S.z.template as<T>(), p_old, p_new,
+                                                                  S.q.template as<T>(), cur, part, sc);
+    PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p_new, S.q.template as<T>(), x, S.r.template as<T>(),
+                                                S.z.template as<T>(), cur, part, sc);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
   LFG_CUDA(ce);
@@ -404,9 +607,9 @@ int RunPcg(lfg_csr* A, const T* val, const T* dinv, T* x, T* r_init_owner, int64
   try {
     while (it < max_it) {
       LFG_CUDA(cudaGraphLaunch(exec, s));
-      CountLaunch(ctx, 3 * body);
+      CountLaunch(ctx, (kFused ? 2 : 3) * body);
       it += body;
-      rr = HostSum(ctx, S.rr.template as<double>(), nb, tmp);
+      rr = ReadRR(ctx, S.scal);
       if (!(rr > target_rr)) break;  // also stops on NaN
     }
   } catch (...) {
@@ -418,20 +621,6 @@ int RunPcg(lfg_csr* A, const T* val, const T* dinv, T* x, T* r_init_owner, int64
   cudaGraphDestroy(graph);
   rr_out = rr;
   return it;
-}
-
-template <class T>
-void AllocState(lfg_ctx* ctx, int64_t n, PcgState<T>& S) {
-  cudaStream_t s = ctx->stream;
-  S.nb = std::max(1, std::min<int>(ctx->num_sms * 8, static_cast<int>((n + kPcgBlock - 1) / kPcgBlock)));
-  S.r.alloc(n * sizeof(T), s);
-  S.z.alloc(n * sizeof(T), s);
-  S.p.alloc(n * sizeof(T), s);
-  S.q.alloc(n * sizeof(T), s);
-  S.pq.alloc(S.nb * sizeof(double), s);
-  S.rz[0].alloc(S.nb * sizeof(double), s);
-  S.rz[1].alloc(S.nb * sizeof(double), s);
-  S.rr.alloc(S.nb * sizeof(double), s);
 }
 
 }  // namespace
@@ -569,15 +758,15 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     zero.alloc(n * sizeof(double), s);
     LFG_CUDA(cudaMemsetAsync(zero.p, 0, n * sizeof(double), s));
     ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
-                                                 zero.as<double>(), b, S64.r.as<double>(), S64.rr.as<double>());
+                                                 zero.as<double>(), b, S64.r.as<double>(), S64.res.as<double>());
     LFG_LAUNCHED(ctx);
   }
-  const double bb = HostSum(ctx, S64.rr.as<double>(), nb, tmp);
+  const double bb = HostSum(ctx, S64.res.as<double>(), nb, tmp);
   const double bnorm = std::sqrt(bb);
   ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
-                                               x, b, S64.r.as<double>(), S64.rr.as<double>());
+                                               x, b, S64.r.as<double>(), S64.res.as<double>());
   LFG_LAUNCHED(ctx);
-  double rr = HostSum(ctx, S64.rr.as<double>(), nb, tmp);
+  double rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
   const double target = (rtol * bnorm) * (rtol * bnorm);
   if (bnorm == 0.0) {
     LFG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
@@ -592,13 +781,13 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     double rr_prev = rr;
     while (true) {
       double rr_end = rr;
-      total += RunPcg<double>(A, A->val.as<double>(), A->dinv.as<double>(), x, nullptr, n, target, max_it - total,
+      total += RunPcg<double>(A, A->sell_val.as<double>(), A->dinv.as<double>(), x, n, target, max_it - total,
                               check, S64, rr_end);
       ++restarts;
       ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
-                                                   A->val.as<double>(), x, b, S64.r.as<double>(), S64.rr.as<double>());
+                                                   A->val.as<double>(), x, b, S64.r.as<double>(), S64.res.as<double>());
       LFG_LAUNCHED(ctx);
-      rr = HostSum(ctx, S64.rr.as<double>(), nb, tmp);
+      rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
       if (rr <= target || total >= max_it || restarts >= 16 || !(rr < 0.25 * rr_prev)) break;
       rr_prev = rr;
     }
@@ -625,15 +814,15 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       // inner target relative to ||r/||r|| || = 1, but never below what the outer loop needs
       const double need = std::max(inner, 0.5 * std::sqrt(target) / rnorm);
       double rr_in = 0.0;
-      const int it = RunPcg<float>(A, A->val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), nullptr, n,
+      const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
                                    need * need, max_it - total, check, S32, rr_in);
       total += std::max(it, 1);
       AddCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), rnorm, x);
       LFG_LAUNCHED(ctx);
       ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
-                                                   A->val.as<double>(), x, b, S64.r.as<double>(), S64.rr.as<double>());
+                                                   A->val.as<double>(), x, b, S64.r.as<double>(), S64.res.as<double>());
       LFG_LAUNCHED(ctx);
-      const double rr_new = HostSum(ctx, S64.rr.as<double>(), nb, tmp);
+      const double rr_new = HostSum(ctx, S64.res.as<double>(), nb, tmp);
       ++outer;
       if (!(rr_new < rr)) {  // stagnation: no progress in FP32
         rr = rr_new;

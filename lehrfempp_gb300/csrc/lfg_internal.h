@@ -177,6 +177,14 @@ struct lfg_csr {
   lfg::DevBuf rowptr32;  // int32[rows + 1] when nnz < 2^31 (SpMV)
   lfg::DevBuf dinv;    // double[rows] Jacobi
   lfg::DevBuf dinv32;  // float[rows]
+  // SELL-32 copy for the PCG SpMV (built with the preconditioner): slice s
+  // holds rows 32s..32s+31 column-major, width = longest row of the slice;
+  // entry (s, k, lane) at sell_ptr[s] + 32 k + lane; padding has col = row, 0.
+  int64_t nslices = 0, sell_nnz = 0;
+  lfg::DevBuf sell_ptr;    // int64[nslices + 1]
+  lfg::DevBuf sell_col;    // int32[sell_nnz]
+  lfg::DevBuf sell_val;    // double[sell_nnz]
+  lfg::DevBuf sell_val32;  // float[sell_nnz] (mixed precision, built lazily)
 };
 
 namespace lfg {
