@@ -419,7 +419,7 @@ def run_ours(args):
             fam[f] = (t / n, n)
     ctx.profile(False)
     dom = max(fam, key=lambda k: fam[k][0])
-    kind = "quad" if dom.endswith("quad") else "tria"
+    kind = "quad" if "quad" in dom else "tria"
     alg_bytes, per_cell = algorithmic_bytes(space, mesh, kind)
     hbm_peak = 6777.6
     peaks_src = "MEASURED_PEAKS.json hbm_gbs (burst), of measured"

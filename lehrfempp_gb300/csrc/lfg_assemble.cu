@@ -287,15 +287,28 @@ __device__ __forceinline__ int UpperIndex(int i, int j) {
   return a * N - (a * (a - 1)) / 2 + (b - a);
 }
 
-// Writes the staged tile: triplet w of cell cl goes to out + off[cl] + w.
+// (i, j, upper index) of triplet w = i N + j of an element block, packed as
+// i | j << 8 | u << 16; filled once per CTA (no per-triplet index arithmetic).
+template <int N>
+__device__ __forceinline__ void FillTripletMap(int* smap) {
+  for (int w = threadIdx.x; w < N * N; w += blockDim.x) {
+    const int i = w / N, j = w - i * N;
+    smap[w] = i | (j << 8) | (UpperIndex<N>(i, j) << 16);
+  }
+}
+
+// Writes the staged tile: triplet w of cell cl goes to out + off[cl] + w;
+// consecutive threads take consecutive triplets of the tile (blocks of
+// consecutive cells are mostly adjacent), so stores are 16-byte coalesced.
 template <int N>
 __device__ __forceinline__ void WriteTile(lfg_triplet* out, int ncell, const double* svals,
-                                          const int* sdofs, const int64_t* soff) {
+                                          const int* sdofs, const int64_t* soff, const int* smap) {
   constexpr int NN = N * N, E = N * (N + 1) / 2;
   for (int q = threadIdx.x; q < ncell * NN; q += blockDim.x) {
     const int cl = q / NN, w = q - cl * NN;
-    const int i = w / N, j = w - i * N;
-    StoreTriplet(out + soff[cl] + w, sdofs[cl * N + i], sdofs[cl * N + j], svals[cl * E + UpperIndex<N>(i, j)]);
+    const int m = smap[w];
+    const int* dofs = sdofs + cl * N;
+    StoreTriplet(out + soff[cl] + w, dofs[m & 0xff], dofs[(m >> 8) & 0xff], svals[cl * E + (m >> 16)]);
   }
 }
 
@@ -315,8 +328,10 @@ __global__ void __launch_bounds__(128) RDTriaDfKernel(AsmArgs a, DfArgs d) {
   double* svals = reinterpret_cast<double*>(smraw + ((E * 4 * sizeof(f2) + 15) & ~15));
   int64_t* soff = reinterpret_cast<int64_t*>(svals + TILE * E);
   int* sdofs = reinterpret_cast<int*>(soff + TILE);
+  __shared__ int smap[N * N];
   const f2* gR = reinterpret_cast<const f2*>(d.tab) + d.L.off_R;
   for (int i = threadIdx.x; i < E * 4; i += blockDim.x) sR[i] = gR[i];
+  FillTripletMap<N>(smap);
   __syncthreads();
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
        t0 += static_cast<int64_t>(gridDim.x) * TILE) {
@@ -342,7 +357,7 @@ __global__ void __launch_bounds__(128) RDTriaDfKernel(AsmArgs a, DfArgs d) {
       soff[threadIdx.x] = a.tri_offset[c];
     }
     __syncthreads();
-    WriteTile<N>(a.out, ncell, svals, sdofs, soff);
+    WriteTile<N>(a.out, ncell, svals, sdofs, soff, smap);
     __syncthreads();
   }
 }
@@ -371,24 +386,75 @@ __device__ void QuadUniformF64(const double2 (&v)[4], double al, double ga, cons
   }
 }
 
-template <int DEG, int M, bool MASS>
+// Per-point term tables of the direct quad contraction live in shared
+// memory: [NQ][E][4], then W[NQ], t[M].
+template <int DEG, int M>
+constexpr int QuadTabPairs() {
+  return M * M * ((DEG + 1) * (DEG + 1) * ((DEG + 1) * (DEG + 1) + 1) / 2) * 4;
+}
+
+// The sum-factorised path's tables ([3][N1][N1][M] 1D products, W[M*M],
+// t[M]) live in constant memory, one slot per (degree 2-3, points 2-4): with
+// the slot offset and the loop indices known at compile time, the stage-2
+// operands are read by the arithmetic instructions straight from the
+// constant bank (no load instruction, no index arithmetic).
+template <int DEG, int M>
+constexpr int SfSlotPairs() {
+  return 3 * (DEG + 1) * (DEG + 1) * M + M * M + M;
+}
+constexpr int SfSlotIndex(int deg, int m) { return (deg - 2) * 3 + (m - 2); }
+template <int DEG, int M>
+constexpr int SfSlotOffset() {
+  int off = 0;
+  for (int d = 2; d <= 3; ++d)
+    for (int m = 2; m <= 4; ++m) {
+      if (d == DEG && m == M) return off;
+      off += 3 * (d + 1) * (d + 1) * m + m * m + m;
+    }
+  return off;
+}
+constexpr int kSfConstPairs = SfSlotOffset<4, 2>();  // past the last slot
+__constant__ float2 c_sf_tables[kSfConstPairs];
+
+template <int DEG, int M, bool MASS, bool SF>
 __global__ void __launch_bounds__(128) RDQuadDfKernel(AsmArgs a, DfArgs d) {
   using elem::f2;
   constexpr int N = (DEG + 1) * (DEG + 1);
   constexpr int E = N * (N + 1) / 2;
   constexpr int NQ = M * M;
   constexpr int TILE = E > 64 ? 64 : 128;
+  constexpr int TP = SF ? 0 : QuadTabPairs<DEG, M>();
+  constexpr int SMT = SF ? 0 : TP + NQ + M;  // table pairs in shared memory
   extern __shared__ __align__(16) unsigned char smraw[];
-  f2* sT = reinterpret_cast<f2*>(smraw);  // [NQ][E][4], then W[NQ], t[M]
-  f2* sW = sT + NQ * E * 4;
-  f2* st = sW + NQ;
-  double* svals = reinterpret_cast<double*>(smraw + (((NQ * E * 4 + NQ + M) * sizeof(f2) + 15) & ~15));
+  f2* sT = reinterpret_cast<f2*>(smraw);
+  const f2* tW;
+  const f2* tt;
+  const f2* tsf = nullptr;
+  if (SF) {
+    const f2* slot = reinterpret_cast<const f2*>(c_sf_tables) + SfSlotOffset<(SF ? DEG : 2), M>();
+    tsf = slot;
+    tW = slot + 3 * (DEG + 1) * (DEG + 1) * M;
+    tt = tW + NQ;
+  } else {
+    tW = sT + TP;
+    tt = tW + NQ;
+  }
+  double* svals = reinterpret_cast<double*>(smraw + ((SMT * sizeof(f2) + 15) & ~15));
   int64_t* soff = reinterpret_cast<int64_t*>(svals + TILE * E);
   int* sdofs = reinterpret_cast<int*>(soff + TILE);
+  __shared__ int sloc[16];
+  __shared__ int smap[N * N];
+  FillTripletMap<N>(smap);
   const f2* g = reinterpret_cast<const f2*>(d.tab);
-  for (int i = threadIdx.x; i < NQ * E * 4; i += blockDim.x) sT[i] = g[d.L.off_T + i];
-  for (int i = threadIdx.x; i < NQ; i += blockDim.x) sW[i] = g[d.L.off_W + i];
-  for (int i = threadIdx.x; i < M; i += blockDim.x) st[i] = g[d.L.off_t + i];
+  if (!SF) {
+    for (int i = threadIdx.x; i < TP; i += blockDim.x) sT[i] = g[d.L.off_T + i];
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) sT[TP + i] = g[d.L.off_W + i];
+    for (int i = threadIdx.x; i < M; i += blockDim.x) sT[TP + NQ + i] = g[d.L.off_t + i];
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) sloc[i] = d.L.loc[i];  // static indices: no local copy of the parameter
+  }
   __syncthreads();
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
        t0 += static_cast<int64_t>(gridDim.x) * TILE) {
@@ -409,8 +475,9 @@ __global__ void __launch_bounds__(128) RDQuadDfKernel(AsmArgs a, DfArgs d) {
       for (int k = 0; k < 6; ++k) safe = safe && elem::DfSafe(acd[k]);
       if (safe) {
         f2 cpt[NQ][4];
-        elem::QuadPointCoeffsDF<M, MASS>(acd, al, ga, st, sW, cpt);
-        elem::QuadContractDF<E, NQ, MASS>(cpt, sT, vals);
+        elem::QuadPointCoeffsDF<M, MASS>(acd, al, ga, tt, tW, cpt);
+        if (SF) elem::QuadSumFactDF<DEG + 1, M, MASS>(cpt, tsf, sloc, vals);
+        else elem::QuadContractDF<E, NQ, MASS>(cpt, sT, vals);
       } else {
         QuadUniformF64<N, MASS>(v, al, ga, a.tab, a.L, vals);
         atomicAdd(a.fallback, 1ull);
@@ -420,7 +487,7 @@ __global__ void __launch_bounds__(128) RDQuadDfKernel(AsmArgs a, DfArgs d) {
       soff[threadIdx.x] = a.tri_offset[c];
     }
     __syncthreads();
-    WriteTile<N>(a.out, ncell, svals, sdofs, soff);
+    WriteTile<N>(a.out, ncell, svals, sdofs, soff, smap);
     __syncthreads();
   }
 }
@@ -744,8 +811,29 @@ void Launch(K kernel, lfg_ctx* ctx, int64_t count, size_t smem, int block, const
 template <int DEG, int M, bool MASS>
 void LaunchQuadDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   constexpr int N = (DEG + 1) * (DEG + 1), E = N * (N + 1) / 2, NQ = M * M, TILE = E > 64 ? 64 : 128;
-  const size_t smem = (((NQ * E * 4 + NQ + M) * 8 + 15) & ~size_t(15)) + TILE * (E * 8 + 8 + N * 4);
-  Launch(RDQuadDfKernel<DEG, M, MASS>, ctx, a.count, smem, 128, a, d);
+  if (DEG >= 2 && d.L.n1 == DEG + 1 && d.L.m == M) {
+    constexpr int SD = DEG >= 2 ? DEG : 2;  // (the branch is dead for DEG 1)
+    const uint32_t bit = 1u << SfSlotIndex(SD, M);
+    if (!(ctx->sf_const_ready & bit)) {
+      // slot <- [1D products | W | t] from the df32 table block on the device
+      constexpr int sfp = 3 * (SD + 1) * (SD + 1) * M;
+      const size_t off = SfSlotOffset<SD, M>() * sizeof(float2);
+      const float2* src = reinterpret_cast<const float2*>(d.tab);
+      LFG_CUDA(cudaMemcpyToSymbolAsync(c_sf_tables, src + d.L.off_SF, sfp * sizeof(float2), off,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+      LFG_CUDA(cudaMemcpyToSymbolAsync(c_sf_tables, src + d.L.off_W, NQ * sizeof(float2), off + sfp * sizeof(float2),
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+      LFG_CUDA(cudaMemcpyToSymbolAsync(c_sf_tables, src + d.L.off_t, M * sizeof(float2),
+                                       off + (sfp + NQ) * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+      ctx->sf_const_ready |= bit;
+    }
+    const size_t smem = TILE * (E * 8 + 8 + N * 4);
+    Launch(RDQuadDfKernel<SD, M, MASS, true>, ctx, a.count, smem, 128, a, d);
+    return;
+  }
+  constexpr int TP = QuadTabPairs<DEG, M>();
+  const size_t smem = (((TP + NQ + M) * 8 + 15) & ~size_t(15)) + TILE * (E * 8 + 8 + N * 4);
+  Launch(RDQuadDfKernel<DEG, M, MASS, false>, ctx, a.count, smem, 128, a, d);
 }
 
 template <int DEG, bool QUAD>

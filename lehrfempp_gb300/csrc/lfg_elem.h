@@ -135,6 +135,73 @@ DF_HD void QuadPointCoeffsDF(const double (&acd)[6] /* ax, ay, cx, cy, dx, dy */
   }
 }
 
+// Upper-triangle index of the unordered pair {i, j} in "for i: for j >= i" order.
+template <int N>
+DF_HD int UpperIdx(int i, int j) {
+  const int a = i < j ? i : j, b = i < j ? j : i;
+  return a * N - (a * (a - 1)) / 2 + (b - a);
+}
+
+// Sum-factorised contraction for tensor-product bases (Q2, Q3 on the tensor
+// Gauss rule).  With phi_{(a,b)}(x,y) = l_a(x) l_b(y), points k = p M + q at
+// (x_p, y_q) and c[k] = {c00, c01, c11, m}:
+//   H0(a,a',q) = sum_p c00 l'_a l'_a'(x_p),  H2 = sum_p c11 l_a l_a',
+//   H1(a,a',q) = sum_p c01 l'_a l_a',        H3 = sum_p m l_a l_a',
+//   A((a,b),(a',b')) = sum_q H0(a,a') l_b l_b' + H1(a,a') l_b l'_b'
+//                           + H1(a',a) l'_b l_b' + H2(a,a') l'_b l'_b' [+ H3 l_b l_b'](y_q).
+// Unordered x pairs a <= a' run as a runtime loop (H stays in registers);
+// each pair owns the 9 (a < a') or 6 (a = a') unordered entries of its
+// y pairs.  Q2: 729 products per cell instead of 1215.  sf = [3][N1][N1][M]
+// ({l'l', ll, l'l}), loc[a N1 + b] = local dof of (a, b).
+template <int N1, int M, bool MASS>
+DF_HD void QuadSumFactDF(const f2 (*c)[4], const f2* sf, const int* loc, double* out) {
+  using namespace df;
+  constexpr int N = N1 * N1;
+  const f2* DD = sf;
+  const f2* VV = sf + N1 * N1 * M;
+  const f2* DV = sf + 2 * N1 * N1 * M;
+  DF_NOUNROLL
+  for (int pr = 0; pr < N1 * N1; ++pr) {
+    const int a = pr / N1, a2 = pr - a * N1;
+    if (a2 < a) continue;
+    f2 h0[M], h1[M], h1t[M], h2[M], h3[M];
+    DF_UNROLL
+    for (int q = 0; q < M; ++q) {
+      Acc s0, s1, s1t, s2, s3;
+      DF_UNROLL
+      for (int p = 0; p < M; ++p) {
+        const int k = p * M + q;
+        s0.AddProd(c[k][0], DD[pr * M + p]);
+        s1.AddProd(c[k][1], DV[pr * M + p]);
+        s1t.AddProd(c[k][1], DV[(a2 * N1 + a) * M + p]);
+        s2.AddProd(c[k][2], VV[pr * M + p]);
+        if (MASS) s3.AddProd(c[k][3], VV[pr * M + p]);
+      }
+      h0[q] = s0.Value();
+      h1[q] = s1.Value();
+      h1t[q] = s1t.Value();
+      h2[q] = s2.Value();
+      h3[q] = MASS ? s3.Value() : f2{0.0f, 0.0f};
+    }
+    DF_UNROLL
+    for (int yb = 0; yb < N1 * N1; ++yb) {
+      const int b = yb / N1, b2 = yb % N1, yt = b2 * N1 + b;
+      if (a != a2 || b2 >= b) {
+        Acc acc;
+        DF_UNROLL
+        for (int q = 0; q < M; ++q) {
+          acc.AddProd(h0[q], VV[yb * M + q]);
+          acc.AddProd(h1[q], DV[yt * M + q]);
+          acc.AddProd(h1t[q], DV[yb * M + q]);
+          acc.AddProd(h2[q], DD[yb * M + q]);
+          if (MASS) acc.AddProd(h3[q], VV[yb * M + q]);
+        }
+        out[UpperIdx<N>(loc[a * N1 + b], loc[a2 * N1 + b2])] = ToDouble(acc.Value());
+      }
+    }
+  }
+}
+
 // Number of upper-triangle entries contracted together (a divisor of E): the
 // G accumulators give instruction-level parallelism while the loop over the
 // E/G groups stays a runtime loop, so the code fits the instruction cache.

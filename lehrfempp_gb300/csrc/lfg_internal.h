@@ -85,6 +85,7 @@ struct lfg_ctx {
   // reference-element tables keyed by (cell type, degree, rule degree)
   std::map<int, lfg::TableEntry> tables;
   std::map<int, lfg::DfTableEntry> dftables;
+  uint32_t sf_const_ready = 0;  // constant-memory slots of the sum-factorised quad tables filled on this context
   // per-kernel-family event timing (lfg_profile_*)
   bool profiling = false;
   struct ProfRec {

@@ -176,6 +176,68 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
     dphi[9][d] = 27.0 * (dl[0][d] * l[1] * l[2] + l[0] * dl[1][d] * l[2] + l[0] * l[1] * dl[2][d]);
 }
 
+// If the quadrilateral Lagrangian basis of `degree` is the tensor product of
+// the 1D Lagrange basis on the equispaced nodes {0, 1/p, ..., 1}, i.e.
+// phi_{loc[a n1 + b]}(x, y) = l_a(x) l_b(y) with gradients to match at every
+// point of the rule, fill loc and the 1D product tables
+// sf[kind][a][b][p] (kind 0: l'_a l'_b, 1: l_a l_b, 2: l'_a l_b at the m
+// abscissae of the tensor Gauss rule) and return true.
+static bool TensorBasis(int degree, const Rule& r, int m, int* loc, std::vector<long double>& sf) {
+  const int n1 = degree + 1, n = n1 * n1;
+  if (n > 16 || m * m != r.n) return false;
+  std::vector<long double> node(n1);
+  for (int a = 0; a < n1; ++a) node[a] = static_cast<long double>(a) / degree;
+  auto l1 = [&](int a, long double x, long double* d) {
+    long double v = 1.0L, dv = 0.0L;
+    for (int k = 0; k < n1; ++k) {
+      if (k == a) continue;
+      const long double f = (x - node[k]) / (node[a] - node[k]);
+      dv = dv * f + v / (node[a] - node[k]);
+      v *= f;
+    }
+    *d = dv;
+    return v;
+  };
+  double phi[16], dphi[16][2];
+  for (int a = 0; a < n1; ++a)
+    for (int b = 0; b < n1; ++b) {
+      Shape(true, degree, static_cast<double>(node[a]), static_cast<double>(node[b]), phi, dphi);
+      int hit = -1;
+      for (int i = 0; i < n; ++i) {
+        if (std::fabs(phi[i] - 1.0) < 1e-12) hit = i;
+        else if (std::fabs(phi[i]) > 1e-12) return false;
+      }
+      if (hit < 0) return false;
+      loc[a * n1 + b] = hit;
+    }
+  for (int k = 0; k < r.n; ++k) {
+    Shape(true, degree, r.x[k], r.y[k], phi, dphi);
+    for (int a = 0; a < n1; ++a)
+      for (int b = 0; b < n1; ++b) {
+        long double da, db;
+        const long double la = l1(a, r.x[k], &da), lb = l1(b, r.y[k], &db);
+        const int i = loc[a * n1 + b];
+        if (std::fabs(static_cast<double>(la * lb) - phi[i]) > 1e-12 ||
+            std::fabs(static_cast<double>(da * lb) - dphi[i][0]) > 1e-11 ||
+            std::fabs(static_cast<double>(la * db) - dphi[i][1]) > 1e-11)
+          return false;
+      }
+  }
+  // abscissae: x of points (p, 0) (x slow, y fast)
+  sf.assign(3 * n1 * n1 * m, 0.0L);
+  for (int a = 0; a < n1; ++a)
+    for (int b = 0; b < n1; ++b)
+      for (int p = 0; p < m; ++p) {
+        long double da, db;
+        const long double x = r.x[p * m];
+        const long double la = l1(a, x, &da), lb = l1(b, x, &db);
+        sf[((0 * n1 + a) * n1 + b) * m + p] = da * db;
+        sf[((1 * n1 + a) * n1 + b) * m + p] = la * lb;
+        sf[((2 * n1 + a) * n1 + b) * m + p] = da * lb;
+      }
+  return true;
+}
+
 bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& out, DfLayout& L) {
   Rule r;
   if (!MakeRule(quad, rule_degree, r)) return false;
@@ -189,8 +251,15 @@ bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& o
   L.off_T = L.off_L + L.n;
   L.off_W = L.off_T + (quad ? L.nq * L.E * 4 : 0);
   L.off_t = L.off_W + L.nq;
-  L.total = L.off_t + L.m;
+  L.off_SF = L.off_t + L.m;
+  L.total = L.off_SF;
+  std::vector<long double> sf;
+  if (quad && degree >= 2 && TensorBasis(degree, r, L.m, L.loc, sf)) {
+    L.n1 = degree + 1;
+    L.total += static_cast<int>(sf.size());
+  }
   out.assign(2 * static_cast<size_t>(L.total), 0.0f);
+  for (size_t q = 0; q < (L.n1 ? sf.size() : 0); ++q) Split(sf[q], &out[2 * (L.off_SF + q)]);
   std::vector<long double> R(L.E * 4, 0.0L), Ls(L.n, 0.0L);
   double phi[16], dphi[16][2];
   for (int k = 0; k < r.n; ++k) {

@@ -23,9 +23,15 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
 //   L[n]       folded load sums sum_k w_k phi_i
 //   T[nq][E][4] the same terms per point (no weight)      (quads)
 //   W[nq]      point weights,  t[m] 1D abscissae            (quads)
+//   SF[3][n1][n1][m]  1D products {l'_a l'_b, l_a l_b, l'_a l_b} at the m
+//              Gauss abscissae, for quads whose basis is the tensor product
+//              phi_{loc[a n1 + b]}(x, y) = l_a(x) l_b(y) of a 1D basis of
+//              degree n1 - 1 (n1 = 0: not a tensor basis, no SF block)
 struct DfLayout {
   int n = 0, E = 0, nq = 0, m = 0;
   int off_R = 0, off_L = 0, off_T = 0, off_W = 0, off_t = 0, total = 0;
+  int n1 = 0, off_SF = 0;
+  int loc[16] = {};
 };
 bool BuildDfTables(bool is_quad, int degree, int rule_degree, std::vector<float>& out, DfLayout& L);
 

@@ -2,7 +2,9 @@
 // (lehrfempp_gb300/csrc/lfg_elem.h, lfg_df32.h): element matrices of random
 // triangles and bilinear quadrilaterals are compared with a long-double
 // evaluation of the reference's quadrature sum (loc_comp_ellbvp.h:324-337).
-// Prints one line per case: "<type> <degree> <rule> <cells> <max |err|/max|A_K|>".
+// Quadrilaterals of degree 2 and 3 also run through the sum-factorised
+// contraction ("quadsf"), which the kernels use for tensor-product bases.
+// Prints one line per case: "<type> <degree> <rule> <cells> <h> <mass> <max |err|/max|A_K|>".
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -50,11 +52,13 @@ void Reference(bool quad, int degree, const lfg::Rule& r, const double (*v)[2], 
 }
 
 template <int N>
-double RunCase(bool quad, int degree, int rule, int cells, double h, bool mass, std::mt19937_64& rng) {
+double RunCase(bool quad, int degree, int rule, int cells, double h, bool mass, std::mt19937_64& rng,
+               bool sf = false) {
   constexpr int E = N * (N + 1) / 2;
   std::vector<float> tab;
   lfg::DfLayout L;
   if (!lfg::BuildDfTables(quad, degree, rule, tab, L)) return -1;
+  if (sf && L.n1 != degree + 1) return -1;  // no tensor-product tables
   const f2* T = reinterpret_cast<const f2*>(tab.data());
   lfg::Rule r;
   lfg::MakeRule(quad, rule, r);
@@ -92,9 +96,12 @@ double RunCase(bool quad, int degree, int rule, int cells, double h, bool mass, 
         if (m == 2) lfg::elem::QuadPointCoeffsDF<2, MS>(acd, alpha, gamma, T + L.off_t, T + L.off_W, cpt);
         if (m == 3) lfg::elem::QuadPointCoeffsDF<3, MS>(acd, alpha, gamma, T + L.off_t, T + L.off_W, cpt);
         if (m == 4) lfg::elem::QuadPointCoeffsDF<4, MS>(acd, alpha, gamma, T + L.off_t, T + L.off_W, cpt);
-        if (m == 2) lfg::elem::QuadContractDF<E, 4, MS>(cpt, T + L.off_T, got);
-        if (m == 3) lfg::elem::QuadContractDF<E, 9, MS>(cpt, T + L.off_T, got);
-        if (m == 4) lfg::elem::QuadContractDF<E, 16, MS>(cpt, T + L.off_T, got);
+        constexpr int N1 = N == 9 ? 3 : (N == 16 ? 4 : 2);
+        if (sf && m == 3) lfg::elem::QuadSumFactDF<N1, 3, MS>(cpt, T + L.off_SF, L.loc, got);
+        else if (sf && m == 4) lfg::elem::QuadSumFactDF<N1, 4, MS>(cpt, T + L.off_SF, L.loc, got);
+        else if (m == 2) lfg::elem::QuadContractDF<E, 4, MS>(cpt, T + L.off_T, got);
+        else if (m == 3) lfg::elem::QuadContractDF<E, 9, MS>(cpt, T + L.off_T, got);
+        else if (m == 4) lfg::elem::QuadContractDF<E, 16, MS>(cpt, T + L.off_T, got);
       };
       if (mass) contract(std::true_type{});
       else contract(std::false_type{});
@@ -125,6 +132,8 @@ int main(int argc, char** argv) {
       std::printf("quad 1 2 %d %.3g %d %.3e\n", cells, h, mass, RunCase<4>(true, 1, 2, cells, h, mass, rng));
       std::printf("quad 2 4 %d %.3g %d %.3e\n", cells, h, mass, RunCase<9>(true, 2, 4, cells, h, mass, rng));
       std::printf("quad 3 6 %d %.3g %d %.3e\n", cells, h, mass, RunCase<16>(true, 3, 6, cells, h, mass, rng));
+      std::printf("quadsf 2 4 %d %.3g %d %.3e\n", cells, h, mass, RunCase<9>(true, 2, 4, cells, h, mass, rng, true));
+      std::printf("quadsf 3 6 %d %.3g %d %.3e\n", cells, h, mass, RunCase<16>(true, 3, 6, cells, h, mass, rng, true));
     }
   return 0;
 }
