@@ -3,8 +3,8 @@
  *
  * This is the drop-in boundary.  LehrFEM++ has no FFI of its own: its API for
  * this path is a set of C++20 templates and concepts.  Each entry point below
- * replaces one of them and is bound by the header-only C++ facade in
- * include/lf/ (same class and function names as the reference) or, from
+ * replaces one of them and is bound by the header-only C++ facade
+ * include/lf_gb300.hpp (the reference's class and function names) or, from
  * Python, by lehrfempp_gb300/_capi.py (ctypes).  Citations are file:line in the
  * LehrFEM++ source tree.
  *
@@ -84,7 +84,9 @@ lfg_status lfg_l2_flush(lfg_ctx* ctx);
 /* Per-kernel timing (no reference counterpart; replaces lf::base::Timer,
  * base/timer.h:64-278, for device work): while enabled, every element-kernel
  * launch is bracketed by CUDA events on the context stream and accumulated
- * under its kernel family name ("rd_tria_uniform", "rd_general_quad", ...). */
+ * under its kernel family name ("rd_tria_df", "rd_quad_df", "rd_general_tria",
+ * "rd_general_quad", "load_tria", "load_quad", "grad_rd", "misfit",
+ * "batch_assemble"); "fp64_fallback_cells" counts cells that left the df32 range. */
 lfg_status lfg_profile_enable(lfg_ctx* ctx, int enable);
 lfg_status lfg_profile_read(lfg_ctx* ctx, const char* family, double* total_ms, int64_t* launches);
 lfg_status lfg_profile_reset(lfg_ctx* ctx);
@@ -272,22 +274,24 @@ lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
  * matrix.  The reference solves with Eigen::SparseLU in its drivers
  * (examples/ellbvp_linfe/homDir_linfe_demo.cc:168-174); on the GPU the solve is
  * a Jacobi-preconditioned CG:
- *   LFG_SOLVE_FP64   FP64 PCG to ||b - A x|| <= rtol ||b||
- *   LFG_SOLVE_MIXED  FP32 PCG inner iterations (FP32 matrix copy and vectors)
- *                    inside FP64 iterative refinement: r = b - A x in FP64,
- *                    x += d in FP64, to the same FP64 residual criterion.
+ *   LFG_SOLVE_FP64   FP64 PCG to ||b - A x|| <= rtol ||b|| (restarted from the
+ *                    true residual when the recursive one drifts)
+ *   LFG_SOLVE_MIXED  FP32 PCG inner solves (FP32 matrix copy and vectors) of
+ *                    A d = r / ||r|| to inner_rtol, inside FP64 iterative
+ *                    refinement: r = b - A x in FP64, x += ||r|| d in FP64,
+ *                    to the same FP64 residual criterion.
  * x_dev holds the initial guess on entry. */
 enum { LFG_SOLVE_FP64 = 0, LFG_SOLVE_MIXED = 1 };
 typedef struct {
   int32_t precision;
   int32_t max_iterations;        /* total inner PCG iterations allowed           */
   double rtol;                   /* relative residual target (FP64)              */
-  double inner_rtol;             /* mixed: relative reduction per inner solve    */
+  double inner_rtol;             /* mixed: relative reduction per inner solve (0: 1e-4) */
   int32_t check_every;           /* convergence checks every N iterations        */
 } lfg_solve_opts;
 typedef struct {
   int32_t iterations;            /* PCG iterations (all inner iterations)        */
-  int32_t refinements;           /* outer FP64 refinement steps (mixed)          */
+  int32_t refinements;           /* FP64 refinement steps (mixed) / restarts (FP64) */
   double rel_residual;           /* final ||b - A x|| / ||b|| in FP64            */
   int32_t converged;
 } lfg_solve_stats;

@@ -453,7 +453,7 @@ class CSRMatrix:
     def spmv(self, x, y):
         self.ctx.check(lib().lfg_csr_spmv(self.h, x.ptr, y.ptr))
 
-    def solve_pcg(self, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=1e-4,
+    def solve_pcg(self, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=0.0,
                   check_every=32, raise_on_failure=True, noalloc=False):
         """Jacobi-PCG; noalloc=True uses lfg_solve_pcg_noalloc (FP64, <= 2^20 rows,
         work vectors in the library's fixed device array, no allocation)."""
@@ -512,7 +512,7 @@ class Batch:
         self.ctx.check(lib().lfg_batch_boundary_dof_flags(self.h, f.ptr))
         return f
 
-    def solve_pcg(self, csr, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=1e-4,
+    def solve_pcg(self, csr, b, x, precision=SOLVE_FP64, rtol=1e-10, max_iterations=200000, inner_rtol=0.0,
                   check_every=32, raise_on_failure=True):
         o = lfg_solve_opts()
         o.precision, o.rtol, o.max_iterations, o.inner_rtol, o.check_every = (precision, rtol, max_iterations,
@@ -577,7 +577,7 @@ class RDAdjoint:
     object (lfg_rd_adjoint_*): alpha = exp(theta) per cell, gamma = 0."""
 
     def __init__(self, space, u_obs, load, qr_degree_tria=0, qr_degree_quad=0, flags=None, dirichlet=None,
-                 precision=SOLVE_FP64, rtol=1e-12, max_iterations=200000, inner_rtol=1e-4, check_every=32,
+                 precision=SOLVE_FP64, rtol=1e-12, max_iterations=200000, inner_rtol=0.0, check_every=32,
                  recompute=False):
         self.ctx = space.ctx
         self.space = space  # must outlive the object

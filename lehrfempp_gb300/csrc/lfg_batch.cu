@@ -193,19 +193,203 @@ __device__ double BlockReduce(double v, double* red) {
   return s;
 }
 
-// sum of a mesh's chunk partials, in chunk order (thread 0), broadcast
-__device__ double MeshSum(const double* part, const Chunks& C, int b, double* sh) {
+// Per-mesh PCG scalars on the device (rz[cur] = <r, z> of the current
+// residual; the update kernel writes rz[cur ^ 1]).
+struct MeshScal {
+  double rz[2];
+  double alpha, beta, rr, pq;
+  unsigned int cnt;  // chunks of this mesh finished in the current kernel
+  unsigned int pad;
+};
+
+// Called by every block after it wrote the partial(s) of chunk c of mesh b:
+// true for the block that finished the mesh's last chunk (counter after a
+// fence; no block waits for another).  That block then reduces the mesh's
+// chunk partials in chunk order.
+__device__ __forceinline__ bool MeshDone(MeshScal* ms, int b, unsigned int nch) {
+  __shared__ bool last;
   if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int64_t c = C.mesh_chunk[b]; c < C.mesh_chunk[b + 1]; ++c) s += part[c];
-    *sh = s;
+    __threadfence();
+    last = atomicAdd(&ms[b].cnt, 1u) == nch - 1;
   }
   __syncthreads();
-  const double s = *sh;
-  __syncthreads();
-  return s;
+  return last;
 }
 
+__device__ double MeshPartSum(const double* part, int stride, int off, int64_t c0, int64_t c1, double* red) {
+  double v = 0.0;
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) v += __ldcg(part + c * stride + off);
+  v = BlockReduce(v, red);
+  return v;  // valid in thread 0
+}
+
+template <class T>
+struct BDot {
+  double v = 0.0;
+  __device__ void add(T a, T b) { v = fma(a, b, v); }
+  __device__ double get() const { return v; }
+};
+template <>
+struct BDot<float> {
+  float v = 0.0f;
+  __device__ void add(float a, float b) { v = fmaf(a, b, v); }
+  __device__ double get() const { return static_cast<double>(v); }
+};
+
+struct Sell {
+  const int64_t* ptr;
+  const int32_t* col;
+};
+
+// q = A p on the chunk's rows (SELL-32; thread per row), <p, q> per mesh
+// -> alpha_b.  FUSED (FP32): p_new = z + beta_b p_old formed on the fly
+// (neighbours recomputed with the owner's fma), else p_old is the direction.
+template <class T, bool FUSED>
+__global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __restrict__ val,
+                                                   const T* __restrict__ z, const T* __restrict__ p_old,
+                                                   T* __restrict__ p_new, T* __restrict__ q,
+                                                   const int32_t* __restrict__ frozen, int cur,
+                                                   double* __restrict__ part, MeshScal* __restrict__ ms) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) continue;  // uniform per block
+    const T beta = FUSED ? static_cast<T>(ms[b].beta) : T(0);
+    BDot<T> acc;
+    for (int64_t r = C.start[c] + threadIdx.x; r < C.start[c + 1]; r += blockDim.x) {
+      const int64_t sl = r >> 5, lane = r & 31;
+      const int64_t b0 = M.ptr[sl];
+      const int w = static_cast<int>((M.ptr[sl + 1] - b0) >> 5);
+      const int32_t* cp = M.col + b0 + lane;
+      const T* vp = val + b0 + lane;
+      T sum = T(0);
+#pragma unroll 4
+      for (int k = 0; k < w; ++k) {
+        const int cc = cp[k * 32];
+        const T pc = FUSED ? fma(beta, p_old[cc], z[cc]) : p_old[cc];
+        sum = fma(vp[k * 32], pc, sum);
+      }
+      const T pi = FUSED ? fma(beta, p_old[r], z[r]) : p_old[r];
+      if (FUSED) p_new[r] = pi;
+      q[r] = sum;
+      acc.add(pi, sum);
+    }
+    const double tot = BlockReduce(acc.get(), red);
+    if (threadIdx.x == 0) part[c] = tot;
+    const int64_t c0 = C.mesh_chunk[b], c1 = C.mesh_chunk[b + 1];
+    if (MeshDone(ms, b, static_cast<unsigned int>(c1 - c0))) {
+      const double pq = MeshPartSum(part, 1, 0, c0, c1, red);
+      if (threadIdx.x == 0) {
+        ms[b].pq = pq;
+        ms[b].alpha = pq != 0.0 ? ms[b].rz[cur] / pq : 0.0;
+        ms[b].cnt = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// x += alpha_b p; r -= alpha_b q; z = D^-1 r; <r, z>, <r, r> per mesh ->
+// rz[cur ^ 1], rr, beta_b.
+template <class T>
+__global__ void __launch_bounds__(kPB) BUpdateKernel(Chunks C, const T* __restrict__ dinv, const T* __restrict__ p,
+                                                     const T* __restrict__ q, T* __restrict__ x, T* __restrict__ r,
+                                                     T* __restrict__ z, const int32_t* __restrict__ frozen, int cur,
+                                                     double* __restrict__ part, MeshScal* __restrict__ ms) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) continue;
+    const T alpha = static_cast<T>(ms[b].alpha);
+    BDot<T> arz, arr;
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      x[i] = fma(alpha, p[i], x[i]);
+      const T ri = fma(-alpha, q[i], r[i]);
+      r[i] = ri;
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      arz.add(ri, zi);
+      arr.add(ri, ri);
+    }
+    const double s1 = BlockReduce(arz.get(), red);
+    const double s2 = BlockReduce(arr.get(), red);
+    if (threadIdx.x == 0) {
+      part[2 * c] = s1;
+      part[2 * c + 1] = s2;
+    }
+    const int64_t c0 = C.mesh_chunk[b], c1 = C.mesh_chunk[b + 1];
+    if (MeshDone(ms, b, static_cast<unsigned int>(c1 - c0))) {
+      const double rz = MeshPartSum(part, 2, 0, c0, c1, red);
+      const double rr = MeshPartSum(part, 2, 1, c0, c1, red);
+      if (threadIdx.x == 0) {
+        const double rz_old = ms[b].rz[cur];
+        ms[b].rz[cur ^ 1] = rz;
+        ms[b].beta = rz_old != 0.0 ? rz / rz_old : 0.0;
+        ms[b].rr = rr;
+        ms[b].cnt = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// p = z + beta_b p (FP64 path: one FMA per row instead of one per entry).
+template <class T>
+__global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const T* __restrict__ z, T* __restrict__ p,
+                                                        const int32_t* __restrict__ frozen,
+                                                        const MeshScal* __restrict__ ms) {
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) continue;
+    const T beta = static_cast<T>(ms[b].beta);
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
+  }
+}
+
+// z = D^-1 r, p = z; rz[0], rr per mesh; beta = 0 (so the first direction
+// update, fused or not, gives p = z).
+template <class T>
+__global__ void __launch_bounds__(kPB) BStartKernel(Chunks C, const T* __restrict__ dinv, const T* __restrict__ r,
+                                                    T* __restrict__ z, T* __restrict__ p,
+                                                    const int32_t* __restrict__ frozen, double* __restrict__ part,
+                                                    MeshScal* __restrict__ ms) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (frozen[b]) continue;
+    double arz = 0.0, arr = 0.0;
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      const T ri = r[i];
+      const T zi = dinv[i] * ri;
+      z[i] = zi;
+      p[i] = zi;
+      arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
+      arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
+    }
+    const double s1 = BlockReduce(arz, red);
+    const double s2 = BlockReduce(arr, red);
+    if (threadIdx.x == 0) {
+      part[2 * c] = s1;
+      part[2 * c + 1] = s2;
+    }
+    const int64_t c0 = C.mesh_chunk[b], c1 = C.mesh_chunk[b + 1];
+    if (MeshDone(ms, b, static_cast<unsigned int>(c1 - c0))) {
+      const double rz = MeshPartSum(part, 2, 0, c0, c1, red);
+      const double rr = MeshPartSum(part, 2, 1, c0, c1, red);
+      if (threadIdx.x == 0) {
+        ms[b].rz[0] = rz;
+        ms[b].rz[1] = 0.0;
+        ms[b].alpha = 0.0;
+        ms[b].beta = 0.0;
+        ms[b].rr = rr;
+        ms[b].cnt = 0;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Row r of a CSR matrix times x by the 8 lanes of a group (fixed shuffle order).
 template <class T>
 __device__ __forceinline__ T RowDotB(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
                                      const T* __restrict__ val, const T* __restrict__ x, int64_t r, int64_t end,
@@ -216,107 +400,6 @@ __device__ __forceinline__ T RowDotB(const int32_t* __restrict__ rp, const int32
 #pragma unroll
   for (int o = kLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLanes);
   return s;
-}
-
-// q = A p on the chunk's rows, pq partial; frozen meshes skipped.
-template <class T>
-__global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, const int32_t* __restrict__ rp,
-                                                   const int32_t* __restrict__ col, const T* __restrict__ val,
-                                                   const T* __restrict__ p, T* __restrict__ q,
-                                                   const int32_t* __restrict__ frozen, double* __restrict__ pq) {
-  __shared__ double red[32];
-  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
-    if (frozen[C.mesh[c]]) continue;  // uniform per block
-    const int64_t s = C.start[c], e = C.start[c + 1];
-    const int sub = threadIdx.x % kLanes, grp = threadIdx.x / kLanes;
-    T acc = T(0);
-    for (int64_t wb = s; wb < e; wb += kPB / kLanes) {
-      const int64_t r = wb + grp;
-      const T v = RowDotB<T>(rp, col, val, p, r, e, sub);
-      if (sub == 0 && r < e) {
-        q[r] = v;
-        acc = fma(p[r], v, acc);
-      }
-    }
-    const double tot = BlockReduce(static_cast<double>(acc), red);
-    if (threadIdx.x == 0) pq[c] = tot;
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kPB) BUpdateKernel(Chunks C, const double* __restrict__ pq,
-                                                     const double* __restrict__ rz_old, const T* __restrict__ dinv,
-                                                     const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ x,
-                                                     T* __restrict__ r, T* __restrict__ z,
-                                                     const int32_t* __restrict__ frozen, double* __restrict__ rz_new,
-                                                     double* __restrict__ rr) {
-  __shared__ double red[32];
-  __shared__ double sh;
-  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
-    const int b = C.mesh[c];
-    if (frozen[b]) {
-      if (threadIdx.x == 0) rz_new[c] = rz_old[c];
-      continue;
-    }
-    const double pqs = MeshSum(pq, C, b, &sh);
-    const double rzs = MeshSum(rz_old, C, b, &sh);
-    const T alpha = static_cast<T>(pqs != 0.0 ? rzs / pqs : 0.0);
-    T arz = T(0), arr = T(0);
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
-      x[i] = fma(alpha, p[i], x[i]);
-      const T ri = fma(-alpha, q[i], r[i]);
-      r[i] = ri;
-      const T zi = dinv[i] * ri;
-      z[i] = zi;
-      arz = fma(ri, zi, arz);
-      arr = fma(ri, ri, arr);
-    }
-    const double s1 = BlockReduce(static_cast<double>(arz), red);
-    const double s2 = BlockReduce(static_cast<double>(arr), red);
-    if (threadIdx.x == 0) {
-      rz_new[c] = s1;
-      rr[c] = s2;
-    }
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const double* __restrict__ rz_new,
-                                                        const double* __restrict__ rz_old, const T* __restrict__ z,
-                                                        T* __restrict__ p, const int32_t* __restrict__ frozen) {
-  __shared__ double sh;
-  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
-    const int b = C.mesh[c];
-    if (frozen[b]) continue;
-    const double rn = MeshSum(rz_new, C, b, &sh);
-    const double ro = MeshSum(rz_old, C, b, &sh);
-    const T beta = static_cast<T>(ro != 0.0 ? rn / ro : 0.0);
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kPB) BStartKernel(Chunks C, const T* __restrict__ dinv, const T* __restrict__ r,
-                                                    T* __restrict__ z, T* __restrict__ p, double* __restrict__ rz,
-                                                    double* __restrict__ rr) {
-  __shared__ double red[32];
-  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
-    T arz = T(0), arr = T(0);
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
-      const T ri = r[i];
-      const T zi = dinv[i] * ri;
-      z[i] = zi;
-      p[i] = zi;
-      arz = fma(ri, zi, arz);
-      arr = fma(ri, ri, arr);
-    }
-    const double s1 = BlockReduce(static_cast<double>(arz), red);
-    const double s2 = BlockReduce(static_cast<double>(arr), red);
-    if (threadIdx.x == 0) {
-      rz[c] = s1;
-      rr[c] = s2;
-    }
-  }
 }
 
 // r = b - A x (FP64) and rr partials; optional x == null means x = 0.
@@ -367,32 +450,6 @@ __global__ void BCorrectKernel(Chunks C, const float* __restrict__ d, const doub
   }
 }
 
-__global__ void BDiagKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                            const double* __restrict__ val, double* __restrict__ dinv, float* __restrict__ dinv32,
-                            int32_t* st) {
-  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
-       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    double d = 0.0;
-    for (int64_t q = rp[r]; q < rp[r + 1]; ++q)
-      if (col[q] == r) d = val[q];
-    if (!(d > 0.0)) atomicCAS(st, 0, static_cast<int>(r) + 1);
-    dinv[r] = d > 0.0 ? 1.0 / d : 0.0;
-    dinv32[r] = static_cast<float>(dinv[r]);
-  }
-}
-
-__global__ void BToFloatKernel(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    b[i] = static_cast<float>(a[i]);
-}
-
-__global__ void BRowPtr32Kernel(int64_t n, const int64_t* __restrict__ a, int32_t* __restrict__ b) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    b[i] = static_cast<int32_t>(a[i]);
-}
-
 // Per-mesh sums of chunk partials on the host (chunk order).
 void MeshSums(lfg_batch* B, const double* dev_part, std::vector<double>& out) {
   std::vector<double> h(B->nchunks);
@@ -405,57 +462,69 @@ void MeshSums(lfg_batch* B, const double* dev_part, std::vector<double>& out) {
 
 template <class T>
 struct BState {
-  DevBuf r, z, p, q, pq, rz[2], rr;
+  DevBuf r, z, p[2], q, part, ms;
 };
 
 template <class T>
-void BAlloc(lfg_ctx* ctx, int64_t n, int64_t nch, BState<T>& S) {
+void BAlloc(lfg_ctx* ctx, int64_t n, int64_t nch, int nb, BState<T>& S) {
   cudaStream_t s = ctx->stream;
   S.r.alloc(n * sizeof(T), s);
   S.z.alloc(n * sizeof(T), s);
-  S.p.alloc(n * sizeof(T), s);
+  S.p[0].alloc(n * sizeof(T), s);
+  S.p[1].alloc(n * sizeof(T), s);
   S.q.alloc(n * sizeof(T), s);
-  S.pq.alloc(nch * sizeof(double), s);
-  S.rz[0].alloc(nch * sizeof(double), s);
-  S.rz[1].alloc(nch * sizeof(double), s);
-  S.rr.alloc(nch * sizeof(double), s);
+  S.part.alloc(2 * nch * sizeof(double), s);
+  S.ms.alloc(nb * sizeof(MeshScal), s);
+  LFG_CUDA(cudaMemsetAsync(S.ms.p, 0, nb * sizeof(MeshScal), s));
+}
+
+// rr of every mesh (from the device scalars).
+void MeshRR(lfg_batch* B, const DevBuf& ms, std::vector<double>& out) {
+  std::vector<MeshScal> h(B->nb);
+  LFG_CUDA(cudaMemcpyAsync(h.data(), ms.p, B->nb * sizeof(MeshScal), cudaMemcpyDeviceToHost, B->ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(B->ctx->stream));
+  out.resize(B->nb);
+  for (int b = 0; b < B->nb; ++b) out[b] = h[b].rr;
 }
 
 // Batched PCG in precision T on S.r (filled): per-mesh targets target_rr[b]
-// (squared norms); meshes with done[b] start frozen.  Returns per-mesh
+// (squared norms); meshes with frozen_h[b] start frozen.  Returns per-mesh
 // iterations in it_out and final recursive rr in rr_out.
 template <class T>
-void BRunPcg(lfg_batch* B, lfg_csr* A, const T* val, const T* dinv, T* x, BState<T>& S, const Chunks& C,
+void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BState<T>& S, const Chunks& C,
              const std::vector<double>& target_rr, std::vector<int32_t>& frozen_h, DevBuf& frozen_d, int max_it,
              int check_every, std::vector<int>& it_out, std::vector<double>& rr_out) {
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
-  const int32_t* rp = A->rowptr32.as<int32_t>();
-  const int32_t* col = A->col.as<int32_t>();
-  BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(), S.p.template as<T>(),
-                                      S.rz[0].template as<double>(), S.rr.template as<double>());
+  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+  MeshScal* ms = S.ms.template as<MeshScal>();
+  double* part = S.part.template as<double>();
+  LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(), S.p[0].template as<T>(),
+                                      frozen_d.as<int32_t>(), part, ms);
   LFG_LAUNCHED(ctx);
   std::vector<double> rr;
-  MeshSums(B, S.rr.template as<double>(), rr);
+  MeshRR(B, S.ms, rr);
   it_out.assign(B->nb, 0);
   for (int b = 0; b < B->nb; ++b)
     if (!(rr[b] > target_rr[b])) frozen_h[b] = 1;
   LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  constexpr bool kFused = sizeof(T) == 4;
   const int body = std::max(2, check_every + (check_every & 1));
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < body; ++k) {
-    double* rz_old = S.rz[k & 1].template as<double>();
-    double* rz_new = S.rz[(k + 1) & 1].template as<double>();
-    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, rp, col, val, S.p.template as<T>(), S.q.template as<T>(),
-                                       frozen_d.as<int32_t>(), S.pq.template as<double>());
-    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, S.pq.template as<double>(), rz_old, dinv, S.p.template as<T>(),
-                                         S.q.template as<T>(), x, S.r.template as<T>(), S.z.template as<T>(),
-                                         frozen_d.as<int32_t>(), rz_new, S.rr.template as<double>());
-    BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, rz_new, rz_old, S.z.template as<T>(), S.p.template as<T>(),
-                                            frozen_d.as<int32_t>());
+    const int cur = k & 1;
+    T* p_old = S.p[kFused ? cur : 0].template as<T>();
+    T* p_new = S.p[kFused ? (cur ^ 1) : 0].template as<T>();
+    if (!kFused)
+      BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p_old, frozen_d.as<int32_t>(), ms);
+    BSpmvKernel<T, kFused><<<grid, kPB, 0, s>>>(C, M, sval, S.z.template as<T>(), p_old, p_new, S.q.template as<T>(),
+                                                frozen_d.as<int32_t>(), cur, part, ms);
+    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p_new, S.q.template as<T>(), x, S.r.template as<T>(),
+                                         S.z.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
   }
   LFG_CUDA(cudaStreamEndCapture(s, &graph));
   LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
@@ -466,9 +535,9 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* val, const T* dinv, T* x, BState
       for (int b = 0; b < B->nb; ++b) active += !frozen_h[b];
       if (!active) break;
       LFG_CUDA(cudaGraphLaunch(exec, s));
-      CountLaunch(ctx, 3 * body);
+      CountLaunch(ctx, (kFused ? 2 : 3) * body);
       it += body;
-      MeshSums(B, S.rr.template as<double>(), rr);
+      MeshRR(B, S.ms, rr);
       bool changed = false;
       for (int b = 0; b < B->nb; ++b)
         if (!frozen_h[b]) {
@@ -745,43 +814,25 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
   const int64_t n = B->dof_off[B->nb];
   if (A->rows != n || A->cols != n) Fail(LFG_INVALID_ARG, "matrix size differs from the batch");
   if (A->nnz >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "solver needs nnz < 2^31");
-  // solver-side CSR data (same fields lfg_solve_pcg uses)
-  if (!A->rowptr32.p) {
-    A->rowptr32.alloc((n + 1) * sizeof(int32_t), s);
-    BRowPtr32Kernel<<<GridFor(ctx, n + 1, 256), 256, 0, s>>>(n + 1, A->rowptr.as<int64_t>(), A->rowptr32.as<int32_t>());
-    LFG_LAUNCHED(ctx);
-  }
-  if (!A->dinv.p) {
-    A->dinv.alloc(n * sizeof(double), s);
-    A->dinv32.alloc(n * sizeof(float), s);
-    ReadAndClearStatus(ctx);
-    BDiagKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, A->rowptr.as<int64_t>(), A->col.as<int32_t>(),
-                                                     A->val.as<double>(), A->dinv.as<double>(), A->dinv32.as<float>(),
-                                                     StatusWord(ctx));
-    LFG_LAUNCHED(ctx);
-    if (int32_t code = ReadAndClearStatus(ctx)) {
-      A->dinv.reset();
-      Fail(LFG_INVALID_ARG, "Jacobi preconditioner: non-positive diagonal in row " + std::to_string(code - 1));
-    }
-  }
+  PrepareSolve(A);  // Jacobi diagonal, int32 row pointers, SELL-32 copy
   Chunks C{B->chunk_mesh.as<int32_t>(), B->chunk_start.as<int64_t>(), B->mesh_chunk_off.as<int64_t>(), B->nchunks};
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
   const int check = opts->check_every > 0 ? opts->check_every : 32;
   const int max_it = opts->max_iterations > 0 ? opts->max_iterations : 100000;
   const double rtol = opts->rtol > 0 ? opts->rtol : 1e-10;
   BState<double> S;
-  BAlloc(ctx, n, C.nchunks, S);
+  BAlloc(ctx, n, C.nchunks, B->nb, S);
   DevBuf frozen;
   frozen.alloc(B->nb * sizeof(int32_t), s);
   std::vector<double> bb, rr;
   BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), nullptr,
-                                      bvec, S.r.as<double>(), S.rr.as<double>());
+                                      bvec, S.r.as<double>(), S.part.as<double>());
   LFG_LAUNCHED(ctx);
-  MeshSums(B, S.rr.as<double>(), bb);
+  MeshSums(B, S.part.as<double>(), bb);
   BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x, bvec,
-                                      S.r.as<double>(), S.rr.as<double>());
+                                      S.r.as<double>(), S.part.as<double>());
   LFG_LAUNCHED(ctx);
-  MeshSums(B, S.rr.as<double>(), rr);
+  MeshSums(B, S.part.as<double>(), rr);
   std::vector<double> target(B->nb);
   for (int b = 0; b < B->nb; ++b) target[b] = rtol * rtol * bb[b];
   std::vector<int32_t> frozen_h(B->nb, 0);
@@ -798,26 +849,21 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
         active += !fz[b];
       }
       if (!active) break;
-      BRunPcg<double>(B, A, A->val.as<double>(), A->dinv.as<double>(), x, S, C, target, fz, frozen, max_it, check,
+      BRunPcg<double>(B, A, A->sell_val.as<double>(), A->dinv.as<double>(), x, S, C, target, fz, frozen, max_it, check,
                       it1, rr1);
       for (int b = 0; b < B->nb; ++b) {
         its[b] += it1[b];
         refinements[b] += it1[b] > 0;
       }
       BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
-                                          bvec, S.r.as<double>(), S.rr.as<double>());
+                                          bvec, S.r.as<double>(), S.part.as<double>());
       LFG_LAUNCHED(ctx);
-      MeshSums(B, S.rr.as<double>(), rr);
+      MeshSums(B, S.part.as<double>(), rr);
     }
   } else if (opts->precision == LFG_SOLVE_MIXED) {
-    // FP32 matrix copy and FP32 inner PCG state
-    if (!A->val32.p) {
-      A->val32.alloc(std::max<int64_t>(A->nnz, 1) * sizeof(float), s);
-      BToFloatKernel<<<GridFor(ctx, A->nnz, 256), 256, 0, s>>>(A->nnz, A->val.as<double>(), A->val32.as<float>());
-      LFG_LAUNCHED(ctx);
-    }
+    EnsureFloatValues(A);  // FP32 SELL values
     BState<float> S32;
-    BAlloc(ctx, n, C.nchunks, S32);
+    BAlloc(ctx, n, C.nchunks, B->nb, S32);
     DevBuf d32, scale, done;
     d32.alloc(n * sizeof(float), s);
     scale.alloc(B->nb * sizeof(double), s);
@@ -843,15 +889,15 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
       LFG_CUDA(cudaMemcpyAsync(done.p, dn.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
       BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
       LFG_LAUNCHED(ctx);
-      BRunPcg<float>(B, A, A->val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), S32, C, tin, fz, frozen,
+      BRunPcg<float>(B, A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), S32, C, tin, fz, frozen,
                      max_it, check, it1, rr1);
       BCorrectKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), done.as<int32_t>(), x);
       LFG_LAUNCHED(ctx);
       BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
-                                          bvec, S.r.as<double>(), S.rr.as<double>());
+                                          bvec, S.r.as<double>(), S.part.as<double>());
       LFG_LAUNCHED(ctx);
       std::vector<double> rr_new;
-      MeshSums(B, S.rr.as<double>(), rr_new);
+      MeshSums(B, S.part.as<double>(), rr_new);
       bool progress = false;
       for (int b = 0; b < B->nb; ++b)
         if (!dn[b]) {

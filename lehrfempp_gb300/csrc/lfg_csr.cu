@@ -163,6 +163,7 @@ __global__ void ResidualKernel(int64_t rows, const int32_t* __restrict__ rp, con
 
 // ------------------------------------------------------------------- PCG
 constexpr int kPcgBlock = 256;
+constexpr double kDefaultInnerRtol = 1e-4;  // mixed: relative reduction per inner FP32 solve
 constexpr int kSlice = 32;
 
 // Scalars of one PCG run, on the device.  rz[cur] is <r, z> of the current
@@ -455,10 +456,12 @@ __global__ void ScaleToFloatKernel(int64_t n, const double* __restrict__ r, doub
   }
 }
 
-__global__ void AddCorrectionKernel(int64_t n, const float* __restrict__ d, double inv_s, double* __restrict__ x) {
+__global__ void AddCorrectionKernel(int64_t n, float* __restrict__ d, double s, double* __restrict__ x) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    x[i] += static_cast<double>(d[i]) * inv_s;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    x[i] += static_cast<double>(d[i]) * s;
+    d[i] = 0.0f;
+  }
 }
 
 double HostSum(lfg_ctx* ctx, const double* part, int n, std::vector<double>& tmp) {
@@ -470,6 +473,9 @@ double HostSum(lfg_ctx* ctx, const double* part, int n, std::vector<double>& tmp
   return s;
 }
 
+}  // namespace
+
+// Jacobi diagonal + SELL-32 copy (once per matrix); shared with the batched solver.
 void PrepareSolve(lfg_csr* A) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
@@ -526,6 +532,8 @@ void EnsureFloatValues(lfg_csr* A) {
   }
 }
 
+namespace {
+
 // Work vectors of one PCG run in precision T.  r is filled by the caller;
 // res holds the block partials of the FP64 residual kernel.
 template <class T>
@@ -556,15 +564,25 @@ double ReadRR(lfg_ctx* ctx, const DevBuf& scal) {
   return rr;
 }
 
-// PCG on A x = b in precision T from the residual already in S.r (x holds
-// the matching iterate).  Returns the iterations done; rr_out = <r, r> of the
-// recursively updated residual.
+// An instantiated CUDA graph of PCG iterations.
+struct PcgGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+  void Release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
+// The captured iteration body: `body` PCG iterations (even: the p buffers
+// and rz slots alternate).
 template <class T>
-int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double target_rr, int max_it,
-           int check_every, PcgState<T>& S, double& rr_out) {
+PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, int body, PcgState<T>& S) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
-  const int nb = S.nb;
   const int spmv_blocks = static_cast<int>(std::max<int64_t>(
       1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (A->nslices + 7) / 8)));
   constexpr int U = sizeof(T) == 8 ? 2 : 4;
@@ -572,21 +590,11 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
       1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 4, (n + U * kPcgBlock - 1) / (U * kPcgBlock))));
   PcgScalars* sc = S.scal.template as<PcgScalars>();
   double* part = S.part.template as<double>();
-  PcgStartKernel<T><<<nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
-                                             S.p[0].template as<T>(), part, sc);
-  LFG_LAUNCHED(ctx);
-  double rr = ReadRR(ctx, S.scal);
-  int it = 0;
-  if (!(rr > target_rr)) {
-    rr_out = rr;
-    return 0;
-  }
-  // `body` iterations per graph (even: the p buffers and rz slots alternate)
-  const int body = std::max(2, check_every + (check_every & 1));
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  PcgGraph g;
   constexpr bool kFused = sizeof(T) == 4;
+  g.launches = (kFused ? 2 : 3) * body;
+  cudaGraph_t graph = nullptr;
+  LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < body; ++k) {
     const int cur = k & 1;
     T* p_old = S.p[kFused ? cur : 0].template as<T>();
@@ -603,22 +611,44 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
   LFG_CUDA(ce);
-  LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  g.graph = graph;
+  LFG_CUDA(cudaGraphInstantiate(&g.exec, graph, 0));
+  return g;
+}
+
+// PCG on A x = b in precision T from the residual already in S.r (x holds
+// the matching iterate).  Returns the iterations done; rr_out = <r, r> of the
+// recursively updated residual.
+template <class T>
+int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double target_rr, int max_it,
+           int check_every, PcgState<T>& S, double& rr_out) {
+  lfg_ctx* ctx = A->ctx;
+  cudaStream_t s = ctx->stream;
+  PcgStartKernel<T><<<S.nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
+                                               S.p[0].template as<T>(), S.part.template as<double>(),
+                                               S.scal.template as<PcgScalars>());
+  LFG_LAUNCHED(ctx);
+  double rr = ReadRR(ctx, S.scal);
+  int it = 0;
+  if (!(rr > target_rr)) {
+    rr_out = rr;
+    return 0;
+  }
+  const int body = std::max(2, check_every + (check_every & 1));
+  PcgGraph g = CapturePcg<T>(A, sval, dinv, x, n, body, S);
   try {
     while (it < max_it) {
-      LFG_CUDA(cudaGraphLaunch(exec, s));
-      CountLaunch(ctx, (kFused ? 2 : 3) * body);
+      LFG_CUDA(cudaGraphLaunch(g.exec, s));
+      CountLaunch(ctx, g.launches);
       it += body;
       rr = ReadRR(ctx, S.scal);
       if (!(rr > target_rr)) break;  // also stops on NaN
     }
   } catch (...) {
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
+    g.Release();
     throw;
   }
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
+  g.Release();
   rr_out = rr;
   return it;
 }
@@ -801,17 +831,16 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     AllocState(ctx, n, S32);
     DevBuf d32;
     d32.alloc(n * sizeof(float), s);
-    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : 1e-4;
+    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : kDefaultInnerRtol;
     int total = 0, outer = 0;
     while (total < max_it && outer < 200) {
       const double rnorm = std::sqrt(rr);
       if (rr <= target) break;
-      // inner FP32 PCG on A d = r / ||r||
-      const double scale = 1.0 / rnorm;
-      ScaleToFloatKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S64.r.as<double>(), scale, S32.r.as<float>(),
+      // inner FP32 PCG on A d = r / ||r|| (d starts at 0)
+      ScaleToFloatKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S64.r.as<double>(), 1.0 / rnorm, S32.r.as<float>(),
                                                               d32.as<float>());
       LFG_LAUNCHED(ctx);
-      // inner target relative to ||r/||r|| || = 1, but never below what the outer loop needs
+      // inner target relative to ||r / ||r|| || = 1, never below what the outer loop needs
       const double need = std::max(inner, 0.5 * std::sqrt(target) / rnorm);
       double rr_in = 0.0;
       const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
@@ -824,11 +853,9 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       LFG_LAUNCHED(ctx);
       const double rr_new = HostSum(ctx, S64.res.as<double>(), nb, tmp);
       ++outer;
-      if (!(rr_new < rr)) {  // stagnation: no progress in FP32
-        rr = rr_new;
-        break;
-      }
+      const bool progress = rr_new < rr;
       rr = rr_new;
+      if (!progress) break;  // stagnation: no progress in FP32
     }
     st.iterations = total;
     st.refinements = outer;

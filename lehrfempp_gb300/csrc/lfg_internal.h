@@ -212,5 +212,9 @@ int32_t ReadAndClearStatus(lfg_ctx* ctx, int32_t* detail = nullptr);
 int32_t* StatusWord(lfg_ctx* ctx);
 // Copy a small device value to the host synchronously (stream ordered).
 void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
+// Solver data of a CSR matrix (lfg_csr.cu): Jacobi diagonal (FP64 + FP32),
+// int32 row pointers and the SELL-32 copy; FP32 values for mixed precision.
+void PrepareSolve(lfg_csr* A);
+void EnsureFloatValues(lfg_csr* A);
 
 }  // namespace lfg
