@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512, help="config-4 meshes (0: skip the batch leg)")
     ap.add_argument("--grad-size", type=int, default=1024, help="config-5 mesh size (0: skip the gradient leg)")
+    ap.add_argument("--ho-size", type=int, default=1024, help="config-3 mesh size (0: skip the high-order leg)")
     return ap.parse_args()
 
 
@@ -104,6 +105,15 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# DRAM bytes per cell moved by the element kernels, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the 1024x1024 hybrid O2 case
+# (1,048,980 triangles, 524,086 quadrilaterals; outputs 0.6-0.7 GB >> L2), scaled
+# to a full launch by the cell count.  Command and figures:
+# profiles/element_kernels_hybrid_o2.md.
+DRAM_BYTES_PER_CELL = {"rd_tria_df": (134030080 + 547695616) / 1048980,
+                       "rd_quad_df": (120022528 + 620115200) / 524086}
 
 
 def algorithmic_bytes(space, mesh, kind):
@@ -193,6 +203,45 @@ def solve_leg(L, W, ctx, n):
         out[name]["rel_err_vs_fp64_1e-13"] = float(np.linalg.norm(xs[name] - r) / np.linalg.norm(r))
     out["mixed_vs_fp64"] = out["mixed"]["dofs_per_s"] / out["fp64"]["dofs_per_s"]
     return out
+
+
+def high_order_leg(L, W, ctx, n, steps=5):
+    """Config 3: TPTriag n x n, O3, degree-6 rules, alpha = 1 + 0.5 sin(4 pi x)
+    cos(4 pi y), gamma = 1 (matrix), f = O1 interpolant of N(0,1) nodal values
+    (vector).  Triplets/s of the matrix assembly and its HBM fraction."""
+    wl = W.config3(n)
+    keep = []
+    mesh = W.build_mesh(ctx, wl["mesh"])
+    sp = L.Space.lagrange(mesh, 3)
+    prov = L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep), wl["qr_tria"],
+                         wl["qr_quad"])
+    lprov = L.load_provider(W.to_coeff(ctx, wl["f"], keep), wl["qr_tria"], wl["qr_quad"])
+    coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets)
+    b = ctx.zeros(sp.num_dofs)
+    for _ in range(2):
+        coo.set_zero()
+        L.assemble_matrix_rd(sp, prov, coo)
+    ctx.synchronize()
+    ctx.timer_begin()
+    for _ in range(steps):
+        coo.set_zero()
+        L.assemble_matrix_rd(sp, prov, coo)
+    ms = ctx.timer_end() / steps
+    L.assemble_vector_load(sp, lprov, b)
+    ctx.timer_begin()
+    for _ in range(steps):
+        L.assemble_vector_load(sp, lprov, b)
+    vms = ctx.timer_end() / steps
+    # 16 n^2 written + 3 vertex ids (12) + 3 coordinates (48) + dofs (4 n) per cell
+    per_cell = 16 * 100 + 12 + 48 + 40
+    gbs = per_cell * mesh.num_cells / (ms * 1e-3) / 1e9
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"] \
+        if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0
+    return {"workload": "TPTriag %dx%d O3 (%d cells, %d dofs), degree-6 rules, analytic alpha, gamma 1" %
+                        (n, n, mesh.num_cells, sp.num_dofs),
+            "triplets_per_s": sp.num_triplets / (ms * 1e-3), "ms_per_assembly": ms,
+            "hbm_gbs": gbs, "hbm_frac_of_measured": gbs / peak, "bytes_per_cell": per_cell,
+            "load_vector_ms": vms}
 
 
 def batch_leg(L, W, ctx, count):
@@ -465,6 +514,7 @@ def run_ours(args):
         except Exception as e:  # a failing side leg is reported, not fatal to the headline line
             return {"error": "%s: %s" % (type(e).__name__, e)}
 
+    high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size) if args.solve_size > 0 else None
     batch = leg(batch_leg, L, W, ctx, args.batch_count) if args.batch_count > 0 else None
     gradient = leg(gradient_leg, L, W, ctx, args.grad_size, steps=3,
@@ -487,14 +537,19 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single"},
             "clocks": clk, "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "kernel": dom,
+                         "frac": achieved / hbm_peak,
+                         "traffic": DRAM_BYTES_PER_CELL[dom] * (mesh.num_quads if kind == "quad" else mesh.num_trias)
+                         if dom in DRAM_BYTES_PER_CELL else None,
+                         "traffic_source": "ncu dram bytes per cell (1024x1024 case) x cells of one launch",
+                         "kernel": dom,
                          "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_cell": per_cell,
                          "avg_launch_ms": fam[dom][0], "peak_source": peaks_src},
             "kernels_ms": {k: v[0] for k, v in fam.items()},
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "solve": solve, "batch": batch, "gradient": gradient,
+            "e2e": e2e, "cpu_baseline": cpu, "high_order": high_order, "solve": solve, "batch": batch,
+            "gradient": gradient,
         }
         print(json.dumps(line))
     ctx.close()

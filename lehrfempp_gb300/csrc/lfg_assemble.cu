@@ -362,6 +362,146 @@ __global__ void __launch_bounds__(128) RDTriaDfKernel(AsmArgs a, DfArgs d) {
   }
 }
 
+// ------------------------------ point-varying alpha on triangles, df32 path
+// Affine triangles whose alpha varies over the cell (analytic families, O1
+// nodal interpolant) and whose gamma is cell-constant: per point
+// c_k = w_k alpha(x_k) |det J| J^-1 J^-T in df32 (the analytic families through
+// SinCosPiDF / Horner, the global point from the FP64 vertex differences),
+// A(e) = sum_k c_k . T_k(e) + gamma |det J| R_mass(e).  Cells with an input or
+// a point value outside the df32 range take the FP64 per-point formula.
+
+// FP64 per-point formula for one affine triangle with point-varying alpha
+// (rarely taken; runtime loops keep it small).
+template <int N>
+__device__ void TriaVaryF64(const AsmArgs& a, int c, const int4& cn, const double2 (&v)[4], double* vals) {
+  constexpr int E = N * (N + 1) / 2;
+  const double* tab = a.tab;
+  const Tab& L = a.L;
+  double m00, m01, m11, adet;
+  TriaMetric(v, m00, m01, m11, adet);
+  const double ga = CellConst(a.gamma, c);
+  for (int e = 0; e < E; ++e) vals[e] = 0.0;
+#pragma unroll 1
+  for (int k = 0; k < L.nq; ++k) {
+    const double al = EvalCoeff<false>(a.alpha, c, cn, v, k, tab + L.off_w, tab + L.off_qx, tab + L.off_qy,
+                                       tab + L.off_o1);
+    const double s = tab[L.off_w + k] * al;
+    const double mk = tab[L.off_w + k] * adet * ga;
+    const double* Tk = tab + L.off_T + k * E * 4;
+#pragma unroll 1
+    for (int e = 0; e < E; ++e) {
+      double r = vals[e];
+      r = fma(s * m00, Tk[e * 4 + 0], r);
+      r = fma(s * m01, Tk[e * 4 + 1], r);
+      r = fma(s * m11, Tk[e * 4 + 2], r);
+      r = fma(mk, Tk[e * 4 + 3], r);
+      vals[e] = r;
+    }
+  }
+}
+
+template <int DEG, int NQ>
+__global__ void __launch_bounds__(128) RDTriaVaryDfKernel(AsmArgs a, DfArgs d) {
+  using elem::f2;
+  namespace df = lfg::df;
+  constexpr int N = (DEG + 1) * (DEG + 2) / 2;
+  constexpr int E = N * (N + 1) / 2;
+  constexpr int TILE = 128;
+  constexpr int TP = NQ * E * 4 + E * 4 + NQ + 2 * NQ + 4 * NQ + 23;  // T, R, W, X, O1, SC
+  extern __shared__ __align__(16) unsigned char smraw[];
+  f2* sT = reinterpret_cast<f2*>(smraw);
+  f2* sR = sT + NQ * E * 4;
+  f2* sW = sR + E * 4;
+  f2* sX = sW + NQ;
+  f2* sO1 = sX + 2 * NQ;
+  f2* sSC = sO1 + 4 * NQ;
+  double* svals = reinterpret_cast<double*>(smraw + ((TP * sizeof(f2) + 15) & ~15));
+  int64_t* soff = reinterpret_cast<int64_t*>(svals + TILE * E);
+  int* sdofs = reinterpret_cast<int*>(soff + TILE);
+  __shared__ int smap[N * N];
+  const f2* g = reinterpret_cast<const f2*>(d.tab);
+  for (int i = threadIdx.x; i < NQ * E * 4; i += blockDim.x) sT[i] = g[d.L.off_T + i];
+  for (int i = threadIdx.x; i < E * 4; i += blockDim.x) sR[i] = g[d.L.off_R + i];
+  for (int i = threadIdx.x; i < NQ; i += blockDim.x) sW[i] = g[d.L.off_W + i];
+  for (int i = threadIdx.x; i < 2 * NQ; i += blockDim.x) sX[i] = g[d.L.off_X + i];
+  for (int i = threadIdx.x; i < 4 * NQ; i += blockDim.x) sO1[i] = g[d.L.off_O1 + i];
+  for (int i = threadIdx.x; i < 23; i += blockDim.x) sSC[i] = g[d.L.off_SC + i];
+  FillTripletMap<N>(smap);
+  __syncthreads();
+  elem::AnalyticDF af;
+  af.func = a.alpha.func;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) af.p[i] = df::FromDouble(a.alpha.p[i]);
+  const bool mass = a.gamma.kind != LFG_COEFF_ZERO;
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * TILE; t0 < a.count;
+       t0 += static_cast<int64_t>(gridDim.x) * TILE) {
+    const int ncell = static_cast<int>(a.count - t0 < TILE ? a.count - t0 : TILE);
+    if (threadIdx.x < ncell) {
+      const int c = a.bucket[t0 + threadIdx.x];
+      int4 cn;
+      double2 v[4];
+      LoadVerts<false>(a, c, cn, v);
+      const double jac[4] = {v[1].x - v[0].x, v[2].x - v[0].x, v[1].y - v[0].y, v[2].y - v[0].y};
+      const double ga = mass ? CellConst(a.gamma, c) : 0.0;
+      double* vals = svals + threadIdx.x * E;
+      bool safe = elem::DfSafe(ga) && elem::DfSafe(v[0].x) && elem::DfSafe(v[0].y);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) safe = safe && elem::DfSafe(jac[k]);
+      f2 cpt[NQ][3];
+      f2 mm = df::Make(0.0f);
+      if (safe) {
+        const f2 j00 = df::FromDouble(jac[0]), j01 = df::FromDouble(jac[1]);
+        const f2 j10 = df::FromDouble(jac[2]), j11 = df::FromDouble(jac[3]);
+        f2 m00, m01, m11, adet;
+        elem::TriaMetricDF(j00, j01, j10, j11, m00, m01, m11, adet);
+        const f2 x0 = df::FromDouble(v[0].x), y0 = df::FromDouble(v[0].y);
+        f2 nod[3];
+        if (a.alpha.kind == LFG_COEFF_NODAL_O1) {
+          const double n0 = a.alpha.data[cn.x], n1 = a.alpha.data[cn.y], n2 = a.alpha.data[cn.z];
+          safe = elem::DfSafe(n0) && elem::DfSafe(n1) && elem::DfSafe(n2);
+          nod[0] = df::FromDouble(n0);
+          nod[1] = df::FromDouble(n1);
+          nod[2] = df::FromDouble(n2);
+        }
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+          f2 al;
+          if (a.alpha.kind == LFG_COEFF_NODAL_O1) {
+            al = df::Mul(nod[0], sO1[4 * k]);
+            al = df::MulAdd(nod[1], sO1[4 * k + 1], al);
+            al = df::MulAdd(nod[2], sO1[4 * k + 2], al);
+          } else {
+            const f2 xh = sX[2 * k], yh = sX[2 * k + 1];
+            const f2 X = df::MulAdd(j01, yh, df::MulAdd(j00, xh, x0));
+            const f2 Y = df::MulAdd(j11, yh, df::MulAdd(j10, xh, y0));
+            al = elem::EvalAnalyticDF(af, X, Y, sSC, sSC + 11);
+          }
+          // 2^-30 margin below the df32 range of the products
+          const float aa = fabsf(al.h);
+          safe = safe && (aa == 0.0f || (aa > 8.0e-10f && aa < 1.0e9f));
+          const f2 s = df::Mul(sW[k], al);
+          cpt[k][0] = df::Mul(s, m00);
+          cpt[k][1] = df::Mul(s, m01);
+          cpt[k][2] = df::Mul(s, m11);
+        }
+        if (mass) mm = df::Mul(df::FromDouble(ga), adet);
+      }
+      if (safe) {
+        elem::TriaVaryContractDF<E, NQ>(cpt, sT, mm, mass, sR, vals);
+      } else {
+        TriaVaryF64<N>(a, c, cn, v, vals);
+        atomicAdd(a.fallback, 1ull);
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) sdofs[threadIdx.x * N + i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      soff[threadIdx.x] = a.tri_offset[c];
+    }
+    __syncthreads();
+    WriteTile<N>(a.out, ncell, svals, sdofs, soff, smap);
+    __syncthreads();
+  }
+}
+
 // FP64 per-point formula of a quadrilateral with cell-constant coefficients
 // (cells outside the df32 range), accumulating into vals[E].
 template <int N, bool MASS>
@@ -836,9 +976,38 @@ void LaunchQuadDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   Launch(RDQuadDfKernel<DEG, M, MASS, false>, ctx, a.count, smem, 128, a, d);
 }
 
+template <int DEG, int NQ>
+void LaunchTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  constexpr int N = (DEG + 1) * (DEG + 2) / 2, E = N * (N + 1) / 2;
+  constexpr int TP = NQ * E * 4 + E * 4 + NQ + 2 * NQ + 4 * NQ + 23;
+  const size_t smem = ((TP * 8 + 15) & ~size_t(15)) + 128 * (E * 8 + 8 + N * 4);
+  Launch(RDTriaVaryDfKernel<DEG, NQ>, ctx, a.count, smem, 128, a, d);
+}
+
+// df32 kernel for point-varying alpha on triangles: alpha analytic or O1
+// nodal, gamma cell-constant, a rule with a supported point count.
+template <int DEG>
+bool TryTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  if (!d.tab) return false;
+  if (a.alpha.kind != LFG_COEFF_ANALYTIC && a.alpha.kind != LFG_COEFF_NODAL_O1) return false;
+  const int gk = a.gamma.kind;
+  if (gk != LFG_COEFF_ZERO && gk != LFG_COEFF_CONSTANT && gk != LFG_COEFF_PER_CELL && gk != LFG_COEFF_PER_CELL_EXP)
+    return false;
+  ProfScope prof(ctx, "rd_tria_vary_df");
+  switch (d.L.nq) {
+    case 1: LaunchTriaVaryDf<DEG, 1>(ctx, a, d); return true;
+    case 3: LaunchTriaVaryDf<DEG, 3>(ctx, a, d); return true;
+    case 6: LaunchTriaVaryDf<DEG, 6>(ctx, a, d); return true;
+    case 7: LaunchTriaVaryDf<DEG, 7>(ctx, a, d); return true;
+    case 12: LaunchTriaVaryDf<DEG, 12>(ctx, a, d); return true;
+  }
+  return false;
+}
+
 template <int DEG, bool QUAD>
 void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, bool mass) {
   const size_t smem_gen = a.L.total * sizeof(double);
+  if (!uniform && !QUAD && TryTriaVaryDf<DEG>(ctx, a, d)) return;
   if (uniform && d.tab && !QUAD) {
     constexpr int N = (DEG + 1) * (DEG + 2) / 2, E = N * (N + 1) / 2;
     const size_t smem = ((E * 4 * 8 + 15) & ~size_t(15)) + 128 * (E * 8 + 8 + N * 4);
@@ -1002,7 +1171,7 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_
     a.tab = GetTable(sp, false, deg, rd, a.L);
     a.bucket = m->tria_list.as<int32_t>();
     a.count = m->ntria;
-    DispatchRD<false>(sp->mesh->ctx, deg, a, uniform ? GetDfTable(sp, false, deg, rd) : none, uniform, mass);
+    DispatchRD<false>(sp->mesh->ctx, deg, a, GetDfTable(sp, false, deg, rd), uniform, mass);
   }
   if (m->nquad) {
     const int rd = RuleDegree(pr->qr_degree_quad, deg);

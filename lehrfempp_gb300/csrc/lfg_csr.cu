@@ -276,15 +276,16 @@ __global__ void __launch_bounds__(kPcgBlock) PcgSpmvDirKernel(int64_t rows, int6
   }
 }
 
-// x += alpha p; r -= alpha q; z = D^-1 r; rz[cur ^ 1] = <r, z>, rr = <r, r>,
-// beta = rz[cur ^ 1] / rz[cur].  Several elements per thread and trip, loads
+// x += alpha p; r -= alpha q; z = D^-1 r; rz[cur ^ 1] = <r, z>, rr = <r, r>
+// (only when with_rr: the host reads it once per graph replay), beta =
+// rz[cur ^ 1] / rz[cur].  Several elements per thread and trip, loads
 // first, so each thread keeps several independent loads in flight.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock, 4) PcgUpdateKernel(int64_t rows, const T* __restrict__ dinv,
                                                              const T* __restrict__ p, const T* __restrict__ q,
                                                              T* __restrict__ x, T* __restrict__ r,
-                                                             T* __restrict__ z, int cur, double* __restrict__ part,
-                                                             PcgScalars* __restrict__ sc) {
+                                                             T* __restrict__ z, int cur, bool with_rr,
+                                                             double* __restrict__ part, PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
   __shared__ T salpha;
   if (threadIdx.x == 0) salpha = static_cast<T>(sc->alpha);
@@ -312,24 +313,24 @@ __global__ void __launch_bounds__(kPcgBlock, 4) PcgUpdateKernel(int64_t rows, co
         const T zi = dv[u] * ri;
         z[i] = zi;
         arz.add(ri, zi);
-        arr.add(ri, ri);
+        if (with_rr) arr.add(ri, ri);
       }
     }
   }
   const double s1 = BlockSum(arz.get(), red);
-  const double s2 = BlockSum(arr.get(), red);
+  const double s2 = with_rr ? BlockSum(arr.get(), red) : 0.0;
   if (threadIdx.x == 0) {
     part[2 * blockIdx.x] = s1;
     part[2 * blockIdx.x + 1] = s2;
   }
   if (FinishedLast(&sc->counter)) {
     const double rz = SumParts(part, gridDim.x, 2, 0, red);
-    const double rr = SumParts(part, gridDim.x, 2, 1, red);
+    const double rr = with_rr ? SumParts(part, gridDim.x, 2, 1, red) : 0.0;
     if (threadIdx.x == 0) {
       const double rz_old = sc->rz[cur];
       sc->rz[cur ^ 1] = rz;
       sc->beta = rz_old != 0.0 ? rz / rz_old : 0.0;
-      sc->rr = rr;
+      if (with_rr) sc->rr = rr;
       sc->counter = 0;
     }
   }
@@ -607,7 +608,7 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, i
                                                                   S.z.template as<T>(), p_old, p_new,
                                                                   S.q.template as<T>(), cur, part, sc);
     PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p_new, S.q.template as<T>(), x, S.r.template as<T>(),
-                                                S.z.template as<T>(), cur, part, sc);
+                                                           S.z.template as<T>(), cur, k == body - 1, part, sc);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
   LFG_CUDA(ce);

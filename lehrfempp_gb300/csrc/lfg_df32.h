@@ -19,6 +19,8 @@
 #include <cstdint>
 #include <cstring>
 
+#include <math.h>
+
 #if defined(__CUDACC__)
 #define DF_HD __host__ __device__ __forceinline__
 #else

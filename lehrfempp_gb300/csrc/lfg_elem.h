@@ -91,6 +91,98 @@ DF_HD void TriaUniformF64(const double (&jac)[4], double alpha, double gamma, co
   }
 }
 
+// ------------------------------------------- point-varying coefficients (df32)
+
+// Entries contracted together (a divisor of E), as for the quadrilaterals.
+template <int E>
+constexpr int ContractGroupT() {
+  return E % 5 == 0 ? 5 : (E % 4 == 0 ? 4 : (E % 3 == 0 ? 3 : 1));
+}
+
+// sin(pi u) and cos(pi u) of a df32 argument, |u| < 2^22.  Periodicity:
+// u = n + r with n the nearest integer to u.h (exact: r = (u.h - n) + u.l),
+// sin(pi u) = (-1)^n sin(pi r), cos(pi u) = (-1)^n cos(pi r), |r| <= 1/2 + eps.
+// Then the Taylor series sin(pi r) = r sum_k S_k r^2k (k < 11) and
+// cos(pi r) = sum_k C_k r^2k (k < 12), S_k = (-1)^k pi^(2k+1) / (2k+1)!,
+// C_k = (-1)^k pi^(2k) / (2k)!, in Horner form in r^2 (truncation below
+// 3e-16 for |pi r| <= pi/2).  Coefficient pairs come from the host.
+DF_HD void SinCosPiDF(f2 u, const f2* S /* [11] */, const f2* C /* [12] */, f2& sn, f2& cs) {
+  using namespace df;
+  const float n = rintf(u.h);  // round to nearest (even): exact integer
+  const f2 t = TwoSum(u.h, -n);
+  const f2 r = Add(t, Make(u.l));
+  const f2 r2 = Mul(r, r);
+  f2 ps = S[10];
+  DF_UNROLL
+  for (int k = 9; k >= 0; --k) ps = MulAdd(ps, r2, S[k]);
+  f2 pc = C[11];
+  DF_UNROLL
+  for (int k = 10; k >= 0; --k) pc = MulAdd(pc, r2, C[k]);
+  sn = Mul(ps, r);
+  cs = pc;
+  const long ni = static_cast<long>(n);
+  if (ni & 1) {
+    sn = Neg(sn);
+    cs = Neg(cs);
+  }
+}
+
+// Analytic coefficient families at a df32 point (see lfg.h LFG_FN_*):
+// POLY sum p[4i+j] x^i y^j (Horner), SINSIN / SINCOS p0 + p1 sin(p2 pi x)
+// {sin, cos}(p3 pi y).
+struct AnalyticDF {
+  int func = 0;
+  f2 p[16];
+};
+
+DF_HD f2 EvalAnalyticDF(const AnalyticDF& f, f2 x, f2 y, const f2* S, const f2* C) {
+  using namespace df;
+  if (f.func == 1) {  // LFG_FN_POLY
+    f2 acc = Make(0.0f);
+    DF_UNROLL
+    for (int i = 3; i >= 0; --i) {
+      f2 py = f.p[4 * i + 3];
+      DF_UNROLL
+      for (int j = 2; j >= 0; --j) py = MulAdd(py, y, f.p[4 * i + j]);
+      acc = MulAdd(acc, x, py);
+    }
+    return acc;
+  }
+  f2 sx, cx, sy, cy;
+  SinCosPiDF(Mul(f.p[2], x), S, C, sx, cx);
+  SinCosPiDF(Mul(f.p[3], y), S, C, sy, cy);
+  return MulAdd(f.p[1], Mul(sx, f.func == 2 ? sy : cy), f.p[0]);
+}
+
+// Contraction of an affine triangle with point coefficients c[k] = {c00, c01,
+// c11} (c = w_k alpha_k |det J| J^-1 J^-T) over the per-point tables
+// T[k][e][0..2], plus an optional cell-constant mass term mm * R[e][3].
+template <int E, int NQ>
+DF_HD void TriaVaryContractDF(const f2 (*c)[3], const f2* T /* [NQ][E][4] */, f2 mm, bool mass,
+                              const f2* R /* [E][4] */, double* out) {
+  using namespace df;
+  constexpr int G = ContractGroupT<E>();
+  DF_NOUNROLL
+  for (int e0 = 0; e0 < E; e0 += G) {
+    Acc acc[G];
+    DF_UNROLL
+    for (int k = 0; k < NQ; ++k) {
+      const f2* te = T + (static_cast<long>(k) * E + e0) * 4;
+      DF_UNROLL
+      for (int ab = 0; ab < 3; ++ab) {
+        DF_UNROLL
+        for (int g = 0; g < G; ++g) acc[g].AddProd(c[k][ab], te[g * 4 + ab]);
+      }
+    }
+    if (mass) {
+      DF_UNROLL
+      for (int g = 0; g < G; ++g) acc[g].AddProd(mm, R[(e0 + g) * 4 + 3]);
+    }
+    DF_UNROLL
+    for (int g = 0; g < G; ++g) out[e0 + g] = ToDouble(acc[g].Value());
+  }
+}
+
 // -------------------------------------------------------------- quadrilaterals
 
 // Per-point coefficients c[k] = {c00, c01, c11, m} of a bilinear quadrilateral

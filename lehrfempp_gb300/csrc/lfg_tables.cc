@@ -249,9 +249,12 @@ bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& o
   L.off_R = 0;
   L.off_L = L.off_R + L.E * 4;
   L.off_T = L.off_L + L.n;
-  L.off_W = L.off_T + (quad ? L.nq * L.E * 4 : 0);
+  L.off_W = L.off_T + L.nq * L.E * 4;
   L.off_t = L.off_W + L.nq;
-  L.off_SF = L.off_t + L.m;
+  L.off_X = L.off_t + L.m;
+  L.off_O1 = L.off_X + 2 * L.nq;
+  L.off_SC = L.off_O1 + 4 * L.nq;
+  L.off_SF = L.off_SC + 23;
   L.total = L.off_SF;
   std::vector<long double> sf;
   if (quad && degree >= 2 && TensorBasis(degree, r, L.m, L.loc, sf)) {
@@ -261,9 +264,25 @@ bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& o
   out.assign(2 * static_cast<size_t>(L.total), 0.0f);
   for (size_t q = 0; q < (L.n1 ? sf.size() : 0); ++q) Split(sf[q], &out[2 * (L.off_SF + q)]);
   std::vector<long double> R(L.E * 4, 0.0L), Ls(L.n, 0.0L);
-  double phi[16], dphi[16][2];
+  double phi[16], dphi[16][2], p1[16], d1[16][2];
+  // sin(pi r) = sum_k (-1)^k pi^(2k+1) r^(2k+1) / (2k+1)!, cos likewise
+  const long double pi = 3.141592653589793238462643383279502884L;
+  long double term = pi;  // pi^(2k+1) / (2k+1)!
+  for (int k = 0; k < 11; ++k) {
+    Split((k & 1) ? -term : term, &out[2 * (L.off_SC + k)]);
+    term *= pi * pi / ((2.0L * k + 2.0L) * (2.0L * k + 3.0L));
+  }
+  term = 1.0L;  // pi^(2k) / (2k)!
+  for (int k = 0; k < 12; ++k) {
+    Split((k & 1) ? -term : term, &out[2 * (L.off_SC + 11 + k)]);
+    term *= pi * pi / ((2.0L * k + 1.0L) * (2.0L * k + 2.0L));
+  }
   for (int k = 0; k < r.n; ++k) {
     Shape(quad, degree, r.x[k], r.y[k], phi, dphi);
+    Shape(quad, 1, r.x[k], r.y[k], p1, d1);
+    Split(r.x[k], &out[2 * (L.off_X + 2 * k)]);
+    Split(r.y[k], &out[2 * (L.off_X + 2 * k + 1)]);
+    for (int v = 0; v < (quad ? 4 : 3); ++v) Split(p1[v], &out[2 * (L.off_O1 + 4 * k + v)]);
     const long double w = r.w[k];
     int e = 0;
     for (int i = 0; i < L.n; ++i)
@@ -273,11 +292,11 @@ bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& o
                                   static_cast<long double>(phi[i]) * phi[j]};
         for (int q = 0; q < 4; ++q) {
           R[4 * e + q] += w * t[q];
-          if (quad) Split(t[q], &out[2 * (L.off_T + (k * L.E + e) * 4 + q)]);
+          Split(t[q], &out[2 * (L.off_T + (k * L.E + e) * 4 + q)]);
         }
       }
     for (int i = 0; i < L.n; ++i) Ls[i] += w * phi[i];
-    if (quad) Split(w, &out[2 * (L.off_W + k)]);
+    Split(w, &out[2 * (L.off_W + k)]);
   }
   for (int q = 0; q < L.E * 4; ++q) Split(R[q], &out[2 * (L.off_R + q)]);
   for (int i = 0; i < L.n; ++i) Split(Ls[i], &out[2 * (L.off_L + i)]);

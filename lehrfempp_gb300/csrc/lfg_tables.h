@@ -21,8 +21,10 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
 // df32 tables (pairs of floats; offsets in pairs):
 //   R[E][4]    folded sums sum_k w_k {g_i0 g_j0, g_i0 g_j1 + g_i1 g_j0, g_i1 g_j1, phi_i phi_j}
 //   L[n]       folded load sums sum_k w_k phi_i
-//   T[nq][E][4] the same terms per point (no weight)      (quads)
-//   W[nq]      point weights,  t[m] 1D abscissae            (quads)
+//   T[nq][E][4] the same terms per point (no weight)
+//   W[nq]      point weights,  t[m] 1D abscissae            (t: quads)
+//   X[nq][2]   reference point coordinates, O1[nq][4] O1 shape values there
+//   SC[23]     Taylor coefficients of sin(pi r) (11) and cos(pi r) (12)
 //   SF[3][n1][n1][m]  1D products {l'_a l'_b, l_a l_b, l'_a l_b} at the m
 //              Gauss abscissae, for quads whose basis is the tensor product
 //              phi_{loc[a n1 + b]}(x, y) = l_a(x) l_b(y) of a 1D basis of
@@ -30,6 +32,7 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
 struct DfLayout {
   int n = 0, E = 0, nq = 0, m = 0;
   int off_R = 0, off_L = 0, off_T = 0, off_W = 0, off_t = 0, total = 0;
+  int off_X = 0, off_O1 = 0, off_SC = 0;
   int n1 = 0, off_SF = 0;
   int loc[16] = {};
 };
