@@ -160,9 +160,19 @@ def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
                       "not timed" % (ncell, m.num_cells, ntrip, setup)}
 
 
-def solve_leg(L, W, ctx, n):
-    """DOFs/s of assemble + fix + COO->CSR + PCG on the config-2 generator at
-    size n, FP64 PCG vs mixed precision, error vs the FP64 PCG at 1e-12."""
+RTOL_LADDER = (1e-6, 1e-7, 1e-8, 1e-9, 1e-10)
+
+
+def solve_leg(L, W, ctx, n, cpu_check=False):
+    """Config 2's solve at n x n (hybrid O2): DOFs/s of assemble + fix +
+    COO->CSR + PCG, FP64 vs mixed precision.
+    - "to_1e-8_err": the metric's definition -- the largest residual target of
+      RTOL_LADDER whose solution is within 1e-8 (relative 2-norm) of the
+      reference solution (FP64 PCG run to its rounding floor), timed end to end;
+    - "rtol_1e-10": the configuration's residual target 1e-10;
+    - cpu_check: the oracle's SuperLU (the reference drivers' direct FP64
+      solve) on the 256 x 256 subcase, its DOFs/s on one core, and the GPU
+      mixed solution's error against it."""
     wl = W.config2(n)
     keep = []
     mesh = W.build_mesh(ctx, wl["mesh"])
@@ -171,38 +181,78 @@ def solve_leg(L, W, ctx, n):
     lprov = L.load_provider(W.to_coeff(ctx, wl["f"], keep))
     flags = space.boundary_dof_flags()
     zeros = ctx.zeros(space.num_dofs)
-    out = {"workload": "hybrid %dx%d O2 (%d dofs)" % (n, n, space.num_dofs)}
-    xs = {}
-    for name, prec in (("fp64", L.SOLVE_FP64), ("mixed", L.SOLVE_MIXED)):
+    nd = space.num_dofs
+
+    def run(prec, rtol):
         ctx.synchronize()
         t0 = time.perf_counter()
-        coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, space.num_triplets + space.num_dofs)
+        coo = L.COOMatrix(ctx, nd, nd, space.num_triplets + nd)
         L.assemble_matrix_rd(space, prov, coo)
-        b = ctx.zeros(space.num_dofs)
+        b = ctx.zeros(nd)
         L.assemble_vector_load(space, lprov, b)
         coo.fix_flagged_solution_components(flags, zeros, b)
         A = coo.make_sparse()
-        x = ctx.zeros(space.num_dofs)
-        st = A.solve_pcg(b, x, precision=prec, rtol=1e-10, raise_on_failure=False)
+        del coo
+        x = ctx.zeros(nd)
+        st = A.solve_pcg(b, x, precision=prec, rtol=rtol, raise_on_failure=False)
         ctx.synchronize()
-        dt = time.perf_counter() - t0
-        xs[name] = x.download()
-        out[name] = {"dofs_per_s": space.num_dofs / dt, "seconds": dt, "iterations": st["iterations"],
-                     "refinements": st["refinements"], "rel_residual": st["rel_residual"],
-                     "converged": st["converged"]}
-        del coo, A
-    ref = ctx.zeros(space.num_dofs)
-    coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, space.num_triplets + space.num_dofs)
-    L.assemble_matrix_rd(space, prov, coo)
-    b = ctx.zeros(space.num_dofs)
-    L.assemble_vector_load(space, lprov, b)
-    coo.fix_flagged_solution_components(flags, zeros, b)
-    coo.make_sparse().solve_pcg(b, ref, precision=L.SOLVE_FP64, rtol=1e-13, raise_on_failure=False)
-    r = ref.download()
-    for name in xs:
-        out[name]["rel_err_vs_fp64_1e-13"] = float(np.linalg.norm(xs[name] - r) / np.linalg.norm(r))
-    out["mixed_vs_fp64"] = out["mixed"]["dofs_per_s"] / out["fp64"]["dofs_per_s"]
+        return x.download(), st, time.perf_counter() - t0
+
+    r, _, _ = run(L.SOLVE_FP64, 1e-13)  # reference: FP64 PCG to its rounding floor
+    rn = np.linalg.norm(r)
+    out = {"workload": "hybrid %dx%d O2 (%d dofs)" % (n, n, nd)}
+    for name, prec in (("fp64", L.SOLVE_FP64), ("mixed", L.SOLVE_MIXED)):
+        rec = {}
+        for rtol in RTOL_LADDER:
+            x, st, dt = run(prec, rtol)
+            err = float(np.linalg.norm(x - r) / rn)
+            if err <= 1e-8:
+                rec["to_1e-8_err"] = {"dofs_per_s": nd / dt, "seconds": dt, "rtol": rtol, "rel_err": err,
+                                      "iterations": st["iterations"], "refinements": st["refinements"]}
+                break
+        x, st, dt = run(prec, 1e-10)
+        rec["rtol_1e-10"] = {"dofs_per_s": nd / dt, "seconds": dt, "iterations": st["iterations"],
+                             "refinements": st["refinements"], "rel_residual": st["rel_residual"],
+                             "converged": st["converged"], "rel_err_vs_fp64_floor": float(np.linalg.norm(x - r) / rn)}
+        out[name] = rec
+    if "to_1e-8_err" in out["fp64"] and "to_1e-8_err" in out["mixed"]:
+        out["mixed_vs_fp64_at_1e-8_err"] = out["mixed"]["to_1e-8_err"]["dofs_per_s"] / \
+            out["fp64"]["to_1e-8_err"]["dofs_per_s"]
+    if cpu_check:
+        out["cpu_baseline"] = solve_cpu_check(L, W, ctx, 256)
     return out
+
+
+def solve_cpu_check(L, W, ctx, n):
+    """Oracle (reference restatement) assembly + fix + SuperLU on the config-2
+    subcase n x n on one core, and the GPU mixed solve's error against it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import scipy.sparse.linalg as spla
+    import oracle as O
+    from parity import oracle_coeff
+    wl = W.config2(n)
+    t0 = time.perf_counter()
+    osp = O.Space(O.Mesh(wl["mesh"]["xy"], wl["mesh"]["cells"]), 2)
+    A = O.assemble_rd(osp, oracle_coeff(wl["alpha"]), oracle_coeff(wl["gamma"]))
+    b = O.assemble_load(osp, oracle_coeff(wl["f"]))
+    A.fix_flagged(osp.boundary_dof_flags(), np.zeros(osp.num_dofs), b)
+    xo = spla.splu(A.to_scipy().tocsc()).solve(b)
+    cpu_s = time.perf_counter() - t0
+    keep = []
+    mesh = W.build_mesh(ctx, wl["mesh"])
+    sp = L.Space.lagrange(mesh, 2)
+    coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets + sp.num_dofs)
+    L.assemble_matrix_rd(sp, L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep)), coo)
+    bg = ctx.zeros(sp.num_dofs)
+    L.assemble_vector_load(sp, L.load_provider(W.to_coeff(ctx, wl["f"], keep)), bg)
+    coo.fix_flagged_solution_components(sp.boundary_dof_flags(), ctx.zeros(sp.num_dofs), bg)
+    x = ctx.zeros(sp.num_dofs)
+    coo.make_sparse().solve_pcg(bg, x, precision=L.SOLVE_MIXED, rtol=1e-10, raise_on_failure=False)
+    err = float(np.linalg.norm(x.download() - xo) / np.linalg.norm(xo))
+    return {"value": osp.num_dofs / cpu_s, "unit": "DOFs/s", "cores": 1, "kind": "port",
+            "sample": "oracle assembly + fix + SuperLU on hybrid %dx%d O2 (%d dofs)" % (n, n, osp.num_dofs),
+            "gpu_mixed_rtol_1e-10_rel_err_vs_sparselu": err}
 
 
 def high_order_leg(L, W, ctx, n, steps=5):
@@ -246,11 +296,12 @@ def high_order_leg(L, W, ctx, n, steps=5):
 
 def batch_leg(L, W, ctx, count):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
-    one persistent assembly launch + load + fix + COO->CSR + batched PCG to
-    relative residual 1e-10 per mesh.  DOFs/s of the batched mixed and FP64
-    solves, of the plain path (one mesh at a time: assemble, fix, CSR, FP64
-    PCG) on every 8th mesh, and the per-mesh error against a batched FP64
-    solve to 1e-13."""
+    one persistent assembly launch + load + fix + COO->CSR + batched PCG.
+    DOFs/s of the batched mixed and FP64 solves solved to 1e-8 error on every
+    mesh (largest residual target that meets it) and to relative residual
+    1e-10, of the plain path (one mesh at a time: assemble, fix, CSR, FP64
+    PCG at the FP64 target) on every 8th mesh; errors against a batched FP64
+    solve run to its rounding floor."""
     wl = W.config4(count)
     t0 = time.perf_counter()
     meshes = [L.Mesh.tp_triag(ctx, int(n), int(n)) for n in wl["ns"]]
@@ -289,19 +340,33 @@ def batch_leg(L, W, ctx, count):
            "setup_s": setup_s}
     th, ct, ms = batch.tuning()
     out["autotuner"] = {"threads_per_cta": th, "ctas_per_sm": ct, "assembly_ms": ms}
-    xs = {}
-    for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
-        x, st, dt, launches = run(prec, 1e-10)
-        xs[name] = x.download()
-        its = [blk["iterations"] for blk in st["blocks"]]
-        out[name] = {"dofs_per_s": nd / dt, "seconds": dt, "gpu_launches": launches, "max_iterations": max(its),
-                     "all_converged": bool(st["converged"])}
-    xr, st, _, _ = run(L.SOLVE_FP64, 1e-13)
+    xr, st, _, _ = run(L.SOLVE_FP64, 1e-13)  # reference: batched FP64 PCG to its rounding floor
     r = xr.download()
-    for name in xs:
-        errs = [float(np.linalg.norm(xs[name][dof[k]:dof[k + 1]] - r[dof[k]:dof[k + 1]]) /
+
+    def mesh_errs(x):
+        return [float(np.linalg.norm(x[dof[k]:dof[k + 1]] - r[dof[k]:dof[k + 1]]) /
                       np.linalg.norm(r[dof[k]:dof[k + 1]])) for k in range(count)]
-        out[name]["per_mesh_rel_err_vs_fp64_1e-13"] = {"max": max(errs), "median": statistics.median(errs)}
+
+    plain_rtol = 1e-10
+    for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
+        rec = {}
+        for rtol in (1e-6, 1e-7, 1e-8):  # DOFs/s solved to 1e-8 error (every mesh)
+            x, st, dt, launches = run(prec, rtol)
+            errs = mesh_errs(x.download())
+            if max(errs) <= 1e-8:
+                rec["to_1e-8_err"] = {"dofs_per_s": nd / dt, "seconds": dt, "rtol": rtol, "max_mesh_rel_err": max(errs),
+                                      "gpu_launches": launches,
+                                      "max_iterations": max(blk["iterations"] for blk in st["blocks"])}
+                if name == "fp64":
+                    plain_rtol = rtol
+                break
+        x, st, dt, launches = run(prec, 1e-10)
+        errs = mesh_errs(x.download())
+        rec["rtol_1e-10"] = {"dofs_per_s": nd / dt, "seconds": dt, "gpu_launches": launches,
+                             "max_iterations": max(blk["iterations"] for blk in st["blocks"]),
+                             "all_converged": bool(st["converged"]),
+                             "per_mesh_rel_err_vs_fp64_floor": {"max": max(errs), "median": statistics.median(errs)}}
+        out[name] = rec
     # the plain FP64 path, one mesh after another, on every 8th mesh
     sample = list(range(0, count, 8))
     sd = 0
@@ -318,13 +383,15 @@ def batch_leg(L, W, ctx, count):
         coo.fix_flagged_solution_components(sp.boundary_dof_flags(), ctx.zeros(sp.num_dofs), b)
         A = coo.make_sparse()
         x = ctx.zeros(sp.num_dofs)
-        A.solve_pcg(b, x, precision=L.SOLVE_FP64, rtol=1e-10, raise_on_failure=False)
+        A.solve_pcg(b, x, precision=L.SOLVE_FP64, rtol=plain_rtol, raise_on_failure=False)
         sd += sp.num_dofs
     ctx.synchronize()
     dt = time.perf_counter() - t0
-    out["plain_fp64"] = {"dofs_per_s": sd / dt, "seconds": dt, "sample": "every 8th mesh (%d meshes, %d dofs)" %
-                                                                         (len(sample), sd)}
-    out["mixed_batched_vs_plain_fp64"] = out["mixed"]["dofs_per_s"] / out["plain_fp64"]["dofs_per_s"]
+    out["plain_fp64"] = {"dofs_per_s": sd / dt, "seconds": dt, "rtol": plain_rtol,
+                          "sample": "every 8th mesh (%d meshes, %d dofs), one mesh at a time" % (len(sample), sd)}
+    best = max((out[k]["to_1e-8_err"]["dofs_per_s"] for k in ("mixed", "fp64") if "to_1e-8_err" in out[k]), default=None)
+    if best:
+        out["best_batched_vs_plain_fp64_at_1e-8_err"] = best / out["plain_fp64"]["dofs_per_s"]
     return out
 
 
@@ -515,7 +582,8 @@ def run_ours(args):
             return {"error": "%s: %s" % (type(e).__name__, e)}
 
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
-    solve = leg(solve_leg, L, W, ctx, args.solve_size) if args.solve_size > 0 else None
+    solve = leg(solve_leg, L, W, ctx, args.solve_size,
+                cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
     batch = leg(batch_leg, L, W, ctx, args.batch_count) if args.batch_count > 0 else None
     gradient = leg(gradient_leg, L, W, ctx, args.grad_size, steps=3,
                    cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.grad_size > 0 else None
