@@ -242,19 +242,16 @@ struct Sell {
 };
 
 // q = A p on the chunk's rows (SELL-32; thread per row), <p, q> per mesh
-// -> alpha_b.  FUSED (FP32): p_new = z + beta_b p_old formed on the fly
-// (neighbours recomputed with the owner's fma), else p_old is the direction.
-template <class T, bool FUSED>
+// -> alpha_b.
+template <class T>
 __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __restrict__ val,
-                                                   const T* __restrict__ z, const T* __restrict__ p_old,
-                                                   T* __restrict__ p_new, T* __restrict__ q,
+                                                   const T* __restrict__ p, T* __restrict__ q,
                                                    const int32_t* __restrict__ frozen, int cur,
                                                    double* __restrict__ part, MeshScal* __restrict__ ms) {
   __shared__ double red[32];
   for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
     const int b = C.mesh[c];
     if (frozen[b]) continue;  // uniform per block
-    const T beta = FUSED ? static_cast<T>(ms[b].beta) : T(0);
     BDot<T> acc;
     for (int64_t r = C.start[c] + threadIdx.x; r < C.start[c + 1]; r += blockDim.x) {
       const int64_t sl = r >> 5, lane = r & 31;
@@ -264,15 +261,9 @@ __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __
       const T* vp = val + b0 + lane;
       T sum = T(0);
 #pragma unroll 4
-      for (int k = 0; k < w; ++k) {
-        const int cc = cp[k * 32];
-        const T pc = FUSED ? fma(beta, p_old[cc], z[cc]) : p_old[cc];
-        sum = fma(vp[k * 32], pc, sum);
-      }
-      const T pi = FUSED ? fma(beta, p_old[r], z[r]) : p_old[r];
-      if (FUSED) p_new[r] = pi;
+      for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]], sum);
       q[r] = sum;
-      acc.add(pi, sum);
+      acc.add(p[r], sum);
     }
     const double tot = BlockReduce(acc.get(), red);
     if (threadIdx.x == 0) part[c] = tot;
@@ -333,7 +324,7 @@ __global__ void __launch_bounds__(kPB) BUpdateKernel(Chunks C, const T* __restri
   }
 }
 
-// p = z + beta_b p (FP64 path: one FMA per row instead of one per entry).
+// p = z + beta_b p.
 template <class T>
 __global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const T* __restrict__ z, T* __restrict__ p,
                                                         const int32_t* __restrict__ frozen,
@@ -347,7 +338,7 @@ __global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const T* __res
 }
 
 // z = D^-1 r, p = z; rz[0], rr per mesh; beta = 0 (so the first direction
-// update, fused or not, gives p = z).
+// update keeps p = z).
 template <class T>
 __global__ void __launch_bounds__(kPB) BStartKernel(Chunks C, const T* __restrict__ dinv, const T* __restrict__ r,
                                                     T* __restrict__ z, T* __restrict__ p,
@@ -462,7 +453,7 @@ void MeshSums(lfg_batch* B, const double* dev_part, std::vector<double>& out) {
 
 template <class T>
 struct BState {
-  DevBuf r, z, p[2], q, part, ms;
+  DevBuf r, z, p, q, part, ms;
 };
 
 template <class T>
@@ -470,8 +461,7 @@ void BAlloc(lfg_ctx* ctx, int64_t n, int64_t nch, int nb, BState<T>& S) {
   cudaStream_t s = ctx->stream;
   S.r.alloc(n * sizeof(T), s);
   S.z.alloc(n * sizeof(T), s);
-  S.p[0].alloc(n * sizeof(T), s);
-  S.p[1].alloc(n * sizeof(T), s);
+  S.p.alloc(n * sizeof(T), s);
   S.q.alloc(n * sizeof(T), s);
   S.part.alloc(2 * nch * sizeof(double), s);
   S.ms.alloc(nb * sizeof(MeshScal), s);
@@ -501,7 +491,7 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BStat
   MeshScal* ms = S.ms.template as<MeshScal>();
   double* part = S.part.template as<double>();
   LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-  BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(), S.p[0].template as<T>(),
+  BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(), S.p.template as<T>(),
                                       frozen_d.as<int32_t>(), part, ms);
   LFG_LAUNCHED(ctx);
   std::vector<double> rr;
@@ -510,20 +500,16 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BStat
   for (int b = 0; b < B->nb; ++b)
     if (!(rr[b] > target_rr[b])) frozen_h[b] = 1;
   LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-  constexpr bool kFused = sizeof(T) == 4;
   const int body = std::max(2, check_every + (check_every & 1));
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < body; ++k) {
     const int cur = k & 1;
-    T* p_old = S.p[kFused ? cur : 0].template as<T>();
-    T* p_new = S.p[kFused ? (cur ^ 1) : 0].template as<T>();
-    if (!kFused)
-      BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p_old, frozen_d.as<int32_t>(), ms);
-    BSpmvKernel<T, kFused><<<grid, kPB, 0, s>>>(C, M, sval, S.z.template as<T>(), p_old, p_new, S.q.template as<T>(),
-                                                frozen_d.as<int32_t>(), cur, part, ms);
-    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p_new, S.q.template as<T>(), x, S.r.template as<T>(),
+    T* p = S.p.template as<T>();
+    BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p, frozen_d.as<int32_t>(), ms);
+    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, p, S.q.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
+    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                          S.z.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
   }
   LFG_CUDA(cudaStreamEndCapture(s, &graph));
@@ -535,7 +521,7 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BStat
       for (int b = 0; b < B->nb; ++b) active += !frozen_h[b];
       if (!active) break;
       LFG_CUDA(cudaGraphLaunch(exec, s));
-      CountLaunch(ctx, (kFused ? 2 : 3) * body);
+      CountLaunch(ctx, 3 * body);
       it += body;
       MeshRR(B, S.ms, rr);
       bool changed = false;

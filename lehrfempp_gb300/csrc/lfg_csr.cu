@@ -8,19 +8,19 @@
 // order) and each run is summed left to right, which reproduces those sums
 // bit for bit.
 //
-// The solver keeps every scalar on the device.  A PCG iteration is two
-// kernels: (1) the search-direction update p = z + beta p_old fused into the
-// SpMV q = A p over a SELL-32 copy of the matrix (one thread per row, the
-// row's entries loaded column-major across the warp, so every load of a
-// slice is coalesced and a thread's loads are independent), with <p, q>;
-// (2) x += alpha p, r -= alpha q, z = D^-1 r with <r, z> and <r, r>.  Each
-// kernel's block partials are summed by the last block to finish (counter +
-// fence), in block order, so the scalars alpha and beta are deterministic and
-// computed once; the next kernel reads them from device memory.  The neighbour
-// values p_c = z_c + beta p_old_c are recomputed inside the SpMV with the same
-// fma as the row owner, so p needs two buffers (read old, write new).  The
-// iteration body is captured in a CUDA graph replayed `check_every`
-// iterations at a time; the host reads one residual norm per replay.
+// The solver keeps every scalar on the device.  A PCG iteration is three
+// kernels: (1) the search direction p = z + beta p; (2) q = A p over a SELL-32
+// copy of the matrix (one thread per row, the row's entries stored
+// column-major across the warp, so every load of a slice is coalesced and a
+// thread's loads are independent) with <p, q> -> alpha; (3) x += alpha p,
+// r -= alpha q, z = D^-1 r with <r, z> -> beta (and <r, r> on the last
+// iteration of a graph replay).  Each kernel's block partials are summed by
+// the last block to finish (counter + fence), in block order, so alpha and
+// beta are deterministic and computed once; the next kernel reads them from
+// device memory.  The iteration body is captured in a CUDA graph replayed
+// `check_every` iterations at a time; the host reads one residual norm per
+// replay.  (Forming p inside the SpMV instead -- recomputing neighbour values
+// -- doubles the gathers and measured slower in FP32 and FP64.)
 #include <algorithm>
 #include <cstddef>
 #include <cmath>
@@ -223,23 +223,14 @@ struct DotAcc<float> {
   __device__ double get() const { return static_cast<double>(v); }
 };
 
-// q = A p (SELL-32) and alpha = rz[cur] / <p, q>.  FUSED: p is formed on the
-// fly as p_new = z + beta p_old (neighbour values recomputed with the owner's
-// fma; p_new written by the owner) -- used for FP32, where the extra FMAs are
-// cheap.  Otherwise p_old is the finished direction and p_new is unused.
-template <class T, bool FUSED>
-__global__ void __launch_bounds__(kPcgBlock) PcgSpmvDirKernel(int64_t rows, int64_t nslices,
-                                                              const int64_t* __restrict__ sptr,
-                                                              const int32_t* __restrict__ scol,
-                                                              const T* __restrict__ sval, const T* __restrict__ z,
-                                                              const T* __restrict__ p_old, T* __restrict__ p_new,
-                                                              T* __restrict__ q, int cur, double* __restrict__ part,
-                                                              PcgScalars* __restrict__ sc) {
+// q = A p (SELL-32) and alpha = rz[cur] / <p, q>.
+template <class T>
+__global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t nslices,
+                                                           const int64_t* __restrict__ sptr,
+                                                           const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                           const T* __restrict__ p, T* __restrict__ q, int cur,
+                                                           double* __restrict__ part, PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
-  __shared__ T sbeta;
-  if (threadIdx.x == 0) sbeta = FUSED ? static_cast<T>(sc->beta) : T(0);
-  __syncthreads();
-  const T beta = sbeta;
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -253,15 +244,9 @@ __global__ void __launch_bounds__(kPcgBlock) PcgSpmvDirKernel(int64_t rows, int6
       const T* vp = sval + b0 + lane;
       T sum = T(0);
 #pragma unroll 4
-      for (int k = 0; k < w; ++k) {
-        const int c = cp[k * kSlice];
-        const T pc = FUSED ? fma(beta, p_old[c], z[c]) : p_old[c];
-        sum = fma(vp[k * kSlice], pc, sum);
-      }
-      const T pi = FUSED ? fma(beta, p_old[r], z[r]) : p_old[r];
-      if (FUSED) p_new[r] = pi;
+      for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[cp[k * kSlice]], sum);
       q[r] = sum;
-      acc.add(pi, sum);
+      acc.add(p[r], sum);
     }
   }
   const double tot = BlockSum(acc.get(), red);
@@ -336,8 +321,7 @@ __global__ void __launch_bounds__(kPcgBlock, 4) PcgUpdateKernel(int64_t rows, co
   }
 }
 
-// p = z + beta p (the FP64 path's separate direction update: one FP64 FMA
-// per row instead of one per matrix entry in the fused SpMV).
+// p = z + beta p.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgDirectionKernel(int64_t rows, const T* __restrict__ z,
                                                                 T* __restrict__ p, const PcgScalars* __restrict__ sc) {
@@ -350,7 +334,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgDirectionKernel(int64_t rows, co
     p[i] = fma(beta, p[i], z[i]);
 }
 
-// z = D^-1 r, p_old = z (so the first direction update, with beta = 0, gives
+// z = D^-1 r, p = z (so the first direction update, with beta = 0, keeps
 // p = z), rz[0] = <r, z>, rr = <r, r>.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgStartKernel(int64_t rows, const T* __restrict__ dinv,
@@ -539,7 +523,7 @@ namespace {
 // res holds the block partials of the FP64 residual kernel.
 template <class T>
 struct PcgState {
-  DevBuf r, z, p[2], q;
+  DevBuf r, z, p, q;
   DevBuf part, res, scal;
   int nb = 0;
 };
@@ -550,8 +534,7 @@ void AllocState(lfg_ctx* ctx, int64_t n, PcgState<T>& S) {
   S.nb = std::max(1, std::min<int>(ctx->num_sms * 8, static_cast<int>((n + kPcgBlock - 1) / kPcgBlock)));
   S.r.alloc(n * sizeof(T), s);
   S.z.alloc(n * sizeof(T), s);
-  S.p[0].alloc(n * sizeof(T), s);
-  S.p[1].alloc(n * sizeof(T), s);
+  S.p.alloc(n * sizeof(T), s);
   S.q.alloc(n * sizeof(T), s);
   S.part.alloc(2 * static_cast<size_t>(ctx->num_sms) * 8 * sizeof(double), s);  // >= 2 * any grid used
   S.res.alloc(S.nb * sizeof(double), s);
@@ -592,22 +575,17 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, i
   PcgScalars* sc = S.scal.template as<PcgScalars>();
   double* part = S.part.template as<double>();
   PcgGraph g;
-  constexpr bool kFused = sizeof(T) == 4;
-  g.launches = (kFused ? 2 : 3) * body;
+  g.launches = 3 * body;
   cudaGraph_t graph = nullptr;
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < body; ++k) {
     const int cur = k & 1;
-    T* p_old = S.p[kFused ? cur : 0].template as<T>();
-    T* p_new = S.p[kFused ? (cur ^ 1) : 0].template as<T>();
-    if (!kFused) {
-      PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p_old, sc);
-    }
-    PcgSpmvDirKernel<T, kFused><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
-                                                                  A->sell_col.as<int32_t>(), sval,
-                                                                  S.z.template as<T>(), p_old, p_new,
-                                                                  S.q.template as<T>(), cur, part, sc);
-    PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p_new, S.q.template as<T>(), x, S.r.template as<T>(),
+    T* p = S.p.template as<T>();
+    PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p, sc);
+    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
+                                                       A->sell_col.as<int32_t>(), sval, p, S.q.template as<T>(), cur,
+                                                       part, sc);
+    PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                                            S.z.template as<T>(), cur, k == body - 1, part, sc);
   }
   cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -626,7 +604,7 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   PcgStartKernel<T><<<S.nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
-                                               S.p[0].template as<T>(), S.part.template as<double>(),
+                                               S.p.template as<T>(), S.part.template as<double>(),
                                                S.scal.template as<PcgScalars>());
   LFG_LAUNCHED(ctx);
   double rr = ReadRR(ctx, S.scal);
