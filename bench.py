@@ -51,7 +51,8 @@ def parse():
 
 
 def dist_env():
-    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+    from lehrfempp_gb300.replicas import dist_env as env
+    return env()
 
 
 class ClockSampler:
@@ -480,12 +481,10 @@ def run_ours(args):
     rank, world, local = dist_env()
     import lehrfempp_gb300 as L
     from lehrfempp_gb300 import workloads as W
+    from lehrfempp_gb300.replicas import Replicas
     L.load()
     ctx = L.Context(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    reps = Replicas(world)
     wl = W.config2(args.size)
     keep = []
     mesh = W.build_mesh(ctx, wl["mesh"])
@@ -503,8 +502,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         step()
     ctx.synchronize()
-    if dist:
-        dist.barrier()
+    reps.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     l0 = ctx.launches()
@@ -515,13 +513,8 @@ def run_ours(args):
     launches = ctx.launches() - l0
     clk = clocks.stop()
     ms = ms_total / args.steps
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    value = world * ntrip / (ms * 1e-3)
+    value, ms = reps.throughput(ntrip, ms)
+    reps.barrier()
 
     # per-kernel attribution (CUDA events around each launch, separate pass)
     ctx.profile(True)
@@ -621,8 +614,7 @@ def run_ours(args):
         }
         print(json.dumps(line))
     ctx.close()
-    if dist:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def run_reference(args):
