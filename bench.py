@@ -295,6 +295,39 @@ def high_order_leg(L, W, ctx, n, steps=5):
             "load_vector_ms": vms}
 
 
+def edge_leg(L, W, ctx, mesh, space, steps=5):
+    """Boundary-edge providers on the headline mesh (O2): edge mass on every
+    edge (triplets/s of codim-1 AssembleMatrixLocally) and on the boundary
+    edges, edge load on the boundary edges.  FP64, one thread per edge."""
+    ne = mesh.num_edges
+    n = space.degree + 1
+    _, ef = mesh.boundary_flags()
+    nb = int(ef.sum())
+    ef_d = ctx.to_device(ef.astype(np.uint8))
+    gam = L.coeff(L.CONSTANT, 2.0)
+    coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, ne * n * n)
+    out = {"workload": "edges of the headline mesh (%d edges, %d on the boundary), O2, gamma constant" % (ne, nb)}
+    for name, fl, count in (("all_edges", None, ne), ("boundary_edges", ef_d, nb)):
+        prov = L.edge_mass_provider(gam, fl)
+        coo.set_zero()
+        L.assemble_matrix_edge_mass(space, prov, coo)
+        ctx.timer_begin()
+        for _ in range(steps):
+            coo.set_zero()
+            L.assemble_matrix_edge_mass(space, prov, coo)
+        ms = ctx.timer_end() / steps
+        out[name] = {"edges": count, "triplets": count * n * n, "ms": ms, "triplets_per_s": count * n * n / (ms * 1e-3),
+                     "hbm_gbs": count * (n * n * 16 + 8 + 32 + 1) / (ms * 1e-3) / 1e9}
+    b = ctx.zeros(space.num_dofs)
+    lprov = L.edge_load_provider(gam, ef_d)
+    L.assemble_vector_edge_load(space, lprov, b)
+    ctx.timer_begin()
+    for _ in range(steps):
+        L.assemble_vector_edge_load(space, lprov, b)
+    out["boundary_load_ms"] = ctx.timer_end() / steps
+    return out
+
+
 def batch_leg(L, W, ctx, count):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
     one persistent assembly launch + load + fix + COO->CSR + batched PCG.
@@ -574,6 +607,7 @@ def run_ours(args):
         except Exception as e:  # a failing side leg is reported, not fatal to the headline line
             return {"error": "%s: %s" % (type(e).__name__, e)}
 
+    edges = leg(edge_leg, L, W, ctx, mesh, space)
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size,
                 cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
@@ -609,7 +643,8 @@ def run_ours(args):
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "high_order": high_order, "solve": solve, "batch": batch,
+            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "high_order": high_order, "solve": solve,
+            "batch": batch,
             "gradient": gradient,
         }
         print(json.dumps(line))

@@ -24,6 +24,9 @@
 //     (assemble/fix_dof.h:87)                        values, A, b): the selector is given as two
 //                                                    device arrays (flag, value per dof)
 //   Eigen::SparseLU / CG on makeSparse()           solve::SolvePCG (Jacobi PCG, FP64 or mixed)
+//   MassEdgeMatrixProvider, ScalarLoadEdgeVectorProvider (loc_comp_ellbvp.h:367-529,
+//     784-921) with AssembleMatrixLocally / AssembleVectorLocally(1, ...)
+//                                                  the same names; edge selector = device flags
 //   (no counterpart)                               adjoint::InverseConductivityFunction
 //
 // Errors: every failing call throws lf::gb300::Error carrying the lfg_status
@@ -282,6 +285,41 @@ class ScalarLoadElementVectorProvider {
   lfg_load_provider p_{};
 };
 
+// Boundary-edge providers (loc_comp_ellbvp.h:367-529, 784-921).  The edge
+// selector is a device flag array (nullptr: every edge); per-cell coefficient
+// data is indexed by edge.
+class MassEdgeMatrixProvider {
+ public:
+  MassEdgeMatrixProvider(std::shared_ptr<const FeSpaceLagrange> fes, MeshFunction gamma,
+                         const uint8_t* edge_flags_dev = nullptr, int qr_degree = 0)
+      : fes_(std::move(fes)) {
+    p_.gamma = gamma.c;
+    p_.edge_flags_dev = edge_flags_dev;
+    p_.qr_degree = qr_degree;
+  }
+  const lfg_edge_mass_provider* get() const { return &p_; }
+
+ private:
+  std::shared_ptr<const FeSpaceLagrange> fes_;
+  lfg_edge_mass_provider p_{};
+};
+
+class ScalarLoadEdgeVectorProvider {
+ public:
+  ScalarLoadEdgeVectorProvider(std::shared_ptr<const FeSpaceLagrange> fes, MeshFunction g,
+                               const uint8_t* edge_flags_dev = nullptr, int qr_degree = 0)
+      : fes_(std::move(fes)) {
+    p_.g = g.c;
+    p_.edge_flags_dev = edge_flags_dev;
+    p_.qr_degree = qr_degree;
+  }
+  const lfg_edge_load_provider* get() const { return &p_; }
+
+ private:
+  std::shared_ptr<const FeSpaceLagrange> fes_;
+  lfg_edge_load_provider p_{};
+};
+
 }  // namespace uscalfe
 
 namespace solve {
@@ -399,6 +437,22 @@ inline void AssembleVectorLocally(dim_t codim, const uscalfe::FeSpaceLagrange& d
                                   DeviceVector<double>& b) {
   if (codim != 0) throw Error(LFG_UNSUPPORTED, "AssembleVectorLocally: cells only");
   dofh.ctx().Check(lfg_assemble_vector_load(dofh.get(), provider.get(), b.data()));
+}
+
+// Codim 1: the boundary-edge providers.
+inline void AssembleMatrixLocally(dim_t codim, const uscalfe::FeSpaceLagrange& trial,
+                                  const uscalfe::FeSpaceLagrange& test,
+                                  const uscalfe::MassEdgeMatrixProvider& provider, COOMatrix& A) {
+  if (codim != 1 || &trial != &test)
+    throw Error(LFG_UNSUPPORTED, "AssembleMatrixLocally: edge providers act on codim 1 of one space");
+  trial.ctx().Check(lfg_assemble_matrix_edge_mass(trial.get(), provider.get(), A.get()));
+}
+
+inline void AssembleVectorLocally(dim_t codim, const uscalfe::FeSpaceLagrange& dofh,
+                                  const uscalfe::ScalarLoadEdgeVectorProvider& provider,
+                                  DeviceVector<double>& b) {
+  if (codim != 1) throw Error(LFG_UNSUPPORTED, "AssembleVectorLocally: edge providers act on codim 1");
+  dofh.ctx().Check(lfg_assemble_vector_edge_load(dofh.get(), provider.get(), b.data()));
 }
 
 inline void FixFlaggedSolutionComponents(const DeviceVector<uint8_t>& flags, const DeviceVector<double>& values,

@@ -201,6 +201,31 @@ typedef struct {
   int32_t qr_degree_quad;
 } lfg_rd_provider;
 
+/* Boundary-edge providers (codim-1 assembly).
+ * MassEdgeMatrixProvider (uscalfe/loc_comp_ellbvp.h:367-529) with
+ * AssembleMatrixLocally(1, dofh, dofh, provider, A) (assembler.h:114-186):
+ * edges in index order; an edge is active iff edge_flags_dev[e] != 0 (the
+ * EDGESELECTOR; NULL = every edge); per active edge the (p+1)^2 triplets of
+ *   A_e(i,j) = sum_k w_k |e| gamma(x_k) phi_i(t_k) phi_j(t_k)
+ * in row-major order, rows/cols = the edge's dofs (its two endpoint dofs in
+ * edge direction, then its interior dofs), segment basis of the space's
+ * degree (FeLagrangeO{1,2,3}Segment), Gauss rule of degree qr_degree (0:
+ * 2 * degree).  ScalarLoadEdgeVectorProvider (loc_comp_ellbvp.h:784-921) with
+ * AssembleVectorLocally(1, ...) (assembler.h:298-327): b[dof_i] += sum_k
+ * w_k |e| g(x_k) phi_i(t_k), contributions added in edge order.  Coefficients:
+ * CONSTANT, PER_CELL / PER_CELL_EXP (data indexed by EDGE), NODAL_O1,
+ * ANALYTIC.  FP64. */
+typedef struct {
+  lfg_coeff gamma;
+  const uint8_t* edge_flags_dev;
+  int32_t qr_degree;
+} lfg_edge_mass_provider;
+typedef struct {
+  lfg_coeff g;
+  const uint8_t* edge_flags_dev;
+  int32_t qr_degree;
+} lfg_edge_load_provider;
+
 /* ScalarLoadElementVectorProvider (loc_comp_ellbvp.h:562-746). */
 typedef struct {
   lfg_coeff f;
@@ -233,6 +258,8 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* space, const lfg_rd_provider* provi
                                   lfg_coo* coo);
 /* AssembleVectorLocally(0, dofh, provider, b) (assembler.h:298-327):
  * b_dev[dof] += element vector entries, cells in index order (deterministic). */
+lfg_status lfg_assemble_matrix_edge_mass(lfg_space* space, const lfg_edge_mass_provider* provider, lfg_coo* coo);
+lfg_status lfg_assemble_vector_edge_load(lfg_space* space, const lfg_edge_load_provider* provider, double* b_dev);
 lfg_status lfg_assemble_vector_load(lfg_space* space, const lfg_load_provider* provider,
                                     double* b_dev);
 /* Assembly with caller-tabulated element matrices / vectors: elem_dev holds

@@ -21,7 +21,7 @@ import threading
 import numpy as np
 
 from . import _capi
-from ._capi import (lfg_rd_adjoint_opts, lfg_coeff, lfg_load_provider, lfg_rd_provider, lfg_solve_opts, lfg_solve_stats,
+from ._capi import (lfg_edge_load_provider, lfg_edge_mass_provider, lfg_rd_adjoint_opts, lfg_coeff, lfg_load_provider, lfg_rd_provider, lfg_solve_opts, lfg_solve_stats,
                     lfg_triplet)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -540,6 +540,37 @@ def load_provider(f, qr_degree_tria=0, qr_degree_quad=0):
     p.f = f
     p.qr_degree_tria, p.qr_degree_quad = qr_degree_tria, qr_degree_quad
     return p
+
+
+def edge_mass_provider(gamma, flags=None, qr_degree=0):
+    """MassEdgeMatrixProvider: gamma on the edges with flags[e] != 0 (a device
+    uint8 array; None = every edge).  Per-cell coefficient data is per edge."""
+    p = lfg_edge_mass_provider()
+    p.gamma = gamma
+    p.edge_flags_dev = flags.ptr if flags is not None else None
+    p.qr_degree = qr_degree
+    p._keep = flags
+    return p
+
+
+def edge_load_provider(g, flags=None, qr_degree=0):
+    """ScalarLoadEdgeVectorProvider on the edges with flags[e] != 0."""
+    p = lfg_edge_load_provider()
+    p.g = g
+    p.edge_flags_dev = flags.ptr if flags is not None else None
+    p.qr_degree = qr_degree
+    p._keep = flags
+    return p
+
+
+def assemble_matrix_edge_mass(space, provider, coo):
+    """AssembleMatrixLocally(1, dofh, dofh, MassEdgeMatrixProvider, A)."""
+    space.ctx.check(lib().lfg_assemble_matrix_edge_mass(space.h, C.byref(provider), coo.h))
+
+
+def assemble_vector_edge_load(space, provider, b):
+    """AssembleVectorLocally(1, dofh, ScalarLoadEdgeVectorProvider, b)."""
+    space.ctx.check(lib().lfg_assemble_vector_edge_load(space.h, C.byref(provider), b.ptr))
 
 
 def assemble_matrix_rd(space, provider, coo):

@@ -1,7 +1,7 @@
 """ctypes declarations of the C-ABI in include/lfg.h.
 
 This is the Python-side binding a caller uses in place of the reference's C++
-templates (the C++ facade in include/lf/ is the other binding).  Every
+templates (the C++ facade include/lf_gb300.hpp is the other binding).  Every
 function listed in include/lfg.h is declared here; tests check both lists
 against the exported symbols of the shared library.
 """
@@ -30,6 +30,14 @@ class lfg_rd_provider(C.Structure):
 
 class lfg_load_provider(C.Structure):
     _fields_ = [("f", lfg_coeff), ("qr_degree_tria", i32), ("qr_degree_quad", i32)]
+
+
+class lfg_edge_mass_provider(C.Structure):
+    _fields_ = [("gamma", lfg_coeff), ("edge_flags_dev", vp), ("qr_degree", i32)]
+
+
+class lfg_edge_load_provider(C.Structure):
+    _fields_ = [("g", lfg_coeff), ("edge_flags_dev", vp), ("qr_degree", i32)]
 
 
 class lfg_solve_opts(C.Structure):
@@ -95,6 +103,8 @@ SIGNATURES = {
     "lfg_coo_append_host": (c_status, [vp, vp, i64]),
     "lfg_assemble_matrix_rd": (c_status, [vp, P(lfg_rd_provider), vp]),
     "lfg_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
+    "lfg_assemble_matrix_edge_mass": (c_status, [vp, P(lfg_edge_mass_provider), vp]),
+    "lfg_assemble_vector_edge_load": (c_status, [vp, P(lfg_edge_load_provider), vp]),
     "lfg_assemble_matrix_tabulated": (c_status, [vp, vp, i32, vp]),
     "lfg_assemble_vector_tabulated": (c_status, [vp, vp, i32, vp]),
     "lfg_fix_flagged_solution_components": (c_status, [vp, vp, vp, vp]),

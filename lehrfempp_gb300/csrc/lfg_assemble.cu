@@ -823,6 +823,116 @@ __global__ void __launch_bounds__(256) SumPartsKernel(int64_t m, const double* _
   if (threadIdx.x == 0) *out = scale * red[0];
 }
 
+// ------------------------------------------------- boundary-edge providers
+// One thread per edge.  Segment rule and basis come in by value (<= 16
+// points, <= 4 shape functions).
+struct EdgeRule {
+  int nq, n;
+  double t[16], w[16], phi[16 * 4];
+};
+
+struct EdgeArgs {
+  int64_t ne;
+  const int2* edges;       // endpoints in edge direction
+  const double2* xy;
+  const uint8_t* flags;    // null: every edge
+  const int64_t* offset;   // per edge (null: e * stride)
+  int64_t stride;          // n * n (matrix) or n (vector)
+  int np, ns;              // dofs per node / edge interior
+  int64_t node_dofs;       // num_nodes * np
+  CoeffDev f;
+};
+
+__device__ __forceinline__ double EdgeCoeff(const CoeffDev& f, int64_t e, const int2& en, const double2& p0,
+                                            const double2& p1, double t) {
+  switch (f.kind) {
+    case LFG_COEFF_CONSTANT: return f.value;
+    case LFG_COEFF_PER_CELL: return f.data[e];
+    case LFG_COEFF_PER_CELL_EXP: return exp(f.data[e]);
+    case LFG_COEFF_NODAL_O1: return f.data[en.x] * (1.0 - t) + f.data[en.y] * t;
+    case LFG_COEFF_ANALYTIC: return EvalAnalytic(f, p0.x + t * (p1.x - p0.x), p0.y + t * (p1.y - p0.y));
+  }
+  return 0.0;
+}
+
+// Global dofs of edge e: endpoint dofs in edge direction, then the interior
+// dofs (dofhandler.cc:167-195 for codim 1).
+__device__ __forceinline__ int EdgeDofs(const EdgeArgs& a, int64_t e, const int2& en, int* d) {
+  int k = 0;
+  for (int j = 0; j < a.np; ++j) d[k++] = static_cast<int>(static_cast<int64_t>(en.x) * a.np + j);
+  for (int j = 0; j < a.np; ++j) d[k++] = static_cast<int>(static_cast<int64_t>(en.y) * a.np + j);
+  for (int j = 0; j < a.ns; ++j) d[k++] = static_cast<int>(a.node_dofs + e * a.ns + j);
+  return k;
+}
+
+__global__ void EdgeCountKernel(int64_t ne, const uint8_t* __restrict__ flags, int64_t per, int64_t* __restrict__ cnt) {
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < ne;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    cnt[e] = flags[e] ? per : 0;
+}
+
+__global__ void EdgeMassKernel(EdgeArgs a, EdgeRule r, lfg_triplet* __restrict__ out) {
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < a.ne;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (a.flags && !a.flags[e]) continue;
+    const int2 en = a.edges[e];
+    const double2 p0 = a.xy[en.x], p1 = a.xy[en.y];
+    const double len = hypot(p1.x - p0.x, p1.y - p0.y);  // SegmentO1 integration element
+    int d[8];
+    const int n = EdgeDofs(a, e, en, d);
+    double m[16];
+    for (int q = 0; q < n * n; ++q) m[q] = 0.0;
+    for (int k = 0; k < r.nq; ++k) {
+      const double s = (r.w[k] * len) * EdgeCoeff(a.f, e, en, p0, p1, r.t[k]);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) m[i * n + j] += r.phi[k * r.n + i] * r.phi[k * r.n + j] * s;
+    }
+    lfg_triplet* o = out + (a.offset ? a.offset[e] : e * a.stride);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) StoreTriplet(o + i * n + j, d[i], d[j], m[i * n + j]);
+  }
+}
+
+// Element vectors of the active edges into ev (at the edge's offset) and the
+// (dof, slot) items of the ordered gather.
+__global__ void EdgeLoadKernel(EdgeArgs a, EdgeRule r, double* __restrict__ ev, uint64_t* __restrict__ key,
+                               uint32_t* __restrict__ slot) {
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < a.ne;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (a.flags && !a.flags[e]) continue;
+    const int2 en = a.edges[e];
+    const double2 p0 = a.xy[en.x], p1 = a.xy[en.y];
+    const double len = hypot(p1.x - p0.x, p1.y - p0.y);
+    int d[8];
+    const int n = EdgeDofs(a, e, en, d);
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < r.nq; ++k) {
+      const double s = (r.w[k] * len) * EdgeCoeff(a.f, e, en, p0, p1, r.t[k]);
+      for (int i = 0; i < n; ++i) v[i] += r.phi[k * r.n + i] * s;
+    }
+    const int64_t off = a.offset ? a.offset[e] : e * a.stride;
+    for (int i = 0; i < n; ++i) {
+      ev[off + i] = v[i];
+      key[off + i] = static_cast<uint64_t>(d[i]);
+      slot[off + i] = static_cast<uint32_t>(off + i);
+    }
+  }
+}
+
+// b[dof] += contributions in edge order: after a stable sort of the items by
+// dof, the head of each run adds the run's values left to right.
+__global__ void EdgeGatherKernel(int64_t n, const uint64_t* __restrict__ key, const uint32_t* __restrict__ slot,
+                                 const double* __restrict__ ev, double* __restrict__ b) {
+  for (int64_t q = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; q < n;
+       q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (q > 0 && key[q - 1] == key[q]) continue;
+    const uint64_t d = key[q];
+    double s = b[d];
+    for (int64_t p = q; p < n && key[p] == d; ++p) s += ev[slot[p]];
+    b[d] = s;
+  }
+}
+
 // ------------------------------------------------------------------ host side
 
 void BuildTable(bool quad, int degree, int rule_degree, std::vector<double>& h, Tab& L) {
@@ -1256,6 +1366,121 @@ lfg_status lfg_grad_rd_cellwise(lfg_space* sp, const lfg_rd_provider* pr, const 
   if (!sp) return LFG_INVALID_ARG;
   LFG_API_BEGIN(sp->mesh->ctx)
   GradRDCellwise(sp, pr, u, lam, flags, 1.0, grad);
+  LFG_API_END
+}
+
+}  // extern "C"
+
+namespace lfg {
+namespace {
+
+EdgeRule MakeEdgeRule(int degree, int qr_degree) {
+  std::vector<double> t, w, phi;
+  if (qr_degree > 30 || !SegmentTables(degree, qr_degree, t, w, phi))
+    Fail(LFG_UNSUPPORTED, "edge provider: segment rule of degree " + std::to_string(qr_degree) + " not available");
+  EdgeRule r{};
+  r.nq = static_cast<int>(t.size());
+  r.n = degree + 1;
+  for (int k = 0; k < r.nq; ++k) {
+    r.t[k] = t[k];
+    r.w[k] = w[k];
+    for (int i = 0; i < r.n; ++i) r.phi[k * r.n + i] = phi[k * r.n + i];
+  }
+  return r;
+}
+
+// Per-edge output offsets (prefix of `per` over the active edges); returns
+// the total.  Without flags the offsets are e * per and off stays empty.
+int64_t EdgeOffsets(lfg_ctx* ctx, lfg_mesh* m, const uint8_t* flags, int64_t per, DevBuf& off) {
+  if (!flags) return m->ne * per;
+  off.alloc((m->ne + 1) * sizeof(int64_t), ctx->stream);
+  EdgeCountKernel<<<GridFor(ctx, m->ne, 256), 256, 0, ctx->stream>>>(m->ne, flags, per, off.as<int64_t>());
+  LFG_LAUNCHED(ctx);
+  return ExclusiveScanI64(ctx, off.as<int64_t>(), off.as<int64_t>(), m->ne);
+}
+
+EdgeArgs BaseEdgeArgs(lfg_space* sp, const lfg_coeff& f, const uint8_t* flags, const char* what) {
+  lfg_mesh* m = sp->mesh;
+  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, std::string(what) + ": needs a Lagrangian space");
+  if (f.kind == LFG_COEFF_ZERO || f.kind == LFG_COEFF_CONSTANT || f.kind == LFG_COEFF_PER_CELL ||
+      f.kind == LFG_COEFF_PER_CELL_EXP || f.kind == LFG_COEFF_NODAL_O1 || f.kind == LFG_COEFF_ANALYTIC) {
+  } else {
+    Fail(LFG_UNSUPPORTED, std::string(what) + ": unsupported coefficient kind");
+  }
+  EdgeArgs a{};
+  a.ne = m->ne;
+  a.edges = m->edge_nodes.as<int2>();
+  a.xy = m->xy.as<double2>();
+  a.flags = flags;
+  a.np = sp->np;
+  a.ns = sp->ns;
+  a.node_dofs = m->nv * sp->np;
+  a.f = ToDev(f, m, what);
+  return a;
+}
+
+}  // namespace
+}  // namespace lfg
+
+extern "C" {
+
+lfg_status lfg_assemble_matrix_edge_mass(lfg_space* sp, const lfg_edge_mass_provider* pr, lfg_coo* coo) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!pr || !coo) Fail(LFG_INVALID_ARG, "lfg_assemble_matrix_edge_mass: null argument");
+  if (coo->rows < sp->num_dofs || coo->cols < sp->num_dofs)
+    Fail(LFG_INVALID_ARG, "COO matrix smaller than the number of dofs");
+  lfg_ctx* ctx = sp->mesh->ctx;
+  EdgeArgs a = BaseEdgeArgs(sp, pr->gamma, pr->edge_flags_dev, "edge mass");
+  const EdgeRule r = MakeEdgeRule(sp->degree, pr->qr_degree > 0 ? pr->qr_degree : 2 * sp->degree);
+  const int64_t n = 2 * sp->np + sp->ns;
+  a.stride = n * n;
+  DevBuf off;
+  const int64_t total = EdgeOffsets(ctx, sp->mesh, pr->edge_flags_dev, n * n, off);
+  if (coo->size + total > coo->capacity)
+    Fail(LFG_CAPACITY, "COO capacity " + std::to_string(coo->capacity) + " < " + std::to_string(coo->size + total));
+  a.offset = pr->edge_flags_dev ? off.as<int64_t>() : nullptr;
+  if (a.ne > 0) {
+    ProfScope prof(ctx, "edge_mass");
+    EdgeMassKernel<<<GridFor(ctx, a.ne, 128), 128, 0, ctx->stream>>>(a, r, coo->d + coo->size);
+    LFG_LAUNCHED(ctx);
+  }
+  coo->size += total;
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));  // `off` is freed on return
+  LFG_API_END
+}
+
+lfg_status lfg_assemble_vector_edge_load(lfg_space* sp, const lfg_edge_load_provider* pr, double* b) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!pr || !b) Fail(LFG_INVALID_ARG, "lfg_assemble_vector_edge_load: null argument");
+  lfg_ctx* ctx = sp->mesh->ctx;
+  cudaStream_t s = ctx->stream;
+  EdgeArgs a = BaseEdgeArgs(sp, pr->g, pr->edge_flags_dev, "edge load");
+  const EdgeRule r = MakeEdgeRule(sp->degree, pr->qr_degree > 0 ? pr->qr_degree : 2 * sp->degree);
+  const int64_t n = 2 * sp->np + sp->ns;
+  a.stride = n;
+  DevBuf off;
+  const int64_t total = EdgeOffsets(ctx, sp->mesh, pr->edge_flags_dev, n, off);
+  if (total >= (int64_t(1) << 32)) Fail(LFG_UNSUPPORTED, "more than 2^32 edge contributions");
+  a.offset = pr->edge_flags_dev ? off.as<int64_t>() : nullptr;
+  if (total > 0) {
+    ProfScope prof(ctx, "edge_load");
+    DevBuf ev, key, slot;
+    ev.alloc(total * sizeof(double), s);
+    key.alloc(total * sizeof(uint64_t), s);
+    slot.alloc(total * sizeof(uint32_t), s);
+    EdgeLoadKernel<<<GridFor(ctx, a.ne, 128), 128, 0, s>>>(a, r, ev.as<double>(), key.as<uint64_t>(),
+                                                          slot.as<uint32_t>());
+    LFG_LAUNCHED(ctx);
+    int bits = 1;
+    while ((int64_t(1) << bits) < sp->num_dofs + 1) ++bits;
+    RadixSortPairs(ctx, key.as<uint64_t>(), slot.as<uint32_t>(), total, bits);
+    EdgeGatherKernel<<<GridFor(ctx, total, 256), 256, 0, s>>>(total, key.as<uint64_t>(), slot.as<uint32_t>(),
+                                                             ev.as<double>(), b);
+    LFG_LAUNCHED(ctx);
+    LFG_CUDA(cudaStreamSynchronize(s));
+  }
   LFG_API_END
 }
 

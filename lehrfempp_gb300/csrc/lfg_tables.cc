@@ -307,4 +307,26 @@ bool BuildDfTables(bool quad, int degree, int rule_degree, std::vector<float>& o
   return true;
 }
 
+bool SegmentTables(int degree, int rule_degree, std::vector<double>& t, std::vector<double>& w,
+                   std::vector<double>& phi) {
+  if (degree < 1 || degree > 3 || rule_degree < 0) return false;
+  const int m = rule_degree / 2 + 1;
+  GaussLegendre01(m, t, w);
+  const int n = degree + 1;
+  // nodes 0, 1, then 1/p, ..., (p-1)/p
+  std::vector<long double> node(n);
+  node[0] = 0.0L;
+  node[1] = 1.0L;
+  for (int a = 2; a < n; ++a) node[a] = static_cast<long double>(a - 1) / degree;
+  phi.assign(static_cast<size_t>(m) * n, 0.0);
+  for (int k = 0; k < m; ++k)
+    for (int a = 0; a < n; ++a) {
+      long double v = 1.0L;
+      for (int b = 0; b < n; ++b)
+        if (b != a) v *= (static_cast<long double>(t[k]) - node[b]) / (node[a] - node[b]);
+      phi[static_cast<size_t>(k) * n + a] = static_cast<double>(v);
+    }
+  return true;
+}
+
 }  // namespace lfg

@@ -38,4 +38,11 @@ struct DfLayout {
 };
 bool BuildDfTables(bool is_quad, int degree, int rule_degree, std::vector<float>& out, DfLayout& L);
 
+// Segment rule of make_quad_rule.cc:22-27 (Gauss-Legendre, rule_degree/2+1
+// points on [0, 1]) and the segment Lagrange basis of `degree` at its points,
+// phi[k * n + i], n = degree + 1, local order: the two endpoints, then the
+// interior nodes along the segment (FeLagrangeO{1,2,3}Segment numbering).
+bool SegmentTables(int degree, int rule_degree, std::vector<double>& t, std::vector<double>& w,
+                   std::vector<double>& phi);
+
 }  // namespace lfg

@@ -196,6 +196,25 @@ struct LoadProvider {
 void AssembleMatrixLocally(const DofHandler& dh,
                            const std::function<void(idx_t, std::vector<double>&)>& eval,
                            COOMatrix& A);
+
+// ------------------------------------------------- boundary-edge providers
+// FeLagrangeO{1,2,3}Segment shape functions (lagr_fe.h:284, 563-700, 1155-1277).
+void EvalSegmentShape(int degree, double t, double* phi);
+// A MeshFunction on edge e at segment parameters t (SegmentO1: x = p0 + t (p1 - p0)
+// with (p0, p1) the edge's endpoints in edge direction).  Per-cell data is
+// indexed by edge here; the O1 nodal interpolant restricts to the edge.
+void EvalOnEdge(const MeshFunction& f, const Mesh& m, idx_t e, const std::vector<double>& t,
+                std::vector<double>& out);
+// AssembleMatrixLocally(1, dh, dh, MassEdgeMatrixProvider(fes, gamma, selector), A)
+// (assembler.h:114-186 with codim 1; loc_comp_ellbvp.h:367-529): edges in index
+// order, active iff flags[e] (all when flags is null), A_e = sum_k w_k |e|
+// gamma(x_k) phi_k phi_k^T on the Gauss rule of degree qdeg.
+void AssembleEdgeMass(const DofHandler& dh, int degree, const MeshFunction& gamma, const uint8_t* flags, int qdeg,
+                      COOMatrix& A);
+// AssembleVectorLocally(1, dh, ScalarLoadEdgeVectorProvider(fes, g, selector), b)
+// (assembler.h:298-327; loc_comp_ellbvp.h:784-921): b[dof_i] += sum_k w_k |e| g(x_k) phi_i(t_k).
+void AssembleEdgeLoad(const DofHandler& dh, int degree, const MeshFunction& g, const uint8_t* flags, int qdeg,
+                      std::vector<double>& b);
 void AssembleVectorLocally(const DofHandler& dh,
                            const std::function<void(idx_t, std::vector<double>&)>& eval,
                            std::vector<double>& b);

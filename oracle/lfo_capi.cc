@@ -297,6 +297,31 @@ int lfo_assemble_load(void* sp, const lfo_coeff* f, int qdeg_tria, int qdeg_quad
   LFO_CATCH
 }
 
+int lfo_assemble_edge_mass(void* sp, const lfo_coeff* gamma, const uint8_t* flags, int qdeg, void** out,
+                           char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(gamma, gamma && gamma->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_edges);
+  auto A = std::make_unique<COOMatrix>();
+  A->rows = A->cols = s->dh.num_dofs;
+  AssembleEdgeMass(s->dh, s->degree, mf, flags, qdeg > 0 ? qdeg : 2 * s->degree, *A);
+  *out = A.release();
+  LFO_CATCH
+}
+
+int lfo_assemble_edge_load(void* sp, const lfo_coeff* g, const uint8_t* flags, int qdeg, double* b, char* err,
+                           int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(g, g && g->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_edges);
+  std::vector<double> bv(b, b + s->dh.num_dofs);
+  AssembleEdgeLoad(s->dh, s->degree, mf, flags, qdeg > 0 ? qdeg : 2 * s->degree, bv);
+  std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
 int lfo_assemble_tabulated(void* sp, const double* elem, int ld, double* vec_elem, double* b,
                            void** out, char* err, int errlen) {
   LFO_TRY

@@ -724,6 +724,99 @@ void AssembleVectorLocally(const DofHandler& dh,
   }
 }
 
+// ============================================== boundary-edge providers ====
+
+void EvalSegmentShape(int degree, double t, double* phi) {
+  double d[4];
+  if (degree == 1) {  // FeLagrangeO1Segment (lagr_fe.h:284-398)
+    phi[0] = 1.0 - t;
+    phi[1] = t;
+  } else if (degree == 2) {
+    SegO2(t, phi, d);
+  } else if (degree == 3) {
+    SegO3(t, phi, d);
+  } else {
+    throw Error("segment degree must be 1..3");
+  }
+}
+
+void EvalOnEdge(const MeshFunction& f, const Mesh& m, idx_t e, const std::vector<double>& t,
+                std::vector<double>& out) {
+  const idx_t a = m.edge_nodes[e][0], b = m.edge_nodes[e][1];
+  out.assign(t.size(), 0.0);
+  for (size_t k = 0; k < t.size(); ++k) {
+    switch (f.kind) {
+      case MeshFunction::kZero: break;
+      case MeshFunction::kConstant: out[k] = f.value; break;
+      case MeshFunction::kPerCell: out[k] = f.data[e]; break;
+      case MeshFunction::kPerCellExp: out[k] = std::exp(f.data[e]); break;
+      case MeshFunction::kNodalO1: out[k] = f.data[a] * (1.0 - t[k]) + f.data[b] * t[k]; break;
+      case MeshFunction::kAnalytic: {
+        const double x = m.xy[2 * a] + t[k] * (m.xy[2 * b] - m.xy[2 * a]);
+        const double y = m.xy[2 * a + 1] + t[k] * (m.xy[2 * b + 1] - m.xy[2 * a + 1]);
+        out[k] = f.fn(x, y);
+        break;
+      }
+      default: throw Error("bad mesh function kind on an edge");
+    }
+  }
+}
+
+namespace {
+// Edge length |p1 - p0| (SegmentO1::IntegrationElement) and the segment
+// Gauss rule of make_quad_rule.cc:22-27 (degree / 2 + 1 points on [0, 1]).
+double EdgeLength(const Mesh& m, idx_t e) {
+  const idx_t a = m.edge_nodes[e][0], b = m.edge_nodes[e][1];
+  return std::hypot(m.xy[2 * b] - m.xy[2 * a], m.xy[2 * b + 1] - m.xy[2 * a + 1]);
+}
+}  // namespace
+
+void AssembleEdgeMass(const DofHandler& dh, int degree, const MeshFunction& gamma, const uint8_t* flags, int qdeg,
+                      COOMatrix& A) {
+  std::vector<double> t, w, gv;
+  GaussLegendre(qdeg / 2 + 1, t, w);
+  const int n = dh.n_edge;
+  std::vector<double> phi(t.size() * n), mat(n * n);
+  for (size_t k = 0; k < t.size(); ++k) EvalSegmentShape(degree, t[k], &phi[k * n]);
+  const Mesh& m = *dh.mesh;
+  for (idx_t e = 0; e < m.num_edges; ++e) {
+    if (flags && !flags[e]) continue;
+    const double len = EdgeLength(m, e);
+    EvalOnEdge(gamma, m, e, t, gv);
+    std::fill(mat.begin(), mat.end(), 0.0);
+    for (size_t k = 0; k < t.size(); ++k) {
+      const double s = (w[k] * len) * gv[k];
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) mat[i * n + j] += phi[k * n + i] * phi[k * n + j] * s;
+    }
+    const idx_t* dofs = &dh.edge_dofs[e * n];
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) A.AddToEntry(dofs[i], dofs[j], mat[i * n + j]);
+  }
+}
+
+void AssembleEdgeLoad(const DofHandler& dh, int degree, const MeshFunction& g, const uint8_t* flags, int qdeg,
+                      std::vector<double>& b) {
+  std::vector<double> t, w, gv;
+  GaussLegendre(qdeg / 2 + 1, t, w);
+  const int n = dh.n_edge;
+  std::vector<double> phi(t.size() * n), vec(n);
+  for (size_t k = 0; k < t.size(); ++k) EvalSegmentShape(degree, t[k], &phi[k * n]);
+  const Mesh& m = *dh.mesh;
+  for (idx_t e = 0; e < m.num_edges; ++e) {
+    if (flags && !flags[e]) continue;
+    const double len = EdgeLength(m, e);
+    EvalOnEdge(g, m, e, t, gv);
+    std::fill(vec.begin(), vec.end(), 0.0);
+    for (size_t k = 0; k < t.size(); ++k) {
+      const double s = (w[k] * len) * gv[k];
+      for (int i = 0; i < n; ++i) vec[i] += phi[k * n + i] * s;
+    }
+    const idx_t* dofs = &dh.edge_dofs[e * n];
+    for (int i = 0; i < n; ++i) b[dofs[i]] += vec[i];
+  }
+}
+
 void FixFlaggedSolutionComponents(const uint8_t* flags, const double* values,
                                   COOMatrix& A, std::vector<double>& b) {
   const idx_t N = A.cols;

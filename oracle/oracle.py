@@ -75,6 +75,8 @@ def lib():
             L.lfo_quad_rule.argtypes = [C.c_int, C.c_int, P(dp), P(dp), P(dp), P(C.c_int), C.c_char_p, C.c_int]
             L.lfo_assemble_rd.argtypes = [vp, P(lfo_coeff), P(lfo_coeff), C.c_int, C.c_int, i64, i64, P(vp), C.c_char_p, C.c_int]
             L.lfo_assemble_load.argtypes = [vp, P(lfo_coeff), C.c_int, C.c_int, P(dp), C.c_char_p, C.c_int]
+            L.lfo_assemble_edge_mass.argtypes = [vp, P(lfo_coeff), P(C.c_uint8), C.c_int, P(vp), C.c_char_p, C.c_int]
+            L.lfo_assemble_edge_load.argtypes = [vp, P(lfo_coeff), P(C.c_uint8), C.c_int, P(dp), C.c_char_p, C.c_int]
             L.lfo_assemble_tabulated.argtypes = [vp, P(dp), C.c_int, P(dp), P(dp), P(vp), C.c_char_p, C.c_int]
             L.lfo_coo_create.argtypes = [i64, i64, i64, P(i32), P(i32), P(dp)]
             L.lfo_coo_create.restype = vp
@@ -270,6 +272,28 @@ def assemble_rd(space, alpha, gamma, qdeg_tria=0, qdeg_quad=0, cells=(0, -1)):
     _check(lib().lfo_assemble_rd(space.h, C.byref(alpha), C.byref(gamma), qdeg_tria, qdeg_quad, cells[0], cells[1],
                                  C.byref(h), err, 512), err)
     return COO(h, space.num_dofs, space.num_dofs)
+
+
+def assemble_edge_mass(space, gamma, flags=None, qdeg=0):
+    """AssembleMatrixLocally(1, ...) with MassEdgeMatrixProvider on the edges
+    with flags[e] != 0 (all edges when flags is None); per-cell coefficient
+    data is indexed by edge."""
+    h = C.c_void_p()
+    err = _err()
+    fl = None if flags is None else np.ascontiguousarray(flags, np.uint8)
+    _check(lib().lfo_assemble_edge_mass(space.h, C.byref(gamma), _p(fl, C.c_uint8) if fl is not None else None,
+                                        qdeg, C.byref(h), err, 512), err)
+    return COO(h, space.num_dofs, space.num_dofs)
+
+
+def assemble_edge_load(space, g, flags=None, qdeg=0, b=None):
+    """AssembleVectorLocally(1, ...) with ScalarLoadEdgeVectorProvider."""
+    b = np.zeros(space.num_dofs) if b is None else np.ascontiguousarray(b, np.float64).copy()
+    err = _err()
+    fl = None if flags is None else np.ascontiguousarray(flags, np.uint8)
+    _check(lib().lfo_assemble_edge_load(space.h, C.byref(g), _p(fl, C.c_uint8) if fl is not None else None, qdeg,
+                                        _p(b, C.c_double), err, 512), err)
+    return b
 
 
 def assemble_load(space, f, qdeg_tria=0, qdeg_quad=0, b=None):

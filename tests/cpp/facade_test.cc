@@ -141,6 +141,37 @@ static void CheckAssembly(const g::Context& ctx, int nx, int ny, int degree) {
   CHECK(threw, "capacity overflow did not throw LFG_CAPACITY");
 }
 
+// Robin-type boundary terms on the boundary edges: mass and load of O2 on a
+// TPTriag mesh; every boundary edge contributes 9 triplets, the load sums to
+// the boundary length (4) times g.
+static void CheckEdges(const g::Context& ctx) {
+  auto mesh = g::mesh::TPTriagMeshBuilder(ctx).setNumXCells(5).setNumYCells(3).Build();
+  auto fes = g::uscalfe::FeSpaceLagrangeO<2>(mesh);
+  const int64_t nd = fes->NumDofs(), ne = mesh->NumEntities(1);
+  std::vector<uint8_t> nf(mesh->NumEntities(2)), ef(ne);
+  g::DeviceVector<uint8_t> nfd(ctx, nf.size()), efd(ctx, ef.size());
+  ctx.Check(lfg_mesh_boundary_flags(mesh->get(), nfd.data(), efd.data()));
+  ef = efd.Download();
+  int64_t nb = 0;
+  for (uint8_t f : ef) nb += f != 0;
+  g::uscalfe::MassEdgeMatrixProvider mp(fes, g::uscalfe::MeshFunction::Constant(2.0), efd.data());
+  g::assemble::COOMatrix A(ctx, nd, nd, 9 * nb);
+  g::assemble::AssembleMatrixLocally(1, *fes, *fes, mp, A);
+  CHECK(A.size() == 9 * nb, "edge mass: %lld triplets for %lld boundary edges", static_cast<long long>(A.size()),
+        static_cast<long long>(nb));
+  double msum = 0.0;
+  for (const lfg_triplet& t : A.Download()) msum += t.value;
+  CHECK(std::fabs(msum - 2.0 * 4.0) < 1e-12, "edge mass sums to %.15g, not 2 x perimeter", msum);
+  g::uscalfe::ScalarLoadEdgeVectorProvider lp(fes, g::uscalfe::MeshFunction::Constant(3.0), efd.data());
+  g::DeviceVector<double> b(ctx, nd);
+  b.SetZero();
+  g::assemble::AssembleVectorLocally(1, *fes, lp, b);
+  double bsum = 0.0;
+  for (double x : b.Download()) bsum += x;
+  CHECK(std::fabs(bsum - 3.0 * 4.0) < 1e-12, "edge load sums to %.15g, not 3 x perimeter", bsum);
+  std::printf("edges: %lld boundary edges, mass sum %.6f, load sum %.6f\n", static_cast<long long>(nb), msum, bsum);
+}
+
 static double Lcg(uint64_t& s) {
   s = s * 6364136223846793005ull + 1442695040888963407ull;
   return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
@@ -194,6 +225,7 @@ int main() {
     CheckAssembly(ctx, 9, 7, 2);
     CheckAssembly(ctx, 6, 5, 3);
     CheckAdjoint(ctx);
+    CheckEdges(ctx);
   } catch (const g::Error& e) {
     std::printf("FAIL: uncaught lf::gb300::Error %d: %s\n", static_cast<int>(e.code()), e.what());
     return 1;

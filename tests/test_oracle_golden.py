@@ -200,3 +200,27 @@ def test_incomplete_mesh_rejected():
     xy = np.array([[0, 0], [1, 0], [0, 1], [5, 5]], float)
     with pytest.raises(RuntimeError, match="incomplete"):
         O.Mesh(xy, np.array([[0, 1, 2, -1]]))
+
+
+def test_edge_providers_known_answers():
+    """lagr_fe_tests.cc:571-601 and 696-722 (lf_fe_edgemass, lf_fe_edgeload):
+    O1 on the hybrid test mesh, gamma = g = 1, every edge:
+    A_e = |e| [[1/3, 1/6], [1/6, 1/3]] and phi_e = |e| [1/2, 1/2]."""
+    xy, cells, pe = O.factory_input("test0")
+    m = O.Mesh(xy, cells, pe)
+    sp = O.Space(m, 1)
+    r, c, v = O.assemble_edge_mass(sp, O.coeff(O.CONSTANT, 1.0)).arrays()
+    en = m.topology()[0]
+    le = np.hypot(*(m.xy[en[:, 1]] - m.xy[en[:, 0]]).T)
+    assert np.abs(v - (le[:, None] * np.array([1 / 3, 1 / 6, 1 / 6, 1 / 3])).ravel()).max() < 1e-15
+    b = O.assemble_edge_load(sp, O.coeff(O.CONSTANT, 1.0))
+    ref = np.zeros(sp.num_dofs)
+    np.add.at(ref, en[:, 0], 0.5 * le)
+    np.add.at(ref, en[:, 1], 0.5 * le)
+    assert np.abs(b - ref).max() < 1e-14
+    # flags select edges; the load accumulates onto the given vector
+    fl = (np.arange(m.num_edges) % 2).astype(np.uint8)
+    r2, c2, v2 = O.assemble_edge_mass(sp, O.coeff(O.CONSTANT, 1.0), fl).arrays()
+    assert len(v2) == 4 * int(fl.sum())
+    b2 = O.assemble_edge_load(sp, O.coeff(O.CONSTANT, 1.0), fl, b=np.ones(sp.num_dofs))
+    assert b2.min() >= 1.0
