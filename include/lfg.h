@@ -169,6 +169,10 @@ lfg_status lfg_space_boundary_dof_flags(lfg_space* space, uint8_t* flags_dev);
  *     LFG_FN_POLY    sum_{i,j<=3} p[4i+j] x^i y^j
  *     LFG_FN_SINSIN  p0 + p1 sin(p2 pi x) sin(p3 pi y)
  *     LFG_FN_SINCOS  p0 + p1 sin(p2 pi x) cos(p3 pi y)
+ *     LFG_FN_EXP     p0 + p1 exp(p2 + p3 x + p4 y + p5 x y)
+ *     LFG_FN_TRIG    p0 + (p1 + p2 x + p3 y + p4 x y) sin(pi (p5 x + p6)) sin(pi (p7 y + p8))
+ *                    (a cosine is the sine shifted by 1/2 in p6 / p8)
+ *   The post-processing functions also use the exact gradient of each family.
  * Arbitrary host lambdas cannot run on the GPU: anything else is LFG_UNSUPPORTED. */
 enum {
   LFG_COEFF_ZERO = 0,
@@ -178,7 +182,7 @@ enum {
   LFG_COEFF_ANALYTIC = 4,
   LFG_COEFF_PER_CELL_EXP = 5  /* exp(data_dev[cell]): a per-cell log-coefficient */
 };
-enum { LFG_FN_POLY = 1, LFG_FN_SINSIN = 2, LFG_FN_SINCOS = 3 };
+enum { LFG_FN_POLY = 1, LFG_FN_SINSIN = 2, LFG_FN_SINCOS = 3, LFG_FN_EXP = 4, LFG_FN_TRIG = 5 };
 
 typedef struct {
   int32_t kind;
@@ -440,6 +444,60 @@ lfg_status lfg_batch_boundary_dof_flags(lfg_batch* batch, uint8_t* flags_dev);
 lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const double* b_dev,
                                double* x_dev, const lfg_solve_opts* opts, lfg_solve_stats* stats,
                                lfg_solve_stats* per_block_stats);
+
+/* ---------------------------------------------------------- post-processing
+ * The steps after the solve (and the Dirichlet data before it), FP64 on the
+ * device.  An FE function is (space, dof vector) as in MeshFunctionFE
+ * (fe/mesh_function_fe.h:44-115); mesh functions are lfg_coeff values.
+ *
+ * IntegrateMeshFunction(mesh, mf, quad_degree, pred, codim)
+ * (fe/fe_tools.h:110-165) for the integrands
+ *   LFG_INTEGRAND_VALUE         u_h + u
+ *   LFG_INTEGRAND_SQ_DIFF       (u_h - u)^2           squaredNorm(mf_fe - mf_u)
+ *   LFG_INTEGRAND_GRAD_SQ_DIFF  |grad u_h - grad u|^2 squaredNorm(mf_grad_fe - mf_grad_u)
+ * with u_h = 0 when dofs_dev is NULL and u = 0 for LFG_COEFF_ZERO; grad u is
+ * the exact gradient of an analytic u, the gradient of the O1 interpolant for
+ * LFG_COEFF_NODAL_O1, 0 for cell-wise constants.  Rules: make_QuadRule(ref_el,
+ * quad_degree) per reference element (segments for codim 1).  flags_dev
+ * (num_cells or num_edges entries, NULL: all) selects entities; as in the
+ * reference, entity 0 always contributes (fe_tools.h:117-124).  Gradients on
+ * edges are LFG_UNSUPPORTED.  On codim 1 a PER_CELL u is indexed by edge.
+ * The sum is deterministic (fixed per-block order).  *result is host memory;
+ * the call waits for it. */
+enum {
+  LFG_INTEGRAND_VALUE = 0,
+  LFG_INTEGRAND_SQ_DIFF = 1,
+  LFG_INTEGRAND_GRAD_SQ_DIFF = 2
+};
+typedef struct {
+  int32_t kind;             /* LFG_INTEGRAND_* */
+  lfg_coeff u;
+  lfg_space* space;         /* space of u_h (on the integration mesh), may be NULL without dofs */
+  const double* dofs_dev;   /* u_h coefficients, NULL: u_h = 0 */
+} lfg_integrand;
+lfg_status lfg_integrate_mesh_function(lfg_mesh* mesh, const lfg_integrand* integrand, int32_t quad_degree,
+                                       const uint8_t* flags_dev, int32_t codim, double* result);
+/* MeshFunctionFE / MeshFunctionGradFE operator()(cell, local)
+ * (fe/mesh_function_fe.h:72-91, fe/mesh_function_grad_fe.h:93-118) for every
+ * cell at the same npts reference points ref_points[2 k], ref_points[2 k + 1]
+ * (host): values_dev[cell * npts + k] and grads_dev[(cell * npts + k) * 2 + d]
+ * (either may be NULL). */
+lfg_status lfg_fe_eval(lfg_space* space, const double* dofs_dev, int32_t npts, const double* ref_points,
+                       double* values_dev, double* grads_dev);
+/* NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259): out_dev[dof]
+ * = u at the dof's evaluation node, cells selected by cell_flags_dev (NULL:
+ * all) in index order; a dof shared by several selected cells takes the value
+ * of the last one (the reference sets, it does not add); dofs of no selected
+ * cell are 0. */
+lfg_status lfg_nodal_projection(lfg_space* space, const lfg_coeff* u, const uint8_t* cell_flags_dev,
+                                double* out_dev);
+/* InitEssentialConditionFromFunction(fes, esscondflag, g) (fe/fe_tools.h:263-329):
+ * for every edge selected by edge_flags_dev (num_edges entries), its dofs get
+ * flag 1 and the value of g at their segment evaluation node (the last
+ * selected edge wins for a shared node); every other dof gets (0, 0.0).  The
+ * two outputs are the (flag, value) pairs FixFlaggedSolutionComponents takes. */
+lfg_status lfg_init_essential_condition(lfg_space* space, const uint8_t* edge_flags_dev, const lfg_coeff* g,
+                                        uint8_t* dof_flags_dev, double* dof_values_dev);
 
 #ifdef __cplusplus
 }

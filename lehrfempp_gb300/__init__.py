@@ -37,7 +37,9 @@ STATUS_NAMES = ["OK", "INVALID_ARG", "DEGENERATE_CELL", "CAPACITY", "UNSUPPORTED
 
 # coefficient kinds and analytic families
 ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
-FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
+FN_POLY, FN_SINSIN, FN_SINCOS, FN_EXP, FN_TRIG = 1, 2, 3, 4, 5
+# integrands of integrate_mesh_function
+INT_VALUE, INT_SQ_DIFF, INT_GRAD_SQ_DIFF = 0, 1, 2
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 
 TRIPLET_DTYPE = np.dtype([("row", np.int32), ("col", np.int32), ("value", np.float64)])
@@ -601,6 +603,52 @@ def grad_rd_cellwise(space, provider, u, lam, flags, grad):
     """grad[c] = -lambda_K^T (dA_K/dtheta_c) u_K, lambda zero at flagged dofs."""
     space.ctx.check(lib().lfg_grad_rd_cellwise(space.h, C.byref(provider), u.ptr, lam.ptr,
                                                flags.ptr if flags is not None else None, grad.ptr))
+
+
+# ----------------------------------------------------------- post-processing
+
+def integrate_mesh_function(mesh, kind, u=None, space=None, dofs=None, quad_degree=2, flags=None, codim=0):
+    """IntegrateMeshFunction (fe/fe_tools.h:110-165) of the integrand `kind`
+    (INT_VALUE: u_h + u, INT_SQ_DIFF: (u_h - u)^2, INT_GRAD_SQ_DIFF:
+    |grad u_h - grad u|^2) with u a coeff (None: zero) and u_h given by `space`
+    and the DeviceArray `dofs` (None: zero).  flags: device uint8 per entity of
+    the codim (None: all; entity 0 always counts, as in the reference)."""
+    g = _capi.lfg_integrand()
+    g.kind = kind
+    g.u = u if u is not None else coeff(ZERO)
+    g.space = space.h if space is not None else None
+    g.dofs_dev = dofs.ptr if dofs is not None else None
+    out = C.c_double()
+    mesh.ctx.check(lib().lfg_integrate_mesh_function(mesh.h, C.byref(g), quad_degree,
+                                                      flags.ptr if flags is not None else None, codim,
+                                                      C.byref(out)))
+    return out.value
+
+
+def fe_eval(space, dofs, ref_points, values=True, grads=False):
+    """MeshFunctionFE / MeshFunctionGradFE on every cell at reference points
+    [k][2]: DeviceArrays (num_cells, k) and (num_cells, k, 2)."""
+    pts = np.ascontiguousarray(ref_points, np.float64).reshape(-1, 2)
+    nc = space.mesh.num_cells
+    v = DeviceArray(space.ctx, (nc, len(pts)), np.float64) if values else None
+    g = DeviceArray(space.ctx, (nc, len(pts), 2), np.float64) if grads else None
+    space.ctx.check(lib().lfg_fe_eval(space.h, dofs.ptr, len(pts), _p(pts, C.c_double),
+                                      v.ptr if v is not None else None, g.ptr if g is not None else None))
+    return v, g
+
+
+def nodal_projection(space, u, out, cell_flags=None):
+    """NodalProjection (fe/fe_tools.h:198-259) of the coeff u into the
+    DeviceArray out (num_dofs)."""
+    space.ctx.check(lib().lfg_nodal_projection(space.h, C.byref(u), cell_flags.ptr if cell_flags is not None else None,
+                                               out.ptr))
+
+
+def init_essential_condition(space, edge_flags, g, dof_flags, dof_values):
+    """InitEssentialConditionFromFunction (fe/fe_tools.h:263-329) into the
+    DeviceArrays dof_flags (uint8) and dof_values (double)."""
+    space.ctx.check(lib().lfg_init_essential_condition(space.h, edge_flags.ptr, C.byref(g), dof_flags.ptr,
+                                                       dof_values.ptr))
 
 
 class RDAdjoint:

@@ -54,6 +54,10 @@ class lfg_rd_adjoint_opts(C.Structure):
                 ("flags_dev", vp), ("dirichlet_dev", vp), ("solve", lfg_solve_opts), ("recompute", i32)]
 
 
+class lfg_integrand(C.Structure):
+    _fields_ = [("kind", i32), ("u", lfg_coeff), ("space", vp), ("dofs_dev", vp)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "lfg_ctx_create": (c_status, [C.c_int, P(vp)]),
@@ -132,6 +136,10 @@ SIGNATURES = {
     "lfg_batch_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
     "lfg_batch_boundary_dof_flags": (c_status, [vp, vp]),
     "lfg_batch_solve_pcg": (c_status, [vp, vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats), P(lfg_solve_stats)]),
+    "lfg_integrate_mesh_function": (c_status, [vp, P(lfg_integrand), i32, vp, i32, P(dbl)]),
+    "lfg_fe_eval": (c_status, [vp, vp, i32, P(dbl), vp, vp]),
+    "lfg_nodal_projection": (c_status, [vp, P(lfg_coeff), vp, vp]),
+    "lfg_init_essential_condition": (c_status, [vp, vp, P(lfg_coeff), vp, vp]),
 }
 
 

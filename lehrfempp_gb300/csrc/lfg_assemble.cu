@@ -25,6 +25,7 @@
 #include <map>
 
 #include "lfg_api.h"
+#include "lfg_coeff.h"
 #include "lfg_elem.h"
 #include "lfg_internal.h"
 
@@ -34,14 +35,6 @@ void EnsureIncidence(lfg_space* sp);
 namespace {
 
 constexpr int kMaxQ = 25;
-
-struct CoeffDev {
-  int kind;
-  int func;
-  double value;
-  const double* data;
-  double p[16];
-};
 
 Tab TabLayout(int n, int nq) {
   Tab t;
@@ -81,27 +74,6 @@ __device__ __forceinline__ void StoreTriplet(lfg_triplet* p, int r, int c, doubl
   const long long bits = __double_as_longlong(v);
   int4 w = make_int4(r, c, static_cast<int>(bits & 0xffffffffll), static_cast<int>(bits >> 32));
   *reinterpret_cast<int4*>(p) = w;
-}
-
-__device__ double EvalAnalytic(const CoeffDev& f, double x, double y) {
-  const double pi = 3.141592653589793;
-  switch (f.func) {
-    case LFG_FN_POLY: {
-      // Horner in y inside Horner in x: sum_i x^i sum_j p[4i+j] y^j
-      double s = 0.0;
-      for (int i = 3; i >= 0; --i) {
-        const double* q = f.p + 4 * i;
-        const double py = ((q[3] * y + q[2]) * y + q[1]) * y + q[0];
-        s = s * x + py;
-      }
-      return s;
-    }
-    case LFG_FN_SINSIN:
-      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * sin(f.p[3] * pi * y));
-    case LFG_FN_SINCOS:
-      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * cos(f.p[3] * pi * y));
-  }
-  return 0.0;
 }
 
 // Value of a coefficient at reference point k of cell c.
@@ -1023,23 +995,6 @@ DfArgs GetDfTable(lfg_space* sp, bool quad, int degree, int rule_degree) {
   return d;
 }
 
-CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
-  CoeffDev d;
-  d.kind = c.kind;
-  d.func = c.func;
-  d.value = c.value;
-  d.data = c.data_dev;
-  for (int i = 0; i < 16; ++i) d.p[i] = c.p[i];
-  if (c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_PER_CELL_EXP)
-    Fail(LFG_UNSUPPORTED, std::string(what) + ": unsupported coefficient kind");
-  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1 || c.kind == LFG_COEFF_PER_CELL_EXP) &&
-      !c.data_dev)
-    Fail(LFG_INVALID_ARG, std::string(what) + ": coefficient data pointer is null");
-  if (c.kind == LFG_COEFF_ANALYTIC && (c.func < LFG_FN_POLY || c.func > LFG_FN_SINCOS))
-    Fail(LFG_UNSUPPORTED, std::string(what) + ": unknown analytic function");
-  return d;
-}
-
 bool Uniform(const lfg_coeff& c) {
   return c.kind == LFG_COEFF_ZERO || c.kind == LFG_COEFF_CONSTANT || c.kind == LFG_COEFF_PER_CELL ||
          c.kind == LFG_COEFF_PER_CELL_EXP;
@@ -1100,6 +1055,8 @@ template <int DEG>
 bool TryTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   if (!d.tab) return false;
   if (a.alpha.kind != LFG_COEFF_ANALYTIC && a.alpha.kind != LFG_COEFF_NODAL_O1) return false;
+  // the df32 evaluator knows the polynomial and sin/cos families only
+  if (a.alpha.kind == LFG_COEFF_ANALYTIC && a.alpha.func > LFG_FN_SINCOS) return false;
   const int gk = a.gamma.kind;
   if (gk != LFG_COEFF_ZERO && gk != LFG_COEFF_CONSTANT && gk != LFG_COEFF_PER_CELL && gk != LFG_COEFF_PER_CELL_EXP)
     return false;

@@ -78,11 +78,79 @@ const int kQuadO2[9][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0}, {1, 2}, {2, 1
 const int kQuadO3[16][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}, {2, 0}, {3, 0}, {1, 2}, {1, 3},
                             {3, 1}, {2, 1}, {0, 3}, {0, 2}, {2, 2}, {3, 2}, {3, 3}, {2, 3}};
 
+// Gauss-Jacobi rule for the weight (1 - t) on [-1, 1] (alpha = 1, beta = 0).
+// Nodes: eigenvalues of the symmetric Jacobi matrix of the monic recurrence,
+//   a_k = -1 / ((2k+1)(2k+3)),  b_k^2 = k (k+1) / (2k+1)^2,
+// isolated one by one with Sturm-sequence bisection (long double).  Weights:
+// the Christoffel numbers w = 4 / ((1 - t^2) P_n'(t)^2) of P_n^(1,0), with
+//   (m+1)(2m-1) P_m = ((4m^2-1) t + 1) P_{m-1} - (m-1)(2m+1) P_{m-2},
+//   P_n'(t) = 2 n (n+1) P_{n-1}(t) / ((2n+1)(1 - t^2))   at a root.
+void GaussJacobi10(int n, std::vector<long double>& t, std::vector<long double>& w) {
+  std::vector<long double> a(n), b2(n, 0.0L);
+  for (int k = 0; k < n; ++k) {
+    a[k] = -1.0L / ((2.0L * k + 1.0L) * (2.0L * k + 3.0L));
+    if (k > 0) b2[k] = static_cast<long double>(k) * (k + 1) / ((2.0L * k + 1.0L) * (2.0L * k + 1.0L));
+  }
+  // number of eigenvalues below x
+  auto below = [&](long double x) {
+    int cnt = 0;
+    long double q = 1.0L;
+    for (int k = 0; k < n; ++k) {
+      q = (a[k] - x) - (k > 0 ? b2[k] / q : 0.0L);
+      if (q == 0.0L) q = -1e-300L;
+      if (q < 0.0L) ++cnt;
+    }
+    return cnt;
+  };
+  t.assign(n, 0.0L);
+  w.assign(n, 0.0L);
+  for (int i = 0; i < n; ++i) {
+    long double lo = -1.0L, hi = 1.0L;  // the spectrum lies in (-1, 1)
+    for (int it = 0; it < 200 && hi - lo > 1e-19L; ++it) {
+      const long double mid = 0.5L * (lo + hi);
+      if (below(mid) > i) hi = mid; else lo = mid;
+    }
+    const long double x = 0.5L * (lo + hi);
+    long double pm2 = 0.0L, pm1 = 1.0L;  // P_{-1}, P_0
+    for (int m = 1; m < n; ++m) {
+      const long double p = (((4.0L * m * m - 1.0L) * x + 1.0L) * pm1 - (m - 1.0L) * (2.0L * m + 1.0L) * pm2) /
+                            ((m + 1.0L) * (2.0L * m - 1.0L));
+      pm2 = pm1;
+      pm1 = p;
+    }
+    const long double dp = 2.0L * n * (n + 1.0L) * pm1 / ((2.0L * n + 1.0L) * (1.0L - x * x));
+    t[i] = x;
+    w[i] = 4.0L / ((1.0L - x * x) * dp * dp);
+  }
+}
+
 }  // namespace
+
+// Conical (collapsed) product rule on the reference triangle with
+// m = degree/2 + 1 points per direction, exact to degree 2m - 1: Gauss-Legendre
+// u_a on [0,1] (slow index) times Gauss-Jacobi(1,0) s_b = (t_b + 1)/2 (fast),
+// x = u_a (1 - s_b), y = s_b, weight W_a w_b / 4.  This is the rule
+// make_quad_rule.cc:139-152 builds for degrees without a hard-coded table.
+void ConicalTriaRule(int degree, Rule& r) {
+  const int m = degree / 2 + 1;
+  std::vector<double> u, W;
+  GaussLegendre01(m, u, W);
+  std::vector<long double> t, w;
+  GaussJacobi10(m, t, w);
+  r = Rule();
+  for (int a = 0; a < m; ++a)
+    for (int b = 0; b < m; ++b) {
+      const long double s = 0.5L * (t[b] + 1.0L);
+      r.x.push_back(static_cast<double>(static_cast<long double>(u[a]) * (1.0L - s)));
+      r.y.push_back(static_cast<double>(s));
+      r.w.push_back(static_cast<double>(static_cast<long double>(W[a]) * w[b] * 0.25L));
+    }
+  r.n = static_cast<int>(r.w.size());
+}
 
 bool MakeRule(bool is_quad, int degree, Rule& r) {
   r = Rule();
-  if (degree < 1) return false;
+  if (degree < 0 || degree > kMaxRuleDegree) return false;
   if (is_quad) {
     const int m = degree / 2 + 1;  // make_quad_rule.cc:28
     std::vector<double> x, w;
@@ -95,7 +163,10 @@ bool MakeRule(bool is_quad, int degree, Rule& r) {
       }
   } else {
     const int d = degree == 3 ? 4 : degree;
-    if (d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0) return false;
+    if (d < 1 || d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0) {
+      ConicalTriaRule(degree, r);
+      return true;
+    }
     for (int k = 0; k < kTriaRuleIndex[d][0]; ++k) {
       const double* row = kTriaRuleRows[kTriaRuleIndex[d][1] + k];
       r.x.push_back(row[0]);
@@ -105,6 +176,38 @@ bool MakeRule(bool is_quad, int degree, Rule& r) {
   }
   r.n = static_cast<int>(r.w.size());
   return true;
+}
+
+void NodeCoords(bool is_quad, int degree, std::vector<double>& xy) {
+  xy.clear();
+  if (is_quad) {
+    // 1D nodes of the segment elements: {0, 1}, {0, 1, 1/2}, {0, 1, 1/3, 2/3}
+    const double s[3][4] = {{0.0, 1.0}, {0.0, 1.0, 0.5}, {0.0, 1.0, 1.0 / 3.0, 2.0 / 3.0}};
+    const int(*map)[2] = degree == 1 ? kQuadO1 : degree == 2 ? kQuadO2 : kQuadO3;
+    for (int i = 0; i < NumShape(true, degree); ++i) {
+      xy.push_back(s[degree - 1][map[i][0]]);
+      xy.push_back(s[degree - 1][map[i][1]]);
+    }
+    return;
+  }
+  // vertices, then per edge (0,1), (1,2), (2,0) its interior nodes from the
+  // first endpoint on, then the barycentre (the nodes of Shape's basis)
+  const double V[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+  for (auto& v : V) {
+    xy.push_back(v[0]);
+    xy.push_back(v[1]);
+  }
+  const int e[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  for (int k = 0; k < 3 && degree >= 2; ++k)
+    for (int j = 1; j < degree; ++j) {
+      const double tb = static_cast<double>(j) / degree, ta = static_cast<double>(degree - j) / degree;
+      xy.push_back(ta * V[e[k][0]][0] + tb * V[e[k][1]][0]);
+      xy.push_back(ta * V[e[k][0]][1] + tb * V[e[k][1]][1]);
+    }
+  if (degree == 3) {
+    xy.push_back(1.0 / 3.0);
+    xy.push_back(1.0 / 3.0);
+  }
 }
 
 int NumShape(bool is_quad, int degree) {

@@ -12,11 +12,20 @@ struct Rule {
   std::vector<double> x, y, w;
 };
 // make_QuadRule (quad/make_quad_rule.cc:21-157): triangles from the
-// reference's tables (degree <= 8, 3 -> 4), quads tensor Gauss-Legendre with
-// degree/2+1 points per direction, x slow / y fast.  False if not available.
+// reference's tables for degree 1..8 (3 -> 4), otherwise the conical
+// Gauss-Legendre x Gauss-Jacobi(1,0) product rule with degree/2+1 points per
+// direction (the reference's rule above its tables, make_quad_rule.cc:139-152;
+// its tables for degrees 9..50 are not restated); quads tensor
+// Gauss-Legendre with degree/2+1 points per direction, x slow / y fast.
+// False for a degree outside [0, kMaxRuleDegree].
+constexpr int kMaxRuleDegree = 100;
 bool MakeRule(bool is_quad, int degree, Rule& out);
 int NumShape(bool is_quad, int degree);
 void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]);
+// Reference coordinates of the evaluation nodes of the Lagrangian element
+// (EvaluationNodes, uscalfe/lagr_fe.h): xy[2 i], xy[2 i + 1] is the node of
+// local shape function i (phi_j(node_i) = delta_ij).
+void NodeCoords(bool is_quad, int degree, std::vector<double>& xy);
 
 // df32 tables (pairs of floats; offsets in pairs):
 //   R[E][4]    folded sums sum_k w_k {g_i0 g_j0, g_i0 g_j1 + g_i1 g_j0, g_i1 g_j1, phi_i phi_j}

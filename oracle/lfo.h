@@ -236,4 +236,41 @@ void NodalProjection(const DofHandler& dh, int degree,
                      const std::function<double(double, double)>& u,
                      std::vector<double>& out);
 
+// ------------------------------------------------------ post-processing ----
+// Gauss-Jacobi points/weights for alpha = 1, beta = 0 on [-1, 1]
+// (quad/gauss_quadrature.cc:71-196).
+void GaussJacobi10(int n, std::vector<double>& pts, std::vector<double>& wts);
+// Exact gradient of a built-in analytic function (out[0], out[1]).
+std::function<void(double, double, double*)> AnalyticGradient(int func_id, const double* p);
+
+// The integrands the GPU library offers in closed form, over a mesh function
+// u (with its gradient) and an FE function u_h = MeshFunctionFE(dh, dofs)
+// (dofs null: u_h = 0):
+//   kind 0: u_h + u            kind 1: (u_h - u)^2 (squaredNorm(mf_fe - mf_u))
+//   kind 2: |grad u_h - grad u|^2 (squaredNorm(mf_grad_fe - mf_grad_u))
+struct Integrand {
+  int kind = 0;
+  MeshFunction u;
+  std::function<void(double, double, double*)> grad_u;  // analytic u only
+  const DofHandler* dh = nullptr;
+  int degree = 0;
+  const double* dofs = nullptr;
+};
+// IntegrateMeshFunction (fe/fe_tools.h:110-165) with make_QuadRule(., qdeg)
+// per reference element; flags select entities of the given codim (null:
+// all).  As in the reference, entity 0 is always counted.
+double IntegrateMeshFunction(const Mesh& m, const Integrand& g, int qdeg, const uint8_t* flags, int codim);
+// MeshFunctionFE / MeshFunctionGradFE (fe/mesh_function_fe.h:72-91,
+// fe/mesh_function_grad_fe.h:93-118) on one cell at reference points xy.
+void EvalFE(const DofHandler& dh, int degree, const double* dofs, idx_t cell, const std::vector<double>& xy,
+            double* vals, double* grads);
+// NodalProjection (fe/fe_tools.h:198-259) of a mesh function, cells selected
+// by flags (null: all); a dof shared by cells gets the last cell's value.
+void NodalProjectionMF(const DofHandler& dh, int degree, const MeshFunction& u, const uint8_t* cell_flags,
+                       std::vector<double>& out);
+// InitEssentialConditionFromFunction (fe/fe_tools.h:263-329) over the edges
+// selected by edge_flags.
+void InitEssentialCondition(const DofHandler& dh, int degree, const uint8_t* edge_flags, const MeshFunction& g,
+                            std::vector<uint8_t>& flags, std::vector<double>& vals);
+
 }  // namespace lfo

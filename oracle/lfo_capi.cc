@@ -322,6 +322,66 @@ int lfo_assemble_edge_load(void* sp, const lfo_coeff* g, const uint8_t* flags, i
   LFO_CATCH
 }
 
+// Post-processing: IntegrateMeshFunction over an integrand of the closed set
+// (kind 0: u_h + u, 1: (u_h - u)^2, 2: |grad u_h - grad u|^2; dofs null: u_h
+// = 0), over cells (codim 0) or edges (codim 1).
+int lfo_integrate(void* sp, int kind, const lfo_coeff* u, const double* dofs, int qdeg, const uint8_t* flags,
+                  int codim, double* out, char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  Integrand g;
+  g.kind = kind;
+  size_t nd = 0;
+  if (u && u->kind == MeshFunction::kNodalO1) nd = m.num_nodes;
+  else nd = codim == 0 ? m.num_cells : m.num_edges;
+  g.u = ToMF(u, nd);
+  if (u && u->kind == MeshFunction::kAnalytic) g.grad_u = AnalyticGradient(u->func, u->p);
+  g.dh = &s->dh;
+  g.degree = s->degree;
+  g.dofs = dofs;
+  *out = IntegrateMeshFunction(m, g, qdeg, flags, codim);
+  LFO_CATCH
+}
+
+// MeshFunctionFE / MeshFunctionGradFE on every cell at npts reference points:
+// vals[cell][k], grads[cell][k][2] (either may be null).
+int lfo_eval_fe(void* sp, const double* dofs, int npts, const double* xy, double* vals, double* grads, char* err,
+                int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const std::vector<double> pts(xy, xy + 2 * npts);
+  for (idx_t c = 0; c < s->mesh->num_cells; ++c)
+    EvalFE(s->dh, s->degree, dofs, c, pts, vals ? vals + c * npts : nullptr, grads ? grads + 2 * c * npts : nullptr);
+  LFO_CATCH
+}
+
+int lfo_nodal_projection_mf(void* sp, const lfo_coeff* u, const uint8_t* cell_flags, double* out, char* err,
+                            int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(u, u && u->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  std::vector<double> v;
+  NodalProjectionMF(s->dh, s->degree, mf, cell_flags, v);
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
+  LFO_CATCH
+}
+
+int lfo_init_essential(void* sp, const uint8_t* edge_flags, const lfo_coeff* g, uint8_t* flags, double* vals,
+                       char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(g, g && g->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_edges);
+  std::vector<uint8_t> f;
+  std::vector<double> v;
+  InitEssentialCondition(s->dh, s->degree, edge_flags, mf, f, v);
+  std::memcpy(flags, f.data(), f.size());
+  std::memcpy(vals, v.data(), v.size() * sizeof(double));
+  LFO_CATCH
+}
+
 int lfo_assemble_tabulated(void* sp, const double* elem, int ld, double* vec_elem, double* b,
                            void** out, char* err, int errlen) {
   LFO_TRY

@@ -44,6 +44,68 @@ void GaussLegendre(int n, std::vector<double>& pts, std::vector<double>& wts) {
   }
 }
 
+// lib/lf/quad/gauss_quadrature.cc:71-196 for alpha = 1, beta = 0: roots of
+// P_n^(1,0) bracketed by a sign scan on a fine grid, then bisection and a
+// Newton polish on the three-term recurrence (long double); weights are the
+// Christoffel numbers 4 / ((1 - z^2) P_n'(z)^2).
+namespace {
+void Jacobi10(int n, long double z, long double& pn, long double& pn1) {
+  // (m+1)(2m-1) P_m = ((4m^2-1) z + 1) P_{m-1} - (m-1)(2m+1) P_{m-2}
+  long double a = 0.0L, b = 1.0L;  // P_{-1}, P_0
+  for (int m = 1; m <= n; ++m) {
+    const long double c = (((4.0L * m * m - 1.0L) * z + 1.0L) * b - (m - 1.0L) * (2.0L * m + 1.0L) * a) /
+                          ((m + 1.0L) * (2.0L * m - 1.0L));
+    a = b;
+    b = c;
+  }
+  pn = b;
+  pn1 = a;
+}
+}  // namespace
+
+void GaussJacobi10(int n, std::vector<double>& pts, std::vector<double>& wts) {
+  if (n <= 0) throw Error("GaussJacobi: num_points must be positive");
+  pts.clear();
+  wts.clear();
+  const int K = 64 * n * n + 64;
+  long double zl = -1.0L, pl, q;
+  Jacobi10(n, zl, pl, q);
+  for (int k = 1; k <= K; ++k) {
+    const long double zr = -1.0L + 2.0L * k / K;
+    long double pr;
+    Jacobi10(n, zr, pr, q);
+    if ((pl < 0) != (pr < 0) || pr == 0.0L) {
+      long double lo = zl, hi = zr, plo = pl;
+      for (int it = 0; it < 200 && hi - lo > 1e-20L; ++it) {
+        const long double mid = 0.5L * (lo + hi);
+        long double pm;
+        Jacobi10(n, mid, pm, q);
+        if ((pm < 0) == (plo < 0)) { lo = mid; plo = pm; } else hi = mid;
+      }
+      long double z = 0.5L * (lo + hi), pn, pn1;
+      Jacobi10(n, z, pn, pn1);
+      const long double dp = (n * (1.0L - (2.0L * n + 1.0L) * z) * pn + 2.0L * n * (n + 1.0L) * pn1) /
+                             ((2.0L * n + 1.0L) * (1.0L - z * z));
+      if (dp != 0.0L) z -= pn / dp;
+      Jacobi10(n, z, pn, pn1);
+      const long double d2 = (n * (1.0L - (2.0L * n + 1.0L) * z) * pn + 2.0L * n * (n + 1.0L) * pn1) /
+                             ((2.0L * n + 1.0L) * (1.0L - z * z));
+      pts.push_back(static_cast<double>(z));
+      wts.push_back(static_cast<double>(4.0L / ((1.0L - z * z) * d2 * d2)));
+      if (pr == 0.0L) {  // skip past an exact grid root
+        ++k;
+        Jacobi10(n, -1.0L + 2.0L * k / K, pr, q);
+        zl = -1.0L + 2.0L * k / K;
+        pl = pr;
+        continue;
+      }
+    }
+    zl = zr;
+    pl = pr;
+  }
+  if (static_cast<int>(pts.size()) != n) throw Error("GaussJacobi: root isolation failed");
+}
+
 // lib/lf/quad/make_quad_rule.cc:21-157.
 QuadRule MakeQuadRule(bool is_quad, int degree) {
   QuadRule qr;
@@ -64,9 +126,27 @@ QuadRule MakeQuadRule(bool is_quad, int degree) {
   }
   int d = degree;
   if (d == 3) d = 4;  // make_quad_rule.cc:44-46
-  if (d < 1 || d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0)
-    throw Error("MakeQuadRule: triangle rule of degree " + std::to_string(degree) +
-                " is not tabulated in the oracle");
+  if (d < 1 || d > kTriaRuleMaxDegree || kTriaRuleIndex[d][0] == 0) {
+    // make_quad_rule.cc:139-152: the collapsed (conical) Gauss rule with
+    // n = degree/2 + 1 Gauss-Legendre points u_a (slow) and Gauss-Jacobi(1,0)
+    // points (fast) mapped to [0,1]: x = u_a (1 - s_b), y = s_b,
+    // w = W_a w_b / 4.  (The reference's tables for degrees 9..50 are not
+    // restated; the oracle uses this rule for every untabulated degree.)
+    if (degree < 0) throw Error("MakeQuadRule: negative degree");
+    const int n = degree / 2 + 1;
+    std::vector<double> u, W, t, w;
+    GaussLegendre(n, u, W);
+    GaussJacobi10(n, t, w);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        const double s = (t[b] + 1.0) / 2.0;
+        qr.x.push_back(u[a] * (1.0 - s));
+        qr.y.push_back(s);
+        qr.w.push_back(W[a] * (w[b] * 0.25));
+      }
+    qr.degree = 2 * n - 1;
+    return qr;
+  }
   const int np = kTriaRuleIndex[d][0], off = kTriaRuleIndex[d][1];
   for (int k = 0; k < np; ++k) {
     qr.x.push_back(kTriaRuleRows[off + k][0]);
@@ -546,6 +626,59 @@ std::function<double(double, double)> AnalyticFunction(int func_id, const double
       return [q, pi](double x, double y) {
         return q[0] + q[1] * (std::sin(q[2] * pi * x) * std::cos(q[3] * pi * y));
       };
+    case 4:  // p0 + p1 exp(p2 + p3 x + p4 y + p5 x y)
+      return [q](double x, double y) {
+        return q[0] + q[1] * std::exp(q[2] + q[3] * x + q[4] * y + q[5] * (x * y));
+      };
+    case 5:  // p0 + (p1 + p2 x + p3 y + p4 x y) sin(pi (p5 x + p6)) sin(pi (p7 y + p8))
+      return [q, pi](double x, double y) {
+        const double l = q[1] + q[2] * x + q[3] * y + q[4] * (x * y);
+        return q[0] + l * (std::sin(pi * (q[5] * x + q[6])) * std::sin(pi * (q[7] * y + q[8])));
+      };
+    default:
+      throw Error("unknown analytic function id " + std::to_string(func_id));
+  }
+}
+
+std::function<void(double, double, double*)> AnalyticGradient(int func_id, const double* p) {
+  std::vector<double> q(p, p + 16);
+  const double pi = 3.14159265358979323846;
+  switch (func_id) {
+    case 1:
+      return [q](double x, double y, double* g) {
+        double xi[4] = {1, x, x * x, x * x * x}, yj[4] = {1, y, y * y, y * y * y};
+        g[0] = g[1] = 0.0;
+        for (int i = 0; i < 4; ++i)
+          for (int j = 0; j < 4; ++j) {
+            if (i > 0) g[0] += q[4 * i + j] * (i * xi[i - 1] * yj[j]);
+            if (j > 0) g[1] += q[4 * i + j] * (xi[i] * j * yj[j - 1]);
+          }
+      };
+    case 2:
+      return [q, pi](double x, double y, double* g) {
+        const double ax = q[2] * pi * x, ay = q[3] * pi * y;
+        g[0] = q[1] * q[2] * pi * std::cos(ax) * std::sin(ay);
+        g[1] = q[1] * q[3] * pi * std::sin(ax) * std::cos(ay);
+      };
+    case 3:
+      return [q, pi](double x, double y, double* g) {
+        const double ax = q[2] * pi * x, ay = q[3] * pi * y;
+        g[0] = q[1] * q[2] * pi * std::cos(ax) * std::cos(ay);
+        g[1] = -q[1] * q[3] * pi * std::sin(ax) * std::sin(ay);
+      };
+    case 4:
+      return [q](double x, double y, double* g) {
+        const double e = q[1] * std::exp(q[2] + q[3] * x + q[4] * y + q[5] * (x * y));
+        g[0] = e * (q[3] + q[5] * y);
+        g[1] = e * (q[4] + q[5] * x);
+      };
+    case 5:
+      return [q, pi](double x, double y, double* g) {
+        const double l = q[1] + q[2] * x + q[3] * y + q[4] * (x * y);
+        const double ax = pi * (q[5] * x + q[6]), ay = pi * (q[7] * y + q[8]);
+        g[0] = (q[2] + q[4] * y) * std::sin(ax) * std::sin(ay) + l * pi * q[5] * std::cos(ax) * std::sin(ay);
+        g[1] = (q[3] + q[4] * x) * std::sin(ax) * std::sin(ay) + l * std::sin(ax) * pi * q[7] * std::cos(ay);
+      };
     default:
       throw Error("unknown analytic function id " + std::to_string(func_id));
   }
@@ -892,6 +1025,201 @@ void NodalProjection(const DofHandler& dh, int degree,
       double X[2];
       g.Global(nodes[2 * j], nodes[2 * j + 1], X);
       out[dofs[j]] = u(X[0], X[1]);
+    }
+  }
+}
+
+// ====================================================== post-processing ====
+
+namespace {
+// u and grad u of a mesh function at reference point (xh, yh) of a cell
+// (grad only where defined: analytic families, O1 interpolant; cell-wise
+// constants have zero gradient).
+void MFPoint(const MeshFunction& u, const std::function<void(double, double, double*)>& grad_u, const Mesh& m,
+             idx_t c, const CellGeom& geo, double xh, double yh, double* val, double* grad) {
+  double X[2];
+  geo.Global(xh, yh, X);
+  double g[2] = {0.0, 0.0};
+  double v = 0.0;
+  switch (u.kind) {
+    case MeshFunction::kZero: break;
+    case MeshFunction::kConstant: v = u.value; break;
+    case MeshFunction::kPerCell: v = u.data[c]; break;
+    case MeshFunction::kPerCellExp: v = std::exp(u.data[c]); break;
+    case MeshFunction::kNodalO1: {
+      double phi[16], dphi[16][2], JT[2][2];
+      EvalShape(m.IsQuad(c), 1, xh, yh, phi, dphi);
+      double gh[2] = {0.0, 0.0};
+      for (int j = 0; j < m.NumVerts(c); ++j) {
+        const double d = u.data[m.cell_nodes[c][j]];
+        v += d * phi[j];
+        gh[0] += d * dphi[j][0];
+        gh[1] += d * dphi[j][1];
+      }
+      geo.JinvT(xh, yh, JT);
+      g[0] = JT[0][0] * gh[0] + JT[0][1] * gh[1];
+      g[1] = JT[1][0] * gh[0] + JT[1][1] * gh[1];
+      break;
+    }
+    case MeshFunction::kAnalytic:
+      v = u.fn(X[0], X[1]);
+      if (grad && grad_u) grad_u(X[0], X[1], g);
+      break;
+    default: throw Error("bad mesh function kind");
+  }
+  *val = v;
+  if (grad) { grad[0] = g[0]; grad[1] = g[1]; }
+}
+
+// u_h and grad u_h (mesh_function_fe.h:72-91, mesh_function_grad_fe.h:93-118)
+void FEPoint(const DofHandler& dh, int degree, const double* dofs, idx_t c, const CellGeom& geo, double xh,
+             double yh, double* val, double* grad) {
+  const bool q = dh.mesh->IsQuad(c);
+  double phi[16], dphi[16][2], JT[2][2];
+  EvalShape(q, degree, xh, yh, phi, dphi);
+  const idx_t* d = dh.GlobalDofIndices(c);
+  double v = 0.0, gh[2] = {0.0, 0.0};
+  for (int i = 0; i < dh.NumLocalDofs(c); ++i) {
+    v += dofs[d[i]] * phi[i];
+    gh[0] += dofs[d[i]] * dphi[i][0];
+    gh[1] += dofs[d[i]] * dphi[i][1];
+  }
+  *val = v;
+  if (grad) {
+    geo.JinvT(xh, yh, JT);
+    grad[0] = JT[0][0] * gh[0] + JT[0][1] * gh[1];
+    grad[1] = JT[1][0] * gh[0] + JT[1][1] * gh[1];
+  }
+}
+
+double IntegrandAt(const Integrand& g, const Mesh& m, idx_t c, const CellGeom& geo, double xh, double yh) {
+  const bool need_grad = g.kind == 2;
+  double uv = 0.0, ug[2] = {0.0, 0.0}, hv = 0.0, hg[2] = {0.0, 0.0};
+  MFPoint(g.u, g.grad_u, m, c, geo, xh, yh, &uv, need_grad ? ug : nullptr);
+  if (g.dofs) FEPoint(*g.dh, g.degree, g.dofs, c, geo, xh, yh, &hv, need_grad ? hg : nullptr);
+  switch (g.kind) {
+    case 0: return hv + uv;
+    case 1: return (hv - uv) * (hv - uv);
+    case 2: {
+      const double a = hg[0] - ug[0], b = hg[1] - ug[1];
+      return a * a + b * b;
+    }
+  }
+  throw Error("bad integrand kind");
+}
+
+// LocalIntegral (fe_tools.h:35-68): values . (weights .* IntegrationElement)
+double LocalCell(const Integrand& g, const Mesh& m, idx_t c, const QuadRule& qt, const QuadRule& qq) {
+  const CellGeom geo = m.Geom(c);
+  const QuadRule& qr = m.IsQuad(c) ? qq : qt;
+  double s = 0.0;
+  for (int k = 0; k < qr.n(); ++k)
+    s += IntegrandAt(g, m, c, geo, qr.x[k], qr.y[k]) * (qr.w[k] * geo.IntegrationElement(qr.x[k], qr.y[k]));
+  return s;
+}
+
+double LocalEdge(const Integrand& g, const Mesh& m, idx_t e, const std::vector<double>& t,
+                 const std::vector<double>& w) {
+  const idx_t a = m.edge_nodes[e][0], b = m.edge_nodes[e][1];
+  const double len = std::hypot(m.xy[2 * b] - m.xy[2 * a], m.xy[2 * b + 1] - m.xy[2 * a + 1]);
+  std::vector<double> uv;
+  EvalOnEdge(g.u, m, e, t, uv);
+  const int n = g.dofs ? g.dh->n_edge : 0;
+  std::vector<double> phi(n);
+  double s = 0.0;
+  for (size_t k = 0; k < t.size(); ++k) {
+    double hv = 0.0;
+    if (g.dofs) {
+      EvalSegmentShape(g.degree, t[k], phi.data());
+      const idx_t* d = &g.dh->edge_dofs[e * n];
+      for (int i = 0; i < n; ++i) hv += g.dofs[d[i]] * phi[i];
+    }
+    const double v = g.kind == 0 ? hv + uv[k] : (hv - uv[k]) * (hv - uv[k]);
+    s += v * (w[k] * len);
+  }
+  return s;
+}
+}  // namespace
+
+double IntegrateMeshFunction(const Mesh& m, const Integrand& g, int qdeg, const uint8_t* flags, int codim) {
+  if (codim == 0) {
+    const QuadRule qt = MakeQuadRule(false, qdeg), qq = MakeQuadRule(true, qdeg);
+    if (m.num_cells == 0) return 0.0;
+    // fe_tools.h:117-124: entity 0 starts the sum unconditionally
+    double r = LocalCell(g, m, 0, qt, qq);
+    for (idx_t c = 1; c < m.num_cells; ++c) {
+      if (flags && !flags[c]) continue;
+      r = r + LocalCell(g, m, c, qt, qq);
+    }
+    return r;
+  }
+  if (codim != 1) throw Error("IntegrateMeshFunction: codim must be 0 or 1");
+  if (g.kind == 2) throw Error("IntegrateMeshFunction: gradients on edges are not supported");
+  std::vector<double> t, w;
+  GaussLegendre(qdeg / 2 + 1, t, w);
+  if (m.num_edges == 0) return 0.0;
+  double r = LocalEdge(g, m, 0, t, w);
+  for (idx_t e = 1; e < m.num_edges; ++e) {
+    if (flags && !flags[e]) continue;
+    r = r + LocalEdge(g, m, e, t, w);
+  }
+  return r;
+}
+
+void EvalFE(const DofHandler& dh, int degree, const double* dofs, idx_t cell, const std::vector<double>& xy,
+            double* vals, double* grads) {
+  const CellGeom geo = dh.mesh->Geom(cell);
+  const size_t np = xy.size() / 2;
+  for (size_t k = 0; k < np; ++k) {
+    double v, g[2];
+    FEPoint(dh, degree, dofs, cell, geo, xy[2 * k], xy[2 * k + 1], &v, grads ? g : nullptr);
+    if (vals) vals[k] = v;
+    if (grads) { grads[2 * k] = g[0]; grads[2 * k + 1] = g[1]; }
+  }
+}
+
+void NodalProjectionMF(const DofHandler& dh, int degree, const MeshFunction& u, const uint8_t* cell_flags,
+                       std::vector<double>& out) {
+  out.assign(dh.num_dofs, 0.0);
+  std::vector<double> nodes;
+  const Mesh& m = *dh.mesh;
+  for (idx_t c = 0; c < m.num_cells; ++c) {
+    if (cell_flags && !cell_flags[c]) continue;
+    EvaluationNodes(m.IsQuad(c), degree, nodes);
+    QuadRule pts;  // the evaluation nodes as points of a (weightless) rule
+    pts.x.resize(nodes.size() / 2);
+    pts.y.resize(nodes.size() / 2);
+    pts.w.assign(nodes.size() / 2, 0.0);
+    for (size_t j = 0; j < nodes.size() / 2; ++j) {
+      pts.x[j] = nodes[2 * j];
+      pts.y[j] = nodes[2 * j + 1];
+    }
+    std::vector<double> v;
+    u.Eval(m, c, pts, v);
+    const idx_t* d = dh.GlobalDofIndices(c);
+    // NodalValuesToDofs of a Lagrangian element is the identity; "setting,
+    // not adding": a later cell overwrites a shared dof
+    for (int j = 0; j < dh.NumLocalDofs(c); ++j) out[d[j]] = v[j];
+  }
+}
+
+void InitEssentialCondition(const DofHandler& dh, int degree, const uint8_t* edge_flags, const MeshFunction& g,
+                            std::vector<uint8_t>& flags, std::vector<double>& vals) {
+  flags.assign(dh.num_dofs, 0);
+  vals.assign(dh.num_dofs, 0.0);
+  const Mesh& m = *dh.mesh;
+  const int n = dh.n_edge;
+  // segment evaluation nodes: 0, 1, then the interior nodes 1/p .. (p-1)/p
+  std::vector<double> t = {0.0, 1.0};
+  for (int a = 1; a < degree; ++a) t.push_back(static_cast<double>(a) / degree);
+  std::vector<double> v;
+  for (idx_t e = 0; e < m.num_edges; ++e) {
+    if (edge_flags && !edge_flags[e]) continue;
+    EvalOnEdge(g, m, e, t, v);
+    const idx_t* d = &dh.edge_dofs[e * n];
+    for (int i = 0; i < n; ++i) {
+      flags[d[i]] = 1;
+      vals[d[i]] = v[i];
     }
   }
 }

@@ -17,7 +17,8 @@ _lib = None
 _lock = threading.Lock()
 
 ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
-FN_POLY, FN_SINSIN, FN_SINCOS = 1, 2, 3
+FN_POLY, FN_SINSIN, FN_SINCOS, FN_EXP, FN_TRIG = 1, 2, 3, 4, 5
+INT_VALUE, INT_SQ_DIFF, INT_GRAD_SQ_DIFF = 0, 1, 2
 
 
 def build(force=False):
@@ -91,6 +92,12 @@ def lib():
             L.lfo_csr_destroy.argtypes = [vp]
             L.lfo_nodal_projection.argtypes = [vp, C.c_int, P(dp), P(dp), C.c_char_p, C.c_int]
             L.lfo_kat_tensor_rd.argtypes = [P(dp), C.c_char_p, C.c_int]
+            L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
+                                        C.c_char_p, C.c_int]
+            L.lfo_eval_fe.argtypes = [vp, P(dp), C.c_int, P(dp), P(dp), P(dp), C.c_char_p, C.c_int]
+            L.lfo_nodal_projection_mf.argtypes = [vp, P(lfo_coeff), P(C.c_uint8), P(dp), C.c_char_p, C.c_int]
+            L.lfo_init_essential.argtypes = [vp, P(C.c_uint8), P(lfo_coeff), P(C.c_uint8), P(dp), C.c_char_p,
+                                             C.c_int]
             _lib = L
     return _lib
 
@@ -404,3 +411,54 @@ def adjoint_gradient(space, theta, f, u_obs, flags, g=None, qdeg_tria=0, qdeg_qu
     lam_m = np.where(flags != 0, 0.0, lam)
     grad = -cellwise_bilinear(space, A, lam_m, u)
     return J, u, lam, grad
+
+
+def _u8(a):
+    if a is None:
+        return None, None
+    a = np.ascontiguousarray(a, np.uint8)
+    return a, _p(a, C.c_uint8)
+
+
+def integrate(space, kind, u=None, dofs=None, qdeg=2, flags=None, codim=0):
+    """IntegrateMeshFunction of the closed integrands (INT_*); u a coeff (None: zero)."""
+    u = coeff(ZERO) if u is None else u
+    d = None if dofs is None else np.ascontiguousarray(dofs, np.float64)
+    fl, flp = _u8(flags)
+    out = C.c_double()
+    err = _err()
+    _check(lib().lfo_integrate(space.h, kind, C.byref(u), _p(d, C.c_double) if d is not None else None, qdeg, flp,
+                               codim, C.byref(out), err, 512), err)
+    return out.value
+
+
+def eval_fe(space, dofs, ref_points, grads=False):
+    """MeshFunctionFE (and MeshFunctionGradFE) on every cell at reference points [k][2]."""
+    pts = np.ascontiguousarray(ref_points, np.float64).reshape(-1, 2)
+    d = np.ascontiguousarray(dofs, np.float64)
+    nc = space.mesh.num_cells
+    vals = np.zeros((nc, len(pts)))
+    g = np.zeros((nc, len(pts), 2)) if grads else None
+    err = _err()
+    _check(lib().lfo_eval_fe(space.h, _p(d, C.c_double), len(pts), _p(pts, C.c_double), _p(vals, C.c_double),
+                             _p(g, C.c_double) if grads else None, err, 512), err)
+    return (vals, g) if grads else vals
+
+
+def nodal_projection_mf(space, u, cell_flags=None):
+    """NodalProjection of a mesh function (coeff) onto a Lagrangian space."""
+    out = np.zeros(space.num_dofs)
+    fl, flp = _u8(cell_flags)
+    err = _err()
+    _check(lib().lfo_nodal_projection_mf(space.h, C.byref(u), flp, _p(out, C.c_double), err, 512), err)
+    return out
+
+
+def init_essential_condition(space, edge_flags, g):
+    """InitEssentialConditionFromFunction: (flags uint8, values) per dof."""
+    fl, flp = _u8(edge_flags)
+    f = np.zeros(space.num_dofs, np.uint8)
+    v = np.zeros(space.num_dofs)
+    err = _err()
+    _check(lib().lfo_init_essential(space.h, flp, C.byref(g), _p(f, C.c_uint8), _p(v, C.c_double), err, 512), err)
+    return f, v

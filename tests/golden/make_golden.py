@@ -8,6 +8,9 @@ reference checkout.  Sources:
                                            36x36 ref_mat (edge_dof_static)
   lib/lf/assemble/test/coomatrix_tests.cc  fix_dof exact solution
   lib/lf/uscalfe/test/lagr_fe_tests.cc     reaction-diffusion bilinear forms
+  lib/lf/fe/test/fe_tools_tests.cc         IntegrateMeshFunction integrals
+  lib/lf/uscalfe/test/gfe_tests.cc         L2 norms on test mesh 3
+  lib/lf/mesh/test_utils/test_meshes.cc    the nodes and triangles of test mesh 3
 
 usage: python tests/golden/make_golden.py /root/reference
 """
@@ -32,6 +35,35 @@ def main():
     at = open(os.path.join(ref, "lib/lf/assemble/test/assembly_tests.cc")).read()
     ct = open(os.path.join(ref, "lib/lf/assemble/test/coomatrix_tests.cc")).read()
     lt = open(os.path.join(ref, "lib/lf/uscalfe/test/lagr_fe_tests.cc")).read()
+
+    ft = open(os.path.join(ref, "lib/lf/fe/test/fe_tools_tests.cc")).read()
+    gt = open(os.path.join(ref, "lib/lf/uscalfe/test/gfe_tests.cc")).read()
+    tm = open(os.path.join(ref, "lib/lf/mesh/test_utils/test_meshes.cc")).read()
+
+    # test mesh 3: the `case 3:` block of GenerateHybrid2DTestMesh
+    blk = tm[tm.index("case 3: {"):]
+    blk = blk[:blk.index("break;")]
+    pts = [[float(a), float(b)] for a, b in
+           re.findall(r"AddPoint\(coord_t\(\{(-?[\d.]+) \* scale, (-?[\d.]+) \* scale\}\)\)", blk)]
+    tris = [[int(a), int(b), int(c)] for a, b, c in
+            re.findall(r"kTria\(\), std::array<size_type, 3>\{\{(\d+), (\d+), (\d+)\}\}", blk)]
+    assert len(pts) == 13 and len(tris) == 15, (len(pts), len(tris))
+
+    def expect(text, var):
+        # EXPECT_FLOAT_EQ(var, <a> / <b>) or (var, <a>.) with base::kPi allowed
+        mm = re.search(r"EXPECT_FLOAT_EQ\(" + re.escape(var) + r", ([^;]+)\);", text)
+        expr = mm.group(1).strip()
+        val = expr.replace("base::kPi", "3.141592653589793")
+        assert re.fullmatch(r"[\d.\s/*3141592653589793]+", val), expr
+        return expr, float(eval(val))  # arithmetic on literals only (checked above)
+
+    fe_kat = {}
+    for var in ("intScalar", "intVec[0]", "intVec[1]", "intMatrixDyn(0, 0)", "intMatrixDyn(0, 1)",
+                "intMatrixDyn(0, 2)", "intMatrixDyn(1, 0)", "intMatrixDyn(1, 1)", "intMatrixDyn(1, 2)"):
+        expr, val = expect(ft, var)
+        fe_kat[var] = {"expr": expr, "value": val}
+    m1 = re.search(r"EXPECT_NEAR\(norm, (5\.\d+), (1E-4)\)", gt)
+    m2 = re.search(r"EXPECT_NEAR\(norm, (7\.\d+), (1E-4)\)", gt)
 
     ref10 = _matrix_after(at, "Eigen::MatrixXd ref_mat(10, 10);", 10)
     ref36 = _matrix_after(at, "Eigen::MatrixXd ref_mat(36, 36);", 36)
@@ -66,6 +98,22 @@ def main():
             "solution": exact,
         },
         "reaction_diffusion_kat": dict(kat, file="lib/lf/uscalfe/test/lagr_fe_tests.cc:807-883"),
+        "test_mesh_3": {
+            "file": "lib/lf/mesh/test_utils/test_meshes.cc:160-224",
+            "nodes": pts, "triangles": tris,
+        },
+        "integrate_mesh_function_kat": {
+            "file": "lib/lf/fe/test/fe_tools_tests.cc:44-85",
+            "mesh": "test mesh 0, scale 1",
+            "integrals": fe_kat,
+            "tolerance": "EXPECT_FLOAT_EQ (4 ulp in float)",
+        },
+        "gfe_norm_kat": {
+            "file": "lib/lf/uscalfe/test/gfe_tests.cc:27-45, 141-160",
+            "mesh": "test mesh 3",
+            "l2norm_x_1my": {"value": float(m1.group(1)), "tolerance": float(m1.group(2))},
+            "l2norm_vf_y_mx": {"value": float(m2.group(1)), "tolerance": float(m2.group(2))},
+        },
     }
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
     with open(path, "w") as f:
