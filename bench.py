@@ -18,6 +18,7 @@ the data path); value = total triplets of all ranks / max time over ranks.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -328,6 +329,58 @@ def edge_leg(L, W, ctx, mesh, space, steps=5):
     return out
 
 
+def post_leg(L, W, ctx, mesh, space, steps=5, cpu_check=False):
+    """Post-processing on the headline mesh (O2): NodalProjection of an
+    analytic u, then the L2 and H1-seminorm error integrals of that u_h
+    against u (IntegrateMeshFunction of squaredNorm(mf_fe - mf_u) and of the
+    gradients, degree-4 rules), FP64.  Compulsory bytes per launch: the cell
+    records (nodes, list index, dof indices), the node coordinates and the dof
+    vector once each."""
+    u = L.coeff(L.ANALYTIC, func=L.FN_SINSIN, params=[0.0, 1.0, 2.0, 3.0])
+    nd = space.num_dofs
+    x = ctx.zeros(nd)
+    L.nodal_projection(space, u, x)
+    ctx.timer_begin()
+    for _ in range(steps):
+        L.nodal_projection(space, u, x)
+    proj_ms = ctx.timer_end() / steps
+    nc, nv = mesh.num_cells, mesh.num_nodes
+    cell_bytes = nc * (16 + 4 + 4 * space.n_cell)
+    compulsory = cell_bytes + nv * 16 + nd * 8
+    out = {"workload": "headline mesh (%d cells, %d dofs), O2, u = sin(2 pi x) sin(3 pi y), degree-4 rules"
+                       % (nc, nd),
+           "nodal_projection": {"ms": proj_ms, "dofs_per_s": nd / (proj_ms * 1e-3)}}
+    for name, kind in (("l2_error", L.INT_SQ_DIFF), ("h1_error", L.INT_GRAD_SQ_DIFF)):
+        val = L.integrate_mesh_function(mesh, kind, u, space, x, 4)
+        ctx.timer_begin()
+        for _ in range(steps):
+            L.integrate_mesh_function(mesh, kind, u, space, x, 4)
+        ms = ctx.timer_end() / steps
+        out[name] = {"value": math.sqrt(val), "ms": ms, "cells_per_s": nc / (ms * 1e-3),
+                     "compulsory_gbs": compulsory / (ms * 1e-3) / 1e9}
+    if cpu_check:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        xy, cells = W.hybrid_mesh(256, seed=2)
+        om = O.Mesh(xy, cells)
+        osp = O.Space(om, 2)
+        ou = O.coeff(O.ANALYTIC, func=O.FN_SINSIN, params=[0.0, 1.0, 2.0, 3.0])
+        t0 = time.perf_counter()
+        c = O.nodal_projection_mf(osp, ou)
+        tp = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.integrate(osp, O.INT_SQ_DIFF, ou, dofs=c, qdeg=4)
+        tl = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.integrate(osp, O.INT_GRAD_SQ_DIFF, ou, dofs=c, qdeg=4)
+        th = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": 1,
+                               "sample": "oracle on a 256x256 hybrid mesh (%d cells), same u and rules" % om.num_cells,
+                               "projection_dofs_per_s": osp.num_dofs / tp, "l2_cells_per_s": om.num_cells / tl,
+                               "h1_cells_per_s": om.num_cells / th}
+    return out
+
+
 def batch_leg(L, W, ctx, count):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
     one persistent assembly launch + load + fix + COO->CSR + batched PCG.
@@ -608,6 +661,7 @@ def run_ours(args):
             return {"error": "%s: %s" % (type(e).__name__, e)}
 
     edges = leg(edge_leg, L, W, ctx, mesh, space)
+    post = leg(post_leg, L, W, ctx, mesh, space, cpu_check=(rank == 0 and not args.no_cpu_baseline))
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size,
                 cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
@@ -643,7 +697,7 @@ def run_ours(args):
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "high_order": high_order, "solve": solve,
+            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "high_order": high_order, "solve": solve,
             "batch": batch,
             "gradient": gradient,
         }

@@ -27,6 +27,15 @@
 //   MassEdgeMatrixProvider, ScalarLoadEdgeVectorProvider (loc_comp_ellbvp.h:367-529,
 //     784-921) with AssembleMatrixLocally / AssembleVectorLocally(1, ...)
 //                                                  the same names; edge selector = device flags
+//   fe::MeshFunctionFE / MeshFunctionGradFE        fe::MeshFunctionFE / fe::MeshFunctionGradFE
+//     (fe/mesh_function_fe.h:44, mesh_function_grad_fe.h:44)  (space + device dof vector; evaluated on
+//                                                    every cell at shared reference points)
+//   fe::IntegrateMeshFunction(mesh, squaredNorm(   fe::IntegrateMeshFunction(mesh, fe::SquaredNormDiff(
+//     mf_fe - mf_u), degree) (fe/fe_tools.h:158)     mf_fe, u), degree[, pred, codim]) and the other
+//                                                    closed integrands (fe::Value, fe::SquaredNorm)
+//   fe::NodalProjection (fe/fe_tools.h:198)        fe::NodalProjection(fes, u[, pred])
+//   fe::InitEssentialConditionFromFunction         fe::InitEssentialConditionFromFunction(fes, edge
+//     (fe/fe_tools.h:263)                            flags, g) -> (flags, values) device vectors
 //   (no counterpart)                               adjoint::InverseConductivityFunction
 //
 // Errors: every failing call throws lf::gb300::Error carrying the lfg_status
@@ -462,6 +471,119 @@ inline void FixFlaggedSolutionComponents(const DeviceVector<uint8_t>& flags, con
 }
 
 }  // namespace assemble
+
+namespace fe {
+
+// An FE function u_h = sum_i dofs[i] b_i of a Lagrangian space; the dof
+// vector is referenced and must outlive the mesh function.
+class MeshFunctionFE {
+ public:
+  MeshFunctionFE(std::shared_ptr<const uscalfe::FeSpaceLagrange> fes, const DeviceVector<double>& dofs)
+      : fes_(std::move(fes)), dofs_(&dofs) {}
+  // Values on every cell at the reference points local_xy (x0, y0, x1, y1, ...):
+  // result[cell * npts + k].
+  DeviceVector<double> operator()(const std::vector<double>& local_xy) const {
+    const int32_t np = static_cast<int32_t>(local_xy.size() / 2);
+    DeviceVector<double> out(fes_->ctx(), static_cast<size_t>(fes_->Mesh()->NumEntities(0)) * np);
+    fes_->ctx().Check(lfg_fe_eval(fes_->get(), dofs_->data(), np, local_xy.data(), out.data(), nullptr));
+    return out;
+  }
+  const uscalfe::FeSpaceLagrange& space() const { return *fes_; }
+  const DeviceVector<double>& dofs() const { return *dofs_; }
+
+ private:
+  std::shared_ptr<const uscalfe::FeSpaceLagrange> fes_;
+  const DeviceVector<double>* dofs_;
+};
+
+class MeshFunctionGradFE {
+ public:
+  MeshFunctionGradFE(std::shared_ptr<const uscalfe::FeSpaceLagrange> fes, const DeviceVector<double>& dofs)
+      : fe_(std::move(fes), dofs) {}
+  // Gradients on every cell at the reference points: result[(cell * npts + k) * 2 + d].
+  DeviceVector<double> operator()(const std::vector<double>& local_xy) const {
+    const int32_t np = static_cast<int32_t>(local_xy.size() / 2);
+    DeviceVector<double> out(fe_.space().ctx(), static_cast<size_t>(fe_.space().Mesh()->NumEntities(0)) * np * 2);
+    fe_.space().ctx().Check(lfg_fe_eval(fe_.space().get(), fe_.dofs().data(), np, local_xy.data(), nullptr,
+                                        out.data()));
+    return out;
+  }
+  const MeshFunctionFE& function() const { return fe_; }
+
+ private:
+  MeshFunctionFE fe_;
+};
+
+// The integrands IntegrateMeshFunction evaluates on the device.
+struct Integrand {
+  lfg_integrand g{};
+};
+// u (a mesh function) and u_h + u
+inline Integrand Value(uscalfe::MeshFunction u) {
+  Integrand i;
+  i.g.kind = LFG_INTEGRAND_VALUE;
+  i.g.u = u.c;
+  return i;
+}
+inline Integrand Value(const MeshFunctionFE& uh, uscalfe::MeshFunction u = uscalfe::MeshFunction::Zero()) {
+  Integrand i = Value(u);
+  i.g.space = uh.space().get();
+  i.g.dofs_dev = uh.dofs().data();
+  return i;
+}
+// squaredNorm(u), squaredNorm(mf_fe - mf_u), squaredNorm(mf_grad_fe - mf_grad_u)
+inline Integrand SquaredNorm(uscalfe::MeshFunction u) {
+  Integrand i;
+  i.g.kind = LFG_INTEGRAND_SQ_DIFF;
+  i.g.u = u.c;
+  return i;
+}
+inline Integrand SquaredNormDiff(const MeshFunctionFE& uh, uscalfe::MeshFunction u) {
+  Integrand i = SquaredNorm(u);
+  i.g.space = uh.space().get();
+  i.g.dofs_dev = uh.dofs().data();
+  return i;
+}
+inline Integrand SquaredNormDiff(const MeshFunctionGradFE& gh, uscalfe::MeshFunction u) {
+  Integrand i = SquaredNormDiff(gh.function(), u);
+  i.g.kind = LFG_INTEGRAND_GRAD_SQ_DIFF;
+  return i;
+}
+inline Integrand SquaredNorm(const MeshFunctionFE& uh) { return SquaredNormDiff(uh, uscalfe::MeshFunction::Zero()); }
+inline Integrand SquaredNorm(const MeshFunctionGradFE& gh) {
+  return SquaredNormDiff(gh, uscalfe::MeshFunction::Zero());
+}
+
+// IntegrateMeshFunction(mesh, mf, quad_degree, pred, codim) (fe/fe_tools.h:158).
+inline double IntegrateMeshFunction(const mesh::Mesh& m, const Integrand& f, int quad_degree,
+                                    const DeviceVector<uint8_t>* pred = nullptr, int codim = 0) {
+  double r = 0.0;
+  m.ctx().Check(lfg_integrate_mesh_function(m.get(), &f.g, quad_degree, pred ? pred->data() : nullptr, codim, &r));
+  return r;
+}
+
+// NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259).
+inline DeviceVector<double> NodalProjection(const uscalfe::FeSpaceLagrange& fes, uscalfe::MeshFunction u,
+                                            const DeviceVector<uint8_t>* pred = nullptr) {
+  DeviceVector<double> out(fes.ctx(), static_cast<size_t>(fes.NumDofs()));
+  fes.ctx().Check(lfg_nodal_projection(fes.get(), &u.c, pred ? pred->data() : nullptr, out.data()));
+  return out;
+}
+
+// InitEssentialConditionFromFunction(fes, esscondflag, g) (fe/fe_tools.h:263-329):
+// the (flag, value) pair per dof as two device vectors, ready for
+// assemble::FixFlaggedSolutionComponents.
+inline std::pair<DeviceVector<uint8_t>, DeviceVector<double>> InitEssentialConditionFromFunction(
+    const uscalfe::FeSpaceLagrange& fes, const DeviceVector<uint8_t>& edge_flags, uscalfe::MeshFunction g) {
+  const size_t nd = static_cast<size_t>(fes.NumDofs());
+  std::pair<DeviceVector<uint8_t>, DeviceVector<double>> out{DeviceVector<uint8_t>(fes.ctx(), nd),
+                                                             DeviceVector<double>(fes.ctx(), nd)};
+  fes.ctx().Check(lfg_init_essential_condition(fes.get(), edge_flags.data(), &g.c, out.first.data(),
+                                               out.second.data()));
+  return out;
+}
+
+}  // namespace fe
 
 namespace adjoint {
 

@@ -21,7 +21,6 @@ struct CoeffDev {
 
 // f(x, y) of a built-in function (LFG_FN_*), FP64.
 __device__ inline double EvalAnalytic(const CoeffDev& f, double x, double y) {
-  const double pi = 3.141592653589793;
   switch (f.func) {
     case LFG_FN_POLY: {
       // Horner in y inside Horner in x: sum_i x^i sum_j p[4i+j] y^j
@@ -33,10 +32,12 @@ __device__ inline double EvalAnalytic(const CoeffDev& f, double x, double y) {
       }
       return s;
     }
+    // sinpi / cospi (sin(pi t) with an exact argument reduction) instead of
+    // sin(p pi t): the same function up to the rounding of p pi t
     case LFG_FN_SINSIN:
-      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * sin(f.p[3] * pi * y));
+      return f.p[0] + f.p[1] * (sinpi(f.p[2] * x) * sinpi(f.p[3] * y));
     case LFG_FN_SINCOS:
-      return f.p[0] + f.p[1] * (sin(f.p[2] * pi * x) * cos(f.p[3] * pi * y));
+      return f.p[0] + f.p[1] * (sinpi(f.p[2] * x) * cospi(f.p[3] * y));
     case LFG_FN_EXP:
       return f.p[0] + f.p[1] * exp(f.p[2] + f.p[3] * x + f.p[4] * y + f.p[5] * (x * y));
     case LFG_FN_TRIG: {
@@ -68,8 +69,8 @@ __device__ inline void EvalAnalyticGrad(const CoeffDev& f, double x, double y, d
     case LFG_FN_SINSIN:
     case LFG_FN_SINCOS: {
       double sx, cx, sy, cy;
-      sincos(f.p[2] * pi * x, &sx, &cx);
-      sincos(f.p[3] * pi * y, &sy, &cy);
+      sincospi(f.p[2] * x, &sx, &cx);
+      sincospi(f.p[3] * y, &sy, &cy);
       if (f.func == LFG_FN_SINSIN) {
         gx = f.p[1] * (f.p[2] * pi) * cx * sy;
         gy = f.p[1] * (f.p[3] * pi) * sx * cy;

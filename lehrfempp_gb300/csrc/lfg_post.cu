@@ -181,6 +181,28 @@ __device__ __forceinline__ double MFPoint(const CoeffDev& u, int c, const int4& 
   return 0.0;
 }
 
+// grad u alone (cell-wise constants: 0).
+template <bool QUAD>
+__device__ __forceinline__ void MFGrad(const CoeffDev& u, const int4& cn, double xh, double yh, double X, double Y,
+                                       const double (&JT)[2][2], double& gx, double& gy) {
+  gx = gy = 0.0;
+  if (u.kind == LFG_COEFF_ANALYTIC) {
+    EvalAnalyticGrad(u, X, Y, gx, gy);
+  } else if (u.kind == LFG_COEFF_NODAL_O1) {
+    double hx, hy;
+    if (!QUAD) {
+      hx = u.data[cn.y] - u.data[cn.x];
+      hy = u.data[cn.z] - u.data[cn.x];
+    } else {
+      const double d0 = u.data[cn.x], d1 = u.data[cn.y], d2 = u.data[cn.z], d3 = u.data[cn.w];
+      hx = (d1 - d0) * (1 - yh) + (d2 - d3) * yh;
+      hy = (d3 - d0) * (1 - xh) + (d2 - d1) * xh;
+    }
+    gx = JT[0][0] * hx + JT[0][1] * hy;
+    gy = JT[1][0] * hx + JT[1][1] * hy;
+  }
+}
+
 // Deterministic block sum of one double per thread into part[blockIdx.x].
 __device__ __forceinline__ void BlockSumTo(double s, double* part) {
   __shared__ double red[kPostBlock];
@@ -200,13 +222,15 @@ __host__ __device__ constexpr int LocalDofs() {
   return DEG == 0 ? 0 : QUAD ? (DEG + 1) * (DEG + 1) : (DEG + 1) * (DEG + 2) / 2;
 }
 
-// DEG: degree of the FE part (0: no u_h), fixing the local dof count.
-template <bool QUAD, int DEG>
+// DEG: degree of the FE part (0: no u_h), fixing the local dof count; KIND:
+// the integrand (compile time, so the value or the gradient of u that the
+// integrand does not use is never computed).
+template <bool QUAD, int DEG, int KIND>
 __global__ void __launch_bounds__(kPostBlock) IntegrateCellsKernel(PostArgs a, CellSide s, double* part) {
   constexpr int N = LocalDofs<QUAD, DEG>();
+  constexpr bool need_grad = KIND == LFG_INTEGRAND_GRAD_SQ_DIFF;
   const double* __restrict__ tab = s.tab;
   const PostTab L = s.L;
-  const bool need_grad = a.kind == LFG_INTEGRAND_GRAD_SQ_DIFF;
   double acc = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < s.count;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -223,21 +247,23 @@ __global__ void __launch_bounds__(kPostBlock) IntegrateCellsKernel(PostArgs a, C
       const double xh = tab[L.off_x + k], yh = tab[L.off_y + k];
       double X, Y, ie, JT[2][2];
       Geometry<QUAD>(v, xh, yh, X, Y, ie, JT);
-      double gx, gy;
-      const double uv = MFPoint<QUAD>(a.u, c, cn, xh, yh, X, Y, JT, need_grad, gx, gy);
+      double gx, gy, uv = 0.0;
+      if (need_grad) MFGrad<QUAD>(a.u, cn, xh, yh, X, Y, JT, gx, gy);
+      else uv = MFPoint<QUAD>(a.u, c, cn, xh, yh, X, Y, JT, false, gx, gy);
       double hv = 0.0, hx = 0.0, hy = 0.0;
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        hv += d[j] * tab[L.off_phi + k * N + j];
         if (need_grad) {
           hx += d[j] * tab[L.off_g + (k * N + j) * 2];
           hy += d[j] * tab[L.off_g + (k * N + j) * 2 + 1];
+        } else {
+          hv += d[j] * tab[L.off_phi + k * N + j];
         }
       }
       double val;
-      if (a.kind == LFG_INTEGRAND_VALUE) {
+      if (KIND == LFG_INTEGRAND_VALUE) {
         val = hv + uv;
-      } else if (a.kind == LFG_INTEGRAND_SQ_DIFF) {
+      } else if (KIND == LFG_INTEGRAND_SQ_DIFF) {
         val = (hv - uv) * (hv - uv);
       } else {
         const double ex = (JT[0][0] * hx + JT[0][1] * hy) - gx;
@@ -444,13 +470,22 @@ __global__ void FillI32Kernel(int64_t n, int32_t v, int32_t* __restrict__ p) {
     p[i] = v;
 }
 
+template <bool QUAD, int KIND>
+void LaunchCellsK(int deg, int grid, cudaStream_t st, const PostArgs& a, const CellSide& s, double* part) {
+  switch (deg) {
+    case 0: IntegrateCellsKernel<QUAD, 0, KIND><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
+    case 1: IntegrateCellsKernel<QUAD, 1, KIND><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
+    case 2: IntegrateCellsKernel<QUAD, 2, KIND><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
+    default: IntegrateCellsKernel<QUAD, 3, KIND><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
+  }
+}
+
 template <bool QUAD>
 void LaunchCells(int deg, int grid, cudaStream_t st, const PostArgs& a, const CellSide& s, double* part) {
-  switch (deg) {
-    case 0: IntegrateCellsKernel<QUAD, 0><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
-    case 1: IntegrateCellsKernel<QUAD, 1><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
-    case 2: IntegrateCellsKernel<QUAD, 2><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
-    default: IntegrateCellsKernel<QUAD, 3><<<grid, kPostBlock, 0, st>>>(a, s, part); break;
+  switch (a.kind) {
+    case LFG_INTEGRAND_VALUE: LaunchCellsK<QUAD, LFG_INTEGRAND_VALUE>(deg, grid, st, a, s, part); break;
+    case LFG_INTEGRAND_SQ_DIFF: LaunchCellsK<QUAD, LFG_INTEGRAND_SQ_DIFF>(deg, grid, st, a, s, part); break;
+    default: LaunchCellsK<QUAD, LFG_INTEGRAND_GRAD_SQ_DIFF>(deg, grid, st, a, s, part); break;
   }
 }
 

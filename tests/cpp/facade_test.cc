@@ -172,6 +172,58 @@ static void CheckEdges(const g::Context& ctx) {
   std::printf("edges: %lld boundary edges, mass sum %.6f, load sum %.6f\n", static_cast<long long>(nb), msum, bsum);
 }
 
+// The demo's post-processing (homDir_linfe_demo.cc:150-188): Dirichlet data
+// from InitEssentialConditionFromFunction, solve, then the L2 and H1-seminorm
+// errors through the fe:: facade; O2 interpolation of a quadratic is exact.
+static void CheckPost(const g::Context& ctx) {
+  // u = x(1-x)y(1-y) + 1 + x, -lap u = 2 (x(1-x) + y(1-y))
+  const std::vector<double> pu = {1, 0, 0, 0, 1, 1, -1, 0, 0, -1, 1, 0, 0, 0, 0, 0};
+  const std::vector<double> pf = {0, 2, -2, 0, 2, 0, 0, 0, -2, 0, 0, 0, 0, 0, 0, 0};
+  double err[2][2];
+  for (int r = 0; r < 2; ++r) {
+    const int n = 16 << r;
+    auto mesh = g::mesh::TPTriagMeshBuilder(ctx).setNumXCells(n).setNumYCells(n).Build();
+    auto fes = g::uscalfe::FeSpaceLagrangeO<1>(mesh);
+    const int64_t nd = fes->NumDofs(), ne = mesh->NumEntities(1);
+    g::DeviceVector<uint8_t> nfd(ctx, mesh->NumEntities(2)), efd(ctx, ne);
+    ctx.Check(lfg_mesh_boundary_flags(mesh->get(), nfd.data(), efd.data()));
+    const auto u = g::uscalfe::MeshFunction::Analytic(LFG_FN_POLY, pu);
+    auto ess = g::fe::InitEssentialConditionFromFunction(*fes, efd, u);
+    g::uscalfe::ReactionDiffusionElementMatrixProvider ep(fes, g::uscalfe::MeshFunction::Constant(1.0),
+                                                          g::uscalfe::MeshFunction::Zero());
+    g::uscalfe::ScalarLoadElementVectorProvider lp(fes, g::uscalfe::MeshFunction::Analytic(LFG_FN_POLY, pf));
+    g::assemble::COOMatrix A(ctx, nd, nd, fes->NumTriplets() + nd);
+    g::assemble::AssembleMatrixLocally(0, *fes, *fes, ep, A);
+    g::DeviceVector<double> b(ctx, nd);
+    b.SetZero();
+    g::assemble::AssembleVectorLocally(0, *fes, lp, b);
+    g::assemble::FixFlaggedSolutionComponents(ess.first, ess.second, A, b);
+    auto csr = A.makeSparse();
+    g::DeviceVector<double> x(ctx, nd);
+    x.SetZero();
+    g::solve::SolveOptions so;
+    so.rtol = 1e-12;
+    g::solve::SolvePCG(ctx, csr, b, x, so);
+    const g::fe::MeshFunctionFE mf_sol(fes, x);
+    const g::fe::MeshFunctionGradFE mf_grad_sol(fes, x);
+    err[r][0] = std::sqrt(g::fe::IntegrateMeshFunction(*mesh, g::fe::SquaredNormDiff(mf_sol, u), 4));
+    err[r][1] = std::sqrt(g::fe::IntegrateMeshFunction(*mesh, g::fe::SquaredNormDiff(mf_grad_sol, u), 4));
+    // the projection of u onto O2 on the same mesh: exact for the quadratic part only
+    auto fes2 = g::uscalfe::FeSpaceLagrangeO<2>(mesh);
+    const auto lin = g::uscalfe::MeshFunction::Analytic(LFG_FN_POLY, {1, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+    auto c2 = g::fe::NodalProjection(*fes2, lin);
+    const g::fe::MeshFunctionFE mf2(fes2, c2);
+    const double e2 = g::fe::IntegrateMeshFunction(*mesh, g::fe::SquaredNormDiff(mf2, lin), 4);
+    CHECK(e2 < 1e-28, "O2 projection of 1 + x is not exact: %.3g", e2);
+    const auto vals = mf2({0.25, 0.25});
+    CHECK(vals.size() == static_cast<size_t>(mesh->NumEntities(0)), "MeshFunctionFE output size");
+  }
+  const double rl2 = std::log2(err[0][0] / err[1][0]), rh1 = std::log2(err[0][1] / err[1][1]);
+  CHECK(std::fabs(rl2 - 2.0) < 0.2 && std::fabs(rh1 - 1.0) < 0.15, "error rates L2 %.3f H1 %.3f", rl2, rh1);
+  std::printf("post: L2 errors %.3e %.3e (rate %.2f), H1 %.3e %.3e (rate %.2f)\n", err[0][0], err[1][0], rl2,
+              err[0][1], err[1][1], rh1);
+}
+
 static double Lcg(uint64_t& s) {
   s = s * 6364136223846793005ull + 1442695040888963407ull;
   return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
@@ -226,6 +278,7 @@ int main() {
     CheckAssembly(ctx, 6, 5, 3);
     CheckAdjoint(ctx);
     CheckEdges(ctx);
+    CheckPost(ctx);
   } catch (const g::Error& e) {
     std::printf("FAIL: uncaught lf::gb300::Error %d: %s\n", static_cast<int>(e.code()), e.what());
     return 1;
