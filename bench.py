@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=512, help="config-4 meshes (0: skip the batch leg)")
     ap.add_argument("--grad-size", type=int, default=1024, help="config-5 mesh size (0: skip the gradient leg)")
     ap.add_argument("--ho-size", type=int, default=1024, help="config-3 mesh size (0: skip the high-order leg)")
+    ap.add_argument("--gmsh", type=int, default=1, help="run the Gmsh-reader leg (0: skip)")
     return ap.parse_args()
 
 
@@ -381,6 +382,50 @@ def post_leg(L, W, ctx, mesh, space, steps=5, cpu_check=False):
     return out
 
 
+def gmsh_leg(L, W, ctx, n=512, cpu_check=False):
+    """Gmsh reader: a hybrid n x n mesh with two physical groups written as
+    MSH 4.1 binary, 4.1 ASCII and 2.2 ASCII; host parse time (GmshReader
+    without a context) and parse + device mesh build (lfg_gmsh_build_mesh)."""
+    import tempfile
+    xy, cells = W.hybrid_mesh(n, seed=2)
+    bottom = np.where(np.abs(xy[:, 1]) < 1e-12)[0]
+    bottom = bottom[np.argsort(xy[bottom, 0])]
+    edges = np.stack([bottom[:-1], bottom[1:]], 1)
+    cp = 1 + (np.arange(len(cells)) % 2)
+    out = {"workload": "hybrid %dx%d squares (%d cells, %d nodes), %d segment elements" %
+                       (n, n, len(cells), len(xy), len(edges))}
+    with tempfile.TemporaryDirectory() as d:
+        for tag, ver, binary in (("v41_binary", 4, True), ("v41_ascii", 4, False), ("v22_ascii", 2, False)):
+            p = os.path.join(d, tag + ".msh")
+            W.write_msh(p, xy, cells, edges, cell_phys=cp, version=ver, binary=binary)
+            size = os.path.getsize(p)
+            L.GmshReader(filename=p)  # warm the page cache
+            t0 = time.perf_counter()
+            L.GmshReader(filename=p)
+            parse_s = time.perf_counter() - t0
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            rd = L.GmshReader(ctx, p)
+            ctx.synchronize()
+            total_s = time.perf_counter() - t0
+            assert rd.mesh.num_cells == len(cells)
+            out[tag] = {"mb": size / 1e6, "parse_s": parse_s, "parse_mb_per_s": size / 1e6 / parse_s,
+                        "parse_cells_per_s": len(cells) / parse_s, "parse_and_device_mesh_s": total_s}
+            del rd
+        if cpu_check:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import gmsh as G
+            xs, cs = W.hybrid_mesh(64, seed=2)
+            p = os.path.join(d, "small.msh")
+            W.write_msh(p, xs, cs, version=4, binary=False)
+            t0 = time.perf_counter()
+            G.read(p)
+            dt = time.perf_counter() - t0
+            out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "oracle (Python) on a 64x64 hybrid "
+                                   "mesh, MSH 4.1 ASCII (%d cells)" % len(cs), "cells_per_s": len(cs) / dt}
+    return out
+
+
 def batch_leg(L, W, ctx, count):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
     one persistent assembly launch + load + fix + COO->CSR + batched PCG.
@@ -662,6 +707,7 @@ def run_ours(args):
 
     edges = leg(edge_leg, L, W, ctx, mesh, space)
     post = leg(post_leg, L, W, ctx, mesh, space, cpu_check=(rank == 0 and not args.no_cpu_baseline))
+    gmsh = leg(gmsh_leg, L, W, ctx, cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.gmsh else None
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size,
                 cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
@@ -697,7 +743,7 @@ def run_ours(args):
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "high_order": high_order, "solve": solve,
+            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "gmsh": gmsh, "high_order": high_order, "solve": solve,
             "batch": batch,
             "gradient": gradient,
         }

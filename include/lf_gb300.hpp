@@ -36,6 +36,10 @@
 //   fe::NodalProjection (fe/fe_tools.h:198)        fe::NodalProjection(fes, u[, pred])
 //   fe::InitEssentialConditionFromFunction         fe::InitEssentialConditionFromFunction(fes, edge
 //     (fe/fe_tools.h:263)                            flags, g) -> (flags, values) device vectors
+//   io::GmshReader(factory, filename)              io::GmshReader(ctx, filename): mesh(),
+//     (io/gmsh_reader.h)                             PhysicalEntityNr, IsPhysicalEntity,
+//                                                    PhysicalEntityName2Nr / Nr2Name,
+//                                                    PhysicalEntities (+ device flags per group)
 //   (no counterpart)                               adjoint::InverseConductivityFunction
 //
 // Errors: every failing call throws lf::gb300::Error carrying the lfg_status
@@ -584,6 +588,75 @@ inline std::pair<DeviceVector<uint8_t>, DeviceVector<double>> InitEssentialCondi
 }
 
 }  // namespace fe
+
+namespace io {
+
+// GmshReader for 2D first-order meshes (MSH 2.2 / 4.1, ASCII / binary).
+class GmshReader {
+ public:
+  GmshReader(const Context& ctx, const std::string& filename) : ctx_(&ctx) {
+    lfg_gmsh* g = nullptr;
+    const lfg_status st = lfg_gmsh_open(filename.c_str(), &g);
+    if (st != LFG_OK) throw Error(st, lfg_gmsh_last_error());
+    g_.reset(g, [](lfg_gmsh* p) { lfg_gmsh_destroy(p); });
+    lfg_mesh* m = nullptr;
+    ctx.Check(lfg_gmsh_build_mesh(ctx.get(), g, &m));
+    mesh_ = mesh::Mesh::Adopt(ctx, m);
+  }
+  std::shared_ptr<mesh::Mesh> mesh() const { return mesh_; }
+  // PhysicalEntityNr(e) of entity `index` of `codim` (0 cells, 1 edges, 2 nodes).
+  std::vector<int32_t> PhysicalEntityNr(int codim, int64_t index) const {
+    const int64_t n = mesh_->NumEntities(codim);
+    if (index < 0 || index >= n) throw Error(LFG_INVALID_ARG, "GmshReader::PhysicalEntityNr: index out of range");
+    std::vector<int64_t> off(static_cast<size_t>(n) + 1);
+    Check(lfg_gmsh_physical_entity_nrs(g_.get(), codim, n, off.data(), nullptr));
+    std::vector<int32_t> all(static_cast<size_t>(off.back()) + 1);
+    Check(lfg_gmsh_physical_entity_nrs(g_.get(), codim, n, off.data(), all.data()));
+    return std::vector<int32_t>(all.begin() + off[index], all.begin() + off[index + 1]);
+  }
+  bool IsPhysicalEntity(int codim, int64_t index, int32_t nr) const {
+    for (int32_t x : PhysicalEntityNr(codim, index))
+      if (x == nr) return true;
+    return false;
+  }
+  // IsPhysicalEntity(e, nr) for every entity of codim, as a device selector
+  // (e.g. the edge flags of MassEdgeMatrixProvider).
+  DeviceVector<uint8_t> PhysicalEntityFlags(int codim, int32_t nr) const {
+    const int64_t n = mesh_->NumEntities(codim);
+    std::vector<uint8_t> h(static_cast<size_t>(n));
+    Check(lfg_gmsh_is_physical_entity(g_.get(), codim, nr, n, h.data()));
+    return DeviceVector<uint8_t>(*ctx_, h);
+  }
+  int32_t PhysicalEntityName2Nr(const std::string& name, int codim = -1) const {
+    int32_t nr = 0;
+    Check(lfg_gmsh_name_to_nr(g_.get(), name.c_str(), codim, &nr));
+    return nr;
+  }
+  std::string PhysicalEntityNr2Name(int32_t nr, int codim = -1) const {
+    std::vector<char> buf(4096);
+    Check(lfg_gmsh_nr_to_name(g_.get(), nr, codim, buf.data(), static_cast<int64_t>(buf.size())));
+    return std::string(buf.data());
+  }
+  std::vector<std::pair<int32_t, std::string>> PhysicalEntities(int codim) const {
+    int32_t cnt = 0;
+    Check(lfg_gmsh_physical_entities(g_.get(), codim, &cnt, nullptr));
+    std::vector<int32_t> nrs(static_cast<size_t>(cnt) + 1);
+    Check(lfg_gmsh_physical_entities(g_.get(), codim, &cnt, nrs.data()));
+    std::vector<std::pair<int32_t, std::string>> out;
+    for (int32_t i = 0; i < cnt; ++i) out.emplace_back(nrs[i], PhysicalEntityNr2Name(nrs[i], codim));
+    return out;
+  }
+
+ private:
+  static void Check(lfg_status st) {
+    if (st != LFG_OK) throw Error(st, lfg_gmsh_last_error());
+  }
+  const Context* ctx_;
+  std::shared_ptr<lfg_gmsh> g_;
+  std::shared_ptr<mesh::Mesh> mesh_;
+};
+
+}  // namespace io
 
 namespace adjoint {
 

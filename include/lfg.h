@@ -41,7 +41,9 @@ typedef enum {
   LFG_CUDA_ERROR = 6,       /* a CUDA runtime call failed                                      */
   LFG_MISSING_RULE = 7,     /* no quadrature rule for a cell type (loc_comp_ellbvp.h:278-287)  */
   LFG_INCOMPLETE_MESH = 8,  /* hybrid2d/mesh.cc:566-600 check_completeness                     */
-  LFG_OUT_OF_MEMORY = 9
+  LFG_OUT_OF_MEMORY = 9,
+  LFG_IO_ERROR = 10,        /* file missing or not parseable (io/gmsh_reader.cc:622-660, LF_VERIFY_MSG) */
+  LFG_NOT_FOUND = 11        /* name or number lookup failed (gmsh_reader.cc:32-99, LfException) */
 } lfg_status;
 
 typedef struct lfg_ctx lfg_ctx;
@@ -444,6 +446,45 @@ lfg_status lfg_batch_boundary_dof_flags(lfg_batch* batch, uint8_t* flags_dev);
 lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const double* b_dev,
                                double* x_dev, const lfg_solve_opts* opts, lfg_solve_stats* stats,
                                lfg_solve_stats* per_block_stats);
+
+/* ---------------------------------------------------------------- Gmsh reader
+ * GmshReader(factory, filename) (io/gmsh_reader.h, io/gmsh_reader.cc:22-30,
+ * 116-620) for 2D meshes of first-order cells: MSH 2.2 and 4.1, ASCII and
+ * binary.  Parsing runs on the host and needs no device; lfg_gmsh_build_mesh
+ * hands the MeshFactory input (main nodes in file order, cells in element
+ * order, segment elements as pre-registered edges) to lfg_mesh_create, so the
+ * device mesh is numbered exactly as the reference's hybrid2d factory numbers
+ * the file.  Element types: 15 point, 1 segment, 2 triangle, 3 quadrilateral;
+ * second-order (curved) types 8, 9, 10, 16 and all others: LFG_UNSUPPORTED.
+ * The calls below take no context: a failing call stores its message for
+ * lfg_gmsh_last_error() (per thread). */
+typedef struct lfg_gmsh lfg_gmsh;
+const char* lfg_gmsh_last_error(void);
+lfg_status lfg_gmsh_open(const char* filename, lfg_gmsh** out);
+lfg_status lfg_gmsh_open_buffer(const char* data, int64_t size, lfg_gmsh** out);
+lfg_status lfg_gmsh_destroy(lfg_gmsh* g);
+/* The MeshFactory input: num_nodes x (x, y); num_cells x 4 node indices (-1
+ * in the last slot of a triangle); num_preset_edges x 2 node indices. */
+lfg_status lfg_gmsh_sizes(const lfg_gmsh* g, int64_t* num_nodes, int64_t* num_cells, int64_t* num_preset_edges);
+lfg_status lfg_gmsh_factory_input(const lfg_gmsh* g, double* xy, int32_t* cells, int32_t* preset_edges);
+/* GmshReader::mesh(): the device mesh (destroy with lfg_mesh_destroy). */
+lfg_status lfg_gmsh_build_mesh(lfg_ctx* ctx, const lfg_gmsh* g, lfg_mesh** mesh);
+/* PhysicalEntityNr(e) for the entities 0..num_entities-1 of a codim (0 cells,
+ * 1 edges, 2 nodes), host arrays: offsets[num_entities + 1], nrs[offsets[n]]
+ * (NULL: offsets only).  Edges the file does not list have no numbers. */
+lfg_status lfg_gmsh_physical_entity_nrs(const lfg_gmsh* g, int32_t codim, int64_t num_entities, int64_t* offsets,
+                                        int32_t* nrs);
+/* IsPhysicalEntity(e, nr) for every entity of a codim: host flags (the
+ * selector the edge providers and lfg_init_essential_condition take, after a
+ * copy to the device). */
+lfg_status lfg_gmsh_is_physical_entity(const lfg_gmsh* g, int32_t codim, int32_t nr, int64_t num_entities,
+                                       uint8_t* flags);
+/* PhysicalEntityName2Nr / PhysicalEntityNr2Name (gmsh_reader.cc:32-99),
+ * codim -1 = any (an ambiguous lookup fails with LFG_NOT_FOUND, as the
+ * reference throws); PhysicalEntities(codim) (gmsh_reader.cc:101-110). */
+lfg_status lfg_gmsh_name_to_nr(const lfg_gmsh* g, const char* name, int32_t codim, int32_t* nr);
+lfg_status lfg_gmsh_nr_to_name(const lfg_gmsh* g, int32_t nr, int32_t codim, char* name, int64_t capacity);
+lfg_status lfg_gmsh_physical_entities(const lfg_gmsh* g, int32_t codim, int32_t* count, int32_t* nrs);
 
 /* ---------------------------------------------------------- post-processing
  * The steps after the solve (and the Dirichlet data before it), FP64 on the

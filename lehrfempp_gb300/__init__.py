@@ -31,9 +31,9 @@ _lock = threading.Lock()
 
 # status codes (include/lfg.h)
 OK, INVALID_ARG, DEGENERATE_CELL, CAPACITY, UNSUPPORTED, NOT_CONVERGED, CUDA_ERROR, MISSING_RULE, \
-    INCOMPLETE_MESH, OUT_OF_MEMORY = range(10)
+    INCOMPLETE_MESH, OUT_OF_MEMORY, IO_ERROR, NOT_FOUND = range(12)
 STATUS_NAMES = ["OK", "INVALID_ARG", "DEGENERATE_CELL", "CAPACITY", "UNSUPPORTED", "NOT_CONVERGED",
-                "CUDA_ERROR", "MISSING_RULE", "INCOMPLETE_MESH", "OUT_OF_MEMORY"]
+                "CUDA_ERROR", "MISSING_RULE", "INCOMPLETE_MESH", "OUT_OF_MEMORY", "IO_ERROR", "NOT_FOUND"]
 
 # coefficient kinds and analytic families
 ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
@@ -603,6 +603,101 @@ def grad_rd_cellwise(space, provider, u, lam, flags, grad):
     """grad[c] = -lambda_K^T (dA_K/dtheta_c) u_K, lambda zero at flagged dofs."""
     space.ctx.check(lib().lfg_grad_rd_cellwise(space.h, C.byref(provider), u.ptr, lam.ptr,
                                                flags.ptr if flags is not None else None, grad.ptr))
+
+
+# ---------------------------------------------------------------- Gmsh reader
+
+class GmshReader:
+    """lf::io::GmshReader (io/gmsh_reader.h) for 2D first-order meshes: MSH
+    2.2 / 4.1, ASCII / binary.  The file is parsed on the host (no device
+    needed); `mesh` is built on `ctx` when one is given.
+
+        r = GmshReader(ctx, "domain.msh")
+        r.mesh                                   # Mesh (device)
+        r.physical_entity_nr(1)                  # per edge: physical numbers
+        r.is_physical_entity(1, r.physical_entity_name2nr("arc"))  # uint8 flags
+    """
+
+    def __init__(self, ctx=None, filename=None, data=None):
+        L = lib()
+        self.h = C.c_void_p()
+        if data is not None:
+            buf = bytes(data)
+            st = L.lfg_gmsh_open_buffer(buf, len(buf), C.byref(self.h))
+        else:
+            st = L.lfg_gmsh_open(os.fsencode(filename), C.byref(self.h))
+        if st != OK:
+            raise LfgError(st, L.lfg_gmsh_last_error().decode(errors="replace"))
+        nv, nc, ne = C.c_int64(), C.c_int64(), C.c_int64()
+        L.lfg_gmsh_sizes(self.h, C.byref(nv), C.byref(nc), C.byref(ne))
+        self.num_nodes, self.num_cells, self.num_preset_edges = nv.value, nc.value, ne.value
+        self.mesh = None
+        if ctx is not None:
+            mh = C.c_void_p()
+            ctx.check(L.lfg_gmsh_build_mesh(ctx.h, self.h, C.byref(mh)))
+            self.mesh = Mesh(ctx, mh)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().lfg_gmsh_destroy(self.h)
+        except Exception:
+            pass
+        self.h = None
+
+    def _check(self, st):
+        if st != OK:
+            raise LfgError(st, lib().lfg_gmsh_last_error().decode(errors="replace"))
+
+    def factory_input(self):
+        """(xy (N, 2), cells (C, 4) int32, preset edges (E, 2) int32): the MeshFactory input."""
+        xy = np.zeros((self.num_nodes, 2))
+        cells = np.zeros((self.num_cells, 4), np.int32)
+        edges = np.zeros((max(self.num_preset_edges, 1), 2), np.int32)
+        self._check(lib().lfg_gmsh_factory_input(self.h, _p(xy, C.c_double), _p(cells, C.c_int32),
+                                                 _p(edges, C.c_int32)))
+        return xy, cells, edges[: self.num_preset_edges]
+
+    def _count(self, codim, num_entities):
+        if num_entities is not None:
+            return num_entities
+        if self.mesh is not None:
+            return {0: self.mesh.num_cells, 1: self.mesh.num_edges, 2: self.mesh.num_nodes}[codim]
+        return {0: self.num_cells, 1: self.num_preset_edges, 2: self.num_nodes}[codim]
+
+    def physical_entity_nr(self, codim, num_entities=None):
+        """PhysicalEntityNr(e) for every entity of `codim`: a list of lists."""
+        n = self._count(codim, num_entities)
+        off = np.zeros(n + 1, np.int64)
+        self._check(lib().lfg_gmsh_physical_entity_nrs(self.h, codim, n, _p(off, C.c_int64), None))
+        nrs = np.zeros(max(int(off[-1]), 1), np.int32)
+        self._check(lib().lfg_gmsh_physical_entity_nrs(self.h, codim, n, _p(off, C.c_int64), _p(nrs, C.c_int32)))
+        return [list(map(int, nrs[off[i]:off[i + 1]])) for i in range(n)]
+
+    def is_physical_entity(self, codim, nr, num_entities=None):
+        """IsPhysicalEntity(e, nr) for every entity of `codim` (host uint8 flags)."""
+        n = self._count(codim, num_entities)
+        fl = np.zeros(max(n, 1), np.uint8)
+        self._check(lib().lfg_gmsh_is_physical_entity(self.h, codim, nr, n, _p(fl, C.c_uint8)))
+        return fl[:n]
+
+    def physical_entity_name2nr(self, name, codim=-1):
+        nr = C.c_int32()
+        self._check(lib().lfg_gmsh_name_to_nr(self.h, name.encode(), codim, C.byref(nr)))
+        return nr.value
+
+    def physical_entity_nr2name(self, nr, codim=-1):
+        buf = C.create_string_buffer(4096)
+        self._check(lib().lfg_gmsh_nr_to_name(self.h, nr, codim, buf, len(buf)))
+        return buf.value.decode()
+
+    def physical_entities(self, codim):
+        """PhysicalEntities(codim): [(nr, name)] in ascending number order."""
+        cnt = C.c_int32()
+        self._check(lib().lfg_gmsh_physical_entities(self.h, codim, C.byref(cnt), None))
+        nrs = np.zeros(max(cnt.value, 1), np.int32)
+        self._check(lib().lfg_gmsh_physical_entities(self.h, codim, C.byref(cnt), _p(nrs, C.c_int32)))
+        return [(int(n), self.physical_entity_nr2name(int(n), codim)) for n in nrs[: cnt.value]]
 
 
 # ----------------------------------------------------------- post-processing

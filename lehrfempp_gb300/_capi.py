@@ -136,6 +136,18 @@ SIGNATURES = {
     "lfg_batch_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
     "lfg_batch_boundary_dof_flags": (c_status, [vp, vp]),
     "lfg_batch_solve_pcg": (c_status, [vp, vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats), P(lfg_solve_stats)]),
+    "lfg_gmsh_last_error": (C.c_char_p, []),
+    "lfg_gmsh_open": (c_status, [C.c_char_p, P(vp)]),
+    "lfg_gmsh_open_buffer": (c_status, [C.c_char_p, i64, P(vp)]),
+    "lfg_gmsh_destroy": (c_status, [vp]),
+    "lfg_gmsh_sizes": (c_status, [vp, P(i64), P(i64), P(i64)]),
+    "lfg_gmsh_factory_input": (c_status, [vp, P(dbl), P(i32), P(i32)]),
+    "lfg_gmsh_build_mesh": (c_status, [vp, vp, P(vp)]),
+    "lfg_gmsh_physical_entity_nrs": (c_status, [vp, i32, i64, P(i64), P(i32)]),
+    "lfg_gmsh_is_physical_entity": (c_status, [vp, i32, i32, i64, P(u8)]),
+    "lfg_gmsh_name_to_nr": (c_status, [vp, C.c_char_p, i32, P(i32)]),
+    "lfg_gmsh_nr_to_name": (c_status, [vp, i32, i32, C.c_char_p, i64]),
+    "lfg_gmsh_physical_entities": (c_status, [vp, i32, P(i32), P(i32)]),
     "lfg_integrate_mesh_function": (c_status, [vp, P(lfg_integrand), i32, vp, i32, P(dbl)]),
     "lfg_fe_eval": (c_status, [vp, vp, i32, P(dbl), vp, vp]),
     "lfg_nodal_projection": (c_status, [vp, P(lfg_coeff), vp, vp]),

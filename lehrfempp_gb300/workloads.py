@@ -190,3 +190,165 @@ def to_coeff(ctx, spec, keep):
     if k == "sincos":
         return L.coeff(L.ANALYTIC, func=L.FN_SINCOS, params=list(spec[1:]))
     raise ValueError(spec)
+
+
+def write_msh(path, xy, cells, edges=None, cell_phys=None, edge_phys=None, version=4, binary=True,
+              names=None):
+    """Write a 2D first-order mesh as a Gmsh MSH 2.2 or 4.1 file (ASCII or
+    binary, little endian) -- the synthetic input of the Gmsh-reader tests and
+    benchmark.  cells: (C, 4) node indices, -1 in slot 3 for triangles; edges:
+    (E, 2) segment elements written before the cells; *_phys: one physical
+    number per element (default 1 for cells, 2 for edges); names: list of
+    (dim, nr, name).  Node tags are 1-based node indices.  For 4.1 every
+    distinct (dimension, physical number) becomes one model entity and the
+    elements are written in blocks per (entity, element type), in order of
+    first appearance, keeping their relative order inside a block."""
+    import struct
+    xy = np.asarray(xy, np.float64).reshape(-1, 2)
+    cells = np.asarray(cells, np.int64).reshape(-1, 4)
+    edges = np.zeros((0, 2), np.int64) if edges is None else np.asarray(edges, np.int64).reshape(-1, 2)
+    cp = np.ones(len(cells), np.int64) if cell_phys is None else np.asarray(cell_phys, np.int64)
+    ep = np.full(len(edges), 2, np.int64) if edge_phys is None else np.asarray(edge_phys, np.int64)
+    names = names or []
+    nn = len(xy)
+    quad = cells[:, 3] >= 0
+    out = bytearray()
+
+    def w(s):
+        out.extend(s.encode())
+
+    w("$MeshFormat\n%s %d 8\n" % ("2.2" if version == 2 else "4.1", 1 if binary else 0))
+    if binary:
+        out.extend(struct.pack("<i", 1))
+        w("\n")
+    w("$EndMeshFormat\n")
+    if names:
+        w("$PhysicalNames\n%d\n" % len(names))
+        for d, nr, nm in names:
+            w('%d %d "%s"\n' % (d, nr, nm))
+        w("$EndPhysicalNames\n")
+    if version == 2:
+        w("$Nodes\n%d\n" % nn)
+        if binary:
+            rec = np.zeros(nn, dtype=[("id", "<i4"), ("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
+            rec["id"] = np.arange(1, nn + 1)
+            rec["x"], rec["y"] = xy[:, 0], xy[:, 1]
+            out.extend(rec.tobytes())
+            w("\n")
+        else:
+            w("".join("%d %.17g %.17g 0\n" % (i + 1, x, y) for i, (x, y) in enumerate(xy)))
+        w("$EndNodes\n")
+        ne = len(edges) + len(cells)
+        w("$Elements\n%d\n" % ne)
+        groups = [(1, edges, ep)]
+        # keep the cell order: runs of equal type become binary groups
+        if binary:
+            items = [(1, e, p) for e, p in zip(edges, ep)] + \
+                    [((3 if q else 2), c, p) for c, p, q in zip(cells, cp, quad)]
+            k, num = 0, 1
+            while k < len(items):
+                t = items[k][0]
+                j = k
+                while j < len(items) and items[j][0] == t:
+                    j += 1
+                nv = {1: 2, 2: 3, 3: 4}[t]
+                out.extend(struct.pack("<iii", t, j - k, 2))
+                arr = np.zeros((j - k, 3 + nv), np.int32)
+                arr[:, 0] = np.arange(num, num + j - k)
+                arr[:, 1] = [items[m][2] for m in range(k, j)]
+                arr[:, 2] = arr[:, 1]
+                arr[:, 3:] = np.array([items[m][1][:nv] for m in range(k, j)]) + 1
+                out.extend(arr.astype("<i4").tobytes())
+                num += j - k
+                k = j
+            w("\n")
+        else:
+            lines = []
+            num = 1
+            for e, p in zip(edges, ep):
+                lines.append("%d 1 2 %d %d %d %d\n" % (num, p, p, e[0] + 1, e[1] + 1))
+                num += 1
+            for c, p, q in zip(cells, cp, quad):
+                nv = 4 if q else 3
+                lines.append("%d %d 2 %d %d %s\n" % (num, 3 if q else 2, p, p, " ".join(str(v + 1) for v in c[:nv])))
+                num += 1
+            w("".join(lines))
+        del groups
+        w("$EndElements\n")
+        with open(path, "wb") as fh:
+            fh.write(bytes(out))
+        return
+    # ---- 4.1: entities per (dim, physical number)
+    ent = {}
+    for d, phys in ((1, ep), (2, cp)):
+        for p in phys:
+            ent.setdefault((d, int(p)), len([k for k in ent if k[0] == d]) + 1)
+    ncurve = len([k for k in ent if k[0] == 1])
+    nsurf = len([k for k in ent if k[0] == 2])
+    w("$Entities\n")
+    if binary:
+        out.extend(struct.pack("<QQQQ", 0, ncurve, nsurf, 0))
+        for d in (1, 2):
+            for (dd, p), tag in ent.items():
+                if dd != d:
+                    continue
+                out.extend(struct.pack("<i6dQi Q", tag, 0, 0, 0, 1, 1, 0, 1, p, 0))
+        w("\n")
+    else:
+        w("0 %d %d 0\n" % (ncurve, nsurf))
+        for d in (1, 2):
+            for (dd, p), tag in ent.items():
+                if dd == d:
+                    w("%d 0 0 0 1 1 0 1 %d 0\n" % (tag, p))
+    w("$EndEntities\n")
+    # nodes: one block on surface entity 1
+    w("$Nodes\n")
+    if binary:
+        out.extend(struct.pack("<QQQQ", 1, nn, 1, nn))
+        out.extend(struct.pack("<iiiQ", 2, 1, 0, nn))
+        out.extend(np.arange(1, nn + 1, dtype="<u8").tobytes())
+        xyz = np.zeros((nn, 3), "<f8")
+        xyz[:, :2] = xy
+        out.extend(xyz.tobytes())
+        w("\n")
+    else:
+        w("1 %d 1 %d\n2 1 0 %d\n" % (nn, nn, nn))
+        w("".join("%d\n" % (i + 1) for i in range(nn)))
+        w("".join("%.17g %.17g 0\n" % (x, y) for x, y in xy))
+    w("$EndNodes\n")
+    # element blocks: per (entity, type) in order of first appearance
+    items = [((1, int(p)), 1, e[:2]) for e, p in zip(edges, ep)] + \
+            [((2, int(p)), 3 if q else 2, c[:4] if q else c[:3]) for c, p, q in zip(cells, cp, quad)]
+    order = []
+    blocks = {}
+    for key, t, nodes in items:
+        b = (key, t)
+        if b not in blocks:
+            blocks[b] = []
+            order.append(b)
+        blocks[b].append(nodes)
+    ne = len(items)
+    w("$Elements\n")
+    if binary:
+        out.extend(struct.pack("<QQQQ", len(order), ne, 1, ne))
+        num = 1
+        for (key, t) in order:
+            lst = np.array(blocks[(key, t)], np.int64)
+            out.extend(struct.pack("<iiiQ", key[0], ent[key], t, len(lst)))
+            arr = np.zeros((len(lst), 1 + lst.shape[1]), "<u8")
+            arr[:, 0] = np.arange(num, num + len(lst))
+            arr[:, 1:] = lst + 1
+            out.extend(arr.tobytes())
+            num += len(lst)
+        w("\n")
+    else:
+        w("%d %d 1 %d\n" % (len(order), ne, ne))
+        num = 1
+        for (key, t) in order:
+            lst = blocks[(key, t)]
+            w("%d %d %d %d\n" % (key[0], ent[key], t, len(lst)))
+            w("".join("%d %s\n" % (num + k, " ".join(str(v + 1) for v in nodes)) for k, nodes in enumerate(lst)))
+            num += len(lst)
+    w("$EndElements\n")
+    with open(path, "wb") as fh:
+        fh.write(bytes(out))

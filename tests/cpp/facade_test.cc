@@ -224,6 +224,31 @@ static void CheckPost(const g::Context& ctx) {
               err[0][1], err[1][1], rh1);
 }
 
+// io::GmshReader on the two-element fixture (gmsh_reader_tests.cc:22-140).
+static void CheckGmsh(const g::Context& ctx, const char* dir) {
+  const std::string path = std::string(dir) + "/two_element_hybrid_2d_v4_binary.msh";
+  g::io::GmshReader reader(ctx, path);
+  auto mesh = reader.mesh();
+  CHECK(mesh->NumEntities(0) == 2 && mesh->NumEntities(1) == 6 && mesh->NumEntities(2) == 5,
+        "two-element mesh has %lld cells, %lld edges, %lld nodes", static_cast<long long>(mesh->NumEntities(0)),
+        static_cast<long long>(mesh->NumEntities(1)), static_cast<long long>(mesh->NumEntities(2)));
+  const int32_t diag = reader.PhysicalEntityName2Nr("diagonal");
+  CHECK(diag == 4 && reader.PhysicalEntityNr2Name(4) == "diagonal", "diagonal lookup");
+  auto flags = reader.PhysicalEntityFlags(1, diag).Download();
+  int64_t nd = 0;
+  for (uint8_t f : flags) nd += f;
+  CHECK(nd == 1, "%lld edges in the diagonal group", static_cast<long long>(nd));
+  CHECK(reader.PhysicalEntities(0).size() == 3, "three cell groups");
+  bool threw = false;
+  try {
+    reader.PhysicalEntityName2Nr("gugus");
+  } catch (const g::Error& e) {
+    threw = e.code() == LFG_NOT_FOUND;
+  }
+  CHECK(threw, "unknown name must throw LFG_NOT_FOUND");
+  std::printf("gmsh: two-element mesh read, diagonal group = edge set of size %lld\n", static_cast<long long>(nd));
+}
+
 static double Lcg(uint64_t& s) {
   s = s * 6364136223846793005ull + 1442695040888963407ull;
   return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
@@ -270,9 +295,10 @@ static void CheckAdjoint(const g::Context& ctx) {
   std::printf("adjoint: J %.6g, max |dJ/dtheta| %.3g, FD error %.3g\n", J, gmax, worst);
 }
 
-int main() {
+int main(int argc, char** argv) {
   try {
     g::Context ctx(0);
+    if (argc > 1) CheckGmsh(ctx, argv[1]);
     CheckAssembly(ctx, 12, 10, 1);
     CheckAssembly(ctx, 9, 7, 2);
     CheckAssembly(ctx, 6, 5, 3);

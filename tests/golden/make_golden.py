@@ -11,6 +11,8 @@ reference checkout.  Sources:
   lib/lf/fe/test/fe_tools_tests.cc         IntegrateMeshFunction integrals
   lib/lf/uscalfe/test/gfe_tests.cc         L2 norms on test mesh 3
   lib/lf/mesh/test_utils/test_meshes.cc    the nodes and triangles of test mesh 3
+  lib/lf/io/test/msh_files/*.msh           copied byte for byte into msh/ (the
+                                           reader's input fixtures)
 
 usage: python tests/golden/make_golden.py /root/reference
 """
@@ -115,6 +117,18 @@ def main():
             "l2norm_vf_y_mx": {"value": float(m2.group(1)), "tolerance": float(m2.group(2))},
         },
     }
+    # the Gmsh reader's test inputs, copied unchanged
+    src = os.path.join(ref, "lib/lf/io/test/msh_files")
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "msh")
+    os.makedirs(dst, exist_ok=True)
+    copied = []
+    for name in sorted(os.listdir(src)):
+        if name.endswith(".msh"):
+            with open(os.path.join(src, name), "rb") as fi, open(os.path.join(dst, name), "wb") as fo:
+                fo.write(fi.read())
+            copied.append(name)
+    out["gmsh_fixtures"] = {"dir": "lib/lf/io/test/msh_files", "files": copied,
+                            "tests": "lib/lf/io/test/gmsh_reader_tests.cc"}
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1)

@@ -19,7 +19,8 @@ def test_cpp_facade_driver(tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "facade_test.cc"), "-L", lib_dir, "-llfg", "-L", orc_dir,
                     "-loracle", "-Wl,-rpath," + lib_dir + ":" + orc_dir, "-o", exe], check=True)
-    p = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    p = subprocess.run([exe, os.path.join(ROOT, "tests", "golden", "msh")], capture_output=True, text=True,
+                       timeout=600)
     print(p.stdout)
     assert p.returncode == 0, p.stdout + p.stderr
     assert "facade_test OK" in p.stdout
