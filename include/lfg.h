@@ -145,6 +145,15 @@ lfg_status lfg_mesh_boundary_flags(lfg_mesh* mesh, uint8_t* node_flags_dev,
  * (uscalfe/fe_space_lagrange_o1.h:45-51 etc.; layout uniform_scalar_fe_space.h:241-342). */
 lfg_status lfg_space_create(lfg_mesh* mesh, int np, int ns, int nt, int nq, lfg_space** out);
 lfg_status lfg_space_create_lagrange(lfg_mesh* mesh, int degree, lfg_space** out);
+/* fe::HierarchicScalarFESpace(mesh, degree) (fe/hierarchic_scalar_fe_space.h:
+ * 36-46) of uniform degree 1..20: hierarchic (integrated Legendre / Jacobi)
+ * shape functions (fe/hierarchic_fe.h), dofs numbered like
+ * DynamicFEDofHandler (nodes, edge interiors, cell interiors).  With such a
+ * space, lfg_assemble_matrix_rd is fe::DiffusionElementMatrixProvider
+ * (alpha) + fe::MassElementMatrixProvider (gamma) (fe/loc_comp_ellbvp.h:
+ * 169-214, 349-378) and lfg_assemble_vector_load fe::ScalarLoadElementVector-
+ * Provider (:642-685), with make_QuadRule(ref_el, 2 * degree) by default. */
+lfg_status lfg_space_create_hierarchic(lfg_mesh* mesh, int32_t degree, lfg_space** out);
 lfg_status lfg_space_destroy(lfg_space* space);
 /* NumDofs, NumLocalDofs per tria / quad, row stride of the cell dof table,
  * and the number of triplets one AssembleMatrixLocally call emits. */

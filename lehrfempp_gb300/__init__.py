@@ -340,6 +340,15 @@ class Space:
         return cls(mesh, h, degree)
 
     @classmethod
+    def hierarchic(cls, mesh, degree):
+        """fe::HierarchicScalarFESpace(mesh, degree) (uniform degree 1..20)."""
+        h = C.c_void_p()
+        mesh.ctx.check(lib().lfg_space_create_hierarchic(mesh.h, degree, C.byref(h)))
+        sp = cls(mesh, h, 0)
+        sp.hier_degree = degree
+        return sp
+
+    @classmethod
     def layout(cls, mesh, np_, ns, nt, nq):
         h = C.c_void_p()
         mesh.ctx.check(lib().lfg_space_create(mesh.h, np_, ns, nt, nq, C.byref(h)))

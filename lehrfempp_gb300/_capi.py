@@ -92,6 +92,7 @@ SIGNATURES = {
     "lfg_mesh_boundary_flags": (c_status, [vp, vp, vp]),
     "lfg_space_create": (c_status, [vp, C.c_int, C.c_int, C.c_int, C.c_int, P(vp)]),
     "lfg_space_create_lagrange": (c_status, [vp, C.c_int, P(vp)]),
+    "lfg_space_create_hierarchic": (c_status, [vp, i32, P(vp)]),
     "lfg_space_destroy": (c_status, [vp]),
     "lfg_space_info": (c_status, [vp, P(i64), P(i32), P(i32), P(i32), P(i64)]),
     "lfg_space_download_cell_dofs": (c_status, [vp, P(i32)]),

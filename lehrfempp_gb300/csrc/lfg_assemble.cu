@@ -1213,6 +1213,10 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_
   if (!sp) return LFG_INVALID_ARG;
   LFG_API_BEGIN(sp->mesh->ctx)
   if (!pr || !coo) Fail(LFG_INVALID_ARG, "lfg_assemble_matrix_rd: null argument");
+  if (sp->hier_degree > 0) {
+    HierAssembleMatrix(sp, pr, coo);
+    return LFG_OK;
+  }
   if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "reaction-diffusion provider needs a Lagrangian space");
   if (coo->rows < sp->num_dofs || coo->cols < sp->num_dofs)
     Fail(LFG_INVALID_ARG, "COO matrix smaller than the number of dofs");
@@ -1255,6 +1259,10 @@ lfg_status lfg_assemble_vector_load(lfg_space* sp, const lfg_load_provider* pr, 
   if (!sp) return LFG_INVALID_ARG;
   LFG_API_BEGIN(sp->mesh->ctx)
   if (!pr || !b) Fail(LFG_INVALID_ARG, "lfg_assemble_vector_load: null argument");
+  if (sp->hier_degree > 0) {
+    HierAssembleVector(sp, pr, b);
+    return LFG_OK;
+  }
   if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "load provider needs a Lagrangian space");
   lfg_ctx* ctx = sp->mesh->ctx;
   EnsureIncidence(sp);
@@ -1264,6 +1272,19 @@ lfg_status lfg_assemble_vector_load(lfg_space* sp, const lfg_load_provider* pr, 
   LFG_LAUNCHED(ctx);
   LFG_API_END
 }
+
+}  // extern "C"
+
+namespace lfg {
+void GatherElementVectors(lfg_space* sp, double* b) {
+  lfg_ctx* ctx = sp->mesh->ctx;
+  GatherVectorKernel<<<GridFor(ctx, sp->num_dofs, 256), 256, 0, ctx->stream>>>(
+      sp->num_dofs, sp->inc_ptr.as<int64_t>(), sp->inc_slot.as<uint64_t>(), sp->scratch_vec.as<double>(), b);
+  LFG_LAUNCHED(ctx);
+}
+}  // namespace lfg
+
+extern "C" {
 
 lfg_status lfg_assemble_matrix_tabulated(lfg_space* sp, const double* elem, int32_t ld, lfg_coo* coo) {
   if (!sp) return LFG_INVALID_ARG;

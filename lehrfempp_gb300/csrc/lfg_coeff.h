@@ -99,6 +99,24 @@ __device__ inline void EvalAnalyticGrad(const CoeffDev& f, double x, double y, d
   gx = gy = 0.0;
 }
 
+// Value of a coefficient at reference point (xh, yh) of cell c with global
+// coordinates (X, Y): cell-wise constants, the O1 interpolant of nodal data
+// (tria_o1 / quad_o1 shape functions), or the analytic function at (X, Y).
+__device__ inline double EvalCoeffPoint(const CoeffDev& f, int c, const int4& cn, bool quad, double xh, double yh,
+                                        double X, double Y) {
+  switch (f.kind) {
+    case LFG_COEFF_CONSTANT: return f.value;
+    case LFG_COEFF_PER_CELL: return f.data[c];
+    case LFG_COEFF_PER_CELL_EXP: return exp(f.data[c]);
+    case LFG_COEFF_NODAL_O1:
+      if (!quad) return f.data[cn.x] * (1.0 - xh - yh) + f.data[cn.y] * xh + f.data[cn.z] * yh;
+      return f.data[cn.x] * ((1 - xh) * (1 - yh)) + f.data[cn.y] * (xh * (1 - yh)) + f.data[cn.z] * (xh * yh) +
+             f.data[cn.w] * ((1 - xh) * yh);
+    case LFG_COEFF_ANALYTIC: return EvalAnalytic(f, X, Y);
+  }
+  return 0.0;
+}
+
 inline bool KnownAnalytic(int func) { return func >= LFG_FN_POLY && func <= LFG_FN_TRIG; }
 
 // Host conversion with the argument checks every entry point shares.

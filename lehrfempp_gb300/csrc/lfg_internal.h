@@ -140,10 +140,16 @@ struct lfg_mesh {
   lfg::DevBuf quad_list;   // int32[nquad]
 };
 
+namespace lfg {
+constexpr int kMaxLocalDofs = 1024;  // local shape functions per cell ((p+1)^2 <= 1024)
+constexpr int kMaxHierDegree = 20;   // hierarchic degree (quadrilateral: 441 local dofs)
+}  // namespace lfg
+
 struct lfg_space {
   lfg::CtxRef ref;
   lfg_mesh* mesh = nullptr;
   int degree = 0;  // 0 = generic layout
+  int hier_degree = 0;  // > 0: HierarchicScalarFESpace of this uniform degree (generic layout)
   int np = 0, ns = 0, nt = 0, nq = 0;
   int n_tria = 0, n_quad = 0, n_cell = 0, n_edge = 0;
   int64_t num_dofs = 0;
@@ -216,5 +222,13 @@ void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
 // int32 row pointers and the SELL-32 copy; FP32 values for mixed precision.
 void PrepareSolve(lfg_csr* A);
 void EnsureFloatValues(lfg_csr* A);
+// b[dof] += the element vectors in sp->scratch_vec, cells in ascending order
+// (AssembleVectorLocally order), through the space's dof incidence.
+void GatherElementVectors(lfg_space* sp, double* b);
+void EnsureIncidence(lfg_space* sp);
+// Hierarchic (hp) spaces (lfg_hier.cu): fe::DiffusionElementMatrixProvider +
+// fe::MassElementMatrixProvider and fe::ScalarLoadElementVectorProvider.
+void HierAssembleMatrix(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo);
+void HierAssembleVector(lfg_space* sp, const lfg_load_provider* pr, double* b);
 
 }  // namespace lfg

@@ -7,6 +7,7 @@
 // the cell), then the cell's own interior dofs.  Rows of the cell table have
 // the stride max(n_tria, n_quad) like dofs_[kCellOrd] in the reference.
 #include <algorithm>
+#include <string>
 
 #include "lfg_api.h"
 #include "lfg_internal.h"
@@ -144,8 +145,8 @@ lfg_status lfg_space_create(lfg_mesh* m, int np, int ns, int nt, int nq, lfg_spa
     sp->n_tria = 3 * np + 3 * ns + nt;
     sp->n_quad = 4 * np + 4 * ns + nq;
     sp->n_cell = std::max(sp->n_tria, sp->n_quad);
-    if (sp->n_cell > 16 || sp->n_cell == 0)
-      Fail(LFG_UNSUPPORTED, "at most 16 local dofs per cell are supported");
+    if (sp->n_cell > kMaxLocalDofs || sp->n_cell == 0)
+      Fail(LFG_UNSUPPORTED, "at most " + std::to_string(kMaxLocalDofs) + " local dofs per cell are supported");
     const int64_t nc = m->nc;
     DevBuf nint;
     nint.alloc((nc + 1) * sizeof(int64_t), s);
@@ -185,6 +186,21 @@ lfg_status lfg_space_create_lagrange(lfg_mesh* m, int degree, lfg_space** out) {
   const int p = degree;
   lfg_status st = lfg_space_create(m, 1, p - 1, (p - 1) * (p - 2) / 2, (p - 1) * (p - 1), out);
   if (st == LFG_OK) (*out)->degree = degree;
+  return st;
+}
+
+// HierarchicScalarFESpace(mesh, degree) (fe/hierarchic_scalar_fe_space.h:36-46):
+// one dof per node, degree-1 per edge, (p-2)(p-1)/2 per triangle and (p-1)^2
+// per quadrilateral, numbered like DynamicFEDofHandler (assemble/dofhandler.h:
+// 550-650), which for uniform counts is the uniform layout.
+lfg_status lfg_space_create_hierarchic(lfg_mesh* m, int32_t degree, lfg_space** out) {
+  if (degree < 1 || degree > kMaxHierDegree) {
+    if (m) m->ctx->last_error = "hierarchic spaces of degree 1.." + std::to_string(kMaxHierDegree) + " only";
+    return LFG_UNSUPPORTED;
+  }
+  const int p = degree;
+  lfg_status st = lfg_space_create(m, 1, p - 1, p <= 2 ? 0 : (p - 2) * (p - 1) / 2, (p - 1) * (p - 1), out);
+  if (st == LFG_OK) (*out)->hier_degree = degree;
   return st;
 }
 

@@ -178,6 +178,152 @@ bool MakeRule(bool is_quad, int degree, Rule& r) {
   return true;
 }
 
+// ------------------------------------------------ hierarchic (hp) elements
+namespace {
+using ld = long double;
+
+// Legendre polynomials in homogeneous form, P_n(x; t) = t^n P_n((2x - t) / t):
+// P_0 = 1, P_1 = 2x - t, (n+1) P_{n+1} = (2n+1)(2x - t) P_n - n t^2 P_{n-1}.
+void ScaledLegendre(int nmax, ld x, ld t, ld* P) {
+  P[0] = 1.0L;
+  if (nmax >= 1) P[1] = 2.0L * x - t;
+  for (int n = 1; n < nmax; ++n)
+    P[n + 1] = ((2.0L * n + 1.0L) * (2.0L * x - t) * P[n] - n * t * t * P[n - 1]) / (n + 1.0L);
+}
+
+// Integrated Legendre function L_n(x; t) = (P_n - t^2 P_{n-2}) / (2 (2n - 1)),
+// n >= 2 (for t = 1 the integral of P_{n-1}(2s - 1) over [0, x]), with
+// dL/dx = P_{n-1}, dL/dt = -(P_{n-1} + t P_{n-2}) / 2.
+void IntLegendre(int n, ld x, ld t, ld& L, ld& Lx, ld& Lt) {
+  ld P[64];
+  ScaledLegendre(n, x, t, P);
+  L = (P[n] - t * t * P[n - 2]) / (2.0L * (2.0L * n - 1.0L));
+  Lx = P[n - 1];
+  Lt = -0.5L * (P[n - 1] + t * P[n - 2]);
+}
+
+// Jacobi polynomial P_k^{(a,0)}(2x - 1) by the standard three-term recurrence.
+ld JacobiA0(int k, ld a, ld x) {
+  const ld z = 2.0L * x - 1.0L;
+  ld p0 = 1.0L;
+  if (k == 0) return p0;
+  ld p1 = 0.5L * (a + (a + 2.0L) * z);
+  for (int m = 1; m < k; ++m) {
+    const ld c = 2.0L * m + a;
+    const ld a1 = 2.0L * (m + 1) * (m + 1 + a) * c;
+    const ld a2 = (c + 1.0L) * a * a;
+    const ld a3 = c * (c + 1.0L) * (c + 2.0L);
+    const ld a4 = 2.0L * (m + a) * m * (c + 2.0L);
+    const ld p2 = ((a2 + a3 * z) * p1 - a4 * p0) / a1;
+    p0 = p1;
+    p1 = p2;
+  }
+  return p1;
+}
+
+// Integrated Jacobi function IJ_n^a(x) = int_0^x P_{n-1}^{(a,0)}(2s - 1) ds
+// (n >= 1), by Gauss-Legendre quadrature on [0, x] that is exact for its
+// degree n - 1; derivative P_{n-1}^{(a,0)}(2x - 1).
+ld IntJacobi(int n, ld a, ld x, ld& dx) {
+  dx = JacobiA0(n - 1, a, x);
+  std::vector<double> gx, gw;
+  const int m = (n - 1) / 2 + 1;
+  GaussLegendre01(m, gx, gw);
+  ld s = 0.0L;
+  for (int k = 0; k < m; ++k) s += static_cast<ld>(gw[k]) * JacobiA0(n - 1, a, x * static_cast<ld>(gx[k]));
+  return s * x;
+}
+}  // namespace
+
+double HierSegment(int n, double t, double* dt) {
+  ld L, Lx, Lt;
+  IntLegendre(n, t, 1.0L, L, Lx, Lt);
+  if (dt) *dt = static_cast<double>(Lx);
+  return static_cast<double>(L);
+}
+
+void HierShape(bool is_quad, int p, int pat, double xd, double yd, double* phi, double (*dphi)[2]) {
+  const ld x = xd, y = yd;
+  auto put = [&](int slot, ld v, ld gx, ld gy) {
+    phi[slot] = static_cast<double>(v);
+    dphi[slot][0] = static_cast<double>(gx);
+    dphi[slot][1] = static_cast<double>(gy);
+  };
+  if (!is_quad) {
+    // barycentric coordinates of the vertices and their gradients
+    const ld l[3] = {1.0L - x - y, x, y};
+    const ld gl[3][2] = {{-1.0L, -1.0L}, {1.0L, 0.0L}, {0.0L, 1.0L}};
+    for (int v = 0; v < 3; ++v) put(v, l[v], gl[v][0], gl[v][1]);
+    int slot = 3;
+    for (int e = 0; e < 3; ++e) {
+      const int a = e, b = (e + 1) % 3;  // local edge e runs from vertex a to vertex b
+      const bool neg = (pat >> e) & 1;
+      const int s = neg ? a : b;          // the edge coordinate grows towards its end vertex
+      const ld t = l[a] + l[b];
+      const ld gt[2] = {gl[a][0] + gl[b][0], gl[a][1] + gl[b][1]};
+      for (int i = 0; i < p - 1; ++i) {
+        ld L, Lx, Lt;
+        IntLegendre(i + 2, l[s], t, L, Lx, Lt);
+        const int k = neg ? slot + (p - 2 - i) : slot + i;
+        put(k, L, Lx * gl[s][0] + Lt * gt[0], Lx * gl[s][1] + Lt * gt[1]);
+      }
+      slot += p - 1;
+    }
+    // interior: edge-0 function of order i times an integrated Jacobi function of l2
+    const int s0 = (pat & 1) ? 0 : 1;
+    const ld t0 = l[0] + l[1];
+    for (int i = 0; i + 3 <= p; ++i) {
+      ld E, Ex, Et;
+      IntLegendre(i + 2, l[s0], t0, E, Ex, Et);
+      const ld Egx = Ex * gl[s0][0] + Et * (gl[0][0] + gl[1][0]);
+      const ld Egy = Ex * gl[s0][1] + Et * (gl[0][1] + gl[1][1]);
+      for (int j = 0; j + i + 3 <= p; ++j) {
+        ld dJ;
+        const ld J = IntJacobi(j + 1, 2.0L * i + 4.0L, l[2], dJ);
+        put(slot++, E * J, Egx * J + E * dJ * gl[2][0], Egy * J + E * dJ * gl[2][1]);
+      }
+    }
+    return;
+  }
+  // quadrilateral: products of segment functions b_0 = 1 - t, b_1 = t,
+  // b_k = L_k(t) (k >= 2), in x and y, and of their reversals b_k(1 - t)
+  auto seg = [&](int k, ld t, ld& d) -> ld {
+    if (k == 0) { d = -1.0L; return 1.0L - t; }
+    if (k == 1) { d = 1.0L; return t; }
+    ld L, Lx, Lt;
+    IntLegendre(k, t, 1.0L, L, Lx, Lt);
+    d = Lx;
+    return L;
+  };
+  // term b_kx(sx) * b_ky(sy) with sx = x or 1 - x (rx), sy = y or 1 - y (ry)
+  auto prod = [&](int slot, int kx, bool rx, int ky, bool ry) {
+    ld dx, dy;
+    const ld bx = seg(kx, rx ? 1.0L - x : x, dx);
+    const ld by = seg(ky, ry ? 1.0L - y : y, dy);
+    put(slot, bx * by, (rx ? -dx : dx) * by, bx * (ry ? -dy : dy));
+  };
+  prod(0, 0, false, 0, false);
+  prod(1, 1, false, 0, false);
+  prod(2, 1, false, 1, false);
+  prod(3, 0, false, 1, false);
+  int slot = 4;
+  for (int e = 0; e < 4; ++e) {
+    const bool neg = (pat >> e) & 1;
+    for (int i = 0; i < p - 1; ++i) {
+      const int k = neg ? slot + (p - 2 - i) : slot + i;
+      switch (e) {
+        case 0: prod(k, i + 2, neg, 0, false); break;   // bottom, x from v0 to v1
+        case 1: prod(k, 1, false, i + 2, neg); break;   // right, y from v1 to v2
+        case 2: prod(k, i + 2, !neg, 1, false); break;  // top, x from v2 back to v3
+        default: prod(k, 0, false, i + 2, !neg); break; // left, y from v3 back to v0
+      }
+    }
+    slot += p - 1;
+  }
+  for (int i = 0; i < p - 1; ++i)
+    for (int j = 0; j < p - 1; ++j) prod(slot++, j + 2, false, i + 2, false);
+}
+
 void NodeCoords(bool is_quad, int degree, std::vector<double>& xy) {
   xy.clear();
   if (is_quad) {

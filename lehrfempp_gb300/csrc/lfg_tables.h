@@ -22,6 +22,19 @@ constexpr int kMaxRuleDegree = 100;
 bool MakeRule(bool is_quad, int degree, Rule& out);
 int NumShape(bool is_quad, int degree);
 void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*dphi)[2]);
+// Hierarchic (hp) reference elements of uniform degree p >= 1
+// (fe/hierarchic_fe.h: FeHierarchicTria, FeHierarchicQuad): vertex functions,
+// per local edge p-1 integrated Legendre functions in the edge's own
+// direction, then the interior functions.  `pattern` bit j set = local edge j
+// negatively oriented (the cell's relative orientation): such an edge's
+// functions use the reversed edge coordinate and sit in reversed slots, and
+// the triangle's interior functions follow edge 0's direction.  Counts equal
+// the Lagrangian ones, (p+1)(p+2)/2 and (p+1)^2.
+void HierShape(bool is_quad, int p, int pattern, double x, double y, double* phi, double (*dphi)[2]);
+// Integrated Legendre function of the segment element: L_n(t) = int_0^t P_{n-1}(2s-1) ds
+// for n >= 2 (FeHierarchicSegment's shape function n), and its derivative.
+double HierSegment(int n, double t, double* dt);
+
 // Reference coordinates of the evaluation nodes of the Lagrangian element
 // (EvaluationNodes, uscalfe/lagr_fe.h): xy[2 i], xy[2 i + 1] is the node of
 // local shape function i (phi_j(node_i) = delta_ij).

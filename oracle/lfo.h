@@ -273,4 +273,24 @@ void NodalProjectionMF(const DofHandler& dh, int degree, const MeshFunction& u, 
 void InitEssentialCondition(const DofHandler& dh, int degree, const uint8_t* edge_flags, const MeshFunction& g,
                             std::vector<uint8_t>& flags, std::vector<double>& vals);
 
+// ------------------------------------------------ hierarchic (hp) FE ----
+// fe/hierarchic_fe.cc: scaled Legendre and (integrated) Jacobi polynomials.
+double HierLegendre(unsigned n, double x, double t = 1.0);
+double HierILegendre(unsigned n, double x, double t = 1.0);
+double HierILegendreDx(unsigned n, double x, double t = 1.0);
+double HierILegendreDt(unsigned n, double x, double t = 1.0);
+double HierJacobi(unsigned n, double alpha, double beta, double x);
+double HierIJacobi(unsigned n, double alpha, double x);
+// FeHierarchicTria / FeHierarchicQuad (fe/hierarchic_fe.h:473-1680) of
+// uniform degree p with the cell's relative edge orientations ori[j] = +1/-1.
+void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, double* phi, double (*dphi)[2]);
+// fe::DiffusionElementMatrixProvider + fe::MassElementMatrixProvider
+// (fe/loc_comp_ellbvp.h:169-214, 349-378; rule degree 2p) summed, assembled
+// over a HierarchicScalarFESpace of uniform degree p (dh from
+// MakeDofHandler(m, 1, p-1, ...)); fe::ScalarLoadElementVectorProvider
+// (:642-685).  qdeg 0 = 2p.
+void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, const MeshFunction& gamma,
+                        int qdeg, COOMatrix& A);
+void AssembleHierLoad(const DofHandler& dh, int p, const MeshFunction& f, int qdeg, std::vector<double>& b);
+
 }  // namespace lfo

@@ -382,6 +382,56 @@ int lfo_init_essential(void* sp, const uint8_t* edge_flags, const lfo_coeff* g, 
   LFO_CATCH
 }
 
+// Hierarchic (hp) FE of uniform degree p on a space created with the layout
+// (1, p-1, interior tria, interior quad): fe::Diffusion + fe::Mass element
+// matrices (summed) and fe::ScalarLoadElementVectorProvider.
+int lfo_assemble_hier(void* sp, int p, const lfo_coeff* alpha, const lfo_coeff* gamma, int qdeg, void** out,
+                      char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction a = ToMF(alpha, alpha && alpha->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  const MeshFunction g = ToMF(gamma, gamma && gamma->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  auto A = std::make_unique<COOMatrix>();
+  A->rows = A->cols = s->dh.num_dofs;
+  AssembleHierMatrix(s->dh, p, a, g, qdeg, *A);
+  *out = A.release();
+  LFO_CATCH
+}
+
+int lfo_assemble_hier_load(void* sp, int p, const lfo_coeff* f, int qdeg, double* b, char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(f, f && f->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  std::vector<double> bv(b, b + s->dh.num_dofs);
+  AssembleHierLoad(s->dh, p, mf, qdeg, bv);
+  std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
+// FeHierarchicTria / Quad shape values and reference gradients at npts points.
+int lfo_hier_shape(int is_quad, int p, const int8_t* ori, int npts, const double* xy, double* phi, double* dphi,
+                   char* err, int errlen) {
+  LFO_TRY
+  const int n = is_quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
+  for (int k = 0; k < npts; ++k)
+    EvalHierShape(is_quad != 0, p, ori, xy[2 * k], xy[2 * k + 1], phi + static_cast<size_t>(k) * n,
+                  reinterpret_cast<double(*)[2]>(dphi + static_cast<size_t>(k) * n * 2));
+  LFO_CATCH
+}
+
+double lfo_hier_fn(int which, int n, double a, double b, double x) {
+  switch (which) {
+    case 0: return HierLegendre(n, x, a);
+    case 1: return HierILegendre(n, x, a);
+    case 2: return HierILegendreDx(n, x, a);
+    case 3: return HierILegendreDt(n, x, a);
+    case 4: return HierJacobi(n, a, b, x);
+    default: return HierIJacobi(n, a, x);
+  }
+}
+
 int lfo_assemble_tabulated(void* sp, const double* elem, int ld, double* vec_elem, double* b,
                            void** out, char* err, int errlen) {
   LFO_TRY

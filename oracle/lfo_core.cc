@@ -1225,3 +1225,229 @@ void InitEssentialCondition(const DofHandler& dh, int degree, const uint8_t* edg
 }
 
 }  // namespace lfo
+
+// ====================================================== hierarchic (hp) FE ==
+namespace lfo {
+
+// fe/hierarchic_fe.cc:10-27 -- shifted, scaled Legendre polynomials by their
+// three-term recurrence.
+double HierLegendre(unsigned n, double x, double t) {
+  if (n == 0) return 1.0;
+  if (n == 1) return 2 * x - t;
+  double pm = 1.0, pc = 2 * x - t;
+  for (unsigned i = 2; i <= n; ++i) {
+    const double pn = (2.0 * i - 1) * (2 * x - t) / i * pc - (i - 1.0) * t * t / i * pm;
+    pm = pc;
+    pc = pn;
+  }
+  return pc;
+}
+
+// fe/hierarchic_fe.cc:29-45
+double HierILegendre(unsigned n, double x, double t) {
+  if (n == 1) return x;
+  return (HierLegendre(n, x, t) - t * t * HierLegendre(n - 2, x, t)) / (2.0 * (2.0 * n - 1));
+}
+double HierILegendreDx(unsigned n, double x, double t) { return HierLegendre(n - 1, x, t); }
+double HierILegendreDt(unsigned n, double x, double t) {
+  if (n == 1) return 0.0;
+  return -0.5 * (HierLegendre(n - 1, x, t) + t * HierLegendre(n - 2, x, t));
+}
+
+// fe/hierarchic_fe.cc:55-81 -- Jacobi polynomials P_n^(alpha,beta)(2x - 1).
+double HierJacobi(unsigned n, double alpha, double beta, double x) {
+  x = 2 * x - 1;
+  if (n == 0) return 1.0;
+  const double ab = alpha + beta;
+  double p0 = 1.0, p1 = 0.5 * (alpha - beta + x * (ab + 2));
+  for (unsigned j = 1; j < n; ++j) {
+    const double a1 = 2 * (j + 1) * (j + ab + 1) * (2 * j + ab);
+    const double a2 = (2 * j + ab + 1) * (alpha * alpha - beta * beta);
+    const double a3 = (2 * j + ab) * (2 * j + ab + 1) * (2 * j + ab + 2);
+    const double a4 = 2 * (j + alpha) * (j + beta) * (2 * j + ab + 2);
+    const double p2 = ((a2 + a3 * x) * p1 - a4 * p0) / a1;
+    p0 = p1;
+    p1 = p2;
+  }
+  return p1;
+}
+
+// fe/hierarchic_fe.cc:87-127 -- integrated Jacobi polynomials through the
+// recurrence of P^(alpha-1, 0)-type terms and the final three-term
+// combination of that file.
+double HierIJacobi(unsigned n, double alpha, double x) {
+  if (n == 0) return -1.0;
+  if (n == 1) return x;
+  auto coef = [alpha](unsigned j, double& a, double& b, double& c, double& d) {
+    a = 2.0 * j * (j + alpha) * (2.0 * j + alpha - 2);
+    b = 2.0 * j + alpha - 1;
+    c = (2.0 * j + alpha) * (2.0 * j + alpha - 2);
+    d = 2.0 * (j + alpha - 1) * (j - 1.0) * (2.0 * j + alpha);
+  };
+  double a, b, c, d;
+  double q2 = 1.0, q1 = (2 + alpha) * x - 1;  // terms j-2, j-1
+  coef(2, a, b, c, d);
+  double q0 = (b * (c * (2 * x - 1) + alpha * alpha) * q1 - d * q2) / a;
+  for (unsigned j = 2; j < n; ++j) {
+    coef(j + 1, a, b, c, d);
+    const double qn = (b * (c * (2 * x - 1) + alpha * alpha) * q0 - d * q1) / a;
+    q2 = q1;
+    q1 = q0;
+    q0 = qn;
+  }
+  const double an = (n + alpha) / ((2.0 * n + alpha - 1) * (2.0 * n + alpha));
+  const double bn = alpha / ((2.0 * n + alpha - 2) * (2.0 * n + alpha));
+  const double cn = (n - 1.0) / ((2.0 * n + alpha - 2) * (2.0 * n + alpha - 1));
+  return an * q0 + bn * q1 - cn * q2;
+}
+
+void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, double* phi, double (*dphi)[2]) {
+  if (!is_quad) {
+    // FeHierarchicTria::EvalReferenceShapeFunctions / Gradients... (hierarchic_fe.h:576-870)
+    const double l[3] = {1 - x - y, x, y};
+    const double g[3][2] = {{-1, -1}, {1, 0}, {0, 1}};
+    for (int v = 0; v < 3; ++v) {
+      phi[v] = l[v];
+      dphi[v][0] = g[v][0];
+      dphi[v][1] = g[v][1];
+    }
+    int cur = 3;
+    for (int e = 0; e < 3; ++e) {
+      const int a = e, b = (e + 1) % 3;
+      const double t = l[a] + l[b];
+      const double tx = g[a][0] + g[b][0], ty = g[a][1] + g[b][1];
+      for (int i = 0; i < p - 1; ++i) {
+        const int src = ori[e] > 0 ? b : a;
+        const int row = ori[e] > 0 ? cur + i : cur + p - 2 - i;
+        phi[row] = HierILegendre(i + 2, l[src], t);
+        const double lx = HierILegendreDx(i + 2, l[src], t), lt = HierILegendreDt(i + 2, l[src], t);
+        dphi[row][0] = lx * g[src][0] + lt * tx;
+        dphi[row][1] = lx * g[src][1] + lt * ty;
+      }
+      cur += p - 1;
+    }
+    if (p > 2) {
+      const int src = ori[0] > 0 ? 1 : 0;
+      const double t = l[0] + l[1];
+      for (int i = 0; i < p - 2; ++i) {
+        const double ev = HierILegendre(i + 2, l[src], t);
+        const double lx = HierILegendreDx(i + 2, l[src], t), lt = HierILegendreDt(i + 2, l[src], t);
+        const double ex = lx * g[src][0] + lt * (g[0][0] + g[1][0]);
+        const double ey = lx * g[src][1] + lt * (g[0][1] + g[1][1]);
+        for (int j = 0; j < p - i - 2; ++j) {
+          const double ji = HierIJacobi(j + 1, 2.0 * i + 4, l[2]);
+          const double jd = HierJacobi(j, 2.0 * i + 4, 0.0, l[2]);  // IJacobiDx(j+1) = Jacobi(j)
+          phi[cur] = ev * ji;
+          dphi[cur][0] = ji * ex + ev * jd * g[2][0];
+          dphi[cur][1] = ji * ey + ev * jd * g[2][1];
+          ++cur;
+        }
+      }
+    }
+    return;
+  }
+  // FeHierarchicQuad (hierarchic_fe.h:1238-1430): products of the segment
+  // functions s_0 = 1 - t, s_1 = t, s_k = ILegendre(k, t), in x, y, 1-x, 1-y.
+  auto s = [](int k, double t) { return k == 0 ? 1 - t : k == 1 ? t : HierILegendre(k, t); };
+  auto ds = [](int k, double t) { return k == 0 ? -1.0 : k == 1 ? 1.0 : HierILegendreDx(k, t); };
+  auto term = [&](int row, int kx, double sx, double sgnx, int ky, double sy, double sgny) {
+    phi[row] = s(kx, sx) * s(ky, sy);
+    dphi[row][0] = sgnx * ds(kx, sx) * s(ky, sy);
+    dphi[row][1] = s(kx, sx) * sgny * ds(ky, sy);
+  };
+  term(0, 0, x, 1, 0, y, 1);
+  term(1, 1, x, 1, 0, y, 1);
+  term(2, 1, x, 1, 1, y, 1);
+  term(3, 0, x, 1, 1, y, 1);
+  int cur = 4;
+  for (int i = 0; i < p - 1; ++i) {
+    if (ori[0] > 0) term(cur + i, 2 + i, x, 1, 0, y, 1);
+    else term(cur + p - 2 - i, 2 + i, 1 - x, -1, 0, y, 1);
+  }
+  cur += p - 1;
+  for (int i = 0; i < p - 1; ++i) {
+    if (ori[1] > 0) term(cur + i, 1, x, 1, 2 + i, y, 1);
+    else term(cur + p - 2 - i, 1, x, 1, 2 + i, 1 - y, -1);
+  }
+  cur += p - 1;
+  for (int i = 0; i < p - 1; ++i) {
+    if (ori[2] > 0) term(cur + i, 2 + i, 1 - x, -1, 1, y, 1);
+    else term(cur + p - 2 - i, 2 + i, x, 1, 1, y, 1);
+  }
+  cur += p - 1;
+  for (int i = 0; i < p - 1; ++i) {
+    if (ori[3] > 0) term(cur + i, 0, x, 1, 2 + i, 1 - y, -1);
+    else term(cur + p - 2 - i, 0, x, 1, 2 + i, y, 1);
+  }
+  cur += p - 1;
+  for (int i = 0; i < p - 1; ++i)
+    for (int j = 0; j < p - 1; ++j) term(cur++, j + 2, x, 1, i + 2, y, 1);
+}
+
+namespace {
+int HierNumShape(bool q, int p) { return q ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2; }
+
+void HierCellData(const DofHandler& dh, idx_t c, int p, int qdeg, std::vector<double>& phi, std::vector<double>& dphi,
+                  QuadRule& qr) {
+  const Mesh& m = *dh.mesh;
+  const bool q = m.IsQuad(c);
+  qr = MakeQuadRule(q, qdeg > 0 ? qdeg : 2 * p);
+  int8_t ori[4];
+  for (int j = 0; j < 4; ++j) ori[j] = m.cell_ori[c][j];
+  const int n = HierNumShape(q, p);
+  phi.assign(static_cast<size_t>(qr.n()) * n, 0.0);
+  dphi.assign(static_cast<size_t>(qr.n()) * n * 2, 0.0);
+  for (int k = 0; k < qr.n(); ++k)
+    EvalHierShape(q, p, ori, qr.x[k], qr.y[k], &phi[k * n],
+                  reinterpret_cast<double(*)[2]>(&dphi[static_cast<size_t>(k) * n * 2]));
+}
+}  // namespace
+
+void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, const MeshFunction& gamma,
+                        int qdeg, COOMatrix& A) {
+  const Mesh& m = *dh.mesh;
+  std::vector<double> phi, dphi, av, gv, mat;
+  QuadRule qr;
+  AssembleMatrixLocally(dh, [&](idx_t c, std::vector<double>& out) {
+    HierCellData(dh, c, p, qdeg, phi, dphi, qr);
+    const int n = HierNumShape(m.IsQuad(c), p);
+    const CellGeom geo = m.Geom(c);
+    alpha.Eval(m, c, qr, av);
+    gamma.Eval(m, c, qr, gv);
+    out.assign(static_cast<size_t>(n) * n, 0.0);
+    std::vector<double> gx(n), gy(n);
+    for (int k = 0; k < qr.n(); ++k) {
+      const double w = qr.w[k] * geo.IntegrationElement(qr.x[k], qr.y[k]);
+      double JT[2][2];
+      geo.JinvT(qr.x[k], qr.y[k], JT);
+      for (int i = 0; i < n; ++i) {
+        const double* d = &dphi[(static_cast<size_t>(k) * n + i) * 2];
+        gx[i] = JT[0][0] * d[0] + JT[0][1] * d[1];
+        gy[i] = JT[1][0] * d[0] + JT[1][1] * d[1];
+      }
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          out[i * n + j] += w * (gx[i] * (av[k] * gx[j]) + gy[i] * (av[k] * gy[j])) +
+                            w * (gv[k] * phi[k * n + i]) * phi[k * n + j];
+    }
+  }, A);
+}
+
+void AssembleHierLoad(const DofHandler& dh, int p, const MeshFunction& f, int qdeg, std::vector<double>& b) {
+  const Mesh& m = *dh.mesh;
+  std::vector<double> phi, dphi, fv;
+  QuadRule qr;
+  AssembleVectorLocally(dh, [&](idx_t c, std::vector<double>& out) {
+    HierCellData(dh, c, p, qdeg, phi, dphi, qr);
+    const int n = HierNumShape(m.IsQuad(c), p);
+    const CellGeom geo = m.Geom(c);
+    f.Eval(m, c, qr, fv);
+    out.assign(n, 0.0);
+    for (int k = 0; k < qr.n(); ++k) {
+      const double s = qr.w[k] * geo.IntegrationElement(qr.x[k], qr.y[k]) * fv[k];
+      for (int i = 0; i < n; ++i) out[i] += s * phi[k * n + i];
+    }
+  }, b);
+}
+
+}  // namespace lfo

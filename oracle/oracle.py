@@ -92,6 +92,13 @@ def lib():
             L.lfo_csr_destroy.argtypes = [vp]
             L.lfo_nodal_projection.argtypes = [vp, C.c_int, P(dp), P(dp), C.c_char_p, C.c_int]
             L.lfo_kat_tensor_rd.argtypes = [P(dp), C.c_char_p, C.c_int]
+            L.lfo_assemble_hier.argtypes = [vp, C.c_int, P(lfo_coeff), P(lfo_coeff), C.c_int, P(vp), C.c_char_p,
+                                            C.c_int]
+            L.lfo_assemble_hier_load.argtypes = [vp, C.c_int, P(lfo_coeff), C.c_int, P(dp), C.c_char_p, C.c_int]
+            L.lfo_hier_shape.argtypes = [C.c_int, C.c_int, P(C.c_int8), C.c_int, P(dp), P(dp), P(dp), C.c_char_p,
+                                         C.c_int]
+            L.lfo_hier_fn.argtypes = [C.c_int, C.c_int, dp, dp, dp]
+            L.lfo_hier_fn.restype = dp
             L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
                                         C.c_char_p, C.c_int]
             L.lfo_eval_fe.argtypes = [vp, P(dp), C.c_int, P(dp), P(dp), P(dp), C.c_char_p, C.c_int]
@@ -462,3 +469,42 @@ def init_essential_condition(space, edge_flags, g):
     err = _err()
     _check(lib().lfo_init_essential(space.h, flp, C.byref(g), _p(f, C.c_uint8), _p(v, C.c_double), err, 512), err)
     return f, v
+
+
+# ----------------------------------------------------------- hierarchic FE
+
+def hier_space(mesh, p):
+    """HierarchicScalarFESpace(mesh, p): the uniform dof layout (1, p-1, tria, quad interior)."""
+    return Space(mesh, 0, (1, p - 1, max(0, (p - 1) * (p - 2) // 2), (p - 1) * (p - 1)))
+
+
+def assemble_hier(space, p, alpha, gamma, qdeg=0):
+    h = C.c_void_p()
+    err = _err()
+    _check(lib().lfo_assemble_hier(space.h, p, C.byref(alpha), C.byref(gamma), qdeg, C.byref(h), err, 512), err)
+    return COO(h, space.num_dofs, space.num_dofs)
+
+
+def assemble_hier_load(space, p, f, qdeg=0, b=None):
+    b = np.zeros(space.num_dofs) if b is None else np.ascontiguousarray(b, np.float64).copy()
+    err = _err()
+    _check(lib().lfo_assemble_hier_load(space.h, p, C.byref(f), qdeg, _p(b, C.c_double), err, 512), err)
+    return b
+
+
+def hier_shape(is_quad, p, ori, pts):
+    """Shape values (k, n) and reference gradients (k, n, 2) of FeHierarchicTria/Quad."""
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 2)
+    n = (p + 1) ** 2 if is_quad else (p + 1) * (p + 2) // 2
+    o = np.ascontiguousarray(list(ori) + [1] * (4 - len(ori)), np.int8)
+    phi = np.zeros((len(pts), n))
+    dphi = np.zeros((len(pts), n, 2))
+    err = _err()
+    _check(lib().lfo_hier_shape(int(is_quad), p, _p(o, C.c_int8), len(pts), _p(pts, C.c_double),
+                                _p(phi, C.c_double), _p(dphi, C.c_double), err, 512), err)
+    return phi, dphi
+
+
+def hier_fn(which, n, a, b, x):
+    """0 Legendre(n,x,t=a) 1 ILegendre 2 ILegendreDx 3 ILegendreDt 4 Jacobi(n,a,b,x) 5 IJacobi(n,a,x)."""
+    return lib().lfo_hier_fn(which, n, a, b, x)
