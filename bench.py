@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--grad-size", type=int, default=1024, help="config-5 mesh size (0: skip the gradient leg)")
     ap.add_argument("--ho-size", type=int, default=1024, help="config-3 mesh size (0: skip the high-order leg)")
     ap.add_argument("--gmsh", type=int, default=1, help="run the Gmsh-reader leg (0: skip)")
+    ap.add_argument("--hier", type=int, default=1, help="run the hierarchic-FE leg (0: skip)")
     return ap.parse_args()
 
 
@@ -426,6 +427,49 @@ def gmsh_leg(L, W, ctx, n=512, cpu_check=False):
     return out
 
 
+def hier_leg(L, W, ctx, steps=3, cpu_check=False):
+    """Hierarchic (hp) FE: DiffusionElementMatrixProvider assembly with a
+    constant coefficient on TPTriag meshes (the folded affine-triangle kernel)
+    for degrees 2, 4, 6, 8 and on TPQuad meshes (the general per-point kernel)
+    for degrees 2 and 4, each mesh sized to about 400M triplets (6.4 GB) or
+    1024 x 1024 cells.  Triplets/s and the HBM rate of the triplet stream (16
+    bytes per triplet written); the oracle on one core on a small mesh."""
+    out = {"workload": "constant alpha = 1, gamma = 0, default rules (degree 2p)"}
+    alpha = L.coeff(L.CONSTANT, 1.0)
+    for kind, degrees in (("tria", (2, 4, 6, 8)), ("quad", (2, 4))):
+        for p in degrees:
+            nloc = (p + 1) * (p + 2) // 2 if kind == "tria" else (p + 1) ** 2
+            cells = 400e6 / (nloc * nloc)
+            nn = int(min(1024, math.sqrt(cells / (2 if kind == "tria" else 1))))
+            mesh = L.Mesh.tp_triag(ctx, nn, nn) if kind == "tria" else L.Mesh.tp_quad(ctx, nn, nn)
+            sp = L.Space.hierarchic(mesh, p)
+            ntrip = sp.num_triplets
+            coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, ntrip)
+            prov = L.rd_provider(alpha, L.coeff(L.ZERO))
+            L.assemble_matrix_rd(sp, prov, coo)
+            ctx.timer_begin()
+            for _ in range(steps):
+                coo.set_zero()
+                L.assemble_matrix_rd(sp, prov, coo)
+            ms = ctx.timer_end() / steps
+            out["%s_p%d" % (kind, p)] = {"mesh": "%dx%d" % (nn, nn), "cells": mesh.num_cells, "dofs": sp.num_dofs,
+                                         "triplets": ntrip, "ms": ms, "triplets_per_s": ntrip / (ms * 1e-3),
+                                         "triplet_write_gbs": ntrip * 16 / (ms * 1e-3) / 1e9}
+            del coo, sp, mesh
+    if cpu_check:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        xy, cells, pe = O.factory_input("tptriag", 32, 32)
+        om = O.Mesh(xy, cells, pe)
+        osp = O.hier_space(om, 4)
+        t0 = time.perf_counter()
+        A = O.assemble_hier(osp, 4, O.coeff(O.CONSTANT, 1.0), O.coeff(O.ZERO))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "oracle, TPTriag 32x32, degree 4",
+                               "triplets_per_s": len(A) / dt}
+    return out
+
+
 def batch_leg(L, W, ctx, count):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
     one persistent assembly launch + load + fix + COO->CSR + batched PCG.
@@ -708,6 +752,7 @@ def run_ours(args):
     edges = leg(edge_leg, L, W, ctx, mesh, space)
     post = leg(post_leg, L, W, ctx, mesh, space, cpu_check=(rank == 0 and not args.no_cpu_baseline))
     gmsh = leg(gmsh_leg, L, W, ctx, cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.gmsh else None
+    hier = leg(hier_leg, L, W, ctx, cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.hier else None
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size,
                 cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
@@ -743,7 +788,7 @@ def run_ours(args):
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
             "load_vector_ms": vec_ms,
-            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "gmsh": gmsh, "high_order": high_order, "solve": solve,
+            "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "gmsh": gmsh, "hier": hier, "high_order": high_order, "solve": solve,
             "batch": batch,
             "gradient": gradient,
         }

@@ -28,6 +28,8 @@
 
 #include "lfg_api.h"
 #include "lfg_coeff.h"
+#include "lfg_df32.h"
+#include "lfg_elem.h"
 #include "lfg_internal.h"
 
 namespace lfg {
@@ -36,17 +38,18 @@ namespace {
 constexpr int kHierBlock = 128;
 
 // Table block (doubles): w[nq] | x[nq] | y[nq] | then per pattern:
-//   phi[nq][n] | g[nq][n][2] | R[E][4] (triangles only)
+//   phi[nq][n] | g[nq][n][2] | R[E][4] | R32[E][4] (binary32 pairs, one
+//   double slot each)
 struct HierTab {
   int n = 0, nq = 0, E = 0, npat = 0;
-  int64_t off_pat = 0, stride = 0, o_g = 0, o_R = 0, total = 0;
+  int64_t off_pat = 0, stride = 0, o_g = 0, o_R = 0, o_R32 = 0, total = 0;
 };
 
 // Every block starts on a multiple of 4 doubles (32 bytes), so the vector
 // loads of the kernels (16 bytes) stay aligned.
 int64_t Pad4(int64_t x) { return (x + 3) & ~int64_t(3); }
 
-HierTab HierLayout(bool quad, int n, int nq) {
+HierTab HierLayout(bool quad, int n, int nq, bool folded) {
   HierTab t;
   t.n = n;
   t.nq = nq;
@@ -55,17 +58,19 @@ HierTab HierLayout(bool quad, int n, int nq) {
   t.off_pat = Pad4(3 * static_cast<int64_t>(nq));
   t.o_g = Pad4(static_cast<int64_t>(nq) * n);
   t.o_R = Pad4(t.o_g + 2 * static_cast<int64_t>(nq) * n);
-  t.stride = Pad4(t.o_R + (quad ? 0 : 4 * static_cast<int64_t>(t.E)));
+  const int64_t eb = folded ? 4 * static_cast<int64_t>(t.E) : 0;  // folded sums only when requested
+  t.o_R32 = Pad4(t.o_R + eb);
+  t.stride = Pad4(t.o_R32 + eb);
   t.total = t.off_pat + t.npat * t.stride;
   return t;
 }
 
-void BuildHierTable(bool quad, int p, int rule_degree, std::vector<double>& h, HierTab& L) {
+void BuildHierTable(bool quad, int p, int rule_degree, bool folded, std::vector<double>& h, HierTab& L) {
   Rule r;
   if (!MakeRule(quad, rule_degree, r))
     Fail(LFG_UNSUPPORTED, "no quadrature rule of degree " + std::to_string(rule_degree));
   const int n = quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
-  L = HierLayout(quad, n, r.n);
+  L = HierLayout(quad, n, r.n, folded);
   h.assign(static_cast<size_t>(L.total), 0.0);
   for (int k = 0; k < r.n; ++k) {
     h[k] = r.w[k];
@@ -83,8 +88,9 @@ void BuildHierTable(bool quad, int p, int rule_degree, std::vector<double>& h, H
         B[L.o_g + (static_cast<int64_t>(k) * n + i) * 2 + 1] = dphi[2 * i + 1];
       }
     }
-    if (quad) continue;
-    // folded sums in long double, upper triangle row by row
+    if (!folded) continue;
+    // folded sums in long double, upper triangle row by row (used for affine
+    // cells: triangles and parallelograms)
     int64_t e = 0;
     for (int i = 0; i < n; ++i)
       for (int j = i; j < n; ++j, ++e) {
@@ -103,17 +109,25 @@ void BuildHierTable(bool quad, int p, int rule_degree, std::vector<double>& h, H
         R[1] = static_cast<double>(s1);
         R[2] = static_cast<double>(s2);
         R[3] = static_cast<double>(s3);
+        float* R32 = reinterpret_cast<float*>(B + L.o_R32 + 4 * e);
+        const long double sv[4] = {s0, s1, s2, s3};
+        for (int q = 0; q < 4; ++q) {
+          const float hi = static_cast<float>(sv[q]);
+          R32[2 * q] = hi;
+          R32[2 * q + 1] = static_cast<float>(sv[q] - static_cast<long double>(hi));
+        }
       }
   }
 }
 
-// Cached on the context per (cell type, degree, rule degree).
-const double* GetHierTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, HierTab& L) {
-  const int key = (1 << 23) | (quad ? 1 << 20 : 0) | (p << 10) | rule_degree;
+// Cached on the context per (cell type, degree, rule degree, with or without
+// the folded sums of the affine kernel).
+const double* GetHierTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, bool folded, HierTab& L) {
+  const int key = (1 << 23) | (folded ? 1 << 24 : 0) | (quad ? 1 << 20 : 0) | (p << 10) | rule_degree;
   auto it = ctx->tables.find(key);
   if (it == ctx->tables.end()) {
     std::vector<double> h;
-    BuildHierTable(quad, p, rule_degree, h, L);
+    BuildHierTable(quad, p, rule_degree, folded, h, L);
     TableEntry& ent = ctx->tables[key];
     ent.layout = Tab{};
     ent.layout.n = L.n;
@@ -123,8 +137,26 @@ const double* GetHierTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, Hier
     LFG_CUDA(cudaStreamSynchronize(ctx->stream));
     return ent.buf.as<double>();
   }
-  L = HierLayout(quad, it->second.layout.n, it->second.layout.nq);
+  L = HierLayout(quad, it->second.layout.n, it->second.layout.nq, folded);
   return it->second.buf.as<double>();
+}
+
+// Division by a run-time constant d without a hardware divide:
+// q / d = (q * m) >> 40 with m = 2^40 / d + 1, exact whenever q * d < 2^40
+// (the error q (m - 2^40/d) / 2^40 < q / 2^40 < 1/d stays below the gap
+// between q/d and the next integer).
+struct FastDiv {
+  uint64_t m = 1;
+  int d = 1;
+};
+FastDiv MakeFastDiv(int d) {
+  FastDiv f;
+  f.d = d;
+  f.m = (uint64_t(1) << 40) / static_cast<uint64_t>(d) + 1;
+  return f;
+}
+__device__ __forceinline__ int Div(int q, const FastDiv& f) {
+  return static_cast<int>((static_cast<uint64_t>(q) * f.m) >> 40);
 }
 
 struct HierArgs {
@@ -140,6 +172,8 @@ struct HierArgs {
   const double* tab;
   HierTab L;
   CoeffDev alpha, gamma;
+  unsigned long long* fallback;  // cells whose coefficients left the df32 range (FP64 route)
+  FastDiv div_n, div_E, div_nn;  // by n, E = n(n+1)/2 and n^2
 };
 
 __device__ __forceinline__ void StoreTriplet(lfg_triplet* p, int r, int c, double v) {
@@ -194,67 +228,118 @@ __device__ __forceinline__ void LoadVerts(const HierArgs& a, int c, int4& cn, do
   v[3] = QUAD ? a.xy[cn.w] : make_double2(0.0, 0.0);
 }
 
-// Affine triangles, cell-constant alpha / gamma: tiles of T cells per CTA.
-// Shared memory: vals[T][E] | coef[T][4] | base[T] (int64) | pat[T] | dofs[T][n].
-__global__ void __launch_bounds__(kHierBlock) HierTriaAffineKernel(HierArgs a, int T) {
+// Affine cells (triangles; parallelogram quadrilaterals), cell-constant
+// alpha / gamma: tiles of T cells per CTA.  The four per-cell coefficients
+// c = {alpha m00, alpha m01, alpha m11, gamma |det J|} are formed in FP64 and
+// each upper-triangle entry c . R_pat(e) is contracted in df32 on the FP32
+// pipes (4 error-free products, one FP64 add to convert), so the FP64 pipe
+// does about half an operation per triplet; a cell whose coefficients leave
+// the df32 range [2^-40, 2^40] is contracted in FP64 instead.
+// Shared memory: vals[T][E] | coef[T][4] | coef32[T][4] | base[T] | pat[T] |
+// cid[T] | safe[T] | dofs[T][n].
+template <bool QUAD, bool MASS>
+__global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T) {
+  using namespace df;
   extern __shared__ __align__(16) double smem[];
   const int n = a.L.n, E = a.L.E, nn = n * n;
   double* vals = smem;
   double* coef = vals + static_cast<int64_t>(T) * E;
-  int64_t* base = reinterpret_cast<int64_t*>(coef + 4 * T);
+  f2* coef32 = reinterpret_cast<f2*>(coef + 4 * T);
+  int64_t* base = reinterpret_cast<int64_t*>(coef32 + 4 * T);
   int* pat = reinterpret_cast<int*>(base + T);
   int* cid = pat + T;
-  int* dofs = cid + T;
+  int* safe = cid + T;
+  int* dofs = safe + T;
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * T; t0 < a.count; t0 += static_cast<int64_t>(gridDim.x) * T) {
     const int tn = static_cast<int>(min(static_cast<int64_t>(T), a.count - t0));
     for (int t = threadIdx.x; t < tn; t += blockDim.x) {
       const int c = a.list[t0 + t];
-      int4 cn;
-      double2 v[4];
-      LoadVerts<false>(a, c, cn, v);
-      double m00, m01, m11, adet, X, Y;
-      Metric<false>(v, 0.0, 0.0, m00, m01, m11, adet, X, Y);
-      const double al = CellConstant(a.alpha, c), ga = CellConstant(a.gamma, c);
-      coef[4 * t + 0] = m00 * al;
-      coef[4 * t + 1] = m01 * al;
-      coef[4 * t + 2] = m11 * al;
-      coef[4 * t + 3] = adet * ga;
+      const int4 cn = a.cells[c];
+      const double2 v0 = a.xy[cn.x], v1 = a.xy[cn.y], v2 = a.xy[QUAD ? cn.w : cn.z];
+      // affine map with columns v1 - v0 and (v2 or v3) - v0
+      const double j00 = v1.x - v0.x, j01 = v2.x - v0.x, j10 = v1.y - v0.y, j11 = v2.y - v0.y;
+      const double det = j00 * j11 - j10 * j01;
+      const double adet = fabs(det), inv = 1.0 / adet;
+      const double al = CellConstant(a.alpha, c), ga = MASS ? CellConstant(a.gamma, c) : 0.0;
+      double cf[4];
+      cf[0] = (j11 * j11 + j01 * j01) * inv * al;
+      cf[1] = -(j11 * j10 + j01 * j00) * inv * al;
+      cf[2] = (j10 * j10 + j00 * j00) * inv * al;
+      cf[3] = adet * ga;
+      bool ok = true;
+      for (int q = 0; q < 4; ++q) {
+        coef[4 * t + q] = cf[q];
+        coef32[4 * t + q] = FromDouble(cf[q]);
+        ok = ok && elem::DfSafe(cf[q]);
+      }
+      safe[t] = ok;
+      if (!ok) atomicAdd(a.fallback, 1ull);
       base[t] = a.tri_offset[c];
-      pat[t] = a.ori[c] & 7;
+      pat[t] = a.ori[c] & (QUAD ? 15 : 7);
       cid[t] = c;
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < tn * n; idx += blockDim.x) {
-      const int t = idx / n, i = idx - t * n;
+      const int t = Div(idx, a.div_n), i = idx - t * n;
       dofs[idx] = a.cell_dofs[static_cast<int64_t>(cid[t]) * a.n_cell + i];
     }
     for (int idx = threadIdx.x; idx < tn * E; idx += blockDim.x) {
-      const int t = idx / E, e = idx - t * E;
-      const double* R = a.tab + a.L.off_pat + pat[t] * a.L.stride + a.L.o_R + 4 * static_cast<int64_t>(e);
-      const double2 r01 = *reinterpret_cast<const double2*>(R);
-      const double2 r23 = *reinterpret_cast<const double2*>(R + 2);
-      const double* cf = coef + 4 * t;
-      vals[idx] = cf[0] * r01.x + cf[1] * r01.y + cf[2] * r23.x + cf[3] * r23.y;
+      const int t = Div(idx, a.div_E), e = idx - t * E;
+      const double* blk = a.tab + a.L.off_pat + pat[t] * a.L.stride;
+      if (safe[t]) {
+        const float4 r01 = *reinterpret_cast<const float4*>(blk + a.L.o_R32 + 4 * static_cast<int64_t>(e));
+        const float4 r23 = *reinterpret_cast<const float4*>(blk + a.L.o_R32 + 4 * static_cast<int64_t>(e) + 2);
+        const f2* cf = coef32 + 4 * t;
+        Acc acc;
+        acc.AddProd(cf[0], f2{r01.x, r01.y});
+        acc.AddProd(cf[1], f2{r01.z, r01.w});
+        acc.AddProd(cf[2], f2{r23.x, r23.y});
+        if (MASS) acc.AddProd(cf[3], f2{r23.z, r23.w});
+        vals[idx] = ToDouble(acc.Value());
+      } else {
+        const double* R = blk + a.L.o_R + 4 * static_cast<int64_t>(e);
+        const double* cf = coef + 4 * t;
+        vals[idx] = cf[0] * R[0] + cf[1] * R[1] + cf[2] * R[2] + cf[3] * R[3];
+      }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < tn * nn; q += blockDim.x) {
-      const int t = q / nn, rr = q - t * nn;
-      const int i = rr / n, j = rr - i * n;
+      const int t = Div(q, a.div_nn), rr = q - t * nn;
+      const int i = Div(rr, a.div_n), j = rr - i * n;
       const int lo = min(i, j), hi = max(i, j);
-      const int e = lo * n - lo * (lo - 1) / 2 + (hi - lo);
+      const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
       StoreTriplet(a.out + base[t] + rr, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
     }
     __syncthreads();
   }
 }
 
-// General path: one cell per CTA iteration.  Shared memory: coef[nq][4] | dofs[n].
-template <bool QUAD>
+// Quadrilaterals that are not parallelograms (their element map is bilinear):
+// count[0] += 1 per such cell.
+__global__ void NonAffineQuadsKernel(int64_t nq, const int32_t* __restrict__ list, const int4* __restrict__ cells,
+                                     const double2* __restrict__ xy, unsigned long long* __restrict__ count) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nq;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int4 cn = cells[list[i]];
+    const double2 v0 = xy[cn.x], v1 = xy[cn.y], v2 = xy[cn.z], v3 = xy[cn.w];
+    const bool par = (v2.x - v3.x == v1.x - v0.x) && (v2.y - v3.y == v1.y - v0.y) &&
+                     (v2.x - v1.x == v3.x - v0.x) && (v2.y - v1.y == v3.y - v0.y);
+    if (!par) atomicAdd(count, 1ull);
+  }
+}
+
+// General path: one cell per CTA iteration.  Shared memory: coef[nq][4] |
+// dofs[n] | (SYM) vals[E].  SYM computes each upper-triangle entry once into
+// shared memory and writes both halves from there (half the FP64 work);
+// without SYM (elements too large for shared memory) every (i, j) sums its
+// own point loop.
+template <bool QUAD, bool SYM>
 __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
   extern __shared__ __align__(16) double smem[];
   const int n = a.L.n, nq = a.L.nq, nn = n * n;
   double* coef = smem;
-  int* dofs = reinterpret_cast<int*>(coef + 4 * nq);
+  double* vals = coef + 4 * nq;
+  int* dofs = reinterpret_cast<int*>(vals + (SYM ? a.L.E : 0));
   const double* __restrict__ tab = a.tab;
   for (int64_t ci = blockIdx.x; ci < a.count; ci += gridDim.x) {
     const int c = a.list[ci];
@@ -280,6 +365,7 @@ __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
     const int64_t base = a.tri_offset[c];
     for (int q = threadIdx.x; q < nn; q += blockDim.x) {
       const int i = q / n, j = q - i * n;
+      if (SYM && j < i) continue;
       double acc = 0.0;
       for (int k = 0; k < nq; ++k) {
         const double2 gi = *reinterpret_cast<const double2*>(G + (static_cast<int64_t>(k) * n + i) * 2);
@@ -288,7 +374,16 @@ __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
         acc += cf[0] * (gi.x * gj.x) + cf[1] * (gi.x * gj.y + gi.y * gj.x) + cf[2] * (gi.y * gj.y) +
                cf[3] * (P[static_cast<int64_t>(k) * n + i] * P[static_cast<int64_t>(k) * n + j]);
       }
-      StoreTriplet(a.out + base + q, dofs[i], dofs[j], acc);
+      if (SYM) vals[i * n - i * (i - 1) / 2 + (j - i)] = acc;
+      else StoreTriplet(a.out + base + q, dofs[i], dofs[j], acc);
+    }
+    if (SYM) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < nn; q += blockDim.x) {
+        const int i = q / n, j = q - i * n;
+        const int lo = min(i, j), hi = max(i, j);
+        StoreTriplet(a.out + base + q, dofs[i], dofs[j], vals[lo * n - lo * (lo - 1) / 2 + (hi - lo)]);
+      }
     }
     __syncthreads();
   }
@@ -359,6 +454,67 @@ int HierGrid(lfg_ctx* ctx, K kernel, size_t smem, int64_t work_items) {
 
 constexpr size_t kHierSmemLimit = 200 * 1024;
 
+// Quadrilaterals of the mesh that are not parallelograms (counted once).
+int64_t NonAffineQuads(lfg_mesh* m) {
+  if (m->nonaffine_quads >= 0) return m->nonaffine_quads;
+  lfg_ctx* ctx = m->ctx;
+  DevBuf cnt;
+  cnt.alloc(sizeof(unsigned long long), ctx->stream);
+  LFG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), ctx->stream));
+  if (m->nquad) {
+    NonAffineQuadsKernel<<<GridFor(ctx, m->nquad, 256), 256, 0, ctx->stream>>>(
+        m->nquad, m->quad_list.as<int32_t>(), m->cell_nodes.as<int4>(), m->xy.as<double2>(),
+        cnt.as<unsigned long long>());
+    LFG_LAUNCHED(ctx);
+  }
+  unsigned long long h = 0;
+  D2HSync(ctx, &h, cnt.p, sizeof(h));
+  m->nonaffine_quads = static_cast<int64_t>(h);
+  return m->nonaffine_quads;
+}
+
+template <bool QUAD>
+void LaunchAffine(lfg_ctx* ctx, const HierArgs& a, bool mass) {
+  const int n = a.L.n, E = a.L.E;
+  auto smem_for = [&](int t) {
+    return static_cast<size_t>(t) * E * 8 + static_cast<size_t>(t) * (4 * 8 + 4 * 8 + 8 + 4 * 4) +
+           static_cast<size_t>(t) * n * 4;
+  };
+  int T = std::max(1, std::min(32, 4096 / (n * n)));
+  while (T > 1 && smem_for(T) > 96 * 1024) --T;
+  const size_t smem = smem_for(T);
+  const int64_t tiles = (a.count + T - 1) / T;
+  ProfScope prof(ctx, QUAD ? "hier_quad_affine" : "hier_tria_affine");
+  if (mass) {
+    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, true>, smem, tiles);
+    HierAffineKernel<QUAD, true><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
+  } else {
+    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, false>, smem, tiles);
+    HierAffineKernel<QUAD, false><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
+  }
+  LFG_LAUNCHED(ctx);
+}
+
+bool AffineFits(bool quad, int p) {
+  const size_t n = quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
+  return n * (n + 1) / 2 * 8 + 96 + n * 4 <= kHierSmemLimit;
+}
+
+template <bool QUAD>
+void LaunchGeneral(lfg_ctx* ctx, const HierArgs& a) {
+  const size_t base = static_cast<size_t>(a.L.nq) * 32 + static_cast<size_t>(a.L.n) * 4;
+  const size_t sym = base + static_cast<size_t>(a.L.E) * 8;
+  ProfScope prof(ctx, QUAD ? "hier_general_quad" : "hier_general_tria");
+  if (sym <= kHierSmemLimit) {
+    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, true>, sym, a.count);
+    HierGeneralKernel<QUAD, true><<<grid, kHierBlock, sym, ctx->stream>>>(a);
+  } else {
+    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, false>, base, a.count);
+    HierGeneralKernel<QUAD, false><<<grid, kHierBlock, base, ctx->stream>>>(a);
+  }
+  LFG_LAUNCHED(ctx);
+}
+
 void HierAssembleMatrix(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo) {
   lfg_mesh* m = sp->mesh;
   lfg_ctx* ctx = m->ctx;
@@ -375,42 +531,32 @@ void HierAssembleMatrix(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo) 
   HierArgs a = BaseHierArgs(sp);
   a.out = coo->d + coo->size;
   a.alpha = ToDev(pr->alpha, m, "alpha");
+  auto set_div = [&](int n) {
+    a.div_n = MakeFastDiv(n);
+    a.div_E = MakeFastDiv(n * (n + 1) / 2);
+    a.div_nn = MakeFastDiv(n * n);
+  };
   a.gamma = ToDev(pr->gamma, m, "gamma");
+  a.fallback = reinterpret_cast<unsigned long long*>(StatusWord(ctx) + 12);
   const bool uniform = CellConstantKind(pr->alpha) && CellConstantKind(pr->gamma);
+  const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
   if (m->ntria) {
-    a.tab = GetHierTable(ctx, false, p, HierRuleDegree(pr->qr_degree_tria, p), a.L);
+    const bool affine = uniform && AffineFits(false, p);
+    a.tab = GetHierTable(ctx, false, p, HierRuleDegree(pr->qr_degree_tria, p), affine, a.L);
     a.list = m->tria_list.as<int32_t>();
     a.count = m->ntria;
-    const int n = a.L.n, E = a.L.E;
-    int T = std::max(1, std::min(32, 4096 / (n * n)));
-    auto smem_for = [&](int t) {
-      return static_cast<size_t>(t) * E * 8 + static_cast<size_t>(t) * (4 * 8 + 8 + 4 + 4) +
-             static_cast<size_t>(t) * n * 4;
-    };
-    while (T > 1 && smem_for(T) > 96 * 1024) --T;
-    if (uniform && smem_for(T) <= kHierSmemLimit) {
-      ProfScope prof(ctx, "hier_tria_affine");
-      const size_t smem = smem_for(T);
-      const int grid = HierGrid(ctx, HierTriaAffineKernel, smem, (a.count + T - 1) / T);
-      HierTriaAffineKernel<<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
-      LFG_LAUNCHED(ctx);
-    } else {
-      ProfScope prof(ctx, "hier_general_tria");
-      const size_t smem = static_cast<size_t>(a.L.nq) * 32 + static_cast<size_t>(n) * 4;
-      const int grid = HierGrid(ctx, HierGeneralKernel<false>, smem, a.count);
-      HierGeneralKernel<false><<<grid, kHierBlock, smem, ctx->stream>>>(a);
-      LFG_LAUNCHED(ctx);
-    }
+    set_div(a.L.n);
+    if (affine) LaunchAffine<false>(ctx, a, mass);
+    else LaunchGeneral<false>(ctx, a);
   }
   if (m->nquad) {
-    a.tab = GetHierTable(ctx, true, p, HierRuleDegree(pr->qr_degree_quad, p), a.L);
+    const bool affine = uniform && AffineFits(true, p) && NonAffineQuads(m) == 0;
+    a.tab = GetHierTable(ctx, true, p, HierRuleDegree(pr->qr_degree_quad, p), affine, a.L);
     a.list = m->quad_list.as<int32_t>();
     a.count = m->nquad;
-    ProfScope prof(ctx, "hier_general_quad");
-    const size_t smem = static_cast<size_t>(a.L.nq) * 32 + static_cast<size_t>(a.L.n) * 4;
-    const int grid = HierGrid(ctx, HierGeneralKernel<true>, smem, a.count);
-    HierGeneralKernel<true><<<grid, kHierBlock, smem, ctx->stream>>>(a);
-    LFG_LAUNCHED(ctx);
+    set_div(a.L.n);
+    if (affine) LaunchAffine<true>(ctx, a, mass);
+    else LaunchGeneral<true>(ctx, a);
   }
   coo->size += sp->num_triplets;
 }
@@ -432,7 +578,8 @@ void HierAssembleVector(lfg_space* sp, const lfg_load_provider* pr, double* b) {
     const bool quad = q == 1;
     const int64_t count = quad ? m->nquad : m->ntria;
     if (!count) continue;
-    a.tab = GetHierTable(ctx, quad, p, HierRuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, p), a.L);
+    a.tab = GetHierTable(ctx, quad, p, HierRuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, p), false,
+                         a.L);
     a.list = quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
     a.count = count;
     const size_t smem = static_cast<size_t>(a.L.nq) * 8;

@@ -136,6 +136,7 @@ struct lfg_mesh {
   lfg::DevBuf cell_ori;    // uint8[nc]: bit j set = local edge j negatively oriented
   lfg::DevBuf edge_nodes;  // int2[ne]
   lfg::DevBuf edge_ncell;  // int32[ne]
+  int64_t nonaffine_quads = -1;  // quadrilaterals that are not parallelograms (-1: not counted yet)
   lfg::DevBuf tria_list;   // int32[ntria]: cell indices of triangles (ascending)
   lfg::DevBuf quad_list;   // int32[nquad]
 };

@@ -527,6 +527,7 @@ lfg_status lfg_mesh_set_coords(lfg_mesh* m, const double* xy, int from_device) {
   LFG_CUDA(cudaMemcpyAsync(m->xy.p, xy, m->nv * sizeof(double2),
                            from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                            m->ctx->stream));
+  m->nonaffine_quads = -1;  // the geometry changed: recount parallelograms on next use
   LFG_API_END
 }
 

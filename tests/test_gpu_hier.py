@@ -102,6 +102,38 @@ def test_hier_high_degree(ctx, p):
         compare_triplets(coo.triplets(), r, c, v, _block_sizes(om.cells, p))
 
 
+@pytest.mark.parametrize("p", [2, 5])
+def test_hier_affine_quads_and_df32_fallback(ctx, p):
+    """TPQuad meshes are parallelograms: the folded (affine) kernel serves
+    them, also after the coordinates move (then the general kernel must take
+    over); a coefficient outside the df32 range takes the FP64 route."""
+    spec = {"kind": "tpquad", "nx": 6, "ny": 5}
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic(mesh, p)
+    om = oracle_mesh(spec)
+    osp = O.hier_space(om, p)
+    vals = np.exp(np.random.default_rng(p).standard_normal(mesh.num_cells))
+    vals[3] = 1e15  # outside [2^-40, 2^40]: FP64 route for that cell
+    vd = ctx.to_device(vals)
+    coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets)
+    L.assemble_matrix_rd(sp, L.rd_provider(L.coeff(L.PER_CELL, data=vd), L.coeff(L.CONSTANT, 0.3)), coo)
+    r, c, v = O.assemble_hier(osp, p, O.coeff(O.PER_CELL, data=vals), O.coeff(O.CONSTANT, 0.3)).arrays()
+    compare_triplets(coo.triplets(), r, c, v, _block_sizes(om.cells, p))
+    # move one interior node: a quad stops being a parallelogram
+    xy, _ = mesh.geometry()
+    xy = xy.copy()
+    inner = np.where((xy[:, 0] > 0.1) & (xy[:, 0] < 0.9) & (xy[:, 1] > 0.1) & (xy[:, 1] < 0.9))[0][0]
+    xy[inner] += [0.013, -0.007]
+    mesh.set_coords(xy)
+    xs, cs, pe = O.factory_input("tpquad", 6, 5)
+    om2 = O.Mesh(xy, cs, pe)
+    osp2 = O.hier_space(om2, p)
+    coo.set_zero()
+    L.assemble_matrix_rd(sp, L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO)), coo)
+    r, c, v = O.assemble_hier(osp2, p, O.coeff(O.CONSTANT, 1.0), O.coeff(O.ZERO)).arrays()
+    compare_triplets(coo.triplets(), r, c, v, _block_sizes(om2.cells, p))
+
+
 def test_degree15_poisson_known_answer(ctx):
     """lf_fe.diffusion_mat_test (loc_comp_tests.cc:47-128): degree 15 on test
     mesh 0, -lap u = 2 pi^2 u, u = sin(pi x) sin(pi y), zero Dirichlet data;
