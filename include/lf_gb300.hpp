@@ -36,6 +36,12 @@
 //   fe::NodalProjection (fe/fe_tools.h:198)        fe::NodalProjection(fes, u[, pred])
 //   fe::InitEssentialConditionFromFunction         fe::InitEssentialConditionFromFunction(fes, edge
 //     (fe/fe_tools.h:263)                            flags, g) -> (flags, values) device vectors
+//   fe::HierarchicScalarFESpace(mesh, degree)      fe::HierarchicScalarFESpace(mesh, degree) (uniform degree)
+//     (fe/hierarchic_scalar_fe_space.h:36)
+//   fe::DiffusionElementMatrixProvider,            fe::DiffusionElementMatrixProvider,
+//   fe::MassElementMatrixProvider,                 fe::MassElementMatrixProvider,
+//   fe::ScalarLoadElementVectorProvider            fe::ScalarLoadElementVectorProvider (on a hierarchic
+//     (fe/loc_comp_ellbvp.h:76-700)                  space; the assemble:: functions take them)
 //   io::GmshReader(factory, filename)              io::GmshReader(ctx, filename): mesh(),
 //     (io/gmsh_reader.h)                             PhysicalEntityNr, IsPhysicalEntity,
 //                                                    PhysicalEntityName2Nr / Nr2Name,
@@ -192,9 +198,10 @@ namespace uscalfe {
 // Lagrangian FE space of degree P on a mesh; it is its own DofHandler.
 class FeSpaceLagrange {
  public:
-  FeSpaceLagrange(std::shared_ptr<const mesh::Mesh> m, int degree) : mesh_(std::move(m)) {
+  FeSpaceLagrange(std::shared_ptr<const mesh::Mesh> m, int degree, bool hierarchic = false) : mesh_(std::move(m)) {
     lfg_space* h = nullptr;
-    mesh_->ctx().Check(lfg_space_create_lagrange(mesh_->get(), degree, &h));
+    mesh_->ctx().Check(hierarchic ? lfg_space_create_hierarchic(mesh_->get(), degree, &h)
+                                  : lfg_space_create_lagrange(mesh_->get(), degree, &h));
     h_ = h;
   }
   ~FeSpaceLagrange() { lfg_space_destroy(h_); }
@@ -477,6 +484,28 @@ inline void FixFlaggedSolutionComponents(const DeviceVector<uint8_t>& flags, con
 }  // namespace assemble
 
 namespace fe {
+
+// HierarchicScalarFESpace(mesh, degree): hierarchic (hp) shape functions of a
+// uniform degree 1..20; the same space handle as the Lagrangian spaces.
+inline std::shared_ptr<uscalfe::FeSpaceLagrange> HierarchicScalarFESpace(std::shared_ptr<const mesh::Mesh> m,
+                                                                        int degree) {
+  return std::make_shared<uscalfe::FeSpaceLagrange>(std::move(m), degree, true);
+}
+// fe::DiffusionElementMatrixProvider(fe_space, alpha) and
+// fe::MassElementMatrixProvider(fe_space, gamma) (fe/loc_comp_ellbvp.h:76,
+// 256); rules make_QuadRule(ref_el, 2 * degree).
+class DiffusionElementMatrixProvider : public uscalfe::ReactionDiffusionElementMatrixProvider {
+ public:
+  DiffusionElementMatrixProvider(std::shared_ptr<const uscalfe::FeSpaceLagrange> fes, uscalfe::MeshFunction alpha)
+      : uscalfe::ReactionDiffusionElementMatrixProvider(std::move(fes), alpha, uscalfe::MeshFunction::Zero()) {}
+};
+class MassElementMatrixProvider : public uscalfe::ReactionDiffusionElementMatrixProvider {
+ public:
+  MassElementMatrixProvider(std::shared_ptr<const uscalfe::FeSpaceLagrange> fes, uscalfe::MeshFunction gamma)
+      : uscalfe::ReactionDiffusionElementMatrixProvider(std::move(fes), uscalfe::MeshFunction::Zero(), gamma) {}
+};
+// fe::ScalarLoadElementVectorProvider (fe/loc_comp_ellbvp.h:569)
+using ScalarLoadElementVectorProvider = uscalfe::ScalarLoadElementVectorProvider;
 
 // An FE function u_h = sum_i dofs[i] b_i of a Lagrangian space; the dof
 // vector is referenced and must outlive the mesh function.

@@ -4,6 +4,7 @@
 // 1e-12 of each element matrix's largest entry, the load vector within 1e-12,
 // a converged PCG solve, and the adjoint Function object against central
 // differences of its own forward.  Exit status 0 = all checks passed.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -249,6 +250,34 @@ static void CheckGmsh(const g::Context& ctx, const char* dir) {
   std::printf("gmsh: two-element mesh read, diagonal group = edge set of size %lld\n", static_cast<long long>(nd));
 }
 
+// fe::HierarchicScalarFESpace with fe::MassElementMatrixProvider: the mass
+// matrix of degree 4 sums (1^T M 1) to the area, the diffusion matrix
+// annihilates constants.
+static void CheckHierarchic(const g::Context& ctx) {
+  auto mesh = g::mesh::TPTriagMeshBuilder(ctx).setNumXCells(6).setNumYCells(5).Build();
+  auto fes = g::fe::HierarchicScalarFESpace(mesh, 4);
+  const int64_t nd = fes->NumDofs();
+  g::fe::MassElementMatrixProvider mp(fes, g::uscalfe::MeshFunction::Constant(1.0));
+  g::assemble::COOMatrix M(ctx, nd, nd, fes->NumTriplets());
+  g::assemble::AssembleMatrixLocally(0, *fes, *fes, mp, M);
+  // the vertex functions sum to one: 1^T M 1 restricted to vertex dofs = area
+  const int64_t nv = mesh->NumEntities(2);
+  double s = 0.0;
+  for (const lfg_triplet& t : M.Download())
+    if (t.row < nv && t.col < nv) s += t.value;
+  CHECK(std::fabs(s - 1.0) < 1e-12, "hierarchic mass matrix over vertex functions sums to %.15g", s);
+  g::fe::DiffusionElementMatrixProvider dp(fes, g::uscalfe::MeshFunction::Constant(2.0));
+  g::assemble::COOMatrix A(ctx, nd, nd, fes->NumTriplets());
+  g::assemble::AssembleMatrixLocally(0, *fes, *fes, dp, A);
+  std::vector<double> row(nv, 0.0);
+  for (const lfg_triplet& t : A.Download())
+    if (t.row < nv && t.col < nv) row[t.row] += t.value;
+  double mx = 0.0;
+  for (double r : row) mx = std::max(mx, std::fabs(r));
+  CHECK(mx < 1e-11, "diffusion matrix rows over vertex functions sum to %.3g", mx);
+  std::printf("hierarchic: degree 4, %lld dofs, mass area %.15f\n", static_cast<long long>(nd), s);
+}
+
 static double Lcg(uint64_t& s) {
   s = s * 6364136223846793005ull + 1442695040888963407ull;
   return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);  // [0, 1)
@@ -305,6 +334,7 @@ int main(int argc, char** argv) {
     CheckAdjoint(ctx);
     CheckEdges(ctx);
     CheckPost(ctx);
+    CheckHierarchic(ctx);
   } catch (const g::Error& e) {
     std::printf("FAIL: uncaught lf::gb300::Error %d: %s\n", static_cast<int>(e.code()), e.what());
     return 1;
