@@ -132,6 +132,20 @@ def algorithmic_bytes(space, mesh, kind):
     return per_cell * cells, per_cell
 
 
+def algorithmic_flops(space, mesh, kind, gamma_nonzero):
+    """FP64 flops of the reference's per-point element matrix sum for one
+    launch: (4 + 2 [gamma != 0]) n^2 nqp per cell (grad-grad 2 FMA per entry
+    and point, mass 1 FMA), with the default rule of degree 2p (triangles:
+    3/6/12 points for p = 1/2/3; quadrilaterals: (p+1)^2 Gauss points)."""
+    p = space.degree
+    if kind == "tria":
+        n, cells, nqp = space.n_tria, mesh.num_trias, {1: 3, 2: 6, 3: 12}[p]
+    else:
+        n, cells, nqp = space.n_quad, mesh.num_quads, (p + 1) ** 2
+    per_cell = (4 + 2 * int(gamma_nonzero)) * n * n * nqp
+    return per_cell * cells, per_cell
+
+
 def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
     """The oracle (C++ restatement of the reference path), timed on host cores
     over a bounded prefix of the same cells."""
@@ -713,6 +727,9 @@ def run_ours(args):
         peaks_src = "fallback 6800 GB/s"
         hbm_peak = 6800.0
     achieved = alg_bytes / (fam[dom][0] * 1e-3) / 1e9
+    alg_flops, flops_cell = algorithmic_flops(space, mesh, kind, wl["gamma"][0] != "zero")
+    fp64_peak = ctx.fp64_peak_tflops()
+    fp64_achieved = alg_flops / (fam[dom][0] * 1e-3) / 1e12
     whole_bytes = sum(algorithmic_bytes(space, mesh, k)[0] for k in ("tria", "quad"))
 
     # load vector (AssembleVectorLocally) time, informational
@@ -783,7 +800,13 @@ def run_ours(args):
                          "traffic_source": "ncu dram bytes per cell (1024x1024 case) x cells of one launch",
                          "kernel": dom,
                          "algorithmic_bytes_per_launch": alg_bytes, "bytes_per_cell": per_cell,
-                         "avg_launch_ms": fam[dom][0], "peak_source": peaks_src},
+                         "avg_launch_ms": fam[dom][0], "peak_source": peaks_src,
+                         "fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                                  "frac": fp64_achieved / fp64_peak, "flops_per_cell": flops_cell,
+                                  "algorithmic_flops_per_launch": alg_flops,
+                                  "peak_source": "lfg_measure_fp64_peak: FP64 FMA loop, this run",
+                                  "note": "the reference's per-point FP64 sum; the kernel contracts "
+                                          "folded tables in df32, so frac > 1 is possible"}},
             "kernels_ms": {k: v[0] for k, v in fam.items()},
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
