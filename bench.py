@@ -711,7 +711,7 @@ def run_ours(args):
     for _ in range(max(3, args.steps // 4)):
         step()
     fam = {}
-    for f in ("rd_tria_df", "rd_quad_df", "rd_general_tria", "rd_general_quad"):
+    for f in ("rd_tria_df", "rd_quad_df", "rd_quad_tc", "rd_general_tria", "rd_general_quad"):
         t, n = ctx.profile_read(f)
         if n:
             fam[f] = (t / n, n)

@@ -88,13 +88,21 @@ lfg_status lfg_l2_flush(lfg_ctx* ctx);
  * launch is bracketed by CUDA events on the context stream and accumulated
  * under its kernel family name ("rd_tria_df", "rd_quad_df", "rd_general_tria",
  * "rd_general_quad", "load_tria", "load_quad", "grad_rd", "misfit",
- * "batch_assemble"); "fp64_fallback_cells" counts cells that left the df32 range. */
+ * "batch_assemble", "rd_quad_tc"); "fp64_fallback_cells" counts cells that left the
+ * df32 range, "tc_timeouts" tensor-core pipeline waits that gave up (always 0
+ * on a healthy device; lfg_ctx_synchronize then fails with LFG_CUDA_ERROR). */
 lfg_status lfg_profile_enable(lfg_ctx* ctx, int enable);
 lfg_status lfg_profile_read(lfg_ctx* ctx, const char* family, double* total_ms, int64_t* launches);
 lfg_status lfg_profile_reset(lfg_ctx* ctx);
 /* Measured FP64 FMA throughput of this device (independent FMA chains on all
  * SMs), the denominator of the FP64 roofline fraction. */
 lfg_status lfg_measure_fp64_peak(lfg_ctx* ctx, double* tflops);
+/* Element matrices of Q2 quadrilaterals (cell-constant alpha, gamma = 0, tensor
+ * Gauss rules of 2x2 or 3x3 points) run on the tcgen05 tensor cores with an
+ * exact integer-digit splitting of the FP64 operands (kernel family
+ * "rd_quad_tc"); enable = 0 selects the df32 CUDA-core kernel ("rd_quad_df")
+ * instead.  Default: enabled.  No reference counterpart (a device choice). */
+lfg_status lfg_ctx_set_tensor_cores(lfg_ctx* ctx, int enable);
 
 /* --------------------------------------------------------------------- mesh
  * Replaces lf::mesh::hybrid2d::MeshFactory::AddPoint/AddEntity/Build

@@ -149,6 +149,11 @@ class Context:
     def profile_reset(self):
         self.check(lib().lfg_profile_reset(self.h))
 
+    def set_tensor_cores(self, enable):
+        """Q2 quadrilateral element matrices on the tcgen05 tensor cores
+        (default) or on the df32 CUDA-core kernel."""
+        self.check(lib().lfg_ctx_set_tensor_cores(self.h, 1 if enable else 0))
+
     def fp64_peak_tflops(self):
         t = C.c_double()
         self.check(lib().lfg_measure_fp64_peak(self.h, C.byref(t)))

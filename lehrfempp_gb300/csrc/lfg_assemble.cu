@@ -22,12 +22,15 @@
 // The device does FP64 arithmetic; cells are processed one per thread from
 // per-type cell lists (triangles and quadrilaterals run as separate launches
 // so a warp never diverges on the cell type).
+#include <algorithm>
+#include <cmath>
 #include <map>
 
 #include "lfg_api.h"
 #include "lfg_coeff.h"
 #include "lfg_elem.h"
 #include "lfg_internal.h"
+#include "lfg_tc.h"
 
 namespace lfg {
 void EnsureIncidence(lfg_space* sp);
@@ -604,6 +607,303 @@ __global__ void __launch_bounds__(128) RDQuadDfKernel(AsmArgs a, DfArgs d) {
   }
 }
 
+// ------------------------------------------ quadrilaterals on the tensor cores
+// Q2 on bilinear quadrilaterals, cell-constant alpha, gamma = 0, tensor Gauss
+// rule of M x M points (M = 2, 3).  The direct contraction
+//     A_K(e) = sum_kap c_kap(K) T(kap; e),  kap = 3 k + ab (point k, metric entry ab)
+// is a (128 cells x K) by (K x 45 entries) product per tile.  It runs on the
+// FP16 tensor cores (tcgen05, FP32 accumulation in tensor memory) without
+// losing FP64 accuracy, by splitting both operands into integer digits of 9
+// bits (an Ozaki-type splitting):
+//   row (cell):     c = 2^Er  sum_{i=1..6} a_i 2^-9i,  Er from the row's largest |c|,
+//   column (entry): T = 2^Ec  sum_{j=1..6} b_j 2^-9j,  Ec from the column's largest |T| (host),
+// |a_i|, |b_j| <= 257.  A digit product is an integer below 2^17, and the sum
+// over the 27 kap of all pairs of one level L = i + j stays below 2^24 for
+// L <= 5 (at most 4 pairs), so the FP32 accumulators of levels 2, 3, 4, 5 are
+// exact.  Levels 6 and 7 share a fifth accumulator in which the level-7 terms
+// enter with 2^-9-scaled table digits; it rounds only below 2^-54 of
+// 2^(Er + Ec).  Levels >= 8 are left out (below 2^-48 of 2^(Er + Ec)).  The
+// epilogue recombines the five accumulators of an entry into one int64
+// (G2 2^36 + G3 2^27 + G4 2^18 + G5 2^9 + G67) and one binary64.
+//
+// Tensor memory: 5 accumulators x 48 columns (45 entries padded) = 240 of the
+// 256 columns this CTA allocates; two CTAs share an SM.  Per tile and K step
+// of 16: five MMAs (A digit i against table digits 1..6-i in one N = (6-i) x 48
+// product whose columns land on levels i+1..6) and six N = 48 MMAs for level 7.
+// Shared memory: A digits [6][128 x KP] (reused for the FP64 tile after the
+// MMAs), table digits [2][6 x 48 x KP] (plain, 2^-9 scaled), column exponents,
+// tile dof indices and offsets.  Cells outside the df32-safe range take the
+// FP64 formula in the epilogue.
+// Threads: 256 per CTA, two per cell (row r = TMEM lane r): half 0 computes
+// the points [0, P0) and fills K columns [0, KP/2), half 1 the other points
+// and columns; in the epilogue each half converts 24 of the 48 entry columns.
+// The tile is then written one warp per cell, 32 consecutive triplets per store.
+constexpr uint32_t kTcMaxPolls = 1u << 22;
+constexpr int kTcNP = 48;       // accumulator columns per level (45 entries + 3)
+constexpr int kTcCols = 256;    // tensor memory columns per CTA
+
+__host__ __device__ constexpr int TcKP(int m) { return (3 * m * m + 15) / 16 * 16; }
+__host__ __device__ constexpr int TcABytes(int m) {
+  return 6 * 256 * TcKP(m) > 128 * 45 * 8 ? 6 * 256 * TcKP(m) : 128 * 45 * 8;
+}
+__host__ __device__ constexpr int TcBHalfBytes(int m) { return 6 * kTcNP * TcKP(m) * 2; }
+__host__ __device__ constexpr int TcImageBytes(int m) { return 2 * TcBHalfBytes(m) + kTcNP * 4; }
+__host__ __device__ constexpr int TcSmemBytes(int m) {
+  return TcABytes(m) + TcImageBytes(m) + 128 * 9 * 4 + 128 * 8;
+}
+
+__device__ __forceinline__ uint32_t HSub2(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+// G2 2^36 + G3 2^27 + G4 2^18 + G5 2^9 + G67 scaled by 2^shift, as binary64.
+__device__ __forceinline__ double TcCombine(float g2, float g3, float g4, float g5, float g67, int shift) {
+  const int hi = __float2int_rn(g2) * 512 + __float2int_rn(g3);
+  const long long mid = static_cast<long long>(__float2int_rn(g4)) * 512 + __float2int_rn(g5);
+  const long long t = static_cast<long long>(hi) * (1ll << 27) + mid * 512 + __float2int_rn(g67);
+  if (t == 0) return 0.0;
+  return __longlong_as_double(__double_as_longlong(__ll2double_rn(t)) + (static_cast<long long>(shift) << 52));
+}
+
+// elem::DfSafe on the exponent bits (integer pipe; |x| = 2^40 exactly counts
+// as outside, which only sends such a cell to the FP64 formula).
+__device__ __forceinline__ bool DfSafeBits(double x) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x)) << 1;
+  const uint32_t ex = static_cast<uint32_t>(u >> 53);
+  return u == 0 || (ex >= 1023u - 40u && ex < 1023u + 40u);
+}
+
+// Inputs of cell bucket[t0 + r] (vertices, alpha), loaded one tile ahead.
+__device__ __forceinline__ void TcFetch(const AsmArgs& a, int64_t t0, int r, int& c, double2 (&v)[4], double& al) {
+  if (t0 + r < a.count) {
+    int4 cn;
+    c = a.bucket[t0 + r];
+    LoadVerts<true>(a, c, cn, v);
+    al = CellConst(a.alpha, c);
+  }
+}
+
+// Kappa column of (point k, entry ab): the points [0, P0) of thread half 0
+// fill columns [0, KP/2), the points [P0, NQ) of half 1 columns [KP/2, KP).
+__host__ __device__ constexpr int TcKappa(int m, int k, int ab) {
+  return k < (m * m + 1) / 2 ? 3 * k + ab : TcKP(m) / 2 + 3 * (k - (m * m + 1) / 2) + ab;
+}
+
+template <int M>
+__global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const uint4* __restrict__ image,
+                                                      int* __restrict__ tc_timeouts) {
+  using elem::f2;
+  constexpr int N = 9, E = 45, NQ = M * M, KP = TcKP(M), KS = KP / 16, NP = kTcNP;
+  constexpr int P0 = (NQ + 1) / 2;   // points of thread half 0
+  constexpr int PH = P0;             // point slots per half (half 1 has NQ - P0 <= P0)
+  constexpr int HC = KP / 16;        // K cores (8 columns) per half
+  constexpr uint32_t SA = 256 * KP;  // one digit slice of the A tile, bytes
+  constexpr uint32_t SBO = KP * 16;  // 8-row group stride of both operands
+  static_assert(3 * P0 <= KP / 2, "a half's points must fit its columns");
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sA = smraw;
+  unsigned char* sB = smraw + TcABytes(M);
+  const int* sEc = reinterpret_cast<const int*>(sB + 2 * TcBHalfBytes(M));
+  int* sdofs = reinterpret_cast<int*>(sB + TcImageBytes(M));
+  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 128 * N);
+  double* svals = reinterpret_cast<double*>(sA);
+  __shared__ f2 sWt[NQ + M];
+  __shared__ uint32_t smax[2][128];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t s_taddr;
+
+  {
+    const f2* g = reinterpret_cast<const f2*>(d.tab);
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) sWt[i] = g[d.L.off_W + i];
+    for (int i = threadIdx.x; i < M; i += blockDim.x) sWt[NQ + i] = g[d.L.off_t + i];
+    uint4* dst = reinterpret_cast<uint4*>(sB);
+    for (int i = threadIdx.x; i < TcImageBytes(M) / 16; i += blockDim.x) dst[i] = image[i];
+  }
+  if (threadIdx.x == 0) tc::MbarInit(&mbar, 1);
+  if (threadIdx.x < 32) tc::TmemAlloc(&s_taddr, kTcCols);
+  tc::FenceProxyAsync();
+  tc::FenceBeforeSync();
+  __syncthreads();
+  tc::FenceAfterSync();
+  const uint32_t taddr = s_taddr;
+  const int half = threadIdx.x >> 7, r = threadIdx.x & 127, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t tlane = taddr + (static_cast<uint32_t>((r >> 5) * 32) << 16);
+  // triplets lane, lane + 32, lane + 64 of a cell: i | j << 8 | upper index << 16
+  int tmap[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const int w = lane + 32 * t, i = w / N, j = w - i * N;
+    tmap[t] = w < N * N ? (i | (j << 8) | (UpperIndex<N>(i, j) << 16)) : -1;
+  }
+  uint32_t phase = 0;
+  bool abort = false;
+  int c = 0;
+  double2 v[4] = {};
+  double al = 0.0;
+  TcFetch(a, static_cast<int64_t>(blockIdx.x) * 128, r, c, v, al);
+
+  for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * 128; t0 < a.count && !abort;
+       t0 += static_cast<int64_t>(gridDim.x) * 128) {
+    const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+    // ---- cell r, points of this half: df32 coefficients
+    bool safe = false;
+    f2 cpt[PH][3];
+#pragma unroll
+    for (int k = 0; k < PH; ++k)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+    float mx = 0.0f;
+    if (r < ncell) {
+      const double acd[6] = {v[1].x - v[0].x, v[1].y - v[0].y, v[3].x - v[0].x, v[3].y - v[0].y,
+                             (v[0].x - v[1].x) + (v[2].x - v[3].x), (v[0].y - v[1].y) + (v[2].y - v[3].y)};
+      safe = DfSafeBits(al);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) safe = safe && DfSafeBits(acd[k]);
+      if (safe) {
+        if (half == 0) elem::QuadPointCoeffsRangeDF<M, 0, P0>(acd, al, sWt + NQ, sWt, cpt);
+        else elem::QuadPointCoeffsRangeDF<M, P0, NQ>(acd, al, sWt + NQ, sWt, cpt);
+      }
+#pragma unroll
+      for (int k = 0; k < PH; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) mx = fmaxf(mx, fabsf(cpt[k][q].h));
+      if (half == 0) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) sdofs[r * N + i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+        soff[r] = a.tri_offset[c];
+      }
+    }
+    smax[half][r] = __float_as_uint(mx);
+    __syncthreads();
+    // ---- row exponent (both halves), digits of this half's columns -> A tile
+    const uint32_t mb = max(smax[0][r], smax[1][r]);
+    int e = mb ? static_cast<int>((mb >> 23) & 0xffu) - 127 : 0;
+    if (e < -70 || e > 70) safe = false;
+    if (!safe) {
+#pragma unroll
+      for (int k = 0; k < PH; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+      e = 0;
+    }
+    const float scale = __uint_as_float(static_cast<uint32_t>(127 + 52 - e) << 23);  // 2^(52 - e)
+    unsigned char* arow = sA + (r >> 3) * SBO + (r & 7) * 16 + half * HC * 128;
+#pragma unroll
+    for (int gk = 0; gk < HC; ++gk) {
+      uint32_t w[6][4];
+#pragma unroll
+      for (int pr = 0; pr < 4; ++pr) {
+        uint32_t p[2][6];
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          const int kl = gk * 8 + 2 * pr + s;  // column within the half
+          const f2 x = kl < 3 * PH ? cpt[kl / 3][kl % 3] : f2{0.0f, 0.0f};
+          // V = round(c 2^(54-Er)) = vhi 2^27 + vlo; W = V + bias = whi 2^27 + wlo, wlo in [0, 2^27)
+          const float hs = x.h * scale;
+          const int vhi = __float2int_rn(hs * 7.450580596923828125e-9f);  // 2^-27
+          const float rem = __fmaf_rn(static_cast<float>(vhi), -134217728.0f, hs);  // exact
+          const int wlo0 = __float2int_rn(rem) + __float2int_rn(x.l * scale) + 256 * ((1 << 18) + (1 << 9) + 1);
+          const int whi = vhi + 256 * ((1 << 9) + 1) + (wlo0 >> 27);
+          const uint32_t wlo = static_cast<uint32_t>(wlo0) & ((1u << 27) - 1u);
+          p[s][0] = 0x6600u + static_cast<uint32_t>(whi >> 18);
+          p[s][1] = 0x6400u | ((static_cast<uint32_t>(whi) >> 9) & 511u);
+          p[s][2] = 0x6400u | (static_cast<uint32_t>(whi) & 511u);
+          p[s][3] = 0x6400u | ((wlo >> 18) & 511u);
+          p[s][4] = 0x6400u | ((wlo >> 9) & 511u);
+          p[s][5] = 0x6400u | (wlo & 511u);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+          w[i][pr] = HSub2(__byte_perm(p[0][i], p[1][i], 0x5410), i == 0 ? 0x66006600u : 0x65006500u);
+      }
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+        *reinterpret_cast<uint4*>(arow + i * SA + gk * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+    }
+    tc::FenceProxyAsync();
+    __syncthreads();
+    // ---- one thread issues the tile's MMAs
+    if (threadIdx.x == 0) {
+      tc::FenceAfterSync();
+      const uint32_t a0 = tc::SmemAddr(sA), bu = tc::SmemAddr(sB), bs = bu + TcBHalfBytes(M);
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+#pragma unroll
+        for (int i = 1; i <= 5; ++i)
+          tc::MmaF16(taddr + (i - 1) * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                     tc::SmemDesc(bu + s * 256, 128, SBO), tc::IdescF16(128, (6 - i) * NP), s > 0 || i > 1);
+#pragma unroll
+      for (int s = 0; s < KS; ++s)
+#pragma unroll
+        for (int i = 1; i <= 6; ++i)
+          tc::MmaF16(taddr + 4 * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                     tc::SmemDesc(bs + (6 - i) * (NP / 8) * SBO + s * 256, 128, SBO), tc::IdescF16(128, NP), true);
+      tc::Commit(&mbar);
+    }
+    // next tile's cell inputs load while the tensor cores work
+    int c_n = 0;
+    double2 v_n[4] = {};
+    double al_n = 0.0;
+    TcFetch(a, t0 + static_cast<int64_t>(gridDim.x) * 128, r, c_n, v_n, al_n);
+    const bool ok = tc::MbarWait(&mbar, phase, kTcMaxPolls);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicAdd(tc_timeouts, 1);
+      abort = true;
+      break;
+    }
+    tc::FenceAfterSync();
+    // ---- epilogue: entries [24 half, 24 half + 24) of row r
+    double* vals = svals + r * E;
+    const int shift = e + 2 - 54;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int col = 24 * half + 8 * q;
+      float G[5][8];
+#pragma unroll
+      for (int l = 0; l < 5; ++l) tc::Ld8(tlane + l * NP + col, G[l]);
+      tc::WaitLd();
+      if (safe) {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int en = col + t;
+          if (en < E) vals[en] = TcCombine(G[0][t], G[1][t], G[2][t], G[3][t], G[4][t], shift + sEc[en]);
+        }
+      }
+    }
+    if (half == 0 && r < ncell && !safe) {
+      QuadUniformF64<N, false>(v, al, 0.0, a.tab, a.L, vals);
+      atomicAdd(a.fallback, 1ull);
+    }
+    tc::FenceBeforeSync();
+    __syncthreads();
+    // ---- write: one warp per cell, 32 consecutive triplets per store
+    for (int cl = warp; cl < ncell; cl += 8) {
+      lfg_triplet* base = a.out + soff[cl];
+      const int* dd = sdofs + cl * N;
+      const double* vv = svals + cl * E;
+#pragma unroll
+      for (int t = 0; t < 3; ++t)
+        if (tmap[t] >= 0)
+          StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
+    }
+    c = c_n;
+    al = al_n;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = v_n[i];
+    __syncthreads();
+  }
+  if (abort) tc::MbarWait(&mbar, phase ^ 1u, kTcMaxPolls);  // let an MMA still in flight finish
+  tc::FenceBeforeSync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::FenceAfterSync();
+    tc::TmemFree(taddr, kTcCols);
+  }
+}
+
 // --------------------------------------------------------------- load vector
 template <int DEG, bool QUAD, bool VARY>
 __global__ void __launch_bounds__(128) LoadVectorKernel(AsmArgs a) {
@@ -1041,6 +1341,87 @@ void LaunchQuadDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   Launch(RDQuadDfKernel<DEG, M, MASS, false>, ctx, a.count, smem, 128, a, d);
 }
 
+// FP16 bit pattern of a value that FP16 represents exactly (|v| in [2^-14, 2^15] or 0).
+uint16_t HalfBits(double v) {
+  if (v == 0.0) return 0;
+  const uint16_t s = v < 0.0 ? 0x8000 : 0;
+  int ex;
+  const double f = std::frexp(std::fabs(v), &ex);  // |v| = f 2^ex, f in [0.5, 1)
+  const double m = (2.0 * f - 1.0) * 1024.0;
+  if (ex + 14 < 1 || ex + 14 > 30 || m != std::floor(m)) Fail(LFG_UNSUPPORTED, "tensor-core table digit not exact");
+  return static_cast<uint16_t>(s | ((ex + 14) << 10) | static_cast<int>(m));
+}
+
+// Table digits of RDQuadTcKernel for the quad table block `tab` (FP64 T read
+// back from the device once): [plain | 2^-9 scaled] x [digit j = 1..6] x
+// [48 entries] x [KP] in the core-matrix layout, then the 48 column exponents.
+const uint4* GetQuadTcImage(lfg_ctx* ctx, const double* tab, const Tab& L, int m) {
+  auto it = ctx->tc_images.find(tab);
+  if (it != ctx->tc_images.end()) return it->second.as<uint4>();
+  const int K = 3 * L.nq, KP = TcKP(m), E = L.E;
+  std::vector<double> T(static_cast<size_t>(L.nq) * E * 4);
+  LFG_CUDA(cudaMemcpyAsync(T.data(), tab + L.off_T, T.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<uint16_t> img(static_cast<size_t>(TcImageBytes(m)) / 2, 0);
+  uint16_t* plain = img.data();
+  uint16_t* scaled = plain + TcBHalfBytes(m) / 2;
+  int32_t* ec = reinterpret_cast<int32_t*>(plain + TcBHalfBytes(m));
+  auto at = [&](int k, int ab, int e) { return T[(static_cast<size_t>(k) * E + e) * 4 + ab]; };
+  for (int e = 0; e < E; ++e) {
+    double mt = 0.0;
+    for (int k = 0; k < L.nq; ++k)
+      for (int ab = 0; ab < 3; ++ab) mt = std::max(mt, std::fabs(at(k, ab, e)));
+    int ex = 0;
+    if (mt > 0.0) std::frexp(mt, &ex);
+    ec[e] = mt > 0.0 ? ex + 1 : 0;  // |T| 2^-Ec < 1/2
+    for (int kab = 0; kab < K; ++kab) {
+      const int kap = TcKappa(m, kab / 3, kab % 3);
+      long long Y = std::llround(std::ldexp(at(kab / 3, kab % 3, e), 54 - ec[e]));
+      int b[7];
+      for (int j = 6; j >= 2; --j) {  // balanced 9-bit digits from the bottom
+        long long rr = ((Y % 512) + 512) % 512;
+        if (rr >= 256) rr -= 512;
+        b[j] = static_cast<int>(rr);
+        Y = (Y - rr) / 512;
+      }
+      b[1] = static_cast<int>(Y);
+      for (int j = 1; j <= 6; ++j) {
+        const int n = (j - 1) * kTcNP + e;
+        const size_t off = static_cast<size_t>(n / 8) * (KP / 8) * 64 + (kap / 8) * 64 + (n % 8) * 8 + kap % 8;
+        plain[off] = HalfBits(b[j]);
+        scaled[off] = HalfBits(std::ldexp(static_cast<double>(b[j]), -9));
+      }
+    }
+  }
+  DevBuf& buf = ctx->tc_images[tab];
+  buf.alloc(img.size() * 2, ctx->stream);
+  LFG_CUDA(cudaMemcpyAsync(buf.p, img.data(), img.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return buf.as<uint4>();
+}
+
+template <int M>
+void LaunchQuadTc(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  const uint4* img = GetQuadTcImage(ctx, a.tab, a.L, M);
+  int* timeouts = StatusWord(ctx) + 14;
+  // At least 80 KB of shared memory per CTA: never more than two CTAs on an
+  // SM, so their 2 x 256 tensor-memory columns always fit and no allocation waits.
+  const size_t smem = std::max<size_t>(TcSmemBytes(M), 80 * 1024);
+  auto kernel = RDQuadTcKernel<M>;
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                static_cast<int>(cudaSharedmemCarveoutMaxShared)));
+  // Two CTAs per SM (shared memory admits two; the occupancy query assumes a
+  // smaller carveout and answers one).  CTAs never wait on each other, so
+  // the grid is correct whatever the residency.
+  const int64_t tiles = (a.count + 127) / 128;
+  const int64_t grid = std::min<int64_t>(tiles, static_cast<int64_t>(ctx->num_sms) * 2);
+  if (grid <= 0) return;
+  kernel<<<static_cast<unsigned>(grid), 256, smem, ctx->stream>>>(a, d, img, timeouts);
+  LFG_LAUNCHED(ctx);
+}
+
 template <int DEG, int NQ>
 void LaunchTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   constexpr int N = (DEG + 1) * (DEG + 2) / 2, E = N * (N + 1) / 2;
@@ -1081,6 +1462,13 @@ void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, boo
     ProfScope prof(ctx, "rd_tria_df");
     if (mass) Launch(RDTriaDfKernel<DEG, true>, ctx, a.count, smem, 128, a, d);
     else Launch(RDTriaDfKernel<DEG, false>, ctx, a.count, smem, 128, a, d);
+    return;
+  }
+  if (DEG == 2 && QUAD && uniform && !mass && d.tab && ctx->tensor_cores && a.L.E == 45 && d.L.n1 == 3 &&
+      (d.L.m == 2 || d.L.m == 3) && a.L.nq == d.L.m * d.L.m) {
+    ProfScope prof(ctx, "rd_quad_tc");
+    if (d.L.m == 2) LaunchQuadTc<2>(ctx, a, d);
+    else LaunchQuadTc<3>(ctx, a, d);
     return;
   }
   if (uniform && d.tab && QUAD && d.L.m >= 2 && d.L.m <= 4) {

@@ -127,6 +127,13 @@ lfg_status lfg_profile_enable(lfg_ctx* ctx, int enable) {
 lfg_status lfg_profile_read(lfg_ctx* ctx, const char* family, double* total_ms, int64_t* launches) {
   LFG_API_BEGIN(ctx)
   if (!family) Fail(LFG_INVALID_ARG, "null family");
+  if (std::string(family) == "tc_timeouts") {
+    int32_t n = 0;
+    D2HSync(ctx, &n, StatusWord(ctx) + 14, sizeof(n));
+    if (total_ms) *total_ms = static_cast<double>(n);
+    if (launches) *launches = n;
+    return LFG_OK;
+  }
   if (std::string(family) == "fp64_fallback_cells") {  // element-kernel cells computed in FP64
     unsigned long long n = 0;
     D2HSync(ctx, &n, StatusWord(ctx) + 12, sizeof(n));
@@ -214,6 +221,7 @@ void FreeCtx(lfg_ctx* ctx) {
   ctx->status.reset();
   ctx->tables.clear();
   ctx->dftables.clear();
+  ctx->tc_images.clear();
   cudaStreamSynchronize(ctx->stream);
   for (auto& r : ctx->prof_pending) {
     cudaEventDestroy(r.a);
@@ -253,6 +261,18 @@ void* lfg_ctx_stream(lfg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream
 lfg_status lfg_ctx_synchronize(lfg_ctx* ctx) {
   LFG_API_BEGIN(ctx)
   LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  int32_t timeouts = 0;
+  D2HSync(ctx, &timeouts, StatusWord(ctx) + 14, sizeof(timeouts));
+  if (timeouts) {
+    LFG_CUDA(cudaMemsetAsync(StatusWord(ctx) + 14, 0, sizeof(int32_t), ctx->stream));
+    Fail(LFG_CUDA_ERROR, "tensor-core pipeline wait timed out; element matrices of the affected launch are invalid");
+  }
+  LFG_API_END
+}
+
+lfg_status lfg_ctx_set_tensor_cores(lfg_ctx* ctx, int enable) {
+  LFG_API_BEGIN(ctx)
+  ctx->tensor_cores = enable != 0;
   LFG_API_END
 }
 

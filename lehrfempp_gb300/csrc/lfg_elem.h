@@ -227,6 +227,40 @@ DF_HD void QuadPointCoeffsDF(const double (&acd)[6] /* ax, ay, cx, cy, dx, dy */
   }
 }
 
+// The same coefficients for the points k in [K0, K1) only (c[k - K0]), with
+// gamma = 0: the tensor-core quad kernel splits the points of a cell between
+// two threads.
+template <int M, int K0, int K1>
+DF_HD void QuadPointCoeffsRangeDF(const double (&acd)[6], double alpha, const f2* t, const f2* W, f2 (*c)[3]) {
+  using namespace df;
+  const f2 ax = FromDouble(acd[0]), ay = FromDouble(acd[1]), cx = FromDouble(acd[2]), cy = FromDouble(acd[3]);
+  const f2 dx = FromDouble(acd[4]), dy = FromDouble(acd[5]);
+  const f2 al = FromDouble(alpha);
+  f2 j00[M], j10[M], j01[M], j11[M], m00[M], m11[M];
+  DF_UNROLL
+  for (int q = 0; q < M; ++q) {
+    j00[q] = MulAdd(dx, t[q], ax);
+    j10[q] = MulAdd(dy, t[q], ay);
+    j01[q] = MulAdd(dx, t[q], cx);
+    j11[q] = MulAdd(dy, t[q], cy);
+  }
+  DF_UNROLL
+  for (int q = 0; q < M; ++q) {
+    m00[q] = Add(Mul(j11[q], j11[q]), Mul(j01[q], j01[q]));
+    m11[q] = Add(Mul(j10[q], j10[q]), Mul(j00[q], j00[q]));
+  }
+  DF_UNROLL
+  for (int k = K0; k < K1; ++k) {
+    const int p = k / M, q = k % M;
+    const f2 det = Sub(Mul(j00[q], j11[p]), Mul(j10[q], j01[p]));
+    const f2 s = Mul(Mul(W[k], al), Rcp(Abs(det)));
+    const f2 m01 = Neg(Add(Mul(j11[p], j10[q]), Mul(j01[p], j00[q])));
+    c[k - K0][0] = Mul(s, m00[p]);
+    c[k - K0][1] = Mul(s, m01);
+    c[k - K0][2] = Mul(s, m11[q]);
+  }
+}
+
 // Upper-triangle index of the unordered pair {i, j} in "for i: for j >= i" order.
 template <int N>
 DF_HD int UpperIdx(int i, int j) {
