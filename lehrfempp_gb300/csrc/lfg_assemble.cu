@@ -660,7 +660,10 @@ __device__ __forceinline__ uint32_t HSub2(uint32_t a, uint32_t b) {
 
 // G2 2^36 + G3 2^27 + G4 2^18 + G5 2^9 + G67 scaled by 2^shift, as binary64.
 __device__ __forceinline__ double TcCombine(float g2, float g3, float g4, float g5, float g67, int shift) {
-  const int hi = __float2int_rn(g2) * 512 + __float2int_rn(g3);
+  // |G2|, |G3| < 2^22: integer bits by the 1.5 2^23 shift on the FP32 pipe
+  const int i2 = __float_as_int(__fadd_rn(g2, 12582912.0f)) - 0x4B400000;
+  const int i3 = __float_as_int(__fadd_rn(g3, 12582912.0f)) - 0x4B400000;
+  const int hi = i2 * 512 + i3;
   const long long mid = static_cast<long long>(__float2int_rn(g4)) * 512 + __float2int_rn(g5);
   const long long t = static_cast<long long>(hi) * (1ll << 27) + mid * 512 + __float2int_rn(g67);
   if (t == 0) return 0.0;
@@ -673,6 +676,12 @@ __device__ __forceinline__ bool DfSafeBits(double x) {
   const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x)) << 1;
   const uint32_t ex = static_cast<uint32_t>(u >> 53);
   return u == 0 || (ex >= 1023u - 40u && ex < 1023u + 40u);
+}
+
+// FP64 formula for a cell outside the df32 range (rare; kept out of line so
+// that it stays out of the instruction cache of the main path).
+__device__ __noinline__ void TcFallback(const double2 (&v)[4], double al, const AsmArgs& a, double* vals) {
+  QuadUniformF64<9, false>(v, al, 0.0, a.tab, a.L, vals);
 }
 
 // Inputs of cell bucket[t0 + r] (vertices, alpha), loaded one tile ahead.
@@ -755,6 +764,13 @@ __global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const
 #pragma unroll
       for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
     float mx = 0.0f;
+    if (half == 1 && r < ncell) {  // dof indices and triplet offset of the cell, for the write phase
+      const int32_t* g = a.cell_dofs + static_cast<int64_t>(c) * a.n_cell;
+#pragma unroll
+      for (int i = 0; i < N; ++i) tc::CpAsync4(sdofs + r * N + i, g + i);
+      tc::CpAsync8(soff + r, a.tri_offset + c);
+    }
+    tc::CpAsyncCommit();
     if (r < ncell) {
       const double acd[6] = {v[1].x - v[0].x, v[1].y - v[0].y, v[3].x - v[0].x, v[3].y - v[0].y,
                              (v[0].x - v[1].x) + (v[2].x - v[3].x), (v[0].y - v[1].y) + (v[2].y - v[3].y)};
@@ -769,11 +785,6 @@ __global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const
       for (int k = 0; k < PH; ++k)
 #pragma unroll
         for (int q = 0; q < 3; ++q) mx = fmaxf(mx, fabsf(cpt[k][q].h));
-      if (half == 0) {
-#pragma unroll
-        for (int i = 0; i < N; ++i) sdofs[r * N + i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
-        soff[r] = a.tri_offset[c];
-      }
     }
     smax[half][r] = __float_as_uint(mx);
     __syncthreads();
@@ -874,9 +885,10 @@ __global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const
       }
     }
     if (half == 0 && r < ncell && !safe) {
-      QuadUniformF64<N, false>(v, al, 0.0, a.tab, a.L, vals);
+      TcFallback(v, al, a, vals);
       atomicAdd(a.fallback, 1ull);
     }
+    tc::CpAsyncWaitAll();
     tc::FenceBeforeSync();
     __syncthreads();
     // ---- write: one warp per cell, 32 consecutive triplets per store

@@ -104,6 +104,16 @@ __device__ __forceinline__ void Ld8(uint32_t taddr, float (&r)[8]) {
 }
 __device__ __forceinline__ void WaitLd() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// --- asynchronous global -> shared copies (no registers, no stall at issue)
+__device__ __forceinline__ void CpAsync4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(SmemAddr(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void CpAsync8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(SmemAddr(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void CpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void CpAsyncWaitAll() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // --- mbarrier
 __device__ __forceinline__ void MbarInit(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(mbar)), "r"(count) : "memory");
