@@ -805,8 +805,9 @@ def run_ours(args):
                                   "frac": fp64_achieved / fp64_peak, "flops_per_cell": flops_cell,
                                   "algorithmic_flops_per_launch": alg_flops,
                                   "peak_source": "lfg_measure_fp64_peak: FP64 FMA loop, this run",
-                                  "note": "the reference's per-point FP64 sum; the kernel contracts "
-                                          "folded tables in df32, so frac > 1 is possible"}},
+                                  "note": "the reference's per-point FP64 sum; the kernels contract it in "
+                                          "df32 (triangles) or as exact FP16 digit products on the tensor "
+                                          "cores (quadrilaterals), so frac > 1 is possible"}},
             "kernels_ms": {k: v[0] for k, v in fam.items()},
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
