@@ -151,8 +151,10 @@ class Context:
 
     def set_tensor_cores(self, enable):
         """Q2 quadrilateral element matrices on the tcgen05 tensor cores
-        (default) or on the df32 CUDA-core kernel."""
-        self.check(lib().lfg_ctx_set_tensor_cores(self.h, 1 if enable else 0))
+        (True / 1: warp-specialised kernel, the default; 2: the two-CTA
+        variant) or on the df32 CUDA-core kernel (False / 0)."""
+        mode = int(enable) if not isinstance(enable, bool) else (1 if enable else 0)
+        self.check(lib().lfg_ctx_set_tensor_cores(self.h, mode))
 
     def fp64_peak_tflops(self):
         t = C.c_double()

@@ -26,6 +26,8 @@
 #include <cmath>
 #include <map>
 
+#include <cuda_fp16.h>
+
 #include "lfg_api.h"
 #include "lfg_coeff.h"
 #include "lfg_elem.h"
@@ -647,7 +649,10 @@ __host__ __device__ constexpr int TcABytes(int m) {
   return 6 * 256 * TcKP(m) > 128 * 45 * 8 ? 6 * 256 * TcKP(m) : 128 * 45 * 8;
 }
 __host__ __device__ constexpr int TcBHalfBytes(int m) { return 6 * kTcNP * TcKP(m) * 2; }
-__host__ __device__ constexpr int TcImageBytes(int m) { return 2 * TcBHalfBytes(m) + kTcNP * 4; }
+// one 16-row block whose row 0 picks K column KP-1 of A digit 1 (the row info)
+__host__ __device__ constexpr int TcInfoBytes(int m) { return 16 * TcKP(m) * 2; }
+__host__ __device__ constexpr int TcEcOffset(int m) { return 2 * TcBHalfBytes(m) + TcInfoBytes(m); }
+__host__ __device__ constexpr int TcImageBytes(int m) { return TcEcOffset(m) + kTcNP * 4; }
 __host__ __device__ constexpr int TcSmemBytes(int m) {
   return TcABytes(m) + TcImageBytes(m) + 128 * 9 * 4 + 128 * 8;
 }
@@ -714,7 +719,7 @@ __global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char* sA = smraw;
   unsigned char* sB = smraw + TcABytes(M);
-  const int* sEc = reinterpret_cast<const int*>(sB + 2 * TcBHalfBytes(M));
+  const int* sEc = reinterpret_cast<const int*>(sB + TcEcOffset(M));
   int* sdofs = reinterpret_cast<int*>(sB + TcImageBytes(M));
   int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 128 * N);
   double* svals = reinterpret_cast<double*>(sA);
@@ -913,6 +918,296 @@ __global__ void __launch_bounds__(256) RDQuadTcKernel(AsmArgs a, DfArgs d, const
   if (threadIdx.x < 32) {
     tc::FenceAfterSync();
     tc::TmemFree(taddr, kTcCols);
+  }
+}
+
+// Warp-specialised variant, one CTA (16 warps) per SM, persistent.  Two
+// producer groups of four warps (one thread per cell, all nine points)
+// alternate tiles: tile j of the CTA goes to group j & 1, A-digit buffer
+// j & 1 and tensor-memory accumulator block j & 1 (columns 256 (j & 1) ..
+// + 255).  An eight-warp consumer group (two threads per cell) drains the
+// accumulators of every tile in order into FP64 values and writes the
+// triplets.  Hand-offs: mma_done[b] (tcgen05.commit: A buffer b is free and
+// accumulator block b is ready), tmem_free[b] (the consumers have read
+// accumulator block b).  The row exponent and df32-range flag of each cell
+// travel through the accumulator block too (column 240: A digit 1 at K column
+// KP-1 times a unit table column).  Every wait gives up after 2^22 polls; a
+// group leaves its loop on the same iteration in all its threads.
+constexpr int kWsThreads = 512;
+__host__ __device__ constexpr int WsSmemBytes(int m) {
+  return 2 * 6 * 256 * TcKP(m) + TcImageBytes(m) + 128 * 45 * 8 + 2 * (128 * 9 * 4 + 128 * 8);
+}
+
+template <int M>
+__global__ void __launch_bounds__(kWsThreads, 1)
+    RDQuadTcWsKernel(AsmArgs a, DfArgs d, const uint4* __restrict__ image, int* __restrict__ tc_timeouts) {
+  using elem::f2;
+  constexpr int N = 9, E = 45, NQ = M * M, KP = TcKP(M), KS = KP / 16, NP = kTcNP;
+  constexpr int P0 = (NQ + 1) / 2;   // points in K columns [0, KP/2); the rest from KP/2
+  constexpr uint32_t SA = 256 * KP;  // one digit slice of an A tile, bytes
+  constexpr uint32_t SBO = KP * 16;  // 8-row group stride of both operands
+  constexpr int ABUF = 6 * SA;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sA = smraw;                          // [2][6][128 x KP]
+  unsigned char* sB = smraw + 2 * ABUF;               // table digits, info block, Ec
+  const int* sEc = reinterpret_cast<const int*>(sB + TcEcOffset(M));
+  double* svals = reinterpret_cast<double*>(sB + TcImageBytes(M));      // [128][45]
+  int* sdofs = reinterpret_cast<int*>(svals + 128 * E);                 // [2][128][9]
+  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 2 * 128 * N);      // [2][128]
+  __shared__ f2 sWt[NQ + M];
+  __shared__ __align__(8) uint64_t mma_done[2];
+  __shared__ __align__(8) uint64_t tmem_free[2];
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_abort;
+
+  {
+    const f2* g = reinterpret_cast<const f2*>(d.tab);
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) sWt[i] = g[d.L.off_W + i];
+    for (int i = threadIdx.x; i < M; i += blockDim.x) sWt[NQ + i] = g[d.L.off_t + i];
+    uint4* dst = reinterpret_cast<uint4*>(sB);
+    for (int i = threadIdx.x; i < TcImageBytes(M) / 16; i += blockDim.x) dst[i] = image[i];
+  }
+  if (threadIdx.x == 0) {
+    tc::MbarInit(&mma_done[0], 1);
+    tc::MbarInit(&mma_done[1], 1);
+    tc::MbarInit(&tmem_free[0], 256);
+    tc::MbarInit(&tmem_free[1], 256);
+    s_abort = 0;
+  }
+  if (threadIdx.x < 32) tc::TmemAlloc(&s_taddr, 512);
+  tc::FenceProxyAsync();
+  tc::FenceBeforeSync();
+  __syncthreads();
+  tc::FenceAfterSync();
+  const uint32_t taddr = s_taddr;
+  const int64_t tiles = (a.count + 127) / 128;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x < 256) {
+    // ================= producers: group b, one thread per cell =================
+    const int b = threadIdx.x >> 7, r = threadIdx.x & 127;
+    const int bar = 1 + b;
+    unsigned char* Ab = sA + b * ABUF;
+    const uint32_t dcol = taddr + 256 * b;
+    int c = 0;
+    double2 v[4] = {};
+    double al = 0.0;
+    const int64_t first = blockIdx.x + static_cast<int64_t>(b) * gridDim.x;
+    if (first < tiles) TcFetch(a, first * 128, r, c, v, al);
+    int m = 0;
+    for (;; ++m) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(b + 2 * m) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      const bool ok = m == 0 || tc::MbarWait(&mma_done[b], (m - 1) & 1, kTcMaxPolls);  // A buffer b free
+      if (tc::NamedSyncOr(bar, 128, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (r == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        break;
+      }
+      bool safe = false;
+      f2 cpt[NQ][4];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+      if (r < ncell) {
+        const double acd[6] = {v[1].x - v[0].x, v[1].y - v[0].y, v[3].x - v[0].x, v[3].y - v[0].y,
+                               (v[0].x - v[1].x) + (v[2].x - v[3].x), (v[0].y - v[1].y) + (v[2].y - v[3].y)};
+        safe = DfSafeBits(al);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) safe = safe && DfSafeBits(acd[k]);
+        if (safe) elem::QuadPointCoeffsDF<M, false>(acd, al, 0.0, sWt + NQ, sWt, cpt);
+      }
+      float mx = 0.0f;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) mx = fmaxf(mx, fabsf(cpt[k][q].h));
+      int e = mx > 0.0f ? static_cast<int>((__float_as_uint(mx) >> 23) & 0xffu) - 127 : 0;
+      if (e < -70 || e > 70) safe = false;
+      if (!safe) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+        e = 0;
+      }
+      const float scale = __uint_as_float(static_cast<uint32_t>(127 + 52 - e) << 23);  // 2^(52 - e)
+      unsigned char* arow = Ab + (r >> 3) * SBO + (r & 7) * 16;
+#pragma unroll
+      for (int gk = 0; gk < KP / 8; ++gk) {
+        uint32_t w[6][4];
+#pragma unroll
+        for (int pr = 0; pr < 4; ++pr) {
+          uint32_t p[2][6];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            // K column -> (point, entry) in the TcKappa order of the table image
+            const int kap = gk * 8 + 2 * pr + s, kl = kap < KP / 2 ? kap : kap - KP / 2;
+            const int k = (kap < KP / 2 ? 0 : P0) + kl / 3;
+            const bool used = kap < KP / 2 ? kl < 3 * P0 : kl < 3 * (NQ - P0);
+            const f2 x = used ? cpt[k][kl % 3] : f2{0.0f, 0.0f};
+            const float hs = x.h * scale;
+            const int vhi = __float2int_rn(hs * 7.450580596923828125e-9f);  // 2^-27
+            const float rem = __fmaf_rn(static_cast<float>(vhi), -134217728.0f, hs);  // exact
+            const int wlo0 = __float2int_rn(rem) + __float2int_rn(x.l * scale) + 256 * ((1 << 18) + (1 << 9) + 1);
+            const int whi = vhi + 256 * ((1 << 9) + 1) + (wlo0 >> 27);
+            const uint32_t wlo = static_cast<uint32_t>(wlo0) & ((1u << 27) - 1u);
+            p[s][0] = 0x6600u + static_cast<uint32_t>(whi >> 18);
+            p[s][1] = 0x6400u | ((static_cast<uint32_t>(whi) >> 9) & 511u);
+            p[s][2] = 0x6400u | (static_cast<uint32_t>(whi) & 511u);
+            p[s][3] = 0x6400u | ((wlo >> 18) & 511u);
+            p[s][4] = 0x6400u | ((wlo >> 9) & 511u);
+            p[s][5] = 0x6400u | (wlo & 511u);
+          }
+#pragma unroll
+          for (int i = 0; i < 6; ++i)
+            w[i][pr] = HSub2(__byte_perm(p[0][i], p[1][i], 0x5410), i == 0 ? 0x66006600u : 0x65006500u);
+        }
+        if (gk == KP / 8 - 1) {  // row info in digit 1, K column KP - 1: e + 128, or 0 off the df32 range
+          const uint32_t info = __half_as_ushort(__float2half_rn(safe ? static_cast<float>(e + 128) : 0.0f));
+          w[0][3] = (w[0][3] & 0xffffu) | (info << 16);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+          *reinterpret_cast<uint4*>(arow + i * SA + gk * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+      }
+      tc::FenceProxyAsync();
+      tc::NamedSync(bar, 128);
+      if (r == 0) {
+        bool free_ok = m == 0 || tc::MbarWait(&tmem_free[b], (m - 1) & 1, kTcMaxPolls);
+        if (!free_ok) {
+          atomicAdd(tc_timeouts, 1);
+          s_abort = 1;
+        } else {
+          tc::FenceAfterSync();
+          const uint32_t a0 = tc::SmemAddr(Ab), bu = tc::SmemAddr(sB), bs = bu + TcBHalfBytes(M);
+          const uint32_t bi = bu + 2 * TcBHalfBytes(M);
+#pragma unroll
+          for (int s = 0; s < KS; ++s)
+#pragma unroll
+            for (int i = 1; i <= 5; ++i)
+              tc::MmaF16(dcol + (i - 1) * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                         tc::SmemDesc(bu + s * 256, 128, SBO), tc::IdescF16(128, (6 - i) * NP), s > 0 || i > 1);
+#pragma unroll
+          for (int s = 0; s < KS; ++s)
+#pragma unroll
+            for (int i = 1; i <= 6; ++i)
+              tc::MmaF16(dcol + 4 * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                         tc::SmemDesc(bs + (6 - i) * (NP / 8) * SBO + s * 256, 128, SBO), tc::IdescF16(128, NP),
+                         true);
+          tc::MmaF16(dcol + 5 * NP, tc::SmemDesc(a0 + (KS - 1) * 256, 128, SBO),
+                     tc::SmemDesc(bi + (KS - 1) * 256, 128, SBO), tc::IdescF16(128, 16), false);
+          tc::Commit(&mma_done[b]);
+        }
+      }
+      // inputs of this group's next tile load while the tensor cores work
+      const int64_t nxt = tile + 2 * static_cast<int64_t>(gridDim.x);
+      if (nxt < tiles) TcFetch(a, nxt * 128, r, c, v, al);
+    }
+    // the group's last MMAs finish before the tensor memory is released
+    if (r == 0 && m > 0) tc::MbarWait(&mma_done[b], (m - 1) & 1, kTcMaxPolls);
+  } else {
+    // ================= consumers: two threads per cell =================
+    const int et = threadIdx.x - 256, half = et >> 7, r = et & 127, ew = et >> 5;
+    const uint32_t tl = static_cast<uint32_t>((r >> 5) * 32) << 16;
+    int tmap[3];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      const int w = lane + 32 * t, i = w / N, j = w - i * N;
+      tmap[t] = w < N * N ? (i | (j << 8) | (UpperIndex<N>(i, j) << 16)) : -1;
+    }
+    // dof indices of tile 0 (half 1 stages them; tile j uses buffer j & 1)
+    if (half == 1 && blockIdx.x < tiles && static_cast<int64_t>(blockIdx.x) * 128 + r < a.count) {
+      const int c0 = a.bucket[static_cast<int64_t>(blockIdx.x) * 128 + r];
+      const int32_t* g = a.cell_dofs + static_cast<int64_t>(c0) * a.n_cell;
+#pragma unroll
+      for (int i = 0; i < N; ++i) tc::CpAsync4(sdofs + r * N + i, g + i);
+      tc::CpAsync8(soff + r, a.tri_offset + c0);
+    }
+    tc::CpAsyncCommit();
+    for (int j = 0;; ++j) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(j) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      const int b = j & 1;
+      const int64_t t1 = t0 + static_cast<int64_t>(gridDim.x) * 128;  // next tile
+      int c_next = -1;
+      if (half == 1 && t1 + r < a.count) c_next = a.bucket[t1 + r];
+      const bool ok = tc::MbarWait(&mma_done[b], (j >> 1) & 1, kTcMaxPolls);
+      if (tc::NamedSyncOr(3, 256, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (et == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        break;
+      }
+      tc::FenceAfterSync();
+      const uint32_t acc = taddr + 256 * b + tl;
+      float inf[8];
+      tc::Ld8(acc + 5 * NP, inf);
+      tc::WaitLd();
+      const int info = static_cast<int>(inf[0]);
+      const bool safe = info != 0;
+      const int shift = info - 128 + 2 - 54;
+      double* vals = svals + r * E;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int col = 24 * half + 8 * q;
+        float G[5][8];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) tc::Ld8(acc + l * NP + col, G[l]);
+        tc::WaitLd();
+        if (safe) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int en = col + t;
+            if (en < E) vals[en] = TcCombine(G[0][t], G[1][t], G[2][t], G[3][t], G[4][t], shift + sEc[en]);
+          }
+        }
+      }
+      tc::FenceBeforeSync();
+      tc::MbarArrive(&tmem_free[b]);
+      if (half == 0 && r < ncell && !safe) {
+        int cf = 0;
+        double2 vf[4] = {};
+        double alf = 0.0;
+        TcFetch(a, t0, r, cf, vf, alf);
+        TcFallback(vf, alf, a, vals);
+        atomicAdd(a.fallback, 1ull);
+      }
+      // stage the next tile's dof indices (its buffer was read by tile j - 1)
+      if (c_next >= 0) {
+        const int32_t* g = a.cell_dofs + static_cast<int64_t>(c_next) * a.n_cell;
+        int* dn = sdofs + ((j + 1) & 1) * 128 * N + r * N;
+#pragma unroll
+        for (int i = 0; i < N; ++i) tc::CpAsync4(dn + i, g + i);
+        tc::CpAsync8(soff + ((j + 1) & 1) * 128 + r, a.tri_offset + c_next);
+      }
+      tc::CpAsyncCommit();
+      asm volatile("cp.async.wait_group 1;" ::: "memory");  // this tile's group has landed
+      tc::NamedSync(3, 256);
+      const int* sd = sdofs + b * 128 * N;
+      const int64_t* so = soff + b * 128;
+      for (int cl = ew; cl < ncell; cl += 8) {
+        lfg_triplet* base = a.out + so[cl];
+        const int* dd = sd + cl * N;
+        const double* vv = svals + cl * E;
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+          if (tmap[t] >= 0)
+            StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
+      }
+      tc::NamedSync(3, 256);
+    }
+    tc::CpAsyncWaitAll();
+  }
+  tc::FenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::FenceAfterSync();
+    tc::TmemFree(taddr, 512);
   }
 }
 
@@ -1378,7 +1673,9 @@ const uint4* GetQuadTcImage(lfg_ctx* ctx, const double* tab, const Tab& L, int m
   std::vector<uint16_t> img(static_cast<size_t>(TcImageBytes(m)) / 2, 0);
   uint16_t* plain = img.data();
   uint16_t* scaled = plain + TcBHalfBytes(m) / 2;
-  int32_t* ec = reinterpret_cast<int32_t*>(plain + TcBHalfBytes(m));
+  uint16_t* info = plain + TcBHalfBytes(m);
+  int32_t* ec = reinterpret_cast<int32_t*>(plain + TcEcOffset(m) / 2);
+  info[((KP - 1) / 8) * 64 + 7] = HalfBits(1.0);  // row 0, K column KP - 1
   auto at = [&](int k, int ab, int e) { return T[(static_cast<size_t>(k) * E + e) * 4 + ab]; };
   for (int e = 0; e < E; ++e) {
     double mt = 0.0;
@@ -1411,6 +1708,20 @@ const uint4* GetQuadTcImage(lfg_ctx* ctx, const double* tab, const Tab& L, int m
   LFG_CUDA(cudaMemcpyAsync(buf.p, img.data(), img.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
   LFG_CUDA(cudaStreamSynchronize(ctx->stream));
   return buf.as<uint4>();
+}
+
+template <int M>
+void LaunchQuadTcWs(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  const uint4* img = GetQuadTcImage(ctx, a.tab, a.L, M);
+  int* timeouts = StatusWord(ctx) + 14;
+  const size_t smem = WsSmemBytes(M);
+  auto kernel = RDQuadTcWsKernel<M>;
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  const int64_t tiles = (a.count + 127) / 128;
+  const int64_t grid = std::min<int64_t>(tiles, ctx->num_sms);  // one CTA per SM (512 TMEM columns each)
+  if (grid <= 0) return;
+  kernel<<<static_cast<unsigned>(grid), kWsThreads, smem, ctx->stream>>>(a, d, img, timeouts);
+  LFG_LAUNCHED(ctx);
 }
 
 template <int M>
@@ -1479,8 +1790,13 @@ void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, boo
   if (DEG == 2 && QUAD && uniform && !mass && d.tab && ctx->tensor_cores && a.L.E == 45 && d.L.n1 == 3 &&
       (d.L.m == 2 || d.L.m == 3) && a.L.nq == d.L.m * d.L.m) {
     ProfScope prof(ctx, "rd_quad_tc");
-    if (d.L.m == 2) LaunchQuadTc<2>(ctx, a, d);
-    else LaunchQuadTc<3>(ctx, a, d);
+    if (ctx->tensor_cores == 2) {
+      if (d.L.m == 2) LaunchQuadTc<2>(ctx, a, d);
+      else LaunchQuadTc<3>(ctx, a, d);
+    } else {
+      if (d.L.m == 2) LaunchQuadTcWs<2>(ctx, a, d);
+      else LaunchQuadTcWs<3>(ctx, a, d);
+    }
     return;
   }
   if (uniform && d.tab && QUAD && d.L.m >= 2 && d.L.m <= 4) {

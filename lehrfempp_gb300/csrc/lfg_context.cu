@@ -272,7 +272,8 @@ lfg_status lfg_ctx_synchronize(lfg_ctx* ctx) {
 
 lfg_status lfg_ctx_set_tensor_cores(lfg_ctx* ctx, int enable) {
   LFG_API_BEGIN(ctx)
-  ctx->tensor_cores = enable != 0;
+  if (enable < 0 || enable > 2) Fail(LFG_INVALID_ARG, "lfg_ctx_set_tensor_cores: enable must be 0, 1 or 2");
+  ctx->tensor_cores = enable;
   LFG_API_END
 }
 

@@ -114,6 +114,24 @@ __device__ __forceinline__ void CpAsync8(void* smem, const void* gmem) {
 __device__ __forceinline__ void CpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void CpAsyncWaitAll() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// --- named barriers (ids 1..15; count = threads taking part, a multiple of 32)
+__device__ __forceinline__ void NamedSync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+// bar.sync with an OR over the participants' predicates (the same answer in all of them).
+__device__ __forceinline__ bool NamedSyncOr(int id, int count, bool pred) {
+  uint32_t out;
+  asm volatile(
+      "{\n\t.reg .pred pi, po;\n\t"
+      "setp.ne.u32 pi, %1, 0;\n\t"
+      "bar.red.or.pred po, %2, %3, pi;\n\t"
+      "selp.u32 %0, 1, 0, po;\n\t}"
+      : "=r"(out)
+      : "r"(pred ? 1u : 0u), "r"(id), "r"(count)
+      : "memory");
+  return out != 0;
+}
+
 // --- mbarrier
 __device__ __forceinline__ void MbarInit(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(mbar)), "r"(count) : "memory");
@@ -129,6 +147,9 @@ __device__ __forceinline__ bool MbarTryWait(uint64_t* mbar, uint32_t parity) {
       : "r"(SmemAddr(mbar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+__device__ __forceinline__ void MbarArrive(uint64_t* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(SmemAddr(mbar)) : "memory");
 }
 // Waits for the phase with the given parity to complete; gives up after
 // max_iter polls (each poll may suspend the thread for a short,

@@ -58,14 +58,15 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
 @pytest.mark.parametrize("name,mesh,qr", CASES, ids=[c[0] for c in CASES])
-def test_tensor_core_quads_match_oracle(ctx, name, mesh, qr):
+def test_tensor_core_quads_match_oracle(ctx, name, mesh, qr, mode):
     m = mesh()
     ncell = len(m["cells"])
     rng = np.random.default_rng(len(name))
     alpha = np.exp(rng.uniform(-14, 14, ncell))  # twelve decades inside the df32 range
     wl = {"mesh": m, "degree": 2, "alpha": ("cell", alpha), "gamma": ("zero",), "qr_tria": 0, "qr_quad": qr}
-    t_tc, n_tc, err_tc = _run(ctx, wl, True)
+    t_tc, n_tc, err_tc = _run(ctx, wl, mode)
     t_df, n_df, err_df = _run(ctx, wl, False)
     assert n_tc == 1 and n_df == 0  # the tensor-core kernel ran (once), and only when enabled
     assert np.array_equal(t_tc["row"], t_df["row"]) and np.array_equal(t_tc["col"], t_df["col"])
@@ -73,28 +74,37 @@ def test_tensor_core_quads_match_oracle(ctx, name, mesh, qr):
     assert ctx.profile_read("tc_timeouts")[1] == 0
 
 
-def test_tensor_core_constant_alpha_and_fp64_cells(ctx):
+def test_tensor_core_mode_checked(ctx):
+    with pytest.raises(L.LfgError) as e:
+        ctx.set_tensor_cores(3)
+    assert e.value.code == L.INVALID_ARG
+
+
+@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
+def test_tensor_core_constant_alpha_and_fp64_cells(ctx, mode):
     """Constant alpha, and one tile mixing df32-range cells with cells whose
     alpha (1e15) sends them to the FP64 formula in the epilogue."""
     m = _quads(16, 0.25, 7)
     ncell = len(m["cells"])
     wl = {"mesh": m, "degree": 2, "alpha": ("const", 2.75), "gamma": ("zero",), "qr_tria": 0, "qr_quad": 0}
-    _run(ctx, wl, True)
+    _run(ctx, wl, mode)
     alpha = np.ones(ncell)
     alpha[::7] = 1e15
     before = ctx.profile_read("fp64_fallback_cells")[1]
     wl["alpha"] = ("cell", alpha)
-    _run(ctx, wl, True)
+    _run(ctx, wl, mode)
     assert ctx.profile_read("fp64_fallback_cells")[1] - before == len(alpha[::7])
 
 
-def test_tensor_core_many_tiles(ctx):
-    """90,000 quadrilaterals: 704 tiles of 128 cells, more than two per CTA
-    of the persistent grid, the last one partial."""
+@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
+def test_tensor_core_many_tiles(ctx, mode):
+    """90,000 quadrilaterals: 704 tiles of 128 cells, several per CTA of the
+    persistent grid (both producer groups and buffers cycle), the last one
+    partial."""
     m = _quads(300, 0.3, 8)
     rng = np.random.default_rng(9)
     wl = {"mesh": m, "degree": 2, "alpha": ("cell", np.exp(rng.standard_normal(len(m["cells"])))),
           "gamma": ("zero",), "qr_tria": 0, "qr_quad": 0}
-    _, n_tc, err = _run(ctx, wl, True)
+    _, n_tc, err = _run(ctx, wl, mode)
     assert n_tc == 1 and err < 1e-13
     ctx.synchronize()  # raises if a tensor-core wait had timed out
