@@ -117,7 +117,8 @@ class ClockSampler:
 # to a full launch by the cell count.  Command and figures:
 # profiles/element_kernels_hybrid_o2.md.
 DRAM_BYTES_PER_CELL = {"rd_tria_df": (134030080 + 547695616) / 1048980,
-                       "rd_quad_df": (120022528 + 620115200) / 524086}
+                       "rd_quad_df": (120022528 + 620115200) / 524086,
+                       "rd_quad_tc": (120872960 + 619725824) / 524086}
 
 
 def algorithmic_bytes(space, mesh, kind):
@@ -732,6 +733,23 @@ def run_ours(args):
     fp64_achieved = alg_flops / (fam[dom][0] * 1e-3) / 1e12
     whole_bytes = sum(algorithmic_bytes(space, mesh, k)[0] for k in ("tria", "quad"))
 
+    # pure write stream of 4 GB (informational: the element kernels' bytes are ~80 % writes)
+    write_gbs = None
+    try:
+        import torch
+        wbuf = torch.empty(1 << 30, dtype=torch.int32, device="cuda:%d" % local)
+        wbuf.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            wbuf.zero_()
+        e1.record()
+        torch.cuda.synchronize()
+        write_gbs = wbuf.numel() * 4 * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        del wbuf
+    except Exception:  # torch absent or no memory: the key stays null
+        write_gbs = None
+
     # load vector (AssembleVectorLocally) time, informational
     b = ctx.zeros(space.num_dofs)
     lprov = L.load_provider(W.to_coeff(ctx, wl["f"], keep))
@@ -811,6 +829,7 @@ def run_ours(args):
             "kernels_ms": {k: v[0] for k, v in fam.items()},
             "fp64_route_cells": int(ctx.profile_read("fp64_fallback_cells")[1]),
             "whole_step_hbm_gbs": whole_bytes / (ms * 1e-3) / 1e9,
+            "hbm_write_stream_gbs": write_gbs,
             "load_vector_ms": vec_ms,
             "e2e": e2e, "cpu_baseline": cpu, "edges": edges, "post": post, "gmsh": gmsh, "hier": hier, "high_order": high_order, "solve": solve,
             "batch": batch,
