@@ -1211,6 +1211,352 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   }
 }
 
+// ------------------------- O3 triangles, point-varying alpha, tensor cores
+// Affine triangles, FeSpaceLagrangeO3, the 12-point degree-6 rule, alpha
+// varying over the cell (analytic families / O1 nodal), gamma cell-constant:
+//     A_K(e) = sum_k w_k alpha(x_k) [M00 T0 + M01 T1 + M11 T2](k; e) + gamma |det J| R_mass(e)
+// with M = |det J| J^-1 J^-T.  The 36 point coefficients c(k, ab) = w_k
+// alpha_k M_ab and m = gamma |det J| form a row of K = 37 columns (48 with
+// padding); the table rows are T(k; e, ab) and the folded mass table.  The
+// exact digit splitting, levels and recombination are those of
+// RDQuadTcKernel; here 55 entries (64 accumulator columns per level, 320 in
+// all, plus the row-info column 320) fill one CTA's 512 tensor-memory
+// columns, so one tile is in flight per SM: 16 warps, 8 producer warps (two
+// threads per cell: points 0-5 -> K columns 0-17; points 6-11 and the mass
+// -> columns 24-42) and 8 consumer warps, hand-offs as in RDQuadTcWsKernel
+// with single A and accumulator buffers.
+constexpr int kTtN = 10, kTtE = 55, kTtNQ = 12, kTtNP = 64, kTtKP = 48;
+constexpr int kTtSA = 128 * kTtKP * 2;                    // one digit slice of A
+constexpr int kTtBHalf = 6 * kTtNP * kTtKP * 2;           // plain (or scaled) table digits
+constexpr int kTtInfo = 16 * kTtKP * 2;
+constexpr int kTtEcOff = 2 * kTtBHalf + kTtInfo;
+constexpr int kTtImage = kTtEcOff + kTtNP * 4;
+constexpr int kTtSmem = 6 * kTtSA + kTtImage + 128 * kTtE * 8 + 2 * (128 * kTtN * 4 + 128 * 8);
+
+__host__ __device__ constexpr int TtKappa(int k, int ab) { return k < 6 ? 3 * k + ab : 24 + 3 * (k - 6) + ab; }
+
+__global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, const uint4* __restrict__ image,
+                                                         int* __restrict__ tc_timeouts) {
+  using elem::f2;
+  namespace df = lfg::df;
+  constexpr int N = kTtN, E = kTtE, NQ = kTtNQ, NP = kTtNP, KP = kTtKP, KS = KP / 16;
+  constexpr uint32_t SA = kTtSA, SBO = KP * 16;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sA = smraw;
+  unsigned char* sB = smraw + 6 * SA;
+  const int* sEc = reinterpret_cast<const int*>(sB + kTtEcOff);
+  double* svals = reinterpret_cast<double*>(sB + kTtImage);
+  int* sdofs = reinterpret_cast<int*>(svals + 128 * E);            // [2][128][10]
+  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 2 * 128 * N);  // [2][128]
+  __shared__ f2 sW[NQ], sX[2 * NQ], sO1[4 * NQ], sSC[23];
+  __shared__ elem::AnalyticDF sAf;
+  __shared__ uint32_t smax[2][128];
+  __shared__ __align__(8) uint64_t mma_done, tmem_free;
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_abort;
+  {
+    const f2* g = reinterpret_cast<const f2*>(d.tab);
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) sW[i] = g[d.L.off_W + i];
+    for (int i = threadIdx.x; i < 2 * NQ; i += blockDim.x) sX[i] = g[d.L.off_X + i];
+    for (int i = threadIdx.x; i < 4 * NQ; i += blockDim.x) sO1[i] = g[d.L.off_O1 + i];
+    for (int i = threadIdx.x; i < 23; i += blockDim.x) sSC[i] = g[d.L.off_SC + i];
+    for (int i = threadIdx.x; i < 16; i += blockDim.x) sAf.p[i] = df::FromDouble(a.alpha.p[i]);
+    if (threadIdx.x == 0) sAf.func = a.alpha.func;
+    uint4* dst = reinterpret_cast<uint4*>(sB);
+    for (int i = threadIdx.x; i < kTtImage / 16; i += blockDim.x) dst[i] = image[i];
+  }
+  if (threadIdx.x == 0) {
+    tc::MbarInit(&mma_done, 1);
+    tc::MbarInit(&tmem_free, 256);
+    s_abort = 0;
+  }
+  if (threadIdx.x < 32) tc::TmemAlloc(&s_taddr, 512);
+  tc::FenceProxyAsync();
+  tc::FenceBeforeSync();
+  __syncthreads();
+  tc::FenceAfterSync();
+  const uint32_t taddr = s_taddr;
+  const int64_t tiles = (a.count + 127) / 128;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool nodal = a.alpha.kind == LFG_COEFF_NODAL_O1;
+  const bool mass = a.gamma.kind != LFG_COEFF_ZERO;
+
+  if (threadIdx.x < 256) {
+    // ================= producers: two threads per cell =================
+    const int half = threadIdx.x >> 7, r = threadIdx.x & 127;
+    int c = 0;
+    double2 v[4] = {};
+    double ga = 0.0;
+    int4 cn = make_int4(0, 0, 0, 0);
+    auto fetch = [&](int64_t t0) {
+      if (t0 + r < a.count) {
+        c = a.bucket[t0 + r];
+        LoadVerts<false>(a, c, cn, v);
+        ga = mass ? CellConst(a.gamma, c) : 0.0;
+      }
+    };
+    if (blockIdx.x < tiles) fetch(static_cast<int64_t>(blockIdx.x) * 128);
+    int j = 0;
+    for (;; ++j) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(j) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      // ---- coefficients of this thread's six points (+ the mass column in half 1)
+      bool safe = false;
+      f2 cpt[6][3];
+      f2 mm = df::Make(0.0f);
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+      if (r < ncell) {
+        const double jac[4] = {v[1].x - v[0].x, v[2].x - v[0].x, v[1].y - v[0].y, v[2].y - v[0].y};
+        safe = DfSafeBits(ga) && DfSafeBits(v[0].x) && DfSafeBits(v[0].y);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) safe = safe && DfSafeBits(jac[k]);
+        f2 nod[3] = {};
+        if (safe && nodal) {
+          const double n0 = a.alpha.data[cn.x], n1 = a.alpha.data[cn.y], n2 = a.alpha.data[cn.z];
+          safe = DfSafeBits(n0) && DfSafeBits(n1) && DfSafeBits(n2);
+          nod[0] = df::FromDouble(n0);
+          nod[1] = df::FromDouble(n1);
+          nod[2] = df::FromDouble(n2);
+        }
+        if (safe) {
+          const f2 j00 = df::FromDouble(jac[0]), j01 = df::FromDouble(jac[1]);
+          const f2 j10 = df::FromDouble(jac[2]), j11 = df::FromDouble(jac[3]);
+          f2 m00, m01, m11, adet;
+          elem::TriaMetricDF(j00, j01, j10, j11, m00, m01, m11, adet);
+          const f2 x0 = df::FromDouble(v[0].x), y0 = df::FromDouble(v[0].y);
+#pragma unroll
+          for (int kk = 0; kk < 6; ++kk) {
+            const int k = 6 * half + kk;
+            f2 al;
+            if (nodal) {
+              al = df::Mul(nod[0], sO1[4 * k]);
+              al = df::MulAdd(nod[1], sO1[4 * k + 1], al);
+              al = df::MulAdd(nod[2], sO1[4 * k + 2], al);
+            } else {
+              const f2 xh = sX[2 * k], yh = sX[2 * k + 1];
+              const f2 X = df::MulAdd(j01, yh, df::MulAdd(j00, xh, x0));
+              const f2 Y = df::MulAdd(j11, yh, df::MulAdd(j10, xh, y0));
+              al = elem::EvalAnalyticDF(sAf, X, Y, sSC, sSC + 11);
+            }
+            const float aa = fabsf(al.h);  // 2^-30 margin below the df32 range of the products
+            safe = safe && (aa == 0.0f || (aa > 8.0e-10f && aa < 1.0e9f));
+            const f2 s = df::Mul(sW[k], al);
+            cpt[kk][0] = df::Mul(s, m00);
+            cpt[kk][1] = df::Mul(s, m01);
+            cpt[kk][2] = df::Mul(s, m11);
+          }
+          if (mass && half == 1) mm = df::Mul(df::FromDouble(ga), adet);
+        }
+      }
+      float mx = fabsf(mm.h);
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) mx = fmaxf(mx, fabsf(cpt[k][q].h));
+      // both threads of the cell agree on the row maximum and on the range flag
+      smax[half][r] = safe ? __float_as_uint(mx) : 0xffffffffu;
+      tc::NamedSync(1, 256);
+      const uint32_t m0 = smax[0][r], m1 = smax[1][r];
+      safe = r < ncell && m0 != 0xffffffffu && m1 != 0xffffffffu;
+      const uint32_t mb = safe ? max(m0, m1) : 0u;
+      int e = mb ? static_cast<int>((mb >> 23) & 0xffu) - 127 : 0;
+      if (e < -70 || e > 70) safe = false;
+      if (!safe) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+        mm = f2{0.0f, 0.0f};
+        e = 0;
+      }
+      // ---- the A buffer is free once the previous tile's MMAs are done
+      const bool ok = j == 0 || tc::MbarWait(&mma_done, (j - 1) & 1, kTcMaxPolls);
+      if (tc::NamedSyncOr(1, 256, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (threadIdx.x == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        break;
+      }
+      const float scale = __uint_as_float(static_cast<uint32_t>(127 + 52 - e) << 23);  // 2^(52 - e)
+      unsigned char* arow = sA + (r >> 3) * SBO + (r & 7) * 16;
+#pragma unroll
+      for (int gk = 0; gk < 3; ++gk) {
+        const int G = 3 * half + gk;
+        uint32_t w[6][4];
+#pragma unroll
+        for (int pr = 0; pr < 4; ++pr) {
+          uint32_t p[2][6];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            const int kl = gk * 8 + 2 * pr + s;  // column within this half: point kl / 3, mass at 18 (half 1)
+            f2 x = f2{0.0f, 0.0f};
+            if (kl < 18) x = cpt[kl / 3][kl % 3];
+            else if (kl == 18 && half == 1) x = mm;
+            const float hs = x.h * scale;
+            const int vhi = __float2int_rn(hs * 7.450580596923828125e-9f);  // 2^-27
+            const float rem = __fmaf_rn(static_cast<float>(vhi), -134217728.0f, hs);  // exact
+            const int wlo0 = __float2int_rn(rem) + __float2int_rn(x.l * scale) + 256 * ((1 << 18) + (1 << 9) + 1);
+            const int whi = vhi + 256 * ((1 << 9) + 1) + (wlo0 >> 27);
+            const uint32_t wlo = static_cast<uint32_t>(wlo0) & ((1u << 27) - 1u);
+            p[s][0] = 0x6600u + static_cast<uint32_t>(whi >> 18);
+            p[s][1] = 0x6400u | ((static_cast<uint32_t>(whi) >> 9) & 511u);
+            p[s][2] = 0x6400u | (static_cast<uint32_t>(whi) & 511u);
+            p[s][3] = 0x6400u | ((wlo >> 18) & 511u);
+            p[s][4] = 0x6400u | ((wlo >> 9) & 511u);
+            p[s][5] = 0x6400u | (wlo & 511u);
+          }
+#pragma unroll
+          for (int i = 0; i < 6; ++i)
+            w[i][pr] = HSub2(__byte_perm(p[0][i], p[1][i], 0x5410), i == 0 ? 0x66006600u : 0x65006500u);
+        }
+        if (G == KP / 8 - 1) {  // row info in digit 1, K column KP - 1
+          const uint32_t info = __half_as_ushort(__float2half_rn(safe ? static_cast<float>(e + 128) : 0.0f));
+          w[0][3] = (w[0][3] & 0xffffu) | (info << 16);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+          *reinterpret_cast<uint4*>(arow + i * SA + G * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+      }
+      tc::FenceProxyAsync();
+      tc::NamedSync(1, 256);
+      if (threadIdx.x == 0) {
+        const bool free_ok = j == 0 || tc::MbarWait(&tmem_free, (j - 1) & 1, kTcMaxPolls);
+        if (!free_ok) {
+          atomicAdd(tc_timeouts, 1);
+          s_abort = 1;
+        } else {
+          tc::FenceAfterSync();
+          const uint32_t a0 = tc::SmemAddr(sA), bu = tc::SmemAddr(sB), bs = bu + kTtBHalf, bi = bu + 2 * kTtBHalf;
+#pragma unroll
+          for (int s = 0; s < KS; ++s) {
+            const uint64_t b0 = tc::SmemDesc(bu + s * 256, 128, SBO);
+            // digit 1 against table digits 1..4 (levels 2..5) and digit 5 (level 6)
+            tc::MmaF16(taddr, tc::SmemDesc(a0 + s * 256, 128, SBO), b0, tc::IdescF16(128, 256), s > 0);
+            tc::MmaF16(taddr + 4 * NP, tc::SmemDesc(a0 + s * 256, 128, SBO),
+                       tc::SmemDesc(bu + 4 * (NP / 8) * SBO + s * 256, 128, SBO), tc::IdescF16(128, NP), s > 0);
+#pragma unroll
+            for (int i = 2; i <= 5; ++i)  // digit i against table digits 1..6-i (levels i+1..6)
+              tc::MmaF16(taddr + (i - 1) * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO), b0,
+                         tc::IdescF16(128, (6 - i) * NP), true);
+#pragma unroll
+            for (int i = 1; i <= 6; ++i)  // level 7, 2^-9-scaled table digits
+              tc::MmaF16(taddr + 4 * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                         tc::SmemDesc(bs + (6 - i) * (NP / 8) * SBO + s * 256, 128, SBO), tc::IdescF16(128, NP),
+                         true);
+          }
+          tc::MmaF16(taddr + 5 * NP, tc::SmemDesc(a0 + (KS - 1) * 256, 128, SBO),
+                     tc::SmemDesc(bi + (KS - 1) * 256, 128, SBO), tc::IdescF16(128, 16), false);
+          tc::Commit(&mma_done);
+        }
+      }
+      const int64_t nxt = tile + gridDim.x;
+      if (nxt < tiles) fetch(nxt * 128);
+    }
+    if (threadIdx.x == 0 && j > 0) tc::MbarWait(&mma_done, (j - 1) & 1, kTcMaxPolls);
+  } else {
+    // ================= consumers: two threads per cell =================
+    const int et = threadIdx.x - 256, half = et >> 7, r = et & 127, ew = et >> 5;
+    const uint32_t tl = static_cast<uint32_t>((r >> 5) * 32) << 16;
+    int tmap[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int w = lane + 32 * t, i = w / N, jj = w - i * N;
+      tmap[t] = w < N * N ? (i | (jj << 8) | (UpperIndex<N>(i, jj) << 16)) : -1;
+    }
+    if (half == 1 && blockIdx.x < tiles && static_cast<int64_t>(blockIdx.x) * 128 + r < a.count) {
+      const int c0 = a.bucket[static_cast<int64_t>(blockIdx.x) * 128 + r];
+      const int32_t* g = a.cell_dofs + static_cast<int64_t>(c0) * a.n_cell;
+#pragma unroll
+      for (int i = 0; i < N; ++i) tc::CpAsync4(sdofs + r * N + i, g + i);
+      tc::CpAsync8(soff + r, a.tri_offset + c0);
+    }
+    tc::CpAsyncCommit();
+    for (int j = 0;; ++j) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(j) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      const int bb = j & 1;
+      const int64_t t1 = t0 + static_cast<int64_t>(gridDim.x) * 128;
+      int c_next = -1;
+      if (half == 1 && t1 + r < a.count) c_next = a.bucket[t1 + r];
+      const bool ok = tc::MbarWait(&mma_done, j & 1, kTcMaxPolls);
+      if (tc::NamedSyncOr(3, 256, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (et == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        break;
+      }
+      tc::FenceAfterSync();
+      const uint32_t acc = taddr + tl;
+      float inf[8];
+      tc::Ld8(acc + 5 * NP, inf);
+      tc::WaitLd();
+      const int info = static_cast<int>(inf[0]);
+      const bool safe = info != 0;
+      const int shift = info - 128 + 2 - 54;
+      double* vals = svals + r * E;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int col = 32 * half + 8 * q;
+        float G[5][8];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) tc::Ld8(acc + l * NP + col, G[l]);
+        tc::WaitLd();
+        if (safe) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int en = col + t;
+            if (en < E) vals[en] = TcCombine(G[0][t], G[1][t], G[2][t], G[3][t], G[4][t], shift + sEc[en]);
+          }
+        }
+      }
+      tc::FenceBeforeSync();
+      tc::MbarArrive(&tmem_free);
+      if (half == 0 && r < ncell && !safe) {
+        const int cf = a.bucket[t0 + r];
+        int4 cnf;
+        double2 vf[4];
+        LoadVerts<false>(a, cf, cnf, vf);
+        TriaVaryF64<N>(a, cf, cnf, vf, vals);
+        atomicAdd(a.fallback, 1ull);
+      }
+      if (c_next >= 0) {
+        const int32_t* g = a.cell_dofs + static_cast<int64_t>(c_next) * a.n_cell;
+        int* dn = sdofs + ((j + 1) & 1) * 128 * N + r * N;
+#pragma unroll
+        for (int i = 0; i < N; ++i) tc::CpAsync4(dn + i, g + i);
+        tc::CpAsync8(soff + ((j + 1) & 1) * 128 + r, a.tri_offset + c_next);
+      }
+      tc::CpAsyncCommit();
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+      tc::NamedSync(3, 256);
+      const int* sd = sdofs + bb * 128 * N;
+      const int64_t* so = soff + bb * 128;
+      for (int cl = ew; cl < ncell; cl += 8) {
+        lfg_triplet* base = a.out + so[cl];
+        const int* dd = sd + cl * N;
+        const double* vv = svals + cl * E;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+          if (tmap[t] >= 0)
+            StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
+      }
+      tc::NamedSync(3, 256);
+    }
+    tc::CpAsyncWaitAll();
+  }
+  tc::FenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::FenceAfterSync();
+    tc::TmemFree(taddr, 512);
+  }
+}
+
 // --------------------------------------------------------------- load vector
 template <int DEG, bool QUAD, bool VARY>
 __global__ void __launch_bounds__(128) LoadVectorKernel(AsmArgs a) {
@@ -1745,6 +2091,69 @@ void LaunchQuadTc(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   LFG_LAUNCHED(ctx);
 }
 
+// Table digits of RDTriaTcKernel (O3 triangles, 12-point rule): columns
+// TtKappa(k, ab) = T(k; e, ab), column 42 = the folded mass table R(e); same
+// digit layout as GetQuadTcImage with 64 entries per digit block.
+const uint4* GetTriaTcImage(lfg_ctx* ctx, const double* tab, const Tab& L) {
+  auto it = ctx->tc_images.find(tab);
+  if (it != ctx->tc_images.end()) return it->second.as<uint4>();
+  const int E = L.E, KP = kTtKP;
+  std::vector<double> h(static_cast<size_t>(L.total));
+  LFG_CUDA(cudaMemcpyAsync(h.data(), tab, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<uint16_t> img(static_cast<size_t>(kTtImage) / 2, 0);
+  uint16_t* plain = img.data();
+  uint16_t* scaled = plain + kTtBHalf / 2;
+  uint16_t* info = plain + kTtBHalf;
+  int32_t* ec = reinterpret_cast<int32_t*>(plain + kTtEcOff / 2);
+  info[((KP - 1) / 8) * 64 + 7] = HalfBits(1.0);
+  std::vector<std::pair<int, double>> col;  // (kappa, value) of one entry
+  for (int e = 0; e < E; ++e) {
+    col.clear();
+    for (int k = 0; k < L.nq; ++k)
+      for (int ab = 0; ab < 3; ++ab) col.push_back({TtKappa(k, ab), h[L.off_T + (static_cast<size_t>(k) * E + e) * 4 + ab]});
+    col.push_back({42, h[L.off_R + e * 4 + 3]});
+    double mt = 0.0;
+    for (auto& kv : col) mt = std::max(mt, std::fabs(kv.second));
+    int ex = 0;
+    if (mt > 0.0) std::frexp(mt, &ex);
+    ec[e] = mt > 0.0 ? ex + 1 : 0;
+    for (auto& kv : col) {
+      long long Y = std::llround(std::ldexp(kv.second, 54 - ec[e]));
+      int b[7];
+      for (int j = 6; j >= 2; --j) {
+        long long rr = ((Y % 512) + 512) % 512;
+        if (rr >= 256) rr -= 512;
+        b[j] = static_cast<int>(rr);
+        Y = (Y - rr) / 512;
+      }
+      b[1] = static_cast<int>(Y);
+      for (int j = 1; j <= 6; ++j) {
+        const int n = (j - 1) * kTtNP + e, kap = kv.first;
+        const size_t off = static_cast<size_t>(n / 8) * (KP / 8) * 64 + (kap / 8) * 64 + (n % 8) * 8 + kap % 8;
+        plain[off] = HalfBits(b[j]);
+        scaled[off] = HalfBits(std::ldexp(static_cast<double>(b[j]), -9));
+      }
+    }
+  }
+  DevBuf& buf = ctx->tc_images[tab];
+  buf.alloc(img.size() * 2, ctx->stream);
+  LFG_CUDA(cudaMemcpyAsync(buf.p, img.data(), img.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return buf.as<uint4>();
+}
+
+void LaunchTriaTc(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  const uint4* img = GetTriaTcImage(ctx, a.tab, a.L);
+  int* timeouts = StatusWord(ctx) + 14;
+  LFG_CUDA(cudaFuncSetAttribute(RDTriaTcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTtSmem));
+  const int64_t tiles = (a.count + 127) / 128;
+  const int64_t grid = std::min<int64_t>(tiles, ctx->num_sms);  // one CTA per SM (512 TMEM columns)
+  if (grid <= 0) return;
+  RDTriaTcKernel<<<static_cast<unsigned>(grid), 512, kTtSmem, ctx->stream>>>(a, d, img, timeouts);
+  LFG_LAUNCHED(ctx);
+}
+
 template <int DEG, int NQ>
 void LaunchTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   constexpr int N = (DEG + 1) * (DEG + 2) / 2, E = N * (N + 1) / 2;
@@ -1764,6 +2173,11 @@ bool TryTriaVaryDf(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   const int gk = a.gamma.kind;
   if (gk != LFG_COEFF_ZERO && gk != LFG_COEFF_CONSTANT && gk != LFG_COEFF_PER_CELL && gk != LFG_COEFF_PER_CELL_EXP)
     return false;
+  if (DEG == 3 && d.L.nq == kTtNQ && a.L.E == kTtE && a.L.nq == kTtNQ && ctx->tensor_cores) {
+    ProfScope prof(ctx, "rd_tria_vary_tc");
+    LaunchTriaTc(ctx, a, d);
+    return true;
+  }
   ProfScope prof(ctx, "rd_tria_vary_df");
   switch (d.L.nq) {
     case 1: LaunchTriaVaryDf<DEG, 1>(ctx, a, d); return true;
