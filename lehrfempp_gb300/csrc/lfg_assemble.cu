@@ -1235,6 +1235,11 @@ constexpr int kTtSmem = 6 * kTtSA + kTtImage + 128 * kTtE * 8 + 2 * (128 * kTtN 
 
 __host__ __device__ constexpr int TtKappa(int k, int ab) { return k < 6 ? 3 * k + ab : 24 + 3 * (k - 6) + ab; }
 
+// FAM: 0 alpha O1-nodal, 1 polynomial, 2 sin sin / sin cos (evaluated as
+// sin/cos at the first vertex, once per cell, turned to the points by the
+// angle-addition formulas with short series of the small offsets when
+// pi |p| (|J_0| + |J_1|) <= 0.1, else the full reduction per point).
+template <int FAM>
 __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, const uint4* __restrict__ image,
                                                          int* __restrict__ tc_timeouts) {
   using elem::f2;
@@ -1248,7 +1253,7 @@ __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, co
   double* svals = reinterpret_cast<double*>(sB + kTtImage);
   int* sdofs = reinterpret_cast<int*>(svals + 128 * E);            // [2][128][10]
   int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 2 * 128 * N);  // [2][128]
-  __shared__ f2 sW[NQ], sX[2 * NQ], sO1[4 * NQ], sSC[23];
+  __shared__ f2 sW[NQ], sX[2 * NQ], sO1[4 * NQ], sSC[23], sSm[11];
   __shared__ elem::AnalyticDF sAf;
   __shared__ uint32_t smax[2][128];
   __shared__ __align__(8) uint64_t mma_done, tmem_free;
@@ -1261,6 +1266,13 @@ __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, co
     for (int i = threadIdx.x; i < 4 * NQ; i += blockDim.x) sO1[i] = g[d.L.off_O1 + i];
     for (int i = threadIdx.x; i < 23; i += blockDim.x) sSC[i] = g[d.L.off_SC + i];
     for (int i = threadIdx.x; i < 16; i += blockDim.x) sAf.p[i] = df::FromDouble(a.alpha.p[i]);
+    if (threadIdx.x < 11) {  // small-angle series: 1/1!, -1/3!, .., 1/9!; 1/0!, -1/2!, .., -1/10!
+      const int k = threadIdx.x < 5 ? 2 * threadIdx.x + 1 : 2 * (threadIdx.x - 5);
+      double f = 1.0;
+      for (int i = 2; i <= k; ++i) f *= i;
+      const int sgn = (threadIdx.x < 5 ? threadIdx.x : threadIdx.x - 5) & 1;
+      sSm[threadIdx.x] = df::FromDouble(sgn ? -1.0 / f : 1.0 / f);
+    }
     if (threadIdx.x == 0) sAf.func = a.alpha.func;
     uint4* dst = reinterpret_cast<uint4*>(sB);
     for (int i = threadIdx.x; i < kTtImage / 16; i += blockDim.x) dst[i] = image[i];
@@ -1278,8 +1290,8 @@ __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, co
   const uint32_t taddr = s_taddr;
   const int64_t tiles = (a.count + 127) / 128;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool nodal = a.alpha.kind == LFG_COEFF_NODAL_O1;
   const bool mass = a.gamma.kind != LFG_COEFF_ZERO;
+  const bool sinsin = a.alpha.func == LFG_FN_SINSIN;
 
   if (threadIdx.x < 256) {
     // ================= producers: two threads per cell =================
@@ -1316,7 +1328,7 @@ __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, co
 #pragma unroll
         for (int k = 0; k < 4; ++k) safe = safe && DfSafeBits(jac[k]);
         f2 nod[3] = {};
-        if (safe && nodal) {
+        if (safe && FAM == 0) {
           const double n0 = a.alpha.data[cn.x], n1 = a.alpha.data[cn.y], n2 = a.alpha.data[cn.z];
           safe = DfSafeBits(n0) && DfSafeBits(n1) && DfSafeBits(n2);
           nod[0] = df::FromDouble(n0);
@@ -1329,14 +1341,38 @@ __global__ void __launch_bounds__(512, 1) RDTriaTcKernel(AsmArgs a, DfArgs d, co
           f2 m00, m01, m11, adet;
           elem::TriaMetricDF(j00, j01, j10, j11, m00, m01, m11, adet);
           const f2 x0 = df::FromDouble(v[0].x), y0 = df::FromDouble(v[0].y);
+          // trig families: sin/cos at the first vertex, once per cell
+          f2 sA = {}, cA = {}, sB = {}, cB = {}, pi = {};
+          bool small = false;
+          if (FAM == 2) {
+            const float bound = 3.1416f * fmaxf(fabsf(sAf.p[2].h) * (fabsf(j00.h) + fabsf(j01.h)),
+                                                fabsf(sAf.p[3].h) * (fabsf(j10.h) + fabsf(j11.h)));
+            small = bound <= 0.0999f;
+            if (small) {
+              elem::SinCosPiDF(df::Mul(sAf.p[2], x0), sSC, sSC + 11, sA, cA);
+              elem::SinCosPiDF(df::Mul(sAf.p[3], y0), sSC, sSC + 11, sB, cB);
+              pi = df::FromDouble(3.14159265358979323846);
+            }
+          }
 #pragma unroll
           for (int kk = 0; kk < 6; ++kk) {
             const int k = 6 * half + kk;
             f2 al;
-            if (nodal) {
+            if (FAM == 0) {
               al = df::Mul(nod[0], sO1[4 * k]);
               al = df::MulAdd(nod[1], sO1[4 * k + 1], al);
               al = df::MulAdd(nod[2], sO1[4 * k + 2], al);
+            } else if (FAM == 2 && small) {
+              const f2 xh = sX[2 * k], yh = sX[2 * k + 1];
+              const f2 dx = df::MulAdd(j01, yh, df::Mul(j00, xh));  // X - x0
+              const f2 dy = df::MulAdd(j11, yh, df::Mul(j10, xh));
+              f2 s1, c1, s2, c2;
+              elem::SinCosSmallDF(df::Mul(pi, df::Mul(sAf.p[2], dx)), sSm, sSm + 5, s1, c1);
+              elem::SinCosSmallDF(df::Mul(pi, df::Mul(sAf.p[3], dy)), sSm, sSm + 5, s2, c2);
+              const f2 sx = df::Add(df::Mul(sA, c1), df::Mul(cA, s1));  // sin(a + t)
+              const f2 fy = sinsin ? df::Add(df::Mul(sB, c2), df::Mul(cB, s2))   // sin(b + u)
+                                   : df::Sub(df::Mul(cB, c2), df::Mul(sB, s2));  // cos(b + u)
+              al = df::MulAdd(sAf.p[1], df::Mul(sx, fy), sAf.p[0]);
             } else {
               const f2 xh = sX[2 * k], yh = sX[2 * k + 1];
               const f2 X = df::MulAdd(j01, yh, df::MulAdd(j00, xh, x0));
@@ -2146,11 +2182,13 @@ const uint4* GetTriaTcImage(lfg_ctx* ctx, const double* tab, const Tab& L) {
 void LaunchTriaTc(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   const uint4* img = GetTriaTcImage(ctx, a.tab, a.L);
   int* timeouts = StatusWord(ctx) + 14;
-  LFG_CUDA(cudaFuncSetAttribute(RDTriaTcKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTtSmem));
+  const int fam = a.alpha.kind == LFG_COEFF_NODAL_O1 ? 0 : (a.alpha.func == LFG_FN_POLY ? 1 : 2);
+  auto kernel = fam == 0 ? RDTriaTcKernel<0> : (fam == 1 ? RDTriaTcKernel<1> : RDTriaTcKernel<2>);
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTtSmem));
   const int64_t tiles = (a.count + 127) / 128;
   const int64_t grid = std::min<int64_t>(tiles, ctx->num_sms);  // one CTA per SM (512 TMEM columns)
   if (grid <= 0) return;
-  RDTriaTcKernel<<<static_cast<unsigned>(grid), 512, kTtSmem, ctx->stream>>>(a, d, img, timeouts);
+  kernel<<<static_cast<unsigned>(grid), 512, kTtSmem, ctx->stream>>>(a, d, img, timeouts);
   LFG_LAUNCHED(ctx);
 }
 

@@ -154,6 +154,22 @@ DF_HD f2 EvalAnalyticDF(const AnalyticDF& f, f2 x, f2 y, const f2* S, const f2* 
   return MulAdd(f.p[1], Mul(sx, f.func == 2 ? sy : cy), f.p[0]);
 }
 
+// sin and cos of a small df32 angle, |t| <= 0.1: Taylor series in t^2
+// (next terms below 3e-19), coefficients S[0..4] = (-1)^k / (2k+1)!,
+// C[0..5] = (-1)^k / (2k)! as df32 pairs.
+DF_HD void SinCosSmallDF(f2 t, const f2* S, const f2* C, f2& sn, f2& cs) {
+  using namespace df;
+  const f2 t2 = Mul(t, t);
+  f2 ps = S[4];
+  DF_UNROLL
+  for (int k = 3; k >= 0; --k) ps = MulAdd(ps, t2, S[k]);
+  f2 pc = C[5];
+  DF_UNROLL
+  for (int k = 4; k >= 0; --k) pc = MulAdd(pc, t2, C[k]);
+  sn = Mul(ps, t);
+  cs = pc;
+}
+
 // Contraction of an affine triangle with point coefficients c[k] = {c00, c01,
 // c11} (c = w_k alpha_k |det J| J^-1 J^-T) over the per-point tables
 // T[k][e][0..2], plus an optional cell-constant mass term mm * R[e][3].
