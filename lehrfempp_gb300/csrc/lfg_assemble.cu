@@ -1606,6 +1606,26 @@ __global__ void __launch_bounds__(128) LoadVectorKernel(AsmArgs a) {
   const double* sL = sm + a.L.off_L;
   const double* so1 = sm + a.L.off_o1;
   const int nq = a.L.nq;
+  // Folded rules (exact reformulations of the point sum, computed per block):
+  // bilinear quads with cell-constant f: |det J| is affine in (xh, yh), so
+  //   sum_k w_k |det J_k| phi_i(k) = s (D0 L_i + D1 Lx_i + D2 Ly_i),
+  //   Lx_i = sum_k w_k xh_k phi_i(k), Ly_i = sum_k w_k yh_k phi_i(k);
+  // triangles with an O1-nodal f: sum_k w_k f(x_k) phi_i(k) = sum_v f_v M(v, i),
+  //   M(v, i) = sum_k w_k lambda_v(k) phi_i(k).
+  double* sF = sm + a.L.total;  // [3][N]
+  const bool nodal = VARY && !QUAD && a.alpha.kind == LFG_COEFF_NODAL_O1;
+  if ((QUAD && !VARY) || nodal) {
+    for (int q = threadIdx.x; q < 3 * N; q += blockDim.x) {
+      const int g = q / N, i = q - g * N;
+      double acc = 0.0;
+      for (int k = 0; k < nq; ++k) {
+        const double wk = sw[k] * (QUAD ? (g == 0 ? 1.0 : (g == 1 ? sqx[k] : sqy[k])) : so1[k * 4 + g]);
+        acc = fma(wk, sphi[k * N + i], acc);
+      }
+      sF[q] = acc;
+    }
+    __syncthreads();
+  }
   for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < a.count;
        t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int c = a.bucket[t];
@@ -1613,13 +1633,33 @@ __global__ void __launch_bounds__(128) LoadVectorKernel(AsmArgs a) {
     double2 v[4];
     LoadVerts<QUAD>(a, c, cn, v);
     double vec[N];
+    bool folded = false;
+    if (QUAD && !VARY) {
+      // det J = D0 + D1 xh + D2 yh (quad_o1.cc:93-99 rewritten); one sign on the cell
+      const double ax = v[1].x - v[0].x, ay = v[1].y - v[0].y, cx = v[3].x - v[0].x, cy = v[3].y - v[0].y;
+      const double dx = (v[0].x - v[1].x) + (v[2].x - v[3].x), dy = (v[0].y - v[1].y) + (v[2].y - v[3].y);
+      const double D0 = ax * cy - ay * cx, D1 = ax * dy - ay * dx, D2 = dx * cy - dy * cx;
+      const double c1 = D0 + D1, c2 = D0 + D2, c3 = c1 + D2;
+      if ((D0 > 0 && c1 > 0 && c2 > 0 && c3 > 0) || (D0 < 0 && c1 < 0 && c2 < 0 && c3 < 0)) {
+        const double f = (D0 > 0 ? 1.0 : -1.0) * CellConst(a.alpha, c);
+#pragma unroll
+        for (int i = 0; i < N; ++i) vec[i] = f * fma(D0, sF[i], fma(D1, sF[N + i], D2 * sF[2 * N + i]));
+        folded = true;
+      }
+    }
     if (!QUAD && !VARY) {
       double m00, m01, m11, adet;
       TriaMetric(v, m00, m01, m11, adet);
       const double s = CellConst(a.alpha, c) * adet;
 #pragma unroll
       for (int i = 0; i < N; ++i) vec[i] = s * sL[i];
-    } else {
+    } else if (nodal) {
+      double m00, m01, m11, adet;
+      TriaMetric(v, m00, m01, m11, adet);
+      const double f0 = a.alpha.data[cn.x] * adet, f1 = a.alpha.data[cn.y] * adet, f2 = a.alpha.data[cn.z] * adet;
+#pragma unroll
+      for (int i = 0; i < N; ++i) vec[i] = fma(f0, sF[i], fma(f1, sF[N + i], f2 * sF[2 * N + i]));
+    } else if (!folded) {
 #pragma unroll
       for (int i = 0; i < N; ++i) vec[i] = 0.0;
       double tdet = 0;
@@ -2284,7 +2324,7 @@ void DispatchRD(lfg_ctx* ctx, int degree, const AsmArgs& a, const DfArgs& d, boo
 
 template <bool QUAD>
 void DispatchLoad(lfg_ctx* ctx, int degree, const AsmArgs& a, bool vary) {
-  const size_t smem = a.L.total * sizeof(double);
+  const size_t smem = (a.L.total + 3 * 16) * sizeof(double);  // tables + the folded rules
   ProfScope prof(ctx, QUAD ? "load_quad" : "load_tria");
   switch (degree) {
     case 1: vary ? Launch(LoadVectorKernel<1, QUAD, true>, ctx, a.count, smem, 128, a)

@@ -377,3 +377,20 @@ def test_not_converged_status(ctx):
     with pytest.raises(L.LfgError) as e:
         coo.make_sparse().solve_pcg(b, x, rtol=1e-14, max_iterations=2, check_every=2)
     assert e.value.code == L.NOT_CONVERGED
+
+
+@pytest.mark.parametrize("degree", [1, 2, 3])
+def test_folded_load_vectors(ctx, degree):
+    """Load vectors through the folded rules: bilinear quadrilaterals (jittered,
+    |det J| affine in the reference coordinates) with a per-cell f, and
+    triangles with an O1-nodal f."""
+    rng = np.random.default_rng(degree)
+    xy, cells = W.hybrid_mesh(12, seed=degree)
+    mesh = {"kind": "factory", "xy": xy, "cells": cells, "edges": None}
+    for f in (("cell", np.exp(rng.standard_normal(len(cells)))), ("nodal", 1.0 + rng.random(len(xy)))):
+        wl = {"mesh": mesh, "degree": degree, "alpha": ("const", 1.0), "gamma": ("zero",), "f": f,
+              "qr_tria": 0, "qr_quad": 0}
+        r = Run(ctx, wl)
+        b = r.gpu_vector().download()
+        bo = r.oracle_vector()
+        assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max(), f[0]
