@@ -733,23 +733,6 @@ def run_ours(args):
     fp64_achieved = alg_flops / (fam[dom][0] * 1e-3) / 1e12
     whole_bytes = sum(algorithmic_bytes(space, mesh, k)[0] for k in ("tria", "quad"))
 
-    # pure write stream of 4 GB (informational: the element kernels' bytes are ~80 % writes)
-    write_gbs = None
-    try:
-        import torch
-        wbuf = torch.empty(1 << 30, dtype=torch.int32, device="cuda:%d" % local)
-        wbuf.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(5):
-            wbuf.zero_()
-        e1.record()
-        torch.cuda.synchronize()
-        write_gbs = wbuf.numel() * 4 * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e9
-        del wbuf
-    except Exception:  # torch absent or no memory: the key stays null
-        write_gbs = None
-
     # load vector (AssembleVectorLocally) time, informational
     b = ctx.zeros(space.num_dofs)
     lprov = L.load_provider(W.to_coeff(ctx, wl["f"], keep))
@@ -794,6 +777,25 @@ def run_ours(args):
     batch = leg(batch_leg, L, W, ctx, args.batch_count) if args.batch_count > 0 else None
     gradient = leg(gradient_leg, L, W, ctx, args.grad_size, steps=3,
                    cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.grad_size > 0 else None
+
+    # pure write stream of 4 GB (informational: the element kernels' bytes are ~80 % writes); last,
+    # so that torch's CUDA state cannot touch the timed legs
+    write_gbs = None
+    try:
+        import torch
+        wbuf = torch.empty(1 << 30, dtype=torch.int32, device="cuda:%d" % local)
+        wbuf.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            wbuf.zero_()
+        e1.record()
+        torch.cuda.synchronize()
+        write_gbs = wbuf.numel() * 4 * 5 / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        del wbuf
+        torch.cuda.empty_cache()
+    except Exception:  # torch absent or no memory: the key stays null
+        write_gbs = None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
