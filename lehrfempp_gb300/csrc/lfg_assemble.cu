@@ -1111,8 +1111,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     if (r == 0 && m > 0) tc::MbarWait(&mma_done[b], (m - 1) & 1, kTcMaxPolls);
   } else {
     // ================= consumers: two threads per cell =================
-    const int et = threadIdx.x - 256, half = et >> 7, r = et & 127, ew = et >> 5;
-    const uint32_t tl = static_cast<uint32_t>((r >> 5) * 32) << 16;
+    // The cells of TMEM lane quarter q (32 cells) belong to consumer warps q
+    // (half 0) and q + 4 (half 1); each quarter reads, recombines, stages and
+    // writes its own cells and synchronises on its own named barrier, so the
+    // quarters drift apart and one quarter's triplet writes overlap another's
+    // recombination.
+    const int et = threadIdx.x - 256, half = et >> 7, r = et & 127, q4 = r >> 5, qbar = 4 + q4;
+    const uint32_t tl = static_cast<uint32_t>(q4 * 32) << 16;
     int tmap[3];
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
@@ -1138,8 +1143,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       int c_next = -1;
       if (half == 1 && t1 + r < a.count) c_next = a.bucket[t1 + r];
       const bool ok = tc::MbarWait(&mma_done[b], (j >> 1) & 1, kTcMaxPolls);
-      if (tc::NamedSyncOr(3, 256, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
-        if (et == 0 && !ok) atomicAdd(tc_timeouts, 1);
+      if (tc::NamedSyncOr(qbar, 64, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if ((et & 127) == 32 * q4 && half == 0 && !ok) atomicAdd(tc_timeouts, 1);
         s_abort = 1;
         break;
       }
@@ -1187,10 +1192,10 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       }
       tc::CpAsyncCommit();
       asm volatile("cp.async.wait_group 1;" ::: "memory");  // this tile's group has landed
-      tc::NamedSync(3, 256);
+      tc::NamedSync(qbar, 64);
       const int* sd = sdofs + b * 128 * N;
       const int64_t* so = soff + b * 128;
-      for (int cl = ew; cl < ncell; cl += 8) {
+      for (int cl = 32 * q4 + half; cl < ncell && cl < 32 * q4 + 32; cl += 2) {
         lfg_triplet* base = a.out + so[cl];
         const int* dd = sd + cl * N;
         const double* vv = svals + cl * E;
@@ -1199,7 +1204,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           if (tmap[t] >= 0)
             StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
       }
-      tc::NamedSync(3, 256);
+      tc::NamedSync(qbar, 64);
     }
     tc::CpAsyncWaitAll();
   }
