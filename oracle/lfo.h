@@ -121,13 +121,23 @@ struct DofHandler {
   idx_t num_dofs = 0;
   std::vector<idx_t> node_dofs, edge_dofs, cell_dofs;
   std::vector<std::pair<int, idx_t>> dof_entity;  // (codim, entity index)
-  int NumLocalDofs(idx_t c) const { return mesh->IsQuad(c) ? n_quad : n_tria; }
+  // Variable-degree hierarchic layout (DynamicFEDofHandler): per-cell local
+  // dof counts and the per-entity degrees; empty for the uniform layouts.
+  std::vector<int> nloc, edge_deg, cell_deg;
+  int NumLocalDofs(idx_t c) const { return !nloc.empty() ? nloc[c] : mesh->IsQuad(c) ? n_quad : n_tria; }
   const idx_t* GlobalDofIndices(idx_t c) const { return &cell_dofs[c * n_cell]; }
 };
 DofHandler MakeDofHandler(const Mesh& m, int np, int ns, int nt, int nq,
                           bool check_edge_orientation = true);
 // uniform_scalar_fe_space.h:241-342 for FeSpaceLagrangeO{1,2,3}.
 DofHandler MakeLagrangeDofHandler(const Mesh& m, int degree);
+// HierarchicScalarFESpace(mesh, degree_functor) (fe/hierarchic_scalar_fe_space.h:
+// 93-116, Init :178-220) numbered by DynamicFEDofHandler (assemble/dofhandler.h:
+// 550-680): one dof per node, edge_deg[e] - 1 per edge, the interior count of
+// the cell's degree per cell; node dofs, then edge dofs, then cell dofs, each
+// by entity index; a cell's local dofs are its vertices, per local edge the
+// edge's dofs (reversed on a negatively oriented edge), then its interior.
+DofHandler MakeHierVarDofHandler(const Mesh& m, const std::vector<int>& edge_deg, const std::vector<int>& cell_deg);
 
 // ---------------------------------------------------------- mesh functions
 // A scalar MeshFunction (mesh_function_traits.h:149-155) evaluated on a cell
@@ -284,11 +294,20 @@ double HierIJacobi(unsigned n, double alpha, double x);
 // FeHierarchicTria / FeHierarchicQuad (fe/hierarchic_fe.h:473-1680) of
 // uniform degree p with the cell's relative edge orientations ori[j] = +1/-1.
 void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, double* phi, double (*dphi)[2]);
+// The same with the interior degree pc and per-edge degrees pe[j]
+// (FeHierarchicTria(interior_degree, edge_degrees, ...), hierarchic_fe.h:482-501,
+// and FeHierarchicQuad, :1150-1170): 3 or 4 vertex functions, pe[j] - 1
+// functions per local edge, then the interior functions of degree pc.
+void EvalHierShapeVar(bool is_quad, int pc, const int* pe, const int8_t* ori, double x, double y, double* phi,
+                      double (*dphi)[2]);
+int HierNumShapeVar(bool is_quad, int pc, const int* pe);
 // fe::DiffusionElementMatrixProvider + fe::MassElementMatrixProvider
 // (fe/loc_comp_ellbvp.h:169-214, 349-378; rule degree 2p) summed, assembled
 // over a HierarchicScalarFESpace of uniform degree p (dh from
 // MakeDofHandler(m, 1, p-1, ...)); fe::ScalarLoadElementVectorProvider
-// (:642-685).  qdeg 0 = 2p.
+// (:642-685).  qdeg 0 = 2p.  On a variable-degree space (dh.cell_deg not
+// empty) p is ignored: each cell uses its own degrees and, for qdeg 0, the
+// rule of degree 2 max(pc, pe[j], 1) (2 * Degree(), loc_comp_ellbvp.h:186).
 void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, const MeshFunction& gamma,
                         int qdeg, COOMatrix& A);
 void AssembleHierLoad(const DofHandler& dh, int p, const MeshFunction& f, int qdeg, std::vector<double>& b);

@@ -167,6 +167,26 @@ void lfo_space_cell_dofs(void* sp, int64_t* out) {
   auto* s = static_cast<Space*>(sp);
   std::memcpy(out, s->dh.cell_dofs.data(), s->dh.cell_dofs.size() * sizeof(int64_t));
 }
+// HierarchicScalarFESpace(mesh, degree_functor): degrees per edge (edge
+// order) and per cell (cell order).
+int lfo_space_create_hier_var(void* mp, const int32_t* edge_deg, const int32_t* cell_deg, void** out, char* err,
+                              int errlen) {
+  LFO_TRY
+  auto* m = static_cast<Mesh*>(mp);
+  auto s = std::make_unique<Space>();
+  s->mesh = m;
+  s->degree = 0;
+  s->dh = MakeHierVarDofHandler(*m, std::vector<int>(edge_deg, edge_deg + m->num_edges),
+                                std::vector<int>(cell_deg, cell_deg + m->num_cells));
+  *out = s.release();
+  LFO_CATCH
+}
+// Local dof count of every cell.
+void lfo_space_local_counts(void* sp, int32_t* out) {
+  auto* s = static_cast<Space*>(sp);
+  for (idx_t c = 0; c < s->mesh->num_cells; ++c) out[c] = s->dh.NumLocalDofs(c);
+}
+
 void lfo_space_dof_entity(void* sp, int32_t* codim, int64_t* idx) {
   auto* s = static_cast<Space*>(sp);
   for (size_t k = 0; k < s->dh.dof_entity.size(); ++k) {
@@ -407,6 +427,18 @@ int lfo_assemble_hier_load(void* sp, int p, const lfo_coeff* f, int qdeg, double
   std::vector<double> bv(b, b + s->dh.num_dofs);
   AssembleHierLoad(s->dh, p, mf, qdeg, bv);
   std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
+// Variable-degree FeHierarchicTria / Quad: interior degree pc, edge degrees pe[4].
+int lfo_hier_shape_var(int is_quad, int pc, const int32_t* pe, const int8_t* ori, int npts, const double* xy,
+                       double* phi, double* dphi, char* err, int errlen) {
+  LFO_TRY
+  const int pv[4] = {pe[0], pe[1], pe[2], pe[3]};
+  const int n = HierNumShapeVar(is_quad != 0, pc, pv);
+  for (int k = 0; k < npts; ++k)
+    EvalHierShapeVar(is_quad != 0, pc, pv, ori, xy[2 * k], xy[2 * k + 1], phi + static_cast<size_t>(k) * n,
+                     reinterpret_cast<double(*)[2]>(dphi + static_cast<size_t>(k) * n * 2));
   LFO_CATCH
 }
 

@@ -598,6 +598,70 @@ DofHandler MakeDofHandler(const Mesh& m, int np, int ns, int nt, int nq,
   return d;
 }
 
+DofHandler MakeHierVarDofHandler(const Mesh& m, const std::vector<int>& edge_deg, const std::vector<int>& cell_deg) {
+  if (static_cast<idx_t>(edge_deg.size()) != m.num_edges || static_cast<idx_t>(cell_deg.size()) != m.num_cells)
+    throw Error("one degree per edge and per cell expected");
+  for (int d : edge_deg)
+    if (d < 1) throw Error("edge degrees must be >= 1");
+  for (int d : cell_deg)
+    if (d < 1) throw Error("cell degrees must be >= 1");
+  DofHandler d;
+  d.mesh = &m;
+  d.np = 1;
+  d.edge_deg = edge_deg;
+  d.cell_deg = cell_deg;
+  idx_t dof = 0;
+  // Step I: one dof per node, in node order
+  d.node_dofs.assign(m.num_nodes, -1);
+  for (idx_t v = 0; v < m.num_nodes; ++v) {
+    d.node_dofs[v] = dof++;
+    d.dof_entity.push_back({2, v});
+  }
+  // Step II: edge_deg[e] - 1 interior dofs per edge, in edge order
+  std::vector<idx_t> edge_first(m.num_edges);
+  for (idx_t e = 0; e < m.num_edges; ++e) {
+    edge_first[e] = dof;
+    for (int j = 0; j < edge_deg[e] - 1; ++j) {
+      ++dof;
+      d.dof_entity.push_back({1, e});
+    }
+  }
+  // Step III: per cell its vertices, its edges' dofs, its interior dofs
+  d.nloc.assign(m.num_cells, 0);
+  int nmax = 0;
+  for (idx_t c = 0; c < m.num_cells; ++c) {
+    const int nv = m.NumVerts(c);
+    int pe[4] = {1, 1, 1, 1};
+    for (int k = 0; k < nv; ++k) pe[k] = edge_deg[m.cell_edges[c][k]];
+    d.nloc[c] = HierNumShapeVar(nv == 4, cell_deg[c], pe);
+    nmax = std::max(nmax, d.nloc[c]);
+  }
+  d.n_cell = nmax;
+  d.cell_dofs.assign(m.num_cells * static_cast<idx_t>(nmax), -1);
+  for (idx_t c = 0; c < m.num_cells; ++c) {
+    idx_t off = c * nmax;
+    const int nv = m.NumVerts(c);
+    for (int k = 0; k < nv; ++k) d.cell_dofs[off++] = d.node_dofs[m.cell_nodes[c][k]];
+    for (int k = 0; k < nv; ++k) {
+      const idx_t e = m.cell_edges[c][k];
+      const int ns = edge_deg[e] - 1;
+      if (m.cell_ori[c][k] > 0) {
+        for (int j = 0; j < ns; ++j) d.cell_dofs[off++] = edge_first[e] + j;
+      } else {
+        for (int j = ns - 1; j >= 0; --j) d.cell_dofs[off++] = edge_first[e] + j;
+      }
+    }
+    const int pc = cell_deg[c];
+    const int nint = nv == 4 ? (pc - 1) * (pc - 1) : (pc <= 2 ? 0 : (pc - 2) * (pc - 1) / 2);
+    for (int j = 0; j < nint; ++j) {
+      d.cell_dofs[off++] = dof++;
+      d.dof_entity.push_back({0, c});
+    }
+  }
+  d.num_dofs = dof;
+  return d;
+}
+
 DofHandler MakeLagrangeDofHandler(const Mesh& m, int degree) {
   // {pt:1, seg:p-1, tria:(p-1)(p-2)/2, quad:(p-1)^2} (lagr_fe.h NumRefShapeFunctions)
   const int p = degree;
@@ -1302,6 +1366,21 @@ double HierIJacobi(unsigned n, double alpha, double x) {
 }
 
 void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, double* phi, double (*dphi)[2]) {
+  const int pe[4] = {p, p, p, p};
+  EvalHierShapeVar(is_quad, p, pe, ori, x, y, phi, dphi);
+}
+
+int HierNumShapeVar(bool is_quad, int pc, const int* pe) {
+  const int nv = is_quad ? 4 : 3;
+  int n = nv;
+  for (int j = 0; j < nv; ++j) n += pe[j] - 1;
+  // NumRefShapeFunctions(0) (hierarchic_fe.h:528-535, :1198-1205)
+  n += is_quad ? (pc - 1) * (pc - 1) : (pc <= 2 ? 0 : (pc - 2) * (pc - 1) / 2);
+  return n;
+}
+
+void EvalHierShapeVar(bool is_quad, int pc, const int* pe, const int8_t* ori, double x, double y, double* phi,
+                      double (*dphi)[2]) {
   if (!is_quad) {
     // FeHierarchicTria::EvalReferenceShapeFunctions / Gradients... (hierarchic_fe.h:576-870)
     const double l[3] = {1 - x - y, x, y};
@@ -1316,6 +1395,7 @@ void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, d
       const int a = e, b = (e + 1) % 3;
       const double t = l[a] + l[b];
       const double tx = g[a][0] + g[b][0], ty = g[a][1] + g[b][1];
+      const int p = pe[e];
       for (int i = 0; i < p - 1; ++i) {
         const int src = ori[e] > 0 ? b : a;
         const int row = ori[e] > 0 ? cur + i : cur + p - 2 - i;
@@ -1326,6 +1406,7 @@ void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, d
       }
       cur += p - 1;
     }
+    const int p = pc;
     if (p > 2) {
       const int src = ori[0] > 0 ? 1 : 0;
       const double t = l[0] + l[1];
@@ -1360,46 +1441,63 @@ void EvalHierShape(bool is_quad, int p, const int8_t* ori, double x, double y, d
   term(2, 1, x, 1, 1, y, 1);
   term(3, 0, x, 1, 1, y, 1);
   int cur = 4;
-  for (int i = 0; i < p - 1; ++i) {
+  for (int i = 0; i < pe[0] - 1; ++i) {
     if (ori[0] > 0) term(cur + i, 2 + i, x, 1, 0, y, 1);
-    else term(cur + p - 2 - i, 2 + i, 1 - x, -1, 0, y, 1);
+    else term(cur + pe[0] - 2 - i, 2 + i, 1 - x, -1, 0, y, 1);
   }
-  cur += p - 1;
-  for (int i = 0; i < p - 1; ++i) {
+  cur += pe[0] - 1;
+  for (int i = 0; i < pe[1] - 1; ++i) {
     if (ori[1] > 0) term(cur + i, 1, x, 1, 2 + i, y, 1);
-    else term(cur + p - 2 - i, 1, x, 1, 2 + i, 1 - y, -1);
+    else term(cur + pe[1] - 2 - i, 1, x, 1, 2 + i, 1 - y, -1);
   }
-  cur += p - 1;
-  for (int i = 0; i < p - 1; ++i) {
+  cur += pe[1] - 1;
+  for (int i = 0; i < pe[2] - 1; ++i) {
     if (ori[2] > 0) term(cur + i, 2 + i, 1 - x, -1, 1, y, 1);
-    else term(cur + p - 2 - i, 2 + i, x, 1, 1, y, 1);
+    else term(cur + pe[2] - 2 - i, 2 + i, x, 1, 1, y, 1);
   }
-  cur += p - 1;
-  for (int i = 0; i < p - 1; ++i) {
+  cur += pe[2] - 1;
+  for (int i = 0; i < pe[3] - 1; ++i) {
     if (ori[3] > 0) term(cur + i, 0, x, 1, 2 + i, 1 - y, -1);
-    else term(cur + p - 2 - i, 0, x, 1, 2 + i, y, 1);
+    else term(cur + pe[3] - 2 - i, 0, x, 1, 2 + i, y, 1);
   }
-  cur += p - 1;
-  for (int i = 0; i < p - 1; ++i)
-    for (int j = 0; j < p - 1; ++j) term(cur++, j + 2, x, 1, i + 2, y, 1);
+  cur += pe[3] - 1;
+  for (int i = 0; i < pc - 1; ++i)
+    for (int j = 0; j < pc - 1; ++j) term(cur++, j + 2, x, 1, i + 2, y, 1);
 }
 
 namespace {
-int HierNumShape(bool q, int p) { return q ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2; }
+
+// Degrees of cell c: uniform p, or the cell's and its edges' own degrees on a
+// variable-degree space; returns the cell's Degree() (hierarchic_fe.h:506-509).
+int HierCellDegrees(const DofHandler& dh, idx_t c, int p, int& pc, int (&pe)[4]) {
+  const Mesh& m = *dh.mesh;
+  pc = p;
+  for (int j = 0; j < 4; ++j) pe[j] = p;
+  if (dh.cell_deg.empty()) return std::max(p, 1);
+  pc = dh.cell_deg[c];
+  int deg = std::max(pc, 1);
+  for (int j = 0; j < m.NumVerts(c); ++j) {
+    pe[j] = dh.edge_deg[m.cell_edges[c][j]];
+    deg = std::max(deg, pe[j]);
+  }
+  return deg;
+}
 
 void HierCellData(const DofHandler& dh, idx_t c, int p, int qdeg, std::vector<double>& phi, std::vector<double>& dphi,
                   QuadRule& qr) {
   const Mesh& m = *dh.mesh;
   const bool q = m.IsQuad(c);
-  qr = MakeQuadRule(q, qdeg > 0 ? qdeg : 2 * p);
+  int pc, pe[4];
+  const int deg = HierCellDegrees(dh, c, p, pc, pe);
+  qr = MakeQuadRule(q, qdeg > 0 ? qdeg : 2 * deg);
   int8_t ori[4];
   for (int j = 0; j < 4; ++j) ori[j] = m.cell_ori[c][j];
-  const int n = HierNumShape(q, p);
+  const int n = HierNumShapeVar(q, pc, pe);
   phi.assign(static_cast<size_t>(qr.n()) * n, 0.0);
   dphi.assign(static_cast<size_t>(qr.n()) * n * 2, 0.0);
   for (int k = 0; k < qr.n(); ++k)
-    EvalHierShape(q, p, ori, qr.x[k], qr.y[k], &phi[k * n],
-                  reinterpret_cast<double(*)[2]>(&dphi[static_cast<size_t>(k) * n * 2]));
+    EvalHierShapeVar(q, pc, pe, ori, qr.x[k], qr.y[k], &phi[k * n],
+                     reinterpret_cast<double(*)[2]>(&dphi[static_cast<size_t>(k) * n * 2]));
 }
 }  // namespace
 
@@ -1410,7 +1508,7 @@ void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, 
   QuadRule qr;
   AssembleMatrixLocally(dh, [&](idx_t c, std::vector<double>& out) {
     HierCellData(dh, c, p, qdeg, phi, dphi, qr);
-    const int n = HierNumShape(m.IsQuad(c), p);
+    const int n = dh.NumLocalDofs(c);
     const CellGeom geo = m.Geom(c);
     alpha.Eval(m, c, qr, av);
     gamma.Eval(m, c, qr, gv);
@@ -1439,7 +1537,7 @@ void AssembleHierLoad(const DofHandler& dh, int p, const MeshFunction& f, int qd
   QuadRule qr;
   AssembleVectorLocally(dh, [&](idx_t c, std::vector<double>& out) {
     HierCellData(dh, c, p, qdeg, phi, dphi, qr);
-    const int n = HierNumShape(m.IsQuad(c), p);
+    const int n = dh.NumLocalDofs(c);
     const CellGeom geo = m.Geom(c);
     f.Eval(m, c, qr, fv);
     out.assign(n, 0.0);

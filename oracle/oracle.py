@@ -97,6 +97,10 @@ def lib():
             L.lfo_assemble_hier_load.argtypes = [vp, C.c_int, P(lfo_coeff), C.c_int, P(dp), C.c_char_p, C.c_int]
             L.lfo_hier_shape.argtypes = [C.c_int, C.c_int, P(C.c_int8), C.c_int, P(dp), P(dp), P(dp), C.c_char_p,
                                          C.c_int]
+            L.lfo_space_create_hier_var.argtypes = [vp, P(i32), P(i32), P(vp), C.c_char_p, C.c_int]
+            L.lfo_space_local_counts.argtypes = [vp, P(i32)]
+            L.lfo_hier_shape_var.argtypes = [C.c_int, C.c_int, P(i32), P(C.c_int8), C.c_int, P(dp), P(dp), P(dp),
+                                             C.c_char_p, C.c_int]
             L.lfo_hier_fn.argtypes = [C.c_int, C.c_int, dp, dp, dp]
             L.lfo_hier_fn.restype = dp
             L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
@@ -211,6 +215,12 @@ class Space:
         idx = np.zeros(self.num_dofs, np.int64)
         lib().lfo_space_dof_entity(self.h, _p(cod, C.c_int32), _p(idx, C.c_int64))
         return cod, idx
+
+    def local_counts(self):
+        """Local dof count of every cell (NumLocalDofs)."""
+        out = np.zeros(self.mesh.num_cells, np.int32)
+        lib().lfo_space_local_counts(self.h, _p(out, C.c_int32))
+        return out
 
     def boundary_dof_flags(self):
         """Selector of the reference drivers: dof flagged iff its entity is on the boundary."""
@@ -478,6 +488,25 @@ def hier_space(mesh, p):
     return Space(mesh, 0, (1, p - 1, max(0, (p - 1) * (p - 2) // 2), (p - 1) * (p - 1)))
 
 
+def hier_var_space(mesh, edge_deg, cell_deg):
+    """HierarchicScalarFESpace(mesh, degree_functor) with the functor's values
+    per edge (edge order) and per cell (cell order), numbered like
+    DynamicFEDofHandler.  Assemble on it with p = 0."""
+    sp = Space.__new__(Space)
+    sp.mesh = mesh
+    sp.degree = 0
+    sp.h = C.c_void_p()
+    ed = np.ascontiguousarray(edge_deg, np.int32)
+    cd = np.ascontiguousarray(cell_deg, np.int32)
+    err = _err()
+    _check(lib().lfo_space_create_hier_var(mesh.h, _p(ed, C.c_int32), _p(cd, C.c_int32), C.byref(sp.h), err, 512),
+           err)
+    info = np.zeros(4, np.int64)
+    lib().lfo_space_info(sp.h, _p(info, C.c_int64))
+    sp.num_dofs, sp.n_cell, sp.n_tria, sp.n_quad = (int(v) for v in info)
+    return sp
+
+
 def assemble_hier(space, p, alpha, gamma, qdeg=0):
     h = C.c_void_p()
     err = _err()
@@ -502,6 +531,22 @@ def hier_shape(is_quad, p, ori, pts):
     err = _err()
     _check(lib().lfo_hier_shape(int(is_quad), p, _p(o, C.c_int8), len(pts), _p(pts, C.c_double),
                                 _p(phi, C.c_double), _p(dphi, C.c_double), err, 512), err)
+    return phi, dphi
+
+
+def hier_shape_var(is_quad, pc, pe, ori, pts):
+    """Shapes of FeHierarchicTria/Quad with interior degree pc and edge degrees pe."""
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 2)
+    nv = 4 if is_quad else 3
+    pe4 = np.ascontiguousarray(list(pe) + [1] * (4 - len(pe)), np.int32)
+    n = nv + sum(int(d) - 1 for d in pe[:nv])
+    n += (pc - 1) ** 2 if is_quad else (0 if pc <= 2 else (pc - 2) * (pc - 1) // 2)
+    o = np.ascontiguousarray(list(ori) + [1] * (4 - len(ori)), np.int8)
+    phi = np.zeros((len(pts), n))
+    dphi = np.zeros((len(pts), n, 2))
+    err = _err()
+    _check(lib().lfo_hier_shape_var(int(is_quad), pc, _p(pe4, C.c_int32), _p(o, C.c_int8), len(pts),
+                                    _p(pts, C.c_double), _p(phi, C.c_double), _p(dphi, C.c_double), err, 512), err)
     return phi, dphi
 
 
