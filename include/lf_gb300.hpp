@@ -37,7 +37,9 @@
 //   fe::InitEssentialConditionFromFunction         fe::InitEssentialConditionFromFunction(fes, edge
 //     (fe/fe_tools.h:263)                            flags, g) -> (flags, values) device vectors
 //   fe::HierarchicScalarFESpace(mesh, degree)      fe::HierarchicScalarFESpace(mesh, degree) (uniform degree)
-//     (fe/hierarchic_scalar_fe_space.h:36)
+//     (fe/hierarchic_scalar_fe_space.h:36)           and (mesh, degree_functor) with degree_functor(
+//   fe::HierarchicScalarFESpace(mesh, functor)       mesh::EntityRef{codim, index}) per edge and cell
+//     (fe/hierarchic_scalar_fe_space.h:93)
 //   fe::DiffusionElementMatrixProvider,            fe::DiffusionElementMatrixProvider,
 //   fe::MassElementMatrixProvider,                 fe::MassElementMatrixProvider,
 //   fe::ScalarLoadElementVectorProvider            fe::ScalarLoadElementVectorProvider (on a hierarchic
@@ -191,6 +193,14 @@ class TPMeshBuilder {
 using TPTriagMeshBuilder = TPMeshBuilder<false>;
 using TPQuadMeshBuilder = TPMeshBuilder<true>;
 
+// An entity named by codimension (0 cell, 1 edge, 2 node) and index: what a
+// degree functor receives (the reference passes const lf::mesh::Entity&).
+struct EntityRef {
+  int codim;
+  int64_t index;
+  int Codim() const { return codim; }
+};
+
 }  // namespace mesh
 
 namespace uscalfe {
@@ -202,6 +212,14 @@ class FeSpaceLagrange {
     lfg_space* h = nullptr;
     mesh_->ctx().Check(hierarchic ? lfg_space_create_hierarchic(mesh_->get(), degree, &h)
                                   : lfg_space_create_lagrange(mesh_->get(), degree, &h));
+    h_ = h;
+  }
+  // Hierarchic space with a degree per edge (edge order) and per cell (cell order).
+  FeSpaceLagrange(std::shared_ptr<const mesh::Mesh> m, const std::vector<int32_t>& edge_degree,
+                  const std::vector<int32_t>& cell_degree)
+      : mesh_(std::move(m)) {
+    lfg_space* h = nullptr;
+    mesh_->ctx().Check(lfg_space_create_hierarchic_var(mesh_->get(), edge_degree.data(), cell_degree.data(), &h));
     h_ = h;
   }
   ~FeSpaceLagrange() { lfg_space_destroy(h_); }
@@ -490,6 +508,18 @@ namespace fe {
 inline std::shared_ptr<uscalfe::FeSpaceLagrange> HierarchicScalarFESpace(std::shared_ptr<const mesh::Mesh> m,
                                                                         int degree) {
   return std::make_shared<uscalfe::FeSpaceLagrange>(std::move(m), degree, true);
+}
+// HierarchicScalarFESpace(mesh, degree_functor) (fe/hierarchic_scalar_fe_space.h:
+// 93-116): degree_functor(mesh::EntityRef) gives the degree (1..20) of every
+// edge and every cell, each called once; dofs numbered like DynamicFEDofHandler.
+template <class F, class = decltype(static_cast<int32_t>(std::declval<F&>()(std::declval<const mesh::EntityRef&>())))>
+std::shared_ptr<uscalfe::FeSpaceLagrange> HierarchicScalarFESpace(std::shared_ptr<const mesh::Mesh> m,
+                                                                 F&& degree_functor) {
+  const int64_t ne = m->NumEntities(1), nc = m->NumEntities(0);
+  std::vector<int32_t> ed(static_cast<size_t>(ne)), cd(static_cast<size_t>(nc));
+  for (int64_t e = 0; e < ne; ++e) ed[e] = static_cast<int32_t>(degree_functor(mesh::EntityRef{1, e}));
+  for (int64_t c = 0; c < nc; ++c) cd[c] = static_cast<int32_t>(degree_functor(mesh::EntityRef{0, c}));
+  return std::make_shared<uscalfe::FeSpaceLagrange>(std::move(m), ed, cd);
 }
 // fe::DiffusionElementMatrixProvider(fe_space, alpha) and
 // fe::MassElementMatrixProvider(fe_space, gamma) (fe/loc_comp_ellbvp.h:76,

@@ -163,6 +163,22 @@ lfg_status lfg_space_create_lagrange(lfg_mesh* mesh, int degree, lfg_space** out
  * 169-214, 349-378) and lfg_assemble_vector_load fe::ScalarLoadElementVector-
  * Provider (:642-685), with make_QuadRule(ref_el, 2 * degree) by default. */
 lfg_status lfg_space_create_hierarchic(lfg_mesh* mesh, int32_t degree, lfg_space** out);
+/* fe::HierarchicScalarFESpace(mesh, degree_functor) (fe/hierarchic_scalar_fe_space.h:
+ * 93-116, Init :178-220): the functor's value for every edge (edge_degree[ne],
+ * edge index order) and every cell (cell_degree[nc], cell index order), host
+ * arrays, each 1..20.  Dofs numbered by DynamicFEDofHandler (assemble/
+ * dofhandler.h:550-680): one per node, edge_degree[e] - 1 per edge, the
+ * interior count of cell_degree[c] per cell; a cell's shape functions are
+ * those of FeHierarchicTria/Quad(cell_degree, edge degrees, orientations)
+ * (fe/hierarchic_fe.h:482-501, 1150-1170), and the default rule of a cell is
+ * make_QuadRule(ref_el, 2 * max(cell degree, edge degrees)).  NumLocalDofs
+ * varies by cell (lfg_space_download_local_counts); lfg_space_info reports
+ * the counts of the largest degree as n_tria / n_quad.  Degrees outside 1..20:
+ * LFG_UNSUPPORTED. */
+lfg_status lfg_space_create_hierarchic_var(lfg_mesh* mesh, const int32_t* edge_degree, const int32_t* cell_degree,
+                                           lfg_space** out);
+/* NumLocalDofs of every cell (n_local[nc], host). */
+lfg_status lfg_space_download_local_counts(lfg_space* space, int32_t* n_local);
 lfg_status lfg_space_destroy(lfg_space* space);
 /* NumDofs, NumLocalDofs per tria / quad, row stride of the cell dof table,
  * and the number of triplets one AssembleMatrixLocally call emits. */

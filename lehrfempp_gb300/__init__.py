@@ -356,6 +356,27 @@ class Space:
         return sp
 
     @classmethod
+    def hierarchic_var(cls, mesh, edge_degree, cell_degree):
+        """fe::HierarchicScalarFESpace(mesh, degree_functor): the functor's value
+        per edge (edge order) and per cell (cell order), each 1..20."""
+        ed = np.ascontiguousarray(edge_degree, np.int32)
+        cd = np.ascontiguousarray(cell_degree, np.int32)
+        if len(ed) != mesh.num_edges or len(cd) != mesh.num_cells:
+            raise ValueError("one degree per edge and per cell expected")
+        h = C.c_void_p()
+        mesh.ctx.check(lib().lfg_space_create_hierarchic_var(mesh.h, _p(ed, C.c_int32), _p(cd, C.c_int32),
+                                                             C.byref(h)))
+        sp = cls(mesh, h, 0)
+        sp.hier_degree = int(max(ed.max(initial=1), cd.max(initial=1)))
+        return sp
+
+    def local_counts(self):
+        """NumLocalDofs of every cell."""
+        out = np.zeros(self.mesh.num_cells, np.int32)
+        self.ctx.check(lib().lfg_space_download_local_counts(self.h, _p(out, C.c_int32)))
+        return out
+
+    @classmethod
     def layout(cls, mesh, np_, ns, nt, nq):
         h = C.c_void_p()
         mesh.ctx.check(lib().lfg_space_create(mesh.h, np_, ns, nt, nq, C.byref(h)))

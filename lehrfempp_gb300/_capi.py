@@ -94,6 +94,8 @@ SIGNATURES = {
     "lfg_space_create": (c_status, [vp, C.c_int, C.c_int, C.c_int, C.c_int, P(vp)]),
     "lfg_space_create_lagrange": (c_status, [vp, C.c_int, P(vp)]),
     "lfg_space_create_hierarchic": (c_status, [vp, i32, P(vp)]),
+    "lfg_space_create_hierarchic_var": (c_status, [vp, P(i32), P(i32), P(vp)]),
+    "lfg_space_download_local_counts": (c_status, [vp, P(i32)]),
     "lfg_space_destroy": (c_status, [vp]),
     "lfg_space_info": (c_status, [vp, P(i64), P(i32), P(i32), P(i32), P(i64)]),
     "lfg_space_download_cell_dofs": (c_status, [vp, P(i32)]),

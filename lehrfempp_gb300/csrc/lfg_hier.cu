@@ -174,6 +174,11 @@ struct HierArgs {
   CoeffDev alpha, gamma;
   unsigned long long* fallback;  // cells whose coefficients left the df32 range (FP64 route)
   FastDiv div_n, div_E, div_nn;  // by n, E = n(n+1)/2 and n^2
+  // per-entity degrees: the cell's local shape function s is slot
+  // sel[c * n_cell + s] of the degree-D table; its count is
+  // loc_offset[c + 1] - loc_offset[c]
+  const uint16_t* sel;
+  const int64_t* loc_offset;
 };
 
 __device__ __forceinline__ void StoreTriplet(lfg_triplet* p, int r, int c, double v) {
@@ -236,8 +241,11 @@ __device__ __forceinline__ void LoadVerts(const HierArgs& a, int c, int4& cn, do
 // does about half an operation per triplet; a cell whose coefficients leave
 // the df32 range [2^-40, 2^40] is contracted in FP64 instead.
 // Shared memory: vals[T][E] | coef[T][4] | coef32[T][4] | base[T] | pat[T] |
-// cid[T] | safe[T] | dofs[T][n].
-template <bool QUAD, bool MASS>
+// cid[T] | safe[T] | dofs[T][n] | (VAR) nloc[T] | sel[T][n].  With VAR the
+// cells have their own shape-function subsets of the degree-D table: all E
+// table entries are contracted, and cell t writes its nloc[t]^2 triplets
+// through its selection.
+template <bool QUAD, bool MASS, bool VAR>
 __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T) {
   using namespace df;
   extern __shared__ __align__(16) double smem[];
@@ -250,6 +258,8 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
   int* cid = pat + T;
   int* safe = cid + T;
   int* dofs = safe + T;
+  int* nl = dofs + T * n;
+  uint16_t* ss = reinterpret_cast<uint16_t*>(nl + T);
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * T; t0 < a.count; t0 += static_cast<int64_t>(gridDim.x) * T) {
     const int tn = static_cast<int>(min(static_cast<int64_t>(T), a.count - t0));
     for (int t = threadIdx.x; t < tn; t += blockDim.x) {
@@ -277,11 +287,13 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
       base[t] = a.tri_offset[c];
       pat[t] = a.ori[c] & (QUAD ? 15 : 7);
       cid[t] = c;
+      if (VAR) nl[t] = static_cast<int>(a.loc_offset[c + 1] - a.loc_offset[c]);
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < tn * n; idx += blockDim.x) {
       const int t = Div(idx, a.div_n), i = idx - t * n;
       dofs[idx] = a.cell_dofs[static_cast<int64_t>(cid[t]) * a.n_cell + i];
+      if (VAR) ss[idx] = a.sel[static_cast<int64_t>(cid[t]) * a.n_cell + i];
     }
     for (int idx = threadIdx.x; idx < tn * E; idx += blockDim.x) {
       const int t = Div(idx, a.div_E), e = idx - t * E;
@@ -306,9 +318,18 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
     for (int q = threadIdx.x; q < tn * nn; q += blockDim.x) {
       const int t = Div(q, a.div_nn), rr = q - t * nn;
       const int i = Div(rr, a.div_n), j = rr - i * n;
-      const int lo = min(i, j), hi = max(i, j);
-      const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
-      StoreTriplet(a.out + base[t] + rr, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
+      if (VAR) {
+        const int m = nl[t];
+        if (i >= m || j >= m) continue;
+        const int ui = ss[t * n + i], uj = ss[t * n + j];
+        const int lo = min(ui, uj), hi = max(ui, uj);
+        const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
+        StoreTriplet(a.out + base[t] + i * m + j, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
+      } else {
+        const int lo = min(i, j), hi = max(i, j);
+        const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
+        StoreTriplet(a.out + base[t] + rr, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
+      }
     }
     __syncthreads();
   }
@@ -329,20 +350,23 @@ __global__ void NonAffineQuadsKernel(int64_t nq, const int32_t* __restrict__ lis
 }
 
 // General path: one cell per CTA iteration.  Shared memory: coef[nq][4] |
-// dofs[n] | (SYM) vals[E].  SYM computes each upper-triangle entry once into
-// shared memory and writes both halves from there (half the FP64 work);
-// without SYM (elements too large for shared memory) every (i, j) sums its
-// own point loop.
-template <bool QUAD, bool SYM>
+// (SYM) vals[E] | dofs[n] | (VAR) sel[n].  SYM computes each upper-triangle
+// entry once into shared memory and writes both halves from there (half the
+// FP64 work); without SYM (elements too large for shared memory) every (i, j)
+// sums its own point loop.  With VAR a cell has m <= n shape functions, the
+// degree-D table slots sel[0..m).
+template <bool QUAD, bool SYM, bool VAR>
 __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
   extern __shared__ __align__(16) double smem[];
-  const int n = a.L.n, nq = a.L.nq, nn = n * n;
+  const int n = a.L.n, nq = a.L.nq;
   double* coef = smem;
   double* vals = coef + 4 * nq;
   int* dofs = reinterpret_cast<int*>(vals + (SYM ? a.L.E : 0));
+  uint16_t* ss = reinterpret_cast<uint16_t*>(dofs + n);
   const double* __restrict__ tab = a.tab;
   for (int64_t ci = blockIdx.x; ci < a.count; ci += gridDim.x) {
     const int c = a.list[ci];
+    const int m = VAR ? static_cast<int>(a.loc_offset[c + 1] - a.loc_offset[c]) : n, mm = m * m;
     int4 cn;
     double2 v[4];
     LoadVerts<QUAD>(a, c, cn, v);
@@ -358,14 +382,18 @@ __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
       coef[4 * k + 2] = w * al * m11;
       coef[4 * k + 3] = w * adet * ga;
     }
-    for (int i = threadIdx.x; i < n; i += blockDim.x) dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+      if (VAR) ss[i] = a.sel[static_cast<int64_t>(c) * a.n_cell + i];
+    }
     __syncthreads();
     const double* P = tab + a.L.off_pat + pat * a.L.stride;
     const double* G = P + a.L.o_g;
     const int64_t base = a.tri_offset[c];
-    for (int q = threadIdx.x; q < nn; q += blockDim.x) {
-      const int i = q / n, j = q - i * n;
-      if (SYM && j < i) continue;
+    for (int q = threadIdx.x; q < mm; q += blockDim.x) {
+      const int si = q / m, sj = q - si * m;
+      if (SYM && sj < si) continue;
+      const int i = VAR ? ss[si] : si, j = VAR ? ss[sj] : sj;
       double acc = 0.0;
       for (int k = 0; k < nq; ++k) {
         const double2 gi = *reinterpret_cast<const double2*>(G + (static_cast<int64_t>(k) * n + i) * 2);
@@ -374,15 +402,15 @@ __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
         acc += cf[0] * (gi.x * gj.x) + cf[1] * (gi.x * gj.y + gi.y * gj.x) + cf[2] * (gi.y * gj.y) +
                cf[3] * (P[static_cast<int64_t>(k) * n + i] * P[static_cast<int64_t>(k) * n + j]);
       }
-      if (SYM) vals[i * n - i * (i - 1) / 2 + (j - i)] = acc;
-      else StoreTriplet(a.out + base + q, dofs[i], dofs[j], acc);
+      if (SYM) vals[si * m - si * (si - 1) / 2 + (sj - si)] = acc;
+      else StoreTriplet(a.out + base + q, dofs[si], dofs[sj], acc);
     }
     if (SYM) {
       __syncthreads();
-      for (int q = threadIdx.x; q < nn; q += blockDim.x) {
-        const int i = q / n, j = q - i * n;
+      for (int q = threadIdx.x; q < mm; q += blockDim.x) {
+        const int i = q / m, j = q - i * m;
         const int lo = min(i, j), hi = max(i, j);
-        StoreTriplet(a.out + base + q, dofs[i], dofs[j], vals[lo * n - lo * (lo - 1) / 2 + (hi - lo)]);
+        StoreTriplet(a.out + base + q, dofs[i], dofs[j], vals[lo * m - lo * (lo - 1) / 2 + (hi - lo)]);
       }
     }
     __syncthreads();
@@ -391,7 +419,7 @@ __global__ void __launch_bounds__(kHierBlock) HierGeneralKernel(HierArgs a) {
 
 // Element vectors: s_k = (w_k |det J_k|) f(x_k), v_i = sum_k s_k phi_i(x_k),
 // into ev at the cell's local offset.  Shared memory: s[nq].
-template <bool QUAD>
+template <bool QUAD, bool VAR>
 __global__ void __launch_bounds__(kHierBlock) HierLoadKernel(HierArgs a, CoeffDev f, const int64_t* loc_offset,
                                                             double* ev) {
   extern __shared__ __align__(16) double smem[];
@@ -412,10 +440,12 @@ __global__ void __launch_bounds__(kHierBlock) HierLoadKernel(HierArgs a, CoeffDe
     __syncthreads();
     const double* P = tab + a.L.off_pat + pat * a.L.stride;
     const int64_t b = loc_offset[c];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int m = VAR ? static_cast<int>(loc_offset[c + 1] - b) : n;
+    for (int si = threadIdx.x; si < m; si += blockDim.x) {
+      const int i = VAR ? a.sel[static_cast<int64_t>(c) * a.n_cell + si] : si;
       double s = 0.0;
       for (int k = 0; k < nq; ++k) s += smem[k] * P[static_cast<int64_t>(k) * n + i];
-      ev[b + i] = s;
+      ev[b + si] = s;
     }
     __syncthreads();
   }
@@ -439,6 +469,8 @@ HierArgs BaseHierArgs(lfg_space* sp) {
   a.cell_dofs = sp->cell_dofs.as<int32_t>();
   a.n_cell = sp->n_cell;
   a.tri_offset = sp->tri_offset.as<int64_t>();
+  a.sel = sp->hier_var ? sp->hv_sel.as<uint16_t>() : nullptr;
+  a.loc_offset = sp->loc_offset.as<int64_t>();
   return a;
 }
 
@@ -473,12 +505,12 @@ int64_t NonAffineQuads(lfg_mesh* m) {
   return m->nonaffine_quads;
 }
 
-template <bool QUAD>
+template <bool QUAD, bool VAR>
 void LaunchAffine(lfg_ctx* ctx, const HierArgs& a, bool mass) {
   const int n = a.L.n, E = a.L.E;
   auto smem_for = [&](int t) {
     return static_cast<size_t>(t) * E * 8 + static_cast<size_t>(t) * (4 * 8 + 4 * 8 + 8 + 4 * 4) +
-           static_cast<size_t>(t) * n * 4;
+           static_cast<size_t>(t) * n * 4 + (VAR ? static_cast<size_t>(t) * (4 + 2 * n) : 0);
   };
   int T = std::max(1, std::min(32, 4096 / (n * n)));
   while (T > 1 && smem_for(T) > 96 * 1024) --T;
@@ -486,33 +518,46 @@ void LaunchAffine(lfg_ctx* ctx, const HierArgs& a, bool mass) {
   const int64_t tiles = (a.count + T - 1) / T;
   ProfScope prof(ctx, QUAD ? "hier_quad_affine" : "hier_tria_affine");
   if (mass) {
-    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, true>, smem, tiles);
-    HierAffineKernel<QUAD, true><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
+    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, true, VAR>, smem, tiles);
+    HierAffineKernel<QUAD, true, VAR><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
   } else {
-    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, false>, smem, tiles);
-    HierAffineKernel<QUAD, false><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
+    const int grid = HierGrid(ctx, HierAffineKernel<QUAD, false, VAR>, smem, tiles);
+    HierAffineKernel<QUAD, false, VAR><<<grid, kHierBlock, smem, ctx->stream>>>(a, T);
   }
   LFG_LAUNCHED(ctx);
 }
 
-bool AffineFits(bool quad, int p) {
+bool AffineFits(bool quad, int p, bool var) {
   const size_t n = quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
-  return n * (n + 1) / 2 * 8 + 96 + n * 4 <= kHierSmemLimit;
+  return n * (n + 1) / 2 * 8 + 96 + n * 4 + (var ? 4 + 2 * n : 0) <= kHierSmemLimit;
 }
 
-template <bool QUAD>
+template <bool QUAD, bool VAR>
 void LaunchGeneral(lfg_ctx* ctx, const HierArgs& a) {
-  const size_t base = static_cast<size_t>(a.L.nq) * 32 + static_cast<size_t>(a.L.n) * 4;
+  const size_t base = static_cast<size_t>(a.L.nq) * 32 + static_cast<size_t>(a.L.n) * (VAR ? 6 : 4);
   const size_t sym = base + static_cast<size_t>(a.L.E) * 8;
   ProfScope prof(ctx, QUAD ? "hier_general_quad" : "hier_general_tria");
   if (sym <= kHierSmemLimit) {
-    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, true>, sym, a.count);
-    HierGeneralKernel<QUAD, true><<<grid, kHierBlock, sym, ctx->stream>>>(a);
+    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, true, VAR>, sym, a.count);
+    HierGeneralKernel<QUAD, true, VAR><<<grid, kHierBlock, sym, ctx->stream>>>(a);
   } else {
-    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, false>, base, a.count);
-    HierGeneralKernel<QUAD, false><<<grid, kHierBlock, base, ctx->stream>>>(a);
+    const int grid = HierGrid(ctx, HierGeneralKernel<QUAD, false, VAR>, base, a.count);
+    HierGeneralKernel<QUAD, false, VAR><<<grid, kHierBlock, base, ctx->stream>>>(a);
   }
   LFG_LAUNCHED(ctx);
+}
+
+// The cells of one type (all of them, or one degree group of a
+// variable-degree space) against the degree-p table.
+template <bool QUAD, bool VAR>
+void LaunchHierCells(lfg_ctx* ctx, HierArgs a, int p, int rule_degree, bool uniform, bool mass) {
+  const bool affine = uniform && AffineFits(QUAD, p, VAR);
+  a.tab = GetHierTable(ctx, QUAD, p, rule_degree, affine, a.L);
+  a.div_n = MakeFastDiv(a.L.n);
+  a.div_E = MakeFastDiv(a.L.n * (a.L.n + 1) / 2);
+  a.div_nn = MakeFastDiv(a.L.n * a.L.n);
+  if (affine) LaunchAffine<QUAD, VAR>(ctx, a, mass);
+  else LaunchGeneral<QUAD, VAR>(ctx, a);
 }
 
 void HierAssembleMatrix(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo) {
@@ -531,32 +576,36 @@ void HierAssembleMatrix(lfg_space* sp, const lfg_rd_provider* pr, lfg_coo* coo) 
   HierArgs a = BaseHierArgs(sp);
   a.out = coo->d + coo->size;
   a.alpha = ToDev(pr->alpha, m, "alpha");
-  auto set_div = [&](int n) {
-    a.div_n = MakeFastDiv(n);
-    a.div_E = MakeFastDiv(n * (n + 1) / 2);
-    a.div_nn = MakeFastDiv(n * n);
-  };
   a.gamma = ToDev(pr->gamma, m, "gamma");
   a.fallback = reinterpret_cast<unsigned long long*>(StatusWord(ctx) + 12);
   const bool uniform = CellConstantKind(pr->alpha) && CellConstantKind(pr->gamma);
   const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
+  // the folded kernel serves quadrilaterals only when all are parallelograms
+  const bool quad_uniform = uniform && m->nquad > 0 && NonAffineQuads(m) == 0;
+  if (sp->hier_var) {
+    // one launch per (cell type, degree D) group, D's table and rule 2 D
+    // (2 * Degree(), fe/loc_comp_ellbvp.h:186) unless a rule degree is given
+    for (const HierGroup& g : sp->hv_groups) {
+      a.list = sp->hv_sorted.as<int32_t>() + g.start;
+      a.count = g.count;
+      if (g.quad)
+        LaunchHierCells<true, true>(ctx, a, g.degree, HierRuleDegree(pr->qr_degree_quad, g.degree),
+                                    quad_uniform, mass);
+      else
+        LaunchHierCells<false, true>(ctx, a, g.degree, HierRuleDegree(pr->qr_degree_tria, g.degree), uniform, mass);
+    }
+    coo->size += sp->num_triplets;
+    return;
+  }
   if (m->ntria) {
-    const bool affine = uniform && AffineFits(false, p);
-    a.tab = GetHierTable(ctx, false, p, HierRuleDegree(pr->qr_degree_tria, p), affine, a.L);
     a.list = m->tria_list.as<int32_t>();
     a.count = m->ntria;
-    set_div(a.L.n);
-    if (affine) LaunchAffine<false>(ctx, a, mass);
-    else LaunchGeneral<false>(ctx, a);
+    LaunchHierCells<false, false>(ctx, a, p, HierRuleDegree(pr->qr_degree_tria, p), uniform, mass);
   }
   if (m->nquad) {
-    const bool affine = uniform && AffineFits(true, p) && NonAffineQuads(m) == 0;
-    a.tab = GetHierTable(ctx, true, p, HierRuleDegree(pr->qr_degree_quad, p), affine, a.L);
     a.list = m->quad_list.as<int32_t>();
     a.count = m->nquad;
-    set_div(a.L.n);
-    if (affine) LaunchAffine<true>(ctx, a, mass);
-    else LaunchGeneral<true>(ctx, a);
+    LaunchHierCells<true, false>(ctx, a, p, HierRuleDegree(pr->qr_degree_quad, p), quad_uniform, mass);
   }
   coo->size += sp->num_triplets;
 }
@@ -574,21 +623,39 @@ void HierAssembleVector(lfg_space* sp, const lfg_load_provider* pr, double* b) {
   HierArgs a = BaseHierArgs(sp);
   double* ev = sp->scratch_vec.as<double>();
   ProfScope prof(ctx, "hier_load");
-  for (int q = 0; q < 2; ++q) {
-    const bool quad = q == 1;
-    const int64_t count = quad ? m->nquad : m->ntria;
-    if (!count) continue;
-    a.tab = GetHierTable(ctx, quad, p, HierRuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, p), false,
-                         a.L);
-    a.list = quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
-    a.count = count;
+  // (cell type, degree, first entry, count) of every launch
+  std::vector<HierGroup> groups;
+  if (sp->hier_var) {
+    groups = sp->hv_groups;
+  } else {
+    for (int q = 0; q < 2; ++q) {
+      HierGroup g;
+      g.quad = q == 1;
+      g.degree = p;
+      g.count = g.quad ? m->nquad : m->ntria;
+      if (g.count) groups.push_back(g);
+    }
+  }
+  for (const HierGroup& g : groups) {
+    a.tab = GetHierTable(ctx, g.quad, g.degree,
+                         HierRuleDegree(g.quad ? pr->qr_degree_quad : pr->qr_degree_tria, g.degree), false, a.L);
+    if (sp->hier_var) a.list = sp->hv_sorted.as<int32_t>() + g.start;
+    else a.list = g.quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
+    a.count = g.count;
     const size_t smem = static_cast<size_t>(a.L.nq) * 8;
-    if (quad) {
-      const int grid = HierGrid(ctx, HierLoadKernel<true>, smem, count);
-      HierLoadKernel<true><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, sp->loc_offset.as<int64_t>(), ev);
+    const int64_t* lo = sp->loc_offset.as<int64_t>();
+    if (g.quad && sp->hier_var) {
+      const int grid = HierGrid(ctx, HierLoadKernel<true, true>, smem, g.count);
+      HierLoadKernel<true, true><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, lo, ev);
+    } else if (g.quad) {
+      const int grid = HierGrid(ctx, HierLoadKernel<true, false>, smem, g.count);
+      HierLoadKernel<true, false><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, lo, ev);
+    } else if (sp->hier_var) {
+      const int grid = HierGrid(ctx, HierLoadKernel<false, true>, smem, g.count);
+      HierLoadKernel<false, true><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, lo, ev);
     } else {
-      const int grid = HierGrid(ctx, HierLoadKernel<false>, smem, count);
-      HierLoadKernel<false><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, sp->loc_offset.as<int64_t>(), ev);
+      const int grid = HierGrid(ctx, HierLoadKernel<false, false>, smem, g.count);
+      HierLoadKernel<false, false><<<grid, kHierBlock, smem, ctx->stream>>>(a, f, lo, ev);
     }
     LFG_LAUNCHED(ctx);
   }

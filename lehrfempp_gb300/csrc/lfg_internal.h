@@ -149,11 +149,30 @@ constexpr int kMaxLocalDofs = 1024;  // local shape functions per cell ((p+1)^2 
 constexpr int kMaxHierDegree = 20;   // hierarchic degree (quadrilateral: 441 local dofs)
 }  // namespace lfg
 
+namespace lfg {
+// Cells of one type and one hierarchic degree D (max of the cell's and its
+// edges' degrees): entries [start, start + count) of lfg_space::hv_sorted.
+struct HierGroup {
+  bool quad = false;
+  int degree = 0;
+  int64_t start = 0, count = 0;
+};
+}  // namespace lfg
+
 struct lfg_space {
   lfg::CtxRef ref;
   lfg_mesh* mesh = nullptr;
   int degree = 0;  // 0 = generic layout
   int hier_degree = 0;  // > 0: HierarchicScalarFESpace of this uniform degree (generic layout)
+  // Per-entity hierarchic degrees (HierarchicScalarFESpace with a degree
+  // functor, DynamicFEDofHandler numbering); hier_degree is then the largest.
+  bool hier_var = false;
+  lfg::DevBuf hv_edge_deg;    // int32[ne]
+  lfg::DevBuf hv_edge_first;  // int64[ne + 1]: first interior dof of each edge, minus the node count
+  lfg::DevBuf hv_sel;         // uint16[nc * n_cell]: degree-D basis slot of every local shape function
+  lfg::DevBuf hv_sorted;      // int32[nc]: triangles, then quadrilaterals, each stably grouped by D
+  std::vector<lfg::HierGroup> hv_groups;
+  std::vector<int32_t> hv_edge_deg_host, hv_cell_deg_host;
   int np = 0, ns = 0, nt = 0, nq = 0;
   int n_tria = 0, n_quad = 0, n_cell = 0, n_edge = 0;
   int64_t num_dofs = 0;

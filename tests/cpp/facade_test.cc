@@ -276,6 +276,29 @@ static void CheckHierarchic(const g::Context& ctx) {
   for (double r : row) mx = std::max(mx, std::fabs(r));
   CHECK(mx < 1e-11, "diffusion matrix rows over vertex functions sum to %.3g", mx);
   std::printf("hierarchic: degree 4, %lld dofs, mass area %.15f\n", static_cast<long long>(nd), s);
+  // a degree functor: edges 2 + index % 3, cells 1 + index % 4; with constant
+  // alpha the diffusion matrix still annihilates the constants
+  auto vfes = g::fe::HierarchicScalarFESpace(
+      mesh, [](const g::mesh::EntityRef& e) { return e.Codim() == 1 ? 2 + e.index % 3 : 1 + e.index % 4; });
+  const int64_t vnd = vfes->NumDofs();
+  int64_t want = nv;
+  for (int64_t e = 0; e < mesh->NumEntities(1); ++e) want += 1 + e % 3;
+  for (int64_t c = 0; c < mesh->NumEntities(0); ++c) {
+    const int p = 1 + static_cast<int>(c % 4);
+    want += p <= 2 ? 0 : (p - 2) * (p - 1) / 2;
+  }
+  CHECK(vnd == want, "variable-degree hierarchic space has %lld dofs, expected %lld", static_cast<long long>(vnd),
+        static_cast<long long>(want));
+  g::fe::DiffusionElementMatrixProvider vdp(vfes, g::uscalfe::MeshFunction::Constant(1.0));
+  g::assemble::COOMatrix VA(ctx, vnd, vnd, vfes->NumTriplets());
+  g::assemble::AssembleMatrixLocally(0, *vfes, *vfes, vdp, VA);
+  std::vector<double> vrow(vnd, 0.0);
+  for (const lfg_triplet& t : VA.Download())
+    if (t.col < nv) vrow[t.row] += t.value;
+  double vmx = 0.0;
+  for (double r : vrow) vmx = std::max(vmx, std::fabs(r));
+  CHECK(vmx < 1e-11, "variable-degree diffusion matrix applied to 1 has entries up to %.3g", vmx);
+  std::printf("hierarchic: per-entity degrees, %lld dofs\n", static_cast<long long>(vnd));
 }
 
 static double Lcg(uint64_t& s) {
