@@ -471,6 +471,24 @@ def hier_leg(L, W, ctx, steps=3, cpu_check=False):
                                          "triplets": ntrip, "ms": ms, "triplets_per_s": ntrip / (ms * 1e-3),
                                          "triplet_write_gbs": ntrip * 16 / (ms * 1e-3) / 1e9}
             del coo, sp, mesh
+    # per-entity degrees (HierarchicScalarFESpace with a degree functor): every
+    # edge and cell of a 768 x 768 TPTriag mesh draws its degree from 2..6
+    mesh = L.Mesh.tp_triag(ctx, 768, 768)
+    rng = np.random.default_rng(17)
+    sp = L.Space.hierarchic_var(mesh, rng.integers(2, 7, mesh.num_edges), rng.integers(2, 7, mesh.num_cells))
+    ntrip = sp.num_triplets
+    coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, ntrip)
+    prov = L.rd_provider(alpha, L.coeff(L.ZERO))
+    L.assemble_matrix_rd(sp, prov, coo)
+    ctx.timer_begin()
+    for _ in range(steps):
+        coo.set_zero()
+        L.assemble_matrix_rd(sp, prov, coo)
+    ms = ctx.timer_end() / steps
+    out["tria_var_p2to6"] = {"mesh": "768x768", "degrees": "edges and cells uniform in 2..6 (seed 17)",
+                             "cells": mesh.num_cells, "dofs": sp.num_dofs, "triplets": ntrip, "ms": ms,
+                             "triplets_per_s": ntrip / (ms * 1e-3), "triplet_write_gbs": ntrip * 16 / (ms * 1e-3) / 1e9}
+    del coo, sp, mesh
     if cpu_check:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
