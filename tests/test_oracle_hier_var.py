@@ -9,6 +9,9 @@ DynamicFEDofHandler (assemble/dofhandler.h:550-680).
   `sel_map` (the selection the device kernels use), bit for bit;
 - a random FE function is continuous across interior edges (the variable
   counterpart of fe_space_hierarchic_tests.cc:166-423);
+- the reference's own varying-degree continuity test (its degree pattern,
+  edge traces against the segment functions, fe_space_hierarchic_tests.cc:
+  166-247);
 - the L2 projection onto a space whose degrees are all >= 2 reproduces a
   quadratic exactly (a known answer pinning numbering, functions and rules);
 - constants are in the kernel of the stiffness matrix and the vertex block of
@@ -124,6 +127,43 @@ def test_variable_space_is_continuous_across_edges(seed):
                 vals.append(phi @ u[dofs[c, :nl[c]]])
         assert len(vals) == 2
         assert np.abs(vals[0] - vals[1]).max() < 1e-10, e
+
+
+def test_edge_traces_with_the_reference_degree_pattern():
+    """fe_space_hierarchic_tests.cc:166-247 with its own degree assignment: one
+    counter runs over the cells and then over the edges, and entity k gets
+    degree k % 2 + 2 (nodes degree 1).  For every local edge i of every cell,
+    at p + 1 equispaced points (p = 1..10) along the edge in the edge's own
+    direction, the cell's shape functions of that edge equal the segment's
+    interior functions ILegendre(r + 2, t) (FeHierarchicSegment,
+    hierarchic_fe.h:297-310); on a negatively oriented edge the cell's slots
+    run backwards.  Tolerance 1e-10, as in the reference test."""
+    m = mesh0()
+    k = np.arange(m.num_cells + m.num_edges) % 2 + 2
+    cd, ed = k[: m.num_cells], k[m.num_cells:]
+    s = O.hier_var_space(m, ed, cd)
+    nl = s.local_counts()
+    checked = 0
+    for p in range(1, 11):
+        t = np.linspace(0.0, 1.0, p + 1)
+        seg = np.array([[O.hier_fn(1, r + 2, 1.0, 0.0, x) for x in t] for r in range(int(ed.max()) - 1)])
+        for c in range(m.num_cells):
+            quad = m.cells[c, 3] >= 0
+            nv = 4 if quad else 3
+            pc, pe, ori = cell_degrees(m, c, ed, cd)
+            nint = (pc - 1) ** 2 if quad else max(0, (pc - 2) * (pc - 1) // 2)
+            assert nl[c] == nv + sum(d - 1 for d in pe) + nint
+            off = nv
+            for i in range(nv):
+                tt = t if ori[i] > 0 else 1.0 - t
+                phi, _ = O.hier_shape_var(quad, pc, pe, ori, _ref_edge_points(quad, i, tt))
+                ke = pe[i] - 1
+                for r in range(ke):
+                    slot = off + r if ori[i] > 0 else off + ke - 1 - r
+                    assert np.abs(phi[:, slot] - seg[r]).max() < 1e-10, (p, c, i, r)
+                    checked += 1
+                off += ke
+    assert checked > 0
 
 
 def test_dof_numbering_follows_dynamic_dof_handler():
