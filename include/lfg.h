@@ -177,7 +177,8 @@ lfg_status lfg_space_create_hierarchic(lfg_mesh* mesh, int32_t degree, lfg_space
  * LFG_UNSUPPORTED. */
 lfg_status lfg_space_create_hierarchic_var(lfg_mesh* mesh, const int32_t* edge_degree, const int32_t* cell_degree,
                                            lfg_space** out);
-/* NumLocalDofs of every cell (n_local[nc], host). */
+/* DofHandler::NumLocalDofs(cell) (assemble/dofhandler.h:147) of every cell,
+ * in cell index order (n_local[nc], host). */
 lfg_status lfg_space_download_local_counts(lfg_space* space, int32_t* n_local);
 lfg_status lfg_space_destroy(lfg_space* space);
 /* NumDofs, NumLocalDofs per tria / quad, row stride of the cell dof table,
