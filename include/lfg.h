@@ -59,7 +59,9 @@ typedef struct {
   double value;
 } lfg_triplet;
 
-/* ------------------------------------------------------------------ context */
+/* ------------------------------------------------------------------ context
+ * Library plumbing, no counterpart in the reference (a single-threaded CPU
+ * library with no device or stream): one context per device and stream. */
 lfg_status lfg_ctx_create(int device, lfg_ctx** out);
 lfg_status lfg_ctx_destroy(lfg_ctx* ctx);
 const char* lfg_ctx_last_error(const lfg_ctx* ctx);
@@ -68,7 +70,8 @@ lfg_status lfg_ctx_synchronize(lfg_ctx* ctx);
 /* Kernel launches issued by the library on this context since creation. */
 lfg_status lfg_ctx_launch_count(const lfg_ctx* ctx, int64_t* launches);
 
-/* Device memory and copies on the context's stream (no torch needed). */
+/* Device memory and copies on the context's stream (no torch needed); no
+ * counterpart in the reference, whose data lives in host memory. */
 lfg_status lfg_malloc(lfg_ctx* ctx, size_t bytes, void** dev);
 lfg_status lfg_free(lfg_ctx* ctx, void* dev);
 lfg_status lfg_host_alloc(lfg_ctx* ctx, size_t bytes, void** pinned_host);
@@ -79,7 +82,8 @@ lfg_status lfg_memcpy_d2d(lfg_ctx* ctx, void* dst_dev, const void* src_dev, size
 lfg_status lfg_memset(lfg_ctx* ctx, void* dev, int value, size_t bytes);
 
 /* CUDA-event timing on the context stream, and an L2 flush (writes a buffer
- * larger than L2) for cold-cache measurements. */
+ * larger than L2) for cold-cache measurements; measurement plumbing with no
+ * counterpart in the reference. */
 lfg_status lfg_timer_begin(lfg_ctx* ctx);
 lfg_status lfg_timer_end(lfg_ctx* ctx, float* elapsed_ms);
 lfg_status lfg_l2_flush(lfg_ctx* ctx);
@@ -185,9 +189,11 @@ lfg_status lfg_space_destroy(lfg_space* space);
  * and the number of triplets one AssembleMatrixLocally call emits. */
 lfg_status lfg_space_info(const lfg_space* space, int64_t* num_dofs, int32_t* n_tria,
                           int32_t* n_quad, int32_t* n_cell_stride, int64_t* num_triplets);
-/* GlobalDofIndices of every cell (num_cells x n_cell_stride, -1 pad), host out. */
+/* DofHandler::GlobalDofIndices(cell) (assemble/dofhandler.h:184) of every cell
+ * (num_cells x n_cell_stride, -1 pad), host out. */
 lfg_status lfg_space_download_cell_dofs(lfg_space* space, int32_t* cell_dofs_host);
-/* Entity(dof) for every dof: codim (2 node, 1 edge, 0 cell) and index, host out. */
+/* DofHandler::Entity(dof) (assemble/dofhandler.h:219) for every dof: codim
+ * (2 node, 1 edge, 0 cell) and index, host out. */
 lfg_status lfg_space_download_dof_entities(lfg_space* space, int8_t* codim_host,
                                            int32_t* index_host);
 /* Selector of the reference drivers: dof flagged iff its entity lies on the
@@ -282,13 +288,15 @@ lfg_status lfg_coo_create(lfg_ctx* ctx, int64_t rows, int64_t cols, int64_t capa
 lfg_status lfg_coo_wrap(lfg_ctx* ctx, int64_t rows, int64_t cols, lfg_triplet* triplets_dev,
                         int64_t capacity, int64_t size, lfg_coo** out);
 lfg_status lfg_coo_destroy(lfg_coo* coo);
+/* COOMatrix::triplets() (coomatrix.h:124-125): its length and its device storage. */
 lfg_status lfg_coo_size(const lfg_coo* coo, int64_t* size);
 lfg_status lfg_coo_triplets(lfg_coo* coo, lfg_triplet** triplets_dev);
 /* COOMatrix::setZero() (coomatrix.h:95-98): drop all triplets. */
 lfg_status lfg_coo_set_zero(lfg_coo* coo);
-/* Copy the first `count` triplets to host memory (count <= size). */
+/* Copy the first `count` triplets of COOMatrix::triplets() (coomatrix.h:124)
+ * to host memory (count <= size). */
 lfg_status lfg_coo_download(lfg_coo* coo, lfg_triplet* host, int64_t count);
-/* Append host triplets (AddToEntry for each). */
+/* Append host triplets (COOMatrix::AddToEntry, coomatrix.h:87-91, for each). */
 lfg_status lfg_coo_append_host(lfg_coo* coo, const lfg_triplet* host, int64_t count);
 
 /* ------------------------------------------------------------------ assembly
@@ -335,7 +343,8 @@ lfg_status lfg_csr_destroy(lfg_csr* csr);
 lfg_status lfg_csr_info(const lfg_csr* csr, int64_t* rows, int64_t* cols, int64_t* nnz);
 lfg_status lfg_csr_download(lfg_csr* csr, int64_t* rowptr_host, int32_t* col_host,
                             double* val_host);
-/* y = A x (FP64). */
+/* y = A x (FP64): the product of the Eigen::SparseMatrix that
+ * COOMatrix::makeSparse (coomatrix.h:172-180) returns. */
 lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
 
 /* Solve A x = b for the (symmetric positive definite, after fixing) Galerkin
