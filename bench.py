@@ -9,7 +9,9 @@ alpha per-cell LogNormal(0,1), gamma = 0, default degree-4 rules:
 (129 MB), so every step streams from/to HBM.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--size 2048] [--solve-size 512] [--no-cpu-baseline]
+                  [--size 2048] [--solve-size 2048] [--no-cpu-baseline]
+  python bench.py --case pcg:N:ITERATIONS        # PCG timing case (profiling)
+  python bench.py --case hier:N:DEGREE:tria|quad:REPEATS
 
 --impl reference times the CPU restatement of the reference's assembly
 (oracle/, C++) on the host cores, all threads, on the same workload.
@@ -50,7 +52,65 @@ def parse():
     ap.add_argument("--ho-size", type=int, default=1024, help="config-3 mesh size (0: skip the high-order leg)")
     ap.add_argument("--gmsh", type=int, default=1, help="run the Gmsh-reader leg (0: skip)")
     ap.add_argument("--hier", type=int, default=1, help="run the hierarchic-FE leg (0: skip)")
+    ap.add_argument("--case", default=None,
+                    help="run one timing case instead of the benchmark (used for the ncu captures): "
+                         "pcg:N:ITERATIONS or hier:N:DEGREE:tria|quad:REPEATS")
     return ap.parse_args()
+
+
+def run_case(spec):
+    """One timing case, printed as a JSON line.
+
+    pcg:N:IT   -- TPTriag N x N, LagrangeO1, alpha = exp(theta) per cell (the
+                  inverse-conductivity workload), gamma 0, f 1, Dirichlet 0:
+                  assemble, fix, CSR, then IT PCG iterations (rtol 0: the
+                  iteration cap ends the solve) twice in FP64 and twice in
+                  mixed precision; microseconds per iteration.
+    hier:N:P:K:R -- TPTriag (K = tria) or TPQuad (K = quad) N x N,
+                  HierarchicScalarFESpace of degree P, alpha 1, R assemblies
+                  into one COO matrix; milliseconds per assembly."""
+    import lehrfempp_gb300 as L
+    from lehrfempp_gb300 import workloads as W
+    f = spec.split(":")
+    ctx = L.Context(0)
+    out = {"case": spec}
+    if f[0] == "pcg":
+        n, iters = int(f[1]), int(f[2])
+        mesh = L.Mesh.tp_triag(ctx, n, n)
+        sp = L.Space.lagrange(mesh, 1)
+        theta = ctx.to_device(W.config5(n)["theta"])
+        coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets + sp.num_dofs)
+        L.assemble_matrix_rd(sp, L.rd_provider(L.coeff(L.PER_CELL_EXP, data=theta), L.coeff(L.ZERO)), coo)
+        b = ctx.zeros(sp.num_dofs)
+        L.assemble_vector_load(sp, L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+        coo.fix_flagged_solution_components(sp.boundary_dof_flags(), ctx.zeros(sp.num_dofs), b)
+        A = coo.make_sparse()
+        for prec, name in ((L.SOLVE_FP64, "fp64"), (L.SOLVE_MIXED, "mixed")):
+            for rep in range(2):
+                x = ctx.zeros(sp.num_dofs)
+                ctx.synchronize()
+                t0 = time.perf_counter()
+                st = A.solve_pcg(b, x, precision=prec, rtol=1e-30, max_iterations=iters, raise_on_failure=False)
+                ctx.synchronize()
+                dt = time.perf_counter() - t0
+                out["%s_us_per_iteration_%d" % (name, rep)] = dt * 1e6 / max(st["iterations"], 1)
+    elif f[0] == "hier":
+        n, p, kind, reps = int(f[1]), int(f[2]), f[3], int(f[4])
+        mesh = L.Mesh.tp_triag(ctx, n, n) if kind == "tria" else L.Mesh.tp_quad(ctx, n, n)
+        sp = L.Space.hierarchic(mesh, p)
+        coo = L.COOMatrix(ctx, sp.num_dofs, sp.num_dofs, sp.num_triplets)
+        prov = L.rd_provider(L.coeff(L.CONSTANT, 1.0), L.coeff(L.ZERO))
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            coo.set_zero()
+            L.assemble_matrix_rd(sp, prov, coo)
+        ctx.synchronize()
+        out.update({"triplets": sp.num_triplets, "ms_per_assembly_incl_first": (time.perf_counter() - t0) / reps * 1e3})
+    else:
+        raise SystemExit("unknown case %r" % spec)
+    ctx.close()
+    print(json.dumps(out))
 
 
 def dist_env():
@@ -114,8 +174,9 @@ class ClockSampler:
 # DRAM bytes per cell moved by the element kernels, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the 1024x1024 hybrid O2 case
 # (1,048,980 triangles, 524,086 quadrilaterals; outputs 0.6-0.7 GB >> L2), scaled
-# to a full launch by the cell count.  Command and figures:
-# profiles/element_kernels_hybrid_o2.md.
+# to a full launch by the cell count (`ncu --clock-control none --metrics
+# dram__bytes_read.sum,dram__bytes_write.sum -k regex:RD` on `python bench.py
+# --size 1024` with the side legs switched off).
 DRAM_BYTES_PER_CELL = {"rd_tria_df": (134030080 + 547695616) / 1048980,
                        "rd_quad_df": (120022528 + 620115200) / 524086,
                        "rd_quad_tc": (120872960 + 619725824) / 524086}
@@ -131,6 +192,19 @@ def algorithmic_bytes(space, mesh, kind):
         n, nv, cells = space.n_quad, 4, mesh.num_quads
     per_cell = 16 * n * n + 4 * nv + 16 * nv + 8 + 4 * n
     return per_cell * cells, per_cell
+
+
+def headline_config(size, cells, trias, quads, dofs, ntrip, n_tria, n_quad, world):
+    """The `config` object of the headline workload (both arms print the same)."""
+    per_tria = 16 * n_tria * n_tria + 4 * 3 + 16 * 3 + 8 + 4 * n_tria
+    per_quad = 16 * n_quad * n_quad + 4 * 4 + 16 * 4 + 8 + 4 * n_quad
+    whole = per_tria * trias + per_quad * quads
+    return {"workload": "hybrid %dx%d squares (quad or 2 trias, p=0.5), jitter 0.2h, O2, alpha per-cell "
+                        "LogNormal(0,1), gamma 0, default rules" % (size, size),
+            "cells": int(cells), "trias": int(trias), "quads": int(quads), "dofs": int(dofs),
+            "triplets_per_step": int(ntrip),
+            "l2": "inputs+outputs %.1f GB per step >> 129 MB L2" % (whole / 1e9),
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 def algorithmic_flops(space, mesh, kind, gamma_nonzero):
@@ -174,9 +248,14 @@ def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
         ntrip = len(A)
     else:
         dt, ntrip = O.assemble_rd_parallel(s, a, g, wl["qr_tria"], wl["qr_quad"], (0, ncell), threads)
+    cells = np.asarray(wl["mesh"]["cells"])
+    quads = int((cells[:, 3] >= 0).sum())
+    counts = {"cells": m.num_cells, "trias": m.num_cells - quads, "quads": quads, "dofs": s.num_dofs,
+              "ntrip": int((s.n_tria ** 2) * (m.num_cells - quads) + (s.n_quad ** 2) * quads),
+              "n_tria": s.n_tria, "n_quad": s.n_quad}
     return {"value": ntrip / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "first %d of %d cells (%d triplets) of the same workload; oracle mesh+dof setup %.1f s "
-                      "not timed" % (ncell, m.num_cells, ntrip, setup)}
+                      "not timed" % (ncell, m.num_cells, ntrip, setup), "_counts": counts}
 
 
 RTOL_LADDER = (1e-6, 1e-7, 1e-8, 1e-9, 1e-10)
@@ -685,6 +764,89 @@ def gradient_cpu_check(L, W, ctx, n):
             "loss_rel_diff": abs(Jg - J) / J}
 
 
+def _r(v, digits=4):
+    """Round to `digits` significant digits (None and non-numbers pass)."""
+    if isinstance(v, bool) or not isinstance(v, (int, float)) or v == 0 or v != v:
+        return v
+    return float("%.*g" % (digits, v))
+
+
+def _get(d, *path):
+    for k in path:
+        if not isinstance(d, dict) or k not in d:
+            return None
+        d = d[k]
+    return d
+
+
+def summarize(line):
+    """The figures of every leg in a few short keys (the line's last key, so
+    that a record keeping only the end of the output still holds them).
+    G = 1e9, M = 1e6."""
+    s = {"c2_Gtrip_s": _r(line["value"] / 1e9), "c2_ms": _r(line["ms_per_step"]),
+         "c2_e2e_Gtrip_s": _r(_get(line, "e2e", "value") and line["e2e"]["value"] / 1e9),
+         "tc_quad_hbm_frac": _r(line["roofline"]["frac"], 3), "tria_ms": _r(_get(line, "kernels_ms", "rd_tria_df")),
+         "tc_quad_ms": _r(_get(line, "kernels_ms", "rd_quad_tc"))}
+    ho = line.get("high_order") or {}
+    if "triplets_per_s" in ho:
+        s["c3"] = {"Gtrip_s": _r(ho["triplets_per_s"] / 1e9), "ms": _r(ho["ms_per_assembly"]),
+                   "hbm_frac": _r(ho["hbm_frac_of_measured"], 3), "vec_ms": _r(ho["load_vector_ms"])}
+    so = line.get("solve") or {}
+    if "workload" in so:
+        t = {"dofs": so.get("dofs")}
+        for k in ("fp64", "mixed"):
+            e = _get(so, k, "to_1e-8_err")
+            if e:
+                t[k + "_Mdof_s_1e-8err"] = _r(e["dofs_per_s"] / 1e6)
+                t[k + "_s"] = _r(e["seconds"])
+                t[k + "_it"] = e.get("iterations")
+            e = _get(so, k, "rtol_1e-10")
+            if e:
+                t[k + "_rtol1e-10_s"] = _r(e["seconds"])
+                t[k + "_rtol1e-10_err_vs_fp64"] = _r(e.get("rel_err_vs_fp64_floor"), 2)
+        t["mixed_vs_fp64"] = _r(so.get("mixed_vs_fp64_at_1e-8_err"), 3)
+        t["cpu_superlu_Mdof_s"] = _r(_get(so, "cpu_baseline", "value") and so["cpu_baseline"]["value"] / 1e6)
+        t["gpu_err_vs_superlu_256"] = _r(_get(so, "cpu_baseline", "gpu_mixed_rtol_1e-10_rel_err_vs_sparselu"), 2)
+        s["c2_solve"] = t
+    ba = line.get("batch") or {}
+    if "dofs" in ba:
+        t = {}
+        for k in ("mixed", "fp64"):
+            e = _get(ba, k, "to_1e-8_err")
+            if e:
+                t[k + "_Mdof_s"] = _r(e["dofs_per_s"] / 1e6)
+        t["plain_fp64_Mdof_s"] = _r(_get(ba, "plain_fp64", "dofs_per_s") and ba["plain_fp64"]["dofs_per_s"] / 1e6)
+        t["mixed_vs_fp64"] = _r(ba.get("mixed_vs_fp64_at_1e-8_err"), 3)
+        t["best_vs_plain"] = _r(ba.get("best_batched_vs_plain_fp64_at_1e-8_err"), 3)
+        t["max_err_vs_superlu"] = _r(_get(ba, "superlu_subset", "max_rel_err"), 2)
+        s["c4_batch"] = t
+    gr = line.get("gradient") or {}
+    if "store" in gr:
+        s["c5_grad"] = {"evals_s_store": _r(gr["store"]["grad_evals_per_s"]),
+                        "evals_s_recompute": _r(gr["recompute"]["grad_evals_per_s"]),
+                        "kernel_GBs": _r(_get(gr, "grad_kernel", "achieved_gbs")),
+                        "err_vs_cpu": _r(_get(gr, "cpu_baseline", "gpu_rel_err_vs_cpu_fp64"), 2)}
+    hi = line.get("hier") or {}
+    h = {k: _r(v["triplets_per_s"] / 1e9) for k, v in hi.items() if isinstance(v, dict) and "triplets_per_s" in v}
+    if h:
+        s["hier_Gtrip_s"] = h
+    po = line.get("post") or {}
+    if "l2_error" in po:
+        s["post_ms"] = {"proj": _r(po["nodal_projection"]["ms"]), "l2": _r(po["l2_error"]["ms"]),
+                        "h1": _r(po["h1_error"]["ms"])}
+    ed = line.get("edges") or {}
+    if "all_edges" in ed:
+        s["edge_mass_Gtrip_s"] = _r(ed["all_edges"]["triplets_per_s"] / 1e9)
+    gm = line.get("gmsh") or {}
+    if "v41_binary" in gm:
+        s["gmsh_MB_s"] = {k: _r(gm[k]["parse_mb_per_s"]) for k in ("v41_binary", "v41_ascii", "v22_ascii") if k in gm}
+    errs = [k for k in ("high_order", "solve", "batch", "gradient", "hier", "post", "edges", "gmsh")
+            if isinstance(line.get(k), dict) and "error" in line[k]]
+    if errs:
+        s["leg_errors"] = errs
+    return s
+
+
 def run_ours(args):
     rank, world, local = dist_env()
     import lehrfempp_gb300 as L
@@ -818,18 +980,15 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = run_cpu_baseline(wl, max_seconds=15.0, threads=1)
+        cpu.pop("_counts", None)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": "hybrid %dx%d squares (quad or 2 trias, p=0.5), jitter 0.2h, O2, alpha "
-                                   "per-cell LogNormal(0,1), gamma 0, default rules" % (args.size, args.size),
-                       "cells": mesh.num_cells, "trias": mesh.num_trias, "quads": mesh.num_quads,
-                       "dofs": space.num_dofs, "triplets_per_step": ntrip,
-                       "l2": "inputs+outputs %.1f GB per step >> 129 MB L2" % (whole_bytes / 1e9),
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": headline_config(args.size, mesh.num_cells, mesh.num_trias, mesh.num_quads, space.num_dofs,
+                                      ntrip, space.n_tria, space.n_quad, world),
             "clocks": clk, "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak,
@@ -855,6 +1014,7 @@ def run_ours(args):
             "batch": batch,
             "gradient": gradient,
         }
+        line["summary"] = summarize(line)
         print(json.dumps(line))
     ctx.close()
     reps.close()
@@ -874,21 +1034,25 @@ def run_reference(args):
         if it >= args.warmup:
             rates.append(info["value"])
     value = statistics.median(rates)
+    c = info.pop("_counts")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded generator, no dataset)", "impl": "reference",
-            "config": {"workload": "hybrid %dx%d squares, O2, alpha per-cell LogNormal(0,1), gamma 0" %
-                                   (args.size, args.size)},
+            "config": headline_config(args.size, c["cells"], c["trias"], c["quads"], c["dofs"], c["ntrip"],
+                                      c["n_tria"], c["n_quad"], world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": info["sample"] + "; reference not buildable here (needs Eigen/Boost), "
-                                                        "C++ restatement in oracle/ timed instead"},
+                             "sample": info["sample"] + "; LehrFEM++ itself is not buildable here (needs "
+                                       "Eigen/Boost/Hunter): the oracle's C++ restatement runs instead, on all "
+                                       "host threads (the reference is serial)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args.case)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -70,6 +70,18 @@ lfg_status lfg_ctx_synchronize(lfg_ctx* ctx);
 /* Kernel launches issued by the library on this context since creation. */
 lfg_status lfg_ctx_launch_count(const lfg_ctx* ctx, int64_t* launches);
 
+/* make_QuadRule (lib/lf/quad/make_quad_rule.cc:21-157): the quadrature rule
+ * of `degree` on the reference triangle (is_quad = 0: the tables of
+ * quad/quad_rules_tria.cc for degrees 1..50, degree 3 served by the degree-4
+ * table, the conical Gauss rule for degree 0 and above 50) or on the
+ * reference square (is_quad = 1: tensor Gauss-Legendre, degree/2 + 1 points
+ * per direction, x slow).  These are the rules every provider of this
+ * library integrates with.  Host query, no device or context needed.  With
+ * x, y and w null only *n is written; otherwise each must hold *n entries
+ * (call once with nulls to get the count).  LFG_INVALID_ARG for a degree
+ * outside [0, 100] or a null n. */
+lfg_status lfg_quad_rule(int32_t is_quad, int32_t degree, double* x, double* y, double* w, int32_t* n);
+
 /* Device memory and copies on the context's stream (no torch needed); no
  * counterpart in the reference, whose data lives in host memory. */
 lfg_status lfg_malloc(lfg_ctx* ctx, size_t bytes, void** dev);
@@ -379,14 +391,17 @@ lfg_status lfg_solve_pcg(lfg_csr* csr, const double* b_dev, double* x_dev,
  * memory (an application that owns a fixed GPU memory budget through its own
  * allocator, or a service that must not grow the CUDA memory pool or risk an
  * allocation's implicit synchronisation inside its time loop).  This entry
- * point has no counterpart in the reference.  It runs the FP64 PCG of
- * lfg_solve_pcg (same iterates) with all work vectors in one fixed,
- * file-scope device array of 40 MiB + 32 KiB that every GPU loading the
- * library holds until exit, and calls no allocator.  Limits: FP64 only
- * (LFG_UNSUPPORTED otherwise) and at most 1,048,576 rows (LFG_CAPACITY
- * otherwise).  All calls share the array: calls that overlap on the GPU race.
- * The first call on a device resolves the array's address; make it before any
- * stream capture. */
+ * point has no counterpart in the reference.  It runs the same algorithm and
+ * convergence test as the FP64 PCG of lfg_solve_pcg (restarts from the true
+ * residual included), with all work vectors in one fixed, file-scope device
+ * array of 40 MiB + 48 KiB that every GPU loading the library holds until
+ * exit, and calls no allocator.  Its SpMV reads the CSR arrays directly
+ * instead of lfg_solve_pcg's padded copy, so rounding and iteration counts
+ * can differ slightly between the two.  Limits: FP64 only (LFG_UNSUPPORTED
+ * otherwise) and at most 1,048,576 rows (LFG_CAPACITY otherwise).  All calls
+ * share the array and it keeps the last call's contents: calls that overlap
+ * on the GPU race.  The first call on a device resolves the array's address;
+ * make it before any stream capture. */
 lfg_status lfg_solve_pcg_noalloc(lfg_csr* csr, const double* b_dev, double* x_dev,
                                  const lfg_solve_opts* opts, lfg_solve_stats* stats);
 

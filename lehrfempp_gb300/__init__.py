@@ -443,6 +443,19 @@ class COOMatrix:
         n = len(self) if count is None else count
         self.ctx.check(lib().lfg_coo_download(self.h, pinned.ptr, n))
 
+    def triplets_range(self, lo, hi):
+        """Triplets [lo, hi) of the matrix (host copy of one slice)."""
+        n = len(self)
+        if not 0 <= lo <= hi <= n:
+            raise ValueError("triplet range [%d, %d) outside [0, %d)" % (lo, hi, n))
+        out = np.zeros(hi - lo, TRIPLET_DTYPE)
+        if hi > lo:
+            d = C.c_void_p()
+            self.ctx.check(lib().lfg_coo_triplets(self.h, C.byref(d)))
+            self.ctx.check(lib().lfg_memcpy_d2h(self.ctx.h, out.ctypes.data, C.c_void_p(d.value + 16 * lo),
+                                                16 * (hi - lo)))
+        return out
+
     def append(self, rows, cols, vals):
         t = np.zeros(len(vals), TRIPLET_DTYPE)
         t["row"], t["col"], t["value"] = rows, cols, vals
@@ -565,6 +578,22 @@ class Batch:
                    "converged": bool(p.converged)} for p in per]
         return {"iterations": st.iterations, "refinements": st.refinements, "rel_residual": st.rel_residual,
                 "converged": bool(st.converged), "blocks": blocks}
+
+
+def quad_rule(is_quad, degree):
+    """make_QuadRule (lib/lf/quad/make_quad_rule.cc:21-157) as the library
+    builds it: (x, y, w) arrays of the rule of `degree` on the reference
+    triangle or square.  Host-only; no device needed."""
+    n = C.c_int32(0)
+    rc = lib().lfg_quad_rule(int(is_quad), int(degree), None, None, None, C.byref(n))
+    if rc != OK:
+        raise LfgError(rc, "lfg_quad_rule(%d, %d) failed" % (int(is_quad), int(degree)))
+    x, y, w = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+    rc = lib().lfg_quad_rule(int(is_quad), int(degree), _p(x, C.c_double), _p(y, C.c_double), _p(w, C.c_double),
+                             C.byref(n))
+    if rc != OK:
+        raise LfgError(rc, "lfg_quad_rule(%d, %d) failed" % (int(is_quad), int(degree)))
+    return x, y, w
 
 
 def rd_provider(alpha, gamma, qr_degree_tria=0, qr_degree_quad=0):

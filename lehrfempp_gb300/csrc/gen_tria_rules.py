@@ -5,8 +5,9 @@ The reference hard-codes its triangle rules as generated constants in
 degree d).  Element matrices only agree to 1e-12 with the reference when both
 integrate with *the same* points and weights (a different exact rule changes
 the result by the quadrature error for non-polynomial coefficients), so the
-numbers have to be alike.  This script reads the degrees 1..8 out of the
-reference source and writes them in this project's own compact layout:
+numbers have to be alike.  This script reads every tabulated degree (1..50;
+degree 3 is served by the degree-4 rule) out of the reference source and
+writes them in this project's own compact layout:
 
     {degree, npoints, offset} index + flat {x, y, w} rows
 
@@ -14,13 +15,13 @@ into ``tria_rules.inc`` next to this file (library) and ``oracle/tria_rules.inc`
 (oracle).  Both generated files are committed; the script is only re-run when
 the table has to be regenerated (it needs the reference checkout).
 
-usage: python lehrfempp_gb300/csrc/gen_tria_rules.py /root/reference
+usage: python lehrfempp_gb300/csrc/gen_tria_rules.py <path of the LehrFEM++ checkout>
 """
 import os
 import re
 import sys
 
-MAX_DEGREE = 8
+MAX_DEGREE = 50
 
 
 def parse(src_text):
@@ -46,7 +47,7 @@ def emit(rules, path, guard_comment):
     lines = [
         "// Generated by lehrfempp_gb300/csrc/gen_tria_rules.py -- do not edit.",
         "// " + guard_comment,
-        "// Triangle quadrature rules of degree 1..8 on the reference triangle",
+        "// Triangle quadrature rules of degree 1..%d on the reference triangle" % MAX_DEGREE,
         "// {(0,0),(1,0),(0,1)}; weights sum to 1/2.  Degree 3 requests use the",
         "// degree-4 rule (reference: lib/lf/quad/make_quad_rule.cc:44-46).",
         "// Layout: kTriaRuleIndex[d] = {npoints, first row}; kTriaRuleRows = {x, y, w}.",
@@ -72,11 +73,18 @@ def emit(rules, path, guard_comment):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    ref = sys.argv[1]
     src = os.path.join(ref, "lib/lf/quad/quad_rules_tria.cc")
     with open(src) as f:
         rules = parse(f.read())
     rules = {d: r for d, r in rules.items() if d <= MAX_DEGREE}
+    missing = [d for d in range(1, MAX_DEGREE + 1) if d != 3 and d not in rules]
+    if missing:
+        sys.exit("degrees not found in %s: %s" % (src, missing))
+    for d, rows in rules.items():  # every point and weight parsed
+        assert all(len(r) == 3 and all(r) for r in rows), d
     here = os.path.dirname(os.path.abspath(__file__))
     repo = os.path.dirname(os.path.dirname(here))
     emit(rules, os.path.join(here, "tria_rules.inc"), "library copy")

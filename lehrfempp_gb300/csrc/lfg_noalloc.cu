@@ -14,18 +14,25 @@
 // Limits and sharing rules (also stated in include/lfg.h):
 //   - at most kNoAllocMaxRows = 1,048,576 matrix rows; larger systems are
 //     rejected with LFG_CAPACITY before any work is done;
-//   - the scratch array (40 MiB + 32 KiB) is held by every GPU that loads the
+//   - the scratch array (40 MiB + 48 KiB) is held by every GPU that loads the
 //     library until the process exits;
 //   - all calls share the one array and it keeps the previous call's
-//     contents; every vector is written before it is read and the zero vector
-//     is cleared on each call.  Calls that overlap on the GPU (two contexts or
-//     streams on the same device at the same time) race on the array;
+//     contents; every vector is written before it is read, and the zero
+//     vector and the scalar block (reduction counter included) are cleared on
+//     each call.  Calls that overlap on the GPU (two contexts or streams on
+//     the same device at the same time) race on the array;
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current) and caches it; make that
 //     first call before any stream capture.
-// The arithmetic, grid shape, reduction order and convergence-check cadence
-// are those of lfg_solve_pcg in FP64 mode, so both give the same iterates.
+// The algorithm and the convergence test are those of lfg_solve_pcg in FP64
+// mode (same three-kernel iteration, same check cadence, same restart from
+// the true residual when the recursive one drifts).  The SpMV differs: this
+// path reads the CSR arrays directly (eight lanes per row) because the SELL-32
+// copy that lfg_solve_pcg builds would need an allocation, so the rounding of
+// the two solvers differs and their iteration counts can differ slightly.
+#include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <mutex>
 
@@ -36,11 +43,27 @@ namespace lfg {
 namespace {
 
 constexpr int64_t kNoAllocMaxRows = int64_t(1) << 20;
-constexpr int kNoAllocMaxBlocks = 1024;
+constexpr int kNoAllocMaxBlocks = 2048;  // grids are clamped to this; every row loop is grid-stride
 constexpr int kBlock = 256;
 constexpr int kLanes = 8;
-// r, z, p, q, dinv (one row each) + pq, rz[0], rz[1], rr block partials
-constexpr size_t kScratchDoubles = 5 * static_cast<size_t>(kNoAllocMaxRows) + 4 * kNoAllocMaxBlocks;
+
+// Scalars of one run, on the device (same roles as lfg_solve_pcg's): rz[cur]
+// is <r, z> of the current residual, the update kernel writes rz[cur ^ 1].
+struct NaScalars {
+  double rz[2];
+  double alpha, beta, rr, pq, total;
+  unsigned int counter;
+  unsigned int pad;
+};
+constexpr size_t kScalarDoubles = (sizeof(NaScalars) + sizeof(double) - 1) / sizeof(double);
+
+// Layout (in doubles): r, z, p, q, dinv (one row each), then the block
+// partials of the iteration kernels (two per block), of the residual kernel
+// (one per block), then the scalar block.
+constexpr size_t kOffPart = 5 * static_cast<size_t>(kNoAllocMaxRows);
+constexpr size_t kOffRes = kOffPart + 2 * kNoAllocMaxBlocks;
+constexpr size_t kOffScal = kOffRes + kNoAllocMaxBlocks;
+constexpr size_t kScratchDoubles = kOffScal + kScalarDoubles;
 
 static __device__ __align__(256) double g_pcg_scratch[kScratchDoubles];
 
@@ -75,6 +98,7 @@ __device__ __forceinline__ double RowDot64(const int64_t* __restrict__ rp, const
   return s;
 }
 
+// Warp-uniform row loop: each warp owns 32 / kLanes consecutive rows per trip.
 #define NOALLOC_ROW_LOOP(r)                                                                      \
   const int sub = threadIdx.x % kLanes;                                                          \
   const int64_t warp_id = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;    \
@@ -83,6 +107,7 @@ __device__ __forceinline__ double RowDot64(const int64_t* __restrict__ rp, const
   for (int64_t wb = warp_id * (32 / kLanes); wb < rows; wb += nwarps * (32 / kLanes))            \
     for (int64_t r = wb + grp, once = 0; once < 1; ++once)
 
+// Block sum (warp shuffles, then warps in order); result in thread 0.
 __device__ double BlockSum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
@@ -94,17 +119,23 @@ __device__ double BlockSum(double v, double* red) {
   return s;
 }
 
-__device__ double SumPartials(const double* __restrict__ part, int n, double* red) {
+// Publishes this block's partials (already written by thread 0) and tells
+// whether this block finished last.  No block waits for another.
+__device__ __forceinline__ bool FinishedLast(unsigned int* counter) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
+// Sum of part[j * stride + off], j < n, in a fixed order; last block only.
+__device__ double SumParts(const double* part, int n, int stride, int off, double* red) {
   double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < (blockDim.x >> 5); ++w) s += red[w];
-  __syncthreads();
-  return s;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) v += __ldcg(part + static_cast<int64_t>(j) * stride + off);
+  return BlockSum(v, red);
 }
 
 __global__ void NaDiagKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
@@ -119,12 +150,14 @@ __global__ void NaDiagKernel(int64_t rows, const int64_t* __restrict__ rp, const
   }
 }
 
+// r = b - A x with <r, r>: block partials, then the last block writes the
+// sum to sc->total.
 __global__ void __launch_bounds__(kBlock) NaResidualKernel(int64_t rows, const int64_t* __restrict__ rp,
                                                            const int32_t* __restrict__ col,
                                                            const double* __restrict__ val,
                                                            const double* __restrict__ x,
                                                            const double* __restrict__ b, double* __restrict__ res,
-                                                           double* __restrict__ part) {
+                                                           double* __restrict__ part, NaScalars* __restrict__ sc) {
   __shared__ double red[32];
   double acc = 0.0;
   NOALLOC_ROW_LOOP(i) {
@@ -135,20 +168,22 @@ __global__ void __launch_bounds__(kBlock) NaResidualKernel(int64_t rows, const i
       acc = fma(ri, ri, acc);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < (blockDim.x >> 5); ++w) s += red[w];
-    part[blockIdx.x] = s;
+  const double tot = BlockSum(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+  if (FinishedLast(&sc->counter)) {
+    const double s = SumParts(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      sc->total = s;
+      sc->counter = 0;
+    }
   }
 }
 
+// z = D^-1 r, p = z, rz[0] = <r, z>, rr = <r, r>, beta = 0.
 __global__ void __launch_bounds__(kBlock) NaStartKernel(int64_t rows, const double* __restrict__ dinv,
                                                         const double* __restrict__ r, double* __restrict__ z,
-                                                        double* __restrict__ p, double* __restrict__ rz_part,
-                                                        double* __restrict__ rr_part) {
+                                                        double* __restrict__ p, double* __restrict__ part,
+                                                        NaScalars* __restrict__ sc) {
   __shared__ double red[32];
   double arz = 0.0, arr = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
@@ -163,16 +198,40 @@ __global__ void __launch_bounds__(kBlock) NaStartKernel(int64_t rows, const doub
   const double s1 = BlockSum(arz, red);
   const double s2 = BlockSum(arr, red);
   if (threadIdx.x == 0) {
-    rz_part[blockIdx.x] = s1;
-    rr_part[blockIdx.x] = s2;
+    part[2 * blockIdx.x] = s1;
+    part[2 * blockIdx.x + 1] = s2;
+  }
+  if (FinishedLast(&sc->counter)) {
+    const double rz = SumParts(part, gridDim.x, 2, 0, red);
+    const double rr = SumParts(part, gridDim.x, 2, 1, red);
+    if (threadIdx.x == 0) {
+      sc->rz[0] = rz;
+      sc->rz[1] = 0.0;
+      sc->alpha = 0.0;
+      sc->beta = 0.0;
+      sc->rr = rr;
+      sc->counter = 0;
+    }
   }
 }
 
+// p = z + beta p.
+__global__ void __launch_bounds__(kBlock) NaDirectionKernel(int64_t rows, const double* __restrict__ z,
+                                                            double* __restrict__ p,
+                                                            const NaScalars* __restrict__ sc) {
+  const double beta = sc->beta;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+
+// q = A p and alpha = rz[cur] / <p, q>.
 __global__ void __launch_bounds__(kBlock) NaSpmvDotKernel(int64_t rows, const int64_t* __restrict__ rp,
                                                           const int32_t* __restrict__ col,
                                                           const double* __restrict__ val,
                                                           const double* __restrict__ p, double* __restrict__ q,
-                                                          double* __restrict__ part) {
+                                                          int cur, double* __restrict__ part,
+                                                          NaScalars* __restrict__ sc) {
   __shared__ double red[32];
   double acc = 0.0;
   NOALLOC_ROW_LOOP(i) {
@@ -184,19 +243,25 @@ __global__ void __launch_bounds__(kBlock) NaSpmvDotKernel(int64_t rows, const in
   }
   const double tot = BlockSum(acc, red);
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
+  if (FinishedLast(&sc->counter)) {
+    const double pq = SumParts(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      sc->pq = pq;
+      sc->alpha = pq != 0.0 ? sc->rz[cur] / pq : 0.0;
+      sc->counter = 0;
+    }
+  }
 }
 
-__global__ void __launch_bounds__(kBlock) NaUpdateKernel(int64_t rows, const double* __restrict__ pq_part,
-                                                         const double* __restrict__ rz_old_part, int nparts,
-                                                         const double* __restrict__ dinv,
+// x += alpha p; r -= alpha q; z = D^-1 r; rz[cur ^ 1] = <r, z>, beta, and
+// rr = <r, r> on the last iteration of a check period (with_rr).
+__global__ void __launch_bounds__(kBlock) NaUpdateKernel(int64_t rows, const double* __restrict__ dinv,
                                                          const double* __restrict__ p, const double* __restrict__ q,
                                                          double* __restrict__ x, double* __restrict__ r,
-                                                         double* __restrict__ z, double* __restrict__ rz_part,
-                                                         double* __restrict__ rr_part) {
+                                                         double* __restrict__ z, int cur, bool with_rr,
+                                                         double* __restrict__ part, NaScalars* __restrict__ sc) {
   __shared__ double red[32];
-  const double pq = SumPartials(pq_part, nparts, red);
-  const double rz = SumPartials(rz_old_part, nparts, red);
-  const double alpha = pq != 0.0 ? rz / pq : 0.0;
+  const double alpha = sc->alpha;
   double arz = 0.0, arr = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -206,36 +271,31 @@ __global__ void __launch_bounds__(kBlock) NaUpdateKernel(int64_t rows, const dou
     const double zi = dinv[i] * ri;
     z[i] = zi;
     arz = fma(ri, zi, arz);
-    arr = fma(ri, ri, arr);
+    if (with_rr) arr = fma(ri, ri, arr);
   }
   const double s1 = BlockSum(arz, red);
-  const double s2 = BlockSum(arr, red);
+  const double s2 = with_rr ? BlockSum(arr, red) : 0.0;
   if (threadIdx.x == 0) {
-    rz_part[blockIdx.x] = s1;
-    rr_part[blockIdx.x] = s2;
+    part[2 * blockIdx.x] = s1;
+    part[2 * blockIdx.x + 1] = s2;
+  }
+  if (FinishedLast(&sc->counter)) {
+    const double rz = SumParts(part, gridDim.x, 2, 0, red);
+    const double rr = with_rr ? SumParts(part, gridDim.x, 2, 1, red) : 0.0;
+    if (threadIdx.x == 0) {
+      const double rz_old = sc->rz[cur];
+      sc->rz[cur ^ 1] = rz;
+      sc->beta = rz_old != 0.0 ? rz / rz_old : 0.0;
+      if (with_rr) sc->rr = rr;
+      sc->counter = 0;
+    }
   }
 }
 
-__global__ void __launch_bounds__(kBlock) NaDirectionKernel(int64_t rows, const double* __restrict__ rz_new_part,
-                                                            const double* __restrict__ rz_old_part, int nparts,
-                                                            const double* __restrict__ z, double* __restrict__ p) {
-  __shared__ double red[32];
-  const double rn = SumPartials(rz_new_part, nparts, red);
-  const double ro = SumPartials(rz_old_part, nparts, red);
-  const double beta = ro != 0.0 ? rn / ro : 0.0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    p[i] = fma(beta, p[i], z[i]);
-}
-
-// Sums block partials in index order on one thread (same order as the host
-// sum of lfg_solve_pcg) into out[0].
-__global__ void NaFinalSumKernel(const double* __restrict__ part, int n, double* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += part[i];
-    out[0] = s;
-  }
+double ReadScalar(lfg_ctx* ctx, const NaScalars* sc, size_t offset) {
+  double v = 0.0;
+  D2HSync(ctx, &v, reinterpret_cast<const char*>(sc) + offset, sizeof(double));
+  return v;
 }
 
 }  // namespace
@@ -265,24 +325,24 @@ lfg_status lfg_solve_pcg_noalloc(lfg_csr* A, const double* b, double* x, const l
   double* p = z + kNoAllocMaxRows;
   double* q = p + kNoAllocMaxRows;
   double* dinv = q + kNoAllocMaxRows;
-  double* pq = dinv + kNoAllocMaxRows;
-  double* rz[2] = {pq + kNoAllocMaxBlocks, pq + 2 * kNoAllocMaxBlocks};
-  double* rr = pq + 3 * kNoAllocMaxBlocks;
-  const int nb = std::max(1, std::min<int>(ctx->num_sms * 8, static_cast<int>((n + kBlock - 1) / kBlock)));
-  if (nb > kNoAllocMaxBlocks - 1) Fail(LFG_UNSUPPORTED, "too many SMs for the scratch partial arrays");
+  double* part = base + kOffPart;
+  double* res = base + kOffRes;
+  NaScalars* sc = reinterpret_cast<NaScalars*>(base + kOffScal);
+  const int nb = static_cast<int>(std::clamp<int64_t>(
+      std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (n + kBlock - 1) / kBlock), 1, kNoAllocMaxBlocks));
   const int64_t* rp = A->rowptr.as<int64_t>();
   const int32_t* col = A->col.as<int32_t>();
   const double* val = A->val.as<double>();
   const int check = opts->check_every > 0 ? opts->check_every : 32;
   const int max_it = opts->max_iterations > 0 ? opts->max_iterations : 100000;
   const double rtol = opts->rtol > 0 ? opts->rtol : 1e-10;
-  double* total_dev = rr + kNoAllocMaxBlocks - 1;  // last slot of the rr partial array (never a partial: nb < max)
-  auto sum_partials = [&](const double* part) {
-    NaFinalSumKernel<<<1, 32, 0, s>>>(part, nb, total_dev);
+  // The array keeps the last call's contents: start from a cleared scalar
+  // block (its reduction counter must be zero).
+  LFG_CUDA(cudaMemsetAsync(sc, 0, sizeof(NaScalars), s));
+  auto residual = [&]() {  // r = b - A x, returns <r, r>
+    NaResidualKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, x, b, r, res, sc);
     LFG_LAUNCHED(ctx);
-    double v = 0.0;
-    D2HSync(ctx, &v, total_dev, sizeof(double));
-    return v;
+    return ReadScalar(ctx, sc, offsetof(NaScalars, total));
   };
   // Jacobi diagonal
   ReadAndClearStatus(ctx);
@@ -292,43 +352,48 @@ lfg_status lfg_solve_pcg_noalloc(lfg_csr* A, const double* b, double* x, const l
     Fail(LFG_INVALID_ARG, "Jacobi preconditioner: non-positive diagonal in row " + std::to_string(code - 1));
   // ||b|| from r = b - A*0 (q is cleared to serve as the zero vector)
   LFG_CUDA(cudaMemsetAsync(q, 0, n * sizeof(double), s));
-  NaResidualKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, q, b, r, rr);
+  NaResidualKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, q, b, r, res, sc);
   LFG_LAUNCHED(ctx);
-  const double bnorm = std::sqrt(sum_partials(rr));
+  const double bnorm = std::sqrt(ReadScalar(ctx, sc, offsetof(NaScalars, total)));
   lfg_solve_stats st{};
-  st.refinements = 1;
   if (bnorm == 0.0) {
     LFG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
     st.converged = 1;
   } else {
     const double target = (rtol * bnorm) * (rtol * bnorm);
-    NaResidualKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, x, b, r, rr);
-    LFG_LAUNCHED(ctx);
-    NaStartKernel<<<nb, kBlock, 0, s>>>(n, dinv, r, z, p, rz[0], rr);
-    LFG_LAUNCHED(ctx);
-    double rrv = sum_partials(rr);
-    int it = 0;
     const int body = std::max(2, check + (check & 1));
-    while (rrv > target && it < max_it) {
-      for (int k = 0; k < body; ++k) {
-        double* rz_old = rz[k & 1];
-        double* rz_new = rz[(k + 1) & 1];
-        NaSpmvDotKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, p, q, pq);
-        NaUpdateKernel<<<nb, kBlock, 0, s>>>(n, pq, rz_old, nb, dinv, p, q, x, r, z, rz_new, rr);
-        NaDirectionKernel<<<nb, kBlock, 0, s>>>(n, rz_new, rz_old, nb, z, p);
-        CountLaunch(ctx, 3);
+    double rr = residual();
+    // Same restart rule as lfg_solve_pcg: when the recursive residual reports
+    // convergence but the true one does not, restart from the true residual,
+    // kept while each restart gains at least a factor 2 in the residual norm.
+    int total = 0, restarts = 0;
+    double rr_prev = rr;
+    while (true) {
+      NaStartKernel<<<nb, kBlock, 0, s>>>(n, dinv, r, z, p, part, sc);
+      LFG_LAUNCHED(ctx);
+      double rr_rec = ReadScalar(ctx, sc, offsetof(NaScalars, rr));
+      while (rr_rec > target && total < max_it) {
+        for (int k = 0; k < body; ++k) {
+          const int cur = k & 1;
+          NaDirectionKernel<<<nb, kBlock, 0, s>>>(n, z, p, sc);
+          NaSpmvDotKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, p, q, cur, part, sc);
+          NaUpdateKernel<<<nb, kBlock, 0, s>>>(n, dinv, p, q, x, r, z, cur, k == body - 1, part, sc);
+          CountLaunch(ctx, 3);
+        }
+        LFG_CUDA(cudaGetLastError());
+        total += body;
+        rr_rec = ReadScalar(ctx, sc, offsetof(NaScalars, rr));
+        if (!(rr_rec == rr_rec)) break;  // NaN
       }
-      LFG_CUDA(cudaGetLastError());
-      it += body;
-      rrv = sum_partials(rr);
-      if (!(rrv == rrv)) break;  // NaN
+      ++restarts;
+      rr = residual();
+      if (rr <= target || total >= max_it || restarts >= 16 || !(rr < 0.25 * rr_prev)) break;
+      rr_prev = rr;
     }
-    st.iterations = it;
-    NaResidualKernel<<<nb, kBlock, 0, s>>>(n, rp, col, val, x, b, r, rr);
-    LFG_LAUNCHED(ctx);
-    rrv = sum_partials(rr);
-    st.rel_residual = std::sqrt(rrv) / bnorm;
-    st.converged = st.rel_residual <= rtol * 1.0000001 || rrv <= target;
+    st.iterations = total;
+    st.refinements = restarts;
+    st.rel_residual = std::sqrt(rr) / bnorm;
+    st.converged = st.rel_residual <= rtol * 1.0000001 || rr <= target;
   }
   if (stats) *stats = st;
   if (!st.converged) {

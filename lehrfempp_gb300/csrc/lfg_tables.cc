@@ -4,7 +4,9 @@
 // elements are set-up work in the reference too:
 // uscalfe/precomputed_scalar_reference_finite_element.h:43-184).
 #include <cmath>
+#include <cstring>
 
+#include "../../include/lfg.h"
 #include "lfg_tables.h"
 
 namespace lfg {
@@ -579,3 +581,17 @@ bool SegmentTables(int degree, int rule_degree, std::vector<double>& t, std::vec
 }
 
 }  // namespace lfg
+
+extern "C" lfg_status lfg_quad_rule(int32_t is_quad, int32_t degree, double* x, double* y, double* w, int32_t* n) {
+  if (!n) return LFG_INVALID_ARG;
+  lfg::Rule r;
+  if (!lfg::MakeRule(is_quad != 0, degree, r)) return LFG_INVALID_ARG;
+  if (x || y || w) {
+    if (!x || !y || !w || *n < r.n) return LFG_INVALID_ARG;
+    std::memcpy(x, r.x.data(), r.n * sizeof(double));
+    std::memcpy(y, r.y.data(), r.n * sizeof(double));
+    std::memcpy(w, r.w.data(), r.n * sizeof(double));
+  }
+  *n = r.n;
+  return LFG_OK;
+}

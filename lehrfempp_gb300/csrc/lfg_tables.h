@@ -12,10 +12,10 @@ struct Rule {
   std::vector<double> x, y, w;
 };
 // make_QuadRule (quad/make_quad_rule.cc:21-157): triangles from the
-// reference's tables for degree 1..8 (3 -> 4), otherwise the conical
-// Gauss-Legendre x Gauss-Jacobi(1,0) product rule with degree/2+1 points per
-// direction (the reference's rule above its tables, make_quad_rule.cc:139-152;
-// its tables for degrees 9..50 are not restated); quads tensor
+// reference's tables for degree 1..50 (3 -> 4; quad/quad_rules_tria.cc),
+// otherwise (degree 0 and above 50) the conical Gauss-Legendre x
+// Gauss-Jacobi(1,0) product rule with degree/2+1 points per direction (the
+// reference's rule beyond its tables, make_quad_rule.cc:139-152); quads tensor
 // Gauss-Legendre with degree/2+1 points per direction, x slow / y fast.
 // False for a degree outside [0, kMaxRuleDegree].
 constexpr int kMaxRuleDegree = 100;

@@ -45,7 +45,8 @@ struct QuadRule {
 };
 // lib/lf/quad/gauss_quadrature.cc:16-69 (points on [0,1], weights sum to 1).
 void GaussLegendre(int n, std::vector<double>& pts, std::vector<double>& wts);
-// lib/lf/quad/make_quad_rule.cc:21-157 for kTria (hard-coded tables deg<=8)
+// lib/lf/quad/make_quad_rule.cc:21-157 for kTria (the tables of
+// quad/quad_rules_tria.cc for degrees 1..50, 3 -> 4; conical rule otherwise)
 // and kQuad (tensor Gauss-Legendre, n = deg/2+1).
 QuadRule MakeQuadRule(bool is_quad, int degree);
 

@@ -130,8 +130,7 @@ QuadRule MakeQuadRule(bool is_quad, int degree) {
     // make_quad_rule.cc:139-152: the collapsed (conical) Gauss rule with
     // n = degree/2 + 1 Gauss-Legendre points u_a (slow) and Gauss-Jacobi(1,0)
     // points (fast) mapped to [0,1]: x = u_a (1 - s_b), y = s_b,
-    // w = W_a w_b / 4.  (The reference's tables for degrees 9..50 are not
-    // restated; the oracle uses this rule for every untabulated degree.)
+    // w = W_a w_b / 4, for degree 0 and degrees above the tables (50).
     if (degree < 0) throw Error("MakeQuadRule: negative degree");
     const int n = degree / 2 + 1;
     std::vector<double> u, W, t, w;

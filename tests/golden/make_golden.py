@@ -13,12 +13,17 @@ reference checkout.  Sources:
   lib/lf/mesh/test_utils/test_meshes.cc    the nodes and triangles of test mesh 3
   lib/lf/io/test/msh_files/*.msh           copied byte for byte into msh/ (the
                                            reader's input fixtures)
+  lib/lf/quad/quad_rules_tria.cc           per degree 1..50: point count, first
+                                           point and weight, SHA-256 of all
+                                           (x, y, w) as little-endian binary64
 
-usage: python tests/golden/make_golden.py /root/reference
+usage: python tests/golden/make_golden.py <path of the LehrFEM++ checkout>
 """
+import hashlib
 import json
 import os
 import re
+import struct
 import sys
 
 
@@ -32,8 +37,30 @@ def _matrix_after(text, marker, n):
     return [vals[r * n:(r + 1) * n] for r in range(n)]
 
 
+def tria_rule_digests(text):
+    """Per tabulated degree of quad_rules_tria.cc: the number of points, the
+    first point and weight as written, and a SHA-256 of every (x, y, w) of the
+    rule in point order, each parsed as the nearest binary64 (as a C++
+    compiler does) and packed little endian."""
+    out = {}
+    blocks = re.split(r"HardcodedQuadRule<base::RefEl::kTria\(\),\s*(\d+)>\(\)\s*\{", text)
+    for k in range(1, len(blocks), 2):
+        deg = int(blocks[k])
+        body = blocks[k + 1].split("return QuadRule")[0]
+        pts = {(int(a), int(b)): v for a, b, v in re.findall(r"points\((\d), (\d+)\) = ([-0-9.eE+]+);", body)}
+        wts = {int(a): v for a, v in re.findall(r"weights\((\d+)\) = ([-0-9.eE+]+);", body)}
+        n = len(wts)
+        assert len(pts) == 2 * n, deg
+        packed = b"".join(struct.pack("<3d", float(pts[(0, q)]), float(pts[(1, q)]), float(wts[q])) for q in range(n))
+        out[str(deg)] = {"points": n, "first": [pts[(0, 0)], pts[(1, 0)], wts[0]],
+                         "sha256_xyw_le": hashlib.sha256(packed).hexdigest()}
+    return out
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    ref = sys.argv[1]
     at = open(os.path.join(ref, "lib/lf/assemble/test/assembly_tests.cc")).read()
     ct = open(os.path.join(ref, "lib/lf/assemble/test/coomatrix_tests.cc")).read()
     lt = open(os.path.join(ref, "lib/lf/uscalfe/test/lagr_fe_tests.cc")).read()
@@ -127,6 +154,9 @@ def main():
             with open(os.path.join(src, name), "rb") as fi, open(os.path.join(dst, name), "wb") as fo:
                 fo.write(fi.read())
             copied.append(name)
+    qt = open(os.path.join(ref, "lib/lf/quad/quad_rules_tria.cc")).read()
+    out["tria_rules"] = {"file": "lib/lf/quad/quad_rules_tria.cc (dispatch make_quad_rule.cc:38-137)",
+                         "degrees": tria_rule_digests(qt)}
     out["gmsh_fixtures"] = {"dir": "lib/lf/io/test/msh_files", "files": copied,
                             "tests": "lib/lf/io/test/gmsh_reader_tests.cc"}
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")

@@ -145,6 +145,24 @@ def test_matrix_parity_all_elements(ctx, degree, quad, coef):
     assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
 
 
+@pytest.mark.parametrize("qdeg", [5, 9, 10])
+@pytest.mark.parametrize("degree", [1, 2, 3])
+def test_explicit_high_degree_tria_rules(ctx, degree, qdeg):
+    """Explicit triangle rules (qr_collection, loc_comp_ellbvp.h:237-263) of
+    degree 9 and 10 come from the reference's tables (19 and 25 points) for
+    both the matrix and the load vector, with point-varying coefficients."""
+    xy, cells = W.hybrid_mesh(6, seed=5)
+    wl = {"mesh": {"kind": "factory", "xy": xy, "cells": cells, "edges": None}, "degree": degree,
+          "alpha": ("sincos", 1.0, 0.5, 3.0, 2.0), "gamma": ("poly", W.poly(c=0.5, x1y1=1.0)),
+          "f": ("sinsin", 0.0, 1.0, 2.0, 1.0), "qr_tria": qdeg, "qr_quad": 4}
+    r = Run(ctx, wl)
+    ro, co, vo = r.oracle_matrix().arrays()
+    compare_triplets(r.gpu_matrix().triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
+    b = r.gpu_vector().download()
+    bo = r.oracle_vector()
+    assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
+
+
 @pytest.mark.parametrize("degree", [1, 2, 3])
 def test_fp64_route_for_out_of_range_cells(ctx, degree):
     """Cells whose coefficients fall outside the df32 range (|alpha| > 2^40 or

@@ -148,14 +148,50 @@ def test_volume_row_sums(degree, quad):
     assert abs(f.sum() - 1.5) < 1e-12
 
 
-@pytest.mark.parametrize("degree", range(1, 9))
+@pytest.mark.parametrize("degree", list(range(0, 51)) + [51, 60])
 def test_tria_rule_exactness(degree):
-    """make_quad_rule_tests.cc:107-136: monomials up to the degree exactly."""
+    """make_quad_rule_tests.cc:107-136: monomials up to the degree exactly
+    (the reference's tables up to 50, the conical rule beyond)."""
     x, y, w = O.quad_rule(False, degree)
     for a in range(degree + 1):
         for b in range(degree + 1 - a):
             exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
-            assert abs((w * x ** a * y ** b).sum() - exact) < 1e-14
+            assert abs(math.fsum(w * x ** a * y ** b) - exact) < 2e-15, (a, b)
+
+
+def _rule_digest(x, y, w):
+    import hashlib
+    return hashlib.sha256(np.stack([x, y, w], 1).astype("<f8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("degree", [d for d in range(1, 51) if d != 3])
+def test_tria_rules_equal_reference_tables(goldens, degree):
+    """Every tabulated triangle rule of quad_rules_tria.cc (degrees 1..50),
+    point for point and bit for bit, in the oracle and in the library (host
+    query, no GPU)."""
+    import lehrfempp_gb300 as L
+    ref = goldens["tria_rules"]["degrees"][str(degree)]
+    for name, (x, y, w) in (("oracle", O.quad_rule(False, degree)), ("library", L.quad_rule(False, degree))):
+        assert len(w) == ref["points"], name
+        assert [x[0], y[0], w[0]] == [float(v) for v in ref["first"]], name
+        assert _rule_digest(x, y, w) == ref["sha256_xyw_le"], name
+    # degree 3 is served by the degree-4 table (make_quad_rule.cc:44-46)
+    if degree == 4:
+        assert _rule_digest(*O.quad_rule(False, 3)) == ref["sha256_xyw_le"]
+        assert _rule_digest(*L.quad_rule(False, 3)) == ref["sha256_xyw_le"]
+
+
+@pytest.mark.parametrize("degree", [0, 1, 7, 20, 51, 64, 100])
+def test_library_rules_equal_oracle_rules(degree):
+    """Quadrilateral rules and the conical triangle rule beyond the tables:
+    the library's host rules and the oracle's agree to the last bits."""
+    import lehrfempp_gb300 as L
+    for quad in (False, True):
+        xo, yo, wo = O.quad_rule(quad, degree)
+        xl, yl, wl = L.quad_rule(quad, degree)
+        assert len(wo) == len(wl)
+        for a, b in ((xo, xl), (yo, yl), (wo, wl)):
+            assert np.abs(a - b).max() <= 4e-16 * max(1.0, np.abs(a).max()), (quad, degree)
 
 
 @pytest.mark.parametrize("degree", range(1, 12))

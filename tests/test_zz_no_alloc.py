@@ -7,11 +7,15 @@ synchronisation) inside its time-stepping loop.  For them the library offers
 lfg_solve_pcg_noalloc, which keeps every PCG work vector in one fixed device
 array inside the library and never allocates.
 
-The test solves one Dirichlet problem with the allocating entry point and then
-twice in a row with the non-allocating one (the fixed array keeps the previous
-call's contents, so the second call shows that nothing stale is read); the
-solutions must agree within the solution tolerance of the other solve tests.
-It also checks that a system larger than the array's limit is refused.
+Each case solves one Dirichlet problem with the allocating entry point and
+then twice in a row with the non-allocating one (the fixed array keeps the
+previous call's contents, so the second call shows that nothing stale is
+read); the solutions must agree within the solution tolerance of the other
+solve tests, and the device's free memory must be the same before and after
+the second call.  One case sits at the row limit (1024 x 1024 nodes =
+2^20 rows); a system one row larger is refused.  The two solvers share the
+algorithm but not the SpMV's summation order, so their iteration counts may
+differ slightly.
 This file is collected last on purpose.
 """
 import numpy as np
@@ -23,35 +27,53 @@ SOLUTION_RTOL = 1e-8  # same bound as tests/test_gpu_parity.py::test_solve_parit
 MAX_ROWS = 1 << 20
 
 
-def _system(ctx, L, W):
-    wl = W.config2(24)
+def _system(ctx, L, W, wl):
     keep = []
     mesh = W.build_mesh(ctx, wl["mesh"])
-    space = L.Space.lagrange(mesh, 2)
+    space = L.Space.lagrange(mesh, wl["degree"])
     coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, space.num_triplets + space.num_dofs)
-    L.assemble_matrix_rd(space, L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep)),
-                         coo)
+    L.assemble_matrix_rd(space, L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep),
+                                              wl["qr_tria"], wl["qr_quad"]), coo)
     b = ctx.zeros(space.num_dofs)
-    L.assemble_vector_load(space, L.load_provider(W.to_coeff(ctx, wl["f"], keep)), b)
+    L.assemble_vector_load(space, L.load_provider(W.to_coeff(ctx, wl["f"], keep), wl["qr_tria"], wl["qr_quad"]), b)
     coo.fix_flagged_solution_components(space.boundary_dof_flags(), ctx.zeros(space.num_dofs), b)
     return coo.make_sparse(), b, space.num_dofs
 
 
-def test_noalloc_solve_matches_allocating_solve(ctx):
+def _free_device_bytes(ctx):
+    import torch
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
+@pytest.mark.parametrize("case", ["hybrid24_o2", "tptriag1023_o1_at_limit"])
+def test_noalloc_solve_matches_allocating_solve(ctx, case):
     import lehrfempp_gb300 as L
     from lehrfempp_gb300 import workloads as W
-    A, b, n = _system(ctx, L, W)
+    if case == "hybrid24_o2":
+        wl, rtol = W.config2(24), 1e-12
+    else:
+        wl, rtol = W.config5(1023), 1e-10
+    A, b, n = _system(ctx, L, W, wl)
+    if case.endswith("at_limit"):
+        assert n == MAX_ROWS
     x_ref = ctx.zeros(n)
-    st_ref = A.solve_pcg(b, x_ref, rtol=1e-12)
+    st_ref = A.solve_pcg(b, x_ref, rtol=rtol)
     assert st_ref["converged"]
     xr = x_ref.download()
+    xs = [ctx.zeros(n), ctx.zeros(n)]
+    free = []
     for call in range(2):
-        x = ctx.zeros(n)
-        st = A.solve_pcg(b, x, rtol=1e-12, noalloc=True)
+        free.append(_free_device_bytes(ctx))
+        st = A.solve_pcg(b, xs[call], rtol=rtol, noalloc=True)
         assert st["converged"], (call, st)
-        rel = np.linalg.norm(x.download() - xr) / np.linalg.norm(xr)
+        rel = np.linalg.norm(xs[call].download() - xr) / np.linalg.norm(xr)
         assert rel <= SOLUTION_RTOL, (call, rel)
-        assert st["iterations"] == st_ref["iterations"]
+        assert abs(st["iterations"] - st_ref["iterations"]) <= max(64, st_ref["iterations"] // 20), (st, st_ref)
+    free.append(_free_device_bytes(ctx))
+    # nothing allocated by the second call (the first may load kernels lazily)
+    assert free[2] == free[1], free
 
 
 def test_noalloc_rejects_oversized_system(ctx):
