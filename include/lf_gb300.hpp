@@ -23,6 +23,8 @@
 //   assemble::FixFlaggedSolutionComponents         assemble::FixFlaggedSolutionComponents(flags,
 //     (assemble/fix_dof.h:87)                        values, A, b): the selector is given as two
 //                                                    device arrays (flag, value per dof)
+//   assemble::FixFlaggedSolutionCompAlt (:184),    the same names; FixSolutionComponentsLse takes
+//   assemble::FixSolutionComponentsLse (:251)        fixed_components_t (host (dof, value) pairs)
 //   Eigen::SparseLU / CG on makeSparse()           solve::SolvePCG (Jacobi PCG, FP64 or mixed)
 //   MassEdgeMatrixProvider, ScalarLoadEdgeVectorProvider (loc_comp_ellbvp.h:367-529,
 //     784-921) with AssembleMatrixLocally / AssembleVectorLocally(1, ...)
@@ -453,6 +455,7 @@ class COOMatrix {
     return solve::CSRMatrix(*ctx_, c);
   }
   lfg_coo* get() const { return h_; }
+  const Context& ctx() const { return *ctx_; }
 
  private:
   const Context* ctx_;
@@ -497,6 +500,35 @@ inline void FixFlaggedSolutionComponents(const DeviceVector<uint8_t>& flags, con
                                          COOMatrix& A, DeviceVector<double>& b) {
   const lfg_status st = lfg_fix_flagged_solution_components(A.get(), flags.data(), values.data(), b.data());
   if (st != LFG_OK) throw Error(st, "FixFlaggedSolutionComponents failed");
+}
+
+// FixFlaggedSolutionCompAlt (assemble/fix_dof.h:183-219): only the fixed rows
+// are removed.
+inline void FixFlaggedSolutionCompAlt(const DeviceVector<uint8_t>& flags, const DeviceVector<double>& values,
+                                      COOMatrix& A, DeviceVector<double>& b) {
+  const lfg_status st = lfg_fix_flagged_solution_comp_alt(A.get(), flags.data(), values.data(), b.data());
+  if (st != LFG_OK) throw Error(st, "FixFlaggedSolutionCompAlt failed");
+}
+
+// fixed_components_t / FixSolutionComponentsLse (assemble/fix_dof.h:228-280):
+// (dof, value) pairs; a repeated dof is fixed to the sum of its values.
+template <typename SCALAR>
+using fixed_components_t = std::vector<std::pair<int64_t, SCALAR>>;
+
+inline void FixSolutionComponentsLse(const fixed_components_t<double>& fixed_components, COOMatrix& A,
+                                     DeviceVector<double>& b) {
+  const Context& ctx = A.ctx();
+  std::vector<int64_t> dofs;
+  std::vector<double> vals;
+  for (const auto& dv : fixed_components) {
+    dofs.push_back(dv.first);
+    vals.push_back(dv.second);
+  }
+  DeviceVector<int64_t> d(ctx, dofs);
+  DeviceVector<double> v(ctx, vals);
+  const lfg_status st = lfg_fix_solution_components_lse(A.get(), static_cast<int64_t>(dofs.size()), d.data(),
+                                                        v.data(), b.data());
+  if (st != LFG_OK) throw Error(st, "FixSolutionComponentsLse failed");
 }
 
 }  // namespace assemble

@@ -228,6 +228,15 @@ lfg_status lfg_space_boundary_dof_flags(lfg_space* space, uint8_t* flags_dev);
  *     LFG_FN_TRIG    p0 + (p1 + p2 x + p3 y + p4 x y) sin(pi (p5 x + p6)) sin(pi (p7 y + p8))
  *                    (a cosine is the sine shifted by 1/2 in p6 / p8)
  *   The post-processing functions also use the exact gradient of each family.
+ * Matrix-valued diffusion coefficients (the 2x2 DIFF_COEFF that
+ * ReactionDiffusionElementMatrixProvider accepts, uscalfe/loc_comp_ellbvp.h:
+ * 85-127; row-major a00, a01, a10, a11, not necessarily symmetric) are valid
+ * only as alpha of lfg_assemble_matrix_rd on Lagrangian spaces:
+ *   LFG_COEFF_TENSOR_CONSTANT        p[0..3]
+ *   LFG_COEFF_TENSOR_PER_CELL        data_dev[4 * cell + 0..3]
+ *   LFG_COEFF_TENSOR_BILINEAR        entry e = p[4e] + p[4e+1] x + p[4e+2] y + p[4e+3] x y
+ *                                    at the global point (the reference's
+ *                                    tensor test uses [[1, x], [y, x y]])
  * Arbitrary host lambdas cannot run on the GPU: anything else is LFG_UNSUPPORTED. */
 enum {
   LFG_COEFF_ZERO = 0,
@@ -235,7 +244,10 @@ enum {
   LFG_COEFF_PER_CELL = 2,
   LFG_COEFF_NODAL_O1 = 3,
   LFG_COEFF_ANALYTIC = 4,
-  LFG_COEFF_PER_CELL_EXP = 5  /* exp(data_dev[cell]): a per-cell log-coefficient */
+  LFG_COEFF_PER_CELL_EXP = 5,  /* exp(data_dev[cell]): a per-cell log-coefficient */
+  LFG_COEFF_TENSOR_CONSTANT = 6,
+  LFG_COEFF_TENSOR_PER_CELL = 7,
+  LFG_COEFF_TENSOR_BILINEAR = 8
 };
 enum { LFG_FN_POLY = 1, LFG_FN_SINSIN = 2, LFG_FN_SINCOS = 3, LFG_FN_EXP = 4, LFG_FN_TRIG = 5 };
 
@@ -345,6 +357,13 @@ lfg_status lfg_fix_flagged_solution_components(lfg_coo* coo, const uint8_t* flag
 /* FixFlaggedSolutionCompAlt (fix_dof.h:183-219): only fixed rows are removed. */
 lfg_status lfg_fix_flagged_solution_comp_alt(lfg_coo* coo, const uint8_t* flags_dev,
                                              const double* values_dev, double* b_dev);
+/* FixSolutionComponentsLse (fix_dof.h:250-280) with fixed_components given
+ * as `count` (dof, value) pairs (device arrays, in list order): a dof that
+ * appears several times is fixed to the sum of its values, added in list
+ * order; then FixFlaggedSolutionCompAlt.  LFG_INVALID_ARG (nothing modified)
+ * for a dof outside [0, N). */
+lfg_status lfg_fix_solution_components_lse(lfg_coo* coo, int64_t count, const int64_t* dofs_dev,
+                                           const double* values_dev, double* b_dev);
 
 /* ------------------------------------------------------------- CSR + solve
  * COOMatrix::makeSparse (coomatrix.h:172-180) -> Eigen::setFromTriplets: the

@@ -37,6 +37,9 @@ STATUS_NAMES = ["OK", "INVALID_ARG", "DEGENERATE_CELL", "CAPACITY", "UNSUPPORTED
 
 # coefficient kinds and analytic families
 ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
+# matrix-valued diffusion coefficients (row-major 2x2): constant p[0..3], per cell
+# data[4 cell + e], bilinear entries p[4e] + p[4e+1] x + p[4e+2] y + p[4e+3] x y
+TENSOR_CONSTANT, TENSOR_PER_CELL, TENSOR_BILINEAR = 6, 7, 8
 FN_POLY, FN_SINSIN, FN_SINCOS, FN_EXP, FN_TRIG = 1, 2, 3, 4, 5
 # integrands of integrate_mesh_function
 INT_VALUE, INT_SQ_DIFF, INT_GRAD_SQ_DIFF = 0, 1, 2
@@ -467,6 +470,18 @@ class COOMatrix:
 
     def fix_flagged_solution_comp_alt(self, flags, values, b):
         self.ctx.check(lib().lfg_fix_flagged_solution_comp_alt(self.h, flags.ptr, values.ptr, b.ptr))
+
+    def fix_solution_components_lse(self, dofs, values, b):
+        """FixSolutionComponentsLse: `dofs` / `values` are the (dof, value)
+        pairs in list order (device arrays of int64 / float64, or host
+        arrays, which are copied to the device)."""
+        if not isinstance(dofs, DeviceArray):
+            dofs = self.ctx.to_device(np.ascontiguousarray(dofs, np.int64))
+        if not isinstance(values, DeviceArray):
+            values = self.ctx.to_device(np.ascontiguousarray(values, np.float64))
+        n = dofs.size
+        self.ctx.check(lib().lfg_fix_solution_components_lse(self.h, n, dofs.ptr if n else None,
+                                                             values.ptr if n else None, b.ptr))
 
     def make_sparse(self):
         h = C.c_void_p()

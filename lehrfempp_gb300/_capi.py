@@ -118,6 +118,7 @@ SIGNATURES = {
     "lfg_assemble_vector_tabulated": (c_status, [vp, vp, i32, vp]),
     "lfg_fix_flagged_solution_components": (c_status, [vp, vp, vp, vp]),
     "lfg_fix_flagged_solution_comp_alt": (c_status, [vp, vp, vp, vp]),
+    "lfg_fix_solution_components_lse": (c_status, [vp, i64, vp, vp, vp]),
     "lfg_csr_from_coo": (c_status, [vp, P(vp)]),
     "lfg_csr_destroy": (c_status, [vp]),
     "lfg_csr_info": (c_status, [vp, P(i64), P(i64), P(i64)]),

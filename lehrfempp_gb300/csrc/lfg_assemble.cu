@@ -248,6 +248,116 @@ __global__ void __launch_bounds__(128) RDGeneralKernel(AsmArgs a) {
   }
 }
 
+// ------------------------------------------- matrix-valued diffusion coefficient
+// ReactionDiffusionElementMatrixProvider::Eval (loc_comp_ellbvp.h:266-339)
+// with a 2x2 DIFF_COEFF alpha_k, not necessarily symmetric:
+//   A_K(i, j) = sum_k w_k |det J_k| [(J_k^-T gh_i)^T alpha_k (J_k^-T gh_j)
+//                                     + gamma_k phi_i phi_j].
+// With P = adj(J) (J^-1 = P / det J) the gradient term is gh_i^T B_k gh_j,
+// B_k = w_k P alpha_k P^T / |det J_k|.  FP64, one thread per cell; the full
+// n x n block (no symmetry), one row at a time.
+
+// alpha_k at reference point (xh, yh) of cell c, row-major.
+template <bool QUAD>
+__device__ void EvalTensorCoeff(const CoeffDev& f, int c, const double2 (&v)[4], double xh, double yh,
+                                double (&A)[4]) {
+  if (f.kind == LFG_COEFF_TENSOR_CONSTANT) {
+    for (int e = 0; e < 4; ++e) A[e] = f.p[e];
+  } else if (f.kind == LFG_COEFF_TENSOR_PER_CELL) {
+    for (int e = 0; e < 4; ++e) A[e] = f.data[4 * static_cast<int64_t>(c) + e];
+  } else {
+    double X, Y;
+    if (!QUAD) {
+      const double l0 = 1.0 - xh - yh;
+      X = v[0].x * l0 + v[1].x * xh + v[2].x * yh;
+      Y = v[0].y * l0 + v[1].y * xh + v[2].y * yh;
+    } else {
+      const double b0 = (1 - xh) * (1 - yh), b1 = xh * (1 - yh), b2 = xh * yh, b3 = (1 - xh) * yh;
+      X = v[0].x * b0 + v[1].x * b1 + v[2].x * b2 + v[3].x * b3;
+      Y = v[0].y * b0 + v[1].y * b1 + v[2].y * b2 + v[3].y * b3;
+    }
+    for (int e = 0; e < 4; ++e) A[e] = f.p[4 * e] + f.p[4 * e + 1] * X + f.p[4 * e + 2] * Y + f.p[4 * e + 3] * (X * Y);
+  }
+}
+
+// Jacobian (columns d/dxh, d/dyh) at a reference point: tria_o1.cc:50-74 /
+// quad_o1.cc:93-99.
+template <bool QUAD>
+__device__ __forceinline__ void Jacobian(const double2 (&v)[4], double xh, double yh, double& j00, double& j01,
+                                         double& j10, double& j11) {
+  if (!QUAD) {
+    j00 = v[1].x - v[0].x; j01 = v[2].x - v[0].x;
+    j10 = v[1].y - v[0].y; j11 = v[2].y - v[0].y;
+  } else {
+    j00 = (v[1].x - v[0].x) * (1 - yh) + (v[2].x - v[3].x) * yh;
+    j10 = (v[1].y - v[0].y) * (1 - yh) + (v[2].y - v[3].y) * yh;
+    j01 = (v[3].x - v[0].x) * (1 - xh) + (v[2].x - v[1].x) * xh;
+    j11 = (v[3].y - v[0].y) * (1 - xh) + (v[2].y - v[1].y) * xh;
+  }
+}
+
+// Shared memory: the rule (w, xh, yh), phi [nq][n], then the O1 values
+// [nq][4] and the reference gradients [nq][n][2] (the T / R / L blocks of the
+// table are not needed).
+template <int DEG, bool QUAD, bool MASS>
+__global__ void __launch_bounds__(128) RDTensorKernel(AsmArgs a) {
+  constexpr int N = QUAD ? (DEG + 1) * (DEG + 1) : (DEG + 1) * (DEG + 2) / 2;
+  extern __shared__ double sm[];
+  const int nq = a.L.nq;
+  const int head = a.L.off_T, tail = a.L.total - a.L.off_o1;
+  for (int i = threadIdx.x; i < head; i += blockDim.x) sm[i] = a.tab[i];
+  for (int i = threadIdx.x; i < tail; i += blockDim.x) sm[head + i] = a.tab[a.L.off_o1 + i];
+  __syncthreads();
+  const double* sw = sm + a.L.off_w;
+  const double* sqx = sm + a.L.off_qx;
+  const double* sqy = sm + a.L.off_qy;
+  const double* sphi = sm + a.L.off_phi;
+  const double* so1 = sm + head;
+  const double* sG = so1 + nq * 4;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < a.count;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = a.bucket[t];
+    int4 cn;
+    double2 v[4];
+    LoadVerts<QUAD>(a, c, cn, v);
+    int dofs[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) dofs[i] = a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + i];
+    lfg_triplet* base = a.out + a.tri_offset[c];
+    for (int i = 0; i < N; ++i) {
+      double acc[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) acc[j] = 0.0;
+      for (int k = 0; k < nq; ++k) {
+        double j00, j01, j10, j11;
+        Jacobian<QUAD>(v, sqx[k], sqy[k], j00, j01, j10, j11);
+        const double adet = fabs(j00 * j11 - j10 * j01);
+        double A[4];
+        EvalTensorCoeff<QUAD>(a.alpha, c, v, sqx[k], sqy[k], A);
+        // P = adj(J) = [[j11, -j01], [-j10, j00]]; Q = P alpha; B = w Q P^T / |det J|
+        const double q00 = j11 * A[0] - j01 * A[2], q01 = j11 * A[1] - j01 * A[3];
+        const double q10 = -j10 * A[0] + j00 * A[2], q11 = -j10 * A[1] + j00 * A[3];
+        const double s = sw[k] / adet;
+        const double b00 = s * (q00 * j11 - q01 * j01), b01 = s * (-q00 * j10 + q01 * j00);
+        const double b10 = s * (q10 * j11 - q11 * j01), b11 = s * (-q10 * j10 + q11 * j00);
+        const double gi0 = sG[(k * N + i) * 2], gi1 = sG[(k * N + i) * 2 + 1];
+        const double r0 = gi0 * b00 + gi1 * b10, r1 = gi0 * b01 + gi1 * b11;
+        double mi = 0.0;
+        if (MASS) mi = sw[k] * adet * EvalCoeff<QUAD>(a.gamma, c, cn, v, k, sw, sqx, sqy, so1) * sphi[k * N + i];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          double r = fma(r0, sG[(k * N + j) * 2], acc[j]);
+          r = fma(r1, sG[(k * N + j) * 2 + 1], r);
+          if (MASS) r = fma(mi, sphi[k * N + j], r);
+          acc[j] = r;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < N; ++j) StoreTriplet(base + i * N + j, dofs[i], dofs[j], acc[j]);
+    }
+  }
+}
+
 // ------------------------------------ cell-constant coefficients, df32 path
 // Triangles and quadrilaterals with constant / per-cell alpha and gamma.  One
 // thread per cell computes the upper triangle of A_K in df32 (lfg_elem.h):
@@ -2318,6 +2428,23 @@ void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, boo
   }
 }
 
+template <int DEG, bool QUAD>
+void LaunchTensor(lfg_ctx* ctx, const AsmArgs& a, bool mass) {
+  const size_t smem = static_cast<size_t>(a.L.off_T + a.L.total - a.L.off_o1) * sizeof(double);
+  ProfScope prof(ctx, QUAD ? "rd_tensor_quad" : "rd_tensor_tria");
+  if (mass) Launch(RDTensorKernel<DEG, QUAD, true>, ctx, a.count, smem, 128, a);
+  else Launch(RDTensorKernel<DEG, QUAD, false>, ctx, a.count, smem, 128, a);
+}
+
+template <bool QUAD>
+void DispatchTensor(lfg_ctx* ctx, int degree, const AsmArgs& a, bool mass) {
+  switch (degree) {
+    case 1: LaunchTensor<1, QUAD>(ctx, a, mass); break;
+    case 2: LaunchTensor<2, QUAD>(ctx, a, mass); break;
+    case 3: LaunchTensor<3, QUAD>(ctx, a, mass); break;
+  }
+}
+
 template <bool QUAD>
 void DispatchRD(lfg_ctx* ctx, int degree, const AsmArgs& a, const DfArgs& d, bool uniform, bool mass) {
   switch (degree) {
@@ -2444,12 +2571,25 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_
   AsmArgs a = BaseArgs(sp);
   a.tri_offset = sp->tri_offset.as<int64_t>();
   a.out = coo->d + coo->size;
-  a.alpha = ToDev(pr->alpha, m, "alpha");
+  a.alpha = ToDev(pr->alpha, m, "alpha", true);
   a.gamma = ToDev(pr->gamma, m, "gamma");
   const bool uniform = Uniform(pr->alpha) && Uniform(pr->gamma);
   const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
   const int deg = sp->degree;
   DfArgs none{nullptr, DfLayout()};
+  if (IsTensor(pr->alpha.kind)) {
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool quad = pass == 1;
+      a.count = quad ? m->nquad : m->ntria;
+      if (!a.count) continue;
+      a.tab = GetTable(sp, quad, deg, RuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, deg), a.L);
+      a.bucket = quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
+      if (quad) DispatchTensor<true>(sp->mesh->ctx, deg, a, mass);
+      else DispatchTensor<false>(sp->mesh->ctx, deg, a, mass);
+    }
+    coo->size += sp->num_triplets;
+    return LFG_OK;
+  }
   if (m->ntria) {
     const int rd = RuleDegree(pr->qr_degree_tria, deg);
     a.tab = GetTable(sp, false, deg, rd, a.L);

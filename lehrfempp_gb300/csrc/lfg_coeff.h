@@ -119,8 +119,13 @@ __device__ inline double EvalCoeffPoint(const CoeffDev& f, int c, const int4& cn
 
 inline bool KnownAnalytic(int func) { return func >= LFG_FN_POLY && func <= LFG_FN_TRIG; }
 
+inline bool IsTensor(int kind) {
+  return kind == LFG_COEFF_TENSOR_CONSTANT || kind == LFG_COEFF_TENSOR_PER_CELL || kind == LFG_COEFF_TENSOR_BILINEAR;
+}
+
 // Host conversion with the argument checks every entry point shares.
-inline CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
+// Matrix-valued kinds pass only where the caller accepts them (allow_tensor).
+inline CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what, bool allow_tensor = false) {
   (void)m;
   CoeffDev d;
   d.kind = c.kind;
@@ -128,9 +133,13 @@ inline CoeffDev ToDev(const lfg_coeff& c, const lfg_mesh* m, const char* what) {
   d.value = c.value;
   d.data = c.data_dev;
   for (int i = 0; i < 16; ++i) d.p[i] = c.p[i];
-  if (c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_PER_CELL_EXP)
+  if (IsTensor(c.kind) && !allow_tensor)
+    Fail(LFG_UNSUPPORTED, std::string(what) + ": a matrix-valued coefficient is accepted only as the diffusion "
+                                              "coefficient of the Lagrangian reaction-diffusion provider");
+  if ((c.kind < LFG_COEFF_ZERO || c.kind > LFG_COEFF_PER_CELL_EXP) && !IsTensor(c.kind))
     Fail(LFG_UNSUPPORTED, std::string(what) + ": unsupported coefficient kind");
-  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1 || c.kind == LFG_COEFF_PER_CELL_EXP) &&
+  if ((c.kind == LFG_COEFF_PER_CELL || c.kind == LFG_COEFF_NODAL_O1 || c.kind == LFG_COEFF_PER_CELL_EXP ||
+       c.kind == LFG_COEFF_TENSOR_PER_CELL) &&
       !c.data_dev)
     Fail(LFG_INVALID_ARG, std::string(what) + ": coefficient data pointer is null");
   if (c.kind == LFG_COEFF_ANALYTIC && !KnownAnalytic(c.func))

@@ -1,5 +1,5 @@
 // COOMatrix on the device and FixFlaggedSolutionComponents
-// (assemble/coomatrix.h:51-225, assemble/fix_dof.h:86-219).
+// (assemble/coomatrix.h:51-225, assemble/fix_dof.h:86-280).
 #include <algorithm>
 
 #include "lfg_api.h"
@@ -69,6 +69,40 @@ __global__ void AppendDiagKernel(int64_t ndofs, const uint8_t* __restrict__ flag
       d.value = 1.0;
       out[rank[k]] = d;
     }
+}
+
+// FixSolutionComponentsLse's (dof, value) list: keys = dof, payload = list
+// position; out-of-range dofs are reported through the status word.
+__global__ void LseKeysKernel(int64_t count, const int64_t* __restrict__ dofs, int64_t N,
+                              uint64_t* __restrict__ keys, uint32_t* __restrict__ pos, int32_t* st) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t d = dofs[i];
+    if (d < 0 || d >= N) {
+      atomicCAS(st, 0, 1);
+      keys[i] = 0;
+    } else {
+      keys[i] = static_cast<uint64_t>(d);
+    }
+    pos[i] = static_cast<uint32_t>(i);
+  }
+}
+
+// After a stable sort by dof: the first item of every run writes
+// flags[dof] = 1 and fixed[dof] = 0 + v_1 + v_2 + ... in list order (the
+// `fixed_vec[idx] += value` loop of fix_dof.h:266-272).
+__global__ void LseRunsKernel(int64_t count, const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pos,
+                              const double* __restrict__ vals, uint8_t* __restrict__ flags,
+                              double* __restrict__ fixed) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t k = keys[i];
+    if (i > 0 && keys[i - 1] == k) continue;
+    double s = 0.0;
+    for (int64_t m = i; m < count && keys[m] == k; ++m) s += vals[pos[m]];
+    fixed[k] = s;
+    flags[k] = 1;
+  }
 }
 
 void Fix(lfg_coo* coo, const uint8_t* flags, const double* vals, double* b, bool cols_too) {
@@ -223,6 +257,42 @@ lfg_status lfg_fix_flagged_solution_comp_alt(lfg_coo* coo, const uint8_t* flags,
   LFG_API_BEGIN(coo->ctx)
   if (!flags || !vals || !b) Fail(LFG_INVALID_ARG, "fix: null argument");
   Fix(coo, flags, vals, b, false);
+  LFG_API_END
+}
+
+lfg_status lfg_fix_solution_components_lse(lfg_coo* coo, int64_t count, const int64_t* dofs, const double* vals,
+                                           double* b) {
+  if (!coo) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(coo->ctx)
+  if (count < 0 || (count > 0 && (!dofs || !vals)) || !b)
+    Fail(LFG_INVALID_ARG, "lfg_fix_solution_components_lse: bad argument");
+  if (count >= (int64_t(1) << 32)) Fail(LFG_UNSUPPORTED, "more than 2^32 fixed components");
+  if (coo->rows != coo->cols) Fail(LFG_INVALID_ARG, "Matrix must be square!");
+  lfg_ctx* ctx = coo->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t N = coo->rows;
+  DevBuf flags, fixed;
+  flags.alloc(std::max<int64_t>(N, 1), s);
+  fixed.alloc(std::max<int64_t>(N, 1) * sizeof(double), s);
+  LFG_CUDA(cudaMemsetAsync(flags.p, 0, std::max<int64_t>(N, 1), s));
+  LFG_CUDA(cudaMemsetAsync(fixed.p, 0, std::max<int64_t>(N, 1) * sizeof(double), s));
+  if (count) {
+    DevBuf keys, pos;
+    keys.alloc(count * sizeof(uint64_t), s);
+    pos.alloc(count * sizeof(uint32_t), s);
+    ReadAndClearStatus(ctx);
+    LseKeysKernel<<<GridFor(ctx, count, 256), 256, 0, s>>>(count, dofs, N, keys.as<uint64_t>(), pos.as<uint32_t>(),
+                                                          StatusWord(ctx));
+    LFG_LAUNCHED(ctx);
+    if (ReadAndClearStatus(ctx)) Fail(LFG_INVALID_ARG, "fixed component index out of range [0, N)");
+    int bits = 1;
+    while ((int64_t(1) << bits) < N + 1) ++bits;
+    RadixSortPairs(ctx, keys.as<uint64_t>(), pos.as<uint32_t>(), count, bits);
+    LseRunsKernel<<<GridFor(ctx, count, 256), 256, 0, s>>>(count, keys.as<uint64_t>(), pos.as<uint32_t>(), vals,
+                                                          flags.as<uint8_t>(), fixed.as<double>());
+    LFG_LAUNCHED(ctx);
+  }
+  Fix(coo, flags.as<uint8_t>(), fixed.as<double>(), b, false);
   LFG_API_END
 }
 

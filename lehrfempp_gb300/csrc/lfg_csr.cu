@@ -171,6 +171,7 @@ constexpr int kSlice = 32;
 struct PcgScalars {
   double rz[2];
   double alpha, beta, rr, pq;
+  double trr;  // <t, t> of the true residual t = rhs - A x (inner FP32 solves, gap monitor)
   unsigned int counter;
   unsigned int pad;
 };
@@ -367,6 +368,48 @@ __global__ void __launch_bounds__(kPcgBlock) PcgStartKernel(int64_t rows, const 
       sc->beta = 0.0;
       sc->alpha = 0.0;
       sc->rr = rr;
+      sc->counter = 0;
+    }
+  }
+}
+
+// t = rhs - A x over the SELL copy in precision T; sc->trr = <t, t> (block
+// partials, then the last block).  The inner FP32 solve runs it once per
+// graph replay to see whether its recursively updated residual still tracks
+// the true one.
+template <class T>
+__global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows, int64_t nslices,
+                                                                   const int64_t* __restrict__ sptr,
+                                                                   const int32_t* __restrict__ scol,
+                                                                   const T* __restrict__ sval,
+                                                                   const T* __restrict__ x, const T* __restrict__ rhs,
+                                                                   double* __restrict__ part,
+                                                                   PcgScalars* __restrict__ sc) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  DotAcc<T> acc;
+  for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+    const int64_t r = sl * kSlice + lane;
+    const int64_t b0 = sptr[sl];
+    const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
+    if (r < rows) {
+      const int32_t* cp = scol + b0 + lane;
+      const T* vp = sval + b0 + lane;
+      T sum = T(0);
+#pragma unroll 4
+      for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], x[cp[k * kSlice]], sum);
+      const T t = rhs[r] - sum;
+      acc.add(t, t);
+    }
+  }
+  const double tot = BlockSum(acc.get(), red);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+  if (FinishedLast(&sc->counter)) {
+    const double v = SumParts(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      sc->trr = v;
       sc->counter = 0;
     }
   }
@@ -597,10 +640,14 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, i
 
 // PCG on A x = b in precision T from the residual already in S.r (x holds
 // the matching iterate).  Returns the iterations done; rr_out = <r, r> of the
-// recursively updated residual.
+// recursively updated residual.  With `rhs` (the inner FP32 solves of the
+// mixed solver, x = 0 at the start) the true residual rhs - A x is measured
+// after every graph replay, and the solve stops as soon as its norm exceeds
+// twice the recursive residual's: from there on the FP32 iterates no longer
+// improve the solution, and the FP64 refinement takes over.
 template <class T>
 int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double target_rr, int max_it,
-           int check_every, PcgState<T>& S, double& rr_out) {
+           int check_every, PcgState<T>& S, double& rr_out, const T* rhs = nullptr) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   PcgStartKernel<T><<<S.nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
@@ -615,11 +662,25 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
   }
   const int body = std::max(2, check_every + (check_every & 1));
   PcgGraph g = CapturePcg<T>(A, sval, dinv, x, n, body, S);
+  const int spmv_blocks = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (A->nslices + 7) / 8)));
   try {
     while (it < max_it) {
       LFG_CUDA(cudaGraphLaunch(g.exec, s));
       CountLaunch(ctx, g.launches);
       it += body;
+      if (rhs) {
+        PcgTrueResidualKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
+            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, x, rhs,
+            S.part.template as<double>(), S.scal.template as<PcgScalars>());
+        LFG_LAUNCHED(ctx);
+        PcgScalars h{};
+        D2HSync(ctx, &h, S.scal.p, sizeof(PcgScalars));
+        rr = h.rr;
+        if (!(rr > target_rr)) break;
+        if (!(h.trr <= 4.0 * rr)) break;  // the recursion lost the true residual (or NaN)
+        continue;
+      }
       rr = ReadRR(ctx, S.scal);
       if (!(rr > target_rr)) break;  // also stops on NaN
     }
@@ -808,10 +869,13 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     EnsureFloatValues(A);
     PcgState<float> S32;
     AllocState(ctx, n, S32);
-    DevBuf d32;
+    DevBuf d32, rhs32, x_old;
     d32.alloc(n * sizeof(float), s);
+    rhs32.alloc(n * sizeof(float), s);
+    x_old.alloc(n * sizeof(double), s);
     const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : kDefaultInnerRtol;
     int total = 0, outer = 0;
+    bool fp32_failed = false;
     while (total < max_it && outer < 200) {
       const double rnorm = std::sqrt(rr);
       if (rr <= target) break;
@@ -819,11 +883,13 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       ScaleToFloatKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S64.r.as<double>(), 1.0 / rnorm, S32.r.as<float>(),
                                                               d32.as<float>());
       LFG_LAUNCHED(ctx);
+      LFG_CUDA(cudaMemcpyAsync(rhs32.p, S32.r.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      LFG_CUDA(cudaMemcpyAsync(x_old.p, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
       // inner target relative to ||r / ||r|| || = 1, never below what the outer loop needs
       const double need = std::max(inner, 0.5 * std::sqrt(target) / rnorm);
       double rr_in = 0.0;
       const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
-                                   need * need, max_it - total, check, S32, rr_in);
+                                   need * need, max_it - total, check, S32, rr_in, rhs32.as<float>());
       total += std::max(it, 1);
       AddCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), rnorm, x);
       LFG_LAUNCHED(ctx);
@@ -832,9 +898,42 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       LFG_LAUNCHED(ctx);
       const double rr_new = HostSum(ctx, S64.res.as<double>(), nb, tmp);
       ++outer;
-      const bool progress = rr_new < rr;
+      if (!(rr_new < 0.25 * rr)) {
+        // the FP32 correction did not halve the FP64 residual: FP32 cannot
+        // make progress on this system.  Keep the better iterate and finish
+        // in FP64 (same restart rule as the FP64 solver).
+        if (!(rr_new < rr)) {
+          LFG_CUDA(cudaMemcpyAsync(x, x_old.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+          ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                                       A->val.as<double>(), x, b, S64.r.as<double>(),
+                                                       S64.res.as<double>());
+          LFG_LAUNCHED(ctx);
+        } else {
+          rr = rr_new;
+        }
+        fp32_failed = true;
+        break;
+      }
       rr = rr_new;
-      if (!progress) break;  // stagnation: no progress in FP32
+    }
+    if (fp32_failed) {
+      rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
+      double rr_prev = rr;
+      int restarts = 0;
+      while (rr > target && total < max_it) {
+        double rr_end = rr;
+        total += RunPcg<double>(A, A->sell_val.as<double>(), A->dinv.as<double>(), x, n, target, max_it - total,
+                                check, S64, rr_end);
+        ++restarts;
+        ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                                     A->val.as<double>(), x, b, S64.r.as<double>(),
+                                                     S64.res.as<double>());
+        LFG_LAUNCHED(ctx);
+        rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
+        if (restarts >= 16 || !(rr < 0.25 * rr_prev)) break;
+        rr_prev = rr;
+      }
+      outer += restarts;
     }
     st.iterations = total;
     st.refinements = outer;

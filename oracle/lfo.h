@@ -152,9 +152,11 @@ struct MeshFunction {
   double value = 0.0;
   std::vector<double> data;
   std::function<double(double, double)> fn;
-  // Optional 2x2 tensor-valued coefficient (only used by the reference's
-  // tensor-coefficient test): returns row-major a00,a01,a10,a11.
-  std::function<void(double, double, double*)> tensor_fn;
+  // 2x2 tensor-valued diffusion coefficient (the matrix-valued DIFF_COEFF of
+  // loc_comp_ellbvp.h:85-127): (cell, x, y) -> row-major a00, a01, a10, a11.
+  // Set for the tensor kinds 6 (constant), 7 (per cell) and 8 (bilinear
+  // entries), and by the reference's tensor-coefficient known answer.
+  std::function<void(idx_t, double, double, double*)> tensor_fn;
   bool IsTensor() const { return static_cast<bool>(tensor_fn); }
   void Eval(const Mesh& m, idx_t cell, const QuadRule& qr,
             std::vector<double>& out) const;
@@ -236,6 +238,10 @@ void FixFlaggedSolutionComponents(const uint8_t* flags, const double* values,
 // FixFlaggedSolutionCompAlt (fix_dof.h:183-219).
 void FixFlaggedSolutionCompAlt(const uint8_t* flags, const double* values,
                                COOMatrix& A, std::vector<double>& b);
+// FixSolutionComponentsLse (fix_dof.h:250-280): (dof, value) pairs; repeated
+// dofs accumulate their values in list order; then FixFlaggedSolutionCompAlt.
+void FixSolutionComponentsLse(const std::vector<std::pair<idx_t, double>>& fixed, COOMatrix& A,
+                              std::vector<double>& b);
 
 // COOMatrix::makeSparse (coomatrix.h:172-180) = Eigen setFromTriplets: per
 // (row,col) the duplicates are summed in triplet order.  Output is CSR.

@@ -1,6 +1,7 @@
 // Oracle (test infrastructure only): flat C entry points so that the Python
 // test-suite can drive the restatement through ctypes.  Every call returns 0
 // on success; on failure it returns -1 and copies the message into err.
+#include <array>
 #include <cstring>
 #include <chrono>
 #include <memory>
@@ -53,6 +54,22 @@ static MeshFunction ToMF(const lfo_coeff* c, size_t n_data) {
       c->kind == MeshFunction::kPerCellExp)
     mf.data.assign(c->data, c->data + n_data);
   if (c->kind == MeshFunction::kAnalytic) mf.fn = AnalyticFunction(c->func, c->p);
+  // matrix-valued kinds (the library's LFG_COEFF_TENSOR_*)
+  if (c->kind == 6) {
+    const std::array<double, 4> a{c->p[0], c->p[1], c->p[2], c->p[3]};
+    mf.tensor_fn = [a](idx_t, double, double, double* o) { std::copy(a.begin(), a.end(), o); };
+  } else if (c->kind == 7) {
+    auto d = std::make_shared<std::vector<double>>(c->data, c->data + 4 * n_data);
+    mf.tensor_fn = [d](idx_t cell, double, double, double* o) {
+      for (int e = 0; e < 4; ++e) o[e] = (*d)[4 * cell + e];
+    };
+  } else if (c->kind == 8) {
+    std::array<double, 16> q;
+    std::copy(c->p, c->p + 16, q.begin());
+    mf.tensor_fn = [q](idx_t, double x, double y, double* o) {
+      for (int e = 0; e < 4; ++e) o[e] = q[4 * e] + q[4 * e + 1] * x + q[4 * e + 2] * y + q[4 * e + 3] * (x * y);
+    };
+  }
   return mf;
 }
 
@@ -518,6 +535,18 @@ int lfo_fix_flagged(void* a, const uint8_t* flags, const double* vals, double* b
   LFO_CATCH
 }
 
+int lfo_fix_lse(void* a, int64_t count, const int64_t* dofs, const double* vals, double* b, char* err,
+                int errlen) {
+  LFO_TRY
+  auto* A = static_cast<COOMatrix*>(a);
+  std::vector<std::pair<idx_t, double>> fixed;
+  for (int64_t k = 0; k < count; ++k) fixed.emplace_back(static_cast<idx_t>(dofs[k]), vals[k]);
+  std::vector<double> bv(b, b + A->rows);
+  FixSolutionComponentsLse(fixed, *A, bv);
+  std::memcpy(b, bv.data(), bv.size() * sizeof(double));
+  LFO_CATCH
+}
+
 void* lfo_csr_create(void* a, int64_t* sizes) {
   auto* A = static_cast<COOMatrix*>(a);
   auto* C = new CSR;
@@ -556,7 +585,7 @@ int lfo_kat_tensor_rd(double* value, char* err, int errlen) {
   p.mesh = &m;
   p.degree = 1;
   p.alpha.kind = MeshFunction::kAnalytic;
-  p.alpha.tensor_fn = [](double x, double y, double* a) {
+  p.alpha.tensor_fn = [](idx_t, double x, double y, double* a) {
     a[0] = 1; a[1] = x; a[2] = y; a[3] = x * y;
   };
   p.gamma.kind = MeshFunction::kAnalytic;

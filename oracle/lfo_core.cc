@@ -794,7 +794,7 @@ void MeshFunction::EvalTensor(const Mesh& m, idx_t cell, const QuadRule& qr,
   for (int k = 0; k < qr.n(); ++k) {
     double X[2];
     g.Global(qr.x[k], qr.y[k], X);
-    tensor_fn(X[0], X[1], out[k].data());
+    tensor_fn(cell, X[0], X[1], out[k].data());
   }
 }
 
@@ -1043,6 +1043,20 @@ void FixFlaggedSolutionCompAlt(const uint8_t* flags, const double* values,
   A.triplets.erase(last, A.triplets.end());
   for (idx_t k = 0; k < N; ++k)
     if (flags[k]) A.AddToEntry(k, k, 1.0);
+}
+
+void FixSolutionComponentsLse(const std::vector<std::pair<idx_t, double>>& fixed, COOMatrix& A,
+                              std::vector<double>& b) {
+  const idx_t N = A.cols;
+  if (A.rows != N) throw Error("Matrix must be square!");
+  std::vector<double> fixed_vec(N, 0.0);
+  std::vector<uint8_t> flags(N, 0);
+  for (const auto& iv : fixed) {
+    if (iv.first < 0 || iv.first >= N) throw Error("FixSolutionComponentsLse: index out of range");
+    fixed_vec[iv.first] += iv.second;
+    flags[iv.first] = 1;
+  }
+  FixFlaggedSolutionCompAlt(flags.data(), fixed_vec.data(), A, b);
 }
 
 void MakeSparseCSR(const COOMatrix& A, std::vector<int64_t>& rowptr,

@@ -17,6 +17,9 @@ _lib = None
 _lock = threading.Lock()
 
 ZERO, CONSTANT, PER_CELL, NODAL_O1, ANALYTIC, PER_CELL_EXP = 0, 1, 2, 3, 4, 5
+# matrix-valued diffusion coefficients (row-major 2x2): constant p[0..3], per cell
+# data[4 cell + e], bilinear entries p[4e] + p[4e+1] x + p[4e+2] y + p[4e+3] x y
+TENSOR_CONSTANT, TENSOR_PER_CELL, TENSOR_BILINEAR = 6, 7, 8
 FN_POLY, FN_SINSIN, FN_SINCOS, FN_EXP, FN_TRIG = 1, 2, 3, 4, 5
 INT_VALUE, INT_SQ_DIFF, INT_GRAD_SQ_DIFF = 0, 1, 2
 
@@ -86,6 +89,7 @@ def lib():
             L.lfo_coo_size.restype = i64
             L.lfo_coo_copy.argtypes = [vp, P(i32), P(i32), P(dp)]
             L.lfo_fix_flagged.argtypes = [vp, P(C.c_uint8), P(dp), P(dp), C.c_int, C.c_char_p, C.c_int]
+            L.lfo_fix_lse.argtypes = [vp, C.c_int64, P(C.c_int64), P(dp), P(dp), C.c_char_p, C.c_int]
             L.lfo_csr_create.argtypes = [vp, P(i64)]
             L.lfo_csr_create.restype = vp
             L.lfo_csr_copy.argtypes = [vp, P(i64), P(i32), P(dp)]
@@ -270,6 +274,15 @@ class COO:
         err = _err()
         _check(lib().lfo_fix_flagged(self.h, _p(flags, C.c_uint8), _p(values, C.c_double), _p(b, C.c_double),
                                      int(alt), err, 512), err)
+
+    def fix_lse(self, dofs, values, b):
+        """FixSolutionComponentsLse with the (dof, value) pairs in list order."""
+        dofs = np.ascontiguousarray(dofs, np.int64)
+        values = np.ascontiguousarray(values, np.float64)
+        assert b.dtype == np.float64 and b.flags.c_contiguous and len(dofs) == len(values)
+        err = _err()
+        _check(lib().lfo_fix_lse(self.h, len(dofs), _p(dofs, C.c_int64), _p(values, C.c_double),
+                                 _p(b, C.c_double), err, 512), err)
 
     def to_csr(self):
         sizes = np.zeros(2, np.int64)

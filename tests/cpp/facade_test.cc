@@ -347,6 +347,38 @@ static void CheckAdjoint(const g::Context& ctx) {
   std::printf("adjoint: J %.6g, max |dJ/dtheta| %.3g, FD error %.3g\n", J, gmax, worst);
 }
 
+// The reference's fix_dof_test (assemble/test/coomatrix_tests.cc:77-121):
+// FixSolutionComponentsLse on the 10 x 10 tridiagonal system; its exact
+// solution must satisfy the modified system.  A dof listed twice is fixed to
+// the sum of its values.
+static void CheckFixLse(const g::Context& ctx) {
+  const int N = 10;
+  for (int dup = 0; dup < 2; ++dup) {
+    g::assemble::COOMatrix A(ctx, N, N, 64);
+    std::vector<double> bh(N);
+    for (int k = 0; k < N; ++k) {
+      if (k > 0) A.AddToEntry(k, k - 1, -1.0);
+      if (k < N - 1) A.AddToEntry(k, k + 1, -1.0);
+      A.AddToEntry(k, k, 2.0);
+      bh[k] = k + 1;
+    }
+    g::DeviceVector<double> b(ctx, bh);
+    g::assemble::fixed_components_t<double> fixed{{2, -1.0}, {4, -2.0}, {8, -3.0}};
+    if (dup) fixed = {{8, -1.0}, {2, -1.0}, {4, -2.0}, {8, -2.0}};
+    g::assemble::FixSolutionComponentsLse(fixed, A, b);
+    const std::vector<double> exact{1, 1, -1, 0.5, -2, 7.75, 11.5, 8.25, -3, 3.5};
+    auto S = A.makeSparse();
+    g::DeviceVector<double> x(ctx, exact), y(ctx, N);
+    ctx.Check(lfg_csr_spmv(S.get(), x.data(), y.data()));
+    const std::vector<double> ax = y.Download(), bb = b.Download();
+    double res = 0.0;
+    for (int k = 0; k < N; ++k) res = std::max(res, std::fabs(ax[k] - bb[k]));
+    CHECK(res <= 1e-12, "FixSolutionComponentsLse (dup %d): |A x_exact - b| = %g", dup, res);
+    CHECK(A.size() == 3 * N - 2 - 9 + 3, "FixSolutionComponentsLse: %lld triplets", static_cast<long long>(A.size()));
+  }
+  std::printf("fix: FixSolutionComponentsLse meets the reference's exact solution\n");
+}
+
 int main(int argc, char** argv) {
   try {
     g::Context ctx(0);
@@ -358,6 +390,7 @@ int main(int argc, char** argv) {
     CheckEdges(ctx);
     CheckPost(ctx);
     CheckHierarchic(ctx);
+    CheckFixLse(ctx);
   } catch (const g::Error& e) {
     std::printf("FAIL: uncaught lf::gb300::Error %d: %s\n", static_cast<int>(e.code()), e.what());
     return 1;

@@ -157,6 +157,22 @@ def test_function_gradient_matches_oracle(ctx, degree):
     assert np.allclose(grad.download(), -2.5 * gd, rtol=1e-12, atol=0.0)
 
 
+def test_function_gradient_matches_oracle_mid_size(ctx):
+    """The inverse-conductivity workload's shape at 256 x 256 (131,072 cells,
+    66,049 dofs): GPU forward + adjoint PCG + gradient kernel against the
+    oracle's FP64 gradient (element matrices and two SparseLU solves)."""
+    mesh, sp, osp, theta, u_obs, flags, g = _problem(ctx, 256, 1, seed=21)
+    fn = _function(ctx, sp, u_obs, rtol=1e-11)
+    J = fn.forward(ctx.to_device(theta))
+    grad = ctx.zeros(mesh.num_cells)
+    fn.backward(grad)
+    Jr, _, _, gr = O.adjoint_gradient(osp, theta, O.coeff(O.CONSTANT, 1.0), u_obs, flags)
+    assert abs(J - Jr) <= 1e-9 * Jr
+    gd = grad.download()
+    err = np.abs(gd - gr).max() / np.abs(gr).max()
+    assert err <= 1e-8, err
+
+
 def test_function_central_differences(ctx):
     """64 random cells, central differences with step 1e-6 through the GPU
     forward (8 x 8 mesh: the PCG solves reach rounding level)."""

@@ -193,6 +193,53 @@ def test_append_semantics(ctx):
     assert len(t) == 2 * n and np.array_equal(t[:n], t[n:])
 
 
+def test_fix_lse_parity(ctx, goldens):
+    """FixSolutionComponentsLse on the device: the reference's fix_dof_test
+    system, and an assembled system with repeated (dof, value) pairs against
+    the oracle (b bit-exact, triplets in order)."""
+    g = goldens["fix_dof_exact"]
+    N = 10
+    coo = L.COOMatrix(ctx, N, N, 64)
+    r, c, v = [], [], []
+    for k in range(N):
+        if k > 0:
+            r.append(k); c.append(k - 1); v.append(-1.0)
+        if k < N - 1:
+            r.append(k); c.append(k + 1); v.append(-1.0)
+        r.append(k); c.append(k); v.append(2.0)
+    coo.append(r, c, v)
+    b = ctx.to_device(np.arange(1, N + 1, dtype=np.float64))
+    dofs, vals = zip(*g["fixed"])
+    coo.fix_solution_components_lse(list(dofs), list(vals), b)
+    A = coo.make_sparse().to_scipy().toarray()
+    x = np.linalg.solve(A, b.download())
+    assert np.linalg.norm(x - np.array(g["solution"])) < g["tolerance"]
+    # assembled system, repeated dofs
+    run = Run(ctx, W.config2(12))
+    gc = run.gpu_matrix()
+    gb = run.gpu_vector()
+    rng = np.random.default_rng(8)
+    nd = run.space.num_dofs
+    dofs = rng.integers(0, nd, 300)
+    dofs = np.concatenate([dofs, dofs[:50]])  # repeats accumulate
+    vals = rng.standard_normal(len(dofs))
+    gc.fix_solution_components_lse(dofs, vals, gb)
+    oA = run.oracle_matrix()
+    ob = run.oracle_vector()
+    oA.fix_lse(dofs, vals, ob)
+    gbh = gb.download()
+    fixed = np.unique(dofs)
+    assert np.array_equal(gbh[fixed], ob[fixed])  # the accumulated values, bit for bit
+    assert np.abs(gbh - ob).max() <= 1e-12 * np.abs(ob).max()
+    ro, co, vo = oA.arrays()
+    t = gc.triplets()
+    assert np.array_equal(t["row"], ro) and np.array_equal(t["col"], co)
+    assert np.abs(t["value"] - vo).max() <= VALUE_RTOL * np.abs(vo).max()
+    with pytest.raises(L.LfgError) as e:
+        gc.fix_solution_components_lse([nd], [1.0], gb)
+    assert e.value.code == L.INVALID_ARG
+
+
 def test_fix_and_csr_parity(ctx):
     r = Run(ctx, W.config2(16))
     coo = r.gpu_matrix()
@@ -284,6 +331,67 @@ def test_solve_parity(ctx, name, precision):
     assert err <= 1e-8, err
 
 
+def test_kat_tensor_coefficient_gpu(ctx, goldens):
+    """lf_fe_linear.ReactionDiffusion (lagr_fe_tests.cc:804-831): O1 on test
+    mesh 0 with the matrix-valued diffusion coefficient [[1, x], [y, x y]] and
+    gamma = x y, degree-4 rules, assembled on the GPU; the bilinear form of the
+    projections of 1 + x + 2y and 3x is 7911/8 (to the reference's 1e-2) and
+    equals the oracle's value to 1e-12."""
+    k = goldens["reaction_diffusion_kat"]
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    m = L.Mesh.from_factory(ctx, xy, cells)
+    s = L.Space.lagrange(m, 1)
+    coo = L.COOMatrix(ctx, s.num_dofs, s.num_dofs, s.num_triplets)
+    tensor = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1]  # [[1, x], [y, x y]]
+    L.assemble_matrix_rd(s, L.rd_provider(L.coeff(L.TENSOR_BILINEAR, params=tensor),
+                                          L.coeff(L.ANALYTIC, func=L.FN_POLY, params=list(W.poly(x1y1=1))), 4, 4), coo)
+    os_ = O.Space(O.Mesh(xy, cells), 1)
+    av = O.nodal_projection(os_, O.FN_POLY, W.poly(c=1, x1=1, y1=2))
+    bv = O.nodal_projection(os_, O.FN_POLY, W.poly(x1=3))
+    val = av @ (coo.make_sparse().to_scipy() @ bv)
+    assert abs(val - k["O1_tensor_deg4"]["value"]) < k["tolerance"]
+    assert abs(val - O.kat_tensor_rd()) <= 1e-12 * abs(val)
+
+
+@pytest.mark.parametrize("kind", ["constant", "per_cell", "bilinear"])
+@pytest.mark.parametrize("degree,mesh", [(1, "hybrid"), (2, "tptriag"), (2, "hybrid"), (3, "tpquad"), (3, "hybrid")])
+def test_tensor_coefficient_parity(ctx, kind, degree, mesh):
+    """Matrix-valued (non-symmetric) diffusion coefficients against the oracle:
+    every element block, full n x n (the block is not symmetric), with and
+    without a reaction term."""
+    if mesh == "hybrid":
+        xy, cells = W.hybrid_mesh(7, seed=4)
+        spec = {"kind": "factory", "xy": xy, "cells": cells, "edges": None}
+    else:
+        spec = {"kind": mesh, "nx": 5, "ny": 4}
+    gm = W.build_mesh(ctx, spec)
+    om = oracle_mesh(spec)
+    gs, os_ = L.Space.lagrange(gm, degree), O.Space(om, degree)
+    rng = np.random.default_rng(degree)
+    keep = None
+    if kind == "constant":
+        ga, oa = L.coeff(L.TENSOR_CONSTANT, params=[2.0, 0.3, -0.2, 1.5]), \
+            O.coeff(O.TENSOR_CONSTANT, params=[2.0, 0.3, -0.2, 1.5])
+    elif kind == "per_cell":
+        d = np.tile([1.0, 0.0, 0.0, 1.0], gm.num_cells) + 0.3 * rng.standard_normal(4 * gm.num_cells)
+        keep = ctx.to_device(d)
+        ga, oa = L.coeff(L.TENSOR_PER_CELL, data=keep), O.coeff(O.TENSOR_PER_CELL, data=d)
+    else:
+        p = [1, 0.5, 0, 0.2, 0, 0.3, 0.1, 0, 0, 0, -0.4, 0.1, 2, 0, 0.5, 1]
+        ga, oa = L.coeff(L.TENSOR_BILINEAR, params=p), O.coeff(O.TENSOR_BILINEAR, params=p)
+    for gamma in (0.0, 0.7):
+        gg = L.coeff(L.CONSTANT, gamma) if gamma else L.coeff(L.ZERO)
+        og = O.coeff(O.CONSTANT, gamma) if gamma else O.coeff(O.ZERO)
+        coo = L.COOMatrix(ctx, gs.num_dofs, gs.num_dofs, gs.num_triplets)
+        L.assemble_matrix_rd(gs, L.rd_provider(ga, gg), coo)
+        ro, co, vo = O.assemble_rd(os_, oa, og).arrays()
+        compare_triplets(coo.triplets(), ro, co, vo, block_sizes(om.cells, os_.n_tria, os_.n_quad))
+    # matrix-valued coefficients are accepted only as the diffusion coefficient
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd(gs, L.rd_provider(L.coeff(L.CONSTANT, 1.0), ga), coo)
+    assert e.value.code == L.UNSUPPORTED
+
+
 @pytest.mark.parametrize("degree,alpha,gamma,a,b,qdeg,key", [
     (2, W.poly(x1=1), W.poly(x1y1=1), W.poly(x2=1, y2=1), W.poly(x2=1, y2=-1), 6, "O2_deg6"),
     (3, W.poly(y1=1), W.poly(x1y1=1), W.poly(x3=1, y3=1), W.poly(x1y2=1), 8, "O3_deg8"),
@@ -302,35 +410,6 @@ def test_kat_reaction_diffusion_gpu(ctx, goldens, degree, alpha, gamma, a, b, qd
     bv = O.nodal_projection(os_, O.FN_POLY, b)
     val = av @ (coo.make_sparse().to_scipy() @ bv)
     assert abs(val - k[key]["value"]) < k["tolerance"]
-
-
-def test_full_size_config3_properties(ctx):
-    """Config 3 at full size (1024x1024 O3, 209.7M triplets): exact symmetry of
-    every element block, total mass = |Omega| (stiffness rows sum to zero), and
-    sampled cell ranges against the oracle."""
-    wl = W.config3(1024)
-    mesh = W.build_mesh(ctx, wl["mesh"])
-    space = L.Space.lagrange(mesh, 3)
-    assert space.num_dofs == 9443329 and space.num_triplets == 2097152 * 100
-    keep = []
-    coo = L.COOMatrix(ctx, space.num_dofs, space.num_dofs, space.num_triplets)
-    L.assemble_matrix_rd(space, L.rd_provider(W.to_coeff(ctx, wl["alpha"], keep), W.to_coeff(ctx, wl["gamma"], keep),
-                                              6, 6), coo)
-    t = coo.triplets()
-    v = t["value"].reshape(-1, 10, 10)
-    assert np.array_equal(v, v.transpose(0, 2, 1))
-    # per cell: sum_ij A_K(i,j) = gamma |K| (stiffness rows sum to zero)
-    cell_sum = v.sum(axis=(1, 2))
-    scale = np.abs(v).max(axis=(1, 2))
-    assert (np.abs(cell_sum - 0.5 / 1024 ** 2) <= 1e-12 * 100 * scale).all()
-    assert np.array_equal(t["row"].reshape(-1, 10, 10), t["col"].reshape(-1, 10, 10).transpose(0, 2, 1))
-    om = oracle_mesh(wl["mesh"])
-    os_ = O.Space(om, 3)
-    from parity import oracle_coeff
-    for lo, hi in [(0, 512), (1048576, 1049088), (2097152 - 512, 2097152)]:
-        A = O.assemble_rd(os_, oracle_coeff(wl["alpha"]), oracle_coeff(wl["gamma"]), 6, 6, (lo, hi))
-        ro, co, vo = A.arrays()
-        compare_triplets(t[lo * 100:hi * 100], ro, co, vo, np.full(hi - lo, 100))
 
 
 def test_errors(ctx):

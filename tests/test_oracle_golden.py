@@ -94,6 +94,36 @@ def test_fix_dof_exact_solution(goldens, alt):
     assert np.linalg.norm(x - np.array(g["solution"])) < g["tolerance"]
 
 
+def test_fix_lse_exact_solution(goldens):
+    """fix_dof_test (coomatrix_tests.cc:77-121): FixSolutionComponentsLse with
+    {2: -1}, {4: -2}, {8: -3}, then a direct solve, meets the exact solution."""
+    import scipy.sparse.linalg as spla
+    g = goldens["fix_dof_exact"]
+    A, b = _tridiag_coo()
+    dofs, vals = zip(*g["fixed"])
+    A.fix_lse(list(dofs), list(vals), b)
+    x = spla.splu(A.to_scipy().tocsc()).solve(b)
+    assert np.linalg.norm(x - np.array(g["solution"])) < g["tolerance"]
+
+
+def test_fix_lse_accumulates_repeated_dofs():
+    """fix_dof.h:266-272: `fixed_vec[idx] += value` -- a dof listed twice is
+    fixed to the sum of its values, and only fixed rows are removed (CompAlt)."""
+    A1, b1 = _tridiag_coo()
+    A1.fix_lse([8, 2, 4, 8], [-1.0, -1.0, -2.0, -2.0], b1)
+    A2, b2 = _tridiag_coo()
+    flags = np.zeros(10, np.uint8)
+    flags[[2, 4, 8]] = 1
+    vals = np.zeros(10)
+    vals[[2, 4, 8]] = [-1.0, -2.0, -3.0]
+    A2.fix_flagged(flags, vals, b2, alt=True)
+    assert np.array_equal(b1, b2)
+    for u, v in zip(A1.arrays(), A2.arrays()):
+        assert np.array_equal(u, v)
+    with pytest.raises(RuntimeError):
+        A1.fix_lse([10], [1.0], b1)
+
+
 def test_fix_preserves_order_and_appends_diagonal():
     A, b = _tridiag_coo()
     r0, c0, v0 = A.arrays()
@@ -111,6 +141,30 @@ def test_kat_tensor_o1(goldens):
     """lf_fe_linear.ReactionDiffusion (lagr_fe_tests.cc:807-832)."""
     k = goldens["reaction_diffusion_kat"]
     assert abs(O.kat_tensor_rd() - k["O1_tensor_deg4"]["value"]) < k["tolerance"]
+
+
+def test_tensor_coefficient_kinds():
+    """The oracle's matrix-valued coefficient kinds: the bilinear-entry kind
+    reproduces the tensor known answer exactly, and constant / per-cell kinds
+    agree with it where the tensor is the same everywhere."""
+    xy, cells, _ = O.factory_input("test0", x0=1.0)
+    s = O.Space(O.Mesh(xy, cells), 1)
+    tensor = [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1]  # [[1, x], [y, x y]]
+    A = O.assemble_rd(s, O.coeff(O.TENSOR_BILINEAR, params=tensor),
+                      O.coeff(O.ANALYTIC, func=O.FN_POLY, params=list(poly(x1y1=1))), 4, 4).to_scipy()
+    av = O.nodal_projection(s, O.FN_POLY, poly(c=1, x1=1, y1=2))
+    bv = O.nodal_projection(s, O.FN_POLY, poly(x1=3))
+    assert abs(av @ (A @ bv) - O.kat_tensor_rd()) <= 1e-13 * O.kat_tensor_rd()
+    c = [2.0, 0.3, -0.2, 1.5]
+    A1 = O.assemble_rd(s, O.coeff(O.TENSOR_CONSTANT, params=c), O.coeff(O.ZERO)).to_scipy()
+    A2 = O.assemble_rd(s, O.coeff(O.TENSOR_PER_CELL, data=np.tile(c, s.mesh.num_cells)), O.coeff(O.ZERO)).to_scipy()
+    p = [c[0], 0, 0, 0, c[1], 0, 0, 0, c[2], 0, 0, 0, c[3], 0, 0, 0]
+    A3 = O.assemble_rd(s, O.coeff(O.TENSOR_BILINEAR, params=p), O.coeff(O.ZERO)).to_scipy()
+    assert (A1 != A2).nnz == 0 and (A1 != A3).nnz == 0
+    # a symmetric tensor alpha I gives the scalar coefficient's matrix
+    As = O.assemble_rd(s, O.coeff(O.CONSTANT, 1.7), O.coeff(O.ZERO)).to_scipy()
+    At = O.assemble_rd(s, O.coeff(O.TENSOR_CONSTANT, params=[1.7, 0, 0, 1.7]), O.coeff(O.ZERO)).to_scipy()
+    assert abs(As - At).max() <= 1e-14 * abs(As).max()
 
 
 @pytest.mark.parametrize("degree,alpha,gamma,a,b,qdeg,key", [
