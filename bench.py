@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=2048)
-    ap.add_argument("--solve-size", type=int, default=512)
+    ap.add_argument("--solve-size", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512, help="config-4 meshes (0: skip the batch leg)")
@@ -111,6 +111,43 @@ def run_case(spec):
         raise SystemExit("unknown case %r" % spec)
     ctx.close()
     print(json.dumps(out))
+
+
+def host_placement(device):
+    """Where this process runs relative to the GPU (the host link's speed
+    depends on it): usable CPUs, NUMA nodes, and the GPU's NUMA node."""
+    out = {"cpus": len(os.sched_getaffinity(0))}
+    try:
+        nodes = sorted(int(d[4:]) for d in os.listdir("/sys/devices/system/node")
+                       if d.startswith("node") and d[4:].isdigit())
+        out["numa_nodes"] = len(nodes)
+        cpus = os.sched_getaffinity(0)
+        mine = []
+        for n in nodes:
+            with open("/sys/devices/system/node/node%d/cpulist" % n) as f:
+                ids = set()
+                for part in f.read().strip().split(","):
+                    if part:
+                        a, _, b = part.partition("-")
+                        ids.update(range(int(a), int(b or a) + 1))
+            if ids & cpus:
+                mine.append(n)
+        out["process_numa_nodes"] = mine
+    except (OSError, ValueError):
+        pass
+    try:
+        r = subprocess.run(["nvidia-smi", "-i", str(device), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                           capture_output=True, text=True, timeout=20)
+        bus = r.stdout.strip().lower()
+        if bus.startswith("0000") and len(bus) > 12:
+            bus = bus[4:]
+        path = "/sys/bus/pci/devices/%s/numa_node" % bus
+        if os.path.exists(path):
+            with open(path) as f:
+                out["gpu_numa_node"] = int(f.read().strip())
+    except (OSError, ValueError, subprocess.SubprocessError):
+        pass
+    return out
 
 
 def dist_env():
@@ -258,16 +295,16 @@ def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
                       "not timed" % (ncell, m.num_cells, ntrip, setup), "_counts": counts}
 
 
-RTOL_LADDER = (1e-6, 1e-7, 1e-8, 1e-9, 1e-10)
-
-
 def solve_leg(L, W, ctx, n, cpu_check=False):
-    """Config 2's solve at n x n (hybrid O2): DOFs/s of assemble + fix +
-    COO->CSR + PCG, FP64 vs mixed precision.
-    - "to_1e-8_err": the metric's definition -- the largest residual target of
-      RTOL_LADDER whose solution is within 1e-8 (relative 2-norm) of the
-      reference solution (FP64 PCG run to its rounding floor), timed end to end;
-    - "rtol_1e-10": the configuration's residual target 1e-10;
+    """The large hybrid configuration's solve at n x n (O2): DOFs/s of
+    assemble + fix + COO->CSR + PCG, FP64 vs mixed precision.
+    - reference: FP64 PCG to relative residual 1e-8 (at 2048 x 2048 the FP64
+      residual floor eps ||A|| ||x|| / ||b|| of this h^2-scaled system is
+      about 1e-8, so the configuration's 1e-10 is not attainable in FP64; the
+      1e-8 solution is within ~2e-11 of a solve run to the floor);
+    - "to_1e-8_err": the metric's definition -- the largest residual target
+      of (1e-6, 1e-7, 1e-8) whose solution is within 1e-8 (relative 2-norm) of
+      the reference, timed end to end (assembly, fix, CSR and solve);
     - cpu_check: the oracle's SuperLU (the reference drivers' direct FP64
       solve) on the 256 x 256 subcase, its DOFs/s on one core, and the GPU
       mixed solution's error against it."""
@@ -296,22 +333,20 @@ def solve_leg(L, W, ctx, n, cpu_check=False):
         ctx.synchronize()
         return x.download(), st, time.perf_counter() - t0
 
-    r, _, _ = run(L.SOLVE_FP64, 1e-13)  # reference: FP64 PCG to its rounding floor
+    r, st, dt = run(L.SOLVE_FP64, 1e-8)
     rn = np.linalg.norm(r)
-    out = {"workload": "hybrid %dx%d O2 (%d dofs)" % (n, n, nd)}
+    out = {"workload": "hybrid %dx%d O2" % (n, n), "dofs": nd,
+           "reference": {"precision": "fp64", "rtol": 1e-8, "seconds": dt, "iterations": st["iterations"],
+                         "rel_residual": st["rel_residual"], "converged": st["converged"]}}
     for name, prec in (("fp64", L.SOLVE_FP64), ("mixed", L.SOLVE_MIXED)):
         rec = {}
-        for rtol in RTOL_LADDER:
+        for rtol in (1e-6, 1e-7, 1e-8):
             x, st, dt = run(prec, rtol)
             err = float(np.linalg.norm(x - r) / rn)
             if err <= 1e-8:
                 rec["to_1e-8_err"] = {"dofs_per_s": nd / dt, "seconds": dt, "rtol": rtol, "rel_err": err,
                                       "iterations": st["iterations"], "refinements": st["refinements"]}
                 break
-        x, st, dt = run(prec, 1e-10)
-        rec["rtol_1e-10"] = {"dofs_per_s": nd / dt, "seconds": dt, "iterations": st["iterations"],
-                             "refinements": st["refinements"], "rel_residual": st["rel_residual"],
-                             "converged": st["converged"], "rel_err_vs_fp64_floor": float(np.linalg.norm(x - r) / rn)}
         out[name] = rec
     if "to_1e-8_err" in out["fp64"] and "to_1e-8_err" in out["mixed"]:
         out["mixed_vs_fp64_at_1e-8_err"] = out["mixed"]["to_1e-8_err"]["dofs_per_s"] / \
@@ -582,7 +617,7 @@ def hier_leg(L, W, ctx, steps=3, cpu_check=False):
     return out
 
 
-def batch_leg(L, W, ctx, count):
+def batch_leg(L, W, ctx, count, superlu_meshes=0):
     """Config 4: `count` TPTriag meshes (n log-uniform in [24, 320], O1/O2),
     one persistent assembly launch + load + fix + COO->CSR + batched PCG.
     DOFs/s of the batched mixed and FP64 solves solved to 1e-8 error on every
@@ -621,13 +656,21 @@ def batch_leg(L, W, ctx, count):
         dt = time.perf_counter() - t0
         return x, st, dt, ctx.launches() - l0
 
-    run(L.SOLVE_MIXED, 1e-10)  # autotunes the assembly launch, warms allocations
+    # first calls: the autotuner picks the assembly launch shape and, per
+    # precision, the solver's rows per chunk
+    t0 = time.perf_counter()
+    run(L.SOLVE_MIXED, 1e-6)
+    run(L.SOLVE_FP64, 1e-6)
+    first_s = time.perf_counter() - t0
     out = {"workload": "%d TPTriag meshes n in [24, 320] log-uniform, O1/O2 50/50, alpha LogNormal(0, 0.5^2), "
                        "gamma 1, f 1, Dirichlet 0" % count,
            "meshes": count, "dofs": int(nd), "cells": int(batch.num_cells), "triplets": int(batch.num_triplets),
-           "setup_s": setup_s}
+           "setup_s": setup_s, "first_calls_s": first_s}
     th, ct, ms = batch.tuning()
     out["autotuner"] = {"threads_per_cta": th, "ctas_per_sm": ct, "assembly_ms": ms}
+    for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
+        cr, rate = batch.solve_tuning(prec)
+        out["autotuner"]["solve_" + name] = {"chunk_rows": cr, "row_iterations_per_s": rate}
     xr, st, _, _ = run(L.SOLVE_FP64, 1e-13)  # reference: batched FP64 PCG to its rounding floor
     r = xr.download()
 
@@ -636,15 +679,18 @@ def batch_leg(L, W, ctx, count):
                       np.linalg.norm(r[dof[k]:dof[k + 1]])) for k in range(count)]
 
     plain_rtol = 1e-10
+    solutions = {}
     for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
         rec = {}
         for rtol in (1e-6, 1e-7, 1e-8):  # DOFs/s solved to 1e-8 error (every mesh)
             x, st, dt, launches = run(prec, rtol)
-            errs = mesh_errs(x.download())
+            xh = x.download()
+            errs = mesh_errs(xh)
             if max(errs) <= 1e-8:
                 rec["to_1e-8_err"] = {"dofs_per_s": nd / dt, "seconds": dt, "rtol": rtol, "max_mesh_rel_err": max(errs),
                                       "gpu_launches": launches,
                                       "max_iterations": max(blk["iterations"] for blk in st["blocks"])}
+                solutions[name] = xh
                 if name == "fp64":
                     plain_rtol = rtol
                 break
@@ -680,7 +726,40 @@ def batch_leg(L, W, ctx, count):
     best = max((out[k]["to_1e-8_err"]["dofs_per_s"] for k in ("mixed", "fp64") if "to_1e-8_err" in out[k]), default=None)
     if best:
         out["best_batched_vs_plain_fp64_at_1e-8_err"] = best / out["plain_fp64"]["dofs_per_s"]
+    if "to_1e-8_err" in out["mixed"] and "to_1e-8_err" in out["fp64"]:
+        out["mixed_vs_fp64_at_1e-8_err"] = out["mixed"]["to_1e-8_err"]["dofs_per_s"] / \
+            out["fp64"]["to_1e-8_err"]["dofs_per_s"]
+    if superlu_meshes and solutions:
+        out["superlu_subset"] = batch_superlu_subset(wl, dof, solutions, superlu_meshes)
     return out
+
+
+def batch_superlu_subset(wl, dof, solutions, count, seed=4040):
+    """Per-mesh error of the batched solutions (solved to 1e-8 error) against
+    the oracle's system solved by SuperLU (FP64 direct), on a seeded subset of
+    `count` meshes that includes the largest one."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import scipy.sparse.linalg as spla
+    import oracle as O
+    ns, degs = wl["ns"], wl["degrees"]
+    cell_off = np.concatenate([[0], np.cumsum(wl["cells"])])
+    largest = int(np.argmax(np.where(degs == 2, 2 * ns + 1, ns + 1)))
+    pick = sorted(set(np.random.default_rng(seed).choice(len(ns), count - 1, replace=False).tolist()) | {largest})
+    errs = {k: [] for k in solutions}
+    t0 = time.perf_counter()
+    for k in pick:
+        xy, cells, pe = O.factory_input("tptriag", int(ns[k]), int(ns[k]))
+        os_ = O.Space(O.Mesh(xy, cells, pe), int(degs[k]))
+        A = O.assemble_rd(os_, O.coeff(O.PER_CELL, data=wl["alpha"][cell_off[k]:cell_off[k + 1]]),
+                          O.coeff(O.CONSTANT, wl["gamma"]))
+        b = O.assemble_load(os_, O.coeff(O.CONSTANT, wl["f"]))
+        A.fix_flagged(os_.boundary_dof_flags(), np.zeros(os_.num_dofs), b)
+        xo = spla.splu(A.to_scipy().tocsc()).solve(b)
+        for name, x in solutions.items():
+            errs[name].append(float(np.linalg.norm(x[dof[k]:dof[k + 1]] - xo) / np.linalg.norm(xo)))
+    return {"meshes": len(pick), "largest_mesh_n": int(ns[largest]), "seconds": time.perf_counter() - t0,
+            "max_rel_err": max(max(e) for e in errs.values()),
+            "max_rel_err_per_precision": {k: max(e) for k, e in errs.items()}}
 
 
 def gradient_leg(L, W, ctx, n, steps, cpu_check=True):
@@ -800,10 +879,7 @@ def summarize(line):
                 t[k + "_Mdof_s_1e-8err"] = _r(e["dofs_per_s"] / 1e6)
                 t[k + "_s"] = _r(e["seconds"])
                 t[k + "_it"] = e.get("iterations")
-            e = _get(so, k, "rtol_1e-10")
-            if e:
-                t[k + "_rtol1e-10_s"] = _r(e["seconds"])
-                t[k + "_rtol1e-10_err_vs_fp64"] = _r(e.get("rel_err_vs_fp64_floor"), 2)
+        t["fp64_rtol1e-8_s"] = _r(_get(so, "reference", "seconds"))
         t["mixed_vs_fp64"] = _r(so.get("mixed_vs_fp64_at_1e-8_err"), 3)
         t["cpu_superlu_Mdof_s"] = _r(_get(so, "cpu_baseline", "value") and so["cpu_baseline"]["value"] / 1e6)
         t["gpu_err_vs_superlu_256"] = _r(_get(so, "cpu_baseline", "gpu_mixed_rtol_1e-10_rel_err_vs_sparselu"), 2)
@@ -922,7 +998,10 @@ def run_ours(args):
         L.assemble_vector_load(space, lprov, b)
     vec_ms = ctx.timer_end() / 5
 
-    # end to end through the C-ABI with host buffers
+    # end to end through the C-ABI with host buffers: per step the per-cell
+    # alpha goes up from pinned host memory and lfg_assemble_matrix_rd_to_host
+    # assembles cell ranges into a device ring while finished ranges go down
+    # into a pinned host COO (5.1 GB)
     e2e = None
     if not args.no_e2e:
         a_pin = ctx.pinned(alpha_h.shape, np.float64)
@@ -933,11 +1012,17 @@ def run_ours(args):
             if it == 1:
                 t0 = time.perf_counter()
             alpha_d.upload_async(a_pin)
-            step()
-            coo.download_into(t_pin)  # synchronizes
+            L.assemble_matrix_rd_to_host(space, prov, t_pin)  # synchronizes
         e2e_s = (time.perf_counter() - t0) / e2e_steps
+        # the host link alone: one device-to-host copy of the same bytes
+        step()
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        coo.download_into(t_pin)
+        d2h_gbs = ntrip * 16 / (time.perf_counter() - t1) / 1e9
         e2e = {"value": world * ntrip / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(alpha_h.nbytes),
-               "d2h_bytes_per_step": int(ntrip * 16), "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": int(ntrip * 16), "ms_per_step": e2e_s * 1e3,
+               "d2h_link_gbs": d2h_gbs, "host": host_placement(local)}
         del t_pin
     del coo
 
@@ -954,7 +1039,8 @@ def run_ours(args):
     high_order = leg(high_order_leg, L, W, ctx, args.ho_size) if args.ho_size > 0 else None
     solve = leg(solve_leg, L, W, ctx, args.solve_size,
                 cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.solve_size > 0 else None
-    batch = leg(batch_leg, L, W, ctx, args.batch_count) if args.batch_count > 0 else None
+    batch = leg(batch_leg, L, W, ctx, args.batch_count,
+                superlu_meshes=(16 if rank == 0 and not args.no_cpu_baseline else 0)) if args.batch_count > 0 else None
     gradient = leg(gradient_leg, L, W, ctx, args.grad_size, steps=3,
                    cpu_check=(rank == 0 and not args.no_cpu_baseline)) if args.grad_size > 0 else None
 

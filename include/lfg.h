@@ -329,6 +329,17 @@ lfg_status lfg_coo_append_host(lfg_coo* coo, const lfg_triplet* host, int64_t co
  * a cell, row = GlobalDofIndices(K)[i], col = GlobalDofIndices(K)[j]. */
 lfg_status lfg_assemble_matrix_rd(lfg_space* space, const lfg_rd_provider* provider,
                                   lfg_coo* coo);
+/* The same assembly with the COOMatrix in host memory, as the reference keeps
+ * it (assemble/coomatrix.h:51-225): the sum_K n_K^2 triplets are written to
+ * host[0 .. count) in the same order.  The cells are assembled in ranges of
+ * about chunk_triplets triplets (<= 0: 2^24) into a ring of three device
+ * staging buffers while earlier ranges are copied to the host on a second
+ * stream, so the device holds only the ring, not the whole matrix.  host
+ * should be page-locked (lfg_host_alloc) for the copies to overlap.
+ * LFG_CAPACITY if capacity < sum_K n_K^2.  Lagrangian spaces. */
+lfg_status lfg_assemble_matrix_rd_to_host(lfg_space* space, const lfg_rd_provider* provider,
+                                          lfg_triplet* host, int64_t capacity, int64_t chunk_triplets,
+                                          int64_t* count);
 /* AssembleVectorLocally(0, dofh, provider, b) (assembler.h:298-327):
  * b_dev[dof] += element vector entries, cells in index order (deterministic). */
 lfg_status lfg_assemble_matrix_edge_mass(lfg_space* space, const lfg_edge_mass_provider* provider, lfg_coo* coo);
@@ -387,7 +398,14 @@ lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
  *   LFG_SOLVE_MIXED  FP32 PCG inner solves (FP32 matrix copy and vectors) of
  *                    A d = r / ||r|| to inner_rtol, inside FP64 iterative
  *                    refinement: r = b - A x in FP64, x += ||r|| d in FP64,
- *                    to the same FP64 residual criterion.
+ *                    to the same FP64 residual criterion.  The FP32 operator
+ *                    is applied in difference form, (A p)_r = sum_k a_rk
+ *                    (p_k - p_r) + s_r p_r with the FP64 row sum s_r, so that
+ *                    rounding the entries to FP32 keeps it close to A on its
+ *                    smooth modes.  An inner solve stops early when its true
+ *                    residual departs from the recursive one; when an FP32
+ *                    correction does not halve the FP64 residual norm the solve
+ *                    finishes in FP64 from the better iterate.
  * x_dev holds the initial guess on entry. */
 enum { LFG_SOLVE_FP64 = 0, LFG_SOLVE_MIXED = 1 };
 typedef struct {
@@ -518,12 +536,22 @@ lfg_status lfg_batch_boundary_dof_flags(lfg_batch* batch, uint8_t* flags_dev);
 /* Batched PCG: one independent Jacobi-PCG per block of the block-diagonal
  * CSR (each with its own step lengths and stopping test), all advanced
  * together by the same kernels, replayed from a CUDA graph.  precision FP64 or
- * MIXED (FP32 inner iterations, FP64 residual refinement).  per_block_stats
+ * MIXED (FP32 inner iterations, FP64 residual refinement; the FP32 operator
+ * is applied in difference form, see lfg_solve_pcg).  per_block_stats
  * (num_spaces entries, may be NULL) and the summary stats (iterations = the
  * longest block, converged = all blocks). */
 lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const double* b_dev,
                                double* x_dev, const lfg_solve_opts* opts, lfg_solve_stats* stats,
                                lfg_solve_stats* per_block_stats);
+/* The batched PCG works on chunks of rows that never straddle two blocks;
+ * the first solve in each precision times the candidate chunk sizes (512 ..
+ * 4096 rows) on this batch and keeps the fastest.  The choice for `precision`
+ * (0 before the first solve in that precision) and its measured rate in
+ * row-iterations per second; and an override.  The chunk size changes only
+ * the order of each block's partial sums.  No reference counterpart. */
+lfg_status lfg_batch_solve_tuning(const lfg_batch* batch, int32_t precision, int32_t* chunk_rows,
+                                  double* row_iterations_per_s);
+lfg_status lfg_batch_set_solve_chunk_rows(lfg_batch* batch, int32_t precision, int32_t chunk_rows);
 
 /* ---------------------------------------------------------------- Gmsh reader
  * GmshReader(factory, filename) (io/gmsh_reader.h, io/gmsh_reader.cc:22-30,

@@ -571,6 +571,16 @@ class Batch:
         self.ctx.check(lib().lfg_batch_tuning(self.h, C.byref(th), C.byref(ct), C.byref(ms)))
         return th.value, ct.value, ms.value
 
+    def solve_tuning(self, precision=SOLVE_MIXED):
+        """(rows per chunk, row-iterations/s) chosen by the solver autotuner for
+        `precision` (zeros before the first solve in that precision)."""
+        cr, rate = C.c_int32(), C.c_double()
+        self.ctx.check(lib().lfg_batch_solve_tuning(self.h, precision, C.byref(cr), C.byref(rate)))
+        return cr.value, rate.value
+
+    def set_solve_chunk_rows(self, precision, chunk_rows):
+        self.ctx.check(lib().lfg_batch_set_solve_chunk_rows(self.h, precision, int(chunk_rows)))
+
     def assemble_vector_load(self, provider, b):
         self.ctx.check(lib().lfg_batch_assemble_vector_load(self.h, C.byref(provider), b.ptr))
 
@@ -658,6 +668,19 @@ def assemble_vector_edge_load(space, provider, b):
 
 def assemble_matrix_rd(space, provider, coo):
     space.ctx.check(lib().lfg_assemble_matrix_rd(space.h, C.byref(provider), coo.h))
+
+
+def assemble_matrix_rd_to_host(space, provider, out, chunk_triplets=0):
+    """AssembleMatrixLocally into host memory: `out` is a PinnedArray (or a
+    numpy array) of TRIPLET_DTYPE with at least space.num_triplets entries;
+    the device assembly of cell ranges overlaps their download.  Returns the
+    number of triplets written."""
+    arr = out.array if isinstance(out, PinnedArray) else out
+    assert arr.dtype == TRIPLET_DTYPE and arr.flags.c_contiguous
+    n = C.c_int64()
+    space.ctx.check(lib().lfg_assemble_matrix_rd_to_host(space.h, C.byref(provider), arr.ctypes.data, len(arr),
+                                                         int(chunk_triplets), C.byref(n)))
+    return n.value
 
 
 def assemble_vector_load(space, provider, b):

@@ -111,6 +111,7 @@ SIGNATURES = {
     "lfg_coo_download": (c_status, [vp, vp, i64]),
     "lfg_coo_append_host": (c_status, [vp, vp, i64]),
     "lfg_assemble_matrix_rd": (c_status, [vp, P(lfg_rd_provider), vp]),
+    "lfg_assemble_matrix_rd_to_host": (c_status, [vp, P(lfg_rd_provider), vp, i64, i64, P(i64)]),
     "lfg_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
     "lfg_assemble_matrix_edge_mass": (c_status, [vp, P(lfg_edge_mass_provider), vp]),
     "lfg_assemble_vector_edge_load": (c_status, [vp, P(lfg_edge_load_provider), vp]),
@@ -142,6 +143,8 @@ SIGNATURES = {
     "lfg_batch_assemble_vector_load": (c_status, [vp, P(lfg_load_provider), vp]),
     "lfg_batch_boundary_dof_flags": (c_status, [vp, vp]),
     "lfg_batch_solve_pcg": (c_status, [vp, vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats), P(lfg_solve_stats)]),
+    "lfg_batch_solve_tuning": (c_status, [vp, i32, P(i32), P(dbl)]),
+    "lfg_batch_set_solve_chunk_rows": (c_status, [vp, i32, i32]),
     "lfg_gmsh_last_error": (C.c_char_p, []),
     "lfg_gmsh_open": (c_status, [C.c_char_p, P(vp)]),
     "lfg_gmsh_open_buffer": (c_status, [C.c_char_p, i64, P(vp)]),

@@ -2509,6 +2509,66 @@ void LoadElementVectors(lfg_space* sp, const lfg_load_provider* pr, double* ev) 
   }
 }
 
+// Argument checks of the Lagrangian reaction-diffusion assembly.
+void CheckRD(lfg_space* sp, const lfg_rd_provider* pr) {
+  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "reaction-diffusion provider needs a Lagrangian space");
+  lfg_mesh* m = sp->mesh;
+  if (m->ntria && pr->qr_degree_tria < 0)
+    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type TRIA");
+  if (m->nquad && pr->qr_degree_quad < 0)
+    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type QUAD");
+}
+
+// Element matrices of the triangles tria_list[t0, t1) and quadrilaterals
+// quad_list[q0, q1) (each list ascending by cell index): cell c's n_c^2
+// triplets go to out + tri_offset[c], row-major.
+void AssembleRDCells(lfg_space* sp, const lfg_rd_provider* pr, lfg_triplet* out, int64_t t0, int64_t t1,
+                     int64_t q0, int64_t q1) {
+  lfg_mesh* m = sp->mesh;
+  AsmArgs a = BaseArgs(sp);
+  a.tri_offset = sp->tri_offset.as<int64_t>();
+  a.out = out;
+  a.alpha = ToDev(pr->alpha, m, "alpha", true);
+  a.gamma = ToDev(pr->gamma, m, "gamma");
+  const bool uniform = Uniform(pr->alpha) && Uniform(pr->gamma);
+  const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
+  const int deg = sp->degree;
+  DfArgs none{nullptr, DfLayout()};
+  if (IsTensor(pr->alpha.kind)) {
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool quad = pass == 1;
+      a.count = quad ? q1 - q0 : t1 - t0;
+      if (a.count <= 0) continue;
+      a.tab = GetTable(sp, quad, deg, RuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, deg), a.L);
+      a.bucket = quad ? m->quad_list.as<int32_t>() + q0 : m->tria_list.as<int32_t>() + t0;
+      if (quad) DispatchTensor<true>(m->ctx, deg, a, mass);
+      else DispatchTensor<false>(m->ctx, deg, a, mass);
+    }
+    return;
+  }
+  if (t1 > t0) {
+    const int rd = RuleDegree(pr->qr_degree_tria, deg);
+    a.tab = GetTable(sp, false, deg, rd, a.L);
+    a.bucket = m->tria_list.as<int32_t>() + t0;
+    a.count = t1 - t0;
+    DispatchRD<false>(m->ctx, deg, a, GetDfTable(sp, false, deg, rd), uniform, mass);
+  }
+  if (q1 > q0) {
+    const int rd = RuleDegree(pr->qr_degree_quad, deg);
+    a.tab = GetTable(sp, true, deg, rd, a.L);
+    a.bucket = m->quad_list.as<int32_t>() + q0;
+    a.count = q1 - q0;
+    DispatchRD<true>(m->ctx, deg, a, uniform ? GetDfTable(sp, true, deg, rd) : none, uniform, mass);
+  }
+}
+
+__global__ void GatherI64Kernel(int64_t n, const int64_t* __restrict__ idx, const int64_t* __restrict__ src,
+                                int64_t* __restrict__ out) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    out[i] = src[idx[i]];
+}
+
 // grad[c] = -gscale * lambda_K^T (dA_K/dtheta_c) u_K for every cell (the
 // differentiation entry point and the adjoint Function object share it).
 void GradRDCellwise(lfg_space* sp, const lfg_rd_provider* pr, const double* u, const double* lam,
@@ -2557,54 +2617,113 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* sp, const lfg_rd_provider* pr, lfg_
     HierAssembleMatrix(sp, pr, coo);
     return LFG_OK;
   }
-  if (sp->degree < 1) Fail(LFG_UNSUPPORTED, "reaction-diffusion provider needs a Lagrangian space");
+  CheckRD(sp, pr);
   if (coo->rows < sp->num_dofs || coo->cols < sp->num_dofs)
     Fail(LFG_INVALID_ARG, "COO matrix smaller than the number of dofs");
-  lfg_mesh* m = sp->mesh;
-  if (m->ntria && pr->qr_degree_tria < 0)
-    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type TRIA");
-  if (m->nquad && pr->qr_degree_quad < 0)
-    Fail(LFG_MISSING_RULE, "No local shape function information or no quadrature rule for reference element type QUAD");
   if (coo->size + sp->num_triplets > coo->capacity)
     Fail(LFG_CAPACITY, "COO capacity " + std::to_string(coo->capacity) + " < " +
                            std::to_string(coo->size + sp->num_triplets));
-  AsmArgs a = BaseArgs(sp);
-  a.tri_offset = sp->tri_offset.as<int64_t>();
-  a.out = coo->d + coo->size;
-  a.alpha = ToDev(pr->alpha, m, "alpha", true);
-  a.gamma = ToDev(pr->gamma, m, "gamma");
-  const bool uniform = Uniform(pr->alpha) && Uniform(pr->gamma);
-  const bool mass = pr->gamma.kind != LFG_COEFF_ZERO;
-  const int deg = sp->degree;
-  DfArgs none{nullptr, DfLayout()};
-  if (IsTensor(pr->alpha.kind)) {
-    for (int pass = 0; pass < 2; ++pass) {
-      const bool quad = pass == 1;
-      a.count = quad ? m->nquad : m->ntria;
-      if (!a.count) continue;
-      a.tab = GetTable(sp, quad, deg, RuleDegree(quad ? pr->qr_degree_quad : pr->qr_degree_tria, deg), a.L);
-      a.bucket = quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>();
-      if (quad) DispatchTensor<true>(sp->mesh->ctx, deg, a, mass);
-      else DispatchTensor<false>(sp->mesh->ctx, deg, a, mass);
-    }
-    coo->size += sp->num_triplets;
-    return LFG_OK;
-  }
-  if (m->ntria) {
-    const int rd = RuleDegree(pr->qr_degree_tria, deg);
-    a.tab = GetTable(sp, false, deg, rd, a.L);
-    a.bucket = m->tria_list.as<int32_t>();
-    a.count = m->ntria;
-    DispatchRD<false>(sp->mesh->ctx, deg, a, GetDfTable(sp, false, deg, rd), uniform, mass);
-  }
-  if (m->nquad) {
-    const int rd = RuleDegree(pr->qr_degree_quad, deg);
-    a.tab = GetTable(sp, true, deg, rd, a.L);
-    a.bucket = m->quad_list.as<int32_t>();
-    a.count = m->nquad;
-    DispatchRD<true>(sp->mesh->ctx, deg, a, uniform ? GetDfTable(sp, true, deg, rd) : none, uniform, mass);
-  }
+  AssembleRDCells(sp, pr, coo->d + coo->size, 0, sp->mesh->ntria, 0, sp->mesh->nquad);
   coo->size += sp->num_triplets;
+  LFG_API_END
+}
+
+lfg_status lfg_assemble_matrix_rd_to_host(lfg_space* sp, const lfg_rd_provider* pr, lfg_triplet* host,
+                                          int64_t capacity, int64_t chunk_triplets, int64_t* count) {
+  if (!sp) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(sp->mesh->ctx)
+  if (!pr || !host) Fail(LFG_INVALID_ARG, "lfg_assemble_matrix_rd_to_host: null argument");
+  if (sp->hier_degree > 0) Fail(LFG_UNSUPPORTED, "host output: Lagrangian spaces only");
+  CheckRD(sp, pr);
+  if (capacity < sp->num_triplets)
+    Fail(LFG_CAPACITY, "host capacity " + std::to_string(capacity) + " < " + std::to_string(sp->num_triplets));
+  lfg_mesh* m = sp->mesh;
+  lfg_ctx* ctx = m->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t nc = m->nc;
+  const int64_t nmax = std::max(sp->n_tria, sp->n_quad);
+  const int64_t per_cell = nmax * nmax;
+  if (chunk_triplets <= 0) chunk_triplets = int64_t(1) << 24;
+  chunk_triplets = std::max(chunk_triplets, per_cell);
+  const int64_t cells_per_chunk = std::max<int64_t>(1, chunk_triplets / per_cell);
+  const int64_t nchunk = (nc + cells_per_chunk - 1) / cells_per_chunk;
+  // host copies of the ascending type lists (the chunk boundaries are found
+  // in them by binary search) and the triplet offsets of the boundary cells
+  if (m->h_tria_list.size() != static_cast<size_t>(m->ntria) ||
+      m->h_quad_list.size() != static_cast<size_t>(m->nquad)) {
+    m->h_tria_list.resize(m->ntria);
+    m->h_quad_list.resize(m->nquad);
+    if (m->ntria)
+      LFG_CUDA(cudaMemcpyAsync(m->h_tria_list.data(), m->tria_list.p, m->ntria * sizeof(int32_t),
+                               cudaMemcpyDeviceToHost, s));
+    if (m->nquad)
+      LFG_CUDA(cudaMemcpyAsync(m->h_quad_list.data(), m->quad_list.p, m->nquad * sizeof(int32_t),
+                               cudaMemcpyDeviceToHost, s));
+  }
+  std::vector<int64_t> bound(nchunk + 1), toff(nchunk + 1);
+  for (int64_t k = 0; k <= nchunk; ++k) bound[k] = std::min(nc, k * cells_per_chunk);
+  {
+    DevBuf db, dout;
+    db.alloc((nchunk + 1) * sizeof(int64_t), s);
+    dout.alloc((nchunk + 1) * sizeof(int64_t), s);
+    LFG_CUDA(cudaMemcpyAsync(db.p, bound.data(), (nchunk + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    GatherI64Kernel<<<static_cast<unsigned>((nchunk + 256) / 256), 256, 0, s>>>(
+        nchunk + 1, db.as<int64_t>(), sp->tri_offset.as<int64_t>(), dout.as<int64_t>());
+    LFG_LAUNCHED(ctx);
+    LFG_CUDA(cudaMemcpyAsync(toff.data(), dout.p, (nchunk + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    LFG_CUDA(cudaStreamSynchronize(s));
+  }
+  // staging ring: the assembly of range k on the context stream overlaps the
+  // download of range k - 1 on a second stream; events order the reuse
+  constexpr int kRing = 3;
+  int64_t slot_trip = 1;
+  for (int64_t k = 0; k < nchunk; ++k) slot_trip = std::max(slot_trip, toff[k + 1] - toff[k]);
+  DevBuf ring;
+  ring.alloc(slot_trip * kRing * sizeof(lfg_triplet), s);
+  cudaStream_t cs = nullptr;
+  cudaEvent_t assembled[kRing] = {}, copied[kRing] = {};
+  auto release = [&]() {
+    if (cs) cudaStreamSynchronize(cs);
+    for (int i = 0; i < kRing; ++i) {
+      if (assembled[i]) cudaEventDestroy(assembled[i]);
+      if (copied[i]) cudaEventDestroy(copied[i]);
+    }
+    if (cs) cudaStreamDestroy(cs);
+  };
+  try {
+    LFG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    for (int i = 0; i < kRing; ++i) {
+      LFG_CUDA(cudaEventCreateWithFlags(&assembled[i], cudaEventDisableTiming));
+      LFG_CUDA(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming));
+    }
+    for (int64_t k = 0; k < nchunk; ++k) {
+      const int slot = static_cast<int>(k % kRing);
+      lfg_triplet* buf = ring.as<lfg_triplet>() + slot * slot_trip;
+      if (k >= kRing) LFG_CUDA(cudaStreamWaitEvent(s, copied[slot], 0));  // the slot's last download is done
+      const int64_t lo = bound[k], hi = bound[k + 1];
+      const auto& tl = m->h_tria_list;
+      const auto& ql = m->h_quad_list;
+      const int64_t t0 = std::lower_bound(tl.begin(), tl.end(), lo) - tl.begin();
+      const int64_t t1 = std::lower_bound(tl.begin(), tl.end(), hi) - tl.begin();
+      const int64_t q0 = std::lower_bound(ql.begin(), ql.end(), lo) - ql.begin();
+      const int64_t q1 = std::lower_bound(ql.begin(), ql.end(), hi) - ql.begin();
+      // cell c of the range writes at out + tri_offset[c]; out sits toff[k]
+      // triplets before the slot, so every store lands inside the slot
+      AssembleRDCells(sp, pr, buf - toff[k], t0, t1, q0, q1);
+      LFG_CUDA(cudaEventRecord(assembled[slot], s));
+      LFG_CUDA(cudaStreamWaitEvent(cs, assembled[slot], 0));
+      LFG_CUDA(cudaMemcpyAsync(host + toff[k], buf, (toff[k + 1] - toff[k]) * sizeof(lfg_triplet),
+                               cudaMemcpyDeviceToHost, cs));
+      LFG_CUDA(cudaEventRecord(copied[slot], cs));
+    }
+    LFG_CUDA(cudaStreamSynchronize(cs));
+    LFG_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    release();
+    throw;
+  }
+  release();
+  if (count) *count = sp->num_triplets;
   LFG_API_END
 }
 

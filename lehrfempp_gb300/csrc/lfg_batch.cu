@@ -58,10 +58,16 @@ struct lfg_batch {
   bool tuned = false;
   int threads = 128, ctas_per_sm = 0;
   double best_ms = 0.0;
-  // PCG chunks
+  // PCG chunks (chunk_rows rows each, never straddling two meshes)
   lfg::DevBuf chunk_mesh, chunk_start, mesh_chunk_off;
   int64_t nchunks = 0;
+  int chunk_rows = 0;
   std::vector<int64_t> h_mesh_chunk_off;
+  // rows per chunk of the batched PCG per precision (0 FP64, 1 mixed), chosen
+  // by timing the candidates on the first solve in that precision
+  bool solve_tuned[2] = {false, false};
+  int solve_chunk_rows[2] = {2048, 2048};
+  double solve_rate[2] = {0.0, 0.0};  // row-iterations per second of the chosen shape
 };
 
 namespace lfg {
@@ -170,7 +176,7 @@ size_t StagePerCell(int degree) {
 }
 
 // ------------------------------------------------------------ batched PCG
-constexpr int kChunk = 2048;
+constexpr int kChunk = 2048;  // rows per chunk until the solver autotuner has chosen
 constexpr int kPB = 256;  // threads per block of the PCG kernels
 constexpr int kLanes = 8;
 
@@ -243,8 +249,12 @@ struct Sell {
 
 // q = A p on the chunk's rows (SELL-32; thread per row), <p, q> per mesh
 // -> alpha_b.
+// With `rowsum` (the FP32 copy) each row is applied in difference form,
+// sum_k a_rk (p_k - p_r) + s_r p_r with the FP64 row sum s_r rounded once,
+// which keeps the FP32 operator close to A on its smooth modes.
 template <class T>
 __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __restrict__ val,
+                                                   const T* __restrict__ rowsum,
                                                    const T* __restrict__ p, T* __restrict__ q,
                                                    const int32_t* __restrict__ frozen, int cur,
                                                    double* __restrict__ part, MeshScal* __restrict__ ms) {
@@ -260,8 +270,15 @@ __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __
       const int32_t* cp = M.col + b0 + lane;
       const T* vp = val + b0 + lane;
       T sum = T(0);
+      if (rowsum) {
+        const T pr = p[r];
 #pragma unroll 4
-      for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]], sum);
+        for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]] - pr, sum);
+        sum = fma(rowsum[r], pr, sum);
+      } else {
+#pragma unroll 4
+        for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]], sum);
+      }
       q[r] = sum;
       acc.add(p[r], sum);
     }
@@ -481,7 +498,8 @@ void MeshRR(lfg_batch* B, const DevBuf& ms, std::vector<double>& out) {
 // (squared norms); meshes with frozen_h[b] start frozen.  Returns per-mesh
 // iterations in it_out and final recursive rr in rr_out.
 template <class T>
-void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BState<T>& S, const Chunks& C,
+void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, BState<T>& S,
+             const Chunks& C,
              const std::vector<double>& target_rr, std::vector<int32_t>& frozen_h, DevBuf& frozen_d, int max_it,
              int check_every, std::vector<int>& it_out, std::vector<double>& rr_out) {
   lfg_ctx* ctx = B->ctx;
@@ -508,7 +526,8 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BStat
     const int cur = k & 1;
     T* p = S.p.template as<T>();
     BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p, frozen_d.as<int32_t>(), ms);
-    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, p, S.q.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
+    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, rowsum, p, S.q.template as<T>(), frozen_d.as<int32_t>(), cur,
+                                        part, ms);
     BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                          S.z.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
   }
@@ -544,6 +563,117 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* dinv, T* x, BStat
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
   rr_out = rr;
+}
+
+// Chunks of `rows` rows, never straddling two meshes.
+void BuildChunks(lfg_batch* B, int rows) {
+  if (B->chunk_rows == rows) return;
+  lfg_ctx* ctx = B->ctx;
+  const int n = B->nb;
+  std::vector<int32_t> cm;
+  std::vector<int64_t> cs, mc(n + 1, 0);
+  for (int b = 0; b < n; ++b) {
+    mc[b] = static_cast<int64_t>(cm.size());
+    for (int64_t r = B->dof_off[b]; r < B->dof_off[b + 1]; r += rows) {
+      cm.push_back(b);
+      cs.push_back(r);
+    }
+  }
+  mc[n] = static_cast<int64_t>(cm.size());
+  cs.push_back(B->dof_off[n]);
+  B->nchunks = static_cast<int64_t>(cm.size());
+  B->h_mesh_chunk_off = mc;
+  B->chunk_mesh.alloc(std::max<size_t>(cm.size(), 1) * sizeof(int32_t), ctx->stream);
+  B->chunk_start.alloc(cs.size() * sizeof(int64_t), ctx->stream);
+  B->mesh_chunk_off.alloc(mc.size() * sizeof(int64_t), ctx->stream);
+  if (!cm.empty())
+    LFG_CUDA(cudaMemcpyAsync(B->chunk_mesh.p, cm.data(), cm.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             ctx->stream));
+  LFG_CUDA(cudaMemcpyAsync(B->chunk_start.p, cs.data(), cs.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  LFG_CUDA(cudaMemcpyAsync(B->mesh_chunk_off.p, mc.data(), mc.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(ctx->stream));  // the host vectors above are temporaries
+  B->chunk_rows = rows;
+}
+
+// The autotuner's probe vectors: r = 1, x = 0 on every row.
+template <class T>
+__global__ void BFillKernel(int64_t n, T* __restrict__ r, T* __restrict__ x) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    r[i] = T(1);
+    x[i] = T(0);
+  }
+}
+
+// The batched PCG's autotuner: for each candidate number of rows per chunk
+// (the work of one block between reductions), time `body` iterations of
+// all blocks in precision T on scratch vectors and keep the candidate with
+// the most row-iterations per second.
+template <class T>
+void TuneChunks(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, int check) {
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  const int pi = sizeof(T) == 8 ? 0 : 1;
+  const int64_t n = B->dof_off[B->nb];
+  const int body = std::max(2, check + (check & 1));
+  double best = -1.0;
+  for (int rows : {512, 1024, 2048, 4096}) {
+    BuildChunks(B, rows);
+    Chunks C{B->chunk_mesh.as<int32_t>(), B->chunk_start.as<int64_t>(), B->mesh_chunk_off.as<int64_t>(), B->nchunks};
+    const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
+    BState<T> S;
+    BAlloc(ctx, n, C.nchunks, B->nb, S);
+    DevBuf xs, frozen;
+    xs.alloc(n * sizeof(T), s);
+    frozen.alloc(B->nb * sizeof(int32_t), s);
+    LFG_CUDA(cudaMemsetAsync(frozen.p, 0, B->nb * sizeof(int32_t), s));
+    const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+    MeshScal* ms = S.ms.template as<MeshScal>();
+    double* part = S.part.template as<double>();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < body; ++k) {
+      const int cur = k & 1;
+      T* p = S.p.template as<T>();
+      BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p, frozen.as<int32_t>(), ms);
+      BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, rowsum, p, S.q.template as<T>(), frozen.as<int32_t>(), cur,
+                                          part, ms);
+      BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p, S.q.template as<T>(), xs.as<T>(), S.r.template as<T>(),
+                                           S.z.template as<T>(), frozen.as<int32_t>(), cur, part, ms);
+    }
+    LFG_CUDA(cudaStreamEndCapture(s, &graph));
+    float ms_t = 0.f;
+    try {
+      LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+      for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms the caches and the graph
+        BFillKernel<T><<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S.r.template as<T>(), xs.as<T>());
+        BStartKernel<T><<<grid, kPB, 0, s>>>(C, dinv, S.r.template as<T>(), S.z.template as<T>(),
+                                            S.p.template as<T>(), frozen.as<int32_t>(), part, ms);
+        LFG_CUDA(cudaEventRecord(ctx->t0, s));
+        LFG_CUDA(cudaGraphLaunch(exec, s));
+        LFG_CUDA(cudaEventRecord(ctx->t1, s));
+        LFG_CUDA(cudaEventSynchronize(ctx->t1));
+        LFG_CUDA(cudaEventElapsedTime(&ms_t, ctx->t0, ctx->t1));
+      }
+    } catch (...) {
+      if (exec) cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    CountLaunch(ctx, 4 + 6 * body);
+    const double rate = static_cast<double>(n) * body / (ms_t * 1e-3);
+    if (rate > best) {
+      best = rate;
+      B->solve_chunk_rows[pi] = rows;
+    }
+  }
+  B->solve_rate[pi] = best;
+  B->solve_tuned[pi] = true;
 }
 
 }  // namespace
@@ -590,26 +720,7 @@ lfg_status lfg_batch_create(lfg_ctx* ctx, int32_t n, lfg_space* const* spaces, l
     if (B->dof_off[n] >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "batch has more than 2^31 dofs");
     B->meshes.alloc(n * sizeof(BatchMesh), ctx->stream);
     LFG_CUDA(cudaMemcpyAsync(B->meshes.p, hm.data(), n * sizeof(BatchMesh), cudaMemcpyHostToDevice, ctx->stream));
-    // PCG chunks (never straddling two meshes)
-    std::vector<int32_t> cm;
-    std::vector<int64_t> cs, mc(n + 1, 0);
-    for (int b = 0; b < n; ++b) {
-      mc[b] = static_cast<int64_t>(cm.size());
-      for (int64_t r = B->dof_off[b]; r < B->dof_off[b + 1]; r += kChunk) {
-        cm.push_back(b);
-        cs.push_back(r);
-      }
-    }
-    mc[n] = static_cast<int64_t>(cm.size());
-    cs.push_back(B->dof_off[n]);
-    B->nchunks = static_cast<int64_t>(cm.size());
-    B->h_mesh_chunk_off = mc;
-    B->chunk_mesh.alloc(cm.size() * sizeof(int32_t), ctx->stream);
-    B->chunk_start.alloc(cs.size() * sizeof(int64_t), ctx->stream);
-    B->mesh_chunk_off.alloc(mc.size() * sizeof(int64_t), ctx->stream);
-    LFG_CUDA(cudaMemcpyAsync(B->chunk_mesh.p, cm.data(), cm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    LFG_CUDA(cudaMemcpyAsync(B->chunk_start.p, cs.data(), cs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-    LFG_CUDA(cudaMemcpyAsync(B->mesh_chunk_off.p, mc.data(), mc.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    BuildChunks(B, kChunk);
     LFG_CUDA(cudaStreamSynchronize(ctx->stream));
   } catch (...) {
     delete B;
@@ -651,6 +762,27 @@ lfg_status lfg_batch_tuning(const lfg_batch* B, int32_t* threads, int32_t* ctas,
   if (ctas) *ctas = B->tuned ? B->ctas_per_sm : 0;
   if (ms) *ms = B->best_ms;
   return LFG_OK;
+}
+
+lfg_status lfg_batch_solve_tuning(const lfg_batch* B, int32_t precision, int32_t* chunk_rows,
+                                  double* row_iterations_per_s) {
+  if (!B || (precision != LFG_SOLVE_FP64 && precision != LFG_SOLVE_MIXED)) return LFG_INVALID_ARG;
+  const int pi = precision == LFG_SOLVE_MIXED ? 1 : 0;
+  if (chunk_rows) *chunk_rows = B->solve_tuned[pi] ? B->solve_chunk_rows[pi] : 0;
+  if (row_iterations_per_s) *row_iterations_per_s = B->solve_tuned[pi] ? B->solve_rate[pi] : 0.0;
+  return LFG_OK;
+}
+
+lfg_status lfg_batch_set_solve_chunk_rows(lfg_batch* B, int32_t precision, int32_t chunk_rows) {
+  if (!B) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  if (precision != LFG_SOLVE_FP64 && precision != LFG_SOLVE_MIXED) Fail(LFG_INVALID_ARG, "unknown solve precision");
+  if (chunk_rows < 32 || chunk_rows > (1 << 20)) Fail(LFG_INVALID_ARG, "chunk_rows must be in [32, 2^20]");
+  const int pi = precision == LFG_SOLVE_MIXED ? 1 : 0;
+  B->solve_chunk_rows[pi] = chunk_rows;
+  B->solve_rate[pi] = 0.0;
+  B->solve_tuned[pi] = true;
+  LFG_API_END
 }
 
 lfg_status lfg_batch_assemble_matrix_rd(lfg_batch* B, const lfg_rd_provider* pr, lfg_coo* coo) {
@@ -801,6 +933,19 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
   if (A->rows != n || A->cols != n) Fail(LFG_INVALID_ARG, "matrix size differs from the batch");
   if (A->nnz >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "solver needs nnz < 2^31");
   PrepareSolve(A);  // Jacobi diagonal, int32 row pointers, SELL-32 copy
+  const bool mixed = opts->precision == LFG_SOLVE_MIXED;
+  if (mixed) EnsureFloatValues(A);  // FP32 SELL values and row sums
+  {
+    const int pi = mixed ? 1 : 0;
+    const int chk = opts->check_every > 0 ? opts->check_every : 32;
+    if (!B->solve_tuned[pi]) {
+      if (mixed)
+        TuneChunks<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), chk);
+      else if (opts->precision == LFG_SOLVE_FP64)
+        TuneChunks<double>(B, A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), chk);
+    }
+    BuildChunks(B, B->solve_chunk_rows[pi]);
+  }
   Chunks C{B->chunk_mesh.as<int32_t>(), B->chunk_start.as<int64_t>(), B->mesh_chunk_off.as<int64_t>(), B->nchunks};
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
   const int check = opts->check_every > 0 ? opts->check_every : 32;
@@ -835,7 +980,7 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
         active += !fz[b];
       }
       if (!active) break;
-      BRunPcg<double>(B, A, A->sell_val.as<double>(), A->dinv.as<double>(), x, S, C, target, fz, frozen, max_it, check,
+      BRunPcg<double>(B, A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, S, C, target, fz, frozen, max_it, check,
                       it1, rr1);
       for (int b = 0; b < B->nb; ++b) {
         its[b] += it1[b];
@@ -875,7 +1020,8 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
       LFG_CUDA(cudaMemcpyAsync(done.p, dn.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
       BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
       LFG_LAUNCHED(ctx);
-      BRunPcg<float>(B, A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), S32, C, tin, fz, frozen,
+      BRunPcg<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
+                     S32, C, tin, fz, frozen,
                      max_it, check, it1, rr1);
       BCorrectKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), done.as<int32_t>(), x);
       LFG_LAUNCHED(ctx);

@@ -224,11 +224,35 @@ struct DotAcc<float> {
   __device__ double get() const { return static_cast<double>(v); }
 };
 
+// One row of q = A p over the SELL copy.  With `rowsum` (the FP32 copy of
+// the mixed solver) the row is applied in difference form,
+//     (A p)_r = sum_k a_rk (p_k - p_r) + s_r p_r,   s_r = sum_k a_rk (FP64),
+// so that rounding the entries to FP32 perturbs each term relative to the
+// differences p_k - p_r: the FP32 operator then stays close to A on the
+// smooth, small-eigenvalue modes even when cond(A) times the FP32 unit
+// roundoff exceeds 1 (rounding the entries alone shifts each row's sum by
+// about that much).  The diagonal entry drops out (p_r - p_r = 0).
+template <class T>
+__device__ __forceinline__ T SellRow(const int32_t* __restrict__ cp, const T* __restrict__ vp, int w,
+                                     const T* __restrict__ p, int64_t r, const T* __restrict__ rowsum) {
+  T sum = T(0);
+  if (rowsum) {
+    const T pr = p[r];
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[cp[k * kSlice]] - pr, sum);
+    return fma(rowsum[r], pr, sum);
+  }
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[cp[k * kSlice]], sum);
+  return sum;
+}
+
 // q = A p (SELL-32) and alpha = rz[cur] / <p, q>.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t nslices,
                                                            const int64_t* __restrict__ sptr,
                                                            const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                           const T* __restrict__ rowsum,
                                                            const T* __restrict__ p, T* __restrict__ q, int cur,
                                                            double* __restrict__ part, PcgScalars* __restrict__ sc) {
   __shared__ double red[32];
@@ -241,11 +265,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const int32_t* cp = scol + b0 + lane;
-      const T* vp = sval + b0 + lane;
-      T sum = T(0);
-#pragma unroll 4
-      for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[cp[k * kSlice]], sum);
+      const T sum = SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, p, r, rowsum);
       q[r] = sum;
       acc.add(p[r], sum);
     }
@@ -382,6 +402,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
                                                                    const int64_t* __restrict__ sptr,
                                                                    const int32_t* __restrict__ scol,
                                                                    const T* __restrict__ sval,
+                                                                   const T* __restrict__ rowsum,
                                                                    const T* __restrict__ x, const T* __restrict__ rhs,
                                                                    double* __restrict__ part,
                                                                    PcgScalars* __restrict__ sc) {
@@ -395,12 +416,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const int32_t* cp = scol + b0 + lane;
-      const T* vp = sval + b0 + lane;
-      T sum = T(0);
-#pragma unroll 4
-      for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], x[cp[k * kSlice]], sum);
-      const T t = rhs[r] - sum;
+      const T t = rhs[r] - SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum);
       acc.add(t, t);
     }
   }
@@ -459,6 +475,17 @@ __global__ void DiagKernel(int64_t rows, const int64_t* __restrict__ rp, const i
     if (!(d > 0.0)) atomicCAS(st, 0, static_cast<int>(r) + 1);
     dinv[r] = d > 0.0 ? 1.0 / d : 0.0;
     dinv32[r] = static_cast<float>(dinv[r]);
+  }
+}
+
+// s_r = sum_k a_rk in FP64 (left to right), rounded once to FP32.
+__global__ void RowSumKernel(int64_t rows, const int64_t* __restrict__ rp, const double* __restrict__ val,
+                             float* __restrict__ out) {
+  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double s = 0.0;
+    for (int64_t q = rp[r]; q < rp[r + 1]; ++q) s += val[q];
+    out[r] = static_cast<float>(s);
   }
 }
 
@@ -546,6 +573,12 @@ void PrepareSolve(lfg_csr* A) {
 
 void EnsureFloatValues(lfg_csr* A) {
   lfg_ctx* ctx = A->ctx;
+  if (!A->rowsum32.p) {
+    A->rowsum32.alloc(std::max<int64_t>(A->rows, 1) * sizeof(float), ctx->stream);
+    RowSumKernel<<<GridFor(ctx, A->rows, 256), 256, 0, ctx->stream>>>(A->rows, A->rowptr.as<int64_t>(),
+                                                                      A->val.as<double>(), A->rowsum32.as<float>());
+    LFG_LAUNCHED(ctx);
+  }
   if (!A->val32.p) {
     A->val32.alloc(std::max<int64_t>(A->nnz, 1) * sizeof(float), ctx->stream);
     ToFloatKernel<<<GridFor(ctx, A->nnz, 256), 256, 0, ctx->stream>>>(A->nnz, A->val.as<double>(),
@@ -607,7 +640,8 @@ struct PcgGraph {
 // The captured iteration body: `body` PCG iterations (even: the p buffers
 // and rz slots alternate).
 template <class T>
-PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, int body, PcgState<T>& S) {
+PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int64_t n, int body,
+                    PcgState<T>& S) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   const int spmv_blocks = static_cast<int>(std::max<int64_t>(
@@ -626,8 +660,8 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, i
     T* p = S.p.template as<T>();
     PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p, sc);
     PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
-                                                       A->sell_col.as<int32_t>(), sval, p, S.q.template as<T>(), cur,
-                                                       part, sc);
+                                                       A->sell_col.as<int32_t>(), sval, rowsum, p, S.q.template as<T>(),
+                                                       cur, part, sc);
     PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                                            S.z.template as<T>(), cur, k == body - 1, part, sc);
   }
@@ -646,8 +680,8 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, i
 // twice the recursive residual's: from there on the FP32 iterates no longer
 // improve the solution, and the FP64 refinement takes over.
 template <class T>
-int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double target_rr, int max_it,
-           int check_every, PcgState<T>& S, double& rr_out, const T* rhs = nullptr) {
+int RunPcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int64_t n, double target_rr,
+           int max_it, int check_every, PcgState<T>& S, double& rr_out, const T* rhs = nullptr) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   PcgStartKernel<T><<<S.nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
@@ -661,7 +695,7 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
     return 0;
   }
   const int body = std::max(2, check_every + (check_every & 1));
-  PcgGraph g = CapturePcg<T>(A, sval, dinv, x, n, body, S);
+  PcgGraph g = CapturePcg<T>(A, sval, rowsum, dinv, x, n, body, S);
   const int spmv_blocks = static_cast<int>(std::max<int64_t>(
       1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (A->nslices + 7) / 8)));
   try {
@@ -671,7 +705,7 @@ int RunPcg(lfg_csr* A, const T* sval, const T* dinv, T* x, int64_t n, double tar
       it += body;
       if (rhs) {
         PcgTrueResidualKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
-            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, x, rhs,
+            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, rowsum, x, rhs,
             S.part.template as<double>(), S.scal.template as<PcgScalars>());
         LFG_LAUNCHED(ctx);
         PcgScalars h{};
@@ -851,7 +885,7 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     double rr_prev = rr;
     while (true) {
       double rr_end = rr;
-      total += RunPcg<double>(A, A->sell_val.as<double>(), A->dinv.as<double>(), x, n, target, max_it - total,
+      total += RunPcg<double>(A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, n, target, max_it - total,
                               check, S64, rr_end);
       ++restarts;
       ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
@@ -888,7 +922,7 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       // inner target relative to ||r / ||r|| || = 1, never below what the outer loop needs
       const double need = std::max(inner, 0.5 * std::sqrt(target) / rnorm);
       double rr_in = 0.0;
-      const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
+      const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
                                    need * need, max_it - total, check, S32, rr_in, rhs32.as<float>());
       total += std::max(it, 1);
       AddCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), rnorm, x);
@@ -922,7 +956,7 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
       int restarts = 0;
       while (rr > target && total < max_it) {
         double rr_end = rr;
-        total += RunPcg<double>(A, A->sell_val.as<double>(), A->dinv.as<double>(), x, n, target, max_it - total,
+        total += RunPcg<double>(A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, n, target, max_it - total,
                                 check, S64, rr_end);
         ++restarts;
         ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),

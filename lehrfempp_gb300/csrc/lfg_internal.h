@@ -142,6 +142,7 @@ struct lfg_mesh {
   int64_t nonaffine_quads = -1;  // quadrilaterals that are not parallelograms (-1: not counted yet)
   lfg::DevBuf tria_list;   // int32[ntria]: cell indices of triangles (ascending)
   lfg::DevBuf quad_list;   // int32[nquad]
+  std::vector<int32_t> h_tria_list, h_quad_list;  // host copies (cell-range splits), made when first needed
 };
 
 namespace lfg {
@@ -215,6 +216,7 @@ struct lfg_csr {
   lfg::DevBuf sell_col;    // int32[sell_nnz]
   lfg::DevBuf sell_val;    // double[sell_nnz]
   lfg::DevBuf sell_val32;  // float[sell_nnz] (mixed precision, built lazily)
+  lfg::DevBuf rowsum32;    // float[rows]: FP64 row sums rounded once (the FP32 SpMV's difference form)
 };
 
 namespace lfg {

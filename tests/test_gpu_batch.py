@@ -83,3 +83,30 @@ def test_batch_solve_matches_direct_solves(ctx, precision):
     # blocks of different size take different iteration counts
     its = [blk["iterations"] for blk in st["blocks"]]
     assert max(its) > min(its)
+
+
+@pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
+def test_batch_solver_chunk_autotuner(ctx, precision):
+    """The first solve in a precision times the chunk sizes and keeps one; any
+    chunk size gives the same solution up to the order of the partial sums."""
+    ns, degs = [40, 24, 56, 33, 47, 29, 61, 38], [2, 1, 2, 2, 1, 2, 1, 2]
+    meshes, spaces, batch, alpha = _batch(ctx, ns, degs, seed=12)
+    alpha_d = ctx.to_device(alpha)
+    coo = _assemble(ctx, batch, alpha_d)
+    b = ctx.zeros(batch.num_dofs)
+    batch.assemble_vector_load(L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+    coo.fix_flagged_solution_components(batch.boundary_dof_flags(), ctx.zeros(batch.num_dofs), b)
+    csr = coo.make_sparse()
+    assert batch.solve_tuning(precision) == (0, 0.0)
+    x0 = ctx.zeros(batch.num_dofs)
+    assert batch.solve_pcg(csr, b, x0, precision=precision, rtol=1e-11)["converged"]
+    rows, rate = batch.solve_tuning(precision)
+    assert rows in (512, 1024, 2048, 4096) and rate > 0
+    ref = x0.download()
+    for rows in (96, 4096):
+        batch.set_solve_chunk_rows(precision, rows)
+        x = ctx.zeros(batch.num_dofs)
+        assert batch.solve_pcg(csr, b, x, precision=precision, rtol=1e-11)["converged"]
+        assert np.linalg.norm(x.download() - ref) <= 1e-8 * np.linalg.norm(ref)
+    with pytest.raises(L.LfgError):
+        batch.set_solve_chunk_rows(precision, 8)

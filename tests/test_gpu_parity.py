@@ -181,6 +181,27 @@ def test_fp64_route_for_out_of_range_cells(ctx, degree):
     compare_triplets(r.gpu_matrix().triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
 
 
+@pytest.mark.parametrize("chunk", [0, 1000, 77777])
+def test_assemble_to_host(ctx, chunk):
+    """AssembleMatrixLocally into host memory (cell ranges through a ring of
+    device buffers, downloads overlapping assembly): the same triplets, bit
+    for bit, as the device COO, into pinned and into pageable host memory."""
+    r = Run(ctx, W.config2(40))
+    ref = r.gpu_matrix().triplets()
+    p = L.rd_provider(W.to_coeff(ctx, r.wl["alpha"], r.keep), W.to_coeff(ctx, r.wl["gamma"], r.keep))
+    pinned = ctx.pinned((r.space.num_triplets,), L.TRIPLET_DTYPE)
+    assert L.assemble_matrix_rd_to_host(r.space, p, pinned, chunk) == len(ref)
+    bad = np.flatnonzero(pinned.array != ref)
+    assert bad.size == 0, (bad.size, bad[:5], pinned.array[bad[:3]], ref[bad[:3]])
+    host = np.zeros(r.space.num_triplets + 5, L.TRIPLET_DTYPE)
+    assert L.assemble_matrix_rd_to_host(r.space, p, host, chunk) == len(ref)
+    assert np.array_equal(host[:len(ref)], ref) and not host[len(ref):]["row"].any()
+    small = np.zeros(r.space.num_triplets - 1, L.TRIPLET_DTYPE)
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd_to_host(r.space, p, small, chunk)
+    assert e.value.code == L.CAPACITY
+
+
 def test_append_semantics(ctx):
     """AssembleMatrixLocally appends to the triplets already in the matrix."""
     r = Run(ctx, W.config1(8))
