@@ -657,7 +657,8 @@ inline double IntegrateMeshFunction(const mesh::Mesh& m, const Integrand& f, int
   return r;
 }
 
-// NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259).
+// NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259), Lagrangian or
+// hierarchic space.
 inline DeviceVector<double> NodalProjection(const uscalfe::FeSpaceLagrange& fes, uscalfe::MeshFunction u,
                                             const DeviceVector<uint8_t>* pred = nullptr) {
   DeviceVector<double> out(fes.ctx(), static_cast<size_t>(fes.NumDofs()));

@@ -81,6 +81,17 @@ lfg_status lfg_ctx_launch_count(const lfg_ctx* ctx, int64_t* launches);
  * (call once with nulls to get the count).  LFG_INVALID_ARG for a degree
  * outside [0, 100] or a null n. */
 lfg_status lfg_quad_rule(int32_t is_quad, int32_t degree, double* x, double* y, double* w, int32_t* n);
+/* EvaluationNodes and NodalValuesToDofs of FeHierarchicTria / FeHierarchicQuad
+ * (fe/hierarchic_fe.h:820-1083, 1445-1680) with interior degree
+ * interior_degree, edge degrees edge_degrees[0..3) (triangle) or [0..4)
+ * (quadrilateral), each 1..20, and relative orientations `pattern` (bit j set:
+ * local edge j negative).  The dual is linear: the dofs of a function with
+ * values v at the nodes are M v, M row-major (*n_dofs x *n_nodes); node k is
+ * (xy[2 k], xy[2 k + 1]).  These are the tables lfg_nodal_projection applies
+ * on hierarchic spaces.  Host query, same null/count protocol as
+ * lfg_quad_rule (xy and M both null: only the counts are written). */
+lfg_status lfg_hier_dual(int32_t is_quad, int32_t interior_degree, const int32_t* edge_degrees, int32_t pattern,
+                         double* xy, double* M, int32_t* n_nodes, int32_t* n_dofs);
 
 /* Device memory and copies on the context's stream (no torch needed); no
  * counterpart in the reference, whose data lives in host memory. */
@@ -631,11 +642,16 @@ lfg_status lfg_integrate_mesh_function(lfg_mesh* mesh, const lfg_integrand* inte
  * (either may be NULL). */
 lfg_status lfg_fe_eval(lfg_space* space, const double* dofs_dev, int32_t npts, const double* ref_points,
                        double* values_dev, double* grads_dev);
-/* NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259): out_dev[dof]
- * = u at the dof's evaluation node, cells selected by cell_flags_dev (NULL:
- * all) in index order; a dof shared by several selected cells takes the value
- * of the last one (the reference sets, it does not add); dofs of no selected
- * cell are 0. */
+/* NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259): per selected
+ * cell (cell_flags_dev, NULL: all) u at the cell's EvaluationNodes, mapped to
+ * dofs by its NodalValuesToDofs.  Lagrangian spaces: the identity, out_dev[dof]
+ * = u at the dof's node.  Hierarchic spaces (uniform or per-entity degrees):
+ * the dual bases of FeHierarchicTria / FeHierarchicQuad (fe/hierarchic_fe.h:
+ * 820-1083, 1445-1680; the tables of lfg_hier_dual), FP64.  Cells are taken in
+ * index order; a dof shared by several selected cells takes the value of the
+ * last one (the reference sets, it does not add); dofs of no selected cell
+ * are 0.  Per-entity degree spaces whose distinct (type, degrees,
+ * orientation) combinations need more than 1 GiB of tables: LFG_UNSUPPORTED. */
 lfg_status lfg_nodal_projection(lfg_space* space, const lfg_coeff* u, const uint8_t* cell_flags_dev,
                                 double* out_dev);
 /* InitEssentialConditionFromFunction(fes, esscondflag, g) (fe/fe_tools.h:263-329):

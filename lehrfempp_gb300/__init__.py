@@ -621,6 +621,24 @@ def quad_rule(is_quad, degree):
     return x, y, w
 
 
+def hier_dual(is_quad, interior_degree, edge_degrees, pattern):
+    """EvaluationNodes and NodalValuesToDofs of FeHierarchicTria / Quad
+    (lib/lf/fe/hierarchic_fe.h:820-1083, 1445-1680) as the library tabulates
+    them: nodes (ne, 2) and M (n, ne) with dofs = M @ values.  `pattern` bit j
+    set: local edge j negatively oriented.  Host-only; no device needed."""
+    pe = np.ascontiguousarray(list(edge_degrees) + [1] * (4 - len(edge_degrees)), np.int32)
+    ne, n = C.c_int32(0), C.c_int32(0)
+    args = (int(is_quad), int(interior_degree), _p(pe, C.c_int32), int(pattern))
+    rc = lib().lfg_hier_dual(*args, None, None, C.byref(ne), C.byref(n))
+    if rc != OK:
+        raise LfgError(rc, "lfg_hier_dual(%d, %d, %s, %d) failed" % (int(is_quad), interior_degree, list(pe), pattern))
+    xy, M = np.zeros((ne.value, 2)), np.zeros((n.value, ne.value))
+    rc = lib().lfg_hier_dual(*args, _p(xy, C.c_double), _p(M, C.c_double), C.byref(ne), C.byref(n))
+    if rc != OK:
+        raise LfgError(rc, "lfg_hier_dual failed")
+    return xy, M
+
+
 def rd_provider(alpha, gamma, qr_degree_tria=0, qr_degree_quad=0):
     p = lfg_rd_provider()
     p.alpha, p.gamma = alpha, gamma

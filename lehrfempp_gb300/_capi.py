@@ -82,6 +82,7 @@ SIGNATURES = {
     "lfg_profile_reset": (c_status, [vp]),
     "lfg_measure_fp64_peak": (c_status, [vp, P(dbl)]),
     "lfg_quad_rule": (c_status, [i32, i32, P(dbl), P(dbl), P(dbl), P(i32)]),
+    "lfg_hier_dual": (c_status, [i32, i32, P(i32), i32, P(dbl), P(dbl), P(i32), P(i32)]),
     "lfg_ctx_set_tensor_cores": (c_status, [vp, i32]),
     "lfg_mesh_create": (c_status, [vp, i64, P(dbl), i64, P(i32), i64, P(i32), P(vp)]),
     "lfg_mesh_create_tp_triag": (c_status, [vp, i64, i64, dbl, dbl, dbl, dbl, P(vp)]),

@@ -18,6 +18,7 @@
 #include "lfg_api.h"
 #include "lfg_coeff.h"
 #include "lfg_internal.h"
+#include "lfg_tables.h"
 
 namespace lfg {
 namespace {
@@ -433,6 +434,76 @@ __global__ void ProjectKernel(PostArgs a, int64_t nc, NodeSet ns, const int32_t*
   }
 }
 
+// owner[dof] = max selected cell holding it, local counts from loc_offset
+// (hierarchic spaces, whose counts may vary by cell).
+__global__ void ProjectOwnerLocKernel(int64_t nc, const uint8_t* __restrict__ flags,
+                                      const int32_t* __restrict__ cell_dofs, int n_cell,
+                                      const int64_t* __restrict__ loc_offset, int32_t* __restrict__ owner) {
+  for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; c < nc;
+       c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (flags && !flags[c]) continue;
+    const int n = static_cast<int>(loc_offset[c + 1] - loc_offset[c]);
+    for (int j = 0; j < n; ++j) atomicMax(&owner[cell_dofs[c * n_cell + j]], static_cast<int32_t>(c));
+  }
+}
+
+// One dual table of a hierarchic cell kind: evaluation nodes xy[2 ne] at
+// off_xy, the NodalValuesToDofs matrix M[n][ne] at off_M (doubles into one
+// table buffer).
+struct HierDualDir {
+  int64_t off_xy, off_M;
+  int32_t ne, n;
+};
+constexpr int kHierProjWarps = 4;
+
+// NodalProjection on a hierarchic space: one warp per cell.  The lanes
+// evaluate u at the cell's evaluation nodes into shared memory, then each
+// lane forms the dofs it owns as a row of M times those values (k ascending).
+// The cell's table is tid[c], or (tid null: uniform degree) its orientation
+// pattern, quadrilaterals after the 8 triangle patterns.
+__global__ void __launch_bounds__(32 * kHierProjWarps)
+    HierProjectKernel(PostArgs a, int64_t nc, const HierDualDir* __restrict__ dir, const double* __restrict__ tab,
+                      const int32_t* __restrict__ tid, const uint8_t* __restrict__ ori, int ne_max,
+                      const int32_t* __restrict__ owner, double* __restrict__ out) {
+  extern __shared__ __align__(16) double sv[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* v = sv + warp * ne_max;
+  for (int64_t c = blockIdx.x * static_cast<int64_t>(kHierProjWarps) + warp; c < nc;
+       c += static_cast<int64_t>(gridDim.x) * kHierProjWarps) {
+    if (a.flags && !a.flags[c]) continue;
+    const bool quad = a.cells[c].w >= 0;
+    const int t = tid ? tid[c] : (quad ? 8 + (ori[c] & 15) : (ori[c] & 7));
+    const HierDualDir T = dir[t];
+    int4 cn;
+    double2 vx[4];
+    double JT[2][2];
+    double gx, gy, X, Y, ie;
+    if (quad) LoadCell<true>(a, static_cast<int>(c), cn, vx);
+    else LoadCell<false>(a, static_cast<int>(c), cn, vx);
+    const double* xy = tab + T.off_xy;
+    for (int k = lane; k < T.ne; k += 32) {
+      const double xh = xy[2 * k], yh = xy[2 * k + 1];
+      if (quad) {
+        Geometry<true>(vx, xh, yh, X, Y, ie, JT);
+        v[k] = MFPoint<true>(a.u, static_cast<int>(c), cn, xh, yh, X, Y, JT, false, gx, gy);
+      } else {
+        Geometry<false>(vx, xh, yh, X, Y, ie, JT);
+        v[k] = MFPoint<false>(a.u, static_cast<int>(c), cn, xh, yh, X, Y, JT, false, gx, gy);
+      }
+    }
+    __syncwarp();
+    for (int j = lane; j < T.n; j += 32) {
+      const int32_t d = a.cell_dofs[c * a.n_cell + j];
+      if (owner[d] != c) continue;
+      const double* Mr = tab + T.off_M + static_cast<int64_t>(j) * T.ne;
+      double sum = 0.0;
+      for (int k = 0; k < T.ne; ++k) sum = fma(Mr[k], v[k], sum);
+      out[d] = sum;
+    }
+    __syncwarp();
+  }
+}
+
 __global__ void EssentialOwnerKernel(EdgeSide s, const uint8_t* __restrict__ flags, int32_t* __restrict__ owner) {
   for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < s.ne;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -523,6 +594,83 @@ EdgeSide BaseEdgeSide(lfg_mesh* m, const lfg_space* sp) {
     s.node_dofs = m->nv * sp->np;
   }
   return s;
+}
+
+// Dual tables of a hierarchic space and the table of every cell.  Uniform
+// degree: the 8 triangle and 16 quadrilateral orientation patterns (tid
+// stays empty).  Per-entity degrees: one table per distinct (type, interior
+// degree, edge degrees, pattern) among the cells, found on the host.
+struct HierDualSet {
+  std::vector<HierDualDir> dir;
+  std::vector<double> tab;
+  std::vector<int32_t> tid;
+  int ne_max = 0;
+};
+
+void AddHierDual(HierDualSet& H, bool quad, int pc, const int* pe, int pat) {
+  std::vector<double> xy, M;
+  HierDual(quad, pc, pe, pat, xy, M);
+  HierDualDir d{};
+  d.ne = static_cast<int32_t>(xy.size() / 2);
+  d.n = static_cast<int32_t>(d.ne ? M.size() / d.ne : 0);
+  d.off_xy = static_cast<int64_t>(H.tab.size());
+  H.tab.insert(H.tab.end(), xy.begin(), xy.end());
+  d.off_M = static_cast<int64_t>(H.tab.size());
+  H.tab.insert(H.tab.end(), M.begin(), M.end());
+  H.dir.push_back(d);
+  H.ne_max = std::max(H.ne_max, static_cast<int>(d.ne));
+}
+
+constexpr size_t kMaxHierDualTableBytes = size_t(1) << 30;
+
+void BuildHierDuals(lfg_space* sp, HierDualSet& H) {
+  lfg_mesh* m = sp->mesh;
+  if (!sp->hier_var) {
+    const int p = sp->hier_degree;
+    const int pe[4] = {p, p, p, p};
+    for (int q = 0; q < 2; ++q)
+      for (int pat = 0; pat < (q ? 16 : 8); ++pat) {
+        if ((q ? m->nquad : m->ntria) == 0) {
+          H.dir.push_back(HierDualDir{0, 0, 0, 0});
+          continue;
+        }
+        AddHierDual(H, q == 1, p, pe, pat);
+      }
+    return;
+  }
+  const int64_t nc = m->nc;
+  std::vector<int4> cn(nc), ce(nc);
+  std::vector<uint8_t> ori(nc);
+  D2HSync(m->ctx, cn.data(), m->cell_nodes.p, nc * sizeof(int4));
+  D2HSync(m->ctx, ce.data(), m->cell_edges.p, nc * sizeof(int4));
+  D2HSync(m->ctx, ori.data(), m->cell_ori.p, nc);
+  const auto& ed = sp->hv_edge_deg_host;
+  H.tid.resize(nc);
+  std::vector<std::pair<uint64_t, int32_t>> seen;  // sorted (key, table)
+  for (int64_t c = 0; c < nc; ++c) {
+    const bool quad = cn[c].w >= 0;
+    const int nv = quad ? 4 : 3;
+    const int e[4] = {ce[c].x, ce[c].y, ce[c].z, ce[c].w};
+    int pe[4] = {1, 1, 1, 1};
+    const int pc = sp->hv_cell_deg_host[c];
+    const int pat = ori[c] & (quad ? 15 : 7);
+    uint64_t key = (quad ? 1ull : 0ull) << 40 | static_cast<uint64_t>(pc) << 32 | static_cast<uint64_t>(pat) << 24;
+    for (int j = 0; j < nv; ++j) {
+      pe[j] = ed[e[j]];
+      key |= static_cast<uint64_t>(pe[j]) << (6 * j);
+    }
+    auto it = std::lower_bound(seen.begin(), seen.end(), std::make_pair(key, int32_t(-1)));
+    if (it != seen.end() && it->first == key) {
+      H.tid[c] = it->second;
+      continue;
+    }
+    const int32_t id = static_cast<int32_t>(H.dir.size());
+    AddHierDual(H, quad, pc, pe, pat);
+    if (H.tab.size() * sizeof(double) > kMaxHierDualTableBytes)
+      Fail(LFG_UNSUPPORTED, "NodalProjection: the dual tables of this space's degree combinations exceed 1 GiB");
+    seen.insert(it, std::make_pair(key, id));
+    H.tid[c] = id;
+  }
 }
 
 void RequireLagrange(const lfg_space* sp, const char* what) {
@@ -683,6 +831,47 @@ lfg_status lfg_nodal_projection(lfg_space* sp, const lfg_coeff* u, const uint8_t
   LFG_API_BEGIN(sp->mesh->ctx)
   lfg_ctx* ctx = sp->mesh->ctx;
   lfg_mesh* m = sp->mesh;
+  if (sp->hier_degree > 0) {
+    PostArgs a = BasePostArgs(m, *u, "NodalProjection");
+    a.flags = cell_flags;
+    a.cell_dofs = sp->cell_dofs.as<int32_t>();
+    a.n_cell = sp->n_cell;
+    ProfScope prof(ctx, "nodal_projection_hier");
+    LFG_CUDA(cudaMemsetAsync(out, 0, sp->num_dofs * sizeof(double), ctx->stream));
+    if (m->nc == 0 || sp->num_dofs == 0) return LFG_OK;
+    HierDualSet H;
+    BuildHierDuals(sp, H);
+    DevBuf dir, tab, tid, owner;
+    dir.alloc(H.dir.size() * sizeof(HierDualDir), ctx->stream);
+    tab.alloc(std::max<size_t>(H.tab.size(), 1) * sizeof(double), ctx->stream);
+    LFG_CUDA(cudaMemcpyAsync(dir.p, H.dir.data(), H.dir.size() * sizeof(HierDualDir), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    LFG_CUDA(cudaMemcpyAsync(tab.p, H.tab.data(), H.tab.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (!H.tid.empty()) {
+      tid.alloc(H.tid.size() * sizeof(int32_t), ctx->stream);
+      LFG_CUDA(cudaMemcpyAsync(tid.p, H.tid.data(), H.tid.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               ctx->stream));
+    }
+    owner.alloc(sp->num_dofs * sizeof(int32_t), ctx->stream);
+    FillI32Kernel<<<GridFor(ctx, sp->num_dofs, 256), 256, 0, ctx->stream>>>(sp->num_dofs, -1, owner.as<int32_t>());
+    LFG_LAUNCHED(ctx);
+    ProjectOwnerLocKernel<<<GridFor(ctx, m->nc, 256), 256, 0, ctx->stream>>>(
+        m->nc, cell_flags, a.cell_dofs, sp->n_cell, sp->loc_offset.as<int64_t>(), owner.as<int32_t>());
+    LFG_LAUNCHED(ctx);
+    const size_t smem = static_cast<size_t>(kHierProjWarps) * std::max(H.ne_max, 1) * sizeof(double);
+    if (smem > 48 * 1024)
+      LFG_CUDA(cudaFuncSetAttribute(HierProjectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+    const int64_t blocks = std::min<int64_t>((m->nc + kHierProjWarps - 1) / kHierProjWarps,
+                                             static_cast<int64_t>(ctx->num_sms) * 16);
+    HierProjectKernel<<<static_cast<int>(blocks), 32 * kHierProjWarps, smem, ctx->stream>>>(
+        a, m->nc, dir.as<HierDualDir>(), tab.as<double>(), H.tid.empty() ? nullptr : tid.as<int32_t>(),
+        m->cell_ori.as<uint8_t>(), std::max(H.ne_max, 1), owner.as<int32_t>(), out);
+    LFG_LAUNCHED(ctx);
+    // the host tables must outlive their (pageable, possibly deferred) copies
+    LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LFG_OK;
+  }
   RequireLagrange(sp, "NodalProjection");
   PostArgs a = BasePostArgs(m, *u, "NodalProjection");
   a.flags = cell_flags;

@@ -3,6 +3,7 @@
 // device.  Only these tables reach the GPU (lf::quad and the reference finite
 // elements are set-up work in the reference too:
 // uscalfe/precomputed_scalar_reference_finite_element.h:43-184).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -580,6 +581,217 @@ bool SegmentTables(int degree, int rule_degree, std::vector<double>& t, std::vec
   return true;
 }
 
+namespace {
+// P_n^{(a,b)}(2x - 1) by the three-term recurrence of the Jacobi polynomials
+// (Abramowitz & Stegun 22.7.1).
+ld JacobiAB(int n, ld a, ld b, ld x) {
+  const ld z = 2.0L * x - 1.0L;
+  ld p0 = 1.0L;
+  if (n == 0) return p0;
+  ld p1 = (a + 1.0L) + 0.5L * (a + b + 2.0L) * (z - 1.0L);
+  for (int k = 2; k <= n; ++k) {
+    const ld c = 2.0L * k + a + b;
+    const ld p2 = ((c - 1.0L) * (c * (c - 2.0L) * z + a * a - b * b) * p1 -
+                   2.0L * (k + a - 1.0L) * (k + b - 1.0L) * c * p0) /
+                  (2.0L * k * (k + a + b) * (c - 2.0L));
+    p0 = p1;
+    p1 = p2;
+  }
+  return p1;
+}
+
+// d/dx P_n(2x - 1) of the shifted Legendre polynomial (n >= 0).
+ld LegendreDx01(int n, ld x) {
+  if (n == 0) return 0.0L;
+  ld P[64];
+  ScaledLegendre(n, x, 1.0L, P);
+  // P_n'(z) = sum_{k = n-1, n-3, ...} (2k + 1) P_k(z), and dz/dx = 2
+  ld s = 0.0L;
+  for (int k = n - 1; k >= 0; k -= 2) s += (2.0L * k + 1.0L) * P[k];
+  return 2.0L * s;
+}
+
+// Rows of the segment dual of degree d (FeHierarchicSegment::NodalValuesToDofs,
+// hierarchic_fe.h:367-390) for i = 2..d: the coefficients on the value at 0,
+// at 1 and at the Gauss points t of the segment rule of degree 2(d - 1).
+struct SegDual {
+  std::vector<double> t;        // d points
+  std::vector<double> c0, c1;   // [i - 2]
+  std::vector<double> cq;       // [(i - 2) * d + q]
+};
+SegDual MakeSegDual(int d) {
+  SegDual S;
+  std::vector<double> w;
+  GaussLegendre01(d, S.t, w);  // 2(d - 1) / 2 + 1 = d points
+  for (int i = 2; i <= d; ++i) {
+    const ld f = 2.0L * i - 1.0L;
+    ld P[64];
+    ScaledLegendre(i - 1, 0.0L, 1.0L, P);
+    const ld p0 = P[i - 1];
+    ScaledLegendre(i - 1, 1.0L, 1.0L, P);
+    const ld p1 = P[i - 1];
+    S.c0.push_back(static_cast<double>(-p0 * f));
+    S.c1.push_back(static_cast<double>(p1 * f));
+    for (int q = 0; q < d; ++q)
+      S.cq.push_back(static_cast<double>(-static_cast<ld>(w[q]) * LegendreDx01(i - 1, S.t[q]) * f));
+  }
+  return S;
+}
+}  // namespace
+
+int HierNumShapeVar(bool is_quad, int pc, const int* pe) {
+  const int nv = is_quad ? 4 : 3;
+  int n = nv;
+  for (int j = 0; j < nv; ++j) n += pe[j] - 1;
+  return n + (is_quad ? (pc - 1) * (pc - 1) : (pc - 1) * (pc - 2) / 2);
+}
+
+void HierVarSlots(bool is_quad, int pc, const int* pe, int pat, int D, int* sel) {
+  const int nv = is_quad ? 4 : 3;
+  int k = 0;
+  for (int j = 0; j < nv; ++j) sel[k++] = j;
+  for (int j = 0; j < nv; ++j) {
+    const int ns = pe[j] - 1, ub = nv + j * (D - 1);
+    const bool neg = (pat >> j) & 1;
+    for (int a = 0; a < ns; ++a) sel[k++] = ub + (neg ? D - 1 - ns + a : a);
+  }
+  const int ub = nv * D;
+  if (is_quad) {
+    for (int i = 0; i < pc - 1; ++i)
+      for (int jj = 0; jj < pc - 1; ++jj) sel[k++] = ub + i * (D - 1) + jj;
+  } else {
+    for (int i = 0; i < pc - 2; ++i)
+      for (int jj = 0; jj < pc - 2 - i; ++jj) sel[k++] = ub + i * (D - 2) - i * (i - 1) / 2 + jj;
+  }
+}
+
+void HierDual(bool is_quad, int pc, const int* pe, int pat, std::vector<double>& xy, std::vector<double>& M) {
+  const int nv = is_quad ? 4 : 3;
+  const int n = HierNumShapeVar(is_quad, pc, pe);
+  xy.clear();
+  auto add = [&](double x, double y) {
+    xy.push_back(x);
+    xy.push_back(y);
+  };
+  // vertices, then the Gauss points of every edge of degree >= 2 in the edge's
+  // own direction (hierarchic_fe.h:835-873, 1470-1515)
+  const double vx[4] = {0, 1, is_quad ? 1.0 : 0.0, 0}, vy[4] = {0, 0, 1, 1};
+  for (int j = 0; j < nv; ++j) add(vx[j], vy[j]);
+  std::vector<SegDual> ed(nv);
+  std::vector<int> ecol(nv, 0);
+  for (int j = 0; j < nv; ++j) {
+    if (pe[j] <= 1) continue;
+    ed[j] = MakeSegDual(pe[j]);
+    ecol[j] = static_cast<int>(xy.size() / 2);
+    const int a = j, b = (j + 1) % nv;
+    const bool neg = (pat >> j) & 1;
+    for (double u : ed[j].t) {
+      // the edge runs from local vertex a to b; a negative one is parametrised from b
+      const double s = neg ? 1.0 - u : u;
+      add(vx[a] + s * (vx[b] - vx[a]), vy[a] + s * (vy[b] - vy[a]));
+    }
+  }
+  const int icol = static_cast<int>(xy.size() / 2);
+  Rule tr;
+  SegDual fd;
+  int D = pc, nq1 = 0;
+  if (!is_quad) {
+    MakeRule(false, 2 * (pc - 1), tr);  // always part of the nodes (hierarchic_fe.h:874-876)
+    for (int q = 0; q < tr.n; ++q) add(tr.x[q], tr.y[q]);
+  } else if (pc > 1) {
+    for (int j = 0; j < nv; ++j) D = std::max(D, pe[j]);
+    fd = MakeSegDual(D);
+    nq1 = D + 2;
+    std::vector<double> pts = {0.0, 1.0};
+    pts.insert(pts.end(), fd.t.begin(), fd.t.end());
+    for (int r = 0; r < nq1; ++r)
+      for (int k = 0; k < nq1; ++k) add(pts[k], pts[r]);
+  }
+  const int ne = static_cast<int>(xy.size() / 2);
+  M.assign(static_cast<size_t>(n) * ne, 0.0);
+  auto at = [&](int row, int col) -> double& { return M[static_cast<size_t>(row) * ne + col]; };
+  for (int j = 0; j < nv; ++j) at(j, j) = 1.0;
+  // edge dofs: the segment dual along the edge; a negative edge's slots are
+  // reversed and its start is local vertex b
+  int slot = nv;
+  for (int j = 0; j < nv; ++j) {
+    const int pj = pe[j];
+    if (pj <= 1) continue;
+    const bool neg = (pat >> j) & 1;
+    const int va = neg ? (j + 1) % nv : j, vb = neg ? j : (j + 1) % nv;
+    for (int i = 2; i <= pj; ++i) {
+      const int row = slot + (neg ? pj - i : i - 2);
+      at(row, va) += ed[j].c0[i - 2];
+      at(row, vb) += ed[j].c1[i - 2];
+      for (int q = 0; q < pj; ++q) at(row, ecol[j] + q) += ed[j].cq[static_cast<size_t>(i - 2) * pj + q];
+    }
+    slot += pj - 1;
+  }
+  const int nb = slot;
+  if (is_quad) {
+    // interior: the degree-D segment dual along x on every node row, then
+    // along y (hierarchic_fe.h:1640-1665); dof (a, b) at slot a + b (pc - 1)
+    if (pc <= 1) return;
+    auto S = [&](int i, int node) -> double {  // row i >= 2 of the segment dual, node 0 / 1 / 2 + q
+      return node == 0 ? fd.c0[i - 2] : node == 1 ? fd.c1[i - 2] : fd.cq[static_cast<size_t>(i - 2) * D + node - 2];
+    };
+    const int m = pc - 1;
+    for (int b = 0; b < m; ++b)
+      for (int a = 0; a < m; ++a) {
+        const int row = nb + a + b * m;
+        for (int r = 0; r < nq1; ++r) {
+          const double sy = S(b + 2, r);
+          for (int k = 0; k < nq1; ++k) at(row, icol + r * nq1 + k) = sy * S(a + 2, k);
+        }
+      }
+    return;
+  }
+  if (pc <= 2) return;
+  // triangle interior (hierarchic_fe.h:1024-1083): F v with the integrated
+  // Legendre / Jacobi duals over the interior rule, then orthogonalised
+  // against the vertex and edge duals: M_face = F - (F Phi_b^T) M_b, Phi_b
+  // the boundary shape functions at the nodes (hierarchic_fe.h:891-915)
+  const int nf = n - nb;
+  std::vector<double> F(static_cast<size_t>(nf) * ne, 0.0);
+  {
+    int idx = 0;
+    for (int i = 0; i < pc - 2; ++i)
+      for (int j = 0; j < pc - i - 2; ++j, ++idx) {
+        const ld a = 2.0L * i + 4.0L, f = (2.0L * i + 3.0L) * (2.0L * j + 2.0L * i + 5.0L);
+        for (int q = 0; q < tr.n; ++q) {
+          const ld x = tr.x[q], y = tr.y[q];
+          ld xn = x / (1.0L - y);
+          if (pat & 1) xn = 1.0L - xn;
+          const ld psidd = LegendreDx01(i + 1, xn);
+          const ld jdd = j == 0 ? 0.0L : JacobiAB(j - 1, a + 1.0L, 1.0L, y) * (a + j + 1.0L);
+          const ld jd = JacobiAB(j, a, 0.0L, y);
+          const ld term = std::pow(1.0L - y, i + 1) * jdd - a * std::pow(1.0L - y, i) * jd;
+          F[static_cast<size_t>(idx) * ne + icol + q] = static_cast<double>(tr.w[q] * psidd * term * f);
+        }
+      }
+  }
+  D = pc;
+  for (int j = 0; j < nv; ++j) D = std::max(D, pe[j]);
+  const int nD = (D + 1) * (D + 2) / 2;
+  std::vector<int> sel(n);
+  HierVarSlots(false, pc, pe, pat, D, sel.data());
+  std::vector<double> phi(nD), dphi(2 * nD);
+  std::vector<long double> G(static_cast<size_t>(nf) * nb, 0.0L);  // F Phi_b^T
+  for (int k = icol; k < ne; ++k) {  // F is zero outside the interior nodes
+    HierShape(false, D, pat, xy[2 * k], xy[2 * k + 1], phi.data(), reinterpret_cast<double(*)[2]>(dphi.data()));
+    for (int r = 0; r < nf; ++r) {
+      const ld fr = F[static_cast<size_t>(r) * ne + k];
+      for (int a = 0; a < nb; ++a) G[static_cast<size_t>(r) * nb + a] += fr * phi[sel[a]];
+    }
+  }
+  for (int r = 0; r < nf; ++r)
+    for (int k = 0; k < ne; ++k) {
+      ld s = F[static_cast<size_t>(r) * ne + k];
+      for (int a = 0; a < nb; ++a) s -= G[static_cast<size_t>(r) * nb + a] * at(a, k);
+      at(nb + r, k) = static_cast<double>(s);
+    }
+}
+
 }  // namespace lfg
 
 extern "C" lfg_status lfg_quad_rule(int32_t is_quad, int32_t degree, double* x, double* y, double* w, int32_t* n) {
@@ -593,5 +805,29 @@ extern "C" lfg_status lfg_quad_rule(int32_t is_quad, int32_t degree, double* x, 
     std::memcpy(w, r.w.data(), r.n * sizeof(double));
   }
   *n = r.n;
+  return LFG_OK;
+}
+
+extern "C" lfg_status lfg_hier_dual(int32_t is_quad, int32_t interior_degree, const int32_t* edge_degrees,
+                                    int32_t pattern, double* xy, double* M, int32_t* n_nodes, int32_t* n_dofs) {
+  if (!edge_degrees || !n_nodes || !n_dofs) return LFG_INVALID_ARG;
+  const int nv = is_quad ? 4 : 3;
+  int pe[4] = {1, 1, 1, 1};
+  if (interior_degree < 1 || interior_degree > lfg::kMaxHierDualDegree) return LFG_INVALID_ARG;
+  for (int j = 0; j < nv; ++j) {
+    if (edge_degrees[j] < 1 || edge_degrees[j] > lfg::kMaxHierDualDegree) return LFG_INVALID_ARG;
+    pe[j] = edge_degrees[j];
+  }
+  if (pattern < 0 || pattern >= (1 << nv)) return LFG_INVALID_ARG;
+  std::vector<double> nodes, m;
+  lfg::HierDual(is_quad != 0, interior_degree, pe, pattern, nodes, m);
+  const int ne = static_cast<int>(nodes.size() / 2), n = lfg::HierNumShapeVar(is_quad != 0, interior_degree, pe);
+  if (xy || M) {
+    if (!xy || !M || *n_nodes < ne || *n_dofs < n) return LFG_INVALID_ARG;
+    std::memcpy(xy, nodes.data(), nodes.size() * sizeof(double));
+    std::memcpy(M, m.data(), m.size() * sizeof(double));
+  }
+  *n_nodes = ne;
+  *n_dofs = n;
   return LFG_OK;
 }

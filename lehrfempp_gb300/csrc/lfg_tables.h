@@ -31,6 +31,19 @@ void Shape(bool is_quad, int degree, double x, double y, double* phi, double (*d
 // the triangle's interior functions follow edge 0's direction.  Counts equal
 // the Lagrangian ones, (p+1)(p+2)/2 and (p+1)^2.
 void HierShape(bool is_quad, int p, int pattern, double x, double y, double* phi, double (*dphi)[2]);
+// Variable degrees (HierarchicScalarFESpace with a degree functor): a cell
+// with interior degree pc and edge degrees pe[0..nvert) has
+// HierNumShapeVar(...) shape functions, which are the slots sel[0..n) of the
+// uniform degree-D basis (D >= pc and every pe), same pattern convention.
+int HierNumShapeVar(bool is_quad, int pc, const int* pe);
+void HierVarSlots(bool is_quad, int pc, const int* pe, int pattern, int D, int* sel);
+// EvaluationNodes and NodalValuesToDofs of FeHierarchicTria / FeHierarchicQuad
+// (fe/hierarchic_fe.h:820-1083, 1445-1680) with interior degree pc, edge
+// degrees pe and orientation pattern `pattern`, in matrix form: xy[2 k],
+// xy[2 k + 1] is evaluation node k, and the dofs of a function with values v
+// at the nodes are M v (M row-major, HierNumShapeVar rows x node count).
+constexpr int kMaxHierDualDegree = 20;
+void HierDual(bool is_quad, int pc, const int* pe, int pattern, std::vector<double>& xy, std::vector<double>& M);
 // Integrated Legendre function of the segment element: L_n(t) = int_0^t P_{n-1}(2s-1) ds
 // for n >= 2 (FeHierarchicSegment's shape function n), and its derivative.
 double HierSegment(int n, double t, double* dt);

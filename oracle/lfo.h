@@ -317,6 +317,17 @@ int HierNumShapeVar(bool is_quad, int pc, const int* pe);
 // rule of degree 2 max(pc, pe[j], 1) (2 * Degree(), loc_comp_ellbvp.h:186).
 void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, const MeshFunction& gamma,
                         int qdeg, COOMatrix& A);
+// EvaluationNodes / NodalValuesToDofs of FeHierarchicTria / FeHierarchicQuad
+// (hierarchic_fe.h:820-1083, 1445-1665) for interior degree pc, edge degrees
+// pe and relative orientations ori; and fe::NodalProjection (fe_tools.h:
+// 198-259) on a hierarchic space (p: the uniform degree, or 0 for a
+// variable-degree dof handler): a shared dof takes the last selected cell's
+// value.
+void HierEvaluationNodes(bool is_quad, int pc, const int* pe, const int8_t* ori, std::vector<double>& xy);
+void HierNodalValuesToDofs(bool is_quad, int pc, const int* pe, const int8_t* ori, const std::vector<double>& v,
+                           std::vector<double>& dofs);
+void NodalProjectionHier(const DofHandler& dh, int p, const MeshFunction& u, const uint8_t* cell_flags,
+                         std::vector<double>& out);
 void AssembleHierLoad(const DofHandler& dh, int p, const MeshFunction& f, int qdeg, std::vector<double>& b);
 
 }  // namespace lfo

@@ -405,6 +405,45 @@ int lfo_nodal_projection_mf(void* sp, const lfo_coeff* u, const uint8_t* cell_fl
   LFO_CATCH
 }
 
+// FeHierarchicTria / Quad dual: the evaluation nodes (xy[2 k], xy[2 k + 1])
+// and M (n x ne, row-major) with M[:, k] = NodalValuesToDofs(e_k).  With xy
+// null only the counts are written.
+int lfo_hier_dual(int is_quad, int pc, const int32_t* pe, const int8_t* ori, double* xy, double* M, int* ne, int* n,
+                  char* err, int errlen) {
+  LFO_TRY
+  int pv[4] = {pe[0], pe[1], pe[2], is_quad ? pe[3] : 1};
+  std::vector<double> nodes;
+  HierEvaluationNodes(is_quad != 0, pc, pv, ori, nodes);
+  const int nn = static_cast<int>(nodes.size() / 2), nd = HierNumShapeVar(is_quad != 0, pc, pv);
+  if (xy) {
+    std::memcpy(xy, nodes.data(), nodes.size() * sizeof(double));
+    std::vector<double> v(nn, 0.0), d;
+    for (int k = 0; k < nn; ++k) {
+      v[k] = 1.0;
+      HierNodalValuesToDofs(is_quad != 0, pc, pv, ori, v, d);
+      for (int r = 0; r < nd; ++r) M[static_cast<size_t>(r) * nn + k] = d[r];
+      v[k] = 0.0;
+    }
+  }
+  *ne = nn;
+  *n = nd;
+  LFO_CATCH
+}
+
+// fe::NodalProjection on a hierarchic space (uniform degree p, or p = 0 for a
+// space made by lfo_space_create_hier_var).
+int lfo_nodal_projection_hier(void* sp, int p, const lfo_coeff* u, const uint8_t* cell_flags, double* out, char* err,
+                              int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  const MeshFunction mf = ToMF(u, u && u->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  std::vector<double> v;
+  NodalProjectionHier(s->dh, p, mf, cell_flags, v);
+  std::memcpy(out, v.data(), v.size() * sizeof(double));
+  LFO_CATCH
+}
+
 int lfo_init_essential(void* sp, const uint8_t* edge_flags, const lfo_coeff* g, uint8_t* flags, double* vals,
                        char* err, int errlen) {
   LFO_TRY

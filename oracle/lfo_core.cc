@@ -1514,6 +1514,207 @@ void HierCellData(const DofHandler& dh, idx_t c, int p, int qdeg, std::vector<do
 }
 }  // namespace
 
+// ---- NodalProjection on hierarchic spaces (fe/fe_tools.h:198-259 with the
+// EvaluationNodes / NodalValuesToDofs of FeHierarchicSegment, FeHierarchicTria
+// and FeHierarchicQuad, hierarchic_fe.h:330-390, 820-1060, 1445-1680).
+namespace {
+// LegendreDx / JacobiDx / IJacobiDx of hierarchic_fe.cc:53-60, 170-185 (t = 1).
+double HLegendreDx(unsigned n, double x) {
+  if (n == 0) return 0.0;
+  return 2.0 * n * HierLegendre(n - 1, x) + (2.0 * x - 1.0) * HLegendreDx(n - 1, x);
+}
+double HJacobiDx(unsigned n, double alpha, double x) {
+  if (n == 0) return 0.0;
+  return HierJacobi(n - 1, alpha + 1, 1, x) * (alpha + n + 1);
+}
+double HIJacobiDx(unsigned n, double alpha, double x) { return HierJacobi(n - 1, alpha, 0, x); }
+
+// The segment rule of degree d (make_quad_rule.cc:22-27): Gauss-Legendre
+// with d/2 + 1 points on [0, 1].
+void SegmentRule(int d, std::vector<double>& t, std::vector<double>& w) { GaussLegendre(d / 2 + 1, t, w); }
+
+// FeHierarchicSegment(p)::NodalValuesToDofs (hierarchic_fe.h:367-390):
+// values at 0, 1 and the points of the segment rule of degree 2(p-1).
+void SegmentValuesToDofs(int p, const double* v, double* dofs) {
+  std::vector<double> t, w;
+  SegmentRule(2 * (p - 1), t, w);
+  dofs[0] = v[0];
+  dofs[1] = v[1];
+  for (int i = 2; i <= p; ++i) {
+    const double P0 = HierILegendreDx(i, 0.0), P1 = HierILegendreDx(i, 1.0);
+    double integ = 0.0;
+    for (size_t q = 0; q < t.size(); ++q) integ += w[q] * HLegendreDx(i - 1, t[q]) * v[2 + q];
+    dofs[i] = (P1 * v[1] - P0 * v[0] - integ) * (2 * i - 1);
+  }
+}
+
+// Edge dofs of one local edge (degree pe >= 2) from the values at its two
+// end vertices (va: start of the local edge, vb: its end) and at its rule
+// points, written in the cell's slots: positive orientation in order,
+// negative reversed (hierarchic_fe.h:938-1017, 1560-1637).
+void EdgeValuesToDofs(int pe, bool positive, double va, double vb, const double* vals, double* out) {
+  std::vector<double> t, w;
+  SegmentRule(2 * (pe - 1), t, w);
+  for (int i = 2; i <= pe; ++i) {
+    const double P0 = HierILegendreDx(i, 0.0), P1 = HierILegendreDx(i, 1.0);
+    double integ = 0.0;
+    for (size_t q = 0; q < t.size(); ++q) integ += w[q] * HLegendreDx(i - 1, t[q]) * vals[q];
+    if (positive) out[i - 2] = (P1 * vb - P0 * va - integ) * (2 * i - 1);
+    else out[pe - i] = (P1 * va - P0 * vb - integ) * (2 * i - 1);
+  }
+}
+
+// FeHierarchicTria::NodalValuesToFaceDofs (hierarchic_fe.h:1024-1083): the
+// interior values are v[off ..].
+void TriaFaceDofs(int pc, bool ori0_positive, const double* v, int off, double* out) {
+  if (pc <= 2) return;
+  const QuadRule qt = MakeQuadRule(false, 2 * (pc - 1));
+  int idx = 0;
+  for (int i = 0; i < pc - 2; ++i)
+    for (int j = 0; j < pc - i - 2; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < qt.n(); ++q) {
+        const double x = qt.x[q], y = qt.y[q];
+        const double xn = x / (1.0 - y);
+        const double xa = ori0_positive ? xn : 1.0 - xn;
+        const double ypow = std::pow(1.0 - y, i), ypowp1 = std::pow(1.0 - y, i + 1);
+        const double psidd = HLegendreDx(i + 1, xa);
+        const double jacdd = HJacobiDx(j, 2 * i + 4, y), jacd = HIJacobiDx(j + 1, 2 * i + 4, y);
+        s += qt.w[q] * v[off + q] * psidd * (ypowp1 * jacdd - (2 * i + 4) * ypow * jacd);
+      }
+      out[idx++] = s * (2 * i + 3) * (2 * j + 2 * i + 5);
+    }
+}
+}  // namespace
+
+void HierEvaluationNodes(bool is_quad, int pc, const int* pe, const int8_t* ori, std::vector<double>& xy) {
+  xy.clear();
+  auto add = [&](double x, double y) {
+    xy.push_back(x);
+    xy.push_back(y);
+  };
+  std::vector<double> t, w;
+  if (!is_quad) {  // hierarchic_fe.h:828-878
+    add(0, 0);
+    add(1, 0);
+    add(0, 1);
+    for (int j = 0; j < 3; ++j) {
+      if (pe[j] <= 1) continue;
+      SegmentRule(2 * (pe[j] - 1), t, w);
+      for (double u : t) {
+        if (j == 0) add(ori[0] > 0 ? u : 1 - u, 0);
+        else if (j == 1) ori[1] > 0 ? add(1 - u, u) : add(u, 1 - u);
+        else add(0, ori[2] > 0 ? 1 - u : u);
+      }
+    }
+    const QuadRule qt = MakeQuadRule(false, 2 * (pc - 1));
+    for (int q = 0; q < qt.n(); ++q) add(qt.x[q], qt.y[q]);
+    return;
+  }
+  add(0, 0);  // hierarchic_fe.h:1452-1525
+  add(1, 0);
+  add(1, 1);
+  add(0, 1);
+  for (int j = 0; j < 4; ++j) {
+    if (pe[j] <= 1) continue;
+    SegmentRule(2 * (pe[j] - 1), t, w);
+    for (double u : t) {
+      if (j == 0) add(ori[0] > 0 ? u : 1 - u, 0);
+      else if (j == 1) add(1, ori[1] > 0 ? u : 1 - u);
+      else if (j == 2) add(ori[2] > 0 ? 1 - u : u, 1);
+      else add(0, ori[3] > 0 ? 1 - u : u);
+    }
+  }
+  if (pc > 1) {
+    const int D = std::max({pc, pe[0], pe[1], pe[2], pe[3]});
+    SegmentRule(2 * (D - 1), t, w);
+    std::vector<double> pts = {0.0, 1.0};
+    pts.insert(pts.end(), t.begin(), t.end());
+    for (double yv : pts)
+      for (double xv : pts) add(xv, yv);
+  }
+}
+
+void HierNodalValuesToDofs(bool is_quad, int pc, const int* pe, const int8_t* ori, const std::vector<double>& v,
+                           std::vector<double>& dofs) {
+  const int nv = is_quad ? 4 : 3;
+  const int n = HierNumShapeVar(is_quad, pc, pe);
+  dofs.assign(n, 0.0);
+  for (int k = 0; k < nv; ++k) dofs[k] = v[k];
+  // edge dofs
+  std::vector<double> t, w;
+  int node = nv, slot = nv;
+  for (int j = 0; j < nv; ++j) {
+    if (pe[j] <= 1) continue;
+    SegmentRule(2 * (pe[j] - 1), t, w);
+    EdgeValuesToDofs(pe[j], ori[j] > 0, v[j], v[(j + 1) % nv], &v[node], &dofs[slot]);
+    node += static_cast<int>(t.size());
+    slot += pe[j] - 1;
+  }
+  if (!is_quad) {
+    if (pc <= 2) return;
+    // face dofs, then the boundary part of the function taken out of them
+    // (hierarchic_fe.h:891-915)
+    TriaFaceDofs(pc, ori[0] > 0, v.data(), node, &dofs[slot]);
+    std::vector<double> xy;
+    HierEvaluationNodes(false, pc, pe, ori, xy);
+    const int ne = static_cast<int>(xy.size() / 2);
+    std::vector<double> bf(ne, 0.0), phi(n), dphi(2 * n);
+    for (int k = 0; k < ne; ++k) {
+      EvalHierShapeVar(false, pc, pe, ori, xy[2 * k], xy[2 * k + 1], phi.data(),
+                       reinterpret_cast<double(*)[2]>(dphi.data()));
+      for (int a = 0; a < slot; ++a) bf[k] += dofs[a] * phi[a];
+    }
+    std::vector<double> bfd(n - slot, 0.0);
+    TriaFaceDofs(pc, ori[0] > 0, bf.data(), node, bfd.data());
+    for (int a = slot; a < n; ++a) dofs[a] -= bfd[a - slot];
+    return;
+  }
+  if (pc <= 1) return;
+  // face dofs of the quadrilateral (hierarchic_fe.h:1640-1665): the 1D dual of
+  // degree D along x on every node row, then along y on every x-coefficient
+  const int D = std::max({pc, pe[0], pe[1], pe[2], pe[3]});
+  const int nq = D + 2, m = pc - 1;
+  std::vector<double> row(D + 1), tmp(static_cast<size_t>(nq) * m), col(nq), res(D + 1);
+  for (int i = 0; i < nq; ++i) {
+    SegmentValuesToDofs(D, &v[node + nq * i], row.data());
+    for (int a = 0; a < m; ++a) tmp[static_cast<size_t>(i) * m + a] = row[2 + a];
+  }
+  for (int a = 0; a < m; ++a) {  // dof_temp2 row a: the y-dual of the x-coefficient a
+    for (int i = 0; i < nq; ++i) col[i] = tmp[static_cast<size_t>(i) * m + a];
+    SegmentValuesToDofs(D, col.data(), res.data());
+    for (int b = 0; b < m; ++b) dofs[slot + b * m + a] = res[2 + b];  // column-major flattening
+  }
+}
+
+void NodalProjectionHier(const DofHandler& dh, int p, const MeshFunction& u, const uint8_t* cell_flags,
+                         std::vector<double>& out) {
+  const Mesh& m = *dh.mesh;
+  out.assign(dh.num_dofs, 0.0);
+  std::vector<double> xy, v, dofs;
+  for (idx_t c = 0; c < m.num_cells; ++c) {
+    if (cell_flags && !cell_flags[c]) continue;
+    const bool q = m.IsQuad(c);
+    int pc, pe[4];
+    HierCellDegrees(dh, c, p, pc, pe);
+    int8_t ori[4];
+    for (int j = 0; j < 4; ++j) ori[j] = m.cell_ori[c][j];
+    HierEvaluationNodes(q, pc, pe, ori, xy);
+    QuadRule pts;
+    pts.x.resize(xy.size() / 2);
+    pts.y.resize(xy.size() / 2);
+    pts.w.assign(xy.size() / 2, 0.0);
+    for (size_t k = 0; k < xy.size() / 2; ++k) {
+      pts.x[k] = xy[2 * k];
+      pts.y[k] = xy[2 * k + 1];
+    }
+    u.Eval(m, c, pts, v);
+    HierNodalValuesToDofs(q, pc, pe, ori, v, dofs);
+    const idx_t* d = dh.GlobalDofIndices(c);
+    for (int j = 0; j < dh.NumLocalDofs(c); ++j) out[d[j]] = dofs[j];  // set, not add
+  }
+}
+
 void AssembleHierMatrix(const DofHandler& dh, int p, const MeshFunction& alpha, const MeshFunction& gamma,
                         int qdeg, COOMatrix& A) {
   const Mesh& m = *dh.mesh;

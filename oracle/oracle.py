@@ -105,6 +105,10 @@ def lib():
             L.lfo_space_local_counts.argtypes = [vp, P(i32)]
             L.lfo_hier_shape_var.argtypes = [C.c_int, C.c_int, P(i32), P(C.c_int8), C.c_int, P(dp), P(dp), P(dp),
                                              C.c_char_p, C.c_int]
+            L.lfo_hier_dual.argtypes = [C.c_int, C.c_int, P(i32), P(C.c_int8), P(dp), P(dp), P(C.c_int), P(C.c_int),
+                                        C.c_char_p, C.c_int]
+            L.lfo_nodal_projection_hier.argtypes = [vp, C.c_int, P(lfo_coeff), P(C.c_uint8), P(dp), C.c_char_p,
+                                                    C.c_int]
             L.lfo_hier_fn.argtypes = [C.c_int, C.c_int, dp, dp, dp]
             L.lfo_hier_fn.restype = dp
             L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
@@ -561,6 +565,32 @@ def hier_shape_var(is_quad, pc, pe, ori, pts):
     _check(lib().lfo_hier_shape_var(int(is_quad), pc, _p(pe4, C.c_int32), _p(o, C.c_int8), len(pts),
                                     _p(pts, C.c_double), _p(phi, C.c_double), _p(dphi, C.c_double), err, 512), err)
     return phi, dphi
+
+
+def hier_dual(is_quad, pc, pe, ori):
+    """EvaluationNodes (ne, 2) and the NodalValuesToDofs matrix M (n, ne) of
+    FeHierarchicTria/Quad(pc, pe, ori): dofs = M @ values at the nodes."""
+    pe4 = np.ascontiguousarray(list(pe) + [1] * (4 - len(pe)), np.int32)
+    o = np.ascontiguousarray(list(ori) + [1] * (4 - len(ori)), np.int8)
+    ne, n = C.c_int(), C.c_int()
+    err = _err()
+    _check(lib().lfo_hier_dual(int(is_quad), pc, _p(pe4, C.c_int32), _p(o, C.c_int8), None, None, C.byref(ne),
+                               C.byref(n), err, 512), err)
+    xy = np.zeros((ne.value, 2))
+    M = np.zeros((n.value, ne.value))
+    _check(lib().lfo_hier_dual(int(is_quad), pc, _p(pe4, C.c_int32), _p(o, C.c_int8), _p(xy, C.c_double),
+                               _p(M, C.c_double), C.byref(ne), C.byref(n), err, 512), err)
+    return xy, M
+
+
+def nodal_projection_hier(space, p, u, cell_flags=None):
+    """NodalProjection of a mesh function (coeff) onto a hierarchic space of
+    uniform degree p (p = 0: a hier_var_space)."""
+    out = np.zeros(space.num_dofs)
+    fl, flp = _u8(cell_flags)
+    err = _err()
+    _check(lib().lfo_nodal_projection_hier(space.h, p, C.byref(u), flp, _p(out, C.c_double), err, 512), err)
+    return out
 
 
 def hier_fn(which, n, a, b, x):

@@ -1,0 +1,77 @@
+"""NodalProjection (fe/fe_tools.h:198-259) on hierarchic spaces on the GPU
+against the oracle: uniform degrees 1..12 and per-entity degrees on four mesh
+kinds, every coefficient kind, with and without a cell predicate; the
+per-entity path with all degrees equal to p gives the uniform space's result
+value for value; a mid-size hybrid mesh (about 100k cells) end to end."""
+import numpy as np
+import pytest
+
+from parity import O, L, W, oracle_mesh
+from test_gpu_hier import MESHES, _hybrid
+from test_gpu_post import _coeff, _flags
+
+pytestmark = pytest.mark.gpu
+
+UKINDS = ("cell", "nodal", "const", "poly", "sinsin", "sincos", "exp", "trig")
+
+
+def _tol(p):
+    # the dual's rows grow with the degree (segment duals carry (2i - 1) P'_{i-1}
+    # factors); FP64 sums of about n x ne products in another order
+    return 1e-12 if p <= 5 else 1e-11
+
+
+def _check(ctx, sp, osp, p_oracle, tol, mesh, rng, ukinds=UKINDS):
+    out = ctx.zeros(sp.num_dofs)
+    for ukind in ukinds:
+        for fkind in (None, "random"):
+            keep = []
+            gu, ou = _coeff(ctx, ukind, mesh.num_cells, mesh.num_nodes, rng, keep)
+            fl = _flags(fkind, mesh.num_cells, rng)
+            L.nodal_projection(sp, gu, out, ctx.to_device(fl) if fl is not None else None)
+            got = out.download()
+            ref = O.nodal_projection_hier(osp, p_oracle, ou, fl)
+            assert np.abs(got - ref).max() <= tol * max(np.abs(ref).max(), 1.0), (ukind, fkind)
+
+
+@pytest.mark.parametrize("mname,spec", MESHES, ids=[m[0] for m in MESHES])
+@pytest.mark.parametrize("p", [1, 2, 3, 5, 8, 12])
+def test_hier_projection_matches_oracle(ctx, mname, spec, p):
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic(mesh, p)
+    osp = O.hier_space(oracle_mesh(spec), p)
+    _check(ctx, sp, osp, p, _tol(p), mesh, np.random.default_rng(31 * p + len(mname)))
+
+
+@pytest.mark.parametrize("mname,spec", MESHES, ids=[m[0] for m in MESHES])
+def test_hier_var_projection_matches_oracle(ctx, mname, spec):
+    om = oracle_mesh(spec)
+    rng = np.random.default_rng(3 + len(mname))
+    ed = rng.integers(1, 7, om.num_edges).astype(np.int32)
+    cd = rng.integers(1, 7, om.num_cells).astype(np.int32)
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic_var(mesh, ed, cd)
+    osp = O.hier_var_space(om, ed, cd)
+    _check(ctx, sp, osp, 0, _tol(6), mesh, rng)
+
+
+@pytest.mark.parametrize("p", [2, 4])
+def test_hier_var_projection_with_equal_degrees_is_the_uniform_one(ctx, p):
+    spec = _hybrid(6, seed=2)
+    mesh = W.build_mesh(ctx, spec)
+    su = L.Space.hierarchic(mesh, p)
+    sv = L.Space.hierarchic_var(mesh, np.full(mesh.num_edges, p), np.full(mesh.num_cells, p))
+    u = L.coeff(L.ANALYTIC, func=L.FN_SINCOS, params=[0.2, 1.0, 1.5, 0.5])
+    a, b = ctx.zeros(su.num_dofs), ctx.zeros(sv.num_dofs)
+    L.nodal_projection(su, u, a)
+    L.nodal_projection(sv, u, b)
+    assert np.array_equal(a.download(), b.download())
+
+
+def test_hier_projection_mid_size(ctx):
+    """A 224 x 224 hybrid mesh (about 75k cells), degree 4, against the oracle."""
+    spec = _hybrid(224, seed=8)
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic(mesh, 4)
+    osp = O.hier_space(oracle_mesh(spec), 4)
+    _check(ctx, sp, osp, 4, _tol(4), mesh, np.random.default_rng(4), ukinds=("nodal", "trig"))

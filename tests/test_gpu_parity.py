@@ -408,6 +408,7 @@ def test_tensor_coefficient_parity(ctx, kind, degree, mesh):
         ro, co, vo = O.assemble_rd(os_, oa, og).arrays()
         compare_triplets(coo.triplets(), ro, co, vo, block_sizes(om.cells, os_.n_tria, os_.n_quad))
     # matrix-valued coefficients are accepted only as the diffusion coefficient
+    coo = L.COOMatrix(ctx, gs.num_dofs, gs.num_dofs, gs.num_triplets)
     with pytest.raises(L.LfgError) as e:
         L.assemble_matrix_rd(gs, L.rd_provider(L.coeff(L.CONSTANT, 1.0), ga), coo)
     assert e.value.code == L.UNSUPPORTED
