@@ -406,29 +406,32 @@ lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
  * a Jacobi-preconditioned CG:
  *   LFG_SOLVE_FP64   FP64 PCG to ||b - A x|| <= rtol ||b|| (restarted from the
  *                    true residual when the recursive one drifts)
- *   LFG_SOLVE_MIXED  FP32 PCG inner solves (FP32 matrix copy and vectors) of
- *                    A d = r / ||r|| to inner_rtol, inside FP64 iterative
- *                    refinement: r = b - A x in FP64, x += ||r|| d in FP64,
- *                    to the same FP64 residual criterion.  The FP32 operator
- *                    is applied in difference form, (A p)_r = sum_k a_rk
- *                    (p_k - p_r) + s_r p_r with the FP64 row sum s_r, so that
- *                    rounding the entries to FP32 keeps it close to A on its
- *                    smooth modes.  An inner solve stops early when its true
- *                    residual departs from the recursive one; when an FP32
- *                    correction does not halve the FP64 residual norm the solve
- *                    finishes in FP64 from the better iterate.
+ *   LFG_SOLVE_MIXED  FP32 PCG (FP32 matrix copy and vectors) with residual
+ *                    replacement: the FP32 iteration runs on r / ||r_0||, and
+ *                    whenever its recursive residual norm has dropped by
+ *                    inner_rtol since the last replacement (or reaches the
+ *                    target) the FP32 correction is added to x in FP64, the
+ *                    true residual b - A x is formed in FP64 and replaces the
+ *                    recursive one, and CG continues along the same search
+ *                    direction; to the same FP64 residual criterion.  The
+ *                    FP32 operator is applied in difference form, (A p)_r =
+ *                    sum_k a_rk (p_k - p_r) + s_r p_r with the FP64 row sum
+ *                    s_r, so that rounding the entries to FP32 keeps it close
+ *                    to A on its smooth modes.  When a replacement shows that
+ *                    the FP32 recursion no longer tracks the FP64 residual,
+ *                    the solve finishes in FP64 from the better iterate.
  * x_dev holds the initial guess on entry. */
 enum { LFG_SOLVE_FP64 = 0, LFG_SOLVE_MIXED = 1 };
 typedef struct {
   int32_t precision;
   int32_t max_iterations;        /* total inner PCG iterations allowed           */
   double rtol;                   /* relative residual target (FP64)              */
-  double inner_rtol;             /* mixed: relative reduction per inner solve (0: 1e-4) */
+  double inner_rtol;             /* mixed: residual-norm drop between replacements (0: 0.1) */
   int32_t check_every;           /* convergence checks every N iterations        */
 } lfg_solve_opts;
 typedef struct {
   int32_t iterations;            /* PCG iterations (all inner iterations)        */
-  int32_t refinements;           /* FP64 refinement steps (mixed) / restarts (FP64) */
+  int32_t refinements;           /* residual replacements (mixed) / restarts (FP64) */
   double rel_residual;           /* final ||b - A x|| / ||b|| in FP64            */
   int32_t converged;
 } lfg_solve_stats;

@@ -410,13 +410,17 @@ __device__ __forceinline__ T RowDotB(const int32_t* __restrict__ rp, const int32
   return s;
 }
 
-// r = b - A x (FP64) and rr partials; optional x == null means x = 0.
+// r = b - A x (FP64) and rr partials; optional x == null means x = 0.  With
+// `only`, meshes b with only[b] == 0 are skipped (their rows and partials
+// keep their values).
 __global__ void __launch_bounds__(kPB) BResidualKernel(Chunks C, const int32_t* __restrict__ rp,
                                                        const int32_t* __restrict__ col, const double* __restrict__ val,
                                                        const double* __restrict__ x, const double* __restrict__ b,
-                                                       double* __restrict__ r, double* __restrict__ rr) {
+                                                       double* __restrict__ r, double* __restrict__ rr,
+                                                       const int32_t* __restrict__ only = nullptr) {
   __shared__ double red[32];
   for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    if (only && !only[C.mesh[c]]) continue;  // uniform per block
     const int64_t s = C.start[c], e = C.start[c + 1];
     const int sub = threadIdx.x % kLanes, grp = threadIdx.x / kLanes;
     double acc = 0.0;
@@ -446,15 +450,61 @@ __global__ void BScaleKernel(Chunks C, const double* __restrict__ r, const doubl
   }
 }
 
-// x += d32 / scale[mesh] for meshes still being refined
-__global__ void BCorrectKernel(Chunks C, const float* __restrict__ d, const double* __restrict__ scale,
-                               const int32_t* __restrict__ done, double* __restrict__ x) {
+// x += sign * d32 / scale[mesh] for the meshes with sel[mesh] set (the FP32
+// correction at a residual replacement; sign -1 takes it back).
+__global__ void BApplyKernel(Chunks C, const float* __restrict__ d, const double* __restrict__ scale,
+                             const int32_t* __restrict__ sel, double sign, double* __restrict__ x) {
   for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
     const int b = C.mesh[c];
-    if (done[b]) continue;
-    const double inv = 1.0 / scale[b];
+    if (!sel[b]) continue;
+    const double f = sign / scale[b];
     for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x)
-      x[i] += static_cast<double>(d[i]) * inv;
+      x[i] = fma(static_cast<double>(d[i]), f, x[i]);
+  }
+}
+
+// Residual replacement for the meshes with sel[mesh] set: r32 = r64 *
+// scale[mesh] (the FP64 true residual), z = D^-1 r32, d32 = 0; rz[0], rr and
+// beta = rz[0] / rz[1] per mesh from the new residual (p is kept).
+__global__ void __launch_bounds__(kPB) BReplaceKernel(Chunks C, const double* __restrict__ r64,
+                                                      const double* __restrict__ scale,
+                                                      const float* __restrict__ dinv, float* __restrict__ r,
+                                                      float* __restrict__ z, float* __restrict__ d,
+                                                      const int32_t* __restrict__ sel, double* __restrict__ part,
+                                                      MeshScal* __restrict__ ms) {
+  __shared__ double red[32];
+  for (int64_t c = blockIdx.x; c < C.nchunks; c += gridDim.x) {
+    const int b = C.mesh[c];
+    if (!sel[b]) continue;
+    const double sc = scale[b];
+    double arz = 0.0, arr = 0.0;
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      const float ri = static_cast<float>(r64[i] * sc);
+      const float zi = dinv[i] * ri;
+      r[i] = ri;
+      z[i] = zi;
+      d[i] = 0.0f;
+      arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
+      arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
+    }
+    const double s1 = BlockReduce(arz, red);
+    const double s2 = BlockReduce(arr, red);
+    if (threadIdx.x == 0) {
+      part[2 * c] = s1;
+      part[2 * c + 1] = s2;
+    }
+    const int64_t c0 = C.mesh_chunk[b], c1 = C.mesh_chunk[b + 1];
+    if (MeshDone(ms, b, static_cast<unsigned int>(c1 - c0))) {
+      const double rz = MeshPartSum(part, 2, 0, c0, c1, red);
+      const double rr = MeshPartSum(part, 2, 1, c0, c1, red);
+      if (threadIdx.x == 0) {
+        ms[b].beta = ms[b].rz[1] != 0.0 ? rz / ms[b].rz[1] : 0.0;
+        ms[b].rz[0] = rz;
+        ms[b].rr = rr;
+        ms[b].cnt = 0;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -494,6 +544,31 @@ void MeshRR(lfg_batch* B, const DevBuf& ms, std::vector<double>& out) {
   for (int b = 0; b < B->nb; ++b) out[b] = h[b].rr;
 }
 
+// `body` batched PCG iterations (even: the rz slots alternate) captured in a
+// CUDA graph; frozen meshes are skipped by every kernel.
+template <class T>
+void BCapture(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, BState<T>& S,
+              const Chunks& C, DevBuf& frozen_d, int body, cudaGraph_t& graph, cudaGraphExec_t& exec) {
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
+  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+  MeshScal* ms = S.ms.template as<MeshScal>();
+  double* part = S.part.template as<double>();
+  LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < body; ++k) {
+    const int cur = k & 1;
+    T* p = S.p.template as<T>();
+    BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p, frozen_d.as<int32_t>(), ms);
+    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, rowsum, p, S.q.template as<T>(), frozen_d.as<int32_t>(), cur,
+                                        part, ms);
+    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
+                                         S.z.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
+  }
+  LFG_CUDA(cudaStreamEndCapture(s, &graph));
+  LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+}
+
 // Batched PCG in precision T on S.r (filled): per-mesh targets target_rr[b]
 // (squared norms); meshes with frozen_h[b] start frozen.  Returns per-mesh
 // iterations in it_out and final recursive rr in rr_out.
@@ -505,7 +580,6 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* 
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
-  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
   MeshScal* ms = S.ms.template as<MeshScal>();
   double* part = S.part.template as<double>();
   LFG_CUDA(cudaMemcpyAsync(frozen_d.p, frozen_h.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
@@ -521,18 +595,7 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* 
   const int body = std::max(2, check_every + (check_every & 1));
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < body; ++k) {
-    const int cur = k & 1;
-    T* p = S.p.template as<T>();
-    BDirectionKernel<T><<<grid, kPB, 0, s>>>(C, S.z.template as<T>(), p, frozen_d.as<int32_t>(), ms);
-    BSpmvKernel<T><<<grid, kPB, 0, s>>>(C, M, sval, rowsum, p, S.q.template as<T>(), frozen_d.as<int32_t>(), cur,
-                                        part, ms);
-    BUpdateKernel<T><<<grid, kPB, 0, s>>>(C, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
-                                         S.z.template as<T>(), frozen_d.as<int32_t>(), cur, part, ms);
-  }
-  LFG_CUDA(cudaStreamEndCapture(s, &graph));
-  LFG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  BCapture<T>(B, A, sval, rowsum, dinv, x, S, C, frozen_d, body, graph, exec);
   int it = 0;
   try {
     while (it < max_it) {
@@ -992,53 +1055,170 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
       MeshSums(B, S.part.as<double>(), rr);
     }
   } else if (opts->precision == LFG_SOLVE_MIXED) {
-    EnsureFloatValues(A);  // FP32 SELL values
+    // Per mesh: FP32 PCG on r / ||r_0|| with residual replacement (the
+    // single-system solver's scheme, lfg_solve_pcg): once a mesh's recursive
+    // FP32 residual has dropped by `drop` since its last replacement (or
+    // reaches its target), its FP32 correction goes into x in FP64, its true
+    // residual is formed in FP64 and replaces the recursive one, and its CG
+    // continues along the same direction.  Meshes whose FP32 recursion stops
+    // tracking the FP64 residual finish in FP64 afterwards.
     BState<float> S32;
     BAlloc(ctx, n, C.nchunks, B->nb, S32);
-    DevBuf d32, scale, done;
+    DevBuf d32, scale, sel, frozen32;
     d32.alloc(n * sizeof(float), s);
     scale.alloc(B->nb * sizeof(double), s);
-    done.alloc(B->nb * sizeof(int32_t), s);
-    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : 1e-4;
-    std::vector<double> sc(B->nb), tin(B->nb);
-    std::vector<int32_t> dn(B->nb), fz(B->nb);
-    std::vector<int> it1;
-    std::vector<double> rr1;
-    for (int outer = 0; outer < 200; ++outer) {
-      int active = 0;
-      for (int b = 0; b < B->nb; ++b) {
-        dn[b] = !(rr[b] > target[b]);
-        active += !dn[b];
-        const double rn = std::sqrt(rr[b]);
-        sc[b] = rn > 0 ? 1.0 / rn : 1.0;
-        const double need = std::max(inner, rn > 0 ? 0.5 * std::sqrt(target[b]) / rn : inner);
-        tin[b] = need * need;
-        fz[b] = dn[b];
-      }
-      if (!active) break;
-      LFG_CUDA(cudaMemcpyAsync(scale.p, sc.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
-      LFG_CUDA(cudaMemcpyAsync(done.p, dn.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-      BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
-      LFG_LAUNCHED(ctx);
-      BRunPcg<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
-                     S32, C, tin, fz, frozen,
-                     max_it, check, it1, rr1);
-      BCorrectKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), done.as<int32_t>(), x);
-      LFG_LAUNCHED(ctx);
-      BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
-                                          bvec, S.r.as<double>(), S.part.as<double>());
-      LFG_LAUNCHED(ctx);
-      std::vector<double> rr_new;
-      MeshSums(B, S.part.as<double>(), rr_new);
-      bool progress = false;
-      for (int b = 0; b < B->nb; ++b)
-        if (!dn[b]) {
-          its[b] += std::max(it1[b], 1);
-          refinements[b] += 1;
-          progress = progress || rr_new[b] < rr[b];
+    sel.alloc(B->nb * sizeof(int32_t), s);
+    frozen32.alloc(B->nb * sizeof(int32_t), s);
+    const double drop = opts->inner_rtol > 0 ? opts->inner_rtol * opts->inner_rtol : 1e-2;
+    std::vector<double> sc(B->nb), t32(B->nb), ref32(B->nb, 1.0), rr_last(rr);
+    std::vector<int32_t> fz(B->nb), failed(B->nb, 0), sl(B->nb), keep(B->nb);
+    for (int b = 0; b < B->nb; ++b) {
+      fz[b] = !(rr[b] > target[b]);
+      sc[b] = rr[b] > 0 ? 1.0 / std::sqrt(rr[b]) : 1.0;
+      t32[b] = target[b] * sc[b] * sc[b];
+    }
+    LFG_CUDA(cudaMemcpyAsync(scale.p, sc.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
+    LFG_CUDA(cudaMemcpyAsync(frozen32.p, fz.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
+    LFG_LAUNCHED(ctx);
+    BStartKernel<float><<<grid, kPB, 0, s>>>(C, A->dinv32.as<float>(), S32.r.as<float>(), S32.z.as<float>(),
+                                             S32.p.as<float>(), frozen32.as<int32_t>(), S32.part.as<double>(),
+                                             S32.ms.as<MeshScal>());
+    LFG_LAUNCHED(ctx);
+    const int body = std::max(2, check + (check & 1));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BCapture<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
+                    S32, C, frozen32, body, graph, exec);
+    std::vector<double> rr32, rr_new;
+    int it = 0;
+    try {
+      while (true) {
+        int active = 0;
+        for (int b = 0; b < B->nb; ++b) active += !fz[b];
+        if (!active) break;
+        LFG_CUDA(cudaGraphLaunch(exec, s));
+        CountLaunch(ctx, 3 * body);
+        it += body;
+        MeshRR(B, S32.ms, rr32);
+        int nsel = 0;
+        for (int b = 0; b < B->nb; ++b) {
+          sl[b] = 0;
+          if (fz[b]) continue;
+          its[b] += body;
+          if (!std::isfinite(rr32[b])) {  // FP32 broke down: finish this block in FP64 from its x
+            failed[b] = 1;
+            fz[b] = 1;
+            continue;
+          }
+          sl[b] = !(rr32[b] > t32[b]) || !(rr32[b] >= drop * ref32[b]) || it >= max_it;
+          nsel += sl[b];
         }
-      rr = rr_new;
-      if (!progress) break;
+        if (!nsel) {
+          LFG_CUDA(cudaMemcpyAsync(frozen32.p, fz.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+          continue;
+        }
+        LFG_CUDA(cudaMemcpyAsync(sel.p, sl.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        BApplyKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), sel.as<int32_t>(), 1.0, x);
+        LFG_LAUNCHED(ctx);
+        BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
+                                            x, bvec, S.r.as<double>(), S.part.as<double>(), sel.as<int32_t>());
+        LFG_LAUNCHED(ctx);
+        MeshSums(B, S.part.as<double>(), rr_new);
+        int nrevert = 0, nkeep = 0;
+        for (int b = 0; b < B->nb; ++b) {
+          keep[b] = 0;
+          if (!sl[b]) continue;
+          refinements[b] += 1;
+          const double claimed = rr32[b] / (sc[b] * sc[b]);
+          if (rr_new[b] <= target[b]) {
+            rr[b] = rr_new[b];
+            fz[b] = 1;
+          } else if (!(rr_new[b] < 0.25 * rr_last[b]) && !(rr_new[b] <= 16.0 * claimed)) {
+            failed[b] = 1;  // FP32 cannot resolve this block: finish it in FP64
+            fz[b] = 1;
+            if (!(rr_new[b] < rr_last[b])) {
+              sl[b] = 2;  // take the correction back
+              ++nrevert;
+            } else {
+              rr[b] = rr_new[b];
+            }
+          } else {
+            rr[b] = rr_last[b] = rr_new[b];
+            ref32[b] = rr_new[b] * sc[b] * sc[b];
+            if (it >= max_it) {
+              fz[b] = 1;
+            } else {
+              keep[b] = 1;
+              ++nkeep;
+            }
+          }
+        }
+        if (nrevert) {
+          for (int b = 0; b < B->nb; ++b) sl[b] = sl[b] == 2;
+          LFG_CUDA(cudaMemcpyAsync(sel.p, sl.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+          BApplyKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), sel.as<int32_t>(), -1.0, x);
+          LFG_LAUNCHED(ctx);
+          BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                              A->val.as<double>(), x, bvec, S.r.as<double>(), S.part.as<double>(),
+                                              sel.as<int32_t>());
+          LFG_LAUNCHED(ctx);
+          MeshSums(B, S.part.as<double>(), rr_new);
+          for (int b = 0; b < B->nb; ++b)
+            if (sl[b]) rr[b] = rr_new[b];
+        }
+        if (nkeep) {
+          LFG_CUDA(cudaMemcpyAsync(sel.p, keep.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+          BReplaceKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), A->dinv32.as<float>(),
+                                             S32.r.as<float>(), S32.z.as<float>(), d32.as<float>(), sel.as<int32_t>(),
+                                             S32.part.as<double>(), S32.ms.as<MeshScal>());
+          LFG_LAUNCHED(ctx);
+        }
+        LFG_CUDA(cudaMemcpyAsync(frozen32.p, fz.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+      }
+    } catch (...) {
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    // blocks FP32 could not finish: FP64 PCG from their current iterate
+    int nfailed = 0;
+    for (int b = 0; b < B->nb; ++b) nfailed += failed[b] && rr[b] > target[b];
+    if (nfailed) {
+      std::vector<int> it1;
+      std::vector<double> rr1;
+      for (int round = 0; round < 5; ++round) {
+        std::vector<int32_t> f64(B->nb, 1);
+        int act = 0;
+        for (int b = 0; b < B->nb; ++b) {
+          f64[b] = !(failed[b] && rr[b] > target[b]);
+          act += !f64[b];
+        }
+        if (!act) break;
+        std::vector<int32_t> only(B->nb);
+        for (int b = 0; b < B->nb; ++b) only[b] = !f64[b];
+        LFG_CUDA(cudaMemcpyAsync(sel.p, only.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
+                                            x, bvec, S.r.as<double>(), S.part.as<double>(), sel.as<int32_t>());
+        LFG_LAUNCHED(ctx);
+        BRunPcg<double>(B, A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, S, C, target, f64, frozen,
+                        max_it, check, it1, rr1);
+        BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
+                                            x, bvec, S.r.as<double>(), S.part.as<double>(), sel.as<int32_t>());
+        LFG_LAUNCHED(ctx);
+        MeshSums(B, S.part.as<double>(), rr_new);
+        bool progress = false;
+        for (int b = 0; b < B->nb; ++b)
+          if (only[b]) {
+            its[b] += it1[b];
+            refinements[b] += 1;
+            progress = progress || rr_new[b] < 0.25 * rr[b];
+            rr[b] = rr_new[b];
+          }
+        if (!progress) break;
+      }
     }
   } else {
     Fail(LFG_INVALID_ARG, "unknown solve precision");
