@@ -406,32 +406,32 @@ lfg_status lfg_csr_spmv(lfg_csr* csr, const double* x_dev, double* y_dev);
  * a Jacobi-preconditioned CG:
  *   LFG_SOLVE_FP64   FP64 PCG to ||b - A x|| <= rtol ||b|| (restarted from the
  *                    true residual when the recursive one drifts)
- *   LFG_SOLVE_MIXED  FP32 PCG (FP32 matrix copy and vectors) with residual
- *                    replacement: the FP32 iteration runs on r / ||r_0||, and
- *                    whenever its recursive residual norm has dropped by
- *                    inner_rtol since the last replacement (or reaches the
- *                    target) the FP32 correction is added to x in FP64, the
- *                    true residual b - A x is formed in FP64 and replaces the
- *                    recursive one, and CG continues along the same search
- *                    direction; to the same FP64 residual criterion.  The
- *                    FP32 operator is applied in difference form, (A p)_r =
- *                    sum_k a_rk (p_k - p_r) + s_r p_r with the FP64 row sum
- *                    s_r, so that rounding the entries to FP32 keeps it close
- *                    to A on its smooth modes.  When a replacement shows that
- *                    the FP32 recursion no longer tracks the FP64 residual,
+ *   LFG_SOLVE_MIXED  FP32 PCG inner solves (FP32 matrix copy and vectors) of
+ *                    A d = r / ||r|| to inner_rtol, inside FP64 iterative
+ *                    refinement: r = b - A x in FP64, x += ||r|| d in FP64,
+ *                    to the same FP64 residual criterion.  The FP32 operator
+ *                    is applied in difference form, (A p)_r = sum_k a_rk
+ *                    (p_k - p_r) + s_r p_r with the FP64 row sum s_r, so that
+ *                    rounding the entries to FP32 keeps it close to A on its
+ *                    smooth modes.  An inner solve stops early when its true
+ *                    residual departs from the recursive one; when an FP32
+ *                    correction does not reduce the FP64 residual norm by 2x
  *                    the solve finishes in FP64 from the better iterate.
+ *                    (The batched solver, lfg_batch_solve_pcg, uses residual
+ *                    replacement instead, where it needs fewer iterations.)
  * x_dev holds the initial guess on entry. */
 enum { LFG_SOLVE_FP64 = 0, LFG_SOLVE_MIXED = 1 };
 typedef struct {
   int32_t precision;
   int32_t max_iterations;        /* total inner PCG iterations allowed           */
   double rtol;                   /* relative residual target (FP64)              */
-  double inner_rtol;             /* mixed: residual-norm drop between replacements (0: 0.1) */
+  double inner_rtol;             /* mixed: relative reduction per inner solve (0: 1e-4); batched:
+                                    residual-norm drop between replacements (0: 0.1) */
   int32_t check_every;           /* convergence checks every N iterations        */
 } lfg_solve_opts;
 typedef struct {
   int32_t iterations;            /* PCG iterations (all inner iterations)        */
-  int32_t refinements;           /* residual replacements (mixed) / restarts (FP64) */
+  int32_t refinements;           /* FP64 refinement steps or residual replacements (mixed) / restarts (FP64) */
   double rel_residual;           /* final ||b - A x|| / ||b|| in FP64            */
   int32_t converged;
 } lfg_solve_stats;
@@ -550,8 +550,13 @@ lfg_status lfg_batch_boundary_dof_flags(lfg_batch* batch, uint8_t* flags_dev);
 /* Batched PCG: one independent Jacobi-PCG per block of the block-diagonal
  * CSR (each with its own step lengths and stopping test), all advanced
  * together by the same kernels, replayed from a CUDA graph.  precision FP64 or
- * MIXED (FP32 inner iterations, FP64 residual refinement; the FP32 operator
- * is applied in difference form, see lfg_solve_pcg).  per_block_stats
+ * MIXED: per block, FP32 PCG (difference-form operator, see lfg_solve_pcg) on
+ * r / ||r_0|| with residual replacement -- once the block's recursive FP32
+ * residual norm has dropped by inner_rtol (0: 0.1) since its last replacement
+ * or meets the target, its FP32 correction is added to x in FP64, its true
+ * residual b - A x is formed in FP64 and replaces the recursive one, and its
+ * CG continues along the same direction; a block whose FP32 recursion stops
+ * tracking the FP64 residual finishes in FP64.  per_block_stats
  * (num_spaces entries, may be NULL) and the summary stats (iterations = the
  * longest block, converged = all blocks). */
 lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const double* b_dev,

@@ -310,14 +310,31 @@ __global__ void __launch_bounds__(kPB) BUpdateKernel(Chunks C, const T* __restri
     if (frozen[b]) continue;
     const T alpha = static_cast<T>(ms[b].alpha);
     BDot<T> arz, arr;
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
-      x[i] = fma(alpha, p[i], x[i]);
-      const T ri = fma(-alpha, q[i], r[i]);
-      r[i] = ri;
-      const T zi = dinv[i] * ri;
-      z[i] = zi;
-      arz.add(ri, zi);
-      arr.add(ri, ri);
+    // U elements per thread and trip, loads first (more loads in flight)
+    constexpr int U = sizeof(T) == 8 ? 2 : 4;
+    const int64_t e = C.start[c + 1];
+    for (int64_t i0 = C.start[c] + threadIdx.x; i0 < e; i0 += U * blockDim.x) {
+      T pv[U], qv[U], xv[U], rv[U], dv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = i0 + u * blockDim.x;
+        if (i < e) {
+          pv[u] = p[i]; qv[u] = q[i]; xv[u] = x[i]; rv[u] = r[i]; dv[u] = dinv[i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = i0 + u * blockDim.x;
+        if (i < e) {
+          x[i] = fma(alpha, pv[u], xv[u]);
+          const T ri = fma(-alpha, qv[u], rv[u]);
+          r[i] = ri;
+          const T zi = dv[u] * ri;
+          z[i] = zi;
+          arz.add(ri, zi);
+          arr.add(ri, ri);
+        }
+      }
     }
     const double s1 = BlockReduce(arz.get(), red);
     const double s2 = BlockReduce(arr.get(), red);
@@ -350,7 +367,24 @@ __global__ void __launch_bounds__(kPB) BDirectionKernel(Chunks C, const T* __res
     const int b = C.mesh[c];
     if (frozen[b]) continue;
     const T beta = static_cast<T>(ms[b].beta);
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) p[i] = fma(beta, p[i], z[i]);
+    constexpr int U = sizeof(T) == 8 ? 2 : 4;
+    const int64_t e = C.start[c + 1];
+    for (int64_t i0 = C.start[c] + threadIdx.x; i0 < e; i0 += U * blockDim.x) {
+      T pv[U], zv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = i0 + u * blockDim.x;
+        if (i < e) {
+          pv[u] = p[i];
+          zv[u] = z[i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = i0 + u * blockDim.x;
+        if (i < e) p[i] = fma(beta, pv[u], zv[u]);
+      }
+    }
   }
 }
 

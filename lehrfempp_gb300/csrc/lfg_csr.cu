@@ -163,9 +163,7 @@ __global__ void ResidualKernel(int64_t rows, const int32_t* __restrict__ rp, con
 
 // ------------------------------------------------------------------- PCG
 constexpr int kPcgBlock = 256;
-// mixed: a residual replacement once the FP32 recursive <r, r> has dropped
-// by this factor (10x in norm) since the last one
-constexpr double kReplaceDrop = 1e-2;
+constexpr double kDefaultInnerRtol = 1e-4;  // mixed: relative reduction per inner FP32 solve
 constexpr int kSlice = 32;
 
 // Scalars of one PCG run, on the device.  rz[cur] is <r, z> of the current
@@ -173,6 +171,7 @@ constexpr int kSlice = 32;
 struct PcgScalars {
   double rz[2];
   double alpha, beta, rr, pq;
+  double trr;  // <t, t> of the true residual t = rhs - A x (inner FP32 solves, gap monitor)
   unsigned int counter;
   unsigned int pad;
 };
@@ -394,6 +393,43 @@ __global__ void __launch_bounds__(kPcgBlock) PcgStartKernel(int64_t rows, const 
   }
 }
 
+// t = rhs - A x over the SELL copy in precision T; sc->trr = <t, t> (block
+// partials, then the last block).  The inner FP32 solve runs it once per
+// graph replay to see whether its recursively updated residual still tracks
+// the true one.
+template <class T>
+__global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows, int64_t nslices,
+                                                                   const int64_t* __restrict__ sptr,
+                                                                   const int32_t* __restrict__ scol,
+                                                                   const T* __restrict__ sval,
+                                                                   const T* __restrict__ rowsum,
+                                                                   const T* __restrict__ x, const T* __restrict__ rhs,
+                                                                   double* __restrict__ part,
+                                                                   PcgScalars* __restrict__ sc) {
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  DotAcc<T> acc;
+  for (int64_t sl = warp; sl < nslices; sl += nwarps) {
+    const int64_t r = sl * kSlice + lane;
+    const int64_t b0 = sptr[sl];
+    const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
+    if (r < rows) {
+      const T t = rhs[r] - SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum);
+      acc.add(t, t);
+    }
+  }
+  const double tot = BlockSum(acc.get(), red);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+  if (FinishedLast(&sc->counter)) {
+    const double v = SumParts(part, gridDim.x, 1, 0, red);
+    if (threadIdx.x == 0) {
+      sc->trr = v;
+      sc->counter = 0;
+    }
+  }
+}
 
 // SELL-32 construction: width of each slice (longest row, times 32)...
 __global__ void SellWidthKernel(int64_t rows, int64_t nslices, const int64_t* __restrict__ rp,
@@ -480,53 +516,6 @@ __global__ void AddCorrectionKernel(int64_t n, float* __restrict__ d, double s, 
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     x[i] += static_cast<double>(d[i]) * s;
     d[i] = 0.0f;
-  }
-}
-
-// x += sign * d / scale (d kept): the mixed solver's FP32 correction, applied
-// at a residual replacement (sign -1 takes it back).
-__global__ void ApplyCorrectionKernel(int64_t n, const float* __restrict__ d, double inv_scale,
-                                      double* __restrict__ x) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    x[i] = fma(static_cast<double>(d[i]), inv_scale, x[i]);
-}
-
-// Residual replacement of the mixed solver: r32 = r64 * scale (the FP64 true
-// residual), z = D^-1 r32, d32 = 0; rz[0] = <r32, z>, rr = <r32, r32> and the
-// direction update's beta = rz[0] / rz[1] recomputed from the new residual
-// (the search direction p is kept).
-__global__ void __launch_bounds__(kPcgBlock) PcgReplaceKernel(int64_t n, const double* __restrict__ r64, double scale,
-                                                              const float* __restrict__ dinv, float* __restrict__ r,
-                                                              float* __restrict__ z, float* __restrict__ d,
-                                                              double* __restrict__ part, PcgScalars* __restrict__ sc) {
-  __shared__ double red[32];
-  double arz = 0.0, arr = 0.0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const float ri = static_cast<float>(r64[i] * scale);
-    const float zi = dinv[i] * ri;
-    r[i] = ri;
-    z[i] = zi;
-    d[i] = 0.0f;
-    arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
-    arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
-  }
-  const double s1 = BlockSum(arz, red);
-  const double s2 = BlockSum(arr, red);
-  if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = s1;
-    part[2 * blockIdx.x + 1] = s2;
-  }
-  if (FinishedLast(&sc->counter)) {
-    const double rz = SumParts(part, gridDim.x, 2, 0, red);
-    const double rr = SumParts(part, gridDim.x, 2, 1, red);
-    if (threadIdx.x == 0) {
-      sc->beta = sc->rz[1] != 0.0 ? rz / sc->rz[1] : 0.0;
-      sc->rz[0] = rz;
-      sc->rr = rr;
-      sc->counter = 0;
-    }
   }
 }
 
@@ -685,10 +674,14 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T
 
 // PCG on A x = b in precision T from the residual already in S.r (x holds
 // the matching iterate).  Returns the iterations done; rr_out = <r, r> of the
-// recursively updated residual.
+// recursively updated residual.  With `rhs` (the inner FP32 solves of the
+// mixed solver, x = 0 at the start) the true residual rhs - A x is measured
+// after every graph replay, and the solve stops as soon as its norm exceeds
+// twice the recursive residual's: from there on the FP32 iterates no longer
+// improve the solution, and the FP64 refinement takes over.
 template <class T>
 int RunPcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int64_t n, double target_rr,
-           int max_it, int check_every, PcgState<T>& S, double& rr_out) {
+           int max_it, int check_every, PcgState<T>& S, double& rr_out, const T* rhs = nullptr) {
   lfg_ctx* ctx = A->ctx;
   cudaStream_t s = ctx->stream;
   PcgStartKernel<T><<<S.nb, kPcgBlock, 0, s>>>(n, dinv, S.r.template as<T>(), S.z.template as<T>(),
@@ -703,11 +696,25 @@ int RunPcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int6
   }
   const int body = std::max(2, check_every + (check_every & 1));
   PcgGraph g = CapturePcg<T>(A, sval, rowsum, dinv, x, n, body, S);
+  const int spmv_blocks = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(static_cast<int64_t>(ctx->num_sms) * 8, (A->nslices + 7) / 8)));
   try {
     while (it < max_it) {
       LFG_CUDA(cudaGraphLaunch(g.exec, s));
       CountLaunch(ctx, g.launches);
       it += body;
+      if (rhs) {
+        PcgTrueResidualKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
+            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, rowsum, x, rhs,
+            S.part.template as<double>(), S.scal.template as<PcgScalars>());
+        LFG_LAUNCHED(ctx);
+        PcgScalars h{};
+        D2HSync(ctx, &h, S.scal.p, sizeof(PcgScalars));
+        rr = h.rr;
+        if (!(rr > target_rr)) break;
+        if (!(h.trr <= 4.0 * rr)) break;  // the recursion lost the true residual (or NaN)
+        continue;
+      }
       rr = ReadRR(ctx, S.scal);
       if (!(rr > target_rr)) break;  // also stops on NaN
     }
@@ -893,97 +900,58 @@ lfg_status lfg_solve_pcg(lfg_csr* A, const double* b, double* x, const lfg_solve
     st.converged = st.rel_residual <= rtol * 1.0000001 || rr <= target;
     st.refinements = restarts;
   } else if (opts->precision == LFG_SOLVE_MIXED) {
-    // FP32 PCG with residual replacement: the iteration (SELL FP32 values in
-    // difference form, FP32 vectors) runs on r / ||r_0||; whenever its
-    // recursive residual has dropped by kReplaceDrop since the last
-    // replacement (or reaches the target), the FP32 correction is added to
-    // the FP64 iterate, the true residual b - A x is formed in FP64 and
-    // replaces the recursive one, and CG continues along the same search
-    // direction (no restart, so no Krylov information is lost).  If a
-    // replacement shows that the FP32 recursion no longer tracks the FP64
-    // residual, the solve finishes in FP64 from the better iterate.
     EnsureFloatValues(A);
     PcgState<float> S32;
     AllocState(ctx, n, S32);
-    DevBuf d32;
+    DevBuf d32, rhs32, x_old;
     d32.alloc(n * sizeof(float), s);
-    const double scale = 1.0 / std::sqrt(rr), inv_scale = std::sqrt(rr);
-    ScaleToFloatKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S64.r.as<double>(), scale, S32.r.as<float>(),
-                                                            d32.as<float>());
-    LFG_LAUNCHED(ctx);
-    PcgStartKernel<float><<<S32.nb, kPcgBlock, 0, s>>>(n, A->dinv32.as<float>(), S32.r.as<float>(),
-                                                       S32.z.as<float>(), S32.p.as<float>(),
-                                                       S32.part.as<double>(), S32.scal.as<PcgScalars>());
-    LFG_LAUNCHED(ctx);
-    const int body = std::max(2, check + (check & 1));
-    PcgGraph g = CapturePcg<float>(A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(),
-                                   d32.as<float>(), n, body, S32);
-    int total = 0, replacements = 0;
+    rhs32.alloc(n * sizeof(float), s);
+    x_old.alloc(n * sizeof(double), s);
+    const double inner = opts->inner_rtol > 0 ? opts->inner_rtol : kDefaultInnerRtol;
+    int total = 0, outer = 0;
     bool fp32_failed = false;
-    double rr_last = rr;                     // true FP64 <r, r> at the last replacement
-    double rr32_ref = 1.0;                   // recursive FP32 <r, r> right after it (scaled)
-    const double target32 = target * scale * scale;
-    const double drop = opts->inner_rtol > 0 ? opts->inner_rtol * opts->inner_rtol : kReplaceDrop;
-    try {
-      while (true) {
-        double rr32 = rr32_ref;
-        bool replace = total >= max_it;
-        while (!replace) {
-          LFG_CUDA(cudaGraphLaunch(g.exec, s));
-          CountLaunch(ctx, g.launches);
-          total += body;
-          rr32 = ReadRR(ctx, S32.scal);
-          replace = !(rr32 > target32) || !(rr32 >= drop * rr32_ref) || total >= max_it;
-        }
-        if (!std::isfinite(rr32)) {  // the FP32 iteration broke down: x and S64.r are still consistent
-          fp32_failed = true;
-          break;
-        }
-        ApplyCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), inv_scale, x);
-        LFG_LAUNCHED(ctx);
-        ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
-                                                     A->val.as<double>(), x, b, S64.r.as<double>(),
-                                                     S64.res.as<double>());
-        LFG_LAUNCHED(ctx);
-        const double rr_new = HostSum(ctx, S64.res.as<double>(), nb, tmp);
-        ++replacements;
-        if (rr_new <= target) {
+    while (total < max_it && outer < 200) {
+      const double rnorm = std::sqrt(rr);
+      if (rr <= target) break;
+      // inner FP32 PCG on A d = r / ||r|| (d starts at 0)
+      ScaleToFloatKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, S64.r.as<double>(), 1.0 / rnorm, S32.r.as<float>(),
+                                                              d32.as<float>());
+      LFG_LAUNCHED(ctx);
+      LFG_CUDA(cudaMemcpyAsync(rhs32.p, S32.r.p, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      LFG_CUDA(cudaMemcpyAsync(x_old.p, x, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      // inner target relative to ||r / ||r|| || = 1, never below what the outer loop needs
+      const double need = std::max(inner, 0.5 * std::sqrt(target) / rnorm);
+      double rr_in = 0.0;
+      const int it = RunPcg<float>(A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(), n,
+                                   need * need, max_it - total, check, S32, rr_in, rhs32.as<float>());
+      total += std::max(it, 1);
+      AddCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), rnorm, x);
+      LFG_LAUNCHED(ctx);
+      ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                                   A->val.as<double>(), x, b, S64.r.as<double>(), S64.res.as<double>());
+      LFG_LAUNCHED(ctx);
+      const double rr_new = HostSum(ctx, S64.res.as<double>(), nb, tmp);
+      ++outer;
+      if (!(rr_new < 0.25 * rr)) {
+        // the FP32 correction did not halve the FP64 residual: FP32 cannot
+        // make progress on this system.  Keep the better iterate and finish
+        // in FP64 (same restart rule as the FP64 solver).
+        if (!(rr_new < rr)) {
+          LFG_CUDA(cudaMemcpyAsync(x, x_old.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+          ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                                       A->val.as<double>(), x, b, S64.r.as<double>(),
+                                                       S64.res.as<double>());
+          LFG_LAUNCHED(ctx);
+        } else {
           rr = rr_new;
-          break;
         }
-        // the recursion claims more than 4x the true residual's norm and the
-        // true residual gained less than 2x: FP32 cannot resolve this system
-        const double claimed = rr32 * inv_scale * inv_scale;
-        if (!(rr_new < 0.25 * rr_last) && !(rr_new <= 16.0 * claimed)) {
-          if (!(rr_new < rr_last)) {  // take the correction back
-            ApplyCorrectionKernel<<<GridFor(ctx, n, 256), 256, 0, s>>>(n, d32.as<float>(), -inv_scale, x);
-            LFG_LAUNCHED(ctx);
-            ResidualKernel<<<rblocks, kPcgBlock, 0, s>>>(n, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
-                                                         A->val.as<double>(), x, b, S64.r.as<double>(),
-                                                         S64.res.as<double>());
-            LFG_LAUNCHED(ctx);
-            rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
-          } else {
-            rr = rr_new;
-          }
-          fp32_failed = true;
-          break;
-        }
-        rr = rr_last = rr_new;
-        if (total >= max_it) break;
-        PcgReplaceKernel<<<S32.nb, kPcgBlock, 0, s>>>(n, S64.r.as<double>(), scale, A->dinv32.as<float>(),
-                                                      S32.r.as<float>(), S32.z.as<float>(), d32.as<float>(),
-                                                      S32.part.as<double>(), S32.scal.as<PcgScalars>());
-        LFG_LAUNCHED(ctx);
-        rr32_ref = rr_new * scale * scale;
+        fp32_failed = true;
+        break;
       }
-    } catch (...) {
-      g.Release();
-      throw;
+      rr = rr_new;
     }
-    g.Release();
-    int outer = replacements;
     if (fp32_failed) {
+      rr = HostSum(ctx, S64.res.as<double>(), nb, tmp);
       double rr_prev = rr;
       int restarts = 0;
       while (rr > target && total < max_it) {
