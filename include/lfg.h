@@ -571,6 +571,18 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* batch, lfg_csr* block_diagonal, const 
 lfg_status lfg_batch_solve_tuning(const lfg_batch* batch, int32_t precision, int32_t* chunk_rows,
                                   double* row_iterations_per_s);
 lfg_status lfg_batch_set_solve_chunk_rows(lfg_batch* batch, int32_t precision, int32_t chunk_rows);
+/* Scheme of the batched PCG.  group_bytes = 0: every block advances in one
+ * lock-step sweep over the whole batch per iteration (kernels replayed from a
+ * CUDA graph, every iteration streams the batch from HBM).  group_bytes > 0:
+ * blocks are packed, largest first, into groups of at most group_bytes of
+ * solver data (matrix, diagonal, row sums, work vectors) and solved one
+ * group at a time by a persistent cooperative kernel (three phases per
+ * iteration separated by grid barriers, check_every iterations per launch),
+ * so that a group's data stays in the 129 MB L2 across iterations; rows per
+ * chunk are then fixed at 512.  Each block's PCG is the same either way (up
+ * to the order of its partial sums).  No reference counterpart. */
+lfg_status lfg_batch_set_solve_groups(lfg_batch* batch, double group_bytes);
+lfg_status lfg_batch_solve_groups(const lfg_batch* batch, double* group_bytes);
 
 /* ---------------------------------------------------------------- Gmsh reader
  * GmshReader(factory, filename) (io/gmsh_reader.h, io/gmsh_reader.cc:22-30,

@@ -581,6 +581,16 @@ class Batch:
     def set_solve_chunk_rows(self, precision, chunk_rows):
         self.ctx.check(lib().lfg_batch_set_solve_chunk_rows(self.h, precision, int(chunk_rows)))
 
+    def set_solve_groups(self, group_bytes):
+        """0: lock-step sweep over the whole batch; > 0: L2-sized groups of
+        blocks solved one at a time by the persistent cooperative kernel."""
+        self.ctx.check(lib().lfg_batch_set_solve_groups(self.h, float(group_bytes)))
+
+    def solve_groups(self):
+        v = C.c_double(0.0)
+        self.ctx.check(lib().lfg_batch_solve_groups(self.h, C.byref(v)))
+        return v.value
+
     def assemble_vector_load(self, provider, b):
         self.ctx.check(lib().lfg_batch_assemble_vector_load(self.h, C.byref(provider), b.ptr))
 

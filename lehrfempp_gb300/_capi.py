@@ -146,6 +146,8 @@ SIGNATURES = {
     "lfg_batch_solve_pcg": (c_status, [vp, vp, vp, vp, P(lfg_solve_opts), P(lfg_solve_stats), P(lfg_solve_stats)]),
     "lfg_batch_solve_tuning": (c_status, [vp, i32, P(i32), P(dbl)]),
     "lfg_batch_set_solve_chunk_rows": (c_status, [vp, i32, i32]),
+    "lfg_batch_set_solve_groups": (c_status, [vp, dbl]),
+    "lfg_batch_solve_groups": (c_status, [vp, P(dbl)]),
     "lfg_gmsh_last_error": (C.c_char_p, []),
     "lfg_gmsh_open": (c_status, [C.c_char_p, P(vp)]),
     "lfg_gmsh_open_buffer": (c_status, [C.c_char_p, i64, P(vp)]),

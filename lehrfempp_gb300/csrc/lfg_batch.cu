@@ -68,6 +68,9 @@ struct lfg_batch {
   bool solve_tuned[2] = {false, false};
   int solve_chunk_rows[2] = {2048, 2048};
   double solve_rate[2] = {0.0, 0.0};  // row-iterations per second of the chosen shape
+  // grouped solver: meshes packed into groups of at most this many bytes of
+  // solver data (0: every mesh in one lock-step sweep)
+  double solve_group_bytes = 0.0;
 };
 
 namespace lfg {
@@ -542,6 +545,254 @@ __global__ void __launch_bounds__(kPB) BReplaceKernel(Chunks C, const double* __
   }
 }
 
+// ------------------------------------------------------ grouped PCG
+// The lock-step solver streams every mesh's matrix and vectors from HBM on
+// every iteration.  The grouped solver instead packs meshes into groups whose
+// solver data fits in L2 and iterates one group at a time in one cooperative,
+// persistent launch per `check_every` iterations: three phases per iteration
+// (direction p = z + beta p; q = A p with <p, q>; the x / r / z update with
+// <r, z>, <r, r>) separated by grid barriers, so a group's vectors and matrix
+// stay in L2 across iterations and no kernel launch separates the phases.
+// Chunk c of the group's chunk list is always handled by block c % grid, so a
+// block reads and writes its own rows in every phase and only the gathers of
+// the SpMV and the per-mesh partial sums cross blocks (read through L2).
+// Every block that needs a mesh's scalar (beta, alpha, the stopping test)
+// sums that mesh's chunk partials itself, in chunk order, so all blocks get
+// the same bits and the result does not depend on the grid.
+constexpr int kGThreads = 256;
+constexpr int kGMaxSlots = 16;          // chunks per block in one group
+constexpr int kGChunkRows = 512;        // rows per chunk of the grouped solver
+constexpr unsigned int kGBarPolls = 1u << 21;  // about a second of polling
+
+struct GridBar {
+  unsigned int arrive, gen;
+  int err, pad;
+};
+
+// Per-mesh scalars of the grouped solver, published by the block that owns the
+// mesh's first chunk (read by the other blocks and by the host).
+struct GMeshScal {
+  double rz[2];    // <r, z> of iteration i in slot i & 1
+  double rr;       // <r, r> at the last stopping test
+  int32_t frozen;  // converged (or not part of the run)
+  int32_t it;      // iterations done
+};
+
+__device__ __forceinline__ unsigned int LdVolU(const unsigned int* p) {
+  return *reinterpret_cast<const volatile unsigned int*>(p);
+}
+__device__ __forceinline__ int LdVolI(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Grid-wide barrier of a cooperative launch (every block co-resident).  Each
+// wait gives up after kGBarPolls polls: it then sets err, and every block
+// leaves at its next barrier.
+__device__ bool GridSync(GridBar* g) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned int gen = LdVolU(&g->gen);  // read before arriving
+    __threadfence();
+    if (atomicAdd(&g->arrive, 1u) == gridDim.x - 1) {
+      atomicExch(&g->arrive, 0u);
+      __threadfence();
+      atomicAdd(&g->gen, 1u);
+    } else {
+      unsigned int polls = 0;
+      while (LdVolU(&g->gen) == gen) {
+        if (++polls > kGBarPolls || LdVolI(&g->err)) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (!ok) atomicExch(&g->err, 1);
+    if (LdVolI(&g->err)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Sum of part[c * 3 + off] over a mesh's chunks, in chunk order, through L2.
+__device__ double GMeshSum(const double* part, int off, int64_t c0, int64_t c1, double* red) {
+  double v = 0.0;
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) v += __ldcg(part + c * 3 + off);
+  return BlockReduce(v, red);  // valid in thread 0
+}
+
+template <class T>
+struct GArgs {
+  Chunks C;
+  Sell M;
+  const T* val;
+  const T* rowsum;   // difference form (FP32) or null
+  const T* dinv;
+  T *x, *r, *z, *p, *q;
+  double* part;      // per chunk: <p, q>, <r, z>, <r, r>
+  GMeshScal* gs;
+  const double* target;  // per mesh: stop when <r, r> <= target
+  const int32_t* gch;    // the group's chunks
+  int ngch;
+  int iters;             // iterations of this launch
+  int i0;                // index of its first iteration within the group's run
+  GridBar* bar;
+};
+
+template <class T>
+__global__ void __launch_bounds__(kGThreads) BGroupPcgKernel(GArgs<T> g) {
+  __shared__ double red[32];
+  __shared__ double s_rz[kGMaxSlots], s_alpha;
+  __shared__ T s_beta[kGMaxSlots];
+  __shared__ int s_act[kGMaxSlots];
+  const int nslot = g.ngch > static_cast<int>(blockIdx.x)
+                        ? (g.ngch - static_cast<int>(blockIdx.x) + static_cast<int>(gridDim.x) - 1) /
+                              static_cast<int>(gridDim.x)
+                        : 0;
+  for (int k = 0;; ++k) {
+    const int i = g.i0 + k;
+    // ---- phase 1: stopping test and beta per mesh, p = z + beta p
+    for (int sl = 0; sl < nslot; ++sl) {
+      const int c = g.gch[blockIdx.x + sl * gridDim.x];
+      const int b = g.C.mesh[c];
+      const int64_t c0 = g.C.mesh_chunk[b], c1 = g.C.mesh_chunk[b + 1];
+      // read once per block: the flag may be set by the mesh's owner block
+      // during this very phase (its test gives every block the same answer)
+      __shared__ int s_live;
+      if (threadIdx.x == 0) s_live = !LdVolI(&g.gs[b].frozen);
+      __syncthreads();
+      if (s_live) {
+        const double rz = GMeshSum(g.part, 1, c0, c1, red);
+        const double rr = GMeshSum(g.part, 2, c0, c1, red);
+        if (threadIdx.x == 0) {
+          const double prev = i > 0 ? __ldcg(&g.gs[b].rz[(i - 1) & 1]) : 0.0;
+          const bool conv = !(rr > g.target[b]);
+          s_rz[sl] = rz;
+          s_beta[sl] = static_cast<T>(prev != 0.0 ? rz / prev : 0.0);
+          s_act[sl] = !conv && k < g.iters;
+          if (c == c0) {
+            g.gs[b].rz[i & 1] = rz;
+            g.gs[b].rr = rr;
+            g.gs[b].it = i;
+            if (conv) g.gs[b].frozen = 1;
+          }
+        }
+      } else if (threadIdx.x == 0) {
+        s_act[sl] = 0;
+      }
+      __syncthreads();
+      if (s_act[sl]) {
+        const T beta = s_beta[sl];
+        for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x)
+          g.p[rw] = fma(beta, __ldcg(g.p + rw), __ldcg(g.z + rw));
+      }
+    }
+    if (k == g.iters) break;
+    if (!GridSync(g.bar)) return;
+    // ---- phase 2: q = A p, <p, q> per chunk
+    for (int sl = 0; sl < nslot; ++sl) {
+      if (!s_act[sl]) continue;  // uniform per block
+      const int c = g.gch[blockIdx.x + sl * gridDim.x];
+      BDot<T> acc;
+      for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x) {
+        const int64_t slc = rw >> 5, lane = rw & 31;
+        const int64_t b0 = g.M.ptr[slc];
+        const int w = static_cast<int>((g.M.ptr[slc + 1] - b0) >> 5);
+        const int32_t* cp = g.M.col + b0 + lane;
+        const T* vp = g.val + b0 + lane;
+        const T pr = __ldcg(g.p + rw);
+        T sum = T(0);
+        if (g.rowsum) {
+#pragma unroll 4
+          for (int kk = 0; kk < w; ++kk) sum = fma(vp[kk * 32], __ldcg(g.p + cp[kk * 32]) - pr, sum);
+          sum = fma(g.rowsum[rw], pr, sum);
+        } else {
+#pragma unroll 4
+          for (int kk = 0; kk < w; ++kk) sum = fma(vp[kk * 32], __ldcg(g.p + cp[kk * 32]), sum);
+        }
+        g.q[rw] = sum;
+        acc.add(pr, sum);
+      }
+      const double tot = BlockReduce(acc.get(), red);
+      if (threadIdx.x == 0) g.part[3 * c] = tot;
+    }
+    if (!GridSync(g.bar)) return;
+    // ---- phase 3: alpha = rz / <p, q>; x += alpha p, r -= alpha q, z = D^-1 r
+    for (int sl = 0; sl < nslot; ++sl) {
+      if (!s_act[sl]) continue;
+      const int c = g.gch[blockIdx.x + sl * gridDim.x];
+      const int b = g.C.mesh[c];
+      const double pq = GMeshSum(g.part, 0, g.C.mesh_chunk[b], g.C.mesh_chunk[b + 1], red);
+      if (threadIdx.x == 0) s_alpha = pq != 0.0 ? s_rz[sl] / pq : 0.0;
+      __syncthreads();
+      const T alpha = static_cast<T>(s_alpha);
+      BDot<T> arz, arr;
+      for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x) {
+        g.x[rw] = fma(alpha, __ldcg(g.p + rw), __ldcg(g.x + rw));
+        const T ri = fma(-alpha, __ldcg(g.q + rw), __ldcg(g.r + rw));
+        g.r[rw] = ri;
+        const T zi = g.dinv[rw] * ri;
+        g.z[rw] = zi;
+        arz.add(ri, zi);
+        arr.add(ri, ri);
+      }
+      const double s1 = BlockReduce(arz.get(), red);
+      const double s2 = BlockReduce(arr.get(), red);
+      if (threadIdx.x == 0) {
+        g.part[3 * c + 1] = s1;
+        g.part[3 * c + 2] = s2;
+      }
+    }
+    if (!GridSync(g.bar)) return;
+  }
+}
+
+// Start of a grouped run on the listed chunks: z = D^-1 r, p = 0, the <r, z>
+// and <r, r> partials.  With `scale` (mixed), r = r64 * scale[mesh] first and
+// d = 0; with `sel`, only the meshes with sel[mesh] set (a residual
+// replacement: p is kept).
+template <class T>
+__global__ void __launch_bounds__(kGThreads) GStartKernel(Chunks C, const int32_t* __restrict__ gch, int ngch,
+                                                          const T* __restrict__ dinv, const double* __restrict__ r64,
+                                                          const double* __restrict__ scale,
+                                                          const int32_t* __restrict__ sel, T* __restrict__ r,
+                                                          T* __restrict__ z, T* __restrict__ p, T* __restrict__ d,
+                                                          double* __restrict__ part) {
+  __shared__ double red[32];
+  for (int j = blockIdx.x; j < ngch; j += gridDim.x) {
+    const int c = gch ? gch[j] : j;
+    const int b = C.mesh[c];
+    if (sel && !sel[b]) continue;  // uniform per block
+    double arz = 0.0, arr = 0.0;
+    const double sc = scale ? scale[b] : 1.0;
+    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
+      const T ri = scale ? static_cast<T>(r64[i] * sc) : r[i];
+      const T zi = dinv[i] * ri;
+      if (scale) r[i] = ri;
+      z[i] = zi;
+      if (!sel) p[i] = T(0);
+      if (d) d[i] = T(0);
+      arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
+      arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
+    }
+    const double s1 = BlockReduce(arz, red);
+    const double s2 = BlockReduce(arr, red);
+    if (threadIdx.x == 0) {
+      part[3 * c + 1] = s1;
+      part[3 * c + 2] = s2;
+    }
+  }
+}
+
+// Row count of every mesh's CSR rows: nnz[b] = rowptr[dof_off[b + 1]] - rowptr[dof_off[b]].
+__global__ void MeshNnzKernel(int nb, const int64_t* __restrict__ dof_off, const int64_t* __restrict__ rowptr,
+                              int64_t* __restrict__ nnz) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) nnz[b] = rowptr[dof_off[b + 1]] - rowptr[dof_off[b]];
+}
+
 // Per-mesh sums of chunk partials on the host (chunk order).
 void MeshSums(lfg_batch* B, const double* dev_part, std::vector<double>& out) {
   std::vector<double> h(B->nchunks);
@@ -660,6 +911,125 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* 
   cudaGraphExecDestroy(exec);
   cudaGraphDestroy(graph);
   rr_out = rr;
+}
+
+// ---------------------------------------------------- grouped solver host
+struct GBufs {
+  DevBuf part, gs, bar, gch, target;
+  std::vector<GMeshScal> gs_h;
+  int grid = 0;
+};
+
+// nnz of every mesh's block of the CSR matrix.
+std::vector<int64_t> MeshNnz(lfg_batch* B, lfg_csr* A) {
+  lfg_ctx* ctx = B->ctx;
+  DevBuf off, out;
+  off.alloc((B->nb + 1) * sizeof(int64_t), ctx->stream);
+  out.alloc(B->nb * sizeof(int64_t), ctx->stream);
+  LFG_CUDA(cudaMemcpyAsync(off.p, B->dof_off.data(), (B->nb + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  MeshNnzKernel<<<(B->nb + 127) / 128, 128, 0, ctx->stream>>>(B->nb, off.as<int64_t>(), A->rowptr.as<int64_t>(),
+                                                              out.as<int64_t>());
+  LFG_LAUNCHED(ctx);
+  std::vector<int64_t> h(B->nb);
+  D2HSync(ctx, h.data(), out.p, B->nb * sizeof(int64_t));
+  return h;
+}
+
+// Meshes with want[b] packed into groups of at most `budget` bytes of solver
+// data in precision T (padded matrix, Jacobi diagonal, row sums and the five
+// work vectors), largest first; a mesh larger than the budget is a group of
+// its own.  A group also holds at most max_chunks chunks.
+template <class T>
+std::vector<std::vector<int>> PackGroups(lfg_batch* B, const std::vector<int64_t>& nnz,
+                                         const std::vector<int32_t>& want, double budget, int64_t max_chunks) {
+  std::vector<int> order;
+  for (int b = 0; b < B->nb; ++b)
+    if (want[b]) order.push_back(b);
+  auto rows = [&](int b) { return B->dof_off[b + 1] - B->dof_off[b]; };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rows(a) > rows(b); });
+  std::vector<std::vector<int>> groups;
+  double used = 0.0;
+  int64_t chunks = 0;
+  for (int b : order) {
+    const double bytes = 1.1 * static_cast<double>(nnz[b]) * (4.0 + sizeof(T)) +
+                         static_cast<double>(rows(b)) * 7.0 * sizeof(T);
+    const int64_t ch = B->h_mesh_chunk_off[b + 1] - B->h_mesh_chunk_off[b];
+    if (groups.empty() || used + bytes > budget || chunks + ch > max_chunks) {
+      groups.emplace_back();
+      used = 0.0;
+      chunks = 0;
+    }
+    groups.back().push_back(b);
+    used += bytes;
+    chunks += ch;
+  }
+  return groups;
+}
+
+// Grouped PCG in precision T over `groups`: per group, start (z = D^-1 r,
+// p = 0; with r64 / scale the residual is first taken from r64 * scale), then
+// cooperative launches of `body` iterations until every mesh of the group is
+// frozen or max_it; `after(group)` runs after every launch with G.gs_h read
+// back (it may change device state and frozen flags, and then uploads gs).
+// it_out[b] = iterations done by mesh b.
+template <class T, class After>
+void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, T* r, T* z, T* p, T* q,
+          T* d, const double* r64, const double* scale, GBufs& G, const Chunks& C,
+          const std::vector<std::vector<int>>& groups, int max_it, int body, After after, std::vector<int>& it_out) {
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+  for (const std::vector<int>& grp : groups) {
+    std::vector<int32_t> gch;
+    for (int b : grp)
+      for (int64_t c = B->h_mesh_chunk_off[b]; c < B->h_mesh_chunk_off[b + 1]; ++c) gch.push_back(static_cast<int32_t>(c));
+    const int ngch = static_cast<int>(gch.size());
+    if (!ngch) continue;
+    if (ngch > G.grid * kGMaxSlots) Fail(LFG_UNSUPPORTED, "batched PCG: a group exceeds the cooperative grid");
+    LFG_CUDA(cudaMemcpyAsync(G.gch.p, gch.data(), ngch * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    LFG_CUDA(cudaMemsetAsync(G.gs.p, 0, B->nb * sizeof(GMeshScal), s));
+    LFG_CUDA(cudaMemsetAsync(G.bar.p, 0, sizeof(GridBar), s));
+    GStartKernel<T><<<std::min(ngch, G.grid * 4), kGThreads, 0, s>>>(C, G.gch.as<int32_t>(), ngch, dinv, r64, scale,
+                                                                      nullptr, r, z, p, d, G.part.as<double>());
+    LFG_LAUNCHED(ctx);
+    int i0 = 0;
+    while (true) {
+      GArgs<T> ga{C, M, sval, rowsum, dinv, x, r, z, p, q, G.part.as<double>(), G.gs.as<GMeshScal>(),
+                  G.target.as<double>(), G.gch.as<int32_t>(), ngch, std::min(body, max_it - i0), i0,
+                  G.bar.as<GridBar>()};
+      void* args[] = {&ga};
+      LFG_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&BGroupPcgKernel<T>), dim3(G.grid),
+                                           dim3(kGThreads), args, 0, s));
+      CountLaunch(ctx, 1);
+      i0 += ga.iters;
+      GridBar bar{};
+      LFG_CUDA(cudaMemcpyAsync(&bar, G.bar.p, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
+      D2HSync(ctx, G.gs_h.data(), G.gs.p, B->nb * sizeof(GMeshScal));
+      if (bar.err) Fail(LFG_CUDA_ERROR, "batched PCG: a grid barrier of the grouped solver timed out");
+      after(grp, i0);
+      int active = 0;
+      for (int b : grp) active += !G.gs_h[b].frozen;
+      if (!active || i0 >= max_it) break;
+    }
+    for (int b : grp) it_out[b] = G.gs_h[b].it;
+  }
+}
+
+template <class T>
+void GAlloc(lfg_batch* B, GBufs& G) {
+  lfg_ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  G.part.alloc(3 * std::max<int64_t>(B->nchunks, 1) * sizeof(double), s);
+  G.gs.alloc(B->nb * sizeof(GMeshScal), s);
+  G.bar.alloc(sizeof(GridBar), s);
+  G.gch.alloc(std::max<int64_t>(B->nchunks, 1) * sizeof(int32_t), s);
+  G.target.alloc(B->nb * sizeof(double), s);
+  G.gs_h.assign(B->nb, GMeshScal{});
+  int per_sm = 0;
+  LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BGroupPcgKernel<T>, kGThreads, 0));
+  if (per_sm < 1) Fail(LFG_CUDA_ERROR, "grouped PCG kernel cannot be resident");
+  G.grid = ctx->num_sms * std::min(per_sm, 2);
 }
 
 // Chunks of `rows` rows, never straddling two meshes.
@@ -870,6 +1240,20 @@ lfg_status lfg_batch_solve_tuning(const lfg_batch* B, int32_t precision, int32_t
   return LFG_OK;
 }
 
+lfg_status lfg_batch_set_solve_groups(lfg_batch* B, double group_bytes) {
+  if (!B) return LFG_INVALID_ARG;
+  LFG_API_BEGIN(B->ctx)
+  if (!(group_bytes >= 0.0)) Fail(LFG_INVALID_ARG, "group_bytes must be >= 0");
+  B->solve_group_bytes = group_bytes;
+  LFG_API_END
+}
+
+lfg_status lfg_batch_solve_groups(const lfg_batch* B, double* group_bytes) {
+  if (!B || !group_bytes) return LFG_INVALID_ARG;
+  *group_bytes = B->solve_group_bytes;
+  return LFG_OK;
+}
+
 lfg_status lfg_batch_set_solve_chunk_rows(lfg_batch* B, int32_t precision, int32_t chunk_rows) {
   if (!B) return LFG_INVALID_ARG;
   LFG_API_BEGIN(B->ctx)
@@ -1032,7 +1416,20 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
   PrepareSolve(A);  // Jacobi diagonal, int32 row pointers, SELL-32 copy
   const bool mixed = opts->precision == LFG_SOLVE_MIXED;
   if (mixed) EnsureFloatValues(A);  // FP32 SELL values and row sums
-  {
+  bool grouped = B->solve_group_bytes > 0.0;
+  if (grouped) {
+    BuildChunks(B, kGChunkRows);
+    // every mesh must fit one cooperative grid (at most kGMaxSlots chunks per block)
+    int per_sm = 0;
+    LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, mixed ? reinterpret_cast<const void*>(&BGroupPcgKernel<float>)
+                       : reinterpret_cast<const void*>(&BGroupPcgKernel<double>),
+        kGThreads, 0));
+    const int64_t max_chunks = static_cast<int64_t>(ctx->num_sms) * std::min(per_sm, 2) * kGMaxSlots;
+    for (int b = 0; b < B->nb && grouped; ++b)
+      grouped = per_sm >= 1 && B->h_mesh_chunk_off[b + 1] - B->h_mesh_chunk_off[b] <= max_chunks;
+  }
+  if (!grouped) {
     const int pi = mixed ? 1 : 0;
     const int chk = opts->check_every > 0 ? opts->check_every : 32;
     if (!B->solve_tuned[pi]) {
@@ -1065,9 +1462,31 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
   for (int b = 0; b < B->nb; ++b) target[b] = rtol * rtol * bb[b];
   std::vector<int32_t> frozen_h(B->nb, 0);
   std::vector<int> its(B->nb, 0), refinements(B->nb, 0);
+  const int body = std::max(2, check + (check & 1));
   if (opts->precision == LFG_SOLVE_FP64) {
     std::vector<int> it1;
     std::vector<double> rr1;
+    if (grouped) {
+      GBufs G;
+      GAlloc<double>(B, G);
+      std::vector<int32_t> want(B->nb);
+      for (int b = 0; b < B->nb; ++b) want[b] = rr[b] > target[b];
+      const auto groups = PackGroups<double>(B, MeshNnz(B, A), want, B->solve_group_bytes,
+                                             static_cast<int64_t>(G.grid) * kGMaxSlots);
+      LFG_CUDA(cudaMemcpyAsync(G.target.p, target.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
+      std::vector<int> itg(B->nb, 0);
+      GRun<double>(B, A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, S.r.as<double>(),
+                   S.z.as<double>(), S.p.as<double>(), S.q.as<double>(), nullptr, nullptr, nullptr, G, C, groups,
+                   max_it, body, [](const std::vector<int>&, int) {}, itg);
+      for (int b = 0; b < B->nb; ++b) {
+        its[b] += itg[b];
+        refinements[b] += itg[b] > 0;
+      }
+      BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(), x,
+                                          bvec, S.r.as<double>(), S.part.as<double>());
+      LFG_LAUNCHED(ctx);
+      MeshSums(B, S.part.as<double>(), rr);
+    }
     // restart on the true residual when the recursive one drifted (<= 4 times)
     for (int round = 0; round < 5; ++round) {
       std::vector<int32_t> fz(B->nb, 0);
@@ -1112,6 +1531,111 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
       t32[b] = target[b] * sc[b] * sc[b];
     }
     LFG_CUDA(cudaMemcpyAsync(scale.p, sc.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (grouped) {
+      GBufs G;
+      GAlloc<float>(B, G);
+      std::vector<int32_t> want(B->nb), done(B->nb, 0), cont(B->nb);
+      for (int b = 0; b < B->nb; ++b) want[b] = rr[b] > target[b];
+      const auto groups = PackGroups<float>(B, MeshNnz(B, A), want, B->solve_group_bytes,
+                                            static_cast<int64_t>(G.grid) * kGMaxSlots);
+      LFG_CUDA(cudaMemcpyAsync(G.target.p, t32.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
+      std::vector<int> itg(B->nb, 0);
+      std::vector<double> rr_new;
+      // after every launch: residual replacement for the meshes whose FP32
+      // residual dropped by `drop` (or that the kernel stopped as converged)
+      auto after = [&](const std::vector<int>& grp, int i_done) {
+        int nsel = 0;
+        for (int b = 0; b < B->nb; ++b) sl[b] = 0;
+        for (int b : grp) {
+          if (done[b]) continue;
+          const GMeshScal& m = G.gs_h[b];
+          if (!std::isfinite(m.rr)) {  // FP32 broke down: finish this block in FP64 from its x
+            failed[b] = 1;
+            done[b] = 1;
+            G.gs_h[b].frozen = 1;
+            continue;
+          }
+          sl[b] = m.frozen || !(m.rr >= drop * ref32[b]) || i_done >= max_it;
+          nsel += sl[b];
+        }
+        if (!nsel) {
+          LFG_CUDA(cudaMemcpyAsync(G.gs.p, G.gs_h.data(), B->nb * sizeof(GMeshScal), cudaMemcpyHostToDevice, s));
+          return;
+        }
+        LFG_CUDA(cudaMemcpyAsync(sel.p, sl.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        BApplyKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), sel.as<int32_t>(), 1.0, x);
+        LFG_LAUNCHED(ctx);
+        BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(), A->val.as<double>(),
+                                            x, bvec, S.r.as<double>(), S.part.as<double>(), sel.as<int32_t>());
+        LFG_LAUNCHED(ctx);
+        MeshSums(B, S.part.as<double>(), rr_new);
+        int nrevert = 0, nkeep = 0;
+        for (int b = 0; b < B->nb; ++b) {
+          cont[b] = 0;
+          if (!sl[b]) continue;
+          refinements[b] += 1;
+          const double claimed = G.gs_h[b].rr / (sc[b] * sc[b]);
+          if (rr_new[b] <= target[b]) {
+            rr[b] = rr_new[b];
+            done[b] = 1;
+            G.gs_h[b].frozen = 1;
+          } else if (!(rr_new[b] < 0.25 * rr_last[b]) && !(rr_new[b] <= 16.0 * claimed)) {
+            failed[b] = 1;
+            done[b] = 1;
+            G.gs_h[b].frozen = 1;
+            if (!(rr_new[b] < rr_last[b])) {
+              sl[b] = 2;
+              ++nrevert;
+            } else {
+              rr[b] = rr_new[b];
+            }
+          } else {
+            rr[b] = rr_last[b] = rr_new[b];
+            ref32[b] = rr_new[b] * sc[b] * sc[b];
+            if (i_done >= max_it) {
+              done[b] = 1;
+              G.gs_h[b].frozen = 1;
+            } else {
+              cont[b] = 1;
+              ++nkeep;
+              if (G.gs_h[b].frozen) {
+                // resumed after the kernel stopped it at iteration it: its
+                // last <r, z> goes to both slots, whatever the group's parity
+                const double last = G.gs_h[b].rz[G.gs_h[b].it & 1];
+                G.gs_h[b].rz[0] = G.gs_h[b].rz[1] = last;
+                G.gs_h[b].frozen = 0;
+              }
+            }
+          }
+        }
+        if (nrevert) {
+          for (int b = 0; b < B->nb; ++b) sl[b] = sl[b] == 2;
+          LFG_CUDA(cudaMemcpyAsync(sel.p, sl.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+          BApplyKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), sel.as<int32_t>(), -1.0, x);
+          LFG_LAUNCHED(ctx);
+          BResidualKernel<<<grid, kPB, 0, s>>>(C, A->rowptr32.as<int32_t>(), A->col.as<int32_t>(),
+                                              A->val.as<double>(), x, bvec, S.r.as<double>(), S.part.as<double>(),
+                                              sel.as<int32_t>());
+          LFG_LAUNCHED(ctx);
+          MeshSums(B, S.part.as<double>(), rr_new);
+          for (int b = 0; b < B->nb; ++b)
+            if (sl[b]) rr[b] = rr_new[b];
+        }
+        if (nkeep) {
+          LFG_CUDA(cudaMemcpyAsync(sel.p, cont.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+          GStartKernel<float><<<grid, kGThreads, 0, s>>>(C, nullptr, static_cast<int>(C.nchunks),
+                                                         A->dinv32.as<float>(), S.r.as<double>(), scale.as<double>(),
+                                                         sel.as<int32_t>(), S32.r.as<float>(), S32.z.as<float>(),
+                                                         S32.p.as<float>(), d32.as<float>(), G.part.as<double>());
+          LFG_LAUNCHED(ctx);
+        }
+        LFG_CUDA(cudaMemcpyAsync(G.gs.p, G.gs_h.data(), B->nb * sizeof(GMeshScal), cudaMemcpyHostToDevice, s));
+      };
+      GRun<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
+                  S32.r.as<float>(), S32.z.as<float>(), S32.p.as<float>(), S32.q.as<float>(), d32.as<float>(),
+                  S.r.as<double>(), scale.as<double>(), G, C, groups, max_it, body, after, itg);
+      for (int b = 0; b < B->nb; ++b) its[b] += itg[b];
+    } else {
     LFG_CUDA(cudaMemcpyAsync(frozen32.p, fz.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     BScaleKernel<<<grid, kPB, 0, s>>>(C, S.r.as<double>(), scale.as<double>(), S32.r.as<float>(), d32.as<float>());
     LFG_LAUNCHED(ctx);
@@ -1119,7 +1643,6 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
                                              S32.p.as<float>(), frozen32.as<int32_t>(), S32.part.as<double>(),
                                              S32.ms.as<MeshScal>());
     LFG_LAUNCHED(ctx);
-    const int body = std::max(2, check + (check & 1));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     BCapture<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
@@ -1217,12 +1740,13 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
     }
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);
+    }
     // blocks FP32 could not finish: FP64 PCG from their current iterate
     int nfailed = 0;
     for (int b = 0; b < B->nb; ++b) nfailed += failed[b] && rr[b] > target[b];
     if (nfailed) {
       std::vector<int> it1;
-      std::vector<double> rr1;
+      std::vector<double> rr1, rr_new;
       for (int round = 0; round < 5; ++round) {
         std::vector<int32_t> f64(B->nb, 1);
         int act = 0;

@@ -110,3 +110,48 @@ def test_batch_solver_chunk_autotuner(ctx, precision):
         assert np.linalg.norm(x.download() - ref) <= 1e-8 * np.linalg.norm(ref)
     with pytest.raises(L.LfgError):
         batch.set_solve_chunk_rows(precision, 8)
+
+
+@pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
+def test_batch_grouped_solver(ctx, precision):
+    """The grouped solver (L2-sized groups, persistent cooperative kernel with
+    grid barriers) gives every block the solution of the lock-step sweep: one
+    group holding every mesh (a block of 161k rows spreads over more chunks
+    than the grid has blocks), one group per mesh, and a middle budget; each
+    block also against a direct solve of the oracle's system."""
+    import scipy.sparse.linalg as spla
+    ns, degs = [40, 24, 200, 33, 47, 6, 61, 38], [2, 1, 2, 2, 1, 2, 1, 2]
+    meshes, spaces, batch, alpha = _batch(ctx, ns, degs, seed=21)
+    alpha_d = ctx.to_device(alpha)
+    coo = _assemble(ctx, batch, alpha_d)
+    b = ctx.zeros(batch.num_dofs)
+    batch.assemble_vector_load(L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+    coo.fix_flagged_solution_components(batch.boundary_dof_flags(), ctx.zeros(batch.num_dofs), b)
+    csr = coo.make_sparse()
+    assert batch.solve_groups() == 0.0
+    x0 = ctx.zeros(batch.num_dofs)
+    assert batch.solve_pcg(csr, b, x0, precision=precision, rtol=1e-11)["converged"]
+    ref = x0.download()
+    dof, cell, _ = batch.offsets()
+    for budget in (1e12, 1.0, 4e6):
+        batch.set_solve_groups(budget)
+        assert batch.solve_groups() == budget
+        x = ctx.zeros(batch.num_dofs)
+        st = batch.solve_pcg(csr, b, x, precision=precision, rtol=1e-11)
+        assert st["converged"] and all(blk["converged"] for blk in st["blocks"]), budget
+        xs = x.download()
+        for k in range(len(ns)):
+            seg, r = xs[dof[k]:dof[k + 1]], ref[dof[k]:dof[k + 1]]
+            assert np.linalg.norm(seg - r) <= 1e-8 * np.linalg.norm(r), (budget, k)
+    for k in (0, 2, 5):
+        n, d = ns[k], degs[k]
+        xy, cells, pe = O.factory_input("tptriag", n, n)
+        os_ = O.Space(O.Mesh(xy, cells, pe), d)
+        A = O.assemble_rd(os_, O.coeff(O.PER_CELL, data=alpha[cell[k]:cell[k + 1]]), O.coeff(O.CONSTANT, 1.0))
+        bo = O.assemble_load(os_, O.coeff(O.CONSTANT, 1.0))
+        A.fix_flagged(os_.boundary_dof_flags(), np.zeros(os_.num_dofs), bo)
+        xo = spla.splu(A.to_scipy().tocsc()).solve(bo)
+        assert np.linalg.norm(xs[dof[k]:dof[k + 1]] - xo) <= 1e-8 * np.linalg.norm(xo), k
+    with pytest.raises(L.LfgError):
+        batch.set_solve_groups(-1.0)
+    batch.set_solve_groups(0.0)
