@@ -130,14 +130,14 @@ def test_batch_grouped_solver(ctx, precision):
     csr = coo.make_sparse()
     assert batch.solve_groups() == 0.0
     x0 = ctx.zeros(batch.num_dofs)
-    assert batch.solve_pcg(csr, b, x0, precision=precision, rtol=1e-11)["converged"]
+    assert batch.solve_pcg(csr, b, x0, precision=precision, rtol=1e-10)["converged"]
     ref = x0.download()
     dof, cell, _ = batch.offsets()
     for budget in (1e12, 1.0, 4e6):
         batch.set_solve_groups(budget)
         assert batch.solve_groups() == budget
         x = ctx.zeros(batch.num_dofs)
-        st = batch.solve_pcg(csr, b, x, precision=precision, rtol=1e-11)
+        st = batch.solve_pcg(csr, b, x, precision=precision, rtol=1e-10)
         assert st["converged"] and all(blk["converged"] for blk in st["blocks"]), budget
         xs = x.download()
         for k in range(len(ns)):
