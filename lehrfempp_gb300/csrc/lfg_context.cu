@@ -44,6 +44,11 @@ void CountLaunch(lfg_ctx* ctx, int n) { ctx->launches += n; }
 int32_t* StatusWord(lfg_ctx* ctx) { return ctx->status.as<int32_t>(); }
 
 void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes) {
+  if (bytes > kPinnedSmallBytes) {  // larger reads go straight to the (pageable) destination
+    LFG_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    LFG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return;
+  }
   LFG_CUDA(cudaMemcpyAsync(ctx->pinned_small, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   LFG_CUDA(cudaStreamSynchronize(ctx->stream));
   std::memcpy(host, ctx->pinned_small, bytes);
@@ -197,7 +202,7 @@ lfg_status lfg_ctx_create(int device, lfg_ctx** out) {
     }
     ctx->status.alloc(64, ctx->stream);
     LFG_CUDA(cudaMemsetAsync(ctx->status.p, 0, 64, ctx->stream));
-    LFG_CUDA(cudaMallocHost(&ctx->pinned_small, 4096));
+    LFG_CUDA(cudaMallocHost(&ctx->pinned_small, kPinnedSmallBytes));
     LFG_CUDA(cudaStreamSynchronize(ctx->stream));
     *out = ctx;
     return LFG_OK;

@@ -242,6 +242,9 @@ void RadixSortPairs64(lfg_ctx* ctx, uint64_t* keys, uint64_t* vals, int64_t n, i
 int32_t ReadAndClearStatus(lfg_ctx* ctx, int32_t* detail = nullptr);
 int32_t* StatusWord(lfg_ctx* ctx);
 // Copy a small device value to the host synchronously (stream ordered).
+// Stream-ordered device -> host read followed by a stream synchronize; reads
+// up to kPinnedSmallBytes go through the context's pinned staging buffer.
+constexpr size_t kPinnedSmallBytes = 4096;
 void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
 // Solver data of a CSR matrix (lfg_csr.cu): Jacobi diagonal (FP64 + FP32),
 // int32 row pointers and the SELL-32 copy; FP32 values for mixed precision.

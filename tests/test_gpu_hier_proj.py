@@ -55,6 +55,20 @@ def test_hier_var_projection_matches_oracle(ctx, mname, spec):
     _check(ctx, sp, osp, 0, _tol(6), mesh, rng)
 
 
+def test_hier_var_projection_larger_mesh(ctx):
+    """Per-entity degrees 1..5 on a 24 x 24 hybrid mesh (about 900 cells, many
+    distinct dual tables) against the oracle."""
+    spec = _hybrid(24, seed=6)
+    om = oracle_mesh(spec)
+    rng = np.random.default_rng(77)
+    ed = rng.integers(1, 6, om.num_edges).astype(np.int32)
+    cd = rng.integers(1, 6, om.num_cells).astype(np.int32)
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic_var(mesh, ed, cd)
+    osp = O.hier_var_space(om, ed, cd)
+    _check(ctx, sp, osp, 0, _tol(5), mesh, rng, ukinds=("nodal", "sincos"))
+
+
 @pytest.mark.parametrize("p", [2, 4])
 def test_hier_var_projection_with_equal_degrees_is_the_uniform_one(ctx, p):
     spec = _hybrid(6, seed=2)
