@@ -723,6 +723,14 @@ def batch_leg(L, W, ctx, count, superlu_meshes=0):
     dt = time.perf_counter() - t0
     out["plain_fp64"] = {"dofs_per_s": sd / dt, "seconds": dt, "rtol": plain_rtol,
                           "sample": "every 8th mesh (%d meshes, %d dofs), one mesh at a time" % (len(sample), sd)}
+    # the grouped scheme (L2-sized groups, persistent cooperative kernel), FP64
+    # at the same target, for the record (the lock-step sweep is the default)
+    batch.set_solve_groups(96e6)
+    x, st, dt, launches = run(L.SOLVE_FP64, plain_rtol)
+    batch.set_solve_groups(0.0)
+    out["grouped_96MB_fp64"] = {"dofs_per_s": nd / dt, "seconds": dt, "rtol": plain_rtol, "gpu_launches": launches,
+                                "max_mesh_rel_err": max(mesh_errs(x.download())),
+                                "max_iterations": max(blk["iterations"] for blk in st["blocks"])}
     best = max((out[k]["to_1e-8_err"]["dofs_per_s"] for k in ("mixed", "fp64") if "to_1e-8_err" in out[k]), default=None)
     if best:
         out["best_batched_vs_plain_fp64_at_1e-8_err"] = best / out["plain_fp64"]["dofs_per_s"]
@@ -895,6 +903,8 @@ def summarize(line):
         t["mixed_vs_fp64"] = _r(ba.get("mixed_vs_fp64_at_1e-8_err"), 3)
         t["best_vs_plain"] = _r(ba.get("best_batched_vs_plain_fp64_at_1e-8_err"), 3)
         t["max_err_vs_superlu"] = _r(_get(ba, "superlu_subset", "max_rel_err"), 2)
+        t["grouped_fp64_Mdof_s"] = _r(_get(ba, "grouped_96MB_fp64", "dofs_per_s") and
+                                      ba["grouped_96MB_fp64"]["dofs_per_s"] / 1e6)
         s["c4_batch"] = t
     gr = line.get("gradient") or {}
     if "store" in gr:
