@@ -773,24 +773,6 @@ __device__ __forceinline__ uint32_t HSub2(uint32_t a, uint32_t b) {
   return d;
 }
 
-// t 2^shift as binary64 rounded to nearest even (__ll2double_rn(t) with its
-// exponent raised by shift), from integer operations only: a 64-bit integer
-// to FP64 conversion runs on GB300's narrow FP64 pipe (about 64 cycles per
-// warp instruction per SM sub-partition).  The result must be a normal number.
-__device__ __forceinline__ double ScaledI64ToDouble(long long t, int shift) {
-  if (t == 0) return 0.0;
-  const unsigned long long sign = static_cast<unsigned long long>(t) & (1ull << 63);
-  unsigned long long u = sign ? 0ull - static_cast<unsigned long long>(t) : static_cast<unsigned long long>(t);
-  const int lz = __clzll(static_cast<long long>(u));
-  u <<= lz;                                 // leading one at bit 63
-  const unsigned long long mant = u >> 11;  // 53 significant bits
-  const unsigned int tail = static_cast<unsigned int>(u) & 0x7ffu;
-  const unsigned long long up = (tail > 0x400u) || (tail == 0x400u && (mant & 1ull));
-  const unsigned long long e = static_cast<unsigned long long>(1023 + 63 - lz + shift);
-  // a carry out of the mantissa moves into the exponent field
-  return __longlong_as_double(static_cast<long long>(sign | ((e << 52) + (mant - (1ull << 52)) + up)));
-}
-
 // G2 2^36 + G3 2^27 + G4 2^18 + G5 2^9 + G67 scaled by 2^shift, as binary64.
 __device__ __forceinline__ double TcCombine(float g2, float g3, float g4, float g5, float g67, int shift) {
   // |G2|, |G3| < 2^22: integer bits by the 1.5 2^23 shift on the FP32 pipe
@@ -799,7 +781,8 @@ __device__ __forceinline__ double TcCombine(float g2, float g3, float g4, float 
   const int hi = i2 * 512 + i3;
   const long long mid = static_cast<long long>(__float2int_rn(g4)) * 512 + __float2int_rn(g5);
   const long long t = static_cast<long long>(hi) * (1ll << 27) + mid * 512 + __float2int_rn(g67);
-  return ScaledI64ToDouble(t, shift);
+  if (t == 0) return 0.0;
+  return __longlong_as_double(__double_as_longlong(__ll2double_rn(t)) + (static_cast<long long>(shift) << 52));
 }
 
 // elem::DfSafe on the exponent bits (integer pipe; |x| = 2^40 exactly counts

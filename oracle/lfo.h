@@ -272,6 +272,9 @@ struct Integrand {
   const DofHandler* dh = nullptr;
   int degree = 0;
   const double* dofs = nullptr;
+  // u_h on a hierarchic space: its uniform degree, or 0 for per-entity
+  // degrees (-1: Lagrangian of `degree`)
+  int hier = -1;
 };
 // IntegrateMeshFunction (fe/fe_tools.h:110-165) with make_QuadRule(., qdeg)
 // per reference element; flags select entities of the given codim (null:

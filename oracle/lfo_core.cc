@@ -1149,6 +1149,37 @@ void MFPoint(const MeshFunction& u, const std::function<void(double, double, dou
 }
 
 // u_h and grad u_h (mesh_function_fe.h:72-91, mesh_function_grad_fe.h:93-118)
+int HierCellDegrees(const DofHandler& dh, idx_t c, int p, int& pc, int (&pe)[4]);
+
+// MeshFunctionFE / MeshFunctionGradFE on a hierarchic space: the cell's
+// FeHierarchicTria / Quad shape functions (its own degrees and orientations).
+void FEPointHier(const DofHandler& dh, int p, const double* dofs, idx_t c, const CellGeom& geo, double xh, double yh,
+                 double* val, double* grad) {
+  const Mesh& m = *dh.mesh;
+  const bool q = m.IsQuad(c);
+  int pc, pe[4];
+  HierCellDegrees(dh, c, p, pc, pe);
+  int8_t ori[4];
+  for (int j = 0; j < 4; ++j) ori[j] = m.cell_ori[c][j];
+  const int n = HierNumShapeVar(q, pc, pe);
+  std::vector<double> phi(n), dphi(2 * n);
+  EvalHierShapeVar(q, pc, pe, ori, xh, yh, phi.data(), reinterpret_cast<double(*)[2]>(dphi.data()));
+  const idx_t* d = dh.GlobalDofIndices(c);
+  double v = 0.0, gh[2] = {0.0, 0.0};
+  for (int i = 0; i < n; ++i) {
+    v += dofs[d[i]] * phi[i];
+    gh[0] += dofs[d[i]] * dphi[2 * i];
+    gh[1] += dofs[d[i]] * dphi[2 * i + 1];
+  }
+  *val = v;
+  if (grad) {
+    double JT[2][2];
+    geo.JinvT(xh, yh, JT);
+    grad[0] = JT[0][0] * gh[0] + JT[0][1] * gh[1];
+    grad[1] = JT[1][0] * gh[0] + JT[1][1] * gh[1];
+  }
+}
+
 void FEPoint(const DofHandler& dh, int degree, const double* dofs, idx_t c, const CellGeom& geo, double xh,
              double yh, double* val, double* grad) {
   const bool q = dh.mesh->IsQuad(c);
@@ -1173,7 +1204,8 @@ double IntegrandAt(const Integrand& g, const Mesh& m, idx_t c, const CellGeom& g
   const bool need_grad = g.kind == 2;
   double uv = 0.0, ug[2] = {0.0, 0.0}, hv = 0.0, hg[2] = {0.0, 0.0};
   MFPoint(g.u, g.grad_u, m, c, geo, xh, yh, &uv, need_grad ? ug : nullptr);
-  if (g.dofs) FEPoint(*g.dh, g.degree, g.dofs, c, geo, xh, yh, &hv, need_grad ? hg : nullptr);
+  if (g.dofs && g.hier >= 0) FEPointHier(*g.dh, g.hier, g.dofs, c, geo, xh, yh, &hv, need_grad ? hg : nullptr);
+  else if (g.dofs) FEPoint(*g.dh, g.degree, g.dofs, c, geo, xh, yh, &hv, need_grad ? hg : nullptr);
   switch (g.kind) {
     case 0: return hv + uv;
     case 1: return (hv - uv) * (hv - uv);
@@ -1232,6 +1264,7 @@ double IntegrateMeshFunction(const Mesh& m, const Integrand& g, int qdeg, const 
   }
   if (codim != 1) throw Error("IntegrateMeshFunction: codim must be 0 or 1");
   if (g.kind == 2) throw Error("IntegrateMeshFunction: gradients on edges are not supported");
+  if (g.dofs && g.hier >= 0) throw Error("IntegrateMeshFunction: hierarchic u_h on edges is not supported");
   std::vector<double> t, w;
   GaussLegendre(qdeg / 2 + 1, t, w);
   if (m.num_edges == 0) return 0.0;
