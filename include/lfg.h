@@ -640,6 +640,9 @@ lfg_status lfg_gmsh_physical_entities(const lfg_gmsh* g, int32_t codim, int32_t*
  * (num_cells or num_edges entries, NULL: all) selects entities; as in the
  * reference, entity 0 always contributes (fe_tools.h:117-124).  Gradients on
  * edges are LFG_UNSUPPORTED.  On codim 1 a PER_CELL u is indexed by edge.
+ * u_h may live on a Lagrangian (O1-O3) or a hierarchic space (uniform or
+ * per-entity degrees; each cell's own FeHierarchicTria / Quad shape
+ * functions; cells only, codim 1 is LFG_UNSUPPORTED there).
  * The sum is deterministic (fixed per-block order).  *result is host memory;
  * the call waits for it. */
 enum {

@@ -453,6 +453,17 @@ __global__ void __launch_bounds__(kHierBlock) HierLoadKernel(HierArgs a, CoeffDe
 
 }  // namespace
 
+const double* HierShapeTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, HierTabView& v) {
+  HierTab L;
+  const double* t = GetHierTable(ctx, quad, p, rule_degree, false, L);
+  v.n = L.n;
+  v.nq = L.nq;
+  v.off_pat = L.off_pat;
+  v.stride = L.stride;
+  v.o_g = L.o_g;
+  return t;
+}
+
 int HierRuleDegree(int requested, int p) { return requested == 0 ? 2 * p : requested; }
 
 bool CellConstantKind(const lfg_coeff& c) {

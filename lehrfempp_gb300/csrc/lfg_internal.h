@@ -158,6 +158,16 @@ struct HierGroup {
   int degree = 0;
   int64_t start = 0, count = 0;
 };
+// Shape values and reference gradients of the uniform degree-p hierarchic
+// element at the points of the rule of `rule_degree`, cached on the context
+// (lfg_hier.cu): w[nq] | x[nq] | y[nq] at the start, then per orientation
+// pattern pat (stride doubles apart, from off_pat) phi[nq][n] and, at o_g
+// within the pattern block, grad[nq][n][2].
+struct HierTabView {
+  int n = 0, nq = 0;
+  int64_t off_pat = 0, stride = 0, o_g = 0;
+};
+const double* HierShapeTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, HierTabView& v);
 }  // namespace lfg
 
 struct lfg_space {

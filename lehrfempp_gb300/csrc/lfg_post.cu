@@ -278,6 +278,118 @@ __global__ void __launch_bounds__(kPostBlock) IntegrateCellsKernel(PostArgs a, C
   BlockSumTo(acc, part);
 }
 
+// IntegrateMeshFunction with u_h on a hierarchic space (uniform degree, or
+// one degree group of a per-entity-degree space): one warp per cell.  The
+// cell's dof values (and, with VAR, its slots in the degree-D table) go to
+// shared memory; the lanes take the rule points, each forming u_h (or its
+// gradient) from the table block of the cell's orientation pattern, the
+// mesh function and the integrand, then the cell's integral is a fixed
+// shuffle tree.  Per warp the cells are summed in list order, then the warps
+// of a block in order, so the result does not depend on scheduling.
+constexpr int kHierPostWarps = 4;
+struct HierPostSide {
+  const int32_t* list;
+  int64_t count;
+  const double* tab;
+  HierTabView T;
+  const uint8_t* ori;
+  const uint16_t* sel;        // VAR: slot of each local shape function
+  const int64_t* loc_offset;  // VAR: local counts
+};
+
+template <bool QUAD, int KIND, bool VAR>
+__global__ void __launch_bounds__(32 * kHierPostWarps) IntegrateHierKernel(PostArgs a, HierPostSide h, double* part) {
+  extern __shared__ __align__(16) double shd[];
+  constexpr bool need_grad = KIND == LFG_INTEGRAND_GRAD_SQ_DIFF;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = h.T.n, nq = h.T.nq;
+  double* sd = shd + warp * n;
+  int* ss = reinterpret_cast<int*>(shd + kHierPostWarps * n) + warp * n;
+  const double* __restrict__ tab = h.tab;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(kHierPostWarps) + warp; i < h.count;
+       i += static_cast<int64_t>(gridDim.x) * kHierPostWarps) {
+    const int c = h.list[i];
+    if (a.flags && !a.flags[c] && c != 0) continue;  // warp-uniform
+    const int m = VAR ? static_cast<int>(h.loc_offset[c + 1] - h.loc_offset[c]) : n;
+    for (int j = lane; j < m; j += 32) {
+      sd[j] = a.dofs[a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + j]];
+      ss[j] = VAR ? h.sel[static_cast<int64_t>(c) * a.n_cell + j] : j;
+    }
+    __syncwarp();
+    int4 cn;
+    double2 v[4];
+    LoadCell<QUAD>(a, c, cn, v);
+    const double* P = tab + h.T.off_pat + (h.ori[c] & (QUAD ? 15 : 7)) * h.T.stride;
+    double local = 0.0;
+    for (int k = lane; k < nq; k += 32) {
+      const double xh = tab[nq + k], yh = tab[2 * nq + k];
+      double X, Y, ie, JT[2][2];
+      Geometry<QUAD>(v, xh, yh, X, Y, ie, JT);
+      double gx, gy, uv = 0.0;
+      if (need_grad) MFGrad<QUAD>(a.u, cn, xh, yh, X, Y, JT, gx, gy);
+      else uv = MFPoint<QUAD>(a.u, c, cn, xh, yh, X, Y, JT, false, gx, gy);
+      double hv = 0.0, hx = 0.0, hy = 0.0;
+      const double* pk = P + static_cast<int64_t>(k) * n;
+      const double* gk = P + h.T.o_g + static_cast<int64_t>(k) * n * 2;
+      for (int j = 0; j < m; ++j) {
+        const int sj = ss[j];
+        if (need_grad) {
+          hx = fma(sd[j], gk[2 * sj], hx);
+          hy = fma(sd[j], gk[2 * sj + 1], hy);
+        } else {
+          hv = fma(sd[j], pk[sj], hv);
+        }
+      }
+      double val;
+      if (KIND == LFG_INTEGRAND_VALUE) {
+        val = hv + uv;
+      } else if (KIND == LFG_INTEGRAND_SQ_DIFF) {
+        val = (hv - uv) * (hv - uv);
+      } else {
+        const double ex = (JT[0][0] * hx + JT[0][1] * hy) - gx;
+        const double ey = (JT[1][0] * hx + JT[1][1] * hy) - gy;
+        val = ex * ex + ey * ey;
+      }
+      local += val * (tab[k] * ie);
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    acc += local;  // the same value in every lane
+    __syncwarp();
+  }
+  __shared__ double wsum[kHierPostWarps];
+  if (lane == 0) wsum[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kHierPostWarps; ++w) s += wsum[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+template <bool QUAD, bool VAR>
+void LaunchIntegrateHier(int kind, int blocks, size_t smem, cudaStream_t st, const PostArgs& a,
+                         const HierPostSide& h, double* part) {
+  const int thr = 32 * kHierPostWarps;
+  switch (kind) {
+    case LFG_INTEGRAND_VALUE:
+      LFG_CUDA(cudaFuncSetAttribute(IntegrateHierKernel<QUAD, LFG_INTEGRAND_VALUE, VAR>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+      IntegrateHierKernel<QUAD, LFG_INTEGRAND_VALUE, VAR><<<blocks, thr, smem, st>>>(a, h, part);
+      break;
+    case LFG_INTEGRAND_SQ_DIFF:
+      LFG_CUDA(cudaFuncSetAttribute(IntegrateHierKernel<QUAD, LFG_INTEGRAND_SQ_DIFF, VAR>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+      IntegrateHierKernel<QUAD, LFG_INTEGRAND_SQ_DIFF, VAR><<<blocks, thr, smem, st>>>(a, h, part);
+      break;
+    default:
+      LFG_CUDA(cudaFuncSetAttribute(IntegrateHierKernel<QUAD, LFG_INTEGRAND_GRAD_SQ_DIFF, VAR>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+      IntegrateHierKernel<QUAD, LFG_INTEGRAND_GRAD_SQ_DIFF, VAR><<<blocks, thr, smem, st>>>(a, h, part);
+      break;
+  }
+}
+
 // Segment rule and basis for edges (points t on [0,1] along the edge).
 struct EdgeSide {
   int64_t ne;
@@ -673,9 +785,75 @@ void BuildHierDuals(lfg_space* sp, HierDualSet& H) {
   }
 }
 
+// IntegrateMeshFunction (codim 0) with u_h on a hierarchic space: one launch
+// per (cell type, degree) group, block partials summed in one fixed order.
+void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_degree, const uint8_t* flags,
+                   double* result);
+
 void RequireLagrange(const lfg_space* sp, const char* what) {
   if (sp->degree < 1 || sp->degree > 3)
     Fail(LFG_UNSUPPORTED, std::string(what) + ": needs a Lagrangian space of degree 1..3");
+}
+
+void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_degree, const uint8_t* flags,
+                   double* result) {
+  lfg_ctx* ctx = m->ctx;
+  PostArgs a = BasePostArgs(m, g->u, "IntegrateMeshFunction");
+  a.flags = flags;
+  a.kind = g->kind;
+  a.dofs = g->dofs_dev;
+  a.cell_dofs = sp->cell_dofs.as<int32_t>();
+  a.n_cell = sp->n_cell;
+  std::vector<HierGroup> groups;
+  if (sp->hier_var) {
+    groups = sp->hv_groups;
+  } else {
+    for (int q = 0; q < 2; ++q) {
+      HierGroup gr;
+      gr.quad = q == 1;
+      gr.degree = sp->hier_degree;
+      gr.count = gr.quad ? m->nquad : m->ntria;
+      if (gr.count) groups.push_back(gr);
+    }
+  }
+  std::vector<int> blocks;
+  int total = 0;
+  for (const HierGroup& gr : groups) {
+    const int64_t need = (gr.count + kHierPostWarps - 1) / kHierPostWarps;
+    const int b = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(need, static_cast<int64_t>(ctx->num_sms) * 8)));
+    blocks.push_back(b);
+    total += b;
+  }
+  DevBuf part;
+  part.alloc((total + 1) * sizeof(double), ctx->stream);
+  double* p = part.as<double>();
+  ProfScope prof(ctx, "integrate_cells_hier");
+  int off = 0;
+  for (size_t k = 0; k < groups.size(); ++k) {
+    const HierGroup& gr = groups[k];
+    HierPostSide h{};
+    h.tab = HierShapeTable(ctx, gr.quad, gr.degree, quad_degree, h.T);
+    h.list = sp->hier_var ? sp->hv_sorted.as<int32_t>() + gr.start
+                          : (gr.quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>());
+    h.count = gr.count;
+    h.ori = m->cell_ori.as<uint8_t>();
+    h.sel = sp->hier_var ? sp->hv_sel.as<uint16_t>() : nullptr;
+    h.loc_offset = sp->loc_offset.as<int64_t>();
+    const size_t smem = static_cast<size_t>(kHierPostWarps) * h.T.n * (sizeof(double) + sizeof(int));
+    if (gr.quad && sp->hier_var) LaunchIntegrateHier<true, true>(g->kind, blocks[k], smem, ctx->stream, a, h, p + off);
+    else if (gr.quad) LaunchIntegrateHier<true, false>(g->kind, blocks[k], smem, ctx->stream, a, h, p + off);
+    else if (sp->hier_var) LaunchIntegrateHier<false, true>(g->kind, blocks[k], smem, ctx->stream, a, h, p + off);
+    else LaunchIntegrateHier<false, false>(g->kind, blocks[k], smem, ctx->stream, a, h, p + off);
+    LFG_LAUNCHED(ctx);
+    off += blocks[k];
+  }
+  if (total == 0) {
+    LFG_CUDA(cudaMemsetAsync(p, 0, sizeof(double), ctx->stream));
+  } else {
+    SumPartialsKernel<<<1, kPostBlock, 0, ctx->stream>>>(total, p, p + total);
+    LFG_LAUNCHED(ctx);
+  }
+  D2HSync(ctx, result, p + (total == 0 ? 0 : total), sizeof(double));
 }
 
 }  // namespace
@@ -699,6 +877,11 @@ lfg_status lfg_integrate_mesh_function(lfg_mesh* m, const lfg_integrand* g, int3
   if (g->dofs_dev) {
     if (!sp) Fail(LFG_INVALID_ARG, "IntegrateMeshFunction: dofs without a space");
     if (sp->mesh != m) Fail(LFG_INVALID_ARG, "IntegrateMeshFunction: the space lives on another mesh");
+    if (sp->hier_degree > 0) {
+      if (codim != 0) Fail(LFG_UNSUPPORTED, "IntegrateMeshFunction: hierarchic u_h on edges is not supported");
+      IntegrateHier(m, sp, g, quad_degree, flags, result);
+      return LFG_OK;
+    }
     RequireLagrange(sp, "IntegrateMeshFunction");
   }
   PostArgs a = BasePostArgs(m, g->u, "IntegrateMeshFunction");

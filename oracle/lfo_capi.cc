@@ -381,6 +381,25 @@ int lfo_integrate(void* sp, int kind, const lfo_coeff* u, const double* dofs, in
   LFO_CATCH
 }
 
+// The same over the cells (codim 0) with u_h on a hierarchic space of uniform
+// degree p (p = 0: per-entity degrees).
+int lfo_integrate_hier(void* sp, int p, int kind, const lfo_coeff* u, const double* dofs, int qdeg,
+                       const uint8_t* flags, double* out, char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const Mesh& m = *s->mesh;
+  Integrand g;
+  g.kind = kind;
+  g.u = ToMF(u, u && u->kind == MeshFunction::kNodalO1 ? m.num_nodes : m.num_cells);
+  if (u && u->kind == MeshFunction::kAnalytic) g.grad_u = AnalyticGradient(u->func, u->p);
+  g.dh = &s->dh;
+  g.degree = s->degree;
+  g.dofs = dofs;
+  g.hier = p;
+  *out = IntegrateMeshFunction(m, g, qdeg, flags, 0);
+  LFO_CATCH
+}
+
 // MeshFunctionFE / MeshFunctionGradFE on every cell at npts reference points:
 // vals[cell][k], grads[cell][k][2] (either may be null).
 int lfo_eval_fe(void* sp, const double* dofs, int npts, const double* xy, double* vals, double* grads, char* err,

@@ -109,6 +109,8 @@ def lib():
                                         C.c_char_p, C.c_int]
             L.lfo_nodal_projection_hier.argtypes = [vp, C.c_int, P(lfo_coeff), P(C.c_uint8), P(dp), C.c_char_p,
                                                     C.c_int]
+            L.lfo_integrate_hier.argtypes = [vp, C.c_int, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8),
+                                             P(dp), C.c_char_p, C.c_int]
             L.lfo_hier_fn.argtypes = [C.c_int, C.c_int, dp, dp, dp]
             L.lfo_hier_fn.restype = dp
             L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
@@ -591,6 +593,18 @@ def nodal_projection_hier(space, p, u, cell_flags=None):
     err = _err()
     _check(lib().lfo_nodal_projection_hier(space.h, p, C.byref(u), flp, _p(out, C.c_double), err, 512), err)
     return out
+
+
+def integrate_hier(space, p, kind, u, dofs=None, qdeg=4, flags=None):
+    """IntegrateMeshFunction over the cells with u_h (dofs) on a hierarchic
+    space of uniform degree p (p = 0: a hier_var_space)."""
+    out = C.c_double()
+    d = None if dofs is None else np.ascontiguousarray(dofs, np.float64)
+    fl, flp = _u8(flags)
+    err = _err()
+    _check(lib().lfo_integrate_hier(space.h, p, kind, C.byref(u), _p(d, C.c_double) if d is not None else None, qdeg,
+                                    flp, C.byref(out), err, 512), err)
+    return out.value
 
 
 def hier_fn(which, n, a, b, x):

@@ -1,8 +1,13 @@
-"""NodalProjection (fe/fe_tools.h:198-259) on hierarchic spaces on the GPU
-against the oracle: uniform degrees 1..12 and per-entity degrees on four mesh
-kinds, every coefficient kind, with and without a cell predicate; the
-per-entity path with all degrees equal to p gives the uniform space's result
-value for value; a mid-size hybrid mesh (about 100k cells) end to end."""
+"""Post-processing on hierarchic spaces on the GPU against the oracle.
+
+NodalProjection (fe/fe_tools.h:198-259): uniform degrees 1..12 and per-entity
+degrees on four mesh kinds, every coefficient kind, with and without a cell
+predicate; the per-entity path with all degrees equal to p gives the uniform
+space's result value for value; a mid-size hybrid mesh (about 75k cells).
+
+IntegrateMeshFunction (fe/fe_tools.h:110-165) of u_h + u, (u_h - u)^2 and
+|grad u_h - grad u|^2 with u_h on a hierarchic space (uniform degrees 1..10,
+per-entity degrees), with and without a cell predicate."""
 import numpy as np
 import pytest
 
@@ -89,3 +94,47 @@ def test_hier_projection_mid_size(ctx):
     sp = L.Space.hierarchic(mesh, 4)
     osp = O.hier_space(oracle_mesh(spec), 4)
     _check(ctx, sp, osp, 4, _tol(4), mesh, np.random.default_rng(4), ukinds=("nodal", "trig"))
+
+
+@pytest.mark.parametrize("mname,spec", MESHES, ids=[m[0] for m in MESHES])
+@pytest.mark.parametrize("p", [1, 2, 4, 7, 10])
+def test_hier_integrate_matches_oracle(ctx, mname, spec, p):
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic(mesh, p)
+    osp = O.hier_space(oracle_mesh(spec), p)
+    rng = np.random.default_rng(5 * p + len(mname))
+    dofs = rng.standard_normal(sp.num_dofs)
+    dd = ctx.to_device(dofs)
+    for kind in (L.INT_VALUE, L.INT_SQ_DIFF, L.INT_GRAD_SQ_DIFF):
+        for ukind in ("sinsin", "nodal", "cell"):
+            for fkind in (None, "random"):
+                keep = []
+                gu, ou = _coeff(ctx, ukind, mesh.num_cells, mesh.num_nodes, rng, keep)
+                fl = _flags(fkind, mesh.num_cells, rng)
+                fld = ctx.to_device(fl) if fl is not None else None
+                got = L.integrate_mesh_function(mesh, kind, gu, sp, dd, 2 * p + 2, fld)
+                ref = O.integrate_hier(osp, p, kind, ou, dofs, 2 * p + 2, fl)
+                sq = O.integrate_hier(osp, p, O.INT_SQ_DIFF, ou, -dofs, 2 * p + 2, fl)
+                assert abs(got - ref) <= 1e-12 * (abs(ref) + abs(sq) + 1.0), (kind, ukind, fkind, got, ref)
+
+
+def test_hier_var_integrate_matches_oracle(ctx):
+    spec = _hybrid(12, seed=9)
+    om = oracle_mesh(spec)
+    rng = np.random.default_rng(19)
+    ed = rng.integers(1, 7, om.num_edges).astype(np.int32)
+    cd = rng.integers(1, 7, om.num_cells).astype(np.int32)
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic_var(mesh, ed, cd)
+    osp = O.hier_var_space(om, ed, cd)
+    dofs = rng.standard_normal(sp.num_dofs)
+    dd = ctx.to_device(dofs)
+    for kind in (L.INT_VALUE, L.INT_SQ_DIFF, L.INT_GRAD_SQ_DIFF):
+        keep = []
+        gu, ou = _coeff(ctx, "sincos", mesh.num_cells, mesh.num_nodes, rng, keep)
+        got = L.integrate_mesh_function(mesh, kind, gu, sp, dd, 14)
+        ref = O.integrate_hier(osp, 0, kind, ou, dofs, 14)
+        assert abs(got - ref) <= 1e-12 * (abs(ref) + 1.0), (kind, got, ref)
+    with pytest.raises(L.LfgError) as e:
+        L.integrate_mesh_function(mesh, L.INT_SQ_DIFF, gu, sp, dd, 6, None, 1)
+    assert e.value.code == L.UNSUPPORTED

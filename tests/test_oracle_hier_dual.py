@@ -6,7 +6,8 @@ dual of every basis function is its unit vector, all edge orientations), the
 library's tables (lfg_hier_dual, built independently in matrix form) against
 the oracle, and fe::NodalProjection (fe/fe_tools.h:198-259) on uniform and
 per-entity degree spaces: exact reproduction of the polynomials the space
-holds, convergence for a smooth function, and the cell predicate."""
+holds, convergence for a smooth function, and the cell predicate; and
+IntegrateMeshFunction with u_h on hierarchic spaces against NumPy."""
 import itertools
 import math
 import os
@@ -221,3 +222,82 @@ def test_var_degree_projection():
     su = O.hier_space(m, p)
     f = O.coeff(O.ANALYTIC, func=O.FN_SINSIN, params=[0.0, 1.0, 1.0, 2.0])
     assert np.array_equal(O.nodal_projection_hier(sv, 0, f), O.nodal_projection_hier(su, p, f))
+
+
+# ------------------------------------------------- IntegrateMeshFunction
+
+def _integrals(m, s, uh, u, gu, qdeg, p=0, ed=None, cd=None):
+    """(int u_h + u, int (u_h - u)^2, int |grad u_h - grad u|^2) over the
+    mesh by NumPy: the cell's hierarchic shape functions at the rule points,
+    the element map and its inverse transpose."""
+    dofs = s.cell_dofs()
+    _, ce, co, _ = m.topology()
+    r = np.zeros(3)
+    for c in range(m.num_cells):
+        quad = m.cells[c, 3] >= 0
+        pc, pe = _cell_degrees(m, c, quad, p, ed, cd, ce)
+        x, y, w = O.quad_rule(quad, qdeg)
+        phi, dphi = O.hier_shape_var(quad, pc, pe, list(co[c]), np.stack([x, y], 1))
+        v = m.xy[m.cells[c, :4 if quad else 3]]
+        if quad:
+            b = np.stack([(1 - x) * (1 - y), x * (1 - y), x * y, (1 - x) * y], 1)
+            j00 = (v[1, 0] - v[0, 0]) * (1 - y) + (v[2, 0] - v[3, 0]) * y
+            j10 = (v[1, 1] - v[0, 1]) * (1 - y) + (v[2, 1] - v[3, 1]) * y
+            j01 = (v[3, 0] - v[0, 0]) * (1 - x) + (v[2, 0] - v[1, 0]) * x
+            j11 = (v[3, 1] - v[0, 1]) * (1 - x) + (v[2, 1] - v[1, 1]) * x
+        else:
+            b = np.stack([1 - x - y, x, y], 1)
+            one = np.ones_like(x)
+            j00, j01 = (v[1, 0] - v[0, 0]) * one, (v[2, 0] - v[0, 0]) * one
+            j10, j11 = (v[1, 1] - v[0, 1]) * one, (v[2, 1] - v[0, 1]) * one
+        det = j00 * j11 - j10 * j01
+        X = b @ v
+        d = uh[dofs[c, :phi.shape[1]]]
+        hv = phi @ d
+        ghx, ghy = dphi[:, :, 0] @ d, dphi[:, :, 1] @ d
+        gx = (j11 * ghx - j10 * ghy) / det  # J^-T grad_hat
+        gy = (-j01 * ghx + j00 * ghy) / det
+        uv = u(X[:, 0], X[:, 1])
+        ux, uy = gu(X[:, 0], X[:, 1])
+        wd = w * np.abs(det)
+        r += [np.sum(wd * (hv + uv)), np.sum(wd * (hv - uv) ** 2), np.sum(wd * ((gx - ux) ** 2 + (gy - uy) ** 2))]
+    return r
+
+
+def _sinsin():
+    prm = [0.3, 1.0, 1.0, 2.0]
+    u = lambda X, Y: 0.3 + np.sin(np.pi * X) * np.sin(2 * np.pi * Y)
+    gu = lambda X, Y: (np.pi * np.cos(np.pi * X) * np.sin(2 * np.pi * Y),
+                       2 * np.pi * np.sin(np.pi * X) * np.cos(2 * np.pi * Y))
+    return O.coeff(O.ANALYTIC, func=O.FN_SINSIN, params=prm), u, gu
+
+
+@pytest.mark.parametrize("kind", ["tptriag", "tpquad", "hybrid", "test0"])
+@pytest.mark.parametrize("p", [1, 3, 5])
+def test_integrate_with_hierarchic_uh(kind, p):
+    """IntegrateMeshFunction (fe/fe_tools.h:110-165) of u_h + u, (u_h - u)^2
+    and |grad u_h - grad u|^2 with u_h a random dof vector of the hierarchic
+    space (MeshFunctionFE / MeshFunctionGradFE of it), against NumPy."""
+    m = _mesh(kind)
+    s = O.hier_space(m, p)
+    uh = np.random.default_rng(p + len(kind)).standard_normal(s.num_dofs)
+    cf, u, gu = _sinsin()
+    qdeg = 2 * p + 2
+    ref = _integrals(m, s, uh, u, gu, qdeg, p=p)
+    for k in range(3):
+        got = O.integrate_hier(s, p, k, cf, uh, qdeg)
+        assert abs(got - ref[k]) <= 1e-12 * max(1.0, abs(ref[k])), (k, got, ref[k])
+
+
+def test_integrate_with_hierarchic_uh_var_degrees():
+    m = _mesh("hybrid")
+    rng = np.random.default_rng(12)
+    ed = rng.integers(1, 6, m.num_edges).astype(np.int32)
+    cd = rng.integers(1, 6, m.num_cells).astype(np.int32)
+    s = O.hier_var_space(m, ed, cd)
+    uh = rng.standard_normal(s.num_dofs)
+    cf, u, gu = _sinsin()
+    ref = _integrals(m, s, uh, u, gu, 12, ed=ed, cd=cd)
+    for k in range(3):
+        got = O.integrate_hier(s, 0, k, cf, uh, 12)
+        assert abs(got - ref[k]) <= 1e-12 * max(1.0, abs(ref[k])), (k, got, ref[k])
