@@ -662,7 +662,8 @@ lfg_status lfg_integrate_mesh_function(lfg_mesh* mesh, const lfg_integrand* inte
  * (fe/mesh_function_fe.h:72-91, fe/mesh_function_grad_fe.h:93-118) for every
  * cell at the same npts reference points ref_points[2 k], ref_points[2 k + 1]
  * (host): values_dev[cell * npts + k] and grads_dev[(cell * npts + k) * 2 + d]
- * (either may be NULL). */
+ * (either may be NULL).  Lagrangian (O1-O3) or hierarchic spaces (each cell's
+ * own FeHierarchicTria / Quad shape functions). */
 lfg_status lfg_fe_eval(lfg_space* space, const double* dofs_dev, int32_t npts, const double* ref_points,
                        double* values_dev, double* grads_dev);
 /* NodalProjection(fe_space, u, pred) (fe/fe_tools.h:198-259): per selected

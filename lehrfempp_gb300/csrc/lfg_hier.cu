@@ -65,10 +65,16 @@ HierTab HierLayout(bool quad, int n, int nq, bool folded) {
   return t;
 }
 
+void FillHierTable(bool quad, int p, const Rule& r, bool folded, std::vector<double>& h, HierTab& L);
+
 void BuildHierTable(bool quad, int p, int rule_degree, bool folded, std::vector<double>& h, HierTab& L) {
   Rule r;
   if (!MakeRule(quad, rule_degree, r))
     Fail(LFG_UNSUPPORTED, "no quadrature rule of degree " + std::to_string(rule_degree));
+  FillHierTable(quad, p, r, folded, h, L);
+}
+
+void FillHierTable(bool quad, int p, const Rule& r, bool folded, std::vector<double>& h, HierTab& L) {
   const int n = quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
   L = HierLayout(quad, n, r.n, folded);
   h.assign(static_cast<size_t>(L.total), 0.0);
@@ -462,6 +468,22 @@ const double* HierShapeTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, Hi
   v.stride = L.stride;
   v.o_g = L.o_g;
   return t;
+}
+
+void HierShapeTableAt(bool quad, int p, const std::vector<double>& x, const std::vector<double>& y,
+                      std::vector<double>& h, HierTabView& v) {
+  Rule r;
+  r.n = static_cast<int>(x.size());
+  r.x = x;
+  r.y = y;
+  r.w.assign(x.size(), 0.0);
+  HierTab L;
+  FillHierTable(quad, p, r, false, h, L);
+  v.n = L.n;
+  v.nq = L.nq;
+  v.off_pat = L.off_pat;
+  v.stride = L.stride;
+  v.o_g = L.o_g;
 }
 
 int HierRuleDegree(int requested, int p) { return requested == 0 ? 2 * p : requested; }

@@ -168,6 +168,9 @@ struct HierTabView {
   int64_t off_pat = 0, stride = 0, o_g = 0;
 };
 const double* HierShapeTable(lfg_ctx* ctx, bool quad, int p, int rule_degree, HierTabView& v);
+// The same layout at given reference points (weights 0), on the host.
+void HierShapeTableAt(bool quad, int p, const std::vector<double>& x, const std::vector<double>& y,
+                      std::vector<double>& h, HierTabView& v);
 }  // namespace lfg
 
 struct lfg_space {

@@ -367,6 +367,56 @@ __global__ void __launch_bounds__(32 * kHierPostWarps) IntegrateHierKernel(PostA
   }
 }
 
+// MeshFunctionFE / MeshFunctionGradFE of u_h on a hierarchic space at the
+// table's points of every cell of one group: one warp per cell, lanes over
+// the points.
+template <bool QUAD, bool VAR>
+__global__ void __launch_bounds__(32 * kHierPostWarps) FeEvalHierKernel(PostArgs a, HierPostSide h, double* vals,
+                                                                        double* grads) {
+  extern __shared__ __align__(16) double shd[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = h.T.n, nq = h.T.nq;
+  double* sd = shd + warp * n;
+  int* ss = reinterpret_cast<int*>(shd + kHierPostWarps * n) + warp * n;
+  const double* __restrict__ tab = h.tab;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(kHierPostWarps) + warp; i < h.count;
+       i += static_cast<int64_t>(gridDim.x) * kHierPostWarps) {
+    const int c = h.list[i];
+    const int m = VAR ? static_cast<int>(h.loc_offset[c + 1] - h.loc_offset[c]) : n;
+    for (int j = lane; j < m; j += 32) {
+      sd[j] = a.dofs[a.cell_dofs[static_cast<int64_t>(c) * a.n_cell + j]];
+      ss[j] = VAR ? h.sel[static_cast<int64_t>(c) * a.n_cell + j] : j;
+    }
+    __syncwarp();
+    int4 cn;
+    double2 v[4];
+    LoadCell<QUAD>(a, c, cn, v);
+    const double* P = tab + h.T.off_pat + (h.ori[c] & (QUAD ? 15 : 7)) * h.T.stride;
+    for (int k = lane; k < nq; k += 32) {
+      const double* pk = P + static_cast<int64_t>(k) * n;
+      const double* gk = P + h.T.o_g + static_cast<int64_t>(k) * n * 2;
+      double hv = 0.0, hx = 0.0, hy = 0.0;
+      for (int j = 0; j < m; ++j) {
+        const int sj = ss[j];
+        if (vals) hv = fma(sd[j], pk[sj], hv);
+        if (grads) {
+          hx = fma(sd[j], gk[2 * sj], hx);
+          hy = fma(sd[j], gk[2 * sj + 1], hy);
+        }
+      }
+      const int64_t o = static_cast<int64_t>(c) * nq + k;
+      if (vals) vals[o] = hv;
+      if (grads) {
+        double X, Y, ie, JT[2][2];
+        Geometry<QUAD>(v, tab[nq + k], tab[2 * nq + k], X, Y, ie, JT);
+        grads[2 * o] = JT[0][0] * hx + JT[0][1] * hy;
+        grads[2 * o + 1] = JT[1][0] * hx + JT[1][1] * hy;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 template <bool QUAD, bool VAR>
 void LaunchIntegrateHier(int kind, int blocks, size_t smem, cudaStream_t st, const PostArgs& a,
                          const HierPostSide& h, double* part) {
@@ -785,6 +835,10 @@ void BuildHierDuals(lfg_space* sp, HierDualSet& H) {
   }
 }
 
+// MeshFunctionFE / MeshFunctionGradFE on a hierarchic space at npts reference
+// points of every cell.
+void FeEvalHier(lfg_space* sp, const double* dofs, int npts, const double* ref_points, double* vals, double* grads);
+
 // IntegrateMeshFunction (codim 0) with u_h on a hierarchic space: one launch
 // per (cell type, degree) group, block partials summed in one fixed order.
 void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_degree, const uint8_t* flags,
@@ -793,6 +847,76 @@ void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_
 void RequireLagrange(const lfg_space* sp, const char* what) {
   if (sp->degree < 1 || sp->degree > 3)
     Fail(LFG_UNSUPPORTED, std::string(what) + ": needs a Lagrangian space of degree 1..3");
+}
+
+// The (cell type, degree) groups of a hierarchic space.
+std::vector<HierGroup> HierGroups(const lfg_space* sp) {
+  if (sp->hier_var) return sp->hv_groups;
+  std::vector<HierGroup> groups;
+  for (int q = 0; q < 2; ++q) {
+    HierGroup gr;
+    gr.quad = q == 1;
+    gr.degree = sp->hier_degree;
+    gr.count = gr.quad ? sp->mesh->nquad : sp->mesh->ntria;
+    if (gr.count) groups.push_back(gr);
+  }
+  return groups;
+}
+
+void FeEvalHier(lfg_space* sp, const double* dofs, int npts, const double* ref_points, double* vals, double* grads) {
+  lfg_mesh* m = sp->mesh;
+  lfg_ctx* ctx = m->ctx;
+  PostArgs a{};
+  a.cells = m->cell_nodes.as<int4>();
+  a.xy = m->xy.as<double2>();
+  a.cell_dofs = sp->cell_dofs.as<int32_t>();
+  a.n_cell = sp->n_cell;
+  a.dofs = dofs;
+  std::vector<double> x(npts), y(npts);
+  for (int k = 0; k < npts; ++k) {
+    x[k] = ref_points[2 * k];
+    y[k] = ref_points[2 * k + 1];
+  }
+  ProfScope prof(ctx, "fe_eval_hier");
+  for (const HierGroup& gr : HierGroups(sp)) {
+    HierPostSide h{};
+    std::vector<double> tab_h;
+    HierShapeTableAt(gr.quad, gr.degree, x, y, tab_h, h.T);
+    DevBuf tab;
+    tab.alloc(tab_h.size() * sizeof(double), ctx->stream);
+    LFG_CUDA(cudaMemcpyAsync(tab.p, tab_h.data(), tab_h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    h.tab = tab.as<double>();
+    h.list = sp->hier_var ? sp->hv_sorted.as<int32_t>() + gr.start
+                          : (gr.quad ? m->quad_list.as<int32_t>() : m->tria_list.as<int32_t>());
+    h.count = gr.count;
+    h.ori = m->cell_ori.as<uint8_t>();
+    h.sel = sp->hier_var ? sp->hv_sel.as<uint16_t>() : nullptr;
+    h.loc_offset = sp->loc_offset.as<int64_t>();
+    const size_t smem = static_cast<size_t>(kHierPostWarps) * h.T.n * (sizeof(double) + sizeof(int));
+    const int blocks = static_cast<int>(
+        std::max<int64_t>(1, std::min<int64_t>((gr.count + kHierPostWarps - 1) / kHierPostWarps,
+                                               static_cast<int64_t>(ctx->num_sms) * 8)));
+    if (gr.quad && sp->hier_var) {
+      LFG_CUDA(cudaFuncSetAttribute(FeEvalHierKernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+      FeEvalHierKernel<true, true><<<blocks, 32 * kHierPostWarps, smem, ctx->stream>>>(a, h, vals, grads);
+    } else if (gr.quad) {
+      LFG_CUDA(cudaFuncSetAttribute(FeEvalHierKernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+      FeEvalHierKernel<true, false><<<blocks, 32 * kHierPostWarps, smem, ctx->stream>>>(a, h, vals, grads);
+    } else if (sp->hier_var) {
+      LFG_CUDA(cudaFuncSetAttribute(FeEvalHierKernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+      FeEvalHierKernel<false, true><<<blocks, 32 * kHierPostWarps, smem, ctx->stream>>>(a, h, vals, grads);
+    } else {
+      LFG_CUDA(cudaFuncSetAttribute(FeEvalHierKernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+      FeEvalHierKernel<false, false><<<blocks, 32 * kHierPostWarps, smem, ctx->stream>>>(a, h, vals, grads);
+    }
+    LFG_LAUNCHED(ctx);
+    // the table buffer is released stream-ordered after the launch
+  }
 }
 
 void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_degree, const uint8_t* flags,
@@ -804,18 +928,7 @@ void IntegrateHier(lfg_mesh* m, lfg_space* sp, const lfg_integrand* g, int quad_
   a.dofs = g->dofs_dev;
   a.cell_dofs = sp->cell_dofs.as<int32_t>();
   a.n_cell = sp->n_cell;
-  std::vector<HierGroup> groups;
-  if (sp->hier_var) {
-    groups = sp->hv_groups;
-  } else {
-    for (int q = 0; q < 2; ++q) {
-      HierGroup gr;
-      gr.quad = q == 1;
-      gr.degree = sp->hier_degree;
-      gr.count = gr.quad ? m->nquad : m->ntria;
-      if (gr.count) groups.push_back(gr);
-    }
-  }
+  const std::vector<HierGroup> groups = HierGroups(sp);
   std::vector<int> blocks;
   int total = 0;
   for (const HierGroup& gr : groups) {
@@ -970,6 +1083,11 @@ lfg_status lfg_fe_eval(lfg_space* sp, const double* dofs, int32_t npts, const do
   LFG_API_BEGIN(sp->mesh->ctx)
   lfg_ctx* ctx = sp->mesh->ctx;
   lfg_mesh* m = sp->mesh;
+  if (sp->hier_degree > 0) {
+    if (npts == 0 || (!vals && !grads)) return LFG_OK;
+    FeEvalHier(sp, dofs, npts, ref_points, vals, grads);
+    return LFG_OK;
+  }
   RequireLagrange(sp, "MeshFunctionFE");
   if (npts == 0 || (!vals && !grads)) return LFG_OK;
   PostArgs a{};

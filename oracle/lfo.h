@@ -284,6 +284,9 @@ double IntegrateMeshFunction(const Mesh& m, const Integrand& g, int qdeg, const 
 // fe/mesh_function_grad_fe.h:93-118) on one cell at reference points xy.
 void EvalFE(const DofHandler& dh, int degree, const double* dofs, idx_t cell, const std::vector<double>& xy,
             double* vals, double* grads);
+// The same with u_h on a hierarchic space (uniform degree p, 0: per entity).
+void EvalFEHier(const DofHandler& dh, int p, const double* dofs, idx_t cell, const std::vector<double>& xy,
+                double* vals, double* grads);
 // NodalProjection (fe/fe_tools.h:198-259) of a mesh function, cells selected
 // by flags (null: all); a dof shared by cells gets the last cell's value.
 void NodalProjectionMF(const DofHandler& dh, int degree, const MeshFunction& u, const uint8_t* cell_flags,

@@ -412,6 +412,16 @@ int lfo_eval_fe(void* sp, const double* dofs, int npts, const double* xy, double
   LFO_CATCH
 }
 
+int lfo_eval_fe_hier(void* sp, int p, const double* dofs, int npts, const double* xy, double* vals, double* grads,
+                     char* err, int errlen) {
+  LFO_TRY
+  auto* s = static_cast<Space*>(sp);
+  const std::vector<double> pts(xy, xy + 2 * npts);
+  for (idx_t c = 0; c < s->mesh->num_cells; ++c)
+    EvalFEHier(s->dh, p, dofs, c, pts, vals ? vals + c * npts : nullptr, grads ? grads + 2 * c * npts : nullptr);
+  LFO_CATCH
+}
+
 int lfo_nodal_projection_mf(void* sp, const lfo_coeff* u, const uint8_t* cell_flags, double* out, char* err,
                             int errlen) {
   LFO_TRY

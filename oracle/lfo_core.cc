@@ -1288,6 +1288,21 @@ void EvalFE(const DofHandler& dh, int degree, const double* dofs, idx_t cell, co
   }
 }
 
+void EvalFEHier(const DofHandler& dh, int p, const double* dofs, idx_t cell, const std::vector<double>& xy,
+                double* vals, double* grads) {
+  const CellGeom geo = dh.mesh->Geom(cell);
+  const size_t np = xy.size() / 2;
+  for (size_t k = 0; k < np; ++k) {
+    double v, g[2];
+    FEPointHier(dh, p, dofs, cell, geo, xy[2 * k], xy[2 * k + 1], &v, grads ? g : nullptr);
+    if (vals) vals[k] = v;
+    if (grads) {
+      grads[2 * k] = g[0];
+      grads[2 * k + 1] = g[1];
+    }
+  }
+}
+
 void NodalProjectionMF(const DofHandler& dh, int degree, const MeshFunction& u, const uint8_t* cell_flags,
                        std::vector<double>& out) {
   out.assign(dh.num_dofs, 0.0);

@@ -111,6 +111,7 @@ def lib():
                                                     C.c_int]
             L.lfo_integrate_hier.argtypes = [vp, C.c_int, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8),
                                              P(dp), C.c_char_p, C.c_int]
+            L.lfo_eval_fe_hier.argtypes = [vp, C.c_int, P(dp), C.c_int, P(dp), P(dp), P(dp), C.c_char_p, C.c_int]
             L.lfo_hier_fn.argtypes = [C.c_int, C.c_int, dp, dp, dp]
             L.lfo_hier_fn.restype = dp
             L.lfo_integrate.argtypes = [vp, C.c_int, P(lfo_coeff), P(dp), C.c_int, P(C.c_uint8), C.c_int, P(dp),
@@ -605,6 +606,21 @@ def integrate_hier(space, p, kind, u, dofs=None, qdeg=4, flags=None):
     _check(lib().lfo_integrate_hier(space.h, p, kind, C.byref(u), _p(d, C.c_double) if d is not None else None, qdeg,
                                     flp, C.byref(out), err, 512), err)
     return out.value
+
+
+def eval_fe_hier(space, p, dofs, pts):
+    """MeshFunctionFE / GradFE of u_h on a hierarchic space (uniform degree p,
+    0: per entity) at reference points pts (k, 2) of every cell: values
+    (cells, k) and gradients (cells, k, 2)."""
+    pts = np.ascontiguousarray(pts, np.float64).reshape(-1, 2)
+    d = np.ascontiguousarray(dofs, np.float64)
+    nc = space.mesh.num_cells
+    vals = np.zeros((nc, len(pts)))
+    grads = np.zeros((nc, len(pts), 2))
+    err = _err()
+    _check(lib().lfo_eval_fe_hier(space.h, p, _p(d, C.c_double), len(pts), _p(pts, C.c_double), _p(vals, C.c_double),
+                                  _p(grads, C.c_double), err, 512), err)
+    return vals, grads
 
 
 def hier_fn(which, n, a, b, x):

@@ -138,3 +138,39 @@ def test_hier_var_integrate_matches_oracle(ctx):
     with pytest.raises(L.LfgError) as e:
         L.integrate_mesh_function(mesh, L.INT_SQ_DIFF, gu, sp, dd, 6, None, 1)
     assert e.value.code == L.UNSUPPORTED
+
+
+@pytest.mark.parametrize("mname,spec", MESHES, ids=[m[0] for m in MESHES])
+@pytest.mark.parametrize("p", [1, 3, 6, 9])
+def test_hier_fe_eval_matches_oracle(ctx, mname, spec, p):
+    """MeshFunctionFE / MeshFunctionGradFE of a hierarchic u_h at shared
+    reference points of every cell."""
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic(mesh, p)
+    osp = O.hier_space(oracle_mesh(spec), p)
+    rng = np.random.default_rng(p + 3 * len(mname))
+    dofs = rng.standard_normal(sp.num_dofs)
+    pts = np.array([[0.1, 0.2], [0.25, 0.25], [0.6, 0.3], [0.05, 0.9], [0.0, 0.0], [0.5, 0.5]])
+    v, g = L.fe_eval(sp, ctx.to_device(dofs), pts, values=True, grads=True)
+    vals, grads = v.download(), g.download()
+    ov, og = O.eval_fe_hier(osp, p, dofs, pts)
+    assert np.abs(vals - ov).max() <= 1e-12 * max(1.0, np.abs(ov).max())
+    assert np.abs(grads - og).max() <= 1e-12 * max(1.0, np.abs(og).max())
+
+
+def test_hier_var_fe_eval_matches_oracle(ctx):
+    spec = _hybrid(10, seed=3)
+    om = oracle_mesh(spec)
+    rng = np.random.default_rng(23)
+    ed = rng.integers(1, 7, om.num_edges).astype(np.int32)
+    cd = rng.integers(1, 7, om.num_cells).astype(np.int32)
+    mesh = W.build_mesh(ctx, spec)
+    sp = L.Space.hierarchic_var(mesh, ed, cd)
+    osp = O.hier_var_space(om, ed, cd)
+    dofs = rng.standard_normal(sp.num_dofs)
+    pts = np.array([[0.2, 0.1], [0.3, 0.6], [0.45, 0.45]])
+    v, g = L.fe_eval(sp, ctx.to_device(dofs), pts, values=True, grads=True)
+    vals, grads = v.download(), g.download()
+    ov, og = O.eval_fe_hier(osp, 0, dofs, pts)
+    assert np.abs(vals - ov).max() <= 1e-12 * max(1.0, np.abs(ov).max())
+    assert np.abs(grads - og).max() <= 1e-12 * max(1.0, np.abs(og).max())
