@@ -1326,6 +1326,302 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   }
 }
 
+// Warp-specialised variant with the triplet writes moved to the producers.
+// The consumers (eight warps, two threads per cell) only recombine: they
+// write the FP64 entries of tile j into the A-digit buffer of tile j's
+// producer group -- free once tile j's MMAs have completed, and as large as
+// the 128 x 45 values for M = 3 -- and arrive on vals_ready[b].  The
+// producer group then writes tile j's triplets from there (it has slack:
+// it waits for a free accumulator block otherwise) before it splits the
+// digits of its next tile into the same buffer.  So the staged values are
+// double-buffered (one buffer per group) without extra shared memory, and a
+// tile's recombination overlaps the previous tile's writes.  Hand-offs per
+// group b: mma_done[b] (tile's MMAs complete), tmem_free[b] and vals_ready[b]
+// (the consumers have read accumulator block b and written the values).
+// Every wait gives up after 2^22 polls.
+__host__ __device__ constexpr int Ws2BufBytes(int m) {
+  return 6 * 256 * TcKP(m) > 128 * 45 * 8 ? 6 * 256 * TcKP(m) : 128 * 45 * 8;
+}
+__host__ __device__ constexpr int Ws2SmemBytes(int m) {
+  return 2 * Ws2BufBytes(m) + TcImageBytes(m) + 2 * (128 * 9 * 4 + 128 * 8);
+}
+
+template <int M>
+__global__ void __launch_bounds__(kWsThreads, 1)
+    RDQuadTcWs2Kernel(AsmArgs a, DfArgs d, const uint4* __restrict__ image, int* __restrict__ tc_timeouts) {
+  using elem::f2;
+  constexpr int N = 9, E = 45, NQ = M * M, KP = TcKP(M), KS = KP / 16, NP = kTcNP;
+  constexpr int P0 = (NQ + 1) / 2;   // points in K columns [0, KP/2); the rest from KP/2
+  constexpr uint32_t SA = 256 * KP;  // one digit slice of an A tile, bytes
+  constexpr uint32_t SBO = KP * 16;  // 8-row group stride of both operands
+  constexpr int ABUF = Ws2BufBytes(M);
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  unsigned char* sA = smraw;                                          // [2][ABUF]: digits, then values
+  unsigned char* sB = smraw + 2 * ABUF;                               // table digits, info block, Ec
+  const int* sEc = reinterpret_cast<const int*>(sB + TcEcOffset(M));
+  int* sdofs = reinterpret_cast<int*>(sB + TcImageBytes(M));          // [2][128][9]
+  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 2 * 128 * N);    // [2][128]
+  __shared__ f2 sWt[NQ + M];
+  __shared__ __align__(8) uint64_t mma_done[2];
+  __shared__ __align__(8) uint64_t tmem_free[2];
+  __shared__ __align__(8) uint64_t vals_ready[2];
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_abort;
+
+  {
+    const f2* g = reinterpret_cast<const f2*>(d.tab);
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) sWt[i] = g[d.L.off_W + i];
+    for (int i = threadIdx.x; i < M; i += blockDim.x) sWt[NQ + i] = g[d.L.off_t + i];
+    uint4* dst = reinterpret_cast<uint4*>(sB);
+    for (int i = threadIdx.x; i < TcImageBytes(M) / 16; i += blockDim.x) dst[i] = image[i];
+  }
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b) {
+      tc::MbarInit(&mma_done[b], 1);
+      tc::MbarInit(&tmem_free[b], 256);
+      tc::MbarInit(&vals_ready[b], 256);
+    }
+    s_abort = 0;
+  }
+  if (threadIdx.x < 32) tc::TmemAlloc(&s_taddr, 512);
+  tc::FenceProxyAsync();
+  tc::FenceBeforeSync();
+  __syncthreads();
+  tc::FenceAfterSync();
+  const uint32_t taddr = s_taddr;
+  const int64_t tiles = (a.count + 127) / 128;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int tmap[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const int w = lane + 32 * t, i = w / N, j = w - i * N;
+    tmap[t] = w < N * N ? (i | (j << 8) | (UpperIndex<N>(i, j) << 16)) : -1;
+  }
+
+  if (threadIdx.x < 256) {
+    // ================= producers: group b, one thread per cell =================
+    const int b = threadIdx.x >> 7, r = threadIdx.x & 127, wg = (threadIdx.x >> 5) & 3;
+    const int bar = 1 + b;
+    unsigned char* Ab = sA + b * ABUF;
+    const double* vals_b = reinterpret_cast<const double*>(Ab);
+    int* sd_b = sdofs + b * 128 * N;
+    int64_t* so_b = soff + b * 128;
+    const uint32_t dcol = taddr + 256 * b;
+    int c = 0;
+    double2 v[4] = {};
+    double al = 0.0;
+    const int64_t first = blockIdx.x + static_cast<int64_t>(b) * gridDim.x;
+    if (first < tiles) TcFetch(a, first * 128, r, c, v, al);
+    int m = 0, issued = 0;
+    int prev_ncell = 0;
+    // writes the previous tile of this group (its values are in Ab once the
+    // consumers arrive on vals_ready[b]); false when a wait gave up
+    auto write_prev = [&](int mp) -> bool {
+      const bool ok = tc::MbarWait(&vals_ready[b], mp & 1, kTcMaxPolls);
+      asm volatile("cp.async.wait_all;" ::: "memory");  // this group's staged dofs / offsets
+      if (tc::NamedSyncOr(bar, 128, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (r == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        return false;
+      }
+      for (int cl = 32 * wg; cl < prev_ncell && cl < 32 * wg + 32; ++cl) {
+        lfg_triplet* base = a.out + so_b[cl];
+        const int* dd = sd_b + cl * N;
+        const double* vv = vals_b + cl * E;
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+          if (tmap[t] >= 0)
+            StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
+      }
+      tc::NamedSync(bar, 128);  // Ab and the staged dofs are free again
+      return true;
+    };
+    bool alive = true;
+    for (;; ++m) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(b + 2 * m) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      if (m > 0 && !write_prev(m - 1)) {
+        alive = false;
+        break;
+      }
+      // this tile's dof rows and triplet offsets, staged for its writes
+      if (r < ncell) {
+        const int32_t* g = a.cell_dofs + static_cast<int64_t>(c) * a.n_cell;
+#pragma unroll
+        for (int i = 0; i < N; ++i) tc::CpAsync4(sd_b + r * N + i, g + i);
+        tc::CpAsync8(so_b + r, a.tri_offset + c);
+      }
+      tc::CpAsyncCommit();
+      bool safe = false;
+      f2 cpt[NQ][4];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+      if (r < ncell) {
+        const double acd[6] = {v[1].x - v[0].x, v[1].y - v[0].y, v[3].x - v[0].x, v[3].y - v[0].y,
+                               (v[0].x - v[1].x) + (v[2].x - v[3].x), (v[0].y - v[1].y) + (v[2].y - v[3].y)};
+        safe = DfSafeBits(al);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) safe = safe && DfSafeBits(acd[k]);
+        if (safe) elem::QuadPointCoeffsDF<M, false>(acd, al, 0.0, sWt + NQ, sWt, cpt);
+      }
+      float mx = 0.0f;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) mx = fmaxf(mx, fabsf(cpt[k][q].h));
+      int e = mx > 0.0f ? static_cast<int>((__float_as_uint(mx) >> 23) & 0xffu) - 127 : 0;
+      if (e < -70 || e > 70) safe = false;
+      if (!safe) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k)
+#pragma unroll
+          for (int q = 0; q < 3; ++q) cpt[k][q] = f2{0.0f, 0.0f};
+        e = 0;
+      }
+      const float scale = __uint_as_float(static_cast<uint32_t>(127 + 52 - e) << 23);  // 2^(52 - e)
+      unsigned char* arow = Ab + (r >> 3) * SBO + (r & 7) * 16;
+#pragma unroll
+      for (int gk = 0; gk < KP / 8; ++gk) {
+        uint32_t w[6][4];
+#pragma unroll
+        for (int pr = 0; pr < 4; ++pr) {
+          uint32_t p[2][6];
+#pragma unroll
+          for (int s = 0; s < 2; ++s) {
+            const int kap = gk * 8 + 2 * pr + s, kl = kap < KP / 2 ? kap : kap - KP / 2;
+            const int k = (kap < KP / 2 ? 0 : P0) + kl / 3;
+            const bool used = kap < KP / 2 ? kl < 3 * P0 : kl < 3 * (NQ - P0);
+            const f2 x = used ? cpt[k][kl % 3] : f2{0.0f, 0.0f};
+            const float hs = x.h * scale;
+            const int vhi = __float2int_rn(hs * 7.450580596923828125e-9f);  // 2^-27
+            const float rem = __fmaf_rn(static_cast<float>(vhi), -134217728.0f, hs);  // exact
+            const int wlo0 = __float2int_rn(rem) + __float2int_rn(x.l * scale) + 256 * ((1 << 18) + (1 << 9) + 1);
+            const int whi = vhi + 256 * ((1 << 9) + 1) + (wlo0 >> 27);
+            const uint32_t wlo = static_cast<uint32_t>(wlo0) & ((1u << 27) - 1u);
+            p[s][0] = 0x6600u + static_cast<uint32_t>(whi >> 18);
+            p[s][1] = 0x6400u | ((static_cast<uint32_t>(whi) >> 9) & 511u);
+            p[s][2] = 0x6400u | (static_cast<uint32_t>(whi) & 511u);
+            p[s][3] = 0x6400u | ((wlo >> 18) & 511u);
+            p[s][4] = 0x6400u | ((wlo >> 9) & 511u);
+            p[s][5] = 0x6400u | (wlo & 511u);
+          }
+#pragma unroll
+          for (int i = 0; i < 6; ++i)
+            w[i][pr] = HSub2(__byte_perm(p[0][i], p[1][i], 0x5410), i == 0 ? 0x66006600u : 0x65006500u);
+        }
+        if (gk == KP / 8 - 1) {  // row info in digit 1, K column KP - 1: e + 128, or 0 off the df32 range
+          const uint32_t info = __half_as_ushort(__float2half_rn(safe ? static_cast<float>(e + 128) : 0.0f));
+          w[0][3] = (w[0][3] & 0xffffu) | (info << 16);
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+          *reinterpret_cast<uint4*>(arow + i * SA + gk * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+      }
+      tc::FenceProxyAsync();
+      tc::NamedSync(bar, 128);
+      if (r == 0) {
+        bool free_ok = m == 0 || tc::MbarWait(&tmem_free[b], (m - 1) & 1, kTcMaxPolls);
+        if (!free_ok) {
+          atomicAdd(tc_timeouts, 1);
+          s_abort = 1;
+        } else {
+          tc::FenceAfterSync();
+          const uint32_t a0 = tc::SmemAddr(Ab), bu = tc::SmemAddr(sB), bs = bu + TcBHalfBytes(M);
+          const uint32_t bi = bu + 2 * TcBHalfBytes(M);
+#pragma unroll
+          for (int s = 0; s < KS; ++s)
+#pragma unroll
+            for (int i = 1; i <= 5; ++i)
+              tc::MmaF16(dcol + (i - 1) * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                         tc::SmemDesc(bu + s * 256, 128, SBO), tc::IdescF16(128, (6 - i) * NP), s > 0 || i > 1);
+#pragma unroll
+          for (int s = 0; s < KS; ++s)
+#pragma unroll
+            for (int i = 1; i <= 6; ++i)
+              tc::MmaF16(dcol + 4 * NP, tc::SmemDesc(a0 + (i - 1) * SA + s * 256, 128, SBO),
+                         tc::SmemDesc(bs + (6 - i) * (NP / 8) * SBO + s * 256, 128, SBO), tc::IdescF16(128, NP),
+                         true);
+          tc::MmaF16(dcol + 5 * NP, tc::SmemDesc(a0 + (KS - 1) * 256, 128, SBO),
+                     tc::SmemDesc(bi + (KS - 1) * 256, 128, SBO), tc::IdescF16(128, 16), false);
+          tc::Commit(&mma_done[b]);
+        }
+      }
+      ++issued;
+      prev_ncell = ncell;
+      // inputs of this group's next tile load while the tensor cores work
+      const int64_t nxt = tile + 2 * static_cast<int64_t>(gridDim.x);
+      if (nxt < tiles) TcFetch(a, nxt * 128, r, c, v, al);
+    }
+    // the group's last tile
+    if (alive && m > 0) write_prev(m - 1);
+    // after an abort an MMA may still be in flight: it finishes before the
+    // tensor memory is released (a completed phase returns at once)
+    if (r == 0 && issued > 0) tc::MbarWait(&mma_done[b], (issued - 1) & 1, kTcMaxPolls);
+  } else {
+    // ================= consumers: two threads per cell, recombination only =================
+    const int et = threadIdx.x - 256, half = et >> 7, r = et & 127, q4 = r >> 5;
+    const uint32_t tl = static_cast<uint32_t>(q4 * 32) << 16;
+    for (int j = 0;; ++j) {
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(j) * gridDim.x;
+      if (tile >= tiles) break;
+      const int64_t t0 = tile * 128;
+      const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
+      const int b = j & 1;
+      const bool ok = tc::MbarWait(&mma_done[b], (j >> 1) & 1, kTcMaxPolls);
+      if (!ok || *reinterpret_cast<volatile int*>(&s_abort) != 0) {
+        if (!ok && et == 0) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        break;
+      }
+      tc::FenceAfterSync();
+      const uint32_t acc = taddr + 256 * b + tl;
+      float inf[8];
+      tc::Ld8(acc + 5 * NP, inf);
+      tc::WaitLd();
+      const int info = static_cast<int>(inf[0]);
+      const bool safe = info != 0;
+      const int shift = info - 128 + 2 - 54;
+      double* vals = reinterpret_cast<double*>(sA + b * ABUF) + r * E;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int col = 24 * half + 8 * q;
+        float G[5][8];
+#pragma unroll
+        for (int l = 0; l < 5; ++l) tc::Ld8(acc + l * NP + col, G[l]);
+        tc::WaitLd();
+        if (safe) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int en = col + t;
+            if (en < E) vals[en] = TcCombine(G[0][t], G[1][t], G[2][t], G[3][t], G[4][t], shift + sEc[en]);
+          }
+        }
+      }
+      tc::FenceBeforeSync();
+      tc::MbarArrive(&tmem_free[b]);
+      if (half == 0 && r < ncell && !safe) {
+        int cf = 0;
+        double2 vf[4] = {};
+        double alf = 0.0;
+        TcFetch(a, t0, r, cf, vf, alf);
+        TcFallback(vf, alf, a, vals);
+        atomicAdd(a.fallback, 1ull);
+      }
+      tc::MbarArrive(&vals_ready[b]);
+    }
+  }
+  tc::FenceBeforeSync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::FenceAfterSync();
+    tc::TmemFree(taddr, 512);
+  }
+}
+
 // ------------------------- O3 triangles, point-varying alpha, tensor cores
 // Affine triangles, FeSpaceLagrangeO3, the 12-point degree-6 rule, alpha
 // varying over the cell (analytic families / O1 nodal), gamma cell-constant:
@@ -2262,6 +2558,20 @@ void LaunchQuadTcWs(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
 }
 
 template <int M>
+void LaunchQuadTcWs2(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
+  const uint4* img = GetQuadTcImage(ctx, a.tab, a.L, M);
+  int* timeouts = StatusWord(ctx) + 14;
+  const size_t smem = Ws2SmemBytes(M);
+  auto kernel = RDQuadTcWs2Kernel<M>;
+  LFG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  const int64_t tiles = (a.count + 127) / 128;
+  const int64_t grid = std::min<int64_t>(tiles, ctx->num_sms);  // one CTA per SM (512 TMEM columns each)
+  if (grid <= 0) return;
+  kernel<<<static_cast<unsigned>(grid), kWsThreads, smem, ctx->stream>>>(a, d, img, timeouts);
+  LFG_LAUNCHED(ctx);
+}
+
+template <int M>
 void LaunchQuadTc(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d) {
   const uint4* img = GetQuadTcImage(ctx, a.tab, a.L, M);
   int* timeouts = StatusWord(ctx) + 14;
@@ -2400,6 +2710,9 @@ void LaunchRD(lfg_ctx* ctx, const AsmArgs& a, const DfArgs& d, bool uniform, boo
     if (ctx->tensor_cores == 2) {
       if (d.L.m == 2) LaunchQuadTc<2>(ctx, a, d);
       else LaunchQuadTc<3>(ctx, a, d);
+    } else if (ctx->tensor_cores == 3) {
+      if (d.L.m == 2) LaunchQuadTcWs2<2>(ctx, a, d);
+      else LaunchQuadTcWs2<3>(ctx, a, d);
     } else {
       if (d.L.m == 2) LaunchQuadTcWs<2>(ctx, a, d);
       else LaunchQuadTcWs<3>(ctx, a, d);

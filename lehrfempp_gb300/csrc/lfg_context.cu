@@ -277,7 +277,7 @@ lfg_status lfg_ctx_synchronize(lfg_ctx* ctx) {
 
 lfg_status lfg_ctx_set_tensor_cores(lfg_ctx* ctx, int enable) {
   LFG_API_BEGIN(ctx)
-  if (enable < 0 || enable > 2) Fail(LFG_INVALID_ARG, "lfg_ctx_set_tensor_cores: enable must be 0, 1 or 2");
+  if (enable < 0 || enable > 3) Fail(LFG_INVALID_ARG, "lfg_ctx_set_tensor_cores: enable must be 0, 1, 2 or 3");
   ctx->tensor_cores = enable;
   LFG_API_END
 }

@@ -58,7 +58,7 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
+@pytest.mark.parametrize("mode", [1, 2, 3], ids=["specialised", "two_cta", "producer_writes"])
 @pytest.mark.parametrize("name,mesh,qr", CASES, ids=[c[0] for c in CASES])
 def test_tensor_core_quads_match_oracle(ctx, name, mesh, qr, mode):
     m = mesh()
@@ -75,12 +75,13 @@ def test_tensor_core_quads_match_oracle(ctx, name, mesh, qr, mode):
 
 
 def test_tensor_core_mode_checked(ctx):
-    with pytest.raises(L.LfgError) as e:
-        ctx.set_tensor_cores(3)
-    assert e.value.code == L.INVALID_ARG
+    for bad in (-1, 4):
+        with pytest.raises(L.LfgError) as e:
+            ctx.set_tensor_cores(bad)
+        assert e.value.code == L.INVALID_ARG
 
 
-@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
+@pytest.mark.parametrize("mode", [1, 2, 3], ids=["specialised", "two_cta", "producer_writes"])
 def test_tensor_core_constant_alpha_and_fp64_cells(ctx, mode):
     """Constant alpha, and one tile mixing df32-range cells with cells whose
     alpha (1e15) sends them to the FP64 formula in the epilogue."""
@@ -96,7 +97,7 @@ def test_tensor_core_constant_alpha_and_fp64_cells(ctx, mode):
     assert ctx.profile_read("fp64_fallback_cells")[1] - before == len(alpha[::7])
 
 
-@pytest.mark.parametrize("mode", [1, 2], ids=["specialised", "two_cta"])
+@pytest.mark.parametrize("mode", [1, 2, 3], ids=["specialised", "two_cta", "producer_writes"])
 def test_tensor_core_many_tiles(ctx, mode):
     """90,000 quadrilaterals: 704 tiles of 128 cells, several per CTA of the
     persistent grid (both producer groups and buffers cycle), the last one
