@@ -1412,16 +1412,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     const int64_t first = blockIdx.x + static_cast<int64_t>(b) * gridDim.x;
     if (first < tiles) TcFetch(a, first * 128, r, c, v, al);
     int m = 0, issued = 0, prev_ncell = 0;
-    // writes this group's local tile jp (its m-th: vals_ready phase mp) from
-    // staging buffer jp % 3 and frees the buffer; false when a wait gave up
-    auto write_tile = [&](int jp, int mp) -> bool {
-      const bool ok = tc::MbarWait(&vals_ready[b], mp & 1, kTcMaxPolls);
+    // writes this group's local tile jp from staging buffer jp % 3 (its
+    // values are there: the caller waited for vals_ready) and frees the buffer
+    auto write_tile = [&](int jp) {
       asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's staged dofs / offsets
-      if (tc::NamedSyncOr(bar, 128, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
-        if (r == 0 && !ok) atomicAdd(tc_timeouts, 1);
-        s_abort = 1;
-        return false;
-      }
+      tc::NamedSync(bar, 128);
       const int kb = jp % 3;
       const double* vals = reinterpret_cast<const double*>(sA + kb * ABUF);
       const int* sd = sdofs + kb * 128 * N;
@@ -1437,7 +1432,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       }
       tc::NamedSync(bar, 128);  // every read of the buffer is done
       tc::MbarArrive(&buf_free[kb]);
-      return true;
     };
     bool alive = true;
     for (;; ++m) {
@@ -1533,7 +1527,17 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           *reinterpret_cast<uint4*>(arow + i * SA + gk * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
       }
       tc::FenceProxyAsync();
-      tc::NamedSync(bar, 128);
+      // the previous tile's values (vals_ready phase m - 1): every thread of
+      // the group waits before this tile's MMAs are issued, so the phase this
+      // tile completes cannot run ahead of a waiter (phases are told apart by
+      // parity only)
+      const bool vok = m == 0 || tc::MbarWait(&vals_ready[b], (m - 1) & 1, kTcMaxPolls);
+      if (tc::NamedSyncOr(bar, 128, !vok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (r == 0 && !vok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        alive = false;
+        break;
+      }
       if (r == 0) {
         bool free_ok = m == 0 || tc::MbarWait(&tmem_free[b], (m - 1) & 1, kTcMaxPolls);
         if (!free_ok) {
@@ -1566,14 +1570,19 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       const int64_t nxt = tile + 2 * static_cast<int64_t>(gridDim.x);
       if (nxt < tiles) TcFetch(a, nxt * 128, r, c, v, al);
       // the previous tile of this group goes out while this one's MMAs run
-      if (m > 0 && !write_tile(j - 2, m - 1)) {
-        alive = false;
-        break;
-      }
+      if (m > 0) write_tile(j - 2);
       prev_ncell = ncell;
     }
-    // the group's last tile
-    if (alive && m > 0) write_tile(b + 2 * (m - 1), m - 1);
+    // the group's last tile (phase m - 1 is the last one vals_ready[b] completes)
+    if (alive && m > 0) {
+      const bool vok = tc::MbarWait(&vals_ready[b], (m - 1) & 1, kTcMaxPolls);
+      if (tc::NamedSyncOr(bar, 128, !vok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (r == 0 && !vok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+      } else {
+        write_tile(b + 2 * (m - 1));
+      }
+    }
     // after an abort an MMA may still be in flight: it finishes before the
     // tensor memory is released (a completed phase returns at once)
     if (r == 0 && issued > 0) tc::MbarWait(&mma_done[b], (issued - 1) & 1, kTcMaxPolls);
