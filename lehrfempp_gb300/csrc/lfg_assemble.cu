@@ -1327,24 +1327,23 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 }
 
 // Warp-specialised variant with the triplet writes moved to the producers.
-// Local tile j of a CTA uses accumulator block j & 1 (the producer group
-// j & 1 splits its digits and issues its MMAs, as in RDQuadTcWsKernel) and
-// staging buffer j % 3 of three: the buffer first holds tile j's A digits;
-// once tile j's MMAs are complete the consumers (eight warps, two threads
-// per cell, recombination only) write tile j's 128 x 45 FP64 entries into it,
-// and tile j's producer group writes the triplets from there.  A group splits
-// the digits of its tile j into buffer j % 3 as soon as the other group has
-// written out tile j - 3 from it, and writes out its previous tile j - 2 only
-// after issuing tile j's MMAs, so digit splitting, recombination and triplet
-// writes of different tiles run at the same time.  Hand-offs: mma_done[b],
-// tmem_free[b], vals_ready[b] per accumulator block, buf_free[k] per staging
-// buffer (the writing group's 128 threads arrive).  Every wait gives up after
-// 2^22 polls.
+// The consumers (eight warps, two threads per cell) only recombine: they
+// write the FP64 entries of tile j into the A-digit buffer of tile j's
+// producer group -- free once tile j's MMAs have completed, and as large as
+// the 128 x 45 values for M = 3 -- and arrive on vals_ready[b].  The
+// producer group then writes tile j's triplets from there (it has slack:
+// it waits for a free accumulator block otherwise) before it splits the
+// digits of its next tile into the same buffer.  So the staged values are
+// double-buffered (one buffer per group) without extra shared memory, and a
+// tile's recombination overlaps the previous tile's writes.  Hand-offs per
+// group b: mma_done[b] (tile's MMAs complete), tmem_free[b] and vals_ready[b]
+// (the consumers have read accumulator block b and written the values).
+// Every wait gives up after 2^22 polls.
 __host__ __device__ constexpr int Ws2BufBytes(int m) {
   return 6 * 256 * TcKP(m) > 128 * 45 * 8 ? 6 * 256 * TcKP(m) : 128 * 45 * 8;
 }
 __host__ __device__ constexpr int Ws2SmemBytes(int m) {
-  return 3 * Ws2BufBytes(m) + TcImageBytes(m) + 3 * (128 * 9 * 4 + 128 * 8);
+  return 2 * Ws2BufBytes(m) + TcImageBytes(m) + 2 * (128 * 9 * 4 + 128 * 8);
 }
 
 template <int M>
@@ -1357,16 +1356,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   constexpr uint32_t SBO = KP * 16;  // 8-row group stride of both operands
   constexpr int ABUF = Ws2BufBytes(M);
   extern __shared__ __align__(1024) unsigned char smraw[];
-  unsigned char* sA = smraw;                                          // [3][ABUF]: digits, then values
-  unsigned char* sB = smraw + 3 * ABUF;                               // table digits, info block, Ec
+  unsigned char* sA = smraw;                                          // [2][ABUF]: digits, then values
+  unsigned char* sB = smraw + 2 * ABUF;                               // table digits, info block, Ec
   const int* sEc = reinterpret_cast<const int*>(sB + TcEcOffset(M));
-  int* sdofs = reinterpret_cast<int*>(sB + TcImageBytes(M));          // [3][128][9]
-  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 3 * 128 * N);    // [3][128]
+  int* sdofs = reinterpret_cast<int*>(sB + TcImageBytes(M));          // [2][128][9]
+  int64_t* soff = reinterpret_cast<int64_t*>(sdofs + 2 * 128 * N);    // [2][128]
   __shared__ f2 sWt[NQ + M];
   __shared__ __align__(8) uint64_t mma_done[2];
   __shared__ __align__(8) uint64_t tmem_free[2];
   __shared__ __align__(8) uint64_t vals_ready[2];
-  __shared__ __align__(8) uint64_t buf_free[3];
   __shared__ uint32_t s_taddr;
   __shared__ int s_abort;
 
@@ -1383,7 +1381,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       tc::MbarInit(&tmem_free[b], 256);
       tc::MbarInit(&vals_ready[b], 256);
     }
-    for (int k = 0; k < 3; ++k) tc::MbarInit(&buf_free[k], 128);
     s_abort = 0;
   }
   if (threadIdx.x < 32) tc::TmemAlloc(&s_taddr, 512);
@@ -1394,69 +1391,67 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   const uint32_t taddr = s_taddr;
   const int64_t tiles = (a.count + 127) / 128;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int tmap[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const int w = lane + 32 * t, i = w / N, j = w - i * N;
+    tmap[t] = w < N * N ? (i | (j << 8) | (UpperIndex<N>(i, j) << 16)) : -1;
+  }
 
   if (threadIdx.x < 256) {
     // ================= producers: group b, one thread per cell =================
     const int b = threadIdx.x >> 7, r = threadIdx.x & 127, wg = (threadIdx.x >> 5) & 3;
     const int bar = 1 + b;
-    int tmap[3];
-#pragma unroll
-    for (int t = 0; t < 3; ++t) {
-      const int w = lane + 32 * t, i = w / N, jj = w - i * N;
-      tmap[t] = w < N * N ? (i | (jj << 8) | (UpperIndex<N>(i, jj) << 16)) : -1;
-    }
+    unsigned char* Ab = sA + b * ABUF;
+    const double* vals_b = reinterpret_cast<const double*>(Ab);
+    int* sd_b = sdofs + b * 128 * N;
+    int64_t* so_b = soff + b * 128;
     const uint32_t dcol = taddr + 256 * b;
     int c = 0;
     double2 v[4] = {};
     double al = 0.0;
     const int64_t first = blockIdx.x + static_cast<int64_t>(b) * gridDim.x;
     if (first < tiles) TcFetch(a, first * 128, r, c, v, al);
-    int m = 0, issued = 0, prev_ncell = 0;
-    // writes this group's local tile jp from staging buffer jp % 3 (its
-    // values are there: the caller waited for vals_ready) and frees the buffer
-    auto write_tile = [&](int jp) {
-      asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's staged dofs / offsets
-      tc::NamedSync(bar, 128);
-      const int kb = jp % 3;
-      const double* vals = reinterpret_cast<const double*>(sA + kb * ABUF);
-      const int* sd = sdofs + kb * 128 * N;
-      const int64_t* so = soff + kb * 128;
+    int m = 0, issued = 0;
+    int prev_ncell = 0;
+    // writes the previous tile of this group (its values are in Ab once the
+    // consumers arrive on vals_ready[b]); false when a wait gave up
+    auto write_prev = [&](int mp) -> bool {
+      const bool ok = tc::MbarWait(&vals_ready[b], mp & 1, kTcMaxPolls);
+      asm volatile("cp.async.wait_all;" ::: "memory");  // this group's staged dofs / offsets
+      if (tc::NamedSyncOr(bar, 128, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
+        if (r == 0 && !ok) atomicAdd(tc_timeouts, 1);
+        s_abort = 1;
+        return false;
+      }
       for (int cl = 32 * wg; cl < prev_ncell && cl < 32 * wg + 32; ++cl) {
-        lfg_triplet* base = a.out + so[cl];
-        const int* dd = sd + cl * N;
-        const double* vv = vals + cl * E;
+        lfg_triplet* base = a.out + so_b[cl];
+        const int* dd = sd_b + cl * N;
+        const double* vv = vals_b + cl * E;
 #pragma unroll
         for (int t = 0; t < 3; ++t)
           if (tmap[t] >= 0)
             StoreTriplet(base + lane + 32 * t, dd[tmap[t] & 0xff], dd[(tmap[t] >> 8) & 0xff], vv[tmap[t] >> 16]);
       }
-      tc::NamedSync(bar, 128);  // every read of the buffer is done
-      tc::MbarArrive(&buf_free[kb]);
+      tc::NamedSync(bar, 128);  // Ab and the staged dofs are free again
+      return true;
     };
     bool alive = true;
     for (;; ++m) {
-      const int j = b + 2 * m;  // local tile index
-      const int64_t tile = blockIdx.x + static_cast<int64_t>(j) * gridDim.x;
+      const int64_t tile = blockIdx.x + static_cast<int64_t>(b + 2 * m) * gridDim.x;
       if (tile >= tiles) break;
       const int64_t t0 = tile * 128;
       const int ncell = static_cast<int>(a.count - t0 < 128 ? a.count - t0 : 128);
-      const int kb = j % 3;
-      // staging buffer kb is free once local tile j - 3 (the other group's) is written out
-      const bool ok = j < 3 || tc::MbarWait(&buf_free[kb], (j / 3 - 1) & 1, kTcMaxPolls);
-      if (tc::NamedSyncOr(bar, 128, !ok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
-        if (r == 0 && !ok) atomicAdd(tc_timeouts, 1);
-        s_abort = 1;
+      if (m > 0 && !write_prev(m - 1)) {
         alive = false;
         break;
       }
-      unsigned char* Ab = sA + kb * ABUF;
       // this tile's dof rows and triplet offsets, staged for its writes
       if (r < ncell) {
         const int32_t* g = a.cell_dofs + static_cast<int64_t>(c) * a.n_cell;
-        int* sd = sdofs + kb * 128 * N;
 #pragma unroll
-        for (int i = 0; i < N; ++i) tc::CpAsync4(sd + r * N + i, g + i);
-        tc::CpAsync8(soff + kb * 128 + r, a.tri_offset + c);
+        for (int i = 0; i < N; ++i) tc::CpAsync4(sd_b + r * N + i, g + i);
+        tc::CpAsync8(so_b + r, a.tri_offset + c);
       }
       tc::CpAsyncCommit();
       bool safe = false;
@@ -1527,17 +1522,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           *reinterpret_cast<uint4*>(arow + i * SA + gk * 128) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
       }
       tc::FenceProxyAsync();
-      // the previous tile's values (vals_ready phase m - 1): every thread of
-      // the group waits before this tile's MMAs are issued, so the phase this
-      // tile completes cannot run ahead of a waiter (phases are told apart by
-      // parity only)
-      const bool vok = m == 0 || tc::MbarWait(&vals_ready[b], (m - 1) & 1, kTcMaxPolls);
-      if (tc::NamedSyncOr(bar, 128, !vok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
-        if (r == 0 && !vok) atomicAdd(tc_timeouts, 1);
-        s_abort = 1;
-        alive = false;
-        break;
-      }
+      tc::NamedSync(bar, 128);
       if (r == 0) {
         bool free_ok = m == 0 || tc::MbarWait(&tmem_free[b], (m - 1) & 1, kTcMaxPolls);
         if (!free_ok) {
@@ -1566,23 +1551,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         }
       }
       ++issued;
+      prev_ncell = ncell;
       // inputs of this group's next tile load while the tensor cores work
       const int64_t nxt = tile + 2 * static_cast<int64_t>(gridDim.x);
       if (nxt < tiles) TcFetch(a, nxt * 128, r, c, v, al);
-      // the previous tile of this group goes out while this one's MMAs run
-      if (m > 0) write_tile(j - 2);
-      prev_ncell = ncell;
     }
-    // the group's last tile (phase m - 1 is the last one vals_ready[b] completes)
-    if (alive && m > 0) {
-      const bool vok = tc::MbarWait(&vals_ready[b], (m - 1) & 1, kTcMaxPolls);
-      if (tc::NamedSyncOr(bar, 128, !vok || *reinterpret_cast<volatile int*>(&s_abort) != 0)) {
-        if (r == 0 && !vok) atomicAdd(tc_timeouts, 1);
-        s_abort = 1;
-      } else {
-        write_tile(b + 2 * (m - 1));
-      }
-    }
+    // the group's last tile
+    if (alive && m > 0) write_prev(m - 1);
     // after an abort an MMA may still be in flight: it finishes before the
     // tensor memory is released (a completed phase returns at once)
     if (r == 0 && issued > 0) tc::MbarWait(&mma_done[b], (issued - 1) & 1, kTcMaxPolls);
@@ -1610,7 +1585,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       const int info = static_cast<int>(inf[0]);
       const bool safe = info != 0;
       const int shift = info - 128 + 2 - 54;
-      double* vals = reinterpret_cast<double*>(sA + (j % 3) * ABUF) + r * E;
+      double* vals = reinterpret_cast<double*>(sA + b * ABUF) + r * E;
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const int col = 24 * half + 8 * q;
