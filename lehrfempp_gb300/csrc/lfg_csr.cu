@@ -247,11 +247,30 @@ __device__ __forceinline__ T SellRow(const int32_t* __restrict__ cp, const T* __
   return sum;
 }
 
+// The same row with the column of entry k = bp[k] + op[k * 32] (16-bit offsets).
+template <class T>
+__device__ __forceinline__ T SellRowC(const uint16_t* __restrict__ op, const int32_t* __restrict__ bp,
+                                      const T* __restrict__ vp, int w, const T* __restrict__ p, int64_t r,
+                                      const T* __restrict__ rowsum) {
+  T sum = T(0);
+  if (rowsum) {
+    const T pr = p[r];
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[bp[k] + op[k * kSlice]] - pr, sum);
+    return fma(rowsum[r], pr, sum);
+  }
+#pragma unroll 4
+  for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[bp[k] + op[k * kSlice]], sum);
+  return sum;
+}
+
 // q = A p (SELL-32) and alpha = rz[cur] / <p, q>.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t nslices,
                                                            const int64_t* __restrict__ sptr,
                                                            const int32_t* __restrict__ scol, const T* __restrict__ sval,
+                                                           const uint16_t* __restrict__ soff,
+                                                           const int32_t* __restrict__ sbase,
                                                            const T* __restrict__ rowsum,
                                                            const T* __restrict__ p, T* __restrict__ q, int cur,
                                                            double* __restrict__ part, PcgScalars* __restrict__ sc) {
@@ -265,7 +284,8 @@ __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const T sum = SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, p, r, rowsum);
+      const T sum = soff ? SellRowC<T>(soff + b0 + lane, sbase + b0 / kSlice, sval + b0 + lane, w, p, r, rowsum)
+                         : SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, p, r, rowsum);
       q[r] = sum;
       acc.add(p[r], sum);
     }
@@ -402,6 +422,8 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
                                                                    const int64_t* __restrict__ sptr,
                                                                    const int32_t* __restrict__ scol,
                                                                    const T* __restrict__ sval,
+                                                                   const uint16_t* __restrict__ soff,
+                                                                   const int32_t* __restrict__ sbase,
                                                                    const T* __restrict__ rowsum,
                                                                    const T* __restrict__ x, const T* __restrict__ rhs,
                                                                    double* __restrict__ part,
@@ -416,7 +438,8 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const T t = rhs[r] - SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum);
+      const T t = rhs[r] - (soff ? SellRowC<T>(soff + b0 + lane, sbase + b0 / kSlice, sval + b0 + lane, w, x, r, rowsum)
+                                 : SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum));
       acc.add(t, t);
     }
   }
@@ -445,8 +468,9 @@ __global__ void SellWidthKernel(int64_t rows, int64_t nslices, const int64_t* __
   }
 }
 
-// ... and the entries, column-major per slice; padding entries point at the
-// row itself with value 0.
+// ... and the entries, column-major per slice; padding entries have value 0
+// and repeat the row's last column (so that a slice's k-th columns stay close
+// together for the 16-bit offsets below).
 __global__ void SellFillKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                                const double* __restrict__ val, const int64_t* __restrict__ sptr,
                                int32_t* __restrict__ scol, double* __restrict__ sval) {
@@ -456,11 +480,34 @@ __global__ void SellFillKernel(int64_t rows, const int64_t* __restrict__ rp, con
     const int64_t b0 = sptr[sl] + lane;
     const int w = static_cast<int>((sptr[sl + 1] - sptr[sl]) / kSlice);
     const int64_t a = rp[r], len = rp[r + 1] - a;
+    const int32_t pad = len > 0 ? col[a + len - 1] : static_cast<int32_t>(r);
     for (int k = 0; k < w; ++k) {
       const bool in = k < len;
-      scol[b0 + static_cast<int64_t>(k) * kSlice] = in ? col[a + k] : static_cast<int32_t>(r);
+      scol[b0 + static_cast<int64_t>(k) * kSlice] = in ? col[a + k] : pad;
       sval[b0 + static_cast<int64_t>(k) * kSlice] = in ? val[a + k] : 0.0;
     }
+  }
+}
+
+// 16-bit column offsets: one warp per (slice, k) column of 32 entries; the
+// base is the smallest column, and *wide is set when the spread is 2^16 or
+// more.
+__global__ void SellBaseKernel(int64_t ncols32, const int32_t* __restrict__ scol, int32_t* __restrict__ base,
+                               uint16_t* __restrict__ off, int* __restrict__ wide) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t g = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; g < ncols32;
+       g += (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) {
+    const int32_t c = scol[g * kSlice + lane];
+    int32_t lo = c, hi = c;
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if (lane == 0) {
+      base[g] = lo;
+      if (hi - lo > 0xffff) atomicExch(wide, 1);
+    }
+    off[g * kSlice + lane] = static_cast<uint16_t>(c - lo);
   }
 }
 
@@ -568,6 +615,27 @@ void PrepareSolve(lfg_csr* A) {
                                                             A->val.as<double>(), A->sell_ptr.as<int64_t>(),
                                                             A->sell_col.as<int32_t>(), A->sell_val.as<double>());
   LFG_LAUNCHED(ctx);
+  // 16-bit offsets per (slice, k) column: 2 B per entry instead of 4
+  {
+    const int64_t ncols32 = A->sell_nnz / kSlice;
+    A->sell_base.alloc(std::max<int64_t>(ncols32, 1) * sizeof(int32_t), s);
+    A->sell_off.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(uint16_t), s);
+    DevBuf wide;
+    wide.alloc(sizeof(int), s);
+    LFG_CUDA(cudaMemsetAsync(wide.p, 0, sizeof(int), s));
+    if (ncols32) {
+      SellBaseKernel<<<GridFor(ctx, ncols32 * kSlice, 256), 256, 0, s>>>(
+          ncols32, A->sell_col.as<int32_t>(), A->sell_base.as<int32_t>(), A->sell_off.as<uint16_t>(), wide.as<int>());
+      LFG_LAUNCHED(ctx);
+    }
+    int w = 0;
+    D2HSync(ctx, &w, wide.p, sizeof(int));
+    A->sell_c16 = w == 0;
+    if (!A->sell_c16) {
+      A->sell_base.reset();
+      A->sell_off.reset();
+    }
+  }
   LFG_CUDA(cudaStreamSynchronize(s));  // the host copy of sell_nnz above is a stack value
 }
 
@@ -659,9 +727,10 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T
     const int cur = k & 1;
     T* p = S.p.template as<T>();
     PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p, sc);
-    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
-                                                       A->sell_col.as<int32_t>(), sval, rowsum, p, S.q.template as<T>(),
-                                                       cur, part, sc);
+    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
+        n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval,
+        A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr, rowsum,
+        p, S.q.template as<T>(), cur, part, sc);
     PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                                            S.z.template as<T>(), cur, k == body - 1, part, sc);
   }
@@ -705,7 +774,9 @@ int RunPcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int6
       it += body;
       if (rhs) {
         PcgTrueResidualKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
-            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, rowsum, x, rhs,
+            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval,
+            A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
+            rowsum, x, rhs,
             S.part.template as<double>(), S.scal.template as<PcgScalars>());
         LFG_LAUNCHED(ctx);
         PcgScalars h{};
