@@ -250,6 +250,7 @@ struct Sell {
   const int32_t* col;
   const uint16_t* off;   // 16-bit column offsets (null: use col)
   const int32_t* base;   // their per-(slice, k) bases
+  const uint8_t* wide;   // slices that keep their int32 columns
 };
 
 // q = A p on the chunk's rows (SELL-32; thread per row), <p, q> per mesh
@@ -274,7 +275,7 @@ __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __
       const int w = static_cast<int>((M.ptr[sl + 1] - b0) >> 5);
       const T* vp = val + b0 + lane;
       T sum = T(0);
-      if (M.off) {
+      if (M.off && !M.wide[sl]) {
         const uint16_t* op = M.off + b0 + lane;
         const int32_t* bp = M.base + (b0 >> 5);
         if (rowsum) {
@@ -854,7 +855,8 @@ void BCapture(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T*
   cudaStream_t s = ctx->stream;
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
   const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr};
+               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
+               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
   MeshScal* ms = S.ms.template as<MeshScal>();
   double* part = S.part.template as<double>();
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -997,7 +999,8 @@ void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* din
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
   const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr};
+               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
+               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
   for (const std::vector<int>& grp : groups) {
     std::vector<int32_t> gch;
     for (int b : grp)
@@ -1115,7 +1118,8 @@ void TuneChunks(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const 
     frozen.alloc(B->nb * sizeof(int32_t), s);
     LFG_CUDA(cudaMemsetAsync(frozen.p, 0, B->nb * sizeof(int32_t), s));
     const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr};
+               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
+               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
     MeshScal* ms = S.ms.template as<MeshScal>();
     double* part = S.part.template as<double>();
     cudaGraph_t graph = nullptr;
