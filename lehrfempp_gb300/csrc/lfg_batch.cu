@@ -248,9 +248,6 @@ struct BDot<float> {
 struct Sell {
   const int64_t* ptr;
   const int32_t* col;
-  const uint16_t* off;   // 16-bit column offsets (null: use col)
-  const int32_t* base;   // their per-(slice, k) bases
-  const uint8_t* wide;   // slices that keep their int32 columns
 };
 
 // q = A p on the chunk's rows (SELL-32; thread per row), <p, q> per mesh
@@ -273,31 +270,17 @@ __global__ void __launch_bounds__(kPB) BSpmvKernel(Chunks C, Sell M, const T* __
       const int64_t sl = r >> 5, lane = r & 31;
       const int64_t b0 = M.ptr[sl];
       const int w = static_cast<int>((M.ptr[sl + 1] - b0) >> 5);
+      const int32_t* cp = M.col + b0 + lane;
       const T* vp = val + b0 + lane;
       T sum = T(0);
-      if (M.off && !M.wide[sl]) {
-        const uint16_t* op = M.off + b0 + lane;
-        const int32_t* bp = M.base + (b0 >> 5);
-        if (rowsum) {
-          const T pr = p[r];
+      if (rowsum) {
+        const T pr = p[r];
 #pragma unroll 4
-          for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[bp[k] + op[k * 32]] - pr, sum);
-          sum = fma(rowsum[r], pr, sum);
-        } else {
-#pragma unroll 4
-          for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[bp[k] + op[k * 32]], sum);
-        }
+        for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]] - pr, sum);
+        sum = fma(rowsum[r], pr, sum);
       } else {
-        const int32_t* cp = M.col + b0 + lane;
-        if (rowsum) {
-          const T pr = p[r];
 #pragma unroll 4
-          for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]] - pr, sum);
-          sum = fma(rowsum[r], pr, sum);
-        } else {
-#pragma unroll 4
-          for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]], sum);
-        }
+        for (int k = 0; k < w; ++k) sum = fma(vp[k * 32], p[cp[k * 32]], sum);
       }
       q[r] = sum;
       acc.add(p[r], sum);
@@ -854,9 +837,7 @@ void BCapture(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T*
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
   const int grid = static_cast<int>(std::min<int64_t>(C.nchunks, static_cast<int64_t>(ctx->num_sms) * 8));
-  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
-               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
+  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
   MeshScal* ms = S.ms.template as<MeshScal>();
   double* part = S.part.template as<double>();
   LFG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -998,9 +979,7 @@ void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* din
           const std::vector<std::vector<int>>& groups, int max_it, int body, After after, std::vector<int>& it_out) {
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
-  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
-               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
+  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
   for (const std::vector<int>& grp : groups) {
     std::vector<int32_t> gch;
     for (int b : grp)
@@ -1117,9 +1096,7 @@ void TuneChunks(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const 
     xs.alloc(n * sizeof(T), s);
     frozen.alloc(B->nb * sizeof(int32_t), s);
     LFG_CUDA(cudaMemsetAsync(frozen.p, 0, B->nb * sizeof(int32_t), s));
-    const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(),
-               A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
-               A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr};
+    const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
     MeshScal* ms = S.ms.template as<MeshScal>();
     double* part = S.part.template as<double>();
     cudaGraph_t graph = nullptr;

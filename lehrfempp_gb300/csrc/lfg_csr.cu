@@ -247,31 +247,11 @@ __device__ __forceinline__ T SellRow(const int32_t* __restrict__ cp, const T* __
   return sum;
 }
 
-// The same row with the column of entry k = bp[k] + op[k * 32] (16-bit offsets).
-template <class T>
-__device__ __forceinline__ T SellRowC(const uint16_t* __restrict__ op, const int32_t* __restrict__ bp,
-                                      const T* __restrict__ vp, int w, const T* __restrict__ p, int64_t r,
-                                      const T* __restrict__ rowsum) {
-  T sum = T(0);
-  if (rowsum) {
-    const T pr = p[r];
-#pragma unroll 4
-    for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[bp[k] + op[k * kSlice]] - pr, sum);
-    return fma(rowsum[r], pr, sum);
-  }
-#pragma unroll 4
-  for (int k = 0; k < w; ++k) sum = fma(vp[k * kSlice], p[bp[k] + op[k * kSlice]], sum);
-  return sum;
-}
-
 // q = A p (SELL-32) and alpha = rz[cur] / <p, q>.
 template <class T>
 __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t nslices,
                                                            const int64_t* __restrict__ sptr,
                                                            const int32_t* __restrict__ scol, const T* __restrict__ sval,
-                                                           const uint16_t* __restrict__ soff,
-                                                           const int32_t* __restrict__ sbase,
-                                                           const uint8_t* __restrict__ swide,
                                                            const T* __restrict__ rowsum,
                                                            const T* __restrict__ p, T* __restrict__ q, int cur,
                                                            double* __restrict__ part, PcgScalars* __restrict__ sc) {
@@ -285,9 +265,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgSpmvKernel(int64_t rows, int64_t
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const T sum = soff && !swide[sl]
-                        ? SellRowC<T>(soff + b0 + lane, sbase + b0 / kSlice, sval + b0 + lane, w, p, r, rowsum)
-                        : SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, p, r, rowsum);
+      const T sum = SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, p, r, rowsum);
       q[r] = sum;
       acc.add(p[r], sum);
     }
@@ -424,9 +402,6 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
                                                                    const int64_t* __restrict__ sptr,
                                                                    const int32_t* __restrict__ scol,
                                                                    const T* __restrict__ sval,
-                                                                   const uint16_t* __restrict__ soff,
-                                                                   const int32_t* __restrict__ sbase,
-                                                                   const uint8_t* __restrict__ swide,
                                                                    const T* __restrict__ rowsum,
                                                                    const T* __restrict__ x, const T* __restrict__ rhs,
                                                                    double* __restrict__ part,
@@ -441,9 +416,7 @@ __global__ void __launch_bounds__(kPcgBlock) PcgTrueResidualKernel(int64_t rows,
     const int64_t b0 = sptr[sl];
     const int w = static_cast<int>((sptr[sl + 1] - b0) / kSlice);
     if (r < rows) {
-      const T t = rhs[r] - (soff && !swide[sl]
-                                ? SellRowC<T>(soff + b0 + lane, sbase + b0 / kSlice, sval + b0 + lane, w, x, r, rowsum)
-                                : SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum));
+      const T t = rhs[r] - SellRow<T>(scol + b0 + lane, sval + b0 + lane, w, x, r, rowsum);
       acc.add(t, t);
     }
   }
@@ -472,57 +445,21 @@ __global__ void SellWidthKernel(int64_t rows, int64_t nslices, const int64_t* __
   }
 }
 
-// ... and the entries, column-major per slice; padding entries have value 0
-// and repeat the row's last column (so that a slice's k-th columns stay close
-// together for the 16-bit offsets below).
-// The lanes of the last slice past the last row get column rows - 1 and
-// value 0 (every entry of the copy is defined).
-__global__ void SellFillKernel(int64_t rows, int64_t nslices, const int64_t* __restrict__ rp,
-                               const int32_t* __restrict__ col, const double* __restrict__ val,
-                               const int64_t* __restrict__ sptr, int32_t* __restrict__ scol,
-                               double* __restrict__ sval) {
-  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < nslices * kSlice;
+// ... and the entries, column-major per slice; padding entries point at the
+// row itself with value 0.
+__global__ void SellFillKernel(int64_t rows, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                               const double* __restrict__ val, const int64_t* __restrict__ sptr,
+                               int32_t* __restrict__ scol, double* __restrict__ sval) {
+  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < rows;
        r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int64_t sl = r / kSlice, lane = r % kSlice;
     const int64_t b0 = sptr[sl] + lane;
     const int w = static_cast<int>((sptr[sl + 1] - sptr[sl]) / kSlice);
-    const bool real = r < rows;
-    const int64_t a = real ? rp[r] : 0, len = real ? rp[r + 1] - a : 0;
-    const int32_t pad = len > 0 ? col[a + len - 1] : static_cast<int32_t>(real ? r : rows - 1);
+    const int64_t a = rp[r], len = rp[r + 1] - a;
     for (int k = 0; k < w; ++k) {
       const bool in = k < len;
-      scol[b0 + static_cast<int64_t>(k) * kSlice] = in ? col[a + k] : pad;
+      scol[b0 + static_cast<int64_t>(k) * kSlice] = in ? col[a + k] : static_cast<int32_t>(r);
       sval[b0 + static_cast<int64_t>(k) * kSlice] = in ? val[a + k] : 0.0;
-    }
-  }
-}
-
-// 16-bit column offsets: one warp per slice, for each of its k columns of 32
-// entries the base is the smallest column; wide[sl] = 1 when one of them
-// spans 2^16 or more (that slice keeps its int32 columns); *narrow counts the
-// others.
-__global__ void SellBaseKernel(int64_t nslices, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
-                               int32_t* __restrict__ base, uint16_t* __restrict__ off, uint8_t* __restrict__ wide,
-                               unsigned long long* __restrict__ narrow) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t sl = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; sl < nslices;
-       sl += (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) {
-    const int64_t g0 = sptr[sl] / kSlice, g1 = sptr[sl + 1] / kSlice;
-    bool w = false;
-    for (int64_t g = g0; g < g1; ++g) {
-      const int32_t c = scol[g * kSlice + lane];
-      int32_t lo = c, hi = c;
-      for (int o = 16; o > 0; o >>= 1) {
-        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-      }
-      w = w || static_cast<int64_t>(hi) - static_cast<int64_t>(lo) > 0xffff;
-      if (lane == 0) base[g] = lo;
-      off[g * kSlice + lane] = static_cast<uint16_t>(c - lo);
-    }
-    if (lane == 0) {
-      wide[sl] = w ? 1 : 0;
-      if (!w) atomicAdd(narrow, 1ull);
     }
   }
 }
@@ -627,34 +564,10 @@ void PrepareSolve(lfg_csr* A) {
   if (A->sell_nnz >= (int64_t(1) << 31)) Fail(LFG_UNSUPPORTED, "solver needs padded nnz < 2^31");
   A->sell_col.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(int32_t), s);
   A->sell_val.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(double), s);
-  SellFillKernel<<<GridFor(ctx, A->nslices * kSlice, 256), 256, 0, s>>>(
-      A->rows, A->nslices, A->rowptr.as<int64_t>(), A->col.as<int32_t>(), A->val.as<double>(),
-      A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_val.as<double>());
+  SellFillKernel<<<GridFor(ctx, A->rows, 256), 256, 0, s>>>(A->rows, A->rowptr.as<int64_t>(), A->col.as<int32_t>(),
+                                                            A->val.as<double>(), A->sell_ptr.as<int64_t>(),
+                                                            A->sell_col.as<int32_t>(), A->sell_val.as<double>());
   LFG_LAUNCHED(ctx);
-  // 16-bit offsets per (slice, k) column: 2 B per entry instead of 4
-  {
-    const int64_t ncols32 = A->sell_nnz / kSlice;
-    A->sell_base.alloc(std::max<int64_t>(ncols32, 1) * sizeof(int32_t), s);
-    A->sell_off.alloc(std::max<int64_t>(A->sell_nnz, 1) * sizeof(uint16_t), s);
-    A->sell_wide.alloc(std::max<int64_t>(A->nslices, 1), s);
-    DevBuf narrow;
-    narrow.alloc(sizeof(unsigned long long), s);
-    LFG_CUDA(cudaMemsetAsync(narrow.p, 0, sizeof(unsigned long long), s));
-    if (A->nslices) {
-      SellBaseKernel<<<GridFor(ctx, A->nslices * kSlice, 256), 256, 0, s>>>(
-          A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), A->sell_base.as<int32_t>(),
-          A->sell_off.as<uint16_t>(), A->sell_wide.as<uint8_t>(), narrow.as<unsigned long long>());
-      LFG_LAUNCHED(ctx);
-    }
-    unsigned long long nn = 0;
-    D2HSync(ctx, &nn, narrow.p, sizeof(nn));
-    A->sell_c16 = nn > 0;
-    if (!A->sell_c16) {
-      A->sell_base.reset();
-      A->sell_off.reset();
-      A->sell_wide.reset();
-    }
-  }
   LFG_CUDA(cudaStreamSynchronize(s));  // the host copy of sell_nnz above is a stack value
 }
 
@@ -746,10 +659,9 @@ PcgGraph CapturePcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T
     const int cur = k & 1;
     T* p = S.p.template as<T>();
     PcgDirectionKernel<T><<<GridFor(ctx, n, kPcgBlock), kPcgBlock, 0, s>>>(n, S.z.template as<T>(), p, sc);
-    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
-        n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval,
-        A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
-        A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr, rowsum, p, S.q.template as<T>(), cur, part, sc);
+    PcgSpmvKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(n, A->nslices, A->sell_ptr.as<int64_t>(),
+                                                       A->sell_col.as<int32_t>(), sval, rowsum, p, S.q.template as<T>(),
+                                                       cur, part, sc);
     PcgUpdateKernel<T><<<update_blocks, kPcgBlock, 0, s>>>(n, dinv, p, S.q.template as<T>(), x, S.r.template as<T>(),
                                                            S.z.template as<T>(), cur, k == body - 1, part, sc);
   }
@@ -793,9 +705,7 @@ int RunPcg(lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, int6
       it += body;
       if (rhs) {
         PcgTrueResidualKernel<T><<<spmv_blocks, kPcgBlock, 0, s>>>(
-            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval,
-            A->sell_c16 ? A->sell_off.as<uint16_t>() : nullptr, A->sell_c16 ? A->sell_base.as<int32_t>() : nullptr,
-            A->sell_c16 ? A->sell_wide.as<uint8_t>() : nullptr, rowsum, x, rhs,
+            n, A->nslices, A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>(), sval, rowsum, x, rhs,
             S.part.template as<double>(), S.scal.template as<PcgScalars>());
         LFG_LAUNCHED(ctx);
         PcgScalars h{};

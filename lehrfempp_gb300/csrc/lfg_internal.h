@@ -229,13 +229,6 @@ struct lfg_csr {
   lfg::DevBuf sell_col;    // int32[sell_nnz]
   lfg::DevBuf sell_val;    // double[sell_nnz]
   lfg::DevBuf sell_val32;  // float[sell_nnz] (mixed precision, built lazily)
-  // the same column indices as a per-(slice, k) base plus 16-bit offsets,
-  // for the slices whose k-th columns span less than 2^16 (sell_wide[sl] = 0;
-  // the others keep sell_col); sell_c16 when at least one slice qualifies
-  bool sell_c16 = false;
-  lfg::DevBuf sell_base;   // int32[sell_nnz / 32]: slice sl, column k at sell_ptr[sl] / 32 + k
-  lfg::DevBuf sell_off;    // uint16[sell_nnz]
-  lfg::DevBuf sell_wide;   // uint8[nslices]
   lfg::DevBuf rowsum32;    // float[rows]: FP64 row sums rounded once (the FP32 SpMV's difference form)
 };
 
