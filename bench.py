@@ -295,6 +295,21 @@ def run_cpu_baseline(wl, max_seconds=20.0, threads=1):
                       "not timed" % (ncell, m.num_cells, ntrip, setup), "_counts": counts}
 
 
+def hbm_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path))["hbm_gbs"] if os.path.exists(path) else 6800.0
+
+
+def pcg_iteration_bytes(rows, nnz, fp32):
+    """Algorithmic bytes of one Jacobi-PCG iteration (K4/K5): the matrix once
+    (value + int32 column per nonzero, padding not counted) and 13 vector
+    passes (direction 3, SpMV gather and q 2, update 8), plus the row sums of
+    the difference-form FP32 operator."""
+    if fp32:
+        return nnz * 8 + rows * (13 * 4 + 4)
+    return nnz * 12 + rows * 13 * 8
+
+
 def solve_leg(L, W, ctx, n, cpu_check=False):
     """The large hybrid configuration's solve at n x n (O2): DOFs/s of
     assemble + fix + COO->CSR + PCG, FP64 vs mixed precision.
@@ -329,15 +344,24 @@ def solve_leg(L, W, ctx, n, cpu_check=False):
         A = coo.make_sparse()
         del coo
         x = ctx.zeros(nd)
+        ctx.synchronize()
+        t1 = time.perf_counter()
         st = A.solve_pcg(b, x, precision=prec, rtol=rtol, raise_on_failure=False)
         ctx.synchronize()
-        return x.download(), st, time.perf_counter() - t0
+        t2 = time.perf_counter()
+        st["solve_s"], st["nnz"] = t2 - t1, A.nnz
+        return x.download(), st, t2 - t0
 
     r, st, dt = run(L.SOLVE_FP64, 1e-8)
     rn = np.linalg.norm(r)
+    it_s = st["solve_s"] / max(st["iterations"], 1)
+    ib = pcg_iteration_bytes(nd, st["nnz"], False)
     out = {"workload": "hybrid %dx%d O2" % (n, n), "dofs": nd,
            "reference": {"precision": "fp64", "rtol": 1e-8, "seconds": dt, "iterations": st["iterations"],
-                         "rel_residual": st["rel_residual"], "converged": st["converged"]}}
+                         "rel_residual": st["rel_residual"], "converged": st["converged"],
+                         "per_iteration": {"ms": it_s * 1e3, "algorithmic_bytes": ib,
+                                           "achieved_gbs": ib / it_s / 1e9,
+                                           "frac_of_measured_hbm": ib / it_s / 1e9 / hbm_peak_gbs()}}}
     for name, prec in (("fp64", L.SOLVE_FP64), ("mixed", L.SOLVE_MIXED)):
         rec = {}
         for rtol in (1e-6, 1e-7, 1e-8):
@@ -668,9 +692,22 @@ def batch_leg(L, W, ctx, count, superlu_meshes=0):
            "setup_s": setup_s, "first_calls_s": first_s}
     th, ct, ms = batch.tuning()
     out["autotuner"] = {"threads_per_cta": th, "ctas_per_sm": ct, "assembly_ms": ms}
+    nnz_b = None
     for name, prec in (("mixed", L.SOLVE_MIXED), ("fp64", L.SOLVE_FP64)):
         cr, rate = batch.solve_tuning(prec)
         out["autotuner"]["solve_" + name] = {"chunk_rows": cr, "row_iterations_per_s": rate}
+        if nnz_b is None:
+            coo = L.COOMatrix(ctx, nd, nd, batch.num_triplets + nd)
+            batch.assemble_matrix_rd(prov, coo)
+            b0 = ctx.zeros(nd)
+            coo.fix_flagged_solution_components(flags, zeros, b0)
+            nnz_b = coo.make_sparse().nnz
+            del coo
+        # the sweep the tuner timed: every block's rows, kernels only
+        bpr = pcg_iteration_bytes(nd, nnz_b, name == "mixed") / nd
+        out["autotuner"]["solve_" + name]["per_iteration"] = {
+            "bytes_per_row": bpr, "achieved_gbs": rate * bpr / 1e9,
+            "frac_of_measured_hbm": rate * bpr / 1e9 / hbm_peak_gbs()}
     xr, st, _, _ = run(L.SOLVE_FP64, 1e-13)  # reference: batched FP64 PCG to its rounding floor
     r = xr.download()
 
@@ -888,6 +925,7 @@ def summarize(line):
                 t[k + "_s"] = _r(e["seconds"])
                 t[k + "_it"] = e.get("iterations")
         t["fp64_rtol1e-8_s"] = _r(_get(so, "reference", "seconds"))
+        t["fp64_iter_hbm_frac"] = _r(_get(so, "reference", "per_iteration", "frac_of_measured_hbm"), 3)
         t["mixed_vs_fp64"] = _r(so.get("mixed_vs_fp64_at_1e-8_err"), 3)
         t["cpu_superlu_Mdof_s"] = _r(_get(so, "cpu_baseline", "value") and so["cpu_baseline"]["value"] / 1e6)
         t["gpu_err_vs_superlu_256"] = _r(_get(so, "cpu_baseline", "gpu_mixed_rtol_1e-10_rel_err_vs_sparselu"), 2)
@@ -905,6 +943,8 @@ def summarize(line):
         t["max_err_vs_superlu"] = _r(_get(ba, "superlu_subset", "max_rel_err"), 2)
         t["grouped_fp64_Mdof_s"] = _r(_get(ba, "grouped_96MB_fp64", "dofs_per_s") and
                                       ba["grouped_96MB_fp64"]["dofs_per_s"] / 1e6)
+        for k in ("fp64", "mixed"):
+            t["sweep_hbm_frac_" + k] = _r(_get(ba, "autotuner", "solve_" + k, "per_iteration", "frac_of_measured_hbm"), 3)
         s["c4_batch"] = t
     gr = line.get("gradient") or {}
     if "store" in gr:
