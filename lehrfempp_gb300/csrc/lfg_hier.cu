@@ -247,10 +247,12 @@ __device__ __forceinline__ void LoadVerts(const HierArgs& a, int c, int4& cn, do
 // does about half an operation per triplet; a cell whose coefficients leave
 // the df32 range [2^-40, 2^40] is contracted in FP64 instead.
 // Shared memory: vals[T][E] | coef[T][4] | coef32[T][4] | base[T] | pat[T] |
-// cid[T] | safe[T] | dofs[T][n] | (VAR) nloc[T] | sel[T][n].  With VAR the
-// cells have their own shape-function subsets of the degree-D table: all E
-// table entries are contracted, and cell t writes its nloc[t]^2 triplets
-// through its selection.
+// cid[T] | safe[T] | dofs[T][n] | (VAR) nloc[T] | sel[T][n] | ent[T + 1] |
+// trip[T + 1].  With VAR the cells have their own shape-function subsets of
+// the degree-D table: cell t contracts only the m(m+1)/2 table entries its
+// m = nloc[t] functions pair up (ent: their prefix over the tile) and writes
+// its m^2 triplets consecutively (trip: their prefix), both as flat work
+// lists over the tile.
 template <bool QUAD, bool MASS, bool VAR>
 __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T) {
   using namespace df;
@@ -266,6 +268,8 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
   int* dofs = safe + T;
   int* nl = dofs + T * n;
   uint16_t* ss = reinterpret_cast<uint16_t*>(nl + T);
+  int* ent = reinterpret_cast<int*>(ss + ((T * n + 1) & ~1));  // 4-byte aligned after the uint16 block
+  int* trip = ent + T + 1;
   for (int64_t t0 = static_cast<int64_t>(blockIdx.x) * T; t0 < a.count; t0 += static_cast<int64_t>(gridDim.x) * T) {
     const int tn = static_cast<int>(min(static_cast<int64_t>(T), a.count - t0));
     for (int t = threadIdx.x; t < tn; t += blockDim.x) {
@@ -296,13 +300,46 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
       if (VAR) nl[t] = static_cast<int>(a.loc_offset[c + 1] - a.loc_offset[c]);
     }
     __syncthreads();
+    if (VAR && threadIdx.x == 0) {
+      ent[0] = trip[0] = 0;
+      for (int t = 0; t < tn; ++t) {
+        ent[t + 1] = ent[t] + nl[t] * (nl[t] + 1) / 2;
+        trip[t + 1] = trip[t] + nl[t] * nl[t];
+      }
+    }
     for (int idx = threadIdx.x; idx < tn * n; idx += blockDim.x) {
       const int t = Div(idx, a.div_n), i = idx - t * n;
       dofs[idx] = a.cell_dofs[static_cast<int64_t>(cid[t]) * a.n_cell + i];
       if (VAR) ss[idx] = a.sel[static_cast<int64_t>(cid[t]) * a.n_cell + i];
     }
-    for (int idx = threadIdx.x; idx < tn * E; idx += blockDim.x) {
-      const int t = Div(idx, a.div_E), e = idx - t * E;
+    if (VAR) __syncthreads();
+    const int nwork = VAR ? ent[tn] : tn * E;
+    for (int idx = threadIdx.x; idx < nwork; idx += blockDim.x) {
+      int t, e;
+      if (VAR) {
+        // cell of work item idx, then its pair (i <= j) in row-major upper order
+        int lo = 0, hi = tn - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (ent[mid] <= idx) lo = mid;
+          else hi = mid - 1;
+        }
+        t = lo;
+        const int m = nl[t], k = idx - ent[t];
+        const float b2 = 2.0f * m + 1.0f;
+        int i = static_cast<int>((b2 - sqrtf(b2 * b2 - 8.0f * static_cast<float>(k))) * 0.5f);
+        i = max(0, min(i, m - 1));
+        while (i > 0 && i * m - ((i * (i - 1)) >> 1) > k) --i;
+        while (i + 1 < m && (i + 1) * m - (((i + 1) * i) >> 1) <= k) ++i;
+        const int j = i + (k - (i * m - ((i * (i - 1)) >> 1)));
+        const int ui = ss[t * n + i], uj = ss[t * n + j];
+        const int u0 = min(ui, uj), u1 = max(ui, uj);
+        e = u0 * n - ((u0 * (u0 - 1)) >> 1) + (u1 - u0);
+      } else {
+        t = Div(idx, a.div_E);
+        e = idx - t * E;
+      }
+      const int vidx = t * E + e;
       const double* blk = a.tab + a.L.off_pat + pat[t] * a.L.stride;
       if (safe[t]) {
         const float4 r01 = *reinterpret_cast<const float4*>(blk + a.L.o_R32 + 4 * static_cast<int64_t>(e));
@@ -313,25 +350,32 @@ __global__ void __launch_bounds__(kHierBlock) HierAffineKernel(HierArgs a, int T
         acc.AddProd(cf[1], f2{r01.z, r01.w});
         acc.AddProd(cf[2], f2{r23.x, r23.y});
         if (MASS) acc.AddProd(cf[3], f2{r23.z, r23.w});
-        vals[idx] = ToDouble(acc.Value());
+        vals[vidx] = ToDouble(acc.Value());
       } else {
         const double* R = blk + a.L.o_R + 4 * static_cast<int64_t>(e);
         const double* cf = coef + 4 * t;
-        vals[idx] = cf[0] * R[0] + cf[1] * R[1] + cf[2] * R[2] + cf[3] * R[3];
+        vals[vidx] = cf[0] * R[0] + cf[1] * R[1] + cf[2] * R[2] + cf[3] * R[3];
       }
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < tn * nn; q += blockDim.x) {
-      const int t = Div(q, a.div_nn), rr = q - t * nn;
-      const int i = Div(rr, a.div_n), j = rr - i * n;
+    const int nwrite = VAR ? trip[tn] : tn * nn;
+    for (int q = threadIdx.x; q < nwrite; q += blockDim.x) {
       if (VAR) {
-        const int m = nl[t];
-        if (i >= m || j >= m) continue;
+        int lo = 0, hi = tn - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (trip[mid] <= q) lo = mid;
+          else hi = mid - 1;
+        }
+        const int t = lo, m = nl[t], rr = q - trip[t];
+        const int i = rr / m, j = rr - i * m;
         const int ui = ss[t * n + i], uj = ss[t * n + j];
-        const int lo = min(ui, uj), hi = max(ui, uj);
-        const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
-        StoreTriplet(a.out + base[t] + i * m + j, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
+        const int u0 = min(ui, uj), u1 = max(ui, uj);
+        const int e = u0 * n - ((u0 * (u0 - 1)) >> 1) + (u1 - u0);
+        StoreTriplet(a.out + base[t] + rr, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
       } else {
+        const int t = Div(q, a.div_nn), rr = q - t * nn;
+        const int i = Div(rr, a.div_n), j = rr - i * n;
         const int lo = min(i, j), hi = max(i, j);
         const int e = lo * n - ((lo * (lo - 1)) >> 1) + (hi - lo);
         StoreTriplet(a.out + base[t] + rr, dofs[t * n + i], dofs[t * n + j], vals[t * E + e]);
@@ -543,7 +587,10 @@ void LaunchAffine(lfg_ctx* ctx, const HierArgs& a, bool mass) {
   const int n = a.L.n, E = a.L.E;
   auto smem_for = [&](int t) {
     return static_cast<size_t>(t) * E * 8 + static_cast<size_t>(t) * (4 * 8 + 4 * 8 + 8 + 4 * 4) +
-           static_cast<size_t>(t) * n * 4 + (VAR ? static_cast<size_t>(t) * (4 + 2 * n) : 0);
+           static_cast<size_t>(t) * n * 4 +
+           (VAR ? static_cast<size_t>(t) * 4 + ((static_cast<size_t>(t) * n + 1) & ~size_t(1)) * 2 +
+                      2 * (static_cast<size_t>(t) + 1) * 4
+                : 0);
   };
   int T = std::max(1, std::min(32, 4096 / (n * n)));
   while (T > 1 && smem_for(T) > 96 * 1024) --T;
@@ -562,7 +609,7 @@ void LaunchAffine(lfg_ctx* ctx, const HierArgs& a, bool mass) {
 
 bool AffineFits(bool quad, int p, bool var) {
   const size_t n = quad ? (p + 1) * (p + 1) : (p + 1) * (p + 2) / 2;
-  return n * (n + 1) / 2 * 8 + 96 + n * 4 + (var ? 4 + 2 * n : 0) <= kHierSmemLimit;
+  return n * (n + 1) / 2 * 8 + 96 + n * 4 + (var ? 4 + 2 * n + 16 : 0) <= kHierSmemLimit;
 }
 
 template <bool QUAD, bool VAR>
