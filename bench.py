@@ -1050,8 +1050,8 @@ def run_ours(args):
 
     # end to end through the C-ABI with host buffers: per step the per-cell
     # alpha goes up from pinned host memory and lfg_assemble_matrix_rd_to_host
-    # assembles cell ranges into a device ring while finished ranges go down
-    # into a pinned host COO (5.1 GB)
+    # writes the triplets from the element kernels straight into a pinned host
+    # COO (5.1 GB) over the host link
     e2e = None
     if not args.no_e2e:
         a_pin = ctx.pinned(alpha_h.shape, np.float64)

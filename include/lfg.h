@@ -343,11 +343,13 @@ lfg_status lfg_assemble_matrix_rd(lfg_space* space, const lfg_rd_provider* provi
                                   lfg_coo* coo);
 /* The same assembly with the COOMatrix in host memory, as the reference keeps
  * it (assemble/coomatrix.h:51-225): the sum_K n_K^2 triplets are written to
- * host[0 .. count) in the same order.  The cells are assembled in ranges of
- * about chunk_triplets triplets (<= 0: 2^24) into a ring of three device
- * staging buffers while earlier ranges are copied to the host on a second
- * stream, so the device holds only the ring, not the whole matrix.  host
- * should be page-locked (lfg_host_alloc) for the copies to overlap.
+ * host[0 .. count) in the same order.  When host[0 .. sum_K n_K^2) lies inside
+ * one page-locked allocation made by lfg_host_alloc on this context, the
+ * element kernels store the triplets straight into it over the host link
+ * (one pass; chunk_triplets is not used).  Otherwise the cells are assembled
+ * in ranges of about chunk_triplets triplets (<= 0: 2^24) into a ring of three
+ * device staging buffers while earlier ranges are copied to the host on a
+ * second stream, so the device holds only the ring, not the whole matrix.
  * LFG_CAPACITY if capacity < sum_K n_K^2.  Lagrangian spaces. */
 lfg_status lfg_assemble_matrix_rd_to_host(lfg_space* space, const lfg_rd_provider* provider,
                                           lfg_triplet* host, int64_t capacity, int64_t chunk_triplets,

@@ -701,9 +701,10 @@ def assemble_matrix_rd(space, provider, coo):
 
 def assemble_matrix_rd_to_host(space, provider, out, chunk_triplets=0):
     """AssembleMatrixLocally into host memory: `out` is a PinnedArray (or a
-    numpy array) of TRIPLET_DTYPE with at least space.num_triplets entries;
-    the device assembly of cell ranges overlaps their download.  Returns the
-    number of triplets written."""
+    numpy array) of TRIPLET_DTYPE with at least space.num_triplets entries.
+    Pinned memory from ctx.pinned is written by the kernels directly; other
+    host memory through a device ring whose downloads overlap the assembly of
+    later cell ranges.  Returns the number of triplets written."""
     arr = out.array if isinstance(out, PinnedArray) else out
     assert arr.dtype == TRIPLET_DTYPE and arr.flags.c_contiguous
     n = C.c_int64()

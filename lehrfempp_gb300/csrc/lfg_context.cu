@@ -308,12 +308,16 @@ lfg_status lfg_host_alloc(lfg_ctx* ctx, size_t bytes, void** host) {
   LFG_API_BEGIN(ctx)
   if (!host) Fail(LFG_INVALID_ARG, "lfg_host_alloc: null output");
   LFG_CUDA(cudaMallocHost(host, bytes ? bytes : 1));
+  ctx->host_allocs[reinterpret_cast<uintptr_t>(*host)] = bytes ? bytes : 1;
   LFG_API_END
 }
 
 lfg_status lfg_host_free(lfg_ctx* ctx, void* host) {
   LFG_API_BEGIN(ctx)
-  if (host) LFG_CUDA(cudaFreeHost(host));
+  if (host) {
+    ctx->host_allocs.erase(reinterpret_cast<uintptr_t>(host));
+    LFG_CUDA(cudaFreeHost(host));
+  }
   LFG_API_END
 }
 

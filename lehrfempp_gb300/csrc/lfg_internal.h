@@ -98,6 +98,9 @@ struct lfg_ctx {
   std::vector<ProfRec> prof_pending;
   std::map<std::string, std::pair<double, int64_t>> prof_totals;
   std::vector<cudaEvent_t> event_pool;
+  // page-locked host allocations made by lfg_host_alloc (base -> bytes); a
+  // host output that lies inside one is written by the kernels directly
+  std::map<uintptr_t, size_t> host_allocs;
 };
 
 namespace lfg {

@@ -181,24 +181,34 @@ def test_fp64_route_for_out_of_range_cells(ctx, degree):
     compare_triplets(r.gpu_matrix().triplets(), ro, co, vo, block_sizes(r.cells(), r.space.n_tria, r.space.n_quad))
 
 
+@pytest.mark.parametrize("cfg", ["c2", "c3"])
 @pytest.mark.parametrize("chunk", [0, 1000, 77777])
-def test_assemble_to_host(ctx, chunk):
-    """AssembleMatrixLocally into host memory (cell ranges through a ring of
-    device buffers, downloads overlapping assembly): the same triplets, bit
-    for bit, as the device COO, into pinned and into pageable host memory."""
-    r = Run(ctx, W.config2(40))
+def test_assemble_to_host(ctx, chunk, cfg):
+    """AssembleMatrixLocally into host memory: the same triplets, bit for bit,
+    as the device COO -- written by the kernels straight into page-locked
+    memory from lfg_host_alloc (also at an offset inside it), and through the
+    ring of device buffers with overlapped downloads into pageable memory."""
+    r = Run(ctx, W.config2(40) if cfg == "c2" else W.config3(24))
     ref = r.gpu_matrix().triplets()
     p = L.rd_provider(W.to_coeff(ctx, r.wl["alpha"], r.keep), W.to_coeff(ctx, r.wl["gamma"], r.keep))
     pinned = ctx.pinned((r.space.num_triplets,), L.TRIPLET_DTYPE)
     assert L.assemble_matrix_rd_to_host(r.space, p, pinned, chunk) == len(ref)
     bad = np.flatnonzero(pinned.array != ref)
     assert bad.size == 0, (bad.size, bad[:5], pinned.array[bad[:3]], ref[bad[:3]])
+    wide = ctx.pinned((r.space.num_triplets + 8,), L.TRIPLET_DTYPE)
+    wide.array[:] = np.zeros(1, L.TRIPLET_DTYPE)
+    view = wide.array[5:]
+    assert L.assemble_matrix_rd_to_host(r.space, p, view, chunk) == len(ref)
+    assert np.array_equal(view[:len(ref)], ref) and not wide.array[:5]["row"].any() and not view[len(ref):]["row"].any()
     host = np.zeros(r.space.num_triplets + 5, L.TRIPLET_DTYPE)
     assert L.assemble_matrix_rd_to_host(r.space, p, host, chunk) == len(ref)
     assert np.array_equal(host[:len(ref)], ref) and not host[len(ref):]["row"].any()
     small = np.zeros(r.space.num_triplets - 1, L.TRIPLET_DTYPE)
     with pytest.raises(L.LfgError) as e:
         L.assemble_matrix_rd_to_host(r.space, p, small, chunk)
+    assert e.value.code == L.CAPACITY
+    with pytest.raises(L.LfgError) as e:
+        L.assemble_matrix_rd_to_host(r.space, p, wide.array[10:], chunk)
     assert e.value.code == L.CAPACITY
 
 
