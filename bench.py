@@ -68,7 +68,12 @@ def run_case(spec):
                   mixed precision; microseconds per iteration.
     hier:N:P:K:R -- TPTriag (K = tria) or TPQuad (K = quad) N x N,
                   HierarchicScalarFESpace of degree P, alpha 1, R assemblies
-                  into one COO matrix; milliseconds per assembly."""
+                  into one COO matrix; milliseconds per assembly.
+    grouped:BYTES -- a batch of four TPTriag O2 meshes (n = 320, 300, 280,
+                  260; alpha = exp(0.5 N(0,1)) per cell, gamma 1, f 1,
+                  Dirichlet 0) solved in FP64 by the grouped scheme with
+                  groups of BYTES (rtol 1e-4, at most 256 iterations);
+                  seconds of the solve."""
     import lehrfempp_gb300 as L
     from lehrfempp_gb300 import workloads as W
     f = spec.split(":")
@@ -107,6 +112,26 @@ def run_case(spec):
             L.assemble_matrix_rd(sp, prov, coo)
         ctx.synchronize()
         out.update({"triplets": sp.num_triplets, "ms_per_assembly_incl_first": (time.perf_counter() - t0) / reps * 1e3})
+    elif f[0] == "grouped":
+        ns = [320, 300, 280, 260]
+        meshes = [L.Mesh.tp_triag(ctx, n, n) for n in ns]
+        batch = L.Batch(ctx, [L.Space.lagrange(m, 2) for m in meshes])
+        nd = batch.num_dofs
+        alpha = ctx.to_device(np.exp(0.5 * np.random.default_rng(3).standard_normal(batch.num_cells)))
+        coo = L.COOMatrix(ctx, nd, nd, batch.num_triplets + nd)
+        batch.assemble_matrix_rd(L.rd_provider(L.coeff(L.PER_CELL, data=alpha), L.coeff(L.CONSTANT, 1.0)), coo)
+        b = ctx.zeros(nd)
+        batch.assemble_vector_load(L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+        coo.fix_flagged_solution_components(batch.boundary_dof_flags(), ctx.zeros(nd), b)
+        A = coo.make_sparse()
+        del coo
+        batch.set_solve_groups(float(f[1]))
+        x = ctx.zeros(nd)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        st = batch.solve_pcg(A, b, x, precision=L.SOLVE_FP64, rtol=1e-4, max_iterations=256, raise_on_failure=False)
+        ctx.synchronize()
+        out.update({"rows": nd, "iterations": st["iterations"], "solve_s": time.perf_counter() - t0})
     else:
         raise SystemExit("unknown case %r" % spec)
     ctx.close()

@@ -549,240 +549,293 @@ __global__ void __launch_bounds__(kPB) BReplaceKernel(Chunks C, const double* __
 // The lock-step solver streams every mesh's matrix and vectors from HBM on
 // every iteration.  The grouped solver instead packs meshes into groups whose
 // solver data fits in L2 and iterates one group at a time in one cooperative,
-// persistent launch per `check_every` iterations: three phases per iteration
-// (direction p = z + beta p; q = A p with <p, q>; the x / r / z update with
-// <r, z>, <r, r>) separated by grid barriers, so a group's vectors and matrix
-// stay in L2 across iterations and no kernel launch separates the phases.
-// Chunk c of the group's chunk list is always handled by block c % grid, so a
+// persistent launch per `check_every` iterations, so a group's matrix and
+// vectors stay in L2 across iterations.  The iteration is the Chronopoulos-
+// Gear form of Jacobi-PCG (one reduction per iteration):
+//   phase A  p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s,
+//            u = D^-1 r                                   (row-local)
+//   barrier
+//   phase B  w = A u; <r, u>, <w, u>, <r, r> per mesh      (gathers u)
+//   barrier
+//   scalars  beta = g / g_prev, alpha = g / (d - beta g / alpha_prev)
+// (s = A p throughout; at a mesh's (re)start beta = 0 and alpha = g / d, and
+// a non-positive denominator restarts the same way).  The group's rows are
+// cut into lanesets of at most 32 consecutive rows of one mesh; block k owns
+// a contiguous range of at most kGMaxLs lanesets, one warp per laneset, so a
 // block reads and writes its own rows in every phase and only the gathers of
-// the SpMV and the per-mesh partial sums cross blocks (read through L2).
-// Every block that needs a mesh's scalar (beta, alpha, the stopping test)
-// sums that mesh's chunk partials itself, in chunk order, so all blocks get
-// the same bits and the result does not depend on the grid.
-constexpr int kGThreads = 256;
-constexpr int kGMaxSlots = 16;          // chunks per block in one group
-constexpr int kGChunkRows = 512;        // rows per chunk of the grouped solver
-constexpr unsigned int kGBarPolls = 1u << 21;  // about a second of polling
+// u and the partial sums cross blocks (read through L2).  Consecutive
+// lanesets of one mesh within a block form a run; a run's three sums are
+// written once per iteration, and every block that needs a mesh's scalars
+// sums the mesh's run partials itself, in run order with the same warp tree,
+// so all blocks get the same bits and the result does not depend on timing.
+// Within a phase no location is both written and read by different threads,
+// and the barrier's acquire orders each phase after the previous one, so the
+// vectors are read with ordinary (L1-cached) loads.  The per-mesh scalars
+// (a mesh's owner sets its frozen flag while other blocks may read it) and
+// the partial sums are read through L2.
+constexpr int kGThreads = 512;
+constexpr int kGMinBlocks = 2;  // resident blocks per SM the kernel is compiled for
+constexpr int kGWarps = kGThreads / 32;
+constexpr int kGMaxLs = 64;                     // lanesets (so also runs) per block
+constexpr unsigned int kGBarPolls = 1u << 22;   // bounded barrier polls (about a second)
 
 struct GridBar {
-  unsigned int arrive, gen;
-  int err, pad;
+  unsigned int arrive;  // monotone arrival count of the launch (zeroed before it)
+  int err;              // a barrier gave up
 };
 
-// Per-mesh scalars of the grouped solver, published by the block that owns the
-// mesh's first chunk (read by the other blocks and by the host).
+// Per-mesh scalars of the grouped solver, published by the block that owns
+// the mesh's first run (read by the other blocks and by the host).
 struct GMeshScal {
-  double rz[2];    // <r, z> of iteration i in slot i & 1
+  double gam[2];   // <r, u> of iteration i in slot i & 1
+  double alp[2];   // alpha of iteration i in slot i & 1
   double rr;       // <r, r> at the last stopping test
   int32_t frozen;  // converged (or not part of the run)
-  int32_t it;      // iterations done
+  int32_t it;      // iteration index of the last stopping test
+  int32_t fresh;   // iteration at which the mesh (re)starts (beta = 0 there)
+  int32_t pad;
 };
 
-__device__ __forceinline__ unsigned int LdVolU(const unsigned int* p) {
-  return *reinterpret_cast<const volatile unsigned int*>(p);
-}
-__device__ __forceinline__ int LdVolI(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
-
-// Grid-wide barrier of a cooperative launch (every block co-resident).  Each
-// wait gives up after kGBarPolls polls: it then sets err, and every block
-// leaves at its next barrier.
-__device__ bool GridSync(GridBar* g) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned int gen = LdVolU(&g->gen);  // read before arriving
-    __threadfence();
-    if (atomicAdd(&g->arrive, 1u) == gridDim.x - 1) {
-      atomicExch(&g->arrive, 0u);
-      __threadfence();
-      atomicAdd(&g->gen, 1u);
-    } else {
-      unsigned int polls = 0;
-      while (LdVolU(&g->gen) == gen) {
-        if (++polls > kGBarPolls || LdVolI(&g->err)) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    if (!ok) atomicExch(&g->err, 1);
-    if (LdVolI(&g->err)) ok = 0;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
-// Sum of part[c * 3 + off] over a mesh's chunks, in chunk order, through L2.
-__device__ double GMeshSum(const double* part, int off, int64_t c0, int64_t c1, double* red) {
-  double v = 0.0;
-  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) v += __ldcg(part + c * 3 + off);
-  return BlockReduce(v, red);  // valid in thread 0
-}
+struct GGroup {
+  const int64_t* ls_row;    // laneset -> first row
+  const int32_t* ls_n;      // laneset -> rows (1..32)
+  const int32_t* ls_run;    // laneset -> run
+  const int32_t* run_mesh;  // run -> mesh
+  const int32_t* run_ls;    // run -> first laneset (nrun + 1)
+  const int32_t* run_m0;    // run -> first run of its mesh
+  const int32_t* run_m1;    // run -> one past the last run of its mesh
+  const int32_t* blk_ls;    // block -> first laneset (grid + 1)
+  const int32_t* blk_run;   // block -> first run (grid + 1)
+};
 
 template <class T>
 struct GArgs {
-  Chunks C;
+  GGroup g;
   Sell M;
   const T* val;
-  const T* rowsum;   // difference form (FP32) or null
+  const T* rowsum;     // difference form (FP32) or null
   const T* dinv;
-  T *x, *r, *z, *p, *q;
-  double* part;      // per chunk: <p, q>, <r, z>, <r, r>
+  T *x, *r, *u, *w, *p, *s;
+  const double* r64;   // (re)start from r = r64 * scale[mesh] with x = 0 (mixed), else from r
+  const double* scale;
+  const int32_t* sel;  // (re)start only the meshes with sel[mesh] (null: the whole group)
+  double* part;        // per run: <r, u>, <w, u>, <r, r>
   GMeshScal* gs;
   const double* target;  // per mesh: stop when <r, r> <= target
-  const int32_t* gch;    // the group's chunks
-  int ngch;
   int iters;             // iterations of this launch
   int i0;                // index of its first iteration within the group's run
+  int start;             // (re)start phase first
   GridBar* bar;
 };
 
-template <class T>
-__global__ void __launch_bounds__(kGThreads) BGroupPcgKernel(GArgs<T> g) {
-  __shared__ double red[32];
-  __shared__ double s_rz[kGMaxSlots], s_alpha;
-  __shared__ T s_beta[kGMaxSlots];
-  __shared__ int s_act[kGMaxSlots];
-  const int nslot = g.ngch > static_cast<int>(blockIdx.x)
-                        ? (g.ngch - static_cast<int>(blockIdx.x) + static_cast<int>(gridDim.x) - 1) /
-                              static_cast<int>(gridDim.x)
-                        : 0;
-  for (int k = 0;; ++k) {
-    const int i = g.i0 + k;
-    // ---- phase 1: stopping test and beta per mesh, p = z + beta p
-    for (int sl = 0; sl < nslot; ++sl) {
-      const int c = g.gch[blockIdx.x + sl * gridDim.x];
-      const int b = g.C.mesh[c];
-      const int64_t c0 = g.C.mesh_chunk[b], c1 = g.C.mesh_chunk[b + 1];
-      // read once per block: the flag may be set by the mesh's owner block
-      // during this very phase (its test gives every block the same answer)
-      __shared__ int s_live;
-      if (threadIdx.x == 0) s_live = !LdVolI(&g.gs[b].frozen);
-      __syncthreads();
-      if (s_live) {
-        const double rz = GMeshSum(g.part, 1, c0, c1, red);
-        const double rr = GMeshSum(g.part, 2, c0, c1, red);
-        if (threadIdx.x == 0) {
-          const double prev = i > 0 ? __ldcg(&g.gs[b].rz[(i - 1) & 1]) : 0.0;
-          const bool conv = !(rr > g.target[b]);
-          s_rz[sl] = rz;
-          s_beta[sl] = static_cast<T>(prev != 0.0 ? rz / prev : 0.0);
-          s_act[sl] = !conv && k < g.iters;
-          if (c == c0) {
-            g.gs[b].rz[i & 1] = rz;
-            g.gs[b].rr = rr;
-            g.gs[b].it = i;
-            if (conv) g.gs[b].frozen = 1;
-          }
-        }
-      } else if (threadIdx.x == 0) {
-        s_act[sl] = 0;
+// Grid barrier of a cooperative launch: every block adds one to a monotone
+// counter (release) and waits (acquire loads) until it reaches epoch x grid.
+// A wait gives up after kGBarPolls polls or when another block gave up; the
+// block then reports false and leaves the kernel.
+__device__ __forceinline__ bool GBarSync(GridBar* g, unsigned int& epoch, int* s_ok) {
+  __syncthreads();
+  ++epoch;
+  if (threadIdx.x == 0) {
+    const unsigned int want = epoch * gridDim.x;
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&g->arrive) : "memory");
+    unsigned int v = 0, polls = 0;
+    int ok = 1;
+    while (true) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&g->arrive) : "memory");
+      if (static_cast<int>(v - want) >= 0) break;
+      if (++polls > kGBarPolls || *reinterpret_cast<volatile int*>(&g->err)) {
+        ok = 0;
+        atomicExch(&g->err, 1);
+        break;
       }
-      __syncthreads();
-      if (s_act[sl]) {
-        const T beta = s_beta[sl];
-        for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x)
-          g.p[rw] = fma(beta, __ldcg(g.p + rw), __ldcg(g.z + rw));
-      }
+      __nanosleep(32);
     }
-    if (k == g.iters) break;
-    if (!GridSync(g.bar)) return;
-    // ---- phase 2: q = A p, <p, q> per chunk
-    for (int sl = 0; sl < nslot; ++sl) {
-      if (!s_act[sl]) continue;  // uniform per block
-      const int c = g.gch[blockIdx.x + sl * gridDim.x];
-      BDot<T> acc;
-      for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x) {
-        const int64_t slc = rw >> 5, lane = rw & 31;
-        const int64_t b0 = g.M.ptr[slc];
-        const int w = static_cast<int>((g.M.ptr[slc + 1] - b0) >> 5);
-        const int32_t* cp = g.M.col + b0 + lane;
-        const T* vp = g.val + b0 + lane;
-        const T pr = __ldcg(g.p + rw);
-        T sum = T(0);
-        if (g.rowsum) {
-#pragma unroll 4
-          for (int kk = 0; kk < w; ++kk) sum = fma(vp[kk * 32], __ldcg(g.p + cp[kk * 32]) - pr, sum);
-          sum = fma(g.rowsum[rw], pr, sum);
-        } else {
-#pragma unroll 4
-          for (int kk = 0; kk < w; ++kk) sum = fma(vp[kk * 32], __ldcg(g.p + cp[kk * 32]), sum);
-        }
-        g.q[rw] = sum;
-        acc.add(pr, sum);
-      }
-      const double tot = BlockReduce(acc.get(), red);
-      if (threadIdx.x == 0) g.part[3 * c] = tot;
-    }
-    if (!GridSync(g.bar)) return;
-    // ---- phase 3: alpha = rz / <p, q>; x += alpha p, r -= alpha q, z = D^-1 r
-    for (int sl = 0; sl < nslot; ++sl) {
-      if (!s_act[sl]) continue;
-      const int c = g.gch[blockIdx.x + sl * gridDim.x];
-      const int b = g.C.mesh[c];
-      const double pq = GMeshSum(g.part, 0, g.C.mesh_chunk[b], g.C.mesh_chunk[b + 1], red);
-      if (threadIdx.x == 0) s_alpha = pq != 0.0 ? s_rz[sl] / pq : 0.0;
-      __syncthreads();
-      const T alpha = static_cast<T>(s_alpha);
-      BDot<T> arz, arr;
-      for (int64_t rw = g.C.start[c] + threadIdx.x; rw < g.C.start[c + 1]; rw += blockDim.x) {
-        g.x[rw] = fma(alpha, __ldcg(g.p + rw), __ldcg(g.x + rw));
-        const T ri = fma(-alpha, __ldcg(g.q + rw), __ldcg(g.r + rw));
-        g.r[rw] = ri;
-        const T zi = g.dinv[rw] * ri;
-        g.z[rw] = zi;
-        arz.add(ri, zi);
-        arr.add(ri, ri);
-      }
-      const double s1 = BlockReduce(arz.get(), red);
-      const double s2 = BlockReduce(arr.get(), red);
-      if (threadIdx.x == 0) {
-        g.part[3 * c + 1] = s1;
-        g.part[3 * c + 2] = s2;
-      }
-    }
-    if (!GridSync(g.bar)) return;
+    *s_ok = ok;
   }
+  __syncthreads();
+  return *s_ok != 0;
 }
 
-// Start of a grouped run on the listed chunks: z = D^-1 r, p = 0, the <r, z>
-// and <r, r> partials.  With `scale` (mixed), r = r64 * scale[mesh] first and
-// d = 0; with `sel`, only the meshes with sel[mesh] set (a residual
-// replacement: p is kept).
+__device__ __forceinline__ double WarpSum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 template <class T>
-__global__ void __launch_bounds__(kGThreads) GStartKernel(Chunks C, const int32_t* __restrict__ gch, int ngch,
-                                                          const T* __restrict__ dinv, const double* __restrict__ r64,
-                                                          const double* __restrict__ scale,
-                                                          const int32_t* __restrict__ sel, T* __restrict__ r,
-                                                          T* __restrict__ z, T* __restrict__ p, T* __restrict__ d,
-                                                          double* __restrict__ part) {
-  __shared__ double red[32];
-  for (int j = blockIdx.x; j < ngch; j += gridDim.x) {
-    const int c = gch ? gch[j] : j;
-    const int b = C.mesh[c];
-    if (sel && !sel[b]) continue;  // uniform per block
-    double arz = 0.0, arr = 0.0;
-    const double sc = scale ? scale[b] : 1.0;
-    for (int64_t i = C.start[c] + threadIdx.x; i < C.start[c + 1]; i += blockDim.x) {
-      const T ri = scale ? static_cast<T>(r64[i] * sc) : r[i];
-      const T zi = dinv[i] * ri;
-      if (scale) r[i] = ri;
-      z[i] = zi;
-      if (!sel) p[i] = T(0);
-      if (d) d[i] = T(0);
-      arz = fma(static_cast<double>(ri), static_cast<double>(zi), arz);
-      arr = fma(static_cast<double>(ri), static_cast<double>(ri), arr);
+__global__ void __launch_bounds__(kGThreads, kGMinBlocks) BGroupCgKernel(GArgs<T> a) {
+  __shared__ double s_ls[kGMaxLs][3];           // laneset sums of phase B
+  __shared__ double s_al[kGMaxLs], s_be[kGMaxLs];  // per run of this block
+  __shared__ int s_act[kGMaxLs];
+  __shared__ int s_ok;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const GGroup& G = a.g;
+  const int ls0 = G.blk_ls[blockIdx.x], ls1 = G.blk_ls[blockIdx.x + 1];
+  const int rn0 = G.blk_run[blockIdx.x], rn1 = G.blk_run[blockIdx.x + 1];
+  unsigned int epoch = 0;
+  const bool restart_all = a.start && !a.sel;
+
+  // phase B on the lanesets whose run is live: w = A u, the three sums per
+  // laneset, then per run (in laneset order) into part
+  auto phase_b = [&](bool restart) {
+    for (int l = ls0 + warp; l < ls1; l += kGWarps) {
+      const int j = G.ls_run[l] - rn0;
+      const bool live = restart ? (restart_all || a.sel[G.run_mesh[rn0 + j]]) : s_act[j] != 0;
+      if (!live) continue;
+      const int64_t row = G.ls_row[l] + lane;
+      double g = 0.0, d = 0.0, rr = 0.0;
+      if (lane < G.ls_n[l]) {
+        const int64_t slc = row >> 5, li = row & 31;
+        const int64_t b0 = a.M.ptr[slc];
+        const int wd = static_cast<int>((a.M.ptr[slc + 1] - b0) >> 5);
+        const int32_t* cp = a.M.col + b0 + li;
+        const T* vp = a.val + b0 + li;
+        const T ur = a.u[row];
+        const T sh = a.rowsum ? ur : T(0);  // difference form: a_rk (u_k - u_r)
+        T sum = T(0);
+        // eight columns at a time: all their loads, then all their gathers
+        // (positions past the slice width add a zero term)
+        for (int k = 0; k < wd; k += 8) {
+          int32_t c[8];
+          T v[8], g[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const bool in = k + j < wd;
+            c[j] = in ? __ldg(cp + (k + j) * 32) : static_cast<int32_t>(row);
+            v[j] = in ? __ldg(vp + (k + j) * 32) : T(0);
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) g[j] = a.u[c[j]];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) sum = fma(v[j], g[j] - sh, sum);
+        }
+        if (a.rowsum) sum = fma(a.rowsum[row], ur, sum);
+        a.w[row] = sum;
+        const double rv = static_cast<double>(a.r[row]);
+        g = rv * static_cast<double>(ur);
+        d = static_cast<double>(sum) * static_cast<double>(ur);
+        rr = rv * rv;
+      }
+      g = WarpSum(g);
+      d = WarpSum(d);
+      rr = WarpSum(rr);
+      if (lane == 0) {
+        s_ls[l - ls0][0] = g;
+        s_ls[l - ls0][1] = d;
+        s_ls[l - ls0][2] = rr;
+      }
     }
-    const double s1 = BlockReduce(arz, red);
-    const double s2 = BlockReduce(arr, red);
-    if (threadIdx.x == 0) {
-      part[3 * c + 1] = s1;
-      part[3 * c + 2] = s2;
+    __syncthreads();
+    for (int j = warp; j < rn1 - rn0; j += kGWarps) {
+      const int run = rn0 + j;
+      const bool live = restart ? (restart_all || a.sel[G.run_mesh[run]]) : s_act[j] != 0;
+      if (!live) continue;
+      const int f0 = G.run_ls[run] - ls0, f1 = G.run_ls[run + 1] - ls0;
+      double g = 0.0, d = 0.0, rr = 0.0;
+      for (int q = f0 + lane; q < f1; q += 32) {
+        g += s_ls[q][0];
+        d += s_ls[q][1];
+        rr += s_ls[q][2];
+      }
+      g = WarpSum(g);
+      d = WarpSum(d);
+      rr = WarpSum(rr);
+      if (lane == 0) {
+        a.part[3 * run] = g;
+        a.part[3 * run + 1] = d;
+        a.part[3 * run + 2] = rr;
+      }
     }
+  };
+
+  if (a.start) {
+    // (re)start: r (from r64 in the mixed form, with x = 0), u = D^-1 r, p = s = 0
+    for (int l = ls0 + warp; l < ls1; l += kGWarps) {
+      const int mesh = G.run_mesh[G.ls_run[l]];
+      if (!restart_all && !a.sel[mesh]) continue;
+      if (lane >= G.ls_n[l]) continue;
+      const int64_t row = G.ls_row[l] + lane;
+      T ri;
+      if (a.r64) {
+        ri = static_cast<T>(a.r64[row] * a.scale[mesh]);
+        a.r[row] = ri;
+        a.x[row] = T(0);
+      } else {
+        ri = a.r[row];
+      }
+      a.u[row] = a.dinv[row] * ri;
+      a.p[row] = T(0);
+      a.s[row] = T(0);
+    }
+    if (!GBarSync(a.bar, epoch, &s_ok)) return;
+    phase_b(true);
+    if (!GBarSync(a.bar, epoch, &s_ok)) return;
+  }
+  for (int k = 0;; ++k) {
+    const int i = a.i0 + k;
+    // ---- scalars of every run's mesh, the stopping test
+    for (int j = warp; j < rn1 - rn0; j += kGWarps) {
+      const int run = rn0 + j, b = G.run_mesh[run];
+      const int m0 = G.run_m0[run], m1 = G.run_m1[run];
+      // read once per warp: the flag may be set by the mesh's owner during
+      // this very phase (its test gives every block the same answer)
+      const int live = __shfl_sync(0xffffffffu, lane == 0 ? !*reinterpret_cast<volatile int32_t*>(&a.gs[b].frozen) : 0, 0);
+      if (!live) {
+        if (lane == 0) s_act[j] = 0;
+        continue;
+      }
+      double g = 0.0, d = 0.0, rr = 0.0;
+      for (int q = m0 + lane; q < m1; q += 32) {
+        g += __ldcg(a.part + 3 * q);
+        d += __ldcg(a.part + 3 * q + 1);
+        rr += __ldcg(a.part + 3 * q + 2);
+      }
+      g = WarpSum(g);
+      d = WarpSum(d);
+      rr = WarpSum(rr);
+      if (lane == 0) {
+        const bool conv = !(rr > a.target[b]);
+        double al = d > 0.0 ? g / d : 0.0, be = 0.0;
+        if (__ldcg(&a.gs[b].fresh) != i) {
+          const double g0 = __ldcg(&a.gs[b].gam[(i - 1) & 1]), a0 = __ldcg(&a.gs[b].alp[(i - 1) & 1]);
+          const double bt = g0 != 0.0 ? g / g0 : 0.0;
+          const double den = a0 != 0.0 ? d - bt * g / a0 : 0.0;
+          if (den > 0.0 && den < INFINITY) {
+            be = bt;
+            al = g / den;
+          }
+        }
+        s_al[j] = al;
+        s_be[j] = be;
+        s_act[j] = !conv && k < a.iters;
+        if (run == m0) {
+          a.gs[b].gam[i & 1] = g;
+          a.gs[b].alp[i & 1] = al;
+          a.gs[b].rr = rr;
+          a.gs[b].it = i;
+          if (conv) a.gs[b].frozen = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (k == a.iters) break;
+    // ---- phase A
+    for (int l = ls0 + warp; l < ls1; l += kGWarps) {
+      const int j = G.ls_run[l] - rn0;
+      if (!s_act[j] || lane >= G.ls_n[l]) continue;
+      const int64_t row = G.ls_row[l] + lane;
+      const T al = static_cast<T>(s_al[j]), be = static_cast<T>(s_be[j]);
+      const T pi = fma(be, a.p[row], a.u[row]);
+      const T si = fma(be, a.s[row], a.w[row]);
+      a.p[row] = pi;
+      a.s[row] = si;
+      a.x[row] = fma(al, pi, a.x[row]);
+      const T ri = fma(-al, si, a.r[row]);
+      a.r[row] = ri;
+      a.u[row] = a.dinv[row] * ri;
+    }
+    if (!GBarSync(a.bar, epoch, &s_ok)) return;
+    phase_b(false);
+    if (!GBarSync(a.bar, epoch, &s_ok)) return;
   }
 }
 
@@ -915,7 +968,7 @@ void BRunPcg(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* 
 
 // ---------------------------------------------------- grouped solver host
 struct GBufs {
-  DevBuf part, gs, bar, gch, target;
+  DevBuf part, gs, bar, target, tabs, svec;
   std::vector<GMeshScal> gs_h;
   int grid = 0;
 };
@@ -936,13 +989,15 @@ std::vector<int64_t> MeshNnz(lfg_batch* B, lfg_csr* A) {
   return h;
 }
 
+int64_t MeshLanesets(lfg_batch* B, int b) { return (B->dof_off[b + 1] - B->dof_off[b] + 31) / 32; }
+
 // Meshes with want[b] packed into groups of at most `budget` bytes of solver
-// data in precision T (padded matrix, Jacobi diagonal, row sums and the five
+// data in precision T (padded matrix, Jacobi diagonal, row sums and the six
 // work vectors), largest first; a mesh larger than the budget is a group of
-// its own.  A group also holds at most max_chunks chunks.
+// its own.  A group also holds at most max_ls lanesets.
 template <class T>
 std::vector<std::vector<int>> PackGroups(lfg_batch* B, const std::vector<int64_t>& nnz,
-                                         const std::vector<int32_t>& want, double budget, int64_t max_chunks) {
+                                         const std::vector<int32_t>& want, double budget, int64_t max_ls) {
   std::vector<int> order;
   for (int b = 0; b < B->nb; ++b)
     if (want[b]) order.push_back(b);
@@ -950,56 +1005,139 @@ std::vector<std::vector<int>> PackGroups(lfg_batch* B, const std::vector<int64_t
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rows(a) > rows(b); });
   std::vector<std::vector<int>> groups;
   double used = 0.0;
-  int64_t chunks = 0;
+  int64_t ls = 0;
   for (int b : order) {
     const double bytes = 1.1 * static_cast<double>(nnz[b]) * (4.0 + sizeof(T)) +
-                         static_cast<double>(rows(b)) * 7.0 * sizeof(T);
-    const int64_t ch = B->h_mesh_chunk_off[b + 1] - B->h_mesh_chunk_off[b];
-    if (groups.empty() || used + bytes > budget || chunks + ch > max_chunks) {
+                         static_cast<double>(rows(b)) * 9.0 * sizeof(T);
+    const int64_t nl = MeshLanesets(B, b);
+    if (groups.empty() || used + bytes > budget || ls + nl > max_ls) {
       groups.emplace_back();
       used = 0.0;
-      chunks = 0;
+      ls = 0;
     }
     groups.back().push_back(b);
     used += bytes;
-    chunks += ch;
+    ls += nl;
   }
   return groups;
 }
 
-// Grouped PCG in precision T over `groups`: per group, start (z = D^-1 r,
-// p = 0; with r64 / scale the residual is first taken from r64 * scale), then
+// Device tables of one group (lanesets, runs, block ranges) in one buffer.
+struct GTabHost {
+  std::vector<int64_t> ls_row;
+  std::vector<int32_t> ls_n, ls_run, run_mesh, run_ls, run_m0, run_m1, blk_ls, blk_run;
+};
+
+GGroup UploadGroup(lfg_batch* B, const std::vector<int>& grp, int grid, GBufs& G, GTabHost& h) {
+  h = GTabHost{};
+  for (int b : grp) {
+    const int64_t r0 = B->dof_off[b], r1 = B->dof_off[b + 1];
+    for (int64_t r = r0; r < r1; r += 32) {
+      h.ls_row.push_back(r);
+      h.ls_n.push_back(static_cast<int32_t>(std::min<int64_t>(32, r1 - r)));
+      h.run_mesh.push_back(b);  // laneset -> mesh for now
+    }
+  }
+  const int64_t nl = static_cast<int64_t>(h.ls_row.size());
+  if (nl > static_cast<int64_t>(kGMaxLs) * grid) Fail(LFG_UNSUPPORTED, "batched PCG: a group exceeds the cooperative grid");
+  std::vector<int32_t> ls_mesh;
+  ls_mesh.swap(h.run_mesh);
+  h.ls_run.resize(nl);
+  h.blk_ls.resize(grid + 1);
+  h.blk_run.resize(grid + 1);
+  for (int k = 0; k <= grid; ++k) h.blk_ls[k] = static_cast<int32_t>(nl * k / grid);
+  for (int k = 0; k < grid; ++k) {
+    h.blk_run[k] = static_cast<int32_t>(h.run_mesh.size());
+    for (int32_t l = h.blk_ls[k]; l < h.blk_ls[k + 1]; ++l) {
+      if (l == h.blk_ls[k] || ls_mesh[l] != ls_mesh[l - 1]) {
+        h.run_mesh.push_back(ls_mesh[l]);
+        h.run_ls.push_back(l);
+      }
+      h.ls_run[l] = static_cast<int32_t>(h.run_mesh.size()) - 1;
+    }
+  }
+  const int nrun = static_cast<int>(h.run_mesh.size());
+  h.blk_run[grid] = nrun;
+  h.run_ls.push_back(static_cast<int32_t>(nl));
+  h.run_m0.resize(nrun);
+  h.run_m1.resize(nrun);
+  for (int q = 0; q < nrun;) {  // runs of one mesh are consecutive
+    int e = q;
+    while (e < nrun && h.run_mesh[e] == h.run_mesh[q]) ++e;
+    for (int t = q; t < e; ++t) {
+      h.run_m0[t] = q;
+      h.run_m1[t] = e;
+    }
+    q = e;
+  }
+  // one buffer: the int64 laneset rows, then the int32 tables
+  std::vector<int32_t> t32;
+  auto add = [&](const std::vector<int32_t>& v) { t32.insert(t32.end(), v.begin(), v.end()); };
+  add(h.ls_n);
+  add(h.ls_run);
+  add(h.run_mesh);
+  add(h.run_ls);
+  add(h.run_m0);
+  add(h.run_m1);
+  add(h.blk_ls);
+  add(h.blk_run);
+  const size_t bytes = static_cast<size_t>(nl) * 8 + t32.size() * 4;
+  if (G.tabs.bytes < bytes) G.tabs.alloc(bytes, B->ctx->stream);
+  LFG_CUDA(cudaMemcpyAsync(G.tabs.p, h.ls_row.data(), nl * 8, cudaMemcpyHostToDevice, B->ctx->stream));
+  int32_t* d32 = reinterpret_cast<int32_t*>(static_cast<char*>(G.tabs.p) + nl * 8);
+  LFG_CUDA(cudaMemcpyAsync(d32, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice, B->ctx->stream));
+  LFG_CUDA(cudaStreamSynchronize(B->ctx->stream));  // t32 is a local
+  GGroup g;
+  g.ls_row = static_cast<const int64_t*>(G.tabs.p);
+  const int32_t* q = d32;
+  g.ls_n = q;
+  q += nl;
+  g.ls_run = q;
+  q += nl;
+  g.run_mesh = q;
+  q += nrun;
+  g.run_ls = q;
+  q += nrun + 1;
+  g.run_m0 = q;
+  q += nrun;
+  g.run_m1 = q;
+  q += nrun;
+  g.blk_ls = q;
+  q += grid + 1;
+  g.blk_run = q;
+  return g;
+}
+
+// Grouped PCG over `groups`: per group one (re)start of all its meshes, then
 // cooperative launches of `body` iterations until every mesh of the group is
-// frozen or max_it; `after(group)` runs after every launch with G.gs_h read
-// back (it may change device state and frozen flags, and then uploads gs).
-// it_out[b] = iterations done by mesh b.
+// frozen or max_it; after every launch `after(group, iterations)` runs with
+// G.gs_h read back and returns true when it selected meshes (`sel`) to restart
+// at the next launch (it uploads gs itself then).  `base` carries the vectors
+// and operators; it_out[b] = iterations done by mesh b.
 template <class T, class After>
-void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* dinv, T* x, T* r, T* z, T* p, T* q,
-          T* d, const double* r64, const double* scale, GBufs& G, const Chunks& C,
-          const std::vector<std::vector<int>>& groups, int max_it, int body, After after, std::vector<int>& it_out) {
+void GRun(lfg_batch* B, GArgs<T> base, const int32_t* sel, GBufs& G, const std::vector<std::vector<int>>& groups,
+          int max_it, int body, After after, std::vector<int>& it_out) {
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
-  const Sell M{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+  GTabHost h;
   for (const std::vector<int>& grp : groups) {
-    std::vector<int32_t> gch;
-    for (int b : grp)
-      for (int64_t c = B->h_mesh_chunk_off[b]; c < B->h_mesh_chunk_off[b + 1]; ++c) gch.push_back(static_cast<int32_t>(c));
-    const int ngch = static_cast<int>(gch.size());
-    if (!ngch) continue;
-    if (ngch > G.grid * kGMaxSlots) Fail(LFG_UNSUPPORTED, "batched PCG: a group exceeds the cooperative grid");
-    LFG_CUDA(cudaMemcpyAsync(G.gch.p, gch.data(), ngch * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    if (grp.empty()) continue;
+    GArgs<T> ga = base;
+    ga.g = UploadGroup(B, grp, G.grid, G, h);
     LFG_CUDA(cudaMemsetAsync(G.gs.p, 0, B->nb * sizeof(GMeshScal), s));
-    LFG_CUDA(cudaMemsetAsync(G.bar.p, 0, sizeof(GridBar), s));
-    GStartKernel<T><<<std::min(ngch, G.grid * 4), kGThreads, 0, s>>>(C, G.gch.as<int32_t>(), ngch, dinv, r64, scale,
-                                                                      nullptr, r, z, p, d, G.part.as<double>());
-    LFG_LAUNCHED(ctx);
+    ga.part = G.part.as<double>();
+    ga.gs = G.gs.as<GMeshScal>();
+    ga.target = G.target.as<double>();
+    ga.bar = G.bar.as<GridBar>();
+    ga.start = 1;
+    ga.sel = nullptr;
     int i0 = 0;
     while (true) {
-      GArgs<T> ga{C, M, sval, rowsum, dinv, x, r, z, p, q, G.part.as<double>(), G.gs.as<GMeshScal>(),
-                  G.target.as<double>(), G.gch.as<int32_t>(), ngch, std::min(body, max_it - i0), i0,
-                  G.bar.as<GridBar>()};
+      ga.i0 = i0;
+      ga.iters = std::min(body, max_it - i0);
+      LFG_CUDA(cudaMemsetAsync(G.bar.p, 0, sizeof(GridBar), s));
       void* args[] = {&ga};
-      LFG_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&BGroupPcgKernel<T>), dim3(G.grid),
+      LFG_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&BGroupCgKernel<T>), dim3(G.grid),
                                            dim3(kGThreads), args, 0, s));
       CountLaunch(ctx, 1);
       i0 += ga.iters;
@@ -1007,7 +1145,9 @@ void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* din
       LFG_CUDA(cudaMemcpyAsync(&bar, G.bar.p, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
       D2HSync(ctx, G.gs_h.data(), G.gs.p, B->nb * sizeof(GMeshScal));
       if (bar.err) Fail(LFG_CUDA_ERROR, "batched PCG: a grid barrier of the grouped solver timed out");
-      after(grp, i0);
+      const bool restart = after(grp, i0);
+      ga.start = restart ? 1 : 0;
+      ga.sel = restart ? sel : nullptr;
       int active = 0;
       for (int b : grp) active += !G.gs_h[b].frozen;
       if (!active || i0 >= max_it) break;
@@ -1016,20 +1156,26 @@ void GRun(lfg_batch* B, lfg_csr* A, const T* sval, const T* rowsum, const T* din
   }
 }
 
+// Occupancy-sized cooperative grid (at most kGMinBlocks blocks per SM).
 template <class T>
-void GAlloc(lfg_batch* B, GBufs& G) {
+int GGrid(lfg_ctx* ctx) {
+  int per_sm = 0;
+  LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BGroupCgKernel<T>, kGThreads, 0));
+  return ctx->num_sms * std::min(per_sm, kGMinBlocks);
+}
+
+template <class T>
+void GAlloc(lfg_batch* B, int64_t n, GBufs& G) {
   lfg_ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
-  G.part.alloc(3 * std::max<int64_t>(B->nchunks, 1) * sizeof(double), s);
+  G.grid = GGrid<T>(ctx);
+  if (G.grid < ctx->num_sms) Fail(LFG_CUDA_ERROR, "grouped PCG kernel cannot be resident");
+  G.part.alloc(3 * static_cast<size_t>(kGMaxLs) * G.grid * sizeof(double), s);
   G.gs.alloc(B->nb * sizeof(GMeshScal), s);
   G.bar.alloc(sizeof(GridBar), s);
-  G.gch.alloc(std::max<int64_t>(B->nchunks, 1) * sizeof(int32_t), s);
   G.target.alloc(B->nb * sizeof(double), s);
+  G.svec.alloc(n * sizeof(T), s);
   G.gs_h.assign(B->nb, GMeshScal{});
-  int per_sm = 0;
-  LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BGroupPcgKernel<T>, kGThreads, 0));
-  if (per_sm < 1) Fail(LFG_CUDA_ERROR, "grouped PCG kernel cannot be resident");
-  G.grid = ctx->num_sms * std::min(per_sm, 2);
 }
 
 // Chunks of `rows` rows, never straddling two meshes.
@@ -1418,16 +1564,10 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
   if (mixed) EnsureFloatValues(A);  // FP32 SELL values and row sums
   bool grouped = B->solve_group_bytes > 0.0;
   if (grouped) {
-    BuildChunks(B, kGChunkRows);
-    // every mesh must fit one cooperative grid (at most kGMaxSlots chunks per block)
-    int per_sm = 0;
-    LFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, mixed ? reinterpret_cast<const void*>(&BGroupPcgKernel<float>)
-                       : reinterpret_cast<const void*>(&BGroupPcgKernel<double>),
-        kGThreads, 0));
-    const int64_t max_chunks = static_cast<int64_t>(ctx->num_sms) * std::min(per_sm, 2) * kGMaxSlots;
-    for (int b = 0; b < B->nb && grouped; ++b)
-      grouped = per_sm >= 1 && B->h_mesh_chunk_off[b + 1] - B->h_mesh_chunk_off[b] <= max_chunks;
+    // every mesh must fit one cooperative grid (at most kGMaxLs lanesets per block)
+    const int64_t max_ls = static_cast<int64_t>(kGMaxLs) * (mixed ? GGrid<float>(ctx) : GGrid<double>(ctx));
+    for (int b = 0; b < B->nb && grouped; ++b) grouped = MeshLanesets(B, b) <= max_ls;
+    if (grouped) BuildChunks(B, kChunk);
   }
   if (!grouped) {
     const int pi = mixed ? 1 : 0;
@@ -1468,16 +1608,25 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
     std::vector<double> rr1;
     if (grouped) {
       GBufs G;
-      GAlloc<double>(B, G);
+      GAlloc<double>(B, n, G);
       std::vector<int32_t> want(B->nb);
       for (int b = 0; b < B->nb; ++b) want[b] = rr[b] > target[b];
       const auto groups = PackGroups<double>(B, MeshNnz(B, A), want, B->solve_group_bytes,
-                                             static_cast<int64_t>(G.grid) * kGMaxSlots);
+                                             static_cast<int64_t>(G.grid) * kGMaxLs);
       LFG_CUDA(cudaMemcpyAsync(G.target.p, target.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
       std::vector<int> itg(B->nb, 0);
-      GRun<double>(B, A, A->sell_val.as<double>(), nullptr, A->dinv.as<double>(), x, S.r.as<double>(),
-                   S.z.as<double>(), S.p.as<double>(), S.q.as<double>(), nullptr, nullptr, nullptr, G, C, groups,
-                   max_it, body, [](const std::vector<int>&, int) {}, itg);
+      GArgs<double> base{};
+      base.M = Sell{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+      base.val = A->sell_val.as<double>();
+      base.dinv = A->dinv.as<double>();
+      base.x = x;
+      base.r = S.r.as<double>();
+      base.u = S.z.as<double>();
+      base.w = S.q.as<double>();
+      base.p = S.p.as<double>();
+      base.s = G.svec.as<double>();
+      GRun<double>(B, base, nullptr, G, groups, max_it, body, [](const std::vector<int>&, int) { return false; },
+                   itg);
       for (int b = 0; b < B->nb; ++b) {
         its[b] += itg[b];
         refinements[b] += itg[b] > 0;
@@ -1533,17 +1682,18 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
     LFG_CUDA(cudaMemcpyAsync(scale.p, sc.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
     if (grouped) {
       GBufs G;
-      GAlloc<float>(B, G);
+      GAlloc<float>(B, n, G);
       std::vector<int32_t> want(B->nb), done(B->nb, 0), cont(B->nb);
       for (int b = 0; b < B->nb; ++b) want[b] = rr[b] > target[b];
       const auto groups = PackGroups<float>(B, MeshNnz(B, A), want, B->solve_group_bytes,
-                                            static_cast<int64_t>(G.grid) * kGMaxSlots);
+                                            static_cast<int64_t>(G.grid) * kGMaxLs);
       LFG_CUDA(cudaMemcpyAsync(G.target.p, t32.data(), B->nb * sizeof(double), cudaMemcpyHostToDevice, s));
       std::vector<int> itg(B->nb, 0);
       std::vector<double> rr_new;
       // after every launch: residual replacement for the meshes whose FP32
-      // residual dropped by `drop` (or that the kernel stopped as converged)
-      auto after = [&](const std::vector<int>& grp, int i_done) {
+      // residual dropped by `drop` (or that the kernel stopped as converged);
+      // the meshes that go on restart at the next launch (sel = cont)
+      auto after = [&](const std::vector<int>& grp, int i_done) -> bool {
         int nsel = 0;
         for (int b = 0; b < B->nb; ++b) sl[b] = 0;
         for (int b : grp) {
@@ -1560,7 +1710,7 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
         }
         if (!nsel) {
           LFG_CUDA(cudaMemcpyAsync(G.gs.p, G.gs_h.data(), B->nb * sizeof(GMeshScal), cudaMemcpyHostToDevice, s));
-          return;
+          return false;
         }
         LFG_CUDA(cudaMemcpyAsync(sel.p, sl.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
         BApplyKernel<<<grid, kPB, 0, s>>>(C, d32.as<float>(), scale.as<double>(), sel.as<int32_t>(), 1.0, x);
@@ -1598,13 +1748,8 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
             } else {
               cont[b] = 1;
               ++nkeep;
-              if (G.gs_h[b].frozen) {
-                // resumed after the kernel stopped it at iteration it: its
-                // last <r, z> goes to both slots, whatever the group's parity
-                const double last = G.gs_h[b].rz[G.gs_h[b].it & 1];
-                G.gs_h[b].rz[0] = G.gs_h[b].rz[1] = last;
-                G.gs_h[b].frozen = 0;
-              }
+              G.gs_h[b].frozen = 0;
+              G.gs_h[b].fresh = i_done;  // restarts (beta = 0) at the next launch
             }
           }
         }
@@ -1621,19 +1766,24 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
           for (int b = 0; b < B->nb; ++b)
             if (sl[b]) rr[b] = rr_new[b];
         }
-        if (nkeep) {
-          LFG_CUDA(cudaMemcpyAsync(sel.p, cont.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-          GStartKernel<float><<<grid, kGThreads, 0, s>>>(C, nullptr, static_cast<int>(C.nchunks),
-                                                         A->dinv32.as<float>(), S.r.as<double>(), scale.as<double>(),
-                                                         sel.as<int32_t>(), S32.r.as<float>(), S32.z.as<float>(),
-                                                         S32.p.as<float>(), d32.as<float>(), G.part.as<double>());
-          LFG_LAUNCHED(ctx);
-        }
+        if (nkeep) LFG_CUDA(cudaMemcpyAsync(sel.p, cont.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));
         LFG_CUDA(cudaMemcpyAsync(G.gs.p, G.gs_h.data(), B->nb * sizeof(GMeshScal), cudaMemcpyHostToDevice, s));
+        return nkeep > 0;
       };
-      GRun<float>(B, A, A->sell_val32.as<float>(), A->rowsum32.as<float>(), A->dinv32.as<float>(), d32.as<float>(),
-                  S32.r.as<float>(), S32.z.as<float>(), S32.p.as<float>(), S32.q.as<float>(), d32.as<float>(),
-                  S.r.as<double>(), scale.as<double>(), G, C, groups, max_it, body, after, itg);
+      GArgs<float> base{};
+      base.M = Sell{A->sell_ptr.as<int64_t>(), A->sell_col.as<int32_t>()};
+      base.val = A->sell_val32.as<float>();
+      base.rowsum = A->rowsum32.as<float>();
+      base.dinv = A->dinv32.as<float>();
+      base.x = d32.as<float>();
+      base.r = S32.r.as<float>();
+      base.u = S32.z.as<float>();
+      base.w = S32.q.as<float>();
+      base.p = S32.p.as<float>();
+      base.s = G.svec.as<float>();
+      base.r64 = S.r.as<double>();
+      base.scale = scale.as<double>();
+      GRun<float>(B, base, sel.as<int32_t>(), G, groups, max_it, body, after, itg);
       for (int b = 0; b < B->nb; ++b) its[b] += itg[b];
     } else {
     LFG_CUDA(cudaMemcpyAsync(frozen32.p, fz.data(), B->nb * sizeof(int32_t), cudaMemcpyHostToDevice, s));

@@ -115,10 +115,10 @@ def test_batch_solver_chunk_autotuner(ctx, precision):
 @pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
 def test_batch_grouped_solver(ctx, precision):
     """The grouped solver (L2-sized groups, persistent cooperative kernel with
-    grid barriers) gives every block the solution of the lock-step sweep: one
-    group holding every mesh (a block of 161k rows spreads over more chunks
-    than the grid has blocks), one group per mesh, and a middle budget; each
-    block also against a direct solve of the oracle's system."""
+    grid barriers, Chronopoulos-Gear iteration) gives every block the solution
+    of the lock-step sweep: one group holding every mesh (a block of 161k rows
+    spreads over every block of the grid), one group per mesh, and a middle
+    budget; each block also against a direct solve of the oracle's system."""
     import scipy.sparse.linalg as spla
     ns, degs = [40, 24, 200, 33, 47, 6, 61, 38], [2, 1, 2, 2, 1, 2, 1, 2]
     meshes, spaces, batch, alpha = _batch(ctx, ns, degs, seed=21)
