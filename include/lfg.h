@@ -579,11 +579,12 @@ lfg_status lfg_batch_set_solve_chunk_rows(lfg_batch* batch, int32_t precision, i
  * CUDA graph, every iteration streams the batch from HBM).  group_bytes > 0:
  * blocks are packed, largest first, into groups of at most group_bytes of
  * solver data (matrix, diagonal, row sums, work vectors) and solved one
- * group at a time by a persistent cooperative kernel (three phases per
- * iteration separated by grid barriers, check_every iterations per launch),
- * so that a group's data stays in the 129 MB L2 across iterations; rows per
- * chunk are then fixed at 512.  Each block's PCG is the same either way (up
- * to the order of its partial sums).  No reference counterpart. */
+ * group at a time by a persistent cooperative kernel (the Chronopoulos-Gear
+ * form of the same Jacobi-PCG: one reduction and two grid barriers per
+ * iteration, check_every iterations per launch), so that a group's data
+ * stays in the 129 MB L2 across iterations.  The lock-step sweep is the
+ * faster scheme on GB300; both give each block its PCG solution to the same
+ * tolerance (the iterates differ by rounding).  No reference counterpart. */
 lfg_status lfg_batch_set_solve_groups(lfg_batch* batch, double group_bytes);
 lfg_status lfg_batch_solve_groups(const lfg_batch* batch, double* group_bytes);
 
