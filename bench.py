@@ -1089,7 +1089,7 @@ def run_ours(args):
             alpha_d.upload_async(a_pin)
             L.assemble_matrix_rd_to_host(space, prov, t_pin)  # synchronizes
         e2e_s = (time.perf_counter() - t0) / e2e_steps
-        # the host link alone: one device-to-host copy of the same bytes
+        # the host link alone: one download of the same bytes into the pinned COO
         step()
         ctx.synchronize()
         t1 = time.perf_counter()

@@ -2955,22 +2955,11 @@ lfg_status lfg_assemble_matrix_rd_to_host(lfg_space* sp, const lfg_rd_provider* 
   cudaStream_t s = ctx->stream;
   // page-locked output from lfg_host_alloc: the kernels store the triplets
   // straight into it over the host link (one pass, no staging ring)
-  {
-    const uintptr_t h = reinterpret_cast<uintptr_t>(host);
-    const size_t need = static_cast<size_t>(sp->num_triplets) * sizeof(lfg_triplet);
-    auto it = ctx->host_allocs.upper_bound(h);
-    if (it != ctx->host_allocs.begin()) {
-      --it;
-      if (h - it->first <= it->second && need <= it->second - (h - it->first)) {
-        void* base = nullptr;
-        LFG_CUDA(cudaHostGetDevicePointer(&base, reinterpret_cast<void*>(it->first), 0));
-        lfg_triplet* dst = reinterpret_cast<lfg_triplet*>(static_cast<char*>(base) + (h - it->first));
-        AssembleRDCells(sp, pr, dst, 0, m->ntria, 0, m->nquad);
-        LFG_CUDA(cudaStreamSynchronize(s));
-        if (count) *count = sp->num_triplets;
-        return LFG_OK;
-      }
-    }
+  if (void* mapped = MappedHost(ctx, host, static_cast<size_t>(sp->num_triplets) * sizeof(lfg_triplet))) {
+    AssembleRDCells(sp, pr, static_cast<lfg_triplet*>(mapped), 0, m->ntria, 0, m->nquad);
+    LFG_CUDA(cudaStreamSynchronize(s));
+    if (count) *count = sp->num_triplets;
+    return LFG_OK;
   }
   const int64_t nc = m->nc;
   const int64_t nmax = std::max(sp->n_tria, sp->n_quad);

@@ -1,4 +1,5 @@
 // Context, memory helpers, timing and error plumbing of the C-ABI.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -52,6 +53,37 @@ void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes) {
   LFG_CUDA(cudaMemcpyAsync(ctx->pinned_small, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   LFG_CUDA(cudaStreamSynchronize(ctx->stream));
   std::memcpy(host, ctx->pinned_small, bytes);
+}
+
+void* MappedHost(lfg_ctx* ctx, const void* host, size_t bytes) {
+  const uintptr_t h = reinterpret_cast<uintptr_t>(host);
+  auto it = ctx->host_allocs.upper_bound(h);
+  if (it == ctx->host_allocs.begin()) return nullptr;
+  --it;
+  const uintptr_t off = h - it->first;
+  if (off > it->second || bytes > it->second - off) return nullptr;
+  void* base = nullptr;
+  LFG_CUDA(cudaHostGetDevicePointer(&base, reinterpret_cast<void*>(it->first), 0));
+  return static_cast<char*>(base) + off;
+}
+
+__global__ void MappedCopyKernel(const int4* __restrict__ src, int4* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+}
+
+void CopyToHost(lfg_ctx* ctx, void* host, const void* dev, size_t bytes) {
+  if (!bytes) return;
+  void* mapped = bytes >= kMappedCopyBytes ? MappedHost(ctx, host, bytes) : nullptr;
+  if (mapped && ((reinterpret_cast<uintptr_t>(mapped) | reinterpret_cast<uintptr_t>(dev) | bytes) & 15) == 0) {
+    const size_t n = bytes / 16;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>((n + 255) / 256, static_cast<size_t>(ctx->num_sms) * 8));
+    MappedCopyKernel<<<grid, 256, 0, ctx->stream>>>(static_cast<const int4*>(dev), static_cast<int4*>(mapped), n);
+    LFG_LAUNCHED(ctx);
+    return;
+  }
+  LFG_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
 }
 
 int32_t ReadAndClearStatus(lfg_ctx* ctx, int32_t* detail) {
@@ -330,7 +362,7 @@ lfg_status lfg_memcpy_h2d(lfg_ctx* ctx, void* dst, const void* src, size_t bytes
 lfg_status lfg_memcpy_d2h(lfg_ctx* ctx, void* dst, const void* src, size_t bytes) {
   LFG_API_BEGIN(ctx)
   if (bytes) {
-    LFG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CopyToHost(ctx, dst, src, bytes);
     LFG_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   LFG_API_END

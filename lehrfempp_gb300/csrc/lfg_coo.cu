@@ -221,7 +221,7 @@ lfg_status lfg_coo_download(lfg_coo* coo, lfg_triplet* host, int64_t count) {
   LFG_API_BEGIN(coo->ctx)
   if (!host || count < 0 || count > coo->size) Fail(LFG_INVALID_ARG, "lfg_coo_download: bad count");
   if (count) {
-    LFG_CUDA(cudaMemcpyAsync(host, coo->d, count * sizeof(lfg_triplet), cudaMemcpyDeviceToHost, coo->ctx->stream));
+    CopyToHost(coo->ctx, host, coo->d, count * sizeof(lfg_triplet));
     LFG_CUDA(cudaStreamSynchronize(coo->ctx->stream));
   }
   LFG_API_END

@@ -262,6 +262,16 @@ int32_t* StatusWord(lfg_ctx* ctx);
 // up to kPinnedSmallBytes go through the context's pinned staging buffer.
 constexpr size_t kPinnedSmallBytes = 4096;
 void D2HSync(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
+// Device address of host[0 .. bytes) when that range lies inside one
+// page-locked allocation made by lfg_host_alloc on this context, else null.
+void* MappedHost(lfg_ctx* ctx, const void* host, size_t bytes);
+// Device -> host copy on the context stream (not synchronized).  Into a
+// mapped allocation (MappedHost) of at least kMappedCopyBytes with 16-byte
+// aligned ends, a copy kernel stores through the mapping: it runs at the
+// host link's rate, which the copy engines do not reach on every box (they
+// moved 54 GB/s on one GB300 machine where kernel stores moved 190 GB/s).
+constexpr size_t kMappedCopyBytes = size_t(1) << 20;
+void CopyToHost(lfg_ctx* ctx, void* host, const void* dev, size_t bytes);
 // Solver data of a CSR matrix (lfg_csr.cu): Jacobi diagonal (FP64 + FP32),
 // int32 row pointers and the SELL-32 copy; FP32 values for mixed precision.
 void PrepareSolve(lfg_csr* A);
