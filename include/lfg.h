@@ -127,9 +127,10 @@ lfg_status lfg_measure_fp64_peak(lfg_ctx* ctx, double* tflops);
 /* Element matrices of Q2 quadrilaterals (cell-constant alpha, gamma = 0, tensor
  * Gauss rules of 2x2 or 3x3 points) run on the tcgen05 tensor cores with an
  * exact integer-digit splitting of the FP64 operands (kernel family
- * "rd_quad_tc"): enable = 1 (default) the warp-specialised kernel, 2 the
- * two-CTA-per-SM variant, 3 the warp-specialised kernel whose producer warps
- * write the triplets, 0 the df32 CUDA-core kernel ("rd_quad_df").
+ * "rd_quad_tc"): enable = 3 (default) the warp-specialised kernel whose
+ * producer warps write the triplets, 1 the warp-specialised kernel whose
+ * consumer warps write them, 2 the two-CTA-per-SM variant, 0 the df32
+ * CUDA-core kernel ("rd_quad_df"); all tensor-core modes give the same bits.
  * LFG_INVALID_ARG for other values.  No reference counterpart (a device choice). */
 lfg_status lfg_ctx_set_tensor_cores(lfg_ctx* ctx, int enable);
 

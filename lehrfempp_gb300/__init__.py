@@ -154,10 +154,11 @@ class Context:
 
     def set_tensor_cores(self, enable):
         """Q2 quadrilateral element matrices on the tcgen05 tensor cores
-        (True / 1: warp-specialised kernel, the default; 2: the two-CTA
-        variant; 3: warp-specialised with the triplet writes in the producer
-        warps) or on the df32 CUDA-core kernel (False / 0)."""
-        mode = int(enable) if not isinstance(enable, bool) else (1 if enable else 0)
+        (True / 3: warp-specialised with the triplet writes in the producer
+        warps, the default; 1: warp-specialised with the consumer warps
+        writing; 2: the two-CTA variant) or on the df32 CUDA-core kernel
+        (False / 0)."""
+        mode = int(enable) if not isinstance(enable, bool) else (3 if enable else 0)
         self.check(lib().lfg_ctx_set_tensor_cores(self.h, mode))
 
     def fp64_peak_tflops(self):

@@ -88,7 +88,7 @@ struct lfg_ctx {
   uint32_t sf_const_ready = 0;  // constant-memory slots of the sum-factorised quad tables filled on this context
   // table digits of the tensor-core quad kernel, keyed by the FP64 table block
   std::map<const double*, lfg::DevBuf> tc_images;
-  int tensor_cores = 1;  // Q2 quadrilaterals on the tcgen05 path (lfg_ctx_set_tensor_cores)
+  int tensor_cores = 3;  // Q2 quadrilaterals on the tcgen05 path (lfg_ctx_set_tensor_cores; 3 = producer-written triplets)
   // per-kernel-family event timing (lfg_profile_*)
   bool profiling = false;
   struct ProfRec {
