@@ -239,9 +239,9 @@ class ClockSampler:
 # to a full launch by the cell count (`ncu --clock-control none --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum -k regex:RD` on `python bench.py
 # --size 1024` with the side legs switched off).
-DRAM_BYTES_PER_CELL = {"rd_tria_df": (134030080 + 547695616) / 1048980,
+DRAM_BYTES_PER_CELL = {"rd_tria_df": (133993472 + 547919616) / 1048980,
                        "rd_quad_df": (120022528 + 620115200) / 524086,
-                       "rd_quad_tc": (120872960 + 619725824) / 524086}
+                       "rd_quad_tc": (119900928 + 620148480) / 524086}
 
 
 def algorithmic_bytes(space, mesh, kind):
