@@ -535,7 +535,13 @@ __global__ void __launch_bounds__(kPB) BReplaceKernel(Chunks C, const double* __
       const double rz = MeshPartSum(part, 2, 0, c0, c1, red);
       const double rr = MeshPartSum(part, 2, 1, c0, c1, red);
       if (threadIdx.x == 0) {
-        ms[b].beta = ms[b].rz[1] != 0.0 ? rz / ms[b].rz[1] : 0.0;
+        // the search direction is kept (beta from the new and the last
+        // recursive <r, z>) unless the replaced residual exceeds the
+        // recursive one by more than 16: the FP32 recursion had run past what
+        // it can resolve, its direction no longer belongs to this residual,
+        // and the block restarts from p = z
+        const double rz_old = ms[b].rz[1];
+        ms[b].beta = rz_old > 0.0 && rz <= 16.0 * rz_old ? rz / rz_old : 0.0;
         ms[b].rz[0] = rz;
         ms[b].rr = rr;
         ms[b].cnt = 0;
@@ -1674,6 +1680,30 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
     const double drop = opts->inner_rtol > 0 ? opts->inner_rtol * opts->inner_rtol : 1e-2;
     std::vector<double> sc(B->nb), t32(B->nb), ref32(B->nb, 1.0), rr_last(rr);
     std::vector<int32_t> fz(B->nb), failed(B->nb, 0), sl(B->nb), keep(B->nb);
+    // replacements in a row that did not cut the FP64 residual by 4: two end
+    // the block's FP32 phase (else a block whose FP32 solves keep claiming
+    // convergence just above its target would restart without end)
+    std::vector<int32_t> stalls(B->nb, 0);
+    // Smallest FP32 residual of each block since its last replacement, and
+    // the checks in a row without a new minimum: a block whose recursion
+    // found no new minimum in four checks is replaced as well (CG residuals
+    // are not monotone, and a recursion that has lost orthogonality can hover
+    // above the drop threshold for good)
+    std::vector<double> best32(B->nb, INFINITY);
+    std::vector<int32_t> flat(B->nb, 0);
+    auto flat_check = [&](int b, double r32) {
+      if (r32 < best32[b]) {
+        best32[b] = r32;
+        flat[b] = 0;
+      } else {
+        ++flat[b];
+      }
+      return flat[b] >= 4;
+    };
+    auto reset_flat = [&](int b) {
+      best32[b] = INFINITY;
+      flat[b] = 0;
+    };
     for (int b = 0; b < B->nb; ++b) {
       fz[b] = !(rr[b] > target[b]);
       sc[b] = rr[b] > 0 ? 1.0 / std::sqrt(rr[b]) : 1.0;
@@ -1705,7 +1735,8 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
             G.gs_h[b].frozen = 1;
             continue;
           }
-          sl[b] = m.frozen || !(m.rr >= drop * ref32[b]) || i_done >= max_it;
+          sl[b] = m.frozen || !(m.rr >= drop * ref32[b]) || flat_check(b, m.rr) || i_done >= max_it;
+          if (sl[b]) reset_flat(b);
           nsel += sl[b];
         }
         if (!nsel) {
@@ -1725,11 +1756,13 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
           if (!sl[b]) continue;
           refinements[b] += 1;
           const double claimed = G.gs_h[b].rr / (sc[b] * sc[b]);
+          const bool progress = rr_new[b] < 0.25 * rr_last[b];
+          stalls[b] = progress ? 0 : stalls[b] + 1;
           if (rr_new[b] <= target[b]) {
             rr[b] = rr_new[b];
             done[b] = 1;
             G.gs_h[b].frozen = 1;
-          } else if (!(rr_new[b] < 0.25 * rr_last[b]) && !(rr_new[b] <= 16.0 * claimed)) {
+          } else if ((!progress && !(rr_new[b] <= 16.0 * claimed)) || stalls[b] >= 2) {
             failed[b] = 1;
             done[b] = 1;
             G.gs_h[b].frozen = 1;
@@ -1818,7 +1851,8 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
             fz[b] = 1;
             continue;
           }
-          sl[b] = !(rr32[b] > t32[b]) || !(rr32[b] >= drop * ref32[b]) || it >= max_it;
+          sl[b] = !(rr32[b] > t32[b]) || !(rr32[b] >= drop * ref32[b]) || flat_check(b, rr32[b]) || it >= max_it;
+          if (sl[b]) reset_flat(b);
           nsel += sl[b];
         }
         if (!nsel) {
@@ -1838,10 +1872,12 @@ lfg_status lfg_batch_solve_pcg(lfg_batch* B, lfg_csr* A, const double* bvec, dou
           if (!sl[b]) continue;
           refinements[b] += 1;
           const double claimed = rr32[b] / (sc[b] * sc[b]);
+          const bool progress = rr_new[b] < 0.25 * rr_last[b];
+          stalls[b] = progress ? 0 : stalls[b] + 1;
           if (rr_new[b] <= target[b]) {
             rr[b] = rr_new[b];
             fz[b] = 1;
-          } else if (!(rr_new[b] < 0.25 * rr_last[b]) && !(rr_new[b] <= 16.0 * claimed)) {
+          } else if ((!progress && !(rr_new[b] <= 16.0 * claimed)) || stalls[b] >= 2) {
             failed[b] = 1;  // FP32 cannot resolve this block: finish it in FP64
             fz[b] = 1;
             if (!(rr_new[b] < rr_last[b])) {

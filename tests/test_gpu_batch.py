@@ -85,6 +85,38 @@ def test_batch_solve_matches_direct_solves(ctx, precision):
     assert max(its) > min(its)
 
 
+@pytest.mark.parametrize("check_every", [32, 128])
+def test_batch_mixed_long_replays_terminate(ctx, check_every):
+    """Mixed batched solve with long graph replays: every block converges to
+    the FP64 solution within a few times the FP64 iteration count.  With 128
+    iterations per replay a small block's FP32 recursion runs far past what
+    FP32 resolves before its residual is replaced; the replacement then
+    restarts its direction instead of keeping one that no longer belongs to
+    the replaced residual (the 512-mesh batch used to run such blocks to the
+    iteration cap)."""
+    ns, degs = [90, 120, 64, 150], [2, 2, 1, 2]
+    meshes, spaces, batch, alpha = _batch(ctx, ns, degs, seed=11)
+    alpha_d = ctx.to_device(alpha)
+    coo = _assemble(ctx, batch, alpha_d)
+    b = ctx.zeros(batch.num_dofs)
+    batch.assemble_vector_load(L.load_provider(L.coeff(L.CONSTANT, 1.0)), b)
+    coo.fix_flagged_solution_components(batch.boundary_dof_flags(), ctx.zeros(batch.num_dofs), b)
+    csr = coo.make_sparse()
+    x64, x32 = ctx.zeros(batch.num_dofs), ctx.zeros(batch.num_dofs)
+    s64 = batch.solve_pcg(csr, b, x64, precision=L.SOLVE_FP64, rtol=1e-10, check_every=check_every)
+    s32 = batch.solve_pcg(csr, b, x32, precision=L.SOLVE_MIXED, rtol=1e-10, check_every=check_every,
+                          max_iterations=50000)
+    assert s32["converged"] and all(blk["converged"] for blk in s32["blocks"])
+    it64 = max(blk["iterations"] for blk in s64["blocks"])
+    it32 = max(blk["iterations"] for blk in s32["blocks"])
+    assert it32 <= 4 * it64 + 4 * check_every, (it32, it64)
+    a, r = x32.download(), x64.download()
+    dof, _, _ = batch.offsets()
+    for k in range(len(ns)):
+        seg, ref = a[dof[k]:dof[k + 1]], r[dof[k]:dof[k + 1]]
+        assert np.linalg.norm(seg - ref) <= 1e-8 * np.linalg.norm(ref), k
+
+
 @pytest.mark.parametrize("precision", [L.SOLVE_FP64, L.SOLVE_MIXED])
 def test_batch_solver_chunk_autotuner(ctx, precision):
     """The first solve in a precision times the chunk sizes and keeps one; any
