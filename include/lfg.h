@@ -94,7 +94,12 @@ lfg_status lfg_hier_dual(int32_t is_quad, int32_t interior_degree, const int32_t
                          double* xy, double* M, int32_t* n_nodes, int32_t* n_dofs);
 
 /* Device memory and copies on the context's stream (no torch needed); no
- * counterpart in the reference, whose data lives in host memory. */
+ * counterpart in the reference, whose data lives in host memory.
+ * lfg_host_alloc returns page-locked memory that the library also maps into
+ * the device: a device-to-host copy of 1 MB or more into it (lfg_memcpy_d2h,
+ * lfg_coo_download) with 16-byte aligned ends is done by a kernel storing
+ * through the mapping, and lfg_assemble_matrix_rd_to_host writes into it
+ * directly; lfg_memcpy_d2h synchronizes, h2d and d2d are stream-ordered. */
 lfg_status lfg_malloc(lfg_ctx* ctx, size_t bytes, void** dev);
 lfg_status lfg_free(lfg_ctx* ctx, void* dev);
 lfg_status lfg_host_alloc(lfg_ctx* ctx, size_t bytes, void** pinned_host);
