@@ -1028,26 +1028,28 @@ std::vector<std::vector<int>> PackGroups(lfg_batch* B, const std::vector<int64_t
   return groups;
 }
 
-// Device tables of one group (lanesets, runs, block ranges) in one buffer.
+// Host copies of one group's device tables (lanesets, runs, block ranges).
 struct GTabHost {
   std::vector<int64_t> ls_row;
   std::vector<int32_t> ls_n, ls_run, run_mesh, run_ls, run_m0, run_m1, blk_ls, blk_run;
 };
 
+// Lanesets of the group's meshes in group order, each block's contiguous
+// range of them, and the runs (consecutive lanesets of one mesh within one
+// block); uploaded into G.tabs.
 GGroup UploadGroup(lfg_batch* B, const std::vector<int>& grp, int grid, GBufs& G, GTabHost& h) {
   h = GTabHost{};
+  std::vector<int32_t> ls_mesh;
   for (int b : grp) {
     const int64_t r0 = B->dof_off[b], r1 = B->dof_off[b + 1];
     for (int64_t r = r0; r < r1; r += 32) {
       h.ls_row.push_back(r);
       h.ls_n.push_back(static_cast<int32_t>(std::min<int64_t>(32, r1 - r)));
-      h.run_mesh.push_back(b);  // laneset -> mesh for now
+      ls_mesh.push_back(b);
     }
   }
   const int64_t nl = static_cast<int64_t>(h.ls_row.size());
   if (nl > static_cast<int64_t>(kGMaxLs) * grid) Fail(LFG_UNSUPPORTED, "batched PCG: a group exceeds the cooperative grid");
-  std::vector<int32_t> ls_mesh;
-  ls_mesh.swap(h.run_mesh);
   h.ls_run.resize(nl);
   h.blk_ls.resize(grid + 1);
   h.blk_run.resize(grid + 1);
