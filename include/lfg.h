@@ -99,7 +99,9 @@ lfg_status lfg_hier_dual(int32_t is_quad, int32_t interior_degree, const int32_t
  * the device: a device-to-host copy of 1 MB or more into it (lfg_memcpy_d2h,
  * lfg_coo_download) with 16-byte aligned ends is done by a kernel storing
  * through the mapping, and lfg_assemble_matrix_rd_to_host writes into it
- * directly; lfg_memcpy_d2h synchronizes, h2d and d2d are stream-ordered. */
+ * directly; lfg_memcpy_d2h synchronizes, h2d and d2d are stream-ordered.
+ * Memory from lfg_host_alloc must be released with lfg_host_free (on the same
+ * context), which also drops it from the context's list of mapped ranges. */
 lfg_status lfg_malloc(lfg_ctx* ctx, size_t bytes, void** dev);
 lfg_status lfg_free(lfg_ctx* ctx, void* dev);
 lfg_status lfg_host_alloc(lfg_ctx* ctx, size_t bytes, void** pinned_host);
