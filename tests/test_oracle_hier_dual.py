@@ -85,6 +85,28 @@ def test_library_dual_tables_match_the_oracle():
         assert np.abs(Ml - Mo).max() <= 1e-13 * max(1.0, np.abs(Mo).max()), (is_quad, pc, pe, pat)
 
 
+@pytest.mark.parametrize("is_quad", [False, True])
+@pytest.mark.parametrize("p", [12, 16, 20])
+def test_library_dual_at_high_degree(is_quad, p):
+    """Degrees up to the library's limit of 20 (a triangle of 231 and a
+    quadrilateral of 441 local dofs): nodes and dual matrix agree with the
+    oracle, and the library's dual inverts the basis evaluated by the oracle
+    at its nodes (M phi = I within 1e-10)."""
+    L = pytest.importorskip("lehrfempp_gb300")
+    try:
+        L.lib()
+    except Exception as e:  # pragma: no cover
+        pytest.skip("library not built: %s" % e)
+    nv = 4 if is_quad else 3
+    for pat in (0, (1 << nv) - 1, 5):
+        xo, Mo = O.hier_dual(is_quad, p, [p] * nv, _ori(pat, nv))
+        xl, Ml = L.hier_dual(is_quad, p, [p] * nv, pat)
+        assert np.abs(xl - xo).max() <= 1e-15
+        assert np.abs(Ml - Mo).max() <= 1e-13 * max(1.0, np.abs(Mo).max())
+        phi, _ = O.hier_shape_var(is_quad, p, [p] * nv, _ori(pat, nv), xl)
+        assert np.abs(Ml @ phi - np.eye(Ml.shape[0])).max() < 1e-10, (p, pat)
+
+
 def test_library_dual_rejects_bad_arguments():
     L = pytest.importorskip("lehrfempp_gb300")
     try:
