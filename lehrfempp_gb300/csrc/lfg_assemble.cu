@@ -2956,7 +2956,19 @@ lfg_status lfg_assemble_matrix_rd_to_host(lfg_space* sp, const lfg_rd_provider* 
   // page-locked output from lfg_host_alloc: the kernels store the triplets
   // straight into it over the host link (one pass, no staging ring)
   if (void* mapped = MappedHost(ctx, host, static_cast<size_t>(sp->num_triplets) * sizeof(lfg_triplet))) {
-    AssembleRDCells(sp, pr, static_cast<lfg_triplet*>(mapped), 0, m->ntria, 0, m->nquad);
+    // over the host link the quadrilateral kernel whose eight consumer warps
+    // write the triplets keeps more stores in flight than the default, whose
+    // four producer warps of a group write them (29.07 vs 29.60 ms for the
+    // 5.13 GB of the hybrid 2048 x 2048 O2 matrix); same bits either way
+    const int tc = ctx->tensor_cores;
+    if (tc == 3) ctx->tensor_cores = 1;
+    try {
+      AssembleRDCells(sp, pr, static_cast<lfg_triplet*>(mapped), 0, m->ntria, 0, m->nquad);
+    } catch (...) {
+      ctx->tensor_cores = tc;
+      throw;
+    }
+    ctx->tensor_cores = tc;
     LFG_CUDA(cudaStreamSynchronize(s));
     if (count) *count = sp->num_triplets;
     return LFG_OK;
